@@ -1,0 +1,68 @@
+/*
+ * Entry points of the GB300 XPBD library beyond the ABI41 set.  None of them
+ * exists in the reference; they expose what the parity tests, the batched
+ * form and the benchmark need.  Same conventions as ssbl_xpbd_cuda.h:
+ * 1 = success, 0 = failure with ssbl_last_error() set.
+ */
+#pragma once
+
+#include "ssbl_xpbd_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Internal buffers readable with xpbd_gb300_read_buffer. */
+enum {
+    XPBD_BUF_POSITIONS4 = 0,     /* float4 x V (xyz, effective inverse mass) */
+    XPBD_BUF_PREV4 = 1,          /* float4 x V */
+    XPBD_BUF_VEL4 = 2,           /* float4 x V */
+    XPBD_BUF_VERTEX_CELLS = 3,   /* int4 x V: cell x, y, z, bucket */
+    XPBD_BUF_VERTEX_BUCKET_START = 4, /* int x (vertex buckets + 1) */
+    XPBD_BUF_VERTEX_BUCKET_ENTRIES = 5, /* int x V */
+    XPBD_BUF_TRI_BUCKET_START = 6,     /* int x (triangle buckets + 1) */
+    XPBD_BUF_TRI_BUCKET_ENTRIES = 7,   /* int x total entries */
+    XPBD_BUF_EDGE_BUCKET_START = 8,
+    XPBD_BUF_EDGE_BUCKET_ENTRIES = 9,
+    XPBD_BUF_NEIGHBOR_COUNTS = 10,     /* int x V */
+    XPBD_BUF_NEIGHBOR_INDICES = 11,    /* int x V x 32 */
+    XPBD_BUF_STATIC_SDF = 12,          /* float x voxels */
+    XPBD_BUF_COUNTERS = 13             /* uint64 x 38 */
+};
+
+/* Build the self-collision hashes and the vertex-vertex neighbour table from
+ * the current positions without stepping (for integer parity checks). */
+__attribute__((visibility("default"))) int xpbd_gb300_build_self_structures(void* handle);
+
+/* Copy an internal buffer to host memory.  Returns the number of bytes
+ * written, or -1 with ssbl_last_error() set. */
+__attribute__((visibility("default"))) long long xpbd_gb300_read_buffer(void* handle, int buffer_id, void* out, long long max_bytes);
+
+/* Sizes of the hash tables: out[0..2] = vertex / triangle / edge bucket
+ * counts, out[3..5] = 1 when that hash is used (else brute force). */
+__attribute__((visibility("default"))) int xpbd_gb300_hash_info(void* handle, int* out6);
+
+/* Capture each frame's launch sequence as a CUDA graph (default 1). */
+__attribute__((visibility("default"))) int xpbd_gb300_set_graph_capture(void* handle, int enabled);
+
+/* Number of kernel launches (graph nodes count individually) issued by the
+ * last ssbl_step_solver_ex call. */
+__attribute__((visibility("default"))) long long xpbd_gb300_last_step_launches(void* handle);
+
+/* The CUDA stream (cudaStream_t) all of the solver's work is issued on. */
+__attribute__((visibility("default"))) void* xpbd_gb300_stream(void* handle);
+
+/* Run one frame without graph capture, timing every launch with CUDA events
+ * on the solver's stream; per kernel kind (14 kinds: predict, stretch pass,
+ * other vertex pass, bend colour, vertex / triangle / edge hash, neighbour
+ * table, VV, VT, EE, island, self apply, copy) write the summed milliseconds
+ * and the launch count.  Advances the simulation by that frame. */
+__attribute__((visibility("default"))) int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations,
+                                                                     float* kernel_ms, long long* kernel_launches, int kinds);
+
+/* Wait for the solver's stream. */
+__attribute__((visibility("default"))) int xpbd_gb300_synchronize(void* handle);
+
+#ifdef __cplusplus
+}
+#endif

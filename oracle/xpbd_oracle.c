@@ -1,0 +1,1506 @@
+/*
+ * CPU oracle of the XPBD cloth step -- TEST INFRASTRUCTURE ONLY (see
+ * xpbd_oracle.h).  Every function cites the reference lines it restates,
+ * relative to native/src/ssbl_xpbd_cuda_abi41.cu ("abi41.cu").
+ */
+#include "xpbd_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define K_EPS 1.0e-7f
+#define NB_SLOTS 32
+#define BUCKET_SLOTS 32
+#define MAX_PRIM_CELLS 64
+#define N_COUNTS 38
+
+enum {
+    C_SOFT = 0, C_EXACT = 1, C_EE = 2, C_HARD = 3, C_SELF_CAND = 9, C_SELF_OVF = 10, C_SDF = 11, C_LRA = 12,
+    C_WINGS = 13, C_TACK_GUARD = 14, C_BEND_GUARD = 15, C_ISL_CAND = 16, C_ISL_CLUST = 17, C_ISL_REFS = 18,
+    C_ISL_APPLIED = 19, C_ISL_GUARD = 20, C_ISL_MAXD = 21, C_F_SEEN = 22, C_F_ACC_VV = 23, C_F_ACC_VT = 24,
+    C_F_ACC_EE = 25, C_F_REJ_REST = 26, C_F_REJ_DUP = 27, C_F_REJ_OWN = 28, C_CLUSTERS = 31, C_CLUST_OWNED = 32,
+    C_FRICTION = 33
+};
+
+static char g_err[256];
+static int set_err(const char* m) {
+    snprintf(g_err, sizeof(g_err), "%s", m);
+    return 0;
+}
+const char* oracle_last_error(void) { return g_err; }
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------ vectors -- */
+typedef struct { float x, y, z; } V3;
+static inline V3 v3(float x, float y, float z) { V3 r = {x, y, z}; return r; }
+static inline V3 vadd(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline V3 vsub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline V3 vmul(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+/* abi41.cu:625-627: fma(z, fma(y, x*x)) */
+static inline float vdot(V3 a, V3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+/* abi41.cu:629-636 */
+static inline V3 vcross(V3 a, V3 b) {
+    return v3(fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x)));
+}
+static inline float vlen(V3 a) { return sqrtf(fmaxf(vdot(a, a), 0.0f)); }
+static inline float lensq_xyz(V3 d) { return fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z)); }
+static inline int vfinite(V3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+static inline float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+static V3 normalize_or(V3 v, V3 fb) {
+    float l = vlen(v);
+    if (!isfinite(l) || l <= K_EPS) return fb;
+    return vmul(v, 1.0f / l);
+}
+/* abi41.cu:951-960 */
+static V3 limit_delta(V3 d, float max_len) {
+    if (!vfinite(d) || !isfinite(max_len) || max_len <= 0.0f) return v3(0, 0, 0);
+    float l = vlen(d);
+    if (!isfinite(l) || l <= K_EPS) return v3(0, 0, 0);
+    return l > max_len ? vmul(d, max_len / l) : d;
+}
+/* abi41.cu:654-656 */
+static inline int cell_of(float value, float cell) { return (int)floorf(value / fmaxf(cell, K_EPS)); }
+/* abi41.cu:658-664 */
+static inline unsigned bucket_of(int x, int y, int z, int n) {
+    unsigned h = (unsigned)x * 73856093u ^ (unsigned)y * 19349663u ^ (unsigned)z * 83492791u;
+    return n > 0 ? (h & (unsigned)(n - 1)) : 0u;
+}
+/* abi41.cu:1589-1635 */
+static V3 closest_on_tri(V3 p, V3 a, V3 b, V3 c) {
+    V3 ab = vsub(b, a), ac = vsub(c, a), ap = vsub(p, a);
+    float d1 = vdot(ab, ap), d2 = vdot(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) return a;
+    V3 bp = vsub(p, b);
+    float d3 = vdot(ab, bp), d4 = vdot(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3) return b;
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) return vadd(a, vmul(ab, d1 / fmaxf(d1 - d3, K_EPS)));
+    V3 cp = vsub(p, c);
+    float d5 = vdot(ab, cp), d6 = vdot(ac, cp);
+    if (d6 >= 0.0f && d5 <= d6) return c;
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) return vadd(a, vmul(ac, d2 / fmaxf(d2 - d6, K_EPS)));
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f)
+        return vadd(b, vmul(vsub(c, b), (d4 - d3) / fmaxf((d4 - d3) + (d5 - d6), K_EPS)));
+    float denom = 1.0f / fmaxf(va + vb + vc, K_EPS);
+    float v = vb * denom, w = vc * denom;
+    return vadd(a, vadd(vmul(ab, v), vmul(ac, w)));
+}
+/* abi41.cu:4588-4614 */
+static void barycentric(V3 p, V3 a, V3 b, V3 c, float* wa, float* wb, float* wc) {
+    V3 v0 = vsub(b, a), v1 = vsub(c, a), v2 = vsub(p, a);
+    float d00 = vdot(v0, v0), d01 = vdot(v0, v1), d11 = vdot(v1, v1), d20 = vdot(v2, v0), d21 = vdot(v2, v1);
+    float denom = d00 * d11 - d01 * d01;
+    if (fabsf(denom) <= K_EPS) { *wa = *wb = *wc = 1.0f / 3.0f; return; }
+    float v = (d11 * d20 - d01 * d21) / denom, w = (d00 * d21 - d01 * d20) / denom;
+    v = fminf(fmaxf(v, 0.0f), 1.0f);
+    w = fminf(fmaxf(w, 0.0f), 1.0f - v);
+    float u = fmaxf(1.0f - v - w, 0.0f);
+    float sum = fmaxf(u + v + w, K_EPS);
+    *wa = u / sum; *wb = v / sum; *wc = w / sum;
+}
+/* abi41.cu:5458-5505 */
+static void seg_params(V3 p1, V3 q1, V3 p2, V3 q2, float* s, float* t) {
+    V3 d1 = vsub(q1, p1), d2 = vsub(q2, p2), r = vsub(p1, p2);
+    float a = vdot(d1, d1), e = vdot(d2, d2), f = vdot(d2, r);
+    if (a <= K_EPS && e <= K_EPS) { *s = 0; *t = 0; return; }
+    if (a <= K_EPS) { *s = 0; *t = clamp01(f / fmaxf(e, K_EPS)); return; }
+    float c = vdot(d1, r);
+    if (e <= K_EPS) { *t = 0; *s = clamp01(-c / fmaxf(a, K_EPS)); return; }
+    float b = vdot(d1, d2), denom = a * e - b * b;
+    *s = fabsf(denom) > K_EPS ? clamp01((b * f - c * e) / denom) : 0.0f;
+    float tnom = b * (*s) + f;
+    if (tnom < 0.0f) { *t = 0; *s = clamp01(-c / fmaxf(a, K_EPS)); }
+    else if (tnom > e) { *t = 1; *s = clamp01((b - c) / fmaxf(a, K_EPS)); }
+    else *t = tnom / e;
+}
+static inline long long to_fix(float v) {
+    if (!(fabsf(v) < 1.0e6f)) return 0;
+    return llrintf(v * 4294967296.0f);
+}
+static inline float from_fix(long long v) { return (float)v * (1.0f / 4294967296.0f); }
+
+/* ------------------------------------------------------------- solver -- */
+struct OracleSolver {
+    SsblXpbdConfig cfg;
+    SsblXpbdRuntimeColliders col;
+    int V, E, T, B, L;
+    V3 *pos, *snap, *prev, *vel, *rest;
+    float *w, *inv;
+    int *sp_off, *sp_other, *sp_side; float* sp_rest;
+    int *te_off, *te_other, *te_side; float* te_rest;
+    int *bj_off, *bj_other, *bj_side; float* bj_rest;
+    int* bends; float* bend_rest; int* bend_colors; int n_bend_colors;
+    int* tris; int* edges;
+    float* pin_w; V3* pin_t; float* pin_relax; int pin_relax_iter;
+    /* static SDF */
+    float* sdf; int sdf_ready, sdf_signed, dim[3]; float origin[3], voxel;
+    V3* stris; int n_stris;
+    /* self collision */
+    int self_on; float radius; int vhash, thash, ehash, nvb, ntb, neb; float cell;
+    int *vcell, *vb_start, *vb_ent, *tb_start, *tb_ent, *eb_start, *eb_ent, *nb_count, *nb_idx;
+    int tb_total, eb_total;
+    long long* acc;
+    unsigned long long counts[N_COUNTS];
+    float max_delta;
+};
+
+static void cnt(OracleSolver* s, int slot) {
+#pragma omp atomic
+    s->counts[slot] += 1ull;
+}
+static void cnt_add(OracleSolver* s, int slot, unsigned long long v) {
+#pragma omp atomic
+    s->counts[slot] += v;
+}
+
+static void* xcalloc(size_t n, size_t sz) { return n ? calloc(n, sz) : NULL; }
+
+/* Vertex -> constraint lists in constraint order (each vertex's incident
+ * constraints by increasing index; side = 1 when it is the second end). */
+static void build_csr(int V, const int* pairs, const float* rest, int n, int** off, int** other, int** side, float** r) {
+    *off = (int*)calloc((size_t)V + 1, sizeof(int));
+    for (int k = 0; k < n; ++k) {
+        int a = pairs[2 * k], b = pairs[2 * k + 1];
+        if (a < 0 || b < 0 || a >= V || b >= V || a == b) continue;
+        (*off)[a + 1]++; (*off)[b + 1]++;
+    }
+    for (int i = 0; i < V; ++i) (*off)[i + 1] += (*off)[i];
+    int tot = (*off)[V];
+    *other = (int*)xcalloc(tot, sizeof(int));
+    *side = (int*)xcalloc(tot, sizeof(int));
+    *r = (float*)xcalloc(tot, sizeof(float));
+    int* cur = (int*)calloc((size_t)V + 1, sizeof(int));
+    memcpy(cur, *off, sizeof(int) * (size_t)V);
+    for (int k = 0; k < n; ++k) {
+        int a = pairs[2 * k], b = pairs[2 * k + 1];
+        if (a < 0 || b < 0 || a >= V || b >= V || a == b) continue;
+        int ia = cur[a]++, ib = cur[b]++;
+        (*other)[ia] = b; (*side)[ia] = 0; (*r)[ia] = rest[k];
+        (*other)[ib] = a; (*side)[ib] = 1; (*r)[ib] = rest[k];
+    }
+    free(cur);
+}
+
+static int next_pow2(int v) {
+    int r = 1;
+    if (v < 1) v = 1;
+    while (r < v && r < (1 << 30)) r <<= 1;
+    return r;
+}
+
+/* -------------------------------------------------------- static SDF -- */
+typedef struct { long long x, y, z; int id; } QV;
+static int cmp_qv(const void* a, const void* b) {
+    const QV* p = (const QV*)a; const QV* q = (const QV*)b;
+    if (p->x != q->x) return p->x < q->x ? -1 : 1;
+    if (p->y != q->y) return p->y < q->y ? -1 : 1;
+    if (p->z != q->z) return p->z < q->z ? -1 : 1;
+    return p->id - q->id;
+}
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t p = *(const uint64_t*)a, q = *(const uint64_t*)b;
+    return p < q ? -1 : (p > q ? 1 : 0);
+}
+/* Closed-mesh test: weld on a 1e-6 grid, every edge used exactly twice
+ * (abi41.cu:6026-6063). */
+static int mesh_closed(const float* tris, int n) {
+    if (!tris || n <= 0) return 0;
+    int nv = n * 3;
+    QV* q = (QV*)malloc(sizeof(QV) * (size_t)nv);
+    for (int k = 0; k < nv; ++k) {
+        const float* p = tris + 3 * k;
+        if (!isfinite(p[0]) || !isfinite(p[1]) || !isfinite(p[2])) { free(q); return 0; }
+        q[k].x = llround((double)p[0] * 1000000.0); q[k].y = llround((double)p[1] * 1000000.0);
+        q[k].z = llround((double)p[2] * 1000000.0); q[k].id = k;
+    }
+    qsort(q, (size_t)nv, sizeof(QV), cmp_qv);
+    int* weld = (int*)malloc(sizeof(int) * (size_t)nv);
+    int uid = -1;
+    for (int k = 0; k < nv; ++k) {
+        if (k == 0 || q[k].x != q[k - 1].x || q[k].y != q[k - 1].y || q[k].z != q[k - 1].z) ++uid;
+        weld[q[k].id] = uid;
+    }
+    free(q);
+    uint64_t* e = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n * 3);
+    int ne = 0;
+    for (int t = 0; t < n; ++t) {
+        int a = weld[3 * t], b = weld[3 * t + 1], c = weld[3 * t + 2];
+        if (a == b || b == c || c == a) continue;
+        int pr[3][2] = {{a, b}, {b, c}, {c, a}};
+        for (int k = 0; k < 3; ++k) {
+            unsigned lo = (unsigned)(pr[k][0] < pr[k][1] ? pr[k][0] : pr[k][1]);
+            unsigned hi = (unsigned)(pr[k][0] < pr[k][1] ? pr[k][1] : pr[k][0]);
+            e[ne++] = ((uint64_t)lo << 32) | hi;
+        }
+    }
+    free(weld);
+    if (ne == 0) { free(e); return 0; }
+    qsort(e, (size_t)ne, sizeof(uint64_t), cmp_u64);
+    int ok = 1;
+    for (int k = 0; k < ne;) {
+        int j = k;
+        while (j < ne && e[j] == e[k]) ++j;
+        if (j - k != 2) { ok = 0; break; }
+        k = j;
+    }
+    free(e);
+    return ok;
+}
+
+/* abi41.cu:1725-1747 */
+static int ray_x_hits(V3 p, V3 a, V3 b, V3 c) {
+    V3 dir = v3(1, 0, 0), e1 = vsub(b, a), e2 = vsub(c, a), h = vcross(dir, e2);
+    float det = vdot(e1, h);
+    if (fabsf(det) <= 1.0e-8f) return 0;
+    float inv_det = 1.0f / det;
+    V3 s = vsub(p, a);
+    float u = inv_det * vdot(s, h);
+    if (u < -1.0e-5f || u > 1.0f + 1.0e-5f) return 0;
+    V3 q = vcross(s, e1);
+    float v = inv_det * vdot(dir, q);
+    if (v < -1.0e-5f || u + v > 1.0f + 1.0e-5f) return 0;
+    return inv_det * vdot(e2, q) > 1.0e-6f;
+}
+
+/* Grid sizing abi41.cu:6123-6218, voxel distances abi41.cu:1787-1829. */
+static int build_sdf(OracleSolver* s, const float* tris, int n) {
+    s->sdf_ready = 0; s->sdf_signed = 0; s->dim[0] = s->dim[1] = s->dim[2] = 0;
+    s->origin[0] = s->origin[1] = s->origin[2] = 0.0f; s->voxel = 0.0f;
+    s->n_stris = n > 0 ? n : 0;
+    if (n <= 0) return 1;
+    if (!tris) return set_err("static triangle data is required for SDF build");
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < n * 3; ++k) {
+        const float* v = tris + 3 * k;
+        if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2])) return set_err("static triangle data contains non-finite coordinates");
+        for (int a = 0; a < 3; ++a) { lo[a] = fminf(lo[a], v[a]); hi[a] = fmaxf(hi[a], v[a]); }
+    }
+    const SsblXpbdConfig* c = &s->cfg;
+    float voxel = (isfinite(c->static_sdf_voxel_size) && c->static_sdf_voxel_size > 0.0f)
+                      ? c->static_sdf_voxel_size : fmaxf(fmaxf(c->collision_margin, 0.0f) * 0.5f, 0.002f);
+    int band = c->static_sdf_band_voxels > 0 ? c->static_sdf_band_voxels : 4; if (band < 1) band = 1;
+    int max_res = c->static_sdf_max_resolution > 0 ? c->static_sdf_max_resolution : 160; if (max_res < 16) max_res = 16;
+    float margin = fmaxf(c->collision_margin, 0.0f);
+    float expand = margin + (float)band * voxel + voxel * 2.0f;
+    float ext[3];
+    for (int a = 0; a < 3; ++a) { lo[a] = lo[a] - expand; hi[a] = hi[a] + expand; ext[a] = fmaxf(hi[a] - lo[a], voxel); }
+    float largest = fmaxf(ext[0], fmaxf(ext[1], ext[2]));
+    if (largest / voxel + 1.0f > (float)max_res) voxel = largest / (float)(max_res - 1 > 1 ? max_res - 1 : 1);
+    voxel = fmaxf(voxel, 1.0e-5f);
+    for (int a = 0; a < 3; ++a) {
+        int d = (int)ceilf(ext[a] / voxel) + 1;
+        if (d < 2) d = 2;
+        if (d > max_res) d = max_res;
+        s->dim[a] = d; s->origin[a] = lo[a];
+    }
+    s->voxel = voxel;
+    s->sdf_signed = mesh_closed(tris, n);
+    long long nvox = (long long)s->dim[0] * s->dim[1] * s->dim[2];
+    free(s->sdf); free(s->stris);
+    s->sdf = (float*)malloc(sizeof(float) * (size_t)nvox);
+    s->stris = (V3*)malloc(sizeof(V3) * (size_t)n * 3);
+    for (int k = 0; k < n * 3; ++k) s->stris[k] = v3(tris[3 * k], tris[3 * k + 1], tris[3 * k + 2]);
+    const int nx = s->dim[0], ny = s->dim[1];
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long vx = 0; vx < nvox; ++vx) {
+        int x = (int)(vx % nx), y = (int)((vx / nx) % ny), z = (int)(vx / ((long long)nx * ny));
+        V3 p = vadd(v3(s->origin[0], s->origin[1], s->origin[2]), v3((float)x * voxel, (float)y * voxel, (float)z * voxel));
+        V3 ray = vadd(p, v3(0.0f, voxel * 1.37e-4f, voxel * 2.11e-4f));
+        float best = 3.402823466e+38f;
+        int parity = 0;
+        for (int t = 0; t < n; ++t) {
+            V3 a = s->stris[3 * t], b = s->stris[3 * t + 1], c2 = s->stris[3 * t + 2];
+            V3 d = vsub(p, closest_on_tri(p, a, b, c2));
+            best = fminf(best, vdot(d, d));
+            if (s->sdf_signed && ray_x_hits(ray, a, b, c2)) parity ^= 1;
+        }
+        float dist = sqrtf(fmaxf(best, 0.0f));
+        if (s->sdf_signed && parity) dist = -dist;
+        s->sdf[vx] = dist;
+    }
+    s->sdf_ready = 1;
+    return 1;
+}
+
+static inline int sdf_idx(const OracleSolver* s, int x, int y, int z) { return (z * s->dim[1] + y) * s->dim[0] + x; }
+static inline float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+static float sdf_tri(const OracleSolver* s, float gx, float gy, float gz) {
+    int x0 = clampi((int)floorf(gx), 0, s->dim[0] - 1), y0 = clampi((int)floorf(gy), 0, s->dim[1] - 1);
+    int z0 = clampi((int)floorf(gz), 0, s->dim[2] - 1);
+    int x1 = clampi(x0 + 1, 0, s->dim[0] - 1), y1 = clampi(y0 + 1, 0, s->dim[1] - 1), z1 = clampi(z0 + 1, 0, s->dim[2] - 1);
+    float tx = gx - (float)x0, ty = gy - (float)y0, tz = gz - (float)z0;
+    const float* g = s->sdf;
+    float c0 = lerpf(lerpf(g[sdf_idx(s, x0, y0, z0)], g[sdf_idx(s, x1, y0, z0)], tx),
+                     lerpf(g[sdf_idx(s, x0, y1, z0)], g[sdf_idx(s, x1, y1, z0)], tx), ty);
+    float c1 = lerpf(lerpf(g[sdf_idx(s, x0, y0, z1)], g[sdf_idx(s, x1, y0, z1)], tx),
+                     lerpf(g[sdf_idx(s, x0, y1, z1)], g[sdf_idx(s, x1, y1, z1)], tx), ty);
+    return lerpf(c0, c1, tz);
+}
+/* abi41.cu:1645-1691 */
+static int sdf_sample(const OracleSolver* s, V3 p, float* out) {
+    if (s->dim[0] < 2 || s->dim[1] < 2 || s->dim[2] < 2 || s->voxel <= 0.0f) return 0;
+    float inv = 1.0f / s->voxel;
+    float gx = (p.x - s->origin[0]) * inv, gy = (p.y - s->origin[1]) * inv, gz = (p.z - s->origin[2]) * inv;
+    if (gx < 0.0f || gy < 0.0f || gz < 0.0f || gx > (float)(s->dim[0] - 1) || gy > (float)(s->dim[1] - 1) || gz > (float)(s->dim[2] - 1))
+        return 0;
+    *out = sdf_tri(s, gx, gy, gz);
+    return isfinite(*out);
+}
+/* abi41.cu:1693-1723 */
+static float sdf_clamped(const OracleSolver* s, V3 p) {
+    float inv = 1.0f / fmaxf(s->voxel, K_EPS);
+    float gx = fminf(fmaxf((p.x - s->origin[0]) * inv, 0.0f), (float)(s->dim[0] - 1));
+    float gy = fminf(fmaxf((p.y - s->origin[1]) * inv, 0.0f), (float)(s->dim[1] - 1));
+    float gz = fminf(fmaxf((p.z - s->origin[2]) * inv, 0.0f), (float)(s->dim[2] - 1));
+    return sdf_tri(s, gx, gy, gz);
+}
+/* abi41.cu:1749-1769 */
+static V3 nearest_static_normal(const OracleSolver* s, V3 p) {
+    V3 best = v3(0, 0, 1);
+    float best_sq = 3.402823466e+38f;
+    for (int t = 0; t < s->n_stris; ++t) {
+        V3 a = s->stris[3 * t], b = s->stris[3 * t + 1], c = s->stris[3 * t + 2];
+        V3 d = vsub(p, closest_on_tri(p, a, b, c));
+        float dsq = vdot(d, d);
+        if (dsq < best_sq) {
+            best_sq = dsq;
+            best = dsq > K_EPS * K_EPS ? normalize_or(d, best) : normalize_or(vcross(vsub(b, a), vsub(c, a)), best);
+        }
+    }
+    return normalize_or(best, v3(0, 0, 1));
+}
+/* abi41.cu:1771-1785 */
+static V3 sdf_normal(const OracleSolver* s, V3 p) {
+    float h = fmaxf(s->voxel, 1.0e-5f);
+    float dx = sdf_clamped(s, vadd(p, v3(h, 0, 0))) - sdf_clamped(s, vadd(p, v3(-h, 0, 0)));
+    float dy = sdf_clamped(s, vadd(p, v3(0, h, 0))) - sdf_clamped(s, vadd(p, v3(0, -h, 0)));
+    float dz = sdf_clamped(s, vadd(p, v3(0, 0, h))) - sdf_clamped(s, vadd(p, v3(0, 0, -h)));
+    V3 n = v3(dx, dy, dz);
+    float lsq = vdot(n, n);
+    if (!isfinite(lsq) || lsq <= 1.0e-12f) return nearest_static_normal(s, p);
+    return vmul(n, 1.0f / sqrtf(lsq));
+}
+
+/* ------------------------------------------------------ vertex stages -- */
+/* abi41.cu:910-949 */
+static int contact_response(OracleSolver* s, V3 n, float proxy, V3* vel) {
+    if (!vfinite(n) || !vfinite(*vel)) return 0;
+    float vn = vdot(*vel, n);
+    if (vn < 0.0f) *vel = vsub(*vel, vmul(n, vn));
+    int corrected = 0;
+    V3 tg = vsub(*vel, vmul(n, vdot(*vel, n)));
+    float tl = vlen(tg);
+    float damping = clamp01(s->cfg.contact_tangent_damping);
+    if (damping > 0.0f && tl > 1.0e-6f) { *vel = vsub(*vel, vmul(tg, damping)); corrected = 1; }
+    tg = vsub(*vel, vmul(n, vdot(*vel, n)));
+    tl = vlen(tg);
+    float fr = fmaxf(s->cfg.contact_friction, 0.0f);
+    if (fr > 0.0f && proxy > 0.0f && tl > 1.0e-6f) {
+        float drop = fminf(tl, fr * proxy);
+        if (drop > 1.0e-7f) { *vel = vsub(*vel, vmul(tg, drop / fmaxf(tl, K_EPS))); corrected = 1; }
+    }
+    if (corrected) cnt(s, C_FRICTION);
+    return corrected;
+}
+
+/* abi41.cu:1869-1925 (no force fields / pressure) */
+static void integrate_all(OracleSolver* s, float dt) {
+#pragma omp parallel for
+    for (int i = 0; i < s->V; ++i) {
+        s->prev[i] = s->pos[i];
+        if (!(s->w[i] > 0.0f)) { s->vel[i] = v3(0, 0, 0); s->pos[i] = s->rest[i]; continue; }
+        V3 a = vadd(v3(s->cfg.gravity[0], s->cfg.gravity[1], s->cfg.gravity[2]), v3(0, 0, 0));
+        V3 vel = vadd(s->vel[i], vmul(a, dt));
+        vel = vmul(vel, s->cfg.damping);
+        s->vel[i] = vel;
+        s->pos[i] = vadd(s->pos[i], vmul(vel, dt));
+    }
+}
+
+/* abi41.cu:3466-3509; pins kept per vertex (last entry of a vertex wins) */
+static void pin_all(OracleSolver* s, float dt) {
+#pragma omp parallel for
+    for (int i = 0; i < s->V; ++i) {
+        float wgt = s->pin_w[i];
+        if (!isfinite(wgt) || wgt < 0.05f) continue;
+        V3 target = s->pin_t[i];
+        if (wgt >= 0.75f || s->inv[i] <= 0.0f) { s->pos[i] = target; s->prev[i] = target; s->vel[i] = v3(0, 0, 0); continue; }
+        float relax = s->pin_relax[i];
+        if (relax <= 0.0f) continue;
+        V3 corrected = vadd(s->pos[i], vmul(vsub(target, s->pos[i]), relax));
+        V3 damped = vmul(s->vel[i], fmaxf(1.0f - relax, 0.0f));
+        s->pos[i] = corrected;
+        s->prev[i] = vsub(corrected, vmul(damped, fmaxf(dt, K_EPS)));
+        s->vel[i] = damped;
+    }
+}
+
+/* abi41.cu:1927-1980 as a snapshot-Jacobi gather */
+static void spring_all(OracleSolver* s, float dt) {
+    memcpy(s->snap, s->pos, sizeof(V3) * (size_t)s->V);
+    const float alpha = fmaxf(s->cfg.stretch_compliance, 0.0f) / fmaxf(dt * dt, K_EPS);
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < s->V; ++v) {
+        V3 dp = s->snap[v], dprev = s->prev[v];
+        for (int k = s->sp_off[v]; k < s->sp_off[v + 1]; ++k) {
+            int o = s->sp_other[k], is_j = s->sp_side[k];
+            int i = is_j ? o : v, j = is_j ? v : o;
+            float wi = s->w[i], wj = s->w[j], weight = wi + wj;
+            if (weight <= 0.0f) continue;
+            float rest = s->sp_rest[k];
+            V3 delta = vsub(s->snap[j], s->snap[i]);
+            float len = sqrtf(fmaxf(vdot(delta, delta), K_EPS));
+            float c = len - rest;
+            float dl = -c / (weight + alpha);
+            V3 corr = vmul(delta, 0.18f * dl / fmaxf(len, K_EPS));
+            float cl = sqrtf(fmaxf(vdot(corr, corr), 0.0f));
+            float mc = fmaxf(0.0025f, fminf(fmaxf(rest, 0.0f) * 0.10f, 0.025f));
+            if (cl > mc) { corr = vmul(corr, mc / fmaxf(cl, K_EPS)); if (!is_j) cnt(s, C_HARD); }
+            float wself = is_j ? wj : wi;
+            if (wself > 0.0f) {
+                V3 d = is_j ? vmul(corr, wj) : vmul(corr, -wi);
+                dp = vadd(dp, d);
+                if (c > 0.0f) dprev = vadd(dprev, vmul(d, 0.08f));
+            }
+        }
+        s->pos[v] = dp;
+        s->prev[v] = dprev;
+    }
+}
+
+/* abi41.cu:2710-2803 as a snapshot gather over each vertex's tethers */
+static void tether_all(OracleSolver* s, float dt) {
+    memcpy(s->snap, s->pos, sizeof(V3) * (size_t)s->V);
+    const float th = s->cfg.cloth_thickness;
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < s->V; ++v) {
+        V3 dp = s->snap[v], dprev = s->prev[v];
+        for (int k = s->te_off[v]; k < s->te_off[v + 1]; ++k) {
+            int o = s->te_other[k], is_j = s->te_side[k], counter = !is_j;
+            int i = is_j ? o : v, j = is_j ? v : o;
+            float wi = s->w[i], wj = s->w[j], weight = wi + wj;
+            if (!isfinite(weight) || weight <= 0.0f) { if (counter) cnt(s, C_TACK_GUARD); continue; }
+            V3 pi = s->snap[i], pj = s->snap[j];
+            if (!vfinite(pi) || !vfinite(pj)) { if (counter) cnt(s, C_TACK_GUARD); continue; }
+            V3 dx = vsub(pj, pi);
+            float lsq = lensq_xyz(dx), rest = s->te_rest[k];
+            if (!isfinite(lsq) || lsq <= 1.0e-10f || !isfinite(rest) || rest <= K_EPS) { if (counter) cnt(s, C_TACK_GUARD); continue; }
+            float inv_len = 1.0f / sqrtf(lsq), len = lsq * inv_len, stretch = len - rest;
+            if (!isfinite(stretch) || stretch <= 0.0f) continue;
+            dx = vmul(dx, inv_len);
+            float bc = fmaxf(s->cfg.lra_compliance, 1.0e-12f);
+            float stiff = (1.0f / bc) * 500000.0f;
+            float alpha = (bc / 500000.0f) / fmaxf(dt * dt, K_EPS);
+            float sw = stiff / fmaxf(stiff + 500000.0f, 1.0f);
+            float dl = -stretch / fmaxf(weight + alpha, K_EPS);
+            V3 corr = vmul(dx, 0.35f * sw * dl);
+            if (!vfinite(corr)) { if (counter) cnt(s, C_TACK_GUARD); continue; }
+            float cl = vlen(corr);
+            float mc = fmaxf(5.0e-4f, fminf(fmaxf(rest, th) * 0.20f, 0.035f));
+            if (!isfinite(cl) || cl <= 0.0f) continue;
+            if (cl > mc) { corr = vmul(corr, mc / fmaxf(cl, K_EPS)); if (counter) cnt(s, C_TACK_GUARD); }
+            int has_th = th > 0.0f;
+            float cap = has_th ? 0.0025f : 0.012f;
+            float rest_limit = fmaxf(rest, 0.0f) * (has_th ? 0.02f : 0.08f);
+            float th_limit = has_th ? th * 0.12f : cap;
+            float applied = fmaxf(5.0e-4f, fminf(fminf(rest_limit, th_limit), cap));
+            if (is_j) {
+                if (wj > 0.0f) { V3 d = limit_delta(vmul(corr, wj / fmaxf(weight, K_EPS)), applied); dp = vadd(dp, d); dprev = vadd(dprev, vmul(d, 0.32f)); }
+            } else if (wi > 0.0f) {
+                V3 d = limit_delta(vmul(corr, -wi / fmaxf(weight, K_EPS)), applied); dp = vadd(dp, d); dprev = vadd(dprev, vmul(d, 0.32f));
+            }
+            if (counter) cnt(s, C_LRA);
+        }
+        s->pos[v] = dp;
+        s->prev[v] = dprev;
+    }
+}
+
+/* Bend correction shared by the colour kernel and the Jacobi form
+ * (abi41.cu:2805-2970). Returns 1 when applied; *guard as the reference counts. */
+static int bend_corr(OracleSolver* s, float dt, V3 pi, V3 pj, float wi, float wj, float rest, V3* out, int* guard) {
+    *guard = 0;
+    float weight = wi + wj;
+    if (!isfinite(weight) || weight <= 0.0f) return 0;
+    if (!isfinite(rest) || rest <= K_EPS) { *guard = 1; return 0; }
+    if (!vfinite(pi) || !vfinite(pj)) { *guard = 1; return 0; }
+    V3 delta = vsub(pj, pi);
+    float lsq = lensq_xyz(delta);
+    if (!isfinite(lsq) || lsq <= 1.0e-10f) { *guard = 1; return 0; }
+    float inv_len = 1.0f / sqrtf(lsq), len = lsq * inv_len, c = len - rest;
+    if (!isfinite(c) || fabsf(c) <= 1.0e-6f) return 0;
+    float alpha = fmaxf(s->cfg.bend_compliance, 0.0f) / fmaxf(dt * dt, K_EPS);
+    float dl = -c / fmaxf(weight + alpha, K_EPS);
+    V3 corr = vmul(delta, 0.10f * dl * inv_len);
+    if (!vfinite(corr)) { *guard = 1; return 0; }
+    float cl = vlen(corr);
+    float mc = fmaxf(2.5e-4f, fminf(fmaxf(rest, s->cfg.cloth_thickness) * 0.08f, 0.020f));
+    if (!isfinite(cl) || cl <= 0.0f) return 0;
+    if (cl > mc) { corr = vmul(corr, mc / fmaxf(cl, K_EPS)); *guard = 1; }
+    *out = corr;
+    return 1;
+}
+
+/* abi41.cu:2886-2970, per colour in order, in place */
+static void bends_by_color(OracleSolver* s, float dt) {
+    for (int k = 0; k + 1 < s->n_bend_colors + 1 && k < s->n_bend_colors; ++k) {
+        int start = s->bend_colors[k], count = s->bend_colors[k + 1] - start;
+#pragma omp parallel for
+        for (int l = 0; l < count; ++l) {
+            int b = start + l;
+            if (b < 0 || b >= s->B) { cnt(s, C_BEND_GUARD); continue; }
+            int i = s->bends[2 * b], j = s->bends[2 * b + 1];
+            if (i < 0 || j < 0 || i >= s->V || j >= s->V || i == j) { cnt(s, C_BEND_GUARD); continue; }
+            V3 corr; int guard;
+            int ok = bend_corr(s, dt, s->pos[i], s->pos[j], s->w[i], s->w[j], s->bend_rest[b], &corr, &guard);
+            if (guard) cnt(s, C_BEND_GUARD);
+            if (!ok) continue;
+            float wi = s->w[i], wj = s->w[j];
+            if (wi > 0.0f) { V3 d = vmul(corr, -wi); s->pos[i] = vadd(s->pos[i], d); s->prev[i] = vadd(s->prev[i], vmul(d, 0.06f)); }
+            if (wj > 0.0f) { V3 d = vmul(corr, wj); s->pos[j] = vadd(s->pos[j], d); s->prev[j] = vadd(s->prev[j], vmul(d, 0.06f)); }
+            cnt(s, C_WINGS);
+        }
+    }
+}
+
+/* abi41.cu:2805-2884: all bends at once (no colours) as a snapshot gather */
+static void bends_jacobi(OracleSolver* s, float dt) {
+    memcpy(s->snap, s->pos, sizeof(V3) * (size_t)s->V);
+#pragma omp parallel for
+    for (int v = 0; v < s->V; ++v) {
+        V3 dp = s->snap[v], dprev = s->prev[v];
+        for (int k = s->bj_off[v]; k < s->bj_off[v + 1]; ++k) {
+            int o = s->bj_other[k], is_j = s->bj_side[k];
+            int i = is_j ? o : v, j = is_j ? v : o;
+            V3 corr; int guard;
+            int ok = bend_corr(s, dt, s->snap[i], s->snap[j], s->w[i], s->w[j], s->bj_rest[k], &corr, &guard);
+            if (!is_j) { if (guard) cnt(s, C_BEND_GUARD); if (ok) cnt(s, C_WINGS); }
+            if (!ok) continue;
+            float wself = is_j ? s->w[j] : s->w[i];
+            if (wself > 0.0f) {
+                V3 d = is_j ? vmul(corr, s->w[j]) : vmul(corr, -s->w[i]);
+                dp = vadd(dp, d); dprev = vadd(dprev, vmul(d, 0.06f));
+            }
+        }
+        s->pos[v] = dp; s->prev[v] = dprev;
+    }
+}
+
+/* abi41.cu:3511-3590 */
+static void analytic_all(OracleSolver* s, float dt) {
+    const SsblXpbdRuntimeColliders* c = &s->col;
+    const float margin = fmaxf(s->cfg.collision_margin, 0.0f), sdt = fmaxf(dt, K_EPS);
+#pragma omp parallel for
+    for (int i = 0; i < s->V; ++i) {
+        if (s->inv[i] <= 0.0f) continue;
+        V3 p = s->pos[i], vel = s->vel[i];
+        int hit = 0;
+        if (c->use_ground && p.z < c->ground_height + margin) {
+            float tz = c->ground_height + margin, pen = tz - p.z;
+            V3 n = v3(0, 0, 1);
+            float inward = fmaxf(-vdot(vel, n), 0.0f);
+            p.z = tz;
+            contact_response(s, n, inward + pen / sdt, &vel);
+            hit = 1;
+        }
+        if (c->use_sphere && c->sphere_radius > 0.0f) {
+            V3 ctr = v3(c->sphere_center[0], c->sphere_center[1], c->sphere_center[2]);
+            V3 d = vsub(p, ctr);
+            float dist = sqrtf(fmaxf(vdot(d, d), K_EPS)), target = c->sphere_radius + margin;
+            if (dist < target) {
+                V3 n = dist > K_EPS ? vmul(d, 1.0f / dist) : v3(0, 0, 1);
+                float pen = target - dist, inward = fmaxf(-vdot(vel, n), 0.0f);
+                p = vadd(ctr, vmul(n, target));
+                contact_response(s, n, inward + pen / sdt, &vel);
+                hit = 1;
+            }
+        }
+        if (c->use_wall) {
+            V3 o = v3(c->wall_origin[0], c->wall_origin[1], c->wall_origin[2]);
+            V3 n = v3(c->wall_normal[0], c->wall_normal[1], c->wall_normal[2]);
+            float nl = sqrtf(fmaxf(vdot(n, n), K_EPS));
+            n = vmul(n, 1.0f / nl);
+            float gap = vdot(vsub(p, o), n);
+            if (gap < margin) {
+                float pen = margin - gap, inward = fmaxf(-vdot(vel, n), 0.0f);
+                p = vadd(p, vmul(n, margin - gap));
+                contact_response(s, n, inward + pen / sdt, &vel);
+                hit = 1;
+            }
+        }
+        s->pos[i] = p;
+        if (hit) { s->vel[i] = vel; s->prev[i] = vsub(p, vmul(vel, sdt)); }
+    }
+}
+
+/* abi41.cu:1831-1867 */
+static void sdf_all(OracleSolver* s, float dt) {
+    const float margin = fmaxf(s->cfg.collision_margin, 0.0f);
+    if (margin <= 0.0f) return;
+#pragma omp parallel for
+    for (int i = 0; i < s->V; ++i) {
+        if (s->inv[i] <= 0.0f) continue;
+        V3 p = s->pos[i];
+        float d = 0.0f;
+        if (!sdf_sample(s, p, &d) || d >= margin) continue;
+        V3 n = sdf_normal(s, p);
+        if (!vfinite(n)) continue;
+        float pen = margin - d;
+        if (!isfinite(pen) || pen <= 0.0f) continue;
+        V3 corrected = vadd(p, vmul(n, pen)), vel = s->vel[i];
+        float inward = fmaxf(-vdot(vel, n), 0.0f);
+        contact_response(s, n, inward + pen / fmaxf(dt, K_EPS), &vel);
+        s->pos[i] = corrected; s->vel[i] = vel; s->prev[i] = vsub(corrected, vmul(vel, fmaxf(dt, K_EPS)));
+        cnt(s, C_SDF);
+    }
+}
+
+/* abi41.cu:5846-5884 */
+static void velocity_all(OracleSolver* s, float dt) {
+    const float sdt = fmaxf(dt, K_EPS);
+    const float max_delta = fmaxf(2.0e-4f, fmaxf(s->cfg.cloth_thickness, 0.0f) * 0.35f), max_speed = max_delta / sdt;
+#pragma omp parallel for
+    for (int i = 0; i < s->V; ++i) {
+        if (!(s->w[i] > 0.0f)) { s->vel[i] = v3(0, 0, 0); continue; }
+        V3 measured = vmul(vsub(s->pos[i], s->prev[i]), 1.0f / sdt), base = s->vel[i];
+        if (!vfinite(measured) || !vfinite(base)) { s->vel[i] = v3(0, 0, 0); continue; }
+        V3 proj = vsub(measured, base);
+        float pdb = vdot(proj, base);
+        float scale = (isfinite(pdb) && pdb > 0.0f) ? 0.9f : 1.0f;
+        V3 fb = vmul(proj, scale);
+        float fs = vlen(fb);
+        if (scale < 1.0f && isfinite(fs) && fs > max_speed && fs > K_EPS) fb = vmul(fb, max_speed / fs);
+        if (!vfinite(fb)) fb = v3(0, 0, 0);
+        s->vel[i] = vadd(base, fb);
+    }
+}
+
+/* ----------------------------------------------------- self collision -- */
+static int fast_mode(const OracleSolver* s) { return s->cfg.self_collision_mode == 1; }
+
+static void accumulate(OracleSolver* s, int i, V3 d) {
+    if (i < 0 || i >= s->V || !(s->inv[i] > 0.0f)) return;
+    long long* a = s->acc + 4 * (size_t)i;
+    long long x = to_fix(d.x), y = to_fix(d.y), z = to_fix(d.z);
+#pragma omp atomic
+    a[0] += x;
+#pragma omp atomic
+    a[1] += y;
+#pragma omp atomic
+    a[2] += z;
+#pragma omp atomic
+    a[3] += 1;
+}
+
+/* abi41.cu:733-760 */
+static int normal_bucket(float v) { return v > 0.45f ? 2 : (v < -0.45f ? 0 : 1); }
+static unsigned cluster_key(int type, V3 p, V3 n, float cell) {
+    float c = fmaxf(cell, 1.0e-3f);
+    unsigned key = bucket_of(cell_of(p.x, c), cell_of(p.y, c), cell_of(p.z, c), 1 << 20);
+    unsigned nk = (unsigned)normal_bucket(n.x) | ((unsigned)normal_bucket(n.y) << 2) | ((unsigned)normal_bucket(n.z) << 4);
+    key ^= nk * 2654435761u;
+    key ^= (unsigned)(type + 1) * 2246822519u;
+    return key;
+}
+typedef struct { unsigned keys[16]; unsigned char counts[16]; int n; } Clusters;
+typedef struct { int ids[64]; int n; } Seen;
+static int accept_slot(int type) { return type == 0 ? C_F_ACC_VV : (type == 1 ? C_F_ACC_VT : C_F_ACC_EE); }
+/* abi41.cu:793-832 */
+static int local_accept(OracleSolver* s, int type, unsigned key, Clusters* cl) {
+    if (!fast_mode(s)) return 1;
+    if (cl) {
+        int n = cl->n < 16 ? cl->n : 16;
+        for (int i = 0; i < n; ++i)
+            if (cl->keys[i] == key) {
+                if (cl->counts[i] >= 1) { cnt(s, C_F_REJ_OWN); return 0; }
+                cl->counts[i] += 1; cnt(s, C_CLUST_OWNED); cnt(s, accept_slot(type)); return 1;
+            }
+        if (cl->n >= 16) { cnt(s, C_F_REJ_OWN); return 0; }
+        cl->keys[cl->n] = key; cl->counts[cl->n] = 1; cl->n += 1;
+        cnt(s, C_CLUSTERS); cnt(s, C_CLUST_OWNED);
+    }
+    cnt(s, accept_slot(type));
+    return 1;
+}
+/* abi41.cu:762-791 */
+static int note_seen(OracleSolver* s, int key, Seen* seen) {
+    if (!fast_mode(s)) return 1;
+    cnt(s, C_F_SEEN);
+    if (!seen) return 1;
+    int lim = seen->n < 64 ? seen->n : 64;
+    for (int i = 0; i < lim; ++i) if (seen->ids[i] == key) { cnt(s, C_F_REJ_DUP); return 0; }
+    if (seen->n >= 64) { cnt(s, C_SELF_OVF); cnt(s, C_F_REJ_OWN); return 0; }
+    seen->ids[seen->n++] = key;
+    return 1;
+}
+static void filter_count(OracleSolver* s, int slot) { if (fast_mode(s)) cnt(s, slot); }
+
+static int tri_ok(const OracleSolver* s, const int* t) {
+    return t[0] >= 0 && t[1] >= 0 && t[2] >= 0 && t[0] < s->V && t[1] < s->V && t[2] < s->V && t[0] != t[1] && t[1] != t[2] && t[0] != t[2];
+}
+static int edge_ok(const OracleSolver* s, const int* e) { return e[0] >= 0 && e[1] >= 0 && e[0] < s->V && e[1] < s->V && e[0] != e[1]; }
+
+/* Cell box of a primitive with the 64-cell guard (abi41.cu:871-900). */
+static void prim_cells(OracleSolver* s, V3 lo, V3 hi, V3 fb, int* r, int count_guard) {
+    float c = s->cell;
+    r[0] = cell_of(lo.x, c); r[1] = cell_of(hi.x, c); r[2] = cell_of(lo.y, c); r[3] = cell_of(hi.y, c);
+    r[4] = cell_of(lo.z, c); r[5] = cell_of(hi.z, c);
+    long long sx = (long long)r[1] - r[0] + 1, sy = (long long)r[3] - r[2] + 1, sz = (long long)r[5] - r[4] + 1;
+    if (sx <= 0 || sy <= 0 || sz <= 0) return;
+    if (sx * sy * sz <= MAX_PRIM_CELLS) return;
+    int fx = cell_of(fb.x, c), fy = cell_of(fb.y, c), fz = cell_of(fb.z, c);
+    r[0] = r[1] = fx; r[2] = r[3] = fy; r[4] = r[5] = fz;
+    if (count_guard) cnt(s, C_SELF_OVF);
+}
+/* abi41.cu:4632-4694 / 5532-5593: cell box of triangle or edge k */
+static int tri_box(OracleSolver* s, int k, int* r, int count_guard) {
+    const int* t = s->tris + 3 * k;
+    if (!tri_ok(s, t)) return 0;
+    V3 a = s->pos[t[0]], b = s->pos[t[1]], c = s->pos[t[2]];
+    float m = s->radius * 1.8f;
+    V3 lo = v3(fminf(a.x, fminf(b.x, c.x)) - m, fminf(a.y, fminf(b.y, c.y)) - m, fminf(a.z, fminf(b.z, c.z)) - m);
+    V3 hi = v3(fmaxf(a.x, fmaxf(b.x, c.x)) + m, fmaxf(a.y, fmaxf(b.y, c.y)) + m, fmaxf(a.z, fmaxf(b.z, c.z)) + m);
+    prim_cells(s, lo, hi, vmul(vadd(vadd(a, b), c), 1.0f / 3.0f), r, count_guard);
+    return 1;
+}
+static int edge_box(OracleSolver* s, int k, int* r, int count_guard) {
+    const int* e = s->edges + 2 * k;
+    if (!edge_ok(s, e)) return 0;
+    V3 a = s->pos[e[0]], b = s->pos[e[1]];
+    float m = s->radius * 1.8f;
+    V3 lo = v3(fminf(a.x, b.x) - m, fminf(a.y, b.y) - m, fminf(a.z, b.z) - m);
+    V3 hi = v3(fmaxf(a.x, b.x) + m, fmaxf(a.y, b.y) + m, fmaxf(a.z, b.z) + m);
+    prim_cells(s, lo, hi, vmul(vadd(a, b), 0.5f), r, count_guard);
+    return 1;
+}
+
+/* Counting sort by bucket id; entries of a bucket in increasing primitive
+ * order; per-bucket overflow counted beyond 32 like the reference's slot
+ * insertion (abi41.cu:4550-4575, 4632-4694, 5532-5593). */
+static void hash_vertices(OracleSolver* s) {
+    int nb = s->nvb;
+    int* count = (int*)calloc((size_t)nb, sizeof(int));
+    for (int i = 0; i < s->V; ++i) {
+        V3 p = s->pos[i];
+        int cx = cell_of(p.x, s->cell), cy = cell_of(p.y, s->cell), cz = cell_of(p.z, s->cell);
+        int b = (int)bucket_of(cx, cy, cz, nb);
+        s->vcell[4 * i] = cx; s->vcell[4 * i + 1] = cy; s->vcell[4 * i + 2] = cz; s->vcell[4 * i + 3] = b;
+        if (count[b]++ >= BUCKET_SLOTS) cnt(s, C_SELF_OVF);
+    }
+    s->vb_start[0] = 0;
+    for (int b = 0; b < nb; ++b) s->vb_start[b + 1] = s->vb_start[b] + count[b];
+    memcpy(count, s->vb_start, sizeof(int) * (size_t)nb);
+    for (int i = 0; i < s->V; ++i) s->vb_ent[count[s->vcell[4 * i + 3]]++] = i;
+    free(count);
+}
+static void hash_prims(OracleSolver* s, int tri) {
+    int n = tri ? s->T : s->E, nb = tri ? s->ntb : s->neb;
+    int* start = tri ? s->tb_start : s->eb_start;
+    int* ent = tri ? s->tb_ent : s->eb_ent;
+    int* count = (int*)calloc((size_t)nb, sizeof(int));
+    int r[6];
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int k = 0; k < n; ++k) {
+            int ok = tri ? tri_box(s, k, r, pass == 0) : edge_box(s, k, r, pass == 0);
+            if (!ok) continue;
+            for (int z = r[4]; z <= r[5]; ++z)
+                for (int y = r[2]; y <= r[3]; ++y)
+                    for (int x = r[0]; x <= r[1]; ++x) {
+                        int b = (int)bucket_of(x, y, z, nb);
+                        if (pass == 0) { if (count[b]++ >= BUCKET_SLOTS) cnt(s, C_SELF_OVF); }
+                        else ent[count[b]++] = k;
+                    }
+        }
+        if (pass == 0) {
+            start[0] = 0;
+            for (int b = 0; b < nb; ++b) start[b + 1] = start[b] + count[b];
+            memcpy(count, start, sizeof(int) * (size_t)nb);
+        }
+    }
+    if (tri) s->tb_total = start[nb]; else s->eb_total = start[nb];
+    free(count);
+}
+
+/* abi41.cu:4696-4717 */
+static int vv_valid(OracleSolver* s, int src, int other, float target, float onset) {
+    if (src < 0 || other < 0 || src >= s->V || other >= s->V || src == other || target <= 0.0f || onset <= target || !(s->inv[src] > 0.0f))
+        return 0;
+    V3 rd = vsub(s->rest[src], s->rest[other]);
+    float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    if (vdot(rd, rd) < skip * skip) return 0;
+    V3 cd = vsub(s->pos[src], s->pos[other]), pd = vsub(s->prev[src], s->prev[other]);
+    return vdot(cd, cd) < onset * onset || vdot(pd, pd) < onset * onset;
+}
+/* abi41.cu:4738-4812 */
+static void neighbors_all(OracleSolver* s) {
+    const float target = s->radius, onset = fmaxf(target * 1.8f, target + K_EPS);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int src = 0; src < s->V; ++src) {
+        if (target <= 0.0f) { s->nb_count[src] = 0; continue; }
+        int acc = 0;
+        if (s->vhash) {
+            V3 p = s->pos[src];
+            int cx = cell_of(p.x, s->cell), cy = cell_of(p.y, s->cell), cz = cell_of(p.z, s->cell);
+            for (int dz = -1; dz <= 1 && acc < NB_SLOTS; ++dz)
+                for (int dy = -1; dy <= 1 && acc < NB_SLOTS; ++dy)
+                    for (int dx = -1; dx <= 1 && acc < NB_SLOTS; ++dx) {
+                        int qx = cx + dx, qy = cy + dy, qz = cz + dz;
+                        int b = (int)bucket_of(qx, qy, qz, s->nvb), st = s->vb_start[b];
+                        int lim = s->vb_start[b + 1] - st; if (lim > BUCKET_SLOTS) lim = BUCKET_SLOTS;
+                        for (int k = 0; k < lim && acc < NB_SLOTS; ++k) {
+                            int o = s->vb_ent[st + k];
+                            if (s->vcell[4 * o] != qx || s->vcell[4 * o + 1] != qy || s->vcell[4 * o + 2] != qz || !vv_valid(s, src, o, target, onset)) continue;
+                            s->nb_idx[src * NB_SLOTS + acc++] = o;
+                        }
+                    }
+        } else {
+            for (int o = 0; o < s->V && acc < NB_SLOTS; ++o)
+                if (vv_valid(s, src, o, target, onset)) s->nb_idx[src * NB_SLOTS + acc++] = o;
+        }
+        if (acc >= NB_SLOTS) cnt(s, C_SELF_OVF);
+        s->nb_count[src] = acc;
+    }
+}
+
+/* abi41.cu:4816-4951 */
+static void vv_all(OracleSolver* s) {
+    const float target = s->radius;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int src = 0; src < s->V; ++src) {
+        if (!(s->inv[src] > 0.0f)) continue;
+        int count = s->nb_count[src];
+        if (count == 0) continue;
+        V3 pc = s->pos[src], pp = s->prev[src];
+        float r_self = target * 0.5f;
+        int lim = count < NB_SLOTS ? count : NB_SLOTS;
+        Clusters cl; cl.n = 0;
+        for (int n = 0; n < lim; ++n) {
+            int o = s->nb_idx[src * NB_SLOTS + n];
+            if (o < 0 || o >= s->V || o == src) continue;
+            if (fast_mode(s)) cnt(s, C_F_SEEN); else cnt(s, C_SELF_CAND);
+            V3 qc = s->pos[o], qp = s->prev[o];
+            float th = r_self + target * 0.5f;
+            if (th <= 0.0f) continue;
+            float scale = !(s->inv[o] > 0.0f) ? 1.0f : 0.5f;
+            V3 resp = v3(0, 0, 0);
+            int hit = 0;
+            V3 dref = vsub(pp, qp);
+            float cc = vdot(dref, dref) - th * th;
+            V3 rel = vsub(vsub(pc, pp), vsub(qc, qp));
+            float a = vdot(rel, rel), b = vdot(dref, rel);
+            if (cc >= 0.0f && b < 0.0f && a > 1.0e-5f) {
+                float disc = b * b - a * cc;
+                if (disc >= 0.0f) {
+                    float t = (-b - sqrtf(disc)) / a;
+                    if (t > 0.0f && t <= 1.0f) {
+                        float sg = 1.0f - t;
+                        V3 ph = vadd(vmul(pp, sg), vmul(pc, t)), qh = vadd(vmul(qp, sg), vmul(qc, t));
+                        V3 nrm = vsub(ph, qh);
+                        float nl = vdot(nrm, nrm);
+                        if (nl > K_EPS) {
+                            nrm = vmul(nrm, 1.0f / sqrtf(nl));
+                            float vn = vdot(vsub(vsub(pc, ph), vsub(qc, qh)), nrm);
+                            if (vn > 0.0f) { resp = vmul(nrm, -vn * scale); hit = 1; }
+                        }
+                    }
+                }
+            }
+            if (!hit) {
+                V3 delta = vsub(pc, qc);
+                float dsq = vdot(delta, delta);
+                if (dsq >= th * th) continue;
+                V3 nrm = v3(0, 0, 1);
+                float dist = sqrtf(fmaxf(dsq, K_EPS));
+                if (dsq > K_EPS) nrm = vmul(delta, 1.0f / dist);
+                else {
+                    V3 rd = vsub(s->rest[src], s->rest[o]);
+                    float rl = vdot(rd, rd);
+                    if (rl > K_EPS) nrm = vmul(rd, 1.0f / sqrtf(rl));
+                    dist = 0.0f;
+                }
+                resp = vmul(nrm, fminf((th - dist) * scale, th * 0.35f));
+                hit = 1;
+            }
+            if (hit && vdot(resp, resp) > K_EPS) {
+                float ml = fmaxf(th * 0.35f, 1.0e-4f), rl = vlen(resp);
+                if (rl > ml) resp = vmul(resp, ml / rl);
+                if (fast_mode(s)) {
+                    V3 nrm = vmul(resp, 1.0f / fmaxf(vlen(resp), K_EPS));
+                    unsigned key = cluster_key(0, vmul(vadd(pc, qc), 0.5f), nrm, fmaxf(th * 2.5f, 1.0e-3f));
+                    if (!local_accept(s, 0, key, &cl)) continue;
+                    cnt(s, C_SELF_CAND);
+                }
+                accumulate(s, src, resp);
+                cnt(s, C_EXACT);
+            }
+        }
+    }
+}
+
+static int rest_vt_neighbor(OracleSolver* s, int vtx, const int* t, float target, float onset) {
+    if (vtx == t[0] || vtx == t[1] || vtx == t[2]) return 1;
+    V3 rp = s->rest[vtx];
+    V3 rd = vsub(rp, closest_on_tri(rp, s->rest[t[0]], s->rest[t[1]], s->rest[t[2]]));
+    float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    return vdot(rd, rd) < skip * skip;
+}
+/* abi41.cu:4990-5107 */
+static int vt_pair(OracleSolver* s, int vtx, int tri, float target, float onset, Clusters* cl) {
+    if (tri < 0 || tri >= s->T || target <= 0.0f || onset <= target) return 0;
+    const int* t = s->tris + 3 * tri;
+    if (!tri_ok(s, t)) return 0;
+    if (rest_vt_neighbor(s, vtx, t, target, onset)) { filter_count(s, C_F_REJ_REST); return 0; }
+    V3 p = s->pos[vtx], a = s->pos[t[0]], b = s->pos[t[1]], c = s->pos[t[2]];
+    V3 q = closest_on_tri(p, a, b, c), d = vsub(p, q);
+    float dsq = vdot(d, d), dist = sqrtf(fmaxf(dsq, K_EPS));
+    if (dist >= onset) return 0;
+    V3 nrm = v3(0, 0, 1);
+    if (dsq > K_EPS) nrm = vmul(d, 1.0f / dist);
+    else {
+        nrm = vcross(vsub(b, a), vsub(c, a));
+        float nl = vdot(nrm, nrm);
+        if (nl > K_EPS) nrm = vmul(nrm, 1.0f / sqrtf(nl));
+        else {
+            V3 rv = s->rest[vtx];
+            V3 rd = vsub(rv, closest_on_tri(rv, s->rest[t[0]], s->rest[t[1]], s->rest[t[2]]));
+            float rl = vdot(rd, rd);
+            if (rl > K_EPS) nrm = vmul(rd, 1.0f / sqrtf(rl));
+        }
+        d = vmul(nrm, dist);
+        dist = 0.0f;
+    }
+    if (fast_mode(s)) {
+        unsigned key = cluster_key(1, q, v3(0, 0, 0), fmaxf(onset * 12.0f, 1.0e-3f));
+        if (!local_accept(s, 1, key, cl)) return 1;
+    }
+    cnt(s, C_SELF_CAND);
+    float wa, wb, wc;
+    barycentric(q, a, b, c, &wa, &wb, &wc);
+    float pen = target - dist, push;
+    if (pen > 0.0f) push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    else { float x = 1.0f - fminf(dist / onset, 1.0f); push = fminf(x * x * target * 0.06f, target * 0.04f); }
+    float wv = s->inv[vtx], wta = s->inv[t[0]] * wa, wtb = s->inv[t[1]] * wb, wtc = s->inv[t[2]] * wc;
+    float total = wv + wta + wtb + wtc;
+    if (push <= 0.0f || total <= 0.0f) return 1;
+    V3 delta = vmul(nrm, push / total);
+    if (wv > 0.0f) accumulate(s, vtx, vmul(delta, wv));
+    if (wta > 0.0f) accumulate(s, t[0], vmul(delta, -wta));
+    if (wtb > 0.0f) accumulate(s, t[1], vmul(delta, -wtb));
+    if (wtc > 0.0f) accumulate(s, t[2], vmul(delta, -wtc));
+    cnt(s, C_SOFT);
+    return 1;
+}
+static int budget(const OracleSolver* s) {
+    int m = s->cfg.max_self_collision_neighbors;
+    if (m < 1) m = 1;
+    if (m > BUCKET_SLOTS) m = BUCKET_SLOTS;
+    if (fast_mode(s) && m > 16) m = 16;
+    return m;
+}
+/* abi41.cu:5109-5224 */
+static void vt_all(OracleSolver* s) {
+    const float target = s->radius, onset = fmaxf(target * 1.8f, target + K_EPS);
+    if (target <= 0.0f) return;
+    const int bud = budget(s);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int vtx = 0; vtx < s->V; ++vtx) {
+        int acc = 0;
+        Clusters cl; cl.n = 0;
+        if (s->thash) {
+            V3 p = s->pos[vtx];
+            int b = (int)bucket_of(cell_of(p.x, s->cell), cell_of(p.y, s->cell), cell_of(p.z, s->cell), s->ntb);
+            int st = s->tb_start[b], lim = s->tb_start[b + 1] - st;
+            if (lim > BUCKET_SLOTS) lim = BUCKET_SLOTS;
+            if (!fast_mode(s)) {
+                for (int k = 0; k < lim && acc < bud; ++k) if (vt_pair(s, vtx, s->tb_ent[st + k], target, onset, NULL)) ++acc;
+            } else {
+                Seen seen; seen.n = 0;
+                for (int k = 0; k < lim && acc < bud; ++k) {
+                    int tri = s->tb_ent[st + k];
+                    if (!note_seen(s, tri, &seen)) continue;
+                    if (vt_pair(s, vtx, tri, target, onset, &cl)) ++acc;
+                }
+            }
+        } else {
+            for (int tri = 0; tri < s->T && acc < bud; ++tri) {
+                if (!note_seen(s, tri, NULL)) continue;
+                if (vt_pair(s, vtx, tri, target, onset, &cl)) ++acc;
+            }
+        }
+    }
+}
+
+static int rest_ee_neighbor(OracleSolver* s, const int* ea, const int* eb, float target, float onset) {
+    if (ea[0] == eb[0] || ea[0] == eb[1] || ea[1] == eb[0] || ea[1] == eb[1]) return 1;
+    V3 a0 = s->rest[ea[0]], a1 = s->rest[ea[1]], b0 = s->rest[eb[0]], b1 = s->rest[eb[1]];
+    float sp, tp;
+    seg_params(a0, a1, b0, b1, &sp, &tp);
+    V3 d = vsub(vadd(a0, vmul(vsub(a1, a0), sp)), vadd(b0, vmul(vsub(b1, b0), tp)));
+    float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    return vdot(d, d) < skip * skip;
+}
+/* abi41.cu:5595-5722 */
+static int ee_pair(OracleSolver* s, int ia, int ib, float target, float onset, Clusters* cl) {
+    if (ib <= ia || ia < 0 || ib < 0 || ia >= s->E || ib >= s->E || target <= 0.0f || onset <= target) return 0;
+    const int *ea = s->edges + 2 * ia, *eb = s->edges + 2 * ib;
+    if (!edge_ok(s, ea) || !edge_ok(s, eb)) return 0;
+    if (rest_ee_neighbor(s, ea, eb, target, onset)) { filter_count(s, C_F_REJ_REST); return 0; }
+    V3 a0 = s->pos[ea[0]], a1 = s->pos[ea[1]], b0 = s->pos[eb[0]], b1 = s->pos[eb[1]];
+    float sp, tp;
+    seg_params(a0, a1, b0, b1, &sp, &tp);
+    V3 pa = vadd(a0, vmul(vsub(a1, a0), sp)), pb = vadd(b0, vmul(vsub(b1, b0), tp)), d = vsub(pa, pb);
+    float dsq = vdot(d, d), dist = sqrtf(fmaxf(dsq, K_EPS));
+    if (dist >= onset) return 0;
+    V3 nrm = v3(0, 0, 1);
+    if (dsq > K_EPS) nrm = vmul(d, 1.0f / dist);
+    else {
+        nrm = vcross(vsub(a1, a0), vsub(b1, b0));
+        float nl = vdot(nrm, nrm);
+        if (nl > K_EPS) nrm = vmul(nrm, 1.0f / sqrtf(nl));
+        else {
+            V3 r0 = s->rest[ea[0]], r1 = s->rest[ea[1]], r2 = s->rest[eb[0]], r3 = s->rest[eb[1]];
+            float rs, rt;
+            seg_params(r0, r1, r2, r3, &rs, &rt);
+            V3 rd = vsub(vadd(r0, vmul(vsub(r1, r0), rs)), vadd(r2, vmul(vsub(r3, r2), rt)));
+            float rl = vdot(rd, rd);
+            if (rl > K_EPS) nrm = vmul(rd, 1.0f / sqrtf(rl));
+        }
+        dist = 0.0f;
+    }
+    if (fast_mode(s)) {
+        unsigned key = cluster_key(2, vmul(vadd(pa, pb), 0.5f), v3(0, 0, 0), fmaxf(onset * 12.0f, 1.0e-3f));
+        if (!local_accept(s, 2, key, cl)) return 1;
+    }
+    cnt(s, C_SELF_CAND);
+    float pen = target - dist, push;
+    if (pen > 0.0f) push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    else { float x = 1.0f - fminf(dist / onset, 1.0f); push = fminf(x * x * target * 0.06f, target * 0.04f); }
+    float ma0 = s->inv[ea[0]], ma1 = s->inv[ea[1]], mb0 = s->inv[eb[0]], mb1 = s->inv[eb[1]];
+    float ws0 = 1.0f - sp, ws1 = sp, wt0 = 1.0f - tp, wt1 = tp;
+    float wa0 = ma0 * ws0, wa1 = ma1 * ws1, wb0 = mb0 * wt0, wb1 = mb1 * wt1;
+    float total = ma0 * ws0 * ws0 + ma1 * ws1 * ws1 + mb0 * wt0 * wt0 + mb1 * wt1 * wt1;
+    if (push <= 0.0f || total <= 0.0f) return 1;
+    V3 delta = vmul(nrm, push / total);
+    if (wa0 > 0.0f) accumulate(s, ea[0], vmul(delta, wa0));
+    if (wa1 > 0.0f) accumulate(s, ea[1], vmul(delta, wa1));
+    if (wb0 > 0.0f) accumulate(s, eb[0], vmul(delta, -wb0));
+    if (wb1 > 0.0f) accumulate(s, eb[1], vmul(delta, -wb1));
+    cnt(s, C_EE);
+    return 1;
+}
+/* abi41.cu:5724-5844 */
+static void ee_all(OracleSolver* s) {
+    const float target = s->radius, onset = fmaxf(target * 1.8f, target + K_EPS);
+    if (target <= 0.0f) return;
+    const int bud = budget(s);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int e = 0; e < s->E; ++e) {
+        int acc = 0;
+        Clusters cl; cl.n = 0;
+        if (s->ehash) {
+            const int* ed = s->edges + 2 * e;
+            if (!edge_ok(s, ed)) continue;
+            V3 mid = vmul(vadd(s->pos[ed[0]], s->pos[ed[1]]), 0.5f);
+            int b = (int)bucket_of(cell_of(mid.x, s->cell), cell_of(mid.y, s->cell), cell_of(mid.z, s->cell), s->neb);
+            int st = s->eb_start[b], lim = s->eb_start[b + 1] - st;
+            if (lim > BUCKET_SLOTS) lim = BUCKET_SLOTS;
+            if (!fast_mode(s)) {
+                for (int k = 0; k < lim && acc < bud; ++k) if (ee_pair(s, e, s->eb_ent[st + k], target, onset, NULL)) ++acc;
+            } else {
+                Seen seen; seen.n = 0;
+                for (int k = 0; k < lim && acc < bud; ++k) {
+                    int o = s->eb_ent[st + k];
+                    if (!note_seen(s, o, &seen)) continue;
+                    if (ee_pair(s, e, o, target, onset, &cl)) ++acc;
+                }
+            }
+        } else {
+            for (int o = e + 1; o < s->E && acc < bud; ++o) {
+                if (!note_seen(s, o, NULL)) continue;
+                if (ee_pair(s, e, o, target, onset, &cl)) ++acc;
+            }
+        }
+    }
+}
+
+/* abi41.cu:5226-5439 */
+static void island_all(OracleSolver* s) {
+    const float target = s->radius, onset = fmaxf(target * 1.8f, target + K_EPS);
+    if (target <= 0.0f) return;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int vtx = 0; vtx < s->V; ++vtx) {
+        if (!(s->inv[vtx] > 0.0f)) continue;
+        V3 p = s->pos[vtx], pp = s->prev[vtx];
+        if (!vfinite(p) || !vfinite(pp)) { cnt(s, C_ISL_GUARD); continue; }
+        int maxn = s->cfg.max_self_collision_neighbors < 1 ? 1 : s->cfg.max_self_collision_neighbors;
+        int maxc = maxn * 2;
+        if (maxc > 48) maxc = 48;
+        if (maxc < 3) maxc = 3;
+        int scan_limit = maxc * 10, tris_acc[48];
+        int cx = cell_of(p.x, s->cell), cy = cell_of(p.y, s->cell), cz = cell_of(p.z, s->cell);
+        int scanned = 0, contacts = 0;
+        float pen_sum = 0, wsum = 0, max_pen = 0;
+        V3 axis = v3(0, 0, 0), best = v3(0, 0, 1);
+        for (int dz = -1; dz <= 1 && contacts < maxc && scanned < scan_limit; ++dz)
+            for (int dy = -1; dy <= 1 && contacts < maxc && scanned < scan_limit; ++dy)
+                for (int dx = -1; dx <= 1 && contacts < maxc && scanned < scan_limit; ++dx) {
+                    int b = (int)bucket_of(cx + dx, cy + dy, cz + dz, s->ntb), st = s->tb_start[b];
+                    int lim = s->tb_start[b + 1] - st; if (lim > BUCKET_SLOTS) lim = BUCKET_SLOTS;
+                    for (int k = 0; k < lim && contacts < maxc && scanned < scan_limit; ++k) {
+                        ++scanned;
+                        int tri = s->tb_ent[st + k], dup = 0;
+                        for (int q = 0; q < contacts; ++q) if (tris_acc[q] == tri) { dup = 1; break; }
+                        if (dup) continue;
+                        if (tri < 0 || tri >= s->T) { cnt(s, C_ISL_GUARD); continue; }
+                        const int* t = s->tris + 3 * tri;
+                        if (!tri_ok(s, t) || rest_vt_neighbor(s, vtx, t, target, onset)) continue;
+                        V3 a = s->pos[t[0]], b2 = s->pos[t[1]], c = s->pos[t[2]];
+                        V3 ap = s->prev[t[0]], bp = s->prev[t[1]], cp = s->prev[t[2]];
+                        if (!vfinite(a) || !vfinite(b2) || !vfinite(c) || !vfinite(ap) || !vfinite(bp) || !vfinite(cp)) { cnt(s, C_ISL_GUARD); continue; }
+                        V3 q = closest_on_tri(p, a, b2, c), delta = vsub(p, q);
+                        float dsq = vdot(delta, delta), dist = sqrtf(fmaxf(dsq, K_EPS));
+                        if (dist >= target) continue;
+                        V3 nrm = v3(0, 0, 1);
+                        if (dsq > K_EPS) nrm = vmul(delta, 1.0f / dist);
+                        else {
+                            nrm = vcross(vsub(b2, a), vsub(c, a));
+                            float nl = vdot(nrm, nrm);
+                            if (nl > K_EPS) nrm = vmul(nrm, 1.0f / sqrtf(nl));
+                            else {
+                                V3 rv = s->rest[vtx];
+                                V3 rd = vsub(rv, closest_on_tri(rv, s->rest[t[0]], s->rest[t[1]], s->rest[t[2]]));
+                                float rl = vdot(rd, rd);
+                                if (rl > K_EPS) nrm = vmul(rd, 1.0f / sqrtf(rl));
+                            }
+                            delta = vmul(nrm, dist);
+                            dist = 0.0f;
+                        }
+                        if (!vfinite(nrm)) { cnt(s, C_ISL_GUARD); continue; }
+                        V3 pd = vsub(pp, closest_on_tri(pp, ap, bp, cp));
+                        if (vdot(pd, nrm) > target * 0.25f && vdot(delta, nrm) > -target * 0.10f) continue;
+                        float wa, wb, wc;
+                        barycentric(q, a, b2, c, &wa, &wb, &wc);
+                        float pen = target - dist;
+                        if (pen <= 0.0f) continue;
+                        tris_acc[contacts++] = tri;
+                        pen_sum += pen;
+                        wsum += s->inv[t[0]] * wa + s->inv[t[1]] * wb + s->inv[t[2]] * wc;
+                        axis = vadd(axis, vmul(nrm, pen));
+                        if (pen > max_pen) { max_pen = pen; best = nrm; }
+                    }
+                }
+        if (contacts <= 0) continue;
+        cnt_add(s, C_ISL_CAND, (unsigned long long)contacts);
+        if (contacts < 3) { cnt(s, C_ISL_GUARD); continue; }
+        float avg_pen = pen_sum / (float)contacts;
+        if (avg_pen < target * 0.04f) { cnt(s, C_ISL_GUARD); continue; }
+        float al = vlen(axis);
+        V3 agg = al > K_EPS ? vmul(axis, 1.0f / al) : best;
+        float sw = s->inv[vtx], sample = wsum / (float)contacts, share = sw / fmaxf(sw + sample, K_EPS);
+        float md = fmaxf(target * 0.30f, 1.0e-5f), dl = fminf(avg_pen * 0.50f * share, md);
+        if (!vfinite(agg) || !isfinite(dl) || dl <= K_EPS) { cnt(s, C_ISL_GUARD); continue; }
+        accumulate(s, vtx, vmul(agg, dl));
+        cnt(s, C_ISL_CLUST);
+        cnt_add(s, C_ISL_REFS, (unsigned long long)contacts);
+        cnt(s, C_ISL_APPLIED);
+        unsigned long long micro = (unsigned long long)(fminf(dl, 1024.0f) * 1000000.0f);
+#pragma omp critical
+        if (micro > s->counts[C_ISL_MAXD]) s->counts[C_ISL_MAXD] = micro;
+    }
+}
+
+/* abi41.cu:4953-4988 */
+static void self_apply_all(OracleSolver* s) {
+    const float md = fmaxf(s->radius * 0.35f, 1.0e-4f);
+    for (int i = 0; i < s->V; ++i) {
+        long long* a = s->acc + 4 * (size_t)i;
+        long long ax = a[0], ay = a[1], az = a[2], aw = a[3];
+        a[0] = a[1] = a[2] = a[3] = 0;
+        if (!(s->inv[i] > 0.0f) || aw <= 0) continue;
+        V3 avg = vmul(v3(from_fix(ax), from_fix(ay), from_fix(az)), 1.0f / (float)aw);
+        float dl = vlen(avg);
+        if (dl > md) avg = vmul(avg, md / dl);
+        s->pos[i] = vadd(s->pos[i], avg);
+        s->prev[i] = vadd(s->prev[i], vmul(avg, 0.55f));
+        float al = vlen(avg);
+        if (al > s->max_delta) s->max_delta = al;
+    }
+}
+
+static void build_hashes(OracleSolver* s) {
+    if (s->vhash) hash_vertices(s);
+    if (s->thash) hash_prims(s, 1);
+    if (s->ehash) hash_prims(s, 0);
+}
+
+/* Self-collision block of one substep (abi41.cu:9255-9339). */
+static void self_collision(OracleSolver* s) {
+    int passes = s->cfg.fast_self_collision_passes;
+    if (passes > 8) passes = 8;
+    if (passes < 1) passes = 1;
+    int fast = fast_mode(s);
+    build_hashes(s);
+    if (fast) neighbors_all(s);
+    for (int pass = 0; pass < passes; ++pass) {
+        if (!fast) neighbors_all(s);
+        vv_all(s);
+        if (s->T > 0) vt_all(s);
+        if (s->E > 0) ee_all(s);
+        if (pass == passes - 1 && fast && s->T > 0 && s->thash) island_all(s);
+        self_apply_all(s);
+    }
+}
+
+/* ----------------------------------------------------------- lifecycle -- */
+void oracle_destroy(OracleSolver* s) {
+    if (!s) return;
+    void* p[] = {s->pos, s->snap, s->prev, s->vel, s->rest, s->w, s->inv, s->sp_off, s->sp_other, s->sp_side, s->sp_rest,
+                 s->te_off, s->te_other, s->te_side, s->te_rest, s->bj_off, s->bj_other, s->bj_side, s->bj_rest, s->bends,
+                 s->bend_rest, s->bend_colors, s->tris, s->edges, s->pin_w, s->pin_t, s->pin_relax, s->sdf, s->stris,
+                 s->vcell, s->vb_start, s->vb_ent, s->tb_start, s->tb_ent, s->eb_start, s->eb_ent, s->nb_count, s->nb_idx, s->acc};
+    for (size_t k = 0; k < sizeof(p) / sizeof(p[0]); ++k) free(p[k]);
+    free(s);
+}
+
+/* Creation and sanitising as abi41.cu:8791-8967 (without PCG / pressure). */
+OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* mesh) {
+    if (!config || config->vertex_count < 0 || config->edge_count < 0 || config->triangle_count < 0 || !isfinite(config->dt) ||
+        !(config->dt > 0.0f) || !mesh || !mesh->positions || !mesh->inv_mass) {
+        set_err("invalid ABI41 solver create request");
+        return NULL;
+    }
+    OracleSolver* s = (OracleSolver*)calloc(1, sizeof(OracleSolver));
+    SsblXpbdConfig* c = &s->cfg;
+    *c = *config;
+    if (c->vertex_count < 0) c->vertex_count = 0;
+    if (c->bend_count < 0) c->bend_count = 0;
+    if (c->lra_count < 0) c->lra_count = 0;
+    c->damping = isfinite(c->damping) ? fmaxf(0.0f, fminf(c->damping, 1.0f)) : 1.0f;
+    if (!isfinite(c->bend_compliance) || c->bend_compliance < 0.0f) c->bend_compliance = 0.0f;
+    if (!isfinite(c->lra_compliance) || c->lra_compliance < 0.0f) c->lra_compliance = 0.0f;
+    if (!isfinite(c->stretch_optimization_strength)) c->stretch_optimization_strength = 0.0f;
+    c->stretch_optimization_strength = clamp01(c->stretch_optimization_strength);
+    c->stretch_optimization_enabled = (c->edge_count > 0 && c->stretch_optimization_enabled && c->stretch_optimization_strength > 0.0f);
+    if (c->stretch_optimization_enabled) { set_err("oracle: stretch optimization not restated"); oracle_destroy(s); return NULL; }
+    const int V = c->vertex_count, E = c->edge_count, B = c->bend_count, L = c->lra_count, T = c->triangle_count;
+    s->V = V; s->E = E; s->B = B; s->L = L; s->T = T;
+    if (B > 0 && (!mesh->bends || !mesh->bend_rest_lengths)) { set_err("ABI41 bend constraints require bend pairs and rest lengths"); oracle_destroy(s); return NULL; }
+    if (L > 0 && (!mesh->lra_edges || !mesh->lra_rest_lengths)) { set_err("ABI41 LRA constraints require edge pairs and rest lengths"); oracle_destroy(s); return NULL; }
+    s->col.use_ground = c->use_ground; s->col.ground_height = c->ground_height; s->col.use_wall = c->use_wall;
+    memcpy(s->col.wall_origin, c->wall_origin, sizeof(c->wall_origin));
+    memcpy(s->col.wall_normal, c->wall_normal, sizeof(c->wall_normal));
+    s->col.use_sphere = c->use_sphere;
+    memcpy(s->col.sphere_center, c->sphere_center, sizeof(c->sphere_center));
+    s->col.sphere_radius = c->sphere_radius;
+    size_t nv = (size_t)(V > 0 ? V : 1);
+    s->pos = (V3*)calloc(nv, sizeof(V3)); s->snap = (V3*)calloc(nv, sizeof(V3)); s->prev = (V3*)calloc(nv, sizeof(V3));
+    s->vel = (V3*)calloc(nv, sizeof(V3)); s->rest = (V3*)calloc(nv, sizeof(V3));
+    s->w = (float*)calloc(nv, sizeof(float)); s->inv = (float*)calloc(nv, sizeof(float));
+    s->pin_w = (float*)malloc(nv * sizeof(float)); s->pin_t = (V3*)calloc(nv, sizeof(V3)); s->pin_relax = (float*)calloc(nv, sizeof(float));
+    s->pin_relax_iter = -1;
+    for (int i = 0; i < V; ++i) {
+        s->rest[i] = v3(mesh->positions[3 * i], mesh->positions[3 * i + 1], mesh->positions[3 * i + 2]);
+        s->pos[i] = s->prev[i] = s->rest[i];
+        s->inv[i] = mesh->inv_mass[i];
+        s->w[i] = s->inv[i] > 0.0f ? s->inv[i] : 0.0f;
+        s->pin_w[i] = -1.0f;
+    }
+    int* sp = (int*)xcalloc((size_t)E * 2, sizeof(int));
+    float* spr = (float*)xcalloc((size_t)E, sizeof(float));
+    s->edges = (int*)xcalloc((size_t)E * 2, sizeof(int));
+    for (int e = 0; e < E; ++e) {
+        int i = mesh->edges ? mesh->edges[2 * e] : 0, j = mesh->edges ? mesh->edges[2 * e + 1] : 0;
+        sp[2 * e] = i > 0 ? i : 0; sp[2 * e + 1] = j > 0 ? j : 0;
+        spr[e] = mesh->edge_rest_lengths ? mesh->edge_rest_lengths[e] : 0.0f;
+        s->edges[2 * e] = sp[2 * e]; s->edges[2 * e + 1] = sp[2 * e + 1];
+    }
+    build_csr(V, sp, spr, E, &s->sp_off, &s->sp_other, &s->sp_side, &s->sp_rest);
+    free(sp); free(spr);
+    build_csr(V, L > 0 ? mesh->lra_edges : NULL, L > 0 ? mesh->lra_rest_lengths : NULL, L, &s->te_off, &s->te_other, &s->te_side, &s->te_rest);
+    s->bends = (int*)xcalloc((size_t)B * 2, sizeof(int));
+    s->bend_rest = (float*)xcalloc((size_t)B, sizeof(float));
+    if (B > 0) { memcpy(s->bends, mesh->bends, sizeof(int) * 2 * (size_t)B); memcpy(s->bend_rest, mesh->bend_rest_lengths, sizeof(float) * (size_t)B); }
+    if (c->bend_color_count > 0) {
+        if (!mesh->bend_color_offsets) { set_err("ABI41 bend color offsets are required"); oracle_destroy(s); return NULL; }
+        s->n_bend_colors = c->bend_color_count;
+        s->bend_colors = (int*)malloc(sizeof(int) * (size_t)(c->bend_color_count + 1));
+        memcpy(s->bend_colors, mesh->bend_color_offsets, sizeof(int) * (size_t)(c->bend_color_count + 1));
+    } else if (B > 0) {
+        build_csr(V, s->bends, s->bend_rest, B, &s->bj_off, &s->bj_other, &s->bj_side, &s->bj_rest);
+    }
+    s->tris = (int*)xcalloc((size_t)T * 3, sizeof(int));
+    for (int k = 0; k < T * 3; ++k) { int v = mesh->triangles ? mesh->triangles[k] : 0; s->tris[k] = v > 0 ? v : 0; }
+    /* self collision sizing (abi41.cu:4542-4548, 6784-6994) */
+    float req = fmaxf(c->self_collision_distance, 0.0f);
+    s->radius = req > 0.0f ? req : fmaxf(fmaxf(c->cloth_thickness, c->collision_margin), 0.0f);
+    s->self_on = c->self_collision != 0;
+    if (s->self_on && s->radius > 0.0f) {
+        s->cell = fmaxf(s->radius * 1.8f, 1.0e-3f);
+        s->vhash = V >= 128; s->thash = T >= 64; s->ehash = E >= 64;
+        s->nvb = s->vhash ? next_pow2(V * 4 > 1024 ? V * 4 : 1024) : 0;
+        s->ntb = s->thash ? next_pow2(T * 4 > 1024 ? T * 4 : 1024) : 0;
+        s->neb = s->ehash ? next_pow2(E * 4 > 1024 ? E * 4 : 1024) : 0;
+        s->nb_count = (int*)calloc(nv, sizeof(int));
+        s->nb_idx = (int*)calloc(nv * NB_SLOTS, sizeof(int));
+        s->acc = (long long*)calloc(nv * 4, sizeof(long long));
+        if (s->vhash) { s->vcell = (int*)calloc(nv * 4, sizeof(int)); s->vb_start = (int*)calloc((size_t)s->nvb + 1, sizeof(int)); s->vb_ent = (int*)calloc(nv, sizeof(int)); }
+        if (s->thash) { s->tb_start = (int*)calloc((size_t)s->ntb + 1, sizeof(int)); s->tb_ent = (int*)calloc((size_t)T * MAX_PRIM_CELLS, sizeof(int)); }
+        if (s->ehash) { s->eb_start = (int*)calloc((size_t)s->neb + 1, sizeof(int)); s->eb_ent = (int*)calloc((size_t)E * MAX_PRIM_CELLS, sizeof(int)); }
+    }
+    int nst = config->static_triangle_count > 0 ? config->static_triangle_count : 0;
+    if (!build_sdf(s, mesh->static_triangles, nst)) { oracle_destroy(s); return NULL; }
+    return s;
+}
+
+int oracle_update_pin_targets(OracleSolver* s, const int* idx, const float* pos, const float* wts, int count) {
+    if (!s) return set_err("invalid solver handle");
+    if (count < 0) return set_err("invalid pin count");
+    if (count > 0 && (!idx || !pos)) return set_err("pin arrays are required when pin count is nonzero");
+    for (int i = 0; i < s->V; ++i) s->pin_w[i] = -1.0f;
+    for (int k = 0; k < count; ++k) {
+        int i = idx[k];
+        if (i < 0 || i >= s->V) continue;
+        s->pin_w[i] = wts ? wts[k] : 1.0f;
+        s->pin_t[i] = v3(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2]);
+    }
+    s->pin_relax_iter = -1;
+    return 1;
+}
+
+int oracle_update_runtime_colliders(OracleSolver* s, const SsblXpbdRuntimeColliders* c) {
+    if (!s || !c) return set_err("invalid runtime collider update");
+    s->col = *c;
+    return 1;
+}
+
+int oracle_update_positions(OracleSolver* s, const float* p, int max_floats) {
+    if (!s || !p || max_floats < s->V * 3) return set_err("invalid position upload");
+    for (int i = 0; i < s->V; ++i) s->pos[i] = s->prev[i] = v3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+    return 1;
+}
+
+int oracle_update_static_triangles(OracleSolver* s, const float* tris, int count) {
+    if (!s) return set_err("invalid static triangle update");
+    if (count < 0) count = 0;
+    if (count > 0 && !tris) return set_err("static triangle data is required when triangle count is nonzero");
+    return build_sdf(s, tris, count);
+}
+
+/* abi41.cu:3466-3477 */
+static float soft_relax(float weight, float exponent) {
+    if (!isfinite(weight) || weight < 0.05f) return 0.0f;
+    float total = fminf(fmaxf(weight / 0.75f, 0.0f), 1.0f);
+    if (total >= 1.0f) return 1.0f;
+    float rem = fmaxf(1.0f - total, 0.0f);
+    float r = 1.0f - powf(rem, fmaxf(exponent, 1.0e-4f));
+    return isfinite(r) ? fminf(fmaxf(r, 0.0f), 1.0f) : total;
+}
+
+/* ssbl_step_solver_ex schedule (abi41.cu:9087-9398), stage by stage. */
+int oracle_step(OracleSolver* s, int substeps, int iterations) {
+    if (!s) return set_err("invalid solver handle");
+    if (substeps < 1) substeps = 1;
+    if (iterations < 1) iterations = 1;
+    memset(s->counts, 0, sizeof(s->counts));
+    s->max_delta = 0.0f;
+    if (s->pin_relax_iter != iterations) {
+        float ex = 1.0f / (float)(iterations + 1 > 1 ? iterations + 1 : 1);
+        for (int i = 0; i < s->V; ++i) s->pin_relax[i] = soft_relax(s->pin_w[i], ex);
+        s->pin_relax_iter = iterations;
+    }
+    const float dt = s->cfg.dt / (float)substeps;
+    const int analytic = s->col.use_ground || s->col.use_wall || s->col.use_sphere;
+    const int sdf = s->sdf_ready;
+    const int interval = s->cfg.self_collision_interval > 1 ? s->cfg.self_collision_interval : 1;
+    for (int st = 0; st < substeps; ++st) {
+        integrate_all(s, dt);
+        pin_all(s, dt);
+        for (int it = 0; it < iterations; ++it) {
+            int last = it == iterations - 1, final_c = st == substeps - 1 && last;
+            if (s->E > 0) spring_all(s, dt);
+            if (final_c && s->L > 0) tether_all(s, dt);
+            if (final_c && s->B > 0) { if (s->n_bend_colors > 0) bends_by_color(s, dt); else bends_jacobi(s, dt); }
+            pin_all(s, dt);
+            if (analytic) analytic_all(s, dt);
+            if (sdf) sdf_all(s, dt);
+            int self_run = s->self_on && s->cfg.self_collision && last && (((st + 1) % interval) == 0 || st == substeps - 1) &&
+                           s->V > 0 && s->radius > 0.0f;
+            if (self_run) self_collision(s);
+            if (analytic || sdf || last || self_run) pin_all(s, dt);
+        }
+        velocity_all(s, dt);
+    }
+    return 1;
+}
+
+int oracle_download_positions(OracleSolver* s, float* out, int max_floats) {
+    if (!s || !out || max_floats < s->V * 3) return set_err("invalid position download");
+    memcpy(out, s->pos, sizeof(V3) * (size_t)s->V);
+    return 1;
+}
+
+int oracle_download_state(OracleSolver* s, float* p, float* q, float* v) {
+    if (!s) return set_err("invalid solver handle");
+    if (p) memcpy(p, s->pos, sizeof(V3) * (size_t)s->V);
+    if (q) memcpy(q, s->prev, sizeof(V3) * (size_t)s->V);
+    if (v) memcpy(v, s->vel, sizeof(V3) * (size_t)s->V);
+    return 1;
+}
+
+int oracle_build_self_structures(OracleSolver* s) {
+    if (!s) return set_err("invalid solver handle");
+    if (!s->self_on || !s->nb_count) return set_err("self collision is not enabled for this solver");
+    memset(s->counts, 0, sizeof(s->counts));
+    build_hashes(s);
+    neighbors_all(s);
+    return 1;
+}
+
+long long oracle_read_buffer(OracleSolver* s, int which, void* out, long long max_bytes) {
+    if (!s || !out) { set_err("invalid buffer read"); return -1; }
+    const void* src = NULL;
+    long long bytes = 0;
+    switch (which) {
+        case 3: src = s->vcell; bytes = 16ll * s->V; break;
+        case 4: src = s->vb_start; bytes = 4ll * (s->nvb + 1); break;
+        case 5: src = s->vb_ent; bytes = 4ll * s->V; break;
+        case 6: src = s->tb_start; bytes = 4ll * (s->ntb + 1); break;
+        case 7: src = s->tb_ent; bytes = 4ll * s->tb_total; break;
+        case 8: src = s->eb_start; bytes = 4ll * (s->neb + 1); break;
+        case 9: src = s->eb_ent; bytes = 4ll * s->eb_total; break;
+        case 10: src = s->nb_count; bytes = 4ll * s->V; break;
+        case 11: src = s->nb_idx; bytes = 4ll * s->V * NB_SLOTS; break;
+        case 12: src = s->sdf; bytes = s->sdf_ready ? 4ll * s->dim[0] * s->dim[1] * s->dim[2] : 0; break;
+        case 13: src = s->counts; bytes = 8ll * N_COUNTS; break;
+        default: set_err("unknown buffer id"); return -1;
+    }
+    if (!src) { set_err("buffer is not allocated for this solver"); return -1; }
+    if (bytes > max_bytes) { set_err("output buffer too small"); return -1; }
+    memcpy(out, src, (size_t)bytes);
+    return bytes;
+}
+
+int oracle_hash_info(OracleSolver* s, int* o) {
+    if (!s || !o) return set_err("invalid hash info request");
+    o[0] = s->nvb; o[1] = s->ntb; o[2] = s->neb; o[3] = s->vhash; o[4] = s->thash; o[5] = s->ehash;
+    return 1;
+}

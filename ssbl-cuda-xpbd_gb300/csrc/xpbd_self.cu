@@ -1,0 +1,942 @@
+// Self collision: spatial hashes, the vertex-vertex neighbour table, and the
+// vertex-vertex / vertex-triangle / edge-edge repulsion passes
+// (reference native/src/ssbl_xpbd_cuda_abi41.cu:4542-5844, schedule at
+// 9255-9339).
+//
+// Hash layout.  The reference inserts primitives into fixed 32-slot buckets
+// with atomicAdd slot counters, so bucket contents depend on thread timing.
+// Here each hash is a counting sort over the bucket id: count entries per
+// bucket, exclusive-scan the counts into bucket starts, scatter the entries
+// with atomic cursors, then sort each bucket's ids so that its first
+// min(count, 32) members are the 32 smallest primitive ids in increasing
+// order.  Queries read exactly those members, which makes candidate order,
+// the 32-slot caps and the fast-mode cluster filter deterministic.  Bucket
+// ids, cell coordinates, pre-clamp counts and member multisets are the same
+// integers as the reference's when no bucket overflows.
+//
+// Accumulation.  Pushes are scattered into per-vertex fixed-point int64
+// accumulators (2^-32 m units) with integer atomics, so the per-vertex sums do
+// not depend on the order of the atomics.
+#include "xpbd_solver.cuh"
+
+namespace xg {
+
+namespace {
+
+inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
+
+__device__ __forceinline__ float contact_radius(const Params& P) { return P.self_radius; }
+
+__device__ __forceinline__ bool fast_mode(const Params& P) { return P.self_mode == 1; }
+
+__device__ __forceinline__ void accumulate(const View& v, int i, F3 d) {
+    const Params& P = *v.P;
+    if (i < 0 || i >= P.V || !(__ldg(&v.inv_mass[i]) > 0.0f)) return;
+    unsigned long long* a = reinterpret_cast<unsigned long long*>(&v.acc[i]);
+    atomicAdd(a + 0, (unsigned long long)to_fix(d.x));
+    atomicAdd(a + 1, (unsigned long long)to_fix(d.y));
+    atomicAdd(a + 2, (unsigned long long)to_fix(d.z));
+    atomicAdd(a + 3, 1ull);
+}
+
+// ---------------------------------------------------------------- filters --
+// Fast-mode per-thread filters (abi41.cu:714-832).
+__device__ int normal_bucket(float v) { return v > 0.45f ? 2 : (v < -0.45f ? 0 : 1); }
+
+__device__ unsigned cluster_key(int pair_type, F3 point, F3 normal, float cell) {
+    const float c = fmaxf(cell, 1.0e-3f);
+    unsigned key = bucket_of(cell_of(point.x, c), cell_of(point.y, c), cell_of(point.z, c), 1 << 20);
+    const unsigned nk = (unsigned)normal_bucket(normal.x) | ((unsigned)normal_bucket(normal.y) << 2) |
+                        ((unsigned)normal_bucket(normal.z) << 4);
+    key ^= nk * 2654435761u;
+    key ^= (unsigned)(pair_type + 1) * 2246822519u;
+    return key;
+}
+
+struct Clusters {
+    unsigned keys[16];
+    unsigned char counts[16];
+    int n;
+};
+
+__device__ int accept_slot(int pair_type) {
+    return pair_type == 0 ? kCntFilterAcceptedVv : (pair_type == 1 ? kCntFilterAcceptedVt : kCntFilterAcceptedEe);
+}
+
+__device__ bool try_local_accept(const View& v, int pair_type, unsigned key, Clusters* cl) {
+    if (!fast_mode(*v.P)) return true;
+    if (cl) {
+        const int n = cl->n < 16 ? cl->n : 16;
+        for (int i = 0; i < n; ++i) {
+            if (cl->keys[i] == key) {
+                if (cl->counts[i] >= 1) {
+                    count1(v.counts, kCntFilterRejectedOwnership);
+                    return false;
+                }
+                cl->counts[i] += 1;
+                count1(v.counts, kCntClusterOwnedContacts);
+                count1(v.counts, accept_slot(pair_type));
+                return true;
+            }
+        }
+        if (cl->n >= 16) {
+            count1(v.counts, kCntFilterRejectedOwnership);
+            return false;
+        }
+        cl->keys[cl->n] = key;
+        cl->counts[cl->n] = 1;
+        cl->n += 1;
+        count1(v.counts, kCntClusterCount);
+        count1(v.counts, kCntClusterOwnedContacts);
+    }
+    count1(v.counts, accept_slot(pair_type));
+    return true;
+}
+
+struct Seen {
+    int ids[64];
+    int n;
+};
+
+__device__ bool try_note_seen(const View& v, int key, Seen* seen) {
+    if (!fast_mode(*v.P)) return true;
+    count1(v.counts, kCntFilterSeen);
+    if (!seen) return true;
+    const int lim = seen->n < 64 ? seen->n : 64;
+    for (int i = 0; i < lim; ++i) {
+        if (seen->ids[i] == key) {
+            count1(v.counts, kCntFilterRejectedDuplicate);
+            return false;
+        }
+    }
+    if (seen->n >= 64) {
+        count1(v.counts, kCntSelfOverflow);
+        count1(v.counts, kCntFilterRejectedOwnership);
+        return false;
+    }
+    seen->ids[seen->n++] = key;
+    return true;
+}
+
+__device__ __forceinline__ void filter_count(const View& v, int slot) {
+    if (fast_mode(*v.P)) count1(v.counts, slot);
+}
+
+// ------------------------------------------------------------- hash build --
+// Cell range of a primitive's AABB grown by 1.8 r; ranges of more than 64
+// cells collapse to the cell of `fallback` (abi41.cu:871-900).
+struct CellRange {
+    int x0, x1, y0, y1, z0, z1;
+};
+
+__device__ CellRange primitive_cells(const View& v, F3 lo, F3 hi, F3 fallback, float cell, bool count_guard) {
+    CellRange r{cell_of(lo.x, cell), cell_of(hi.x, cell), cell_of(lo.y, cell),
+                cell_of(hi.y, cell), cell_of(lo.z, cell), cell_of(hi.z, cell)};
+    const long long sx = (long long)r.x1 - r.x0 + 1, sy = (long long)r.y1 - r.y0 + 1, sz = (long long)r.z1 - r.z0 + 1;
+    if (sx <= 0 || sy <= 0 || sz <= 0) return r;
+    if (sx * sy * sz <= (long long)kMaxPrimitiveCells) return r;
+    const int fx = cell_of(fallback.x, cell), fy = cell_of(fallback.y, cell), fz = cell_of(fallback.z, cell);
+    if (count_guard) count1(v.counts, kCntSelfOverflow);
+    return CellRange{fx, fx, fy, fy, fz, fz};
+}
+
+__device__ bool tri_valid(const Params& P, int4 t) {
+    return t.x >= 0 && t.y >= 0 && t.z >= 0 && t.x < P.V && t.y < P.V && t.z < P.V && t.x != t.y && t.y != t.z &&
+           t.x != t.z;
+}
+
+__device__ bool edge_valid(const Params& P, int2 e) { return e.x >= 0 && e.y >= 0 && e.x < P.V && e.y < P.V && e.x != e.y; }
+
+__device__ CellRange tri_cells(const View& v, int t, bool* ok, bool count_guard) {
+    const Params& P = *v.P;
+    const int4 tr = __ldg(&v.tris[t]);
+    *ok = tri_valid(P, tr);
+    if (!*ok) return CellRange{0, -1, 0, -1, 0, -1};
+    const F3 a = f3(v.pos[tr.x]), b = f3(v.pos[tr.y]), c = f3(v.pos[tr.z]);
+    const float m = contact_radius(P) * 1.8f;
+    const F3 lo{fminf(a.x, fminf(b.x, c.x)) - m, fminf(a.y, fminf(b.y, c.y)) - m, fminf(a.z, fminf(b.z, c.z)) - m};
+    const F3 hi{fmaxf(a.x, fmaxf(b.x, c.x)) + m, fmaxf(a.y, fmaxf(b.y, c.y)) + m, fmaxf(a.z, fmaxf(b.z, c.z)) + m};
+    const F3 centroid = ((a + b) + c) * (1.0f / 3.0f);
+    return primitive_cells(v, lo, hi, centroid, P.tcell, count_guard);
+}
+
+__device__ CellRange edge_cells(const View& v, int e, bool* ok, bool count_guard) {
+    const Params& P = *v.P;
+    const int2 ed = __ldg(&v.edges[e]);
+    *ok = edge_valid(P, ed);
+    if (!*ok) return CellRange{0, -1, 0, -1, 0, -1};
+    const F3 a = f3(v.pos[ed.x]), b = f3(v.pos[ed.y]);
+    const float m = contact_radius(P) * 1.8f;
+    const F3 lo{fminf(a.x, b.x) - m, fminf(a.y, b.y) - m, fminf(a.z, b.z) - m};
+    const F3 hi{fmaxf(a.x, b.x) + m, fmaxf(a.y, b.y) + m, fmaxf(a.z, b.z) + m};
+    const F3 mid = (a + b) * 0.5f;
+    return primitive_cells(v, lo, hi, mid, P.ecell, count_guard);
+}
+
+__global__ void k_vhash_count(View v) {
+    const Params& P = *v.P;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.V) return;
+    const float4 p = v.pos[i];
+    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
+    const int b = (int)bucket_of(cx, cy, cz, P.vbuckets);
+    v.vcell[i] = make_int4(cx, cy, cz, b);
+    const int slot = atomicAdd(&v.vb_count[b], 1);
+    if (slot >= kBucketSlots) count1(v.counts, kCntSelfOverflow);
+}
+
+__global__ void k_vhash_scatter(View v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.P->V) return;
+    const int b = v.vcell[i].w;
+    v.vb_ent[atomicAdd(&v.vb_count[b], 1)] = i;
+}
+
+// `scatter` = false: count entries per bucket; true: write them.
+template <bool kTri>
+__global__ void k_prim_hash(View v, bool scatter) {
+    const Params& P = *v.P;
+    const int n = kTri ? P.T : P.E;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    bool ok = false;
+    CellRange r = kTri ? tri_cells(v, k, &ok, !scatter) : edge_cells(v, k, &ok, !scatter);
+    if (!ok) return;
+    int* cnt = kTri ? v.tb_count : v.eb_count;
+    int* ent = kTri ? v.tb_ent : v.eb_ent;
+    const int nb = kTri ? P.tbuckets : P.ebuckets;
+    for (int z = r.z0; z <= r.z1; ++z)
+        for (int y = r.y0; y <= r.y1; ++y)
+            for (int x = r.x0; x <= r.x1; ++x) {
+                const int b = (int)bucket_of(x, y, z, nb);
+                const int slot = atomicAdd(&cnt[b], 1);
+                if (scatter)
+                    ent[slot] = k;
+                else if (slot >= kBucketSlots)
+                    count1(v.counts, kCntSelfOverflow);
+            }
+}
+
+// Exclusive scan of counts[0..n) into start[0..n]; counts is overwritten
+// with the starts so it can serve as the scatter cursor.  One block,
+// 4096-element tiles with a running carry.
+__global__ void __launch_bounds__(1024) k_scan(int* counts, int* start, int n) {
+    __shared__ int warp_sums[32];
+    __shared__ int carry_s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry_s = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 4096) {
+        int vals[4];
+        int local = 0;
+        for (int k = 0; k < 4; ++k) {
+            const int idx = base + tid * 4 + k;
+            vals[k] = idx < n ? counts[idx] : 0;
+            local += vals[k];
+        }
+        int incl = local;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_sums[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int w = warp_sums[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += t;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const int carry = carry_s;
+        int run = carry + (wid > 0 ? warp_sums[wid - 1] : 0) + incl - local;
+        for (int k = 0; k < 4; ++k) {
+            const int idx = base + tid * 4 + k;
+            if (idx < n) {
+                start[idx] = run;
+                counts[idx] = run;
+            }
+            run += vals[k];
+        }
+        __syncthreads();
+        if (tid == 1023) carry_s = run;
+        __syncthreads();
+    }
+    if (tid == 0) start[n] = carry_s;
+}
+
+// Order each bucket's members: full insertion sort up to 32 members, else a
+// selection of the 32 smallest ids to the front (queries read no further).
+__global__ void k_bucket_sort(const int* start, int* ent, int nbuckets) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbuckets) return;
+    const int s = start[b], n = start[b + 1] - s;
+    int* e = ent + s;
+    if (n <= 1) return;
+    if (n <= kBucketSlots) {
+        for (int i = 1; i < n; ++i) {
+            const int key = e[i];
+            int j = i - 1;
+            while (j >= 0 && e[j] > key) {
+                e[j + 1] = e[j];
+                --j;
+            }
+            e[j + 1] = key;
+        }
+        return;
+    }
+    for (int i = 0; i < kBucketSlots; ++i) {
+        int best = i;
+        for (int j = i + 1; j < n; ++j)
+            if (e[j] < e[best]) best = j;
+        const int t = e[i];
+        e[i] = e[best];
+        e[best] = t;
+    }
+}
+
+// ------------------------------------------------------- neighbour table --
+// Rest-distance exclusion plus onset test on the current or previous
+// positions (abi41.cu:4696-4717).
+__device__ bool vv_valid(const View& v, int src, int other, float target, float onset) {
+    const Params& P = *v.P;
+    if (src < 0 || other < 0 || src >= P.V || other >= P.V || src == other || target <= 0.0f || onset <= target ||
+        !(__ldg(&v.inv_mass[src]) > 0.0f))
+        return false;
+    const F3 rd = f3(ld4(&v.rest[src])) - f3(ld4(&v.rest[other]));
+    const float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    if (dot3(rd, rd) < skip * skip) return false;
+    const F3 cd = f3(v.pos[src]) - f3(v.pos[other]);
+    const F3 pd = f3(v.prev[src]) - f3(v.prev[other]);
+    return dot3(cd, cd) < onset * onset || dot3(pd, pd) < onset * onset;
+}
+
+__global__ void k_neighbors_hash(View v) {
+    const Params& P = *v.P;
+    const int src = blockIdx.x * blockDim.x + threadIdx.x;
+    if (src >= P.V) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) {
+        v.nb_count[src] = 0;
+        return;
+    }
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const float4 p = v.pos[src];
+    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
+    int accepted = 0;
+    for (int dz = -1; dz <= 1 && accepted < kNeighborSlots; ++dz)
+        for (int dy = -1; dy <= 1 && accepted < kNeighborSlots; ++dy)
+            for (int dx = -1; dx <= 1 && accepted < kNeighborSlots; ++dx) {
+                const int qx = cx + dx, qy = cy + dy, qz = cz + dz;
+                const int b = (int)bucket_of(qx, qy, qz, P.vbuckets);
+                const int s = v.vb_start[b];
+                const int lim = min(v.vb_start[b + 1] - s, kBucketSlots);
+                for (int k = 0; k < lim && accepted < kNeighborSlots; ++k) {
+                    const int other = v.vb_ent[s + k];
+                    const int4 oc = v.vcell[other];
+                    if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
+                    v.nb_idx[src * kNeighborSlots + accepted++] = other;
+                }
+            }
+    if (accepted >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
+    v.nb_count[src] = accepted;
+}
+
+__global__ void k_neighbors_brute(View v) {
+    const Params& P = *v.P;
+    const int src = blockIdx.x * blockDim.x + threadIdx.x;
+    if (src >= P.V) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) {
+        v.nb_count[src] = 0;
+        return;
+    }
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    int accepted = 0;
+    for (int other = 0; other < P.V && accepted < kNeighborSlots; ++other) {
+        if (!vv_valid(v, src, other, target, onset)) continue;
+        v.nb_idx[src * kNeighborSlots + accepted++] = other;
+    }
+    if (accepted >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
+    v.nb_count[src] = accepted;
+}
+
+// -------------------------------------------------------- VV repulsion --
+// Swept-sphere time of impact between the two vertices' prev->current paths,
+// else an overlap push; responses clamped to 0.35 thickness
+// (abi41.cu:4816-4951).
+__global__ void __launch_bounds__(kThreads) k_vv(View v) {
+    const Params& P = *v.P;
+    const int src = blockIdx.x * blockDim.x + threadIdx.x;
+    if (src >= P.V) return;
+    if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
+    const int count = v.nb_count[src];
+    if (count == 0) return;
+    const F3 pc = f3(v.pos[src]), pp = f3(v.prev[src]);
+    const float target = contact_radius(P);
+    const float r_self = target * 0.5f;
+    const int lim = min(count, kNeighborSlots);
+    Clusters cl;
+    cl.n = 0;
+    const bool fast = fast_mode(P);
+    long long ax = 0, ay = 0, az = 0, aw = 0;
+    for (int n = 0; n < lim; ++n) {
+        const int other = v.nb_idx[src * kNeighborSlots + n];
+        if (other < 0 || other >= P.V || other == src) continue;
+        if (fast)
+            count1(v.counts, kCntFilterSeen);
+        else
+            count1(v.counts, kCntSelfCandidates);
+        const F3 qc = f3(v.pos[other]), qp = f3(v.prev[other]);
+        const float th = r_self + target * 0.5f;
+        if (th <= 0.0f) continue;
+        const bool other_pinned = !(__ldg(&v.inv_mass[other]) > 0.0f);
+        const float scale = other_pinned ? 1.0f : 0.5f;
+        F3 resp{0.0f, 0.0f, 0.0f};
+        bool hit = false;
+        const F3 d_ref = pp - qp;
+        const float cc = dot3(d_ref, d_ref) - th * th;
+        const F3 rel = (pc - pp) - (qc - qp);
+        const float a = dot3(rel, rel);
+        const float b = dot3(d_ref, rel);
+        if (cc >= 0.0f && b < 0.0f && a > 1.0e-5f) {
+            const float disc = b * b - a * cc;
+            if (disc >= 0.0f) {
+                const float t = (-b - sqrtf(disc)) / a;
+                if (t > 0.0f && t <= 1.0f) {
+                    const float s = 1.0f - t;
+                    const F3 ph = pp * s + pc * t;
+                    const F3 qh = qp * s + qc * t;
+                    F3 nrm = ph - qh;
+                    const float nl = dot3(nrm, nrm);
+                    if (nl > kEps) {
+                        nrm = nrm * (1.0f / sqrtf(nl));
+                        const float vn = dot3((pc - ph) - (qc - qh), nrm);
+                        if (vn > 0.0f) {
+                            resp = nrm * (-vn * scale);
+                            hit = true;
+                        }
+                    }
+                }
+            }
+        }
+        if (!hit) {
+            const F3 delta = pc - qc;
+            const float dsq = dot3(delta, delta);
+            if (dsq >= th * th) continue;
+            F3 nrm{0.0f, 0.0f, 1.0f};
+            float dist = sqrtf(fmaxf(dsq, kEps));
+            if (dsq > kEps) {
+                nrm = delta * (1.0f / dist);
+            } else {
+                const F3 rd = f3(ld4(&v.rest[src])) - f3(ld4(&v.rest[other]));
+                const float rl = dot3(rd, rd);
+                if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+                dist = 0.0f;
+            }
+            resp = nrm * fminf((th - dist) * scale, th * 0.35f);
+            hit = true;
+        }
+        if (hit && dot3(resp, resp) > kEps) {
+            const float max_len = fmaxf(th * 0.35f, 1.0e-4f);
+            const float rl = len3(resp);
+            if (rl > max_len) resp = resp * (max_len / rl);
+            if (fast) {
+                const F3 nrm = resp * (1.0f / fmaxf(len3(resp), kEps));
+                const F3 mid = (pc + qc) * 0.5f;
+                const unsigned key = cluster_key(0, mid, nrm, fmaxf(th * 2.5f, 1.0e-3f));
+                if (!try_local_accept(v, 0, key, &cl)) continue;
+                count1(v.counts, kCntSelfCandidates);
+            }
+            ax += to_fix(resp.x);
+            ay += to_fix(resp.y);
+            az += to_fix(resp.z);
+            aw += 1;
+            count1(v.counts, kCntExactImpulseContacts);
+        }
+    }
+    if (aw) {
+        unsigned long long* acc = reinterpret_cast<unsigned long long*>(&v.acc[src]);
+        atomicAdd(acc + 0, (unsigned long long)ax);
+        atomicAdd(acc + 1, (unsigned long long)ay);
+        atomicAdd(acc + 2, (unsigned long long)az);
+        atomicAdd(acc + 3, (unsigned long long)aw);
+    }
+}
+
+// --------------------------------------------------------- VT repulsion --
+__device__ bool rest_vt_neighbor(const View& v, int vertex, int4 t, float target, float onset) {
+    if (vertex == t.x || vertex == t.y || vertex == t.z) return true;
+    const F3 rp = f3(ld4(&v.rest[vertex]));
+    const F3 rq = closest_on_triangle(rp, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])), f3(ld4(&v.rest[t.z])));
+    const F3 rd = rp - rq;
+    const float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    return dot3(rd, rd) < skip * skip;
+}
+
+// Soft vertex-triangle push with barycentric split (abi41.cu:4990-5107).
+// Returns whether the pair counts toward the vertex's neighbour budget.
+__device__ bool vt_pair(const View& v, int vertex, int tri, float target, float onset, Clusters* cl) {
+    const Params& P = *v.P;
+    if (tri < 0 || tri >= P.T || target <= 0.0f || onset <= target) return false;
+    const int4 t = __ldg(&v.tris[tri]);
+    if (!tri_valid(P, t)) return false;
+    if (rest_vt_neighbor(v, vertex, t, target, onset)) {
+        filter_count(v, kCntFilterRejectedRest);
+        return false;
+    }
+    const F3 p = f3(v.pos[vertex]), a = f3(v.pos[t.x]), b = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
+    const F3 q = closest_on_triangle(p, a, b, c);
+    F3 d = p - q;
+    const float dsq = dot3(d, d);
+    float dist = sqrtf(fmaxf(dsq, kEps));
+    if (dist >= onset) return false;
+    F3 nrm{0.0f, 0.0f, 1.0f};
+    if (dsq > kEps) {
+        nrm = d * (1.0f / dist);
+    } else {
+        nrm = cross3(b - a, c - a);
+        const float nl = dot3(nrm, nrm);
+        if (nl > kEps) {
+            nrm = nrm * (1.0f / sqrtf(nl));
+        } else {
+            const F3 rv = f3(ld4(&v.rest[vertex]));
+            const F3 rd = rv - closest_on_triangle(rv, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])), f3(ld4(&v.rest[t.z])));
+            const float rl = dot3(rd, rd);
+            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+        }
+        d = nrm * dist;
+        dist = 0.0f;
+    }
+    if (fast_mode(P)) {
+        const unsigned key = cluster_key(1, q, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+        if (!try_local_accept(v, 1, key, cl)) return true;
+    }
+    count1(v.counts, kCntSelfCandidates);
+    float wa, wb, wc;
+    barycentric(q, a, b, c, &wa, &wb, &wc);
+    const float pen = target - dist;
+    float push;
+    if (pen > 0.0f) {
+        push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    } else {
+        const float x = 1.0f - fminf(dist / onset, 1.0f);
+        push = fminf(x * x * target * 0.06f, target * 0.04f);
+    }
+    const float wv = __ldg(&v.inv_mass[vertex]);
+    const float wta = __ldg(&v.inv_mass[t.x]) * wa;
+    const float wtb = __ldg(&v.inv_mass[t.y]) * wb;
+    const float wtc = __ldg(&v.inv_mass[t.z]) * wc;
+    const float total = wv + wta + wtb + wtc;
+    if (push <= 0.0f || total <= 0.0f) return true;
+    const F3 delta = nrm * (push / total);
+    if (wv > 0.0f) accumulate(v, vertex, delta * wv);
+    if (wta > 0.0f) accumulate(v, t.x, delta * (-wta));
+    if (wtb > 0.0f) accumulate(v, t.y, delta * (-wtb));
+    if (wtc > 0.0f) accumulate(v, t.z, delta * (-wtc));
+    count1(v.counts, kCntSoftContacts);
+    return true;
+}
+
+__device__ int neighbor_budget(const Params& P) {
+    int m = P.max_neighbors;
+    if (m < 1) m = 1;
+    if (m > kBucketSlots) m = kBucketSlots;
+    if (fast_mode(P) && m > 16) m = 16;
+    return m;
+}
+
+// Vertex-triangle query over the vertex's own cell bucket only
+// (abi41.cu:5109-5182).
+__global__ void __launch_bounds__(kThreads) k_vt_hash(View v) {
+    const Params& P = *v.P;
+    const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vertex >= P.V) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const int budget = neighbor_budget(P);
+    const float4 p = v.pos[vertex];
+    const int b = (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
+    const int s = v.tb_start[b];
+    const int lim = min(v.tb_start[b + 1] - s, kBucketSlots);
+    int accepted = 0;
+    if (!fast_mode(P)) {
+        for (int k = 0; k < lim && accepted < budget; ++k)
+            if (vt_pair(v, vertex, v.tb_ent[s + k], target, onset, nullptr)) ++accepted;
+        return;
+    }
+    Seen seen;
+    seen.n = 0;
+    Clusters cl;
+    cl.n = 0;
+    for (int k = 0; k < lim && accepted < budget; ++k) {
+        const int tri = v.tb_ent[s + k];
+        if (!try_note_seen(v, tri, &seen)) continue;
+        if (vt_pair(v, vertex, tri, target, onset, &cl)) ++accepted;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_vt_brute(View v) {
+    const Params& P = *v.P;
+    const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vertex >= P.V) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const int budget = neighbor_budget(P);
+    Clusters cl;
+    cl.n = 0;
+    int accepted = 0;
+    for (int tri = 0; tri < P.T && accepted < budget; ++tri) {
+        if (!try_note_seen(v, tri, nullptr)) continue;
+        if (vt_pair(v, vertex, tri, target, onset, &cl)) ++accepted;
+    }
+}
+
+// --------------------------------------------------------- EE repulsion --
+__device__ bool rest_ee_neighbor(const View& v, int2 ea, int2 eb, float target, float onset) {
+    if (ea.x == eb.x || ea.x == eb.y || ea.y == eb.x || ea.y == eb.y) return true;
+    const F3 a0 = f3(ld4(&v.rest[ea.x])), a1 = f3(ld4(&v.rest[ea.y]));
+    const F3 b0 = f3(ld4(&v.rest[eb.x])), b1 = f3(ld4(&v.rest[eb.y]));
+    float s, t;
+    segment_params(a0, a1, b0, b1, &s, &t);
+    const F3 d = (a0 + (a1 - a0) * s) - (b0 + (b1 - b0) * t);
+    const float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    return dot3(d, d) < skip * skip;
+}
+
+// Soft edge-edge push split by the closest-point parameters
+// (abi41.cu:5595-5722).
+__device__ bool ee_pair(const View& v, int ia, int ib, float target, float onset, Clusters* cl) {
+    const Params& P = *v.P;
+    if (ib <= ia || ia < 0 || ib < 0 || ia >= P.E || ib >= P.E || target <= 0.0f || onset <= target) return false;
+    const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
+    if (!edge_valid(P, ea) || !edge_valid(P, eb)) return false;
+    if (rest_ee_neighbor(v, ea, eb, target, onset)) {
+        filter_count(v, kCntFilterRejectedRest);
+        return false;
+    }
+    const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
+    float s, t;
+    segment_params(a0, a1, b0, b1, &s, &t);
+    const F3 pa = a0 + (a1 - a0) * s;
+    const F3 pb = b0 + (b1 - b0) * t;
+    const F3 d = pa - pb;
+    const float dsq = dot3(d, d);
+    float dist = sqrtf(fmaxf(dsq, kEps));
+    if (dist >= onset) return false;
+    F3 nrm{0.0f, 0.0f, 1.0f};
+    if (dsq > kEps) {
+        nrm = d * (1.0f / dist);
+    } else {
+        nrm = cross3(a1 - a0, b1 - b0);
+        const float nl = dot3(nrm, nrm);
+        if (nl > kEps) {
+            nrm = nrm * (1.0f / sqrtf(nl));
+        } else {
+            const F3 r0 = f3(ld4(&v.rest[ea.x])), r1 = f3(ld4(&v.rest[ea.y]));
+            const F3 r2 = f3(ld4(&v.rest[eb.x])), r3 = f3(ld4(&v.rest[eb.y]));
+            float rs, rt;
+            segment_params(r0, r1, r2, r3, &rs, &rt);
+            const F3 rd = (r0 + (r1 - r0) * rs) - (r2 + (r3 - r2) * rt);
+            const float rl = dot3(rd, rd);
+            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+        }
+        dist = 0.0f;
+    }
+    if (fast_mode(P)) {
+        const unsigned key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+        if (!try_local_accept(v, 2, key, cl)) return true;
+    }
+    count1(v.counts, kCntSelfCandidates);
+    const float pen = target - dist;
+    float push;
+    if (pen > 0.0f) {
+        push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    } else {
+        const float x = 1.0f - fminf(dist / onset, 1.0f);
+        push = fminf(x * x * target * 0.06f, target * 0.04f);
+    }
+    const float ma0 = __ldg(&v.inv_mass[ea.x]), ma1 = __ldg(&v.inv_mass[ea.y]);
+    const float mb0 = __ldg(&v.inv_mass[eb.x]), mb1 = __ldg(&v.inv_mass[eb.y]);
+    const float ws0 = 1.0f - s, ws1 = s, wt0 = 1.0f - t, wt1 = t;
+    const float wa0 = ma0 * ws0, wa1 = ma1 * ws1, wb0 = mb0 * wt0, wb1 = mb1 * wt1;
+    const float total = ma0 * ws0 * ws0 + ma1 * ws1 * ws1 + mb0 * wt0 * wt0 + mb1 * wt1 * wt1;
+    if (push <= 0.0f || total <= 0.0f) return true;
+    const F3 delta = nrm * (push / total);
+    if (wa0 > 0.0f) accumulate(v, ea.x, delta * wa0);
+    if (wa1 > 0.0f) accumulate(v, ea.y, delta * wa1);
+    if (wb0 > 0.0f) accumulate(v, eb.x, delta * (-wb0));
+    if (wb1 > 0.0f) accumulate(v, eb.y, delta * (-wb1));
+    count1(v.counts, kCntEdgeEdgeContacts);
+    return true;
+}
+
+// Edge-edge query over the bucket of the edge midpoint's cell
+// (abi41.cu:5724-5802).
+__global__ void __launch_bounds__(kThreads) k_ee_hash(View v) {
+    const Params& P = *v.P;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= P.E) return;
+    const int2 ed = __ldg(&v.edges[e]);
+    if (!edge_valid(P, ed)) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const int budget = neighbor_budget(P);
+    const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
+    const int b = (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
+    const int s = v.eb_start[b];
+    const int lim = min(v.eb_start[b + 1] - s, kBucketSlots);
+    int accepted = 0;
+    if (!fast_mode(P)) {
+        for (int k = 0; k < lim && accepted < budget; ++k)
+            if (ee_pair(v, e, v.eb_ent[s + k], target, onset, nullptr)) ++accepted;
+        return;
+    }
+    Seen seen;
+    seen.n = 0;
+    Clusters cl;
+    cl.n = 0;
+    for (int k = 0; k < lim && accepted < budget; ++k) {
+        const int other = v.eb_ent[s + k];
+        if (!try_note_seen(v, other, &seen)) continue;
+        if (ee_pair(v, e, other, target, onset, &cl)) ++accepted;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
+    const Params& P = *v.P;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= P.E) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const int budget = neighbor_budget(P);
+    Clusters cl;
+    cl.n = 0;
+    int accepted = 0;
+    for (int other = e + 1; other < P.E && accepted < budget; ++other) {
+        if (!try_note_seen(v, other, nullptr)) continue;
+        if (ee_pair(v, e, other, target, onset, &cl)) ++accepted;
+    }
+}
+
+// ------------------------------------------------- fast overlap islands --
+// Fast mode, final pass: aggregate push for a vertex buried in >= 3 nearby
+// triangles of the 27-cell neighbourhood (abi41.cu:5226-5439).
+__global__ void __launch_bounds__(kThreads) k_island(View v) {
+    const Params& P = *v.P;
+    const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vertex >= P.V) return;
+    if (!(__ldg(&v.inv_mass[vertex]) > 0.0f)) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const F3 p = f3(v.pos[vertex]), pp = f3(v.prev[vertex]);
+    if (!finite3(p) || !finite3(pp)) {
+        count1(v.counts, kCntIslandGuarded);
+        return;
+    }
+    int maxn = P.max_neighbors < 1 ? 1 : P.max_neighbors;
+    int max_contacts = maxn * 2;
+    if (max_contacts > 48) max_contacts = 48;
+    if (max_contacts < 3) max_contacts = 3;
+    const int scan_limit = max_contacts * 10;
+    int accepted_tris[48];
+    const int cx = cell_of(p.x, P.tcell), cy = cell_of(p.y, P.tcell), cz = cell_of(p.z, P.tcell);
+    int scanned = 0, contacts = 0;
+    float pen_sum = 0.0f, wsum = 0.0f, max_pen = 0.0f;
+    F3 axis{0.0f, 0.0f, 0.0f}, best{0.0f, 0.0f, 1.0f};
+    for (int dz = -1; dz <= 1 && contacts < max_contacts && scanned < scan_limit; ++dz)
+        for (int dy = -1; dy <= 1 && contacts < max_contacts && scanned < scan_limit; ++dy)
+            for (int dx = -1; dx <= 1 && contacts < max_contacts && scanned < scan_limit; ++dx) {
+                const int b = (int)bucket_of(cx + dx, cy + dy, cz + dz, P.tbuckets);
+                const int s = v.tb_start[b];
+                const int lim = min(v.tb_start[b + 1] - s, kBucketSlots);
+                for (int k = 0; k < lim && contacts < max_contacts && scanned < scan_limit; ++k) {
+                    ++scanned;
+                    const int tri = v.tb_ent[s + k];
+                    bool dup = false;
+                    for (int q = 0; q < contacts; ++q)
+                        if (accepted_tris[q] == tri) {
+                            dup = true;
+                            break;
+                        }
+                    if (dup) continue;
+                    if (tri < 0 || tri >= P.T) {
+                        count1(v.counts, kCntIslandGuarded);
+                        continue;
+                    }
+                    const int4 t = __ldg(&v.tris[tri]);
+                    if (!tri_valid(P, t) || rest_vt_neighbor(v, vertex, t, target, onset)) continue;
+                    const F3 a = f3(v.pos[t.x]), b2 = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
+                    const F3 ap = f3(v.prev[t.x]), bp = f3(v.prev[t.y]), cp = f3(v.prev[t.z]);
+                    if (!finite3(a) || !finite3(b2) || !finite3(c) || !finite3(ap) || !finite3(bp) || !finite3(cp)) {
+                        count1(v.counts, kCntIslandGuarded);
+                        continue;
+                    }
+                    const F3 q = closest_on_triangle(p, a, b2, c);
+                    F3 delta = p - q;
+                    const float dsq = dot3(delta, delta);
+                    float dist = sqrtf(fmaxf(dsq, kEps));
+                    if (dist >= target) continue;
+                    F3 nrm{0.0f, 0.0f, 1.0f};
+                    if (dsq > kEps) {
+                        nrm = delta * (1.0f / dist);
+                    } else {
+                        nrm = cross3(b2 - a, c - a);
+                        const float nl = dot3(nrm, nrm);
+                        if (nl > kEps) {
+                            nrm = nrm * (1.0f / sqrtf(nl));
+                        } else {
+                            const F3 rv = f3(ld4(&v.rest[vertex]));
+                            const F3 rd = rv - closest_on_triangle(rv, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])),
+                                                                   f3(ld4(&v.rest[t.z])));
+                            const float rl = dot3(rd, rd);
+                            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+                        }
+                        delta = nrm * dist;
+                        dist = 0.0f;
+                    }
+                    if (!finite3(nrm)) {
+                        count1(v.counts, kCntIslandGuarded);
+                        continue;
+                    }
+                    const F3 qprev = closest_on_triangle(pp, ap, bp, cp);
+                    const F3 pdelta = pp - qprev;
+                    if (dot3(pdelta, nrm) > target * 0.25f && dot3(delta, nrm) > -target * 0.10f) continue;
+                    float wa, wb, wc;
+                    barycentric(q, a, b2, c, &wa, &wb, &wc);
+                    const float pen = target - dist;
+                    if (pen <= 0.0f) continue;
+                    accepted_tris[contacts++] = tri;
+                    pen_sum += pen;
+                    wsum += __ldg(&v.inv_mass[t.x]) * wa + __ldg(&v.inv_mass[t.y]) * wb + __ldg(&v.inv_mass[t.z]) * wc;
+                    axis = axis + nrm * pen;
+                    if (pen > max_pen) {
+                        max_pen = pen;
+                        best = nrm;
+                    }
+                }
+            }
+    if (contacts <= 0) return;
+    count_add(v.counts, kCntIslandCandidates, (unsigned long long)contacts);
+    if (contacts < 3) {
+        count1(v.counts, kCntIslandGuarded);
+        return;
+    }
+    const float avg_pen = pen_sum / (float)contacts;
+    if (avg_pen < target * 0.04f) {
+        count1(v.counts, kCntIslandGuarded);
+        return;
+    }
+    const float alen = len3(axis);
+    const F3 agg = alen > kEps ? axis * (1.0f / alen) : best;
+    const float sw = __ldg(&v.inv_mass[vertex]);
+    const float sample = wsum / (float)contacts;
+    const float share = sw / fmaxf(sw + sample, kEps);
+    const float max_delta = fmaxf(target * 0.30f, 1.0e-5f);
+    const float dl = fminf(avg_pen * 0.50f * share, max_delta);
+    if (!finite3(agg) || !isfinite(dl) || dl <= kEps) {
+        count1(v.counts, kCntIslandGuarded);
+        return;
+    }
+    accumulate(v, vertex, agg * dl);
+    count1(v.counts, kCntIslandClusters);
+    count_add(v.counts, kCntIslandVertexRefs, (unsigned long long)contacts);
+    count1(v.counts, kCntIslandAppliedVertices);
+    if (isfinite(dl) && dl > 0.0f) {
+        const unsigned long long micro = (unsigned long long)(fminf(dl, 1024.0f) * 1000000.0f);
+        atomicMax(&v.counts[kCntIslandMaxDeltaMicro], micro);
+    }
+}
+
+// Average the accumulated pushes, clamp to 0.35 r, apply with a 0.55 prev
+// shift, and clear the accumulators for the next pass (abi41.cu:4953-4988).
+__global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
+    const Params& P = *v.P;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.V) return;
+    const Acc4 a = v.acc[i];
+    v.acc[i] = Acc4{0, 0, 0, 0};
+    if (!(__ldg(&v.inv_mass[i]) > 0.0f) || a.w <= 0) return;
+    F3 avg = F3{from_fix(a.x), from_fix(a.y), from_fix(a.z)} * (1.0f / (float)a.w);
+    const float max_delta = fmaxf(contact_radius(P) * 0.35f, 1.0e-4f);
+    const float dl = len3(avg);
+    if (dl > max_delta) avg = avg * (max_delta / dl);
+    const float4 p = v.pos[i];
+    v.pos[i] = f4(f3(p) + avg, p.w);
+    v.prev[i] = f4(f3(v.prev[i]) + avg * 0.55f, 0.0f);
+    const float al = len3(avg);
+    if (al > 0.0f) atomicMax(v.max_delta_bits, __float_as_uint(al));
+}
+
+}  // namespace
+
+// Host-side entry points used by the solver orchestration.
+struct SelfLaunch {
+    static void vhash(const View& v, int V, int nb, cudaStream_t s) {
+        k_vhash_count<<<blocks_for(V), kThreads, 0, s>>>(v);
+        k_scan<<<1, 1024, 0, s>>>(v.vb_count, v.vb_start, nb);
+        k_vhash_scatter<<<blocks_for(V), kThreads, 0, s>>>(v);
+        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.vb_start, v.vb_ent, nb);
+    }
+    static void thash(const View& v, int T, int nb, cudaStream_t s) {
+        k_prim_hash<true><<<blocks_for(T), kThreads, 0, s>>>(v, false);
+        k_scan<<<1, 1024, 0, s>>>(v.tb_count, v.tb_start, nb);
+        k_prim_hash<true><<<blocks_for(T), kThreads, 0, s>>>(v, true);
+        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.tb_start, v.tb_ent, nb);
+    }
+    static void ehash(const View& v, int E, int nb, cudaStream_t s) {
+        k_prim_hash<false><<<blocks_for(E), kThreads, 0, s>>>(v, false);
+        k_scan<<<1, 1024, 0, s>>>(v.eb_count, v.eb_start, nb);
+        k_prim_hash<false><<<blocks_for(E), kThreads, 0, s>>>(v, true);
+        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.eb_start, v.eb_ent, nb);
+    }
+};
+
+void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s) {
+    if (V > 0) SelfLaunch::vhash(v, V, nb, s);
+}
+void self_build_triangle_hash(const View& v, int T, int nb, cudaStream_t s) {
+    if (T > 0) SelfLaunch::thash(v, T, nb, s);
+}
+void self_build_edge_hash(const View& v, int E, int nb, cudaStream_t s) {
+    if (E > 0) SelfLaunch::ehash(v, E, nb, s);
+}
+void self_neighbors(const View& v, int V, bool hashed, cudaStream_t s) {
+    if (V <= 0) return;
+    if (hashed)
+        k_neighbors_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
+    else
+        k_neighbors_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
+}
+void self_vv(const View& v, int V, cudaStream_t s) {
+    if (V > 0) k_vv<<<blocks_for(V), kThreads, 0, s>>>(v);
+}
+void self_vt(const View& v, int V, bool hashed, cudaStream_t s) {
+    if (V <= 0) return;
+    if (hashed)
+        k_vt_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
+    else
+        k_vt_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
+}
+void self_ee(const View& v, int E, bool hashed, cudaStream_t s) {
+    if (E <= 0) return;
+    if (hashed)
+        k_ee_hash<<<blocks_for(E), kThreads, 0, s>>>(v);
+    else
+        k_ee_brute<<<blocks_for(E), kThreads, 0, s>>>(v);
+}
+void self_island(const View& v, int V, cudaStream_t s) {
+    if (V > 0) k_island<<<blocks_for(V), kThreads, 0, s>>>(v);
+}
+void self_apply(const View& v, int V, cudaStream_t s) {
+    if (V > 0) k_self_apply<<<blocks_for(V), kThreads, 0, s>>>(v);
+}
+
+}  // namespace xg

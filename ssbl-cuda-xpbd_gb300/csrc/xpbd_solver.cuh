@@ -1,0 +1,199 @@
+// Device-side state of one cloth solver and the declarations shared by the
+// CUDA translation units of the GB300 XPBD library.
+//
+// Layout in HBM (one allocation per array, 256-byte aligned by cudaMalloc):
+//   pos[2]   float4 x V   ping-pong; .w = effective inverse mass (0 = pinned)
+//   prev     float4 x V   previous position (.w unused)
+//   vel      float4 x V
+//   rest     float4 x V   rest pose (.w unused)
+//   spring   CSR by vertex: off[V+1], ent[2E] = {other | side<<31, rest}
+//   tether   CSR by vertex: off[V+1], ent[2L] = {other | side<<31, rest}
+//   bends    int2 x B sorted by colour, rest f32 x B (colour ranges on host)
+//   tris     int4 x T {a, b, c, 0}
+//   edges    int2 x E
+//   pins     per vertex: target float4, weight f32 (-1 = none), relaxation f32
+// float4 rows make every gather of a neighbour one 16-byte load and carry the
+// inverse mass with the position, which the constraint kernels need together.
+#pragma once
+
+#include "xpbd_math.cuh"
+
+namespace xg {
+
+constexpr int kThreads = 256;
+constexpr int kNeighborSlots = 32;    // VV neighbour table width (abi41.cu:38)
+constexpr int kBucketSlots = 32;      // per-bucket query cap (abi41.cu:29, 32, 36)
+constexpr int kMaxPrimitiveCells = 64;
+constexpr int kSideBit = (int)0x80000000u;
+
+// Fixed-point self-collision accumulator of one vertex: delta x, y, z in
+// 2^-32 m units and the number of contributions.
+struct __align__(32) Acc4 {
+    long long x, y, z, w;
+};
+
+// Counter slots of the diagnostics block (same meaning as abi41.cu:41-78).
+enum Counter {
+    kCntSoftContacts = 0,
+    kCntExactImpulseContacts = 1,
+    kCntEdgeEdgeContacts = 2,
+    kCntHardFallbacks = 3,
+    kCntSelfCandidates = 9,
+    kCntSelfOverflow = 10,
+    kCntStaticSdfContacts = 11,
+    kCntLraTacks = 12,
+    kCntBendingWings = 13,
+    kCntTackGuards = 14,
+    kCntBendingGuards = 15,
+    kCntIslandCandidates = 16,
+    kCntIslandClusters = 17,
+    kCntIslandVertexRefs = 18,
+    kCntIslandAppliedVertices = 19,
+    kCntIslandGuarded = 20,
+    kCntIslandMaxDeltaMicro = 21,
+    kCntFilterSeen = 22,
+    kCntFilterAcceptedVv = 23,
+    kCntFilterAcceptedVt = 24,
+    kCntFilterAcceptedEe = 25,
+    kCntFilterRejectedRest = 26,
+    kCntFilterRejectedDuplicate = 27,
+    kCntFilterRejectedOwnership = 28,
+    kCntFilterCacheHits = 29,
+    kCntFilterCacheMisses = 30,
+    kCntClusterCount = 31,
+    kCntClusterOwnedContacts = 32,
+    kCntFrictionCorrections = 33,
+    kCntSlots = 38
+};
+
+// Values that can change between frames without changing the launch
+// sequence.  They live in device memory so a captured CUDA graph stays valid
+// when the caller moves a collider or the pins.
+struct Params {
+    int V, E, T, B, L;
+    float damping;
+    float gravity[3];
+    float stretch_compliance;
+    float bend_compliance;
+    float lra_compliance;
+    float margin;
+    float thickness;
+    float friction;
+    float tangent_damping;
+    int use_ground;
+    float ground_height;
+    int use_wall;
+    float wall_origin[3];
+    float wall_normal[3];
+    int use_sphere;
+    float sphere_center[3];
+    float sphere_radius;
+    // static SDF
+    int sdf_ready;
+    int sdf_signed;
+    int sdf_dim[3];
+    float sdf_origin[3];
+    float sdf_voxel;
+    int static_tri_count;
+    // self collision
+    float self_radius;     // contact target distance r
+    int self_mode;         // 1 fast, 2 strict
+    int max_neighbors;     // clamp of cfg.max_self_collision_neighbors
+    float vcell, tcell, ecell;
+    int vbuckets, tbuckets, ebuckets;
+    int vhash, thash, ehash;  // hash in use (else brute force)
+};
+
+// Device pointers of one solver, passed by value to each kernel.
+struct View {
+    const Params* P;
+    float4* pos_in;       // snapshot read by gathers
+    float4* pos;          // position written by this kernel / in place
+    float4* prev;
+    float4* vel;
+    const float4* rest;
+    const float* inv_mass;
+    const int* sp_off;
+    const int2* sp_ent;
+    const int* te_off;
+    const int2* te_ent;
+    const int* bj_off;    // bends as a gather when no colours are given
+    const int2* bj_ent;
+    const int2* bends;
+    const float* bend_rest;
+    const int4* tris;
+    const int2* edges;
+    const float* edge_rest;
+    const float4* pin_target;  // per vertex
+    const float* pin_weight;   // per vertex; -1 = no pin
+    const float* pin_relax;    // per vertex soft-pin relaxation
+    const int* tri_off;   // vertex -> incident triangles (for normals)
+    const int* tri_inc;
+    unsigned long long* counts;
+    // static SDF
+    const float* sdf;
+    const float4* static_tris;  // 3 per triangle
+    // self collision
+    int4* vcell;            // cx, cy, cz, bucket per vertex
+    int* vb_count;          // [vbuckets]
+    int* vb_start;          // [vbuckets + 1]
+    int* vb_ent;            // [V]
+    int* tb_count;
+    int* tb_start;
+    int* tb_ent;
+    int* ecount;            // per-primitive cell-entry counts scratch
+    int* eb_count;
+    int* eb_start;
+    int* eb_ent;
+    int tb_capacity, eb_capacity;
+    int* nb_count;          // [V]
+    int* nb_idx;            // [V * 32]
+    Acc4* acc;         // fixed-point delta xyz + contact weight
+    unsigned* max_delta_bits;
+};
+
+// Warp-aggregated counter increment: one atomic per warp, lane count from the
+// active mask.
+__device__ __forceinline__ void count1(unsigned long long* counts, int slot) {
+    if (!counts) return;
+    const unsigned mask = __activemask();
+    if ((threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(&counts[slot], (unsigned long long)__popc(mask));
+}
+
+__device__ __forceinline__ void count_add(unsigned long long* counts, int slot, unsigned long long v) {
+    if (counts && v) atomicAdd(&counts[slot], v);
+}
+
+__device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+
+// ---- host launchers (defined in the .cu files) ----
+void launch_predict(const View& v, int V, float dt, cudaStream_t s);
+// pass flags for launch_vertex_pass
+enum PassFlags : unsigned {
+    kPassSpring = 1u,
+    kPassPin = 2u,
+    kPassAnalytic = 4u,
+    kPassSdf = 8u,
+    kPassPinPolish = 16u,
+    kPassVelocity = 32u,
+    kPassTether = 64u,
+    kPassBend = 128u,
+};
+void launch_vertex_pass(const View& v, int V, float dt, unsigned flags, cudaStream_t s);
+void launch_bend_color(const View& v, int start, int count, float dt, cudaStream_t s);
+void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s);
+void launch_pack_positions(float* dst, const float4* src, int V, cudaStream_t s);
+void launch_sdf_build(const View& v, int voxels, cudaStream_t s);
+
+// self collision (bucket counts must be zeroed before each hash build)
+void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s);
+void self_build_triangle_hash(const View& v, int T, int nb, cudaStream_t s);
+void self_build_edge_hash(const View& v, int E, int nb, cudaStream_t s);
+void self_neighbors(const View& v, int V, bool hashed, cudaStream_t s);
+void self_vv(const View& v, int V, cudaStream_t s);
+void self_vt(const View& v, int V, bool hashed, cudaStream_t s);
+void self_ee(const View& v, int E, bool hashed, cudaStream_t s);
+void self_island(const View& v, int V, cudaStream_t s);
+void self_apply(const View& v, int V, cudaStream_t s);
+
+}  // namespace xg

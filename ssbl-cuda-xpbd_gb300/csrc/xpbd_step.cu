@@ -1,0 +1,554 @@
+// Per-vertex kernels of one XPBD substep: prediction, the fused constraint /
+// contact pass, bends per colour, and the position pack for downloads.
+//
+// The reference launches one kernel per stage over every vertex or
+// constraint (native/src/ssbl_xpbd_cuda_abi41.cu:9165-9376): integrate, pins,
+// springs (float atomics into pos), pins, analytic contacts, SDF contacts,
+// pins, velocity.  Pins, analytic contacts, SDF contacts and the velocity
+// update only read and write the vertex they act on, so this library runs
+// them as stages of one per-vertex kernel.  Stretch (and the once-per-frame
+// tethers) become a gather over a vertex->constraint CSR that reads a
+// snapshot of the positions (ping-pong buffer) and sums the corrections of
+// the incident constraints in constraint order: the same snapshot-Jacobi
+// update as the reference's atomics, without float atomics, and therefore
+// deterministic.
+#include "xpbd_solver.cuh"
+
+namespace xg {
+
+namespace {
+
+// Velocity response of a static contact with unit normal n: remove the inward
+// normal velocity, damp the tangent, then Coulomb-style friction bounded by
+// friction * normal_proxy (abi41.cu:910-949).
+__device__ bool contact_response(const Params& P, unsigned long long* counts, F3 n, float normal_proxy, F3* vel) {
+    if (!finite3(n) || !finite3(*vel)) return false;
+    const float vn = dot3(*vel, n);
+    if (vn < 0.0f) *vel = *vel - n * vn;
+    bool corrected = false;
+    F3 tangent = *vel - n * dot3(*vel, n);
+    float tlen = len3(tangent);
+    const float damping = clamp01f(P.tangent_damping);
+    if (damping > 0.0f && tlen > 1.0e-6f) {
+        *vel = *vel - tangent * damping;
+        corrected = true;
+    }
+    tangent = *vel - n * dot3(*vel, n);
+    tlen = len3(tangent);
+    const float friction = fmaxf(P.friction, 0.0f);
+    if (friction > 0.0f && normal_proxy > 0.0f && tlen > 1.0e-6f) {
+        const float drop = fminf(tlen, friction * normal_proxy);
+        if (drop > 1.0e-7f) {
+            *vel = *vel - tangent * (drop / fmaxf(tlen, kEps));
+            corrected = true;
+        }
+    }
+    if (corrected) count1(counts, kCntFrictionCorrections);
+    return corrected;
+}
+
+struct VState {
+    F3 p, prev, vel;
+    float w;  // effective inverse mass
+};
+
+// Weighted pin projection of one vertex (abi41.cu:3466-3509).  Pins are
+// stored per vertex (weight -1 = no pin; a vertex listed twice keeps its last
+// entry) and the relaxation 1 - (1 - s)^(1/(I+1)) is precomputed on the host.
+__device__ void pin_stage(const View& v, int i, float inv_mass, float dt, VState* s) {
+    const float weight = __ldg(&v.pin_weight[i]);
+    if (!isfinite(weight) || weight < 0.05f) return;
+    const F3 target = f3(ld4(&v.pin_target[i]));
+    if (weight >= 0.75f || inv_mass <= 0.0f) {
+        s->p = target;
+        s->prev = target;
+        s->vel = F3{0.0f, 0.0f, 0.0f};
+        return;
+    }
+    const float relax = __ldg(&v.pin_relax[i]);
+    if (relax <= 0.0f) return;
+    const F3 corrected = s->p + (target - s->p) * relax;
+    const F3 damped = s->vel * fmaxf(1.0f - relax, 0.0f);
+    s->p = corrected;
+    s->prev = corrected - damped * fmaxf(dt, kEps);
+    s->vel = damped;
+}
+
+// Ground plane (z up), sphere and wall (abi41.cu:3511-3590).
+__device__ void analytic_stage(const Params& P, unsigned long long* counts, float inv_mass, float dt, VState* s) {
+    if (inv_mass <= 0.0f) return;
+    F3 p = s->p;
+    F3 vel = s->vel;
+    bool contacted = false;
+    const float margin = fmaxf(P.margin, 0.0f);
+    const float sdt = fmaxf(dt, kEps);
+    if (P.use_ground && p.z < P.ground_height + margin) {
+        const float target_z = P.ground_height + margin;
+        const float pen = target_z - p.z;
+        const F3 n{0.0f, 0.0f, 1.0f};
+        const float inward = fmaxf(-dot3(vel, n), 0.0f);
+        p.z = target_z;
+        contact_response(P, counts, n, inward + pen / sdt, &vel);
+        contacted = true;
+    }
+    if (P.use_sphere && P.sphere_radius > 0.0f) {
+        const F3 c{P.sphere_center[0], P.sphere_center[1], P.sphere_center[2]};
+        const F3 d = p - c;
+        const float dist = sqrtf(fmaxf(dot3(d, d), kEps));
+        const float target = P.sphere_radius + margin;
+        if (dist < target) {
+            const F3 n = dist > kEps ? d * (1.0f / dist) : F3{0.0f, 0.0f, 1.0f};
+            const float pen = target - dist;
+            const float inward = fmaxf(-dot3(vel, n), 0.0f);
+            p = c + n * target;
+            contact_response(P, counts, n, inward + pen / sdt, &vel);
+            contacted = true;
+        }
+    }
+    if (P.use_wall) {
+        const F3 o{P.wall_origin[0], P.wall_origin[1], P.wall_origin[2]};
+        F3 n{P.wall_normal[0], P.wall_normal[1], P.wall_normal[2]};
+        const float nlen = sqrtf(fmaxf(dot3(n, n), kEps));
+        n = n * (1.0f / nlen);
+        const float gap = dot3(p - o, n);
+        if (gap < margin) {
+            const float pen = margin - gap;
+            const float inward = fmaxf(-dot3(vel, n), 0.0f);
+            p = p + n * (margin - gap);
+            contact_response(P, counts, n, inward + pen / sdt, &vel);
+            contacted = true;
+        }
+    }
+    s->p = p;
+    if (contacted) {
+        s->vel = vel;
+        s->prev = p - vel * sdt;
+    }
+}
+
+__device__ __forceinline__ int sdf_index(const Params& P, int x, int y, int z) {
+    return (z * P.sdf_dim[1] + y) * P.sdf_dim[0] + x;
+}
+
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+
+__device__ float sdf_trilinear(const Params& P, const float* sdf, float gx, float gy, float gz) {
+    const int x0 = min(max((int)floorf(gx), 0), P.sdf_dim[0] - 1);
+    const int y0 = min(max((int)floorf(gy), 0), P.sdf_dim[1] - 1);
+    const int z0 = min(max((int)floorf(gz), 0), P.sdf_dim[2] - 1);
+    const int x1 = min(x0 + 1, P.sdf_dim[0] - 1);
+    const int y1 = min(y0 + 1, P.sdf_dim[1] - 1);
+    const int z1 = min(z0 + 1, P.sdf_dim[2] - 1);
+    const float tx = gx - (float)x0, ty = gy - (float)y0, tz = gz - (float)z0;
+    const float c000 = __ldg(&sdf[sdf_index(P, x0, y0, z0)]);
+    const float c100 = __ldg(&sdf[sdf_index(P, x1, y0, z0)]);
+    const float c010 = __ldg(&sdf[sdf_index(P, x0, y1, z0)]);
+    const float c110 = __ldg(&sdf[sdf_index(P, x1, y1, z0)]);
+    const float c001 = __ldg(&sdf[sdf_index(P, x0, y0, z1)]);
+    const float c101 = __ldg(&sdf[sdf_index(P, x1, y0, z1)]);
+    const float c011 = __ldg(&sdf[sdf_index(P, x0, y1, z1)]);
+    const float c111 = __ldg(&sdf[sdf_index(P, x1, y1, z1)]);
+    const float c0 = lerpf(lerpf(c000, c100, tx), lerpf(c010, c110, tx), ty);
+    const float c1 = lerpf(lerpf(c001, c101, tx), lerpf(c011, c111, tx), ty);
+    return lerpf(c0, c1, tz);
+}
+
+// Trilinear sample inside the grid, false outside (abi41.cu:1645-1691).
+__device__ bool sdf_sample(const Params& P, const float* sdf, F3 p, float* out) {
+    if (P.sdf_dim[0] < 2 || P.sdf_dim[1] < 2 || P.sdf_dim[2] < 2 || P.sdf_voxel <= 0.0f) return false;
+    const float inv = 1.0f / P.sdf_voxel;
+    const float gx = (p.x - P.sdf_origin[0]) * inv;
+    const float gy = (p.y - P.sdf_origin[1]) * inv;
+    const float gz = (p.z - P.sdf_origin[2]) * inv;
+    if (gx < 0.0f || gy < 0.0f || gz < 0.0f || gx > (float)(P.sdf_dim[0] - 1) || gy > (float)(P.sdf_dim[1] - 1) ||
+        gz > (float)(P.sdf_dim[2] - 1))
+        return false;
+    *out = sdf_trilinear(P, sdf, gx, gy, gz);
+    return isfinite(*out);
+}
+
+// Sample with the point clamped into the grid (abi41.cu:1693-1723).
+__device__ float sdf_sample_clamped(const Params& P, const float* sdf, F3 p) {
+    const float inv = 1.0f / fmaxf(P.sdf_voxel, kEps);
+    const float gx = fminf(fmaxf((p.x - P.sdf_origin[0]) * inv, 0.0f), (float)(P.sdf_dim[0] - 1));
+    const float gy = fminf(fmaxf((p.y - P.sdf_origin[1]) * inv, 0.0f), (float)(P.sdf_dim[1] - 1));
+    const float gz = fminf(fmaxf((p.z - P.sdf_origin[2]) * inv, 0.0f), (float)(P.sdf_dim[2] - 1));
+    return sdf_trilinear(P, sdf, gx, gy, gz);
+}
+
+// Normal of the nearest static triangle, used when the SDF gradient vanishes
+// (abi41.cu:1749-1769).
+__device__ F3 nearest_static_normal(const Params& P, const float4* tris, F3 p) {
+    F3 best{0.0f, 0.0f, 1.0f};
+    float best_sq = 3.402823466e+38f;
+    for (int t = 0; t < P.static_tri_count; ++t) {
+        const F3 a = f3(ld4(&tris[t * 3 + 0])), b = f3(ld4(&tris[t * 3 + 1])), c = f3(ld4(&tris[t * 3 + 2]));
+        const F3 d = p - closest_on_triangle(p, a, b, c);
+        const float dsq = dot3(d, d);
+        if (dsq < best_sq) {
+            best_sq = dsq;
+            best = dsq > kEps * kEps ? normalize_or(d, best) : normalize_or(cross3(b - a, c - a), best);
+        }
+    }
+    return normalize_or(best, F3{0.0f, 0.0f, 1.0f});
+}
+
+// Central-difference SDF gradient (abi41.cu:1771-1785).
+__device__ F3 sdf_normal(const Params& P, const float* sdf, const float4* tris, F3 p) {
+    const float h = fmaxf(P.sdf_voxel, 1.0e-5f);
+    const float dx = sdf_sample_clamped(P, sdf, p + F3{h, 0.0f, 0.0f}) - sdf_sample_clamped(P, sdf, p + F3{-h, 0.0f, 0.0f});
+    const float dy = sdf_sample_clamped(P, sdf, p + F3{0.0f, h, 0.0f}) - sdf_sample_clamped(P, sdf, p + F3{0.0f, -h, 0.0f});
+    const float dz = sdf_sample_clamped(P, sdf, p + F3{0.0f, 0.0f, h}) - sdf_sample_clamped(P, sdf, p + F3{0.0f, 0.0f, -h});
+    const F3 n{dx, dy, dz};
+    const float lsq = dot3(n, n);
+    if (!isfinite(lsq) || lsq <= 1.0e-12f) return nearest_static_normal(P, tris, p);
+    return n * (1.0f / sqrtf(lsq));
+}
+
+// Static SDF contact (abi41.cu:1831-1867).
+__device__ void sdf_stage(const View& v, const Params& P, float inv_mass, float dt, VState* s) {
+    if (inv_mass <= 0.0f || !P.sdf_ready) return;
+    const float margin = fmaxf(P.margin, 0.0f);
+    if (margin <= 0.0f) return;
+    float d = 0.0f;
+    if (!sdf_sample(P, v.sdf, s->p, &d) || d >= margin) return;
+    const F3 n = sdf_normal(P, v.sdf, v.static_tris, s->p);
+    if (!finite3(n)) return;
+    const float pen = margin - d;
+    if (!isfinite(pen) || pen <= 0.0f) return;
+    const F3 corrected = s->p + n * pen;
+    F3 vel = s->vel;
+    const float inward = fmaxf(-dot3(vel, n), 0.0f);
+    contact_response(P, v.counts, n, inward + pen / fmaxf(dt, kEps), &vel);
+    s->p = corrected;
+    s->vel = vel;
+    s->prev = corrected - vel * fmaxf(dt, kEps);
+    count1(v.counts, kCntStaticSdfContacts);
+}
+
+// v = v + feedback(measured - v) with the aligned-feedback clamp
+// (abi41.cu:5846-5884).
+__device__ void velocity_stage(const Params& P, float dt, VState* s) {
+    if (s->w <= 0.0f) {
+        s->vel = F3{0.0f, 0.0f, 0.0f};
+        return;
+    }
+    const float sdt = fmaxf(dt, kEps);
+    const F3 measured = (s->p - s->prev) * (1.0f / sdt);
+    const F3 base = s->vel;
+    if (!finite3(measured) || !finite3(base)) {
+        s->vel = F3{0.0f, 0.0f, 0.0f};
+        return;
+    }
+    const F3 proj = measured - base;
+    const float pdb = dot3(proj, base);
+    const float scale = (isfinite(pdb) && pdb > 0.0f) ? 0.9f : 1.0f;
+    const float max_delta = fmaxf(2.0e-4f, fmaxf(P.thickness, 0.0f) * 0.35f);
+    const float max_speed = max_delta / sdt;
+    F3 fb = proj * scale;
+    const float fspeed = len3(fb);
+    if (scale < 1.0f && isfinite(fspeed) && fspeed > max_speed && fspeed > kEps) fb = fb * (max_speed / fspeed);
+    if (!finite3(fb)) fb = F3{0.0f, 0.0f, 0.0f};
+    s->vel = base + fb;
+}
+
+// Stretch constraint of edge (i, j) seen from one of its endpoints
+// (abi41.cu:1927-1980): the correction is computed in the edge's own
+// orientation so both endpoints get bit-identical values.
+__device__ __forceinline__ void spring_term(const Params& P, unsigned long long* counts, float dt, float4 pi, float4 pj,
+                                            float rest, bool self_is_j, F3* dp, F3* dprev) {
+    const float wi = pi.w, wj = pj.w;
+    const float weight = wi + wj;
+    if (weight <= 0.0f) return;
+    const F3 delta = f3(pj) - f3(pi);
+    const float len = sqrtf(fmaxf(dot3(delta, delta), kEps));
+    const float c = len - rest;
+    const float alpha = fmaxf(P.stretch_compliance, 0.0f) / fmaxf(dt * dt, kEps);
+    const float dlambda = -c / (weight + alpha);
+    F3 corr = delta * (0.18f * dlambda / fmaxf(len, kEps));
+    const float corr_len = sqrtf(fmaxf(dot3(corr, corr), 0.0f));
+    const float max_corr = fmaxf(0.0025f, fminf(fmaxf(rest, 0.0f) * 0.10f, 0.025f));
+    if (corr_len > max_corr) {
+        corr = corr * (max_corr / fmaxf(corr_len, kEps));
+        if (!self_is_j) count1(counts, kCntHardFallbacks);
+    }
+    const float wself = self_is_j ? wj : wi;
+    if (wself > 0.0f) {
+        const F3 d = self_is_j ? corr * wj : corr * (-wi);
+        *dp = *dp + d;
+        if (c > 0.0f) *dprev = *dprev + d * 0.08f;
+    }
+}
+
+// Long-range tether (anchor i, dynamic j) seen from one endpoint
+// (abi41.cu:2710-2803).
+__device__ __forceinline__ void tether_term(const Params& P, unsigned long long* counts, float dt, float4 pi4, float4 pj4,
+                                            float rest, bool self_is_j, F3* dp, F3* dprev) {
+    const bool counter = !self_is_j;  // count once per tether
+    const float wi = pi4.w, wj = pj4.w;
+    const float weight = wi + wj;
+    if (!isfinite(weight) || weight <= 0.0f) {
+        if (counter) count1(counts, kCntTackGuards);
+        return;
+    }
+    const F3 pi = f3(pi4), pj = f3(pj4);
+    if (!finite3(pi) || !finite3(pj)) {
+        if (counter) count1(counts, kCntTackGuards);
+        return;
+    }
+    F3 dx = pj - pi;
+    const float len_sq = len_sq_xyz(dx);
+    if (!isfinite(len_sq) || len_sq <= 1.0e-10f || !isfinite(rest) || rest <= kEps) {
+        if (counter) count1(counts, kCntTackGuards);
+        return;
+    }
+    const float inv_len = 1.0f / sqrtf(len_sq);
+    const float len = len_sq * inv_len;
+    const float stretch = len - rest;
+    if (!isfinite(stretch) || stretch <= 0.0f) return;
+    dx = dx * inv_len;
+    const float base_c = fmaxf(P.lra_compliance, 1.0e-12f);
+    const float stiff = (1.0f / base_c) * 500000.0f;
+    const float alpha = (base_c / 500000.0f) / fmaxf(dt * dt, kEps);
+    const float sw = stiff / fmaxf(stiff + 500000.0f, 1.0f);
+    const float dlambda = -stretch / fmaxf(weight + alpha, kEps);
+    F3 corr = dx * (0.35f * sw * dlambda);
+    if (!finite3(corr)) {
+        if (counter) count1(counts, kCntTackGuards);
+        return;
+    }
+    const float corr_len = len3(corr);
+    const float max_corr = fmaxf(5.0e-4f, fminf(fmaxf(rest, P.thickness) * 0.20f, 0.035f));
+    if (!isfinite(corr_len) || corr_len <= 0.0f) return;
+    if (corr_len > max_corr) {
+        corr = corr * (max_corr / fmaxf(corr_len, kEps));
+        if (counter) count1(counts, kCntTackGuards);
+    }
+    const bool has_th = P.thickness > 0.0f;
+    const float cap = has_th ? 0.0025f : 0.012f;
+    const float rest_limit = fmaxf(rest, 0.0f) * (has_th ? 0.02f : 0.08f);
+    const float th_limit = has_th ? P.thickness * 0.12f : cap;
+    const float applied = fmaxf(5.0e-4f, fminf(fminf(rest_limit, th_limit), cap));
+    if (self_is_j) {
+        if (wj > 0.0f) {
+            const F3 d = limit_delta(corr * (wj / fmaxf(weight, kEps)), applied);
+            *dp = *dp + d;
+            *dprev = *dprev + d * 0.32f;
+        }
+    } else if (wi > 0.0f) {
+        const F3 d = limit_delta(corr * (-wi / fmaxf(weight, kEps)), applied);
+        *dp = *dp + d;
+        *dprev = *dprev + d * 0.32f;
+    }
+    if (counter) count1(counts, kCntLraTacks);
+}
+
+// Bend distance constraint between the two wing-opposite vertices, shared by
+// the per-colour kernel and the Jacobi gather used when no colours are given
+// (abi41.cu:2805-2884 and 2886-2970).  Returns false when the constraint is
+// skipped; `guard` is set when the reference would count a guard.
+__device__ __forceinline__ bool bend_correction(const Params& P, float dt, float4 pi4, float4 pj4, float rest, F3* corr_out,
+                                                bool* guard) {
+    *guard = false;
+    const float wi = pi4.w, wj = pj4.w;
+    const float weight = wi + wj;
+    if (!isfinite(weight) || weight <= 0.0f) return false;
+    if (!isfinite(rest) || rest <= kEps) {
+        *guard = true;
+        return false;
+    }
+    const F3 pi = f3(pi4), pj = f3(pj4);
+    if (!finite3(pi) || !finite3(pj)) {
+        *guard = true;
+        return false;
+    }
+    const F3 delta = pj - pi;
+    const float len_sq = len_sq_xyz(delta);
+    if (!isfinite(len_sq) || len_sq <= 1.0e-10f) {
+        *guard = true;
+        return false;
+    }
+    const float inv_len = 1.0f / sqrtf(len_sq);
+    const float len = len_sq * inv_len;
+    const float c = len - rest;
+    if (!isfinite(c) || fabsf(c) <= 1.0e-6f) return false;
+    const float alpha = fmaxf(P.bend_compliance, 0.0f) / fmaxf(dt * dt, kEps);
+    const float dlambda = -c / fmaxf(weight + alpha, kEps);
+    F3 corr = delta * (0.10f * dlambda * inv_len);
+    if (!finite3(corr)) {
+        *guard = true;
+        return false;
+    }
+    const float corr_len = len3(corr);
+    const float max_corr = fmaxf(2.5e-4f, fminf(fmaxf(rest, P.thickness) * 0.08f, 0.020f));
+    if (!isfinite(corr_len) || corr_len <= 0.0f) return false;
+    if (corr_len > max_corr) {
+        corr = corr * (max_corr / fmaxf(corr_len, kEps));
+        *guard = true;
+    }
+    *corr_out = corr;
+    return true;
+}
+
+__device__ __forceinline__ void bend_term(const Params& P, unsigned long long* counts, float dt, float4 pi, float4 pj,
+                                          float rest, bool self_is_j, F3* dp, F3* dprev) {
+    F3 corr;
+    bool guard;
+    const bool applied = bend_correction(P, dt, pi, pj, rest, &corr, &guard);
+    if (!self_is_j) {
+        if (guard) count1(counts, kCntBendingGuards);
+        if (applied) count1(counts, kCntBendingWings);
+    }
+    if (!applied) return;
+    const float wself = self_is_j ? pj.w : pi.w;
+    if (wself > 0.0f) {
+        const F3 d = self_is_j ? corr * pj.w : corr * (-pi.w);
+        *dp = *dp + d;
+        *dprev = *dprev + d * 0.06f;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_predict(View v, float dt) {
+    const Params& P = *v.P;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.V) return;
+    const float4 p4 = v.pos[i];
+    const float inv_mass = __ldg(&v.inv_mass[i]);
+    VState s;
+    s.w = p4.w;
+    s.prev = f3(p4);
+    if (!(p4.w > 0.0f)) {
+        s.vel = F3{0.0f, 0.0f, 0.0f};
+        s.p = f3(ld4(&v.rest[i]));
+    } else {
+        const F3 accel = F3{P.gravity[0], P.gravity[1], P.gravity[2]} + F3{0.0f, 0.0f, 0.0f};
+        F3 vel = f3(v.vel[i]) + accel * dt;
+        vel = vel * P.damping;
+        s.vel = vel;
+        s.p = f3(p4) + vel * dt;
+    }
+    pin_stage(v, i, inv_mass, dt, &s);
+    v.pos[i] = f4(s.p, s.w);
+    v.prev[i] = f4(s.prev, 0.0f);
+    v.vel[i] = f4(s.vel, 0.0f);
+}
+
+__global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, float dt, unsigned flags) {
+    const Params& P = *v.P;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.V) return;
+    const float4 p4 = v.pos_in[i];
+    VState s;
+    s.w = p4.w;
+    s.p = f3(p4);
+    s.prev = f3(v.prev[i]);
+    s.vel = f3(v.vel[i]);
+    const float inv_mass = __ldg(&v.inv_mass[i]);
+    if (flags & (kPassSpring | kPassTether | kPassBend)) {
+        const int kind = (flags & kPassSpring) ? 0 : ((flags & kPassTether) ? 1 : 2);
+        const int* off = kind == 0 ? v.sp_off : (kind == 1 ? v.te_off : v.bj_off);
+        const int2* ent = kind == 0 ? v.sp_ent : (kind == 1 ? v.te_ent : v.bj_ent);
+        const int begin = __ldg(&off[i]), end = __ldg(&off[i + 1]);
+        F3 dp = s.p, dprev = s.prev;
+        for (int k = begin; k < end; ++k) {
+            const int2 e = __ldg(&ent[k]);
+            const bool self_is_j = (e.x & kSideBit) != 0;
+            const float4 q4 = v.pos_in[e.x & 0x7fffffff];
+            const float rest = __int_as_float(e.y);
+            const float4 pi = self_is_j ? q4 : p4;
+            const float4 pj = self_is_j ? p4 : q4;
+            if (kind == 0)
+                spring_term(P, v.counts, dt, pi, pj, rest, self_is_j, &dp, &dprev);
+            else if (kind == 1)
+                tether_term(P, v.counts, dt, pi, pj, rest, self_is_j, &dp, &dprev);
+            else
+                bend_term(P, v.counts, dt, pi, pj, rest, self_is_j, &dp, &dprev);
+        }
+        s.p = dp;
+        s.prev = dprev;
+    }
+    if (flags & kPassPin) pin_stage(v, i, inv_mass, dt, &s);
+    if (flags & kPassAnalytic) analytic_stage(P, v.counts, inv_mass, dt, &s);
+    if (flags & kPassSdf) sdf_stage(v, P, inv_mass, dt, &s);
+    if (flags & kPassPinPolish) pin_stage(v, i, inv_mass, dt, &s);
+    if (flags & kPassVelocity) velocity_stage(P, dt, &s);
+    v.pos[i] = f4(s.p, s.w);
+    v.prev[i] = f4(s.prev, 0.0f);
+    v.vel[i] = f4(s.vel, 0.0f);
+}
+
+// Bend constraints of one colour, applied in place: no two bends of a colour
+// share a vertex (abi41.cu:2886-2970).
+__global__ void __launch_bounds__(kThreads) k_bend_color(View v, int start, int count, float dt) {
+    const Params& P = *v.P;
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= count) return;
+    const int b = start + local;
+    if (b < 0 || b >= P.B) {
+        count1(v.counts, kCntBendingGuards);
+        return;
+    }
+    const int2 pr = __ldg(&v.bends[b]);
+    const int i = pr.x, j = pr.y;
+    if (i < 0 || j < 0 || i >= P.V || j >= P.V || i == j) {
+        count1(v.counts, kCntBendingGuards);
+        return;
+    }
+    const float4 pi4 = v.pos[i], pj4 = v.pos[j];
+    F3 corr;
+    bool guard;
+    const bool applied = bend_correction(P, dt, pi4, pj4, __ldg(&v.bend_rest[b]), &corr, &guard);
+    if (guard) count1(v.counts, kCntBendingGuards);
+    if (!applied) return;
+    if (pi4.w > 0.0f) {
+        const F3 d = corr * (-pi4.w);
+        v.pos[i] = f4(f3(pi4) + d, pi4.w);
+        v.prev[i] = f4(f3(v.prev[i]) + d * 0.06f, 0.0f);
+    }
+    if (pj4.w > 0.0f) {
+        const F3 d = corr * pj4.w;
+        v.pos[j] = f4(f3(pj4) + d, pj4.w);
+        v.prev[j] = f4(f3(v.prev[j]) + d * 0.06f, 0.0f);
+    }
+    count1(v.counts, kCntBendingWings);
+}
+
+__global__ void k_copy_pos(float4* dst, const float4* src, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+__global__ void k_pack_positions(float* dst, const float4* src, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = src[i];
+    dst[i * 3 + 0] = p.x;
+    dst[i * 3 + 1] = p.y;
+    dst[i * 3 + 2] = p.z;
+}
+
+inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
+
+}  // namespace
+
+void launch_predict(const View& v, int V, float dt, cudaStream_t s) {
+    if (V > 0) k_predict<<<blocks_for(V), kThreads, 0, s>>>(v, dt);
+}
+
+void launch_vertex_pass(const View& v, int V, float dt, unsigned flags, cudaStream_t s) {
+    if (V > 0) k_vertex_pass<<<blocks_for(V), kThreads, 0, s>>>(v, dt, flags);
+}
+
+void launch_bend_color(const View& v, int start, int count, float dt, cudaStream_t s) {
+    if (count > 0) k_bend_color<<<blocks_for(count), kThreads, 0, s>>>(v, start, count, dt);
+}
+
+void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s) {
+    if (V > 0) k_copy_pos<<<blocks_for(V), kThreads, 0, s>>>(dst, src, V);
+}
+
+void launch_pack_positions(float* dst, const float4* src, int V, cudaStream_t s) {
+    if (V > 0) k_pack_positions<<<blocks_for(V), kThreads, 0, s>>>(dst, src, V);
+}
+
+}  // namespace xg

@@ -1,0 +1,473 @@
+"""ctypes host interface of the GB300 XPBD library.
+
+This module mirrors the reference's Python bridge (native_backend.py:
+``_load_library`` :535, ``_config_from_options`` :712, ``NativeXpbdSolver``
+:902-1463): same class and method names, same argument meaning, same errors
+(``NativeBackendUnavailable`` when the library cannot be loaded,
+``NativeSolverError`` carrying ``ssbl_last_error()`` when a call fails).  The
+reference bridge itself can load this library unchanged through
+``SSBL_NATIVE_DLL_PATH``; this module is the in-repo equivalent used by the
+tests and the benchmark.
+
+There is no CPU fallback: when the shared library is missing or no CUDA
+device is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .scene import ClothData, SolverOptions
+
+_CAP_STRETCH_OPTIMIZATION = 1 << 0
+_CAP_PIN_WEIGHTS = 1 << 1
+_CAP_GLOBAL_DYNAMIC_SCENE = 1 << 2
+
+F3 = ctypes.c_float * 3
+
+
+class NativeBackendUnavailable(RuntimeError):
+    pass
+
+
+class NativeSolverError(RuntimeError):
+    pass
+
+
+class NativeConfig(ctypes.Structure):
+    _fields_ = [
+        ("vertex_count", ctypes.c_int), ("edge_count", ctypes.c_int), ("bend_count", ctypes.c_int),
+        ("lra_count", ctypes.c_int), ("triangle_count", ctypes.c_int), ("static_triangle_count", ctypes.c_int),
+        ("edge_color_count", ctypes.c_int), ("bend_color_count", ctypes.c_int), ("lra_color_count", ctypes.c_int),
+        ("dt", ctypes.c_float), ("damping", ctypes.c_float), ("gravity", F3), ("stretch_compliance", ctypes.c_float),
+        ("bend_compliance", ctypes.c_float), ("lra_compliance", ctypes.c_float), ("collision_margin", ctypes.c_float),
+        ("use_ground", ctypes.c_int), ("ground_height", ctypes.c_float), ("use_wall", ctypes.c_int),
+        ("wall_origin", F3), ("wall_normal", F3), ("use_sphere", ctypes.c_int), ("sphere_center", F3),
+        ("sphere_radius", ctypes.c_float), ("self_collision", ctypes.c_int), ("self_collision_mode", ctypes.c_int),
+        ("cloth_thickness", ctypes.c_float), ("self_collision_distance", ctypes.c_float),
+        ("self_collision_interval", ctypes.c_int), ("max_self_collision_neighbors", ctypes.c_int),
+        ("use_volume_pressure", ctypes.c_int), ("rest_volume", ctypes.c_float), ("volume_compliance", ctypes.c_float),
+        ("pressure_strength", ctypes.c_float), ("volume_target_scale", ctypes.c_float),
+        ("volume_solve_interval", ctypes.c_int), ("self_probe_interval", ctypes.c_int),
+        ("self_surface_pair_interval", ctypes.c_int), ("jitter_stabilizer_enabled", ctypes.c_int),
+        ("contact_friction", ctypes.c_float), ("contact_tangent_damping", ctypes.c_float),
+        ("contact_compliance", ctypes.c_float), ("fast_self_collision_passes", ctypes.c_int),
+        ("stretch_optimization_enabled", ctypes.c_int), ("stretch_optimization_strength", ctypes.c_float),
+        ("static_sdf_voxel_size", ctypes.c_float), ("static_sdf_band_voxels", ctypes.c_int),
+        ("static_sdf_max_resolution", ctypes.c_int),
+    ]
+
+
+_PF = ctypes.POINTER(ctypes.c_float)
+_PI = ctypes.POINTER(ctypes.c_int)
+
+
+class NativeMesh(ctypes.Structure):
+    _fields_ = [
+        ("positions", _PF), ("inv_mass", _PF), ("edges", _PI), ("edge_rest_lengths", _PF),
+        ("edge_color_offsets", _PI), ("bends", _PI), ("bend_rest_lengths", _PF), ("bend_color_offsets", _PI),
+        ("lra_edges", _PI), ("lra_rest_lengths", _PF), ("lra_color_offsets", _PI), ("triangles", _PI),
+        ("static_triangles", _PF),
+    ]
+
+
+class NativeRuntimeColliders(ctypes.Structure):
+    _fields_ = [
+        ("use_ground", ctypes.c_int), ("ground_height", ctypes.c_float), ("use_wall", ctypes.c_int),
+        ("wall_origin", F3), ("wall_normal", F3), ("use_sphere", ctypes.c_int), ("sphere_center", F3),
+        ("sphere_radius", ctypes.c_float),
+    ]
+
+
+class NativeForceField(ctypes.Structure):
+    _fields_ = [
+        ("type", ctypes.c_int), ("use_min_distance", ctypes.c_int), ("use_max_distance", ctypes.c_int),
+        ("seed", ctypes.c_int), ("strength", ctypes.c_float), ("origin", F3), ("direction", F3), ("axis", F3),
+        ("falloff_power", ctypes.c_float), ("distance_min", ctypes.c_float), ("distance_max", ctypes.c_float),
+        ("radial_min", ctypes.c_float), ("radial_max", ctypes.c_float), ("noise", ctypes.c_float),
+        ("linear_drag", ctypes.c_float), ("quadratic_drag", ctypes.c_float), ("harmonic_damping", ctypes.c_float),
+        ("flow", ctypes.c_float), ("size", ctypes.c_float), ("rest_length", ctypes.c_float),
+        ("radial_falloff", ctypes.c_float), ("texture_nabla", ctypes.c_float), ("use_radial_min", ctypes.c_int),
+        ("use_radial_max", ctypes.c_int), ("use_2d_force", ctypes.c_int), ("use_global_coords", ctypes.c_int),
+        ("apply_to_location", ctypes.c_int),
+    ]
+
+
+class NativeFrameInputs(ctypes.Structure):
+    _fields_ = [
+        ("update_pin_targets", ctypes.c_int), ("pin_indices", _PI), ("pin_positions", _PF), ("pin_weights", _PF),
+        ("pin_count", ctypes.c_int), ("update_runtime_colliders", ctypes.c_int),
+        ("runtime_colliders", NativeRuntimeColliders), ("update_static_triangles", ctypes.c_int),
+        ("static_triangles", _PF), ("static_triangle_count", ctypes.c_int), ("update_dynamic_triangles", ctypes.c_int),
+        ("dynamic_triangles", _PF), ("dynamic_triangle_count", ctypes.c_int),
+        ("update_dynamic_indexed_triangles", ctypes.c_int), ("dynamic_triangle_vertices", _PF),
+        ("dynamic_triangle_vertex_count", ctypes.c_int), ("dynamic_triangle_indices", _PI),
+        ("dynamic_indexed_triangle_count", ctypes.c_int), ("dynamic_triangle_topology_changed", ctypes.c_int),
+        ("update_dynamic_particles", ctypes.c_int), ("dynamic_particle_positions", _PF),
+        ("dynamic_particle_radii", _PF), ("dynamic_particle_inv_mass", _PF), ("dynamic_particle_slot_ids", _PI),
+        ("dynamic_particle_phases", _PI), ("dynamic_particle_count", ctypes.c_int),
+        ("update_force_fields", ctypes.c_int), ("force_fields", ctypes.POINTER(NativeForceField)),
+        ("force_field_count", ctypes.c_int), ("unsupported_force_field_count", ctypes.c_int),
+    ]
+
+
+_DIAG_FLOATS = {
+    "step_ms", "hash_build_ms", "constraints_ms", "volume_ms", "analytic_collision_ms", "static_collision_ms",
+    "dynamic_collision_ms", "dynamic_particle_collision_ms", "self_hash_ms", "self_solve_ms", "self_probe_ms",
+    "self_recovery_ms", "sync_ms", "diagnostics_fetch_ms", "min_gap", "jitter_max_correction",
+    "fast_soft_repulsion_max_push", "fast_barrier_max_delta", "fast_overlap_island_max_delta",
+    "fast_cc_overlap_max_delta", "abi41_max_smoothed_delta", "static_sdf_build_ms", "abi41_pcg_initial_residual",
+    "abi41_pcg_final_residual", "abi41_pcg_max_delta", "dynamic_collider_pack_ms", "dynamic_triangle_upload_ms",
+    "dynamic_particle_upload_ms", "abi41_pcg_solve_ms", "abi41_pcg_system_ms", "abi41_pcg_ad_ms",
+    "abi41_direct_stretch_ms", "global_dynamic_scene_pack_ms", "global_dynamic_scene_upload_ms",
+    "global_dynamic_hash_ms",
+}
+_DIAG_ORDER = """step_ms hash_build_ms constraints_ms volume_ms analytic_collision_ms static_collision_ms
+dynamic_collision_ms dynamic_particle_collision_ms self_hash_ms self_solve_ms self_probe_ms self_recovery_ms sync_ms
+diagnostics_fetch_ms candidate_count resolved_contacts min_gap ccd_clamp_count recovery_passes local_retry_count
+jitter_stabilized_vertices jitter_rejected_vertices jitter_max_correction external_contact_cache_hits
+external_contact_cache_misses external_contact_cache_count external_contact_cache_overflow
+external_friction_corrections force_field_count unsupported_force_field_count dynamic_particle_count
+dynamic_particle_candidate_count dynamic_particle_contacts dynamic_particle_overflow dynamic_triangle_count
+static_triangle_count finite_flag fast_exact_vt_candidates fast_exact_vt_projected fast_exact_vt_guarded
+fast_exact_vt_skipped_rest fast_soft_repulsion_candidates fast_soft_repulsion_applied fast_soft_repulsion_max_push
+fast_hard_projection_count fast_manifold_contacts fast_manifold_reused fast_barrier_projected
+fast_barrier_smoothed_vertices fast_barrier_overflow fast_barrier_max_delta fast_edge_edge_candidates
+fast_edge_edge_contacts fast_triangle_pair_candidates fast_triangle_pair_contacts fast_triangle_pair_skipped_rest
+fast_contact_classification_guarded fast_region_cluster_candidates fast_region_cluster_contacts
+fast_region_cluster_guarded fast_overlap_island_candidates fast_overlap_island_clusters
+fast_overlap_island_vertex_refs fast_overlap_island_applied_vertices fast_overlap_island_guarded
+fast_overlap_island_max_delta fast_cc_overlap_components fast_cc_overlap_seed_triangles fast_cc_overlap_owned_vertices
+fast_cc_overlap_union_edges fast_cc_overlap_guarded fast_cc_overlap_applied_vertices fast_cc_overlap_max_delta
+abi41_soft_contact_count abi41_exact_impulse_contact_count abi41_edge_edge_contact_count abi41_max_smoothed_delta
+abi41_hard_projection_fallbacks static_sdf_rebuild_count static_sdf_voxel_count static_sdf_grid_x static_sdf_grid_y
+static_sdf_grid_z static_sdf_build_ms static_sdf_contact_count static_sdf_unsigned_fallback_count
+abi41_pcg_iterations abi41_pcg_guarded abi41_pcg_csr_nnz abi41_pcg_texture_ready abi41_pcg_initial_residual
+abi41_pcg_final_residual abi41_pcg_max_delta abi41_lra_tack_count abi41_bending_wing_count
+abi41_bending_texture_ready abi41_tack_jitter_guarded abi41_bending_guarded dynamic_collider_pack_ms
+dynamic_triangle_upload_ms dynamic_particle_upload_ms dynamic_collider_cache_hits dynamic_collider_cache_misses
+abi41_pcg_solve_ms abi41_pcg_system_ms abi41_pcg_ad_ms abi41_direct_stretch_ms dynamic_pair_cache_hits
+dynamic_pair_cache_misses dynamic_pair_cache_reused_triangles dynamic_pair_cache_reused_particles
+dynamic_collision_skipped_launches self_collision_skipped_launches self_candidate_count self_filter_seen
+self_filter_accepted_vv self_filter_accepted_vt self_filter_accepted_ee self_filter_rejected_rest
+self_filter_rejected_duplicate self_filter_rejected_ownership self_filter_cache_hits self_filter_cache_misses
+self_cluster_count self_cluster_owned_contacts dynamic_triangle_candidate_count dynamic_triangle_bucket_overflow
+dynamic_triangle_large_primitive_count dynamic_triangle_aabb_reject_count dynamic_triangle_max_bucket_occupancy
+global_dynamic_scene_pack_ms global_dynamic_scene_upload_ms global_dynamic_hash_ms global_dynamic_particle_count
+global_dynamic_triangle_count global_dynamic_hash_overflow""".split()
+
+
+class NativeDiagnostics(ctypes.Structure):
+    _fields_ = [
+        (n, ctypes.c_float if n in _DIAG_FLOATS else (ctypes.c_int if n == "finite_flag" else ctypes.c_longlong))
+        for n in _DIAG_ORDER
+    ]
+
+
+# ------------------------------------------------------------ loading ----
+_LIB = None
+
+
+def dll_path() -> str:
+    """Library path: SSBL_NATIVE_DLL_PATH, else the in-tree build."""
+    override = os.environ.get("SSBL_NATIVE_DLL_PATH")
+    if override:
+        return override
+    from .build import library_path
+
+    return library_path()
+
+
+def _load_library():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = dll_path()
+    if not os.path.exists(path):
+        raise NativeBackendUnavailable(f"Missing GB300 XPBD library: {path} (run the package build first)")
+    try:
+        lib = ctypes.CDLL(path)
+    except OSError as exc:
+        raise NativeBackendUnavailable(f"Unable to load GB300 XPBD library: {exc}") from exc
+    vp = ctypes.c_void_p
+    sig = {
+        "ssbl_create_solver": (vp, [ctypes.POINTER(NativeConfig), ctypes.POINTER(NativeMesh)]),
+        "ssbl_destroy_solver": (ctypes.c_int, [vp]),
+        "ssbl_reset_solver": (ctypes.c_int, [vp]),
+        "ssbl_update_pin_targets": (ctypes.c_int, [vp, _PI, _PF, _PF, ctypes.c_int]),
+        "ssbl_update_runtime_colliders": (ctypes.c_int, [vp, ctypes.POINTER(NativeRuntimeColliders)]),
+        "ssbl_update_positions": (ctypes.c_int, [vp, _PF, ctypes.c_int]),
+        "ssbl_update_static_triangles": (ctypes.c_int, [vp, _PF, ctypes.c_int]),
+        "ssbl_update_dynamic_triangles": (ctypes.c_int, [vp, _PF, ctypes.c_int]),
+        "ssbl_update_frame_inputs": (ctypes.c_int, [vp, ctypes.POINTER(NativeFrameInputs)]),
+        "ssbl_step_solver": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+        "ssbl_step_solver_ex": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+        "ssbl_download_positions": (ctypes.c_int, [vp, _PF, ctypes.c_int]),
+        "ssbl_get_diagnostics": (ctypes.c_int, [vp, ctypes.POINTER(NativeDiagnostics)]),
+        "ssbl_capabilities": (ctypes.c_uint, []),
+        "ssbl_create_global_dynamic_scene": (vp, []),
+        "ssbl_destroy_global_dynamic_scene": (ctypes.c_int, [vp]),
+        "ssbl_update_global_dynamic_scene": (ctypes.c_int, [vp, vp]),
+        "ssbl_attach_global_dynamic_scene": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+        "ssbl_clear_global_dynamic_scene": (ctypes.c_int, [vp]),
+        "ssbl_last_error": (ctypes.c_char_p, []),
+        "xpbd_gb300_build_self_structures": (ctypes.c_int, [vp]),
+        "xpbd_gb300_read_buffer": (ctypes.c_longlong, [vp, ctypes.c_int, vp, ctypes.c_longlong]),
+        "xpbd_gb300_hash_info": (ctypes.c_int, [vp, _PI]),
+        "xpbd_gb300_set_graph_capture": (ctypes.c_int, [vp, ctypes.c_int]),
+        "xpbd_gb300_last_step_launches": (ctypes.c_longlong, [vp]),
+        "xpbd_gb300_synchronize": (ctypes.c_int, [vp]),
+        "xpbd_gb300_stream": (vp, [vp]),
+        "xpbd_gb300_profile_frame": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _PF,
+                                                    ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        if hasattr(lib, name):
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _fp(a: np.ndarray):
+    return _PF() if a is None or a.size == 0 else a.ctypes.data_as(_PF)
+
+
+def _ip(a: np.ndarray):
+    return _PI() if a is None or a.size == 0 else a.ctypes.data_as(_PI)
+
+
+def _last_error(lib) -> str:
+    raw = lib.ssbl_last_error()
+    return raw.decode("utf-8", errors="replace") if raw else "GB300 XPBD call failed without an error message."
+
+
+def capabilities() -> int:
+    return int(_load_library().ssbl_capabilities())
+
+
+def config_from_options(cloth: ClothData, options: SolverOptions, static_triangles: np.ndarray) -> NativeConfig:
+    """Fill the ABI41 config exactly like native_backend.py:712-766."""
+    c = NativeConfig()
+    c.vertex_count = len(cloth.positions_world)
+    c.edge_count = len(cloth.edges)
+    c.bend_count = len(cloth.bends)
+    c.lra_count = len(cloth.lra_edges)
+    c.triangle_count = len(cloth.triangles)
+    c.static_triangle_count = len(static_triangles)
+    c.edge_color_count = max(len(cloth.edge_color_offsets) - 1, 0)
+    c.bend_color_count = max(len(cloth.bend_color_offsets) - 1, 0)
+    c.lra_color_count = max(len(cloth.lra_color_offsets) - 1, 0)
+    o = options
+    c.dt, c.damping = float(o.dt), float(o.damping)
+    c.gravity = F3(*map(float, o.gravity))
+    c.stretch_compliance, c.bend_compliance, c.lra_compliance = map(float, (o.stretch_compliance, o.bend_compliance, o.lra_compliance))
+    c.collision_margin = float(o.collision_margin)
+    c.use_ground, c.ground_height = int(o.use_ground), float(o.ground_height)
+    c.use_wall = int(o.use_wall)
+    c.wall_origin, c.wall_normal = F3(*map(float, o.wall_origin)), F3(*map(float, o.wall_normal))
+    c.use_sphere, c.sphere_center, c.sphere_radius = int(o.use_sphere), F3(*map(float, o.sphere_center)), float(o.sphere_radius)
+    c.self_collision, c.self_collision_mode = int(o.self_collision), int(o.self_collision_mode)
+    c.cloth_thickness, c.self_collision_distance = float(o.cloth_thickness), float(o.self_collision_distance)
+    c.self_collision_interval, c.max_self_collision_neighbors = int(o.self_collision_interval), int(o.max_self_collision_neighbors)
+    c.use_volume_pressure, c.rest_volume = int(o.use_volume_pressure), float(cloth.rest_volume)
+    c.volume_compliance, c.pressure_strength = float(o.volume_compliance), float(o.pressure_strength)
+    c.volume_target_scale, c.volume_solve_interval = float(o.volume_target_scale), int(o.volume_solve_interval)
+    c.self_probe_interval, c.self_surface_pair_interval = int(o.self_probe_interval), int(o.self_surface_pair_interval)
+    c.jitter_stabilizer_enabled = int(o.jitter_stabilizer_enabled)
+    c.contact_friction, c.contact_tangent_damping = float(o.contact_friction), float(o.contact_tangent_damping)
+    c.contact_compliance, c.fast_self_collision_passes = float(o.contact_compliance), int(o.fast_self_collision_passes)
+    c.stretch_optimization_enabled = int(o.stretch_optimization_enabled)
+    c.stretch_optimization_strength = float(o.stretch_optimization_strength)
+    c.static_sdf_voxel_size, c.static_sdf_band_voxels = float(o.static_sdf_voxel_size), int(o.static_sdf_band_voxels)
+    c.static_sdf_max_resolution = int(o.static_sdf_max_resolution)
+    return c
+
+
+def colliders_from_options(o: SolverOptions) -> NativeRuntimeColliders:
+    r = NativeRuntimeColliders()
+    r.use_ground, r.ground_height, r.use_wall = int(o.use_ground), float(o.ground_height), int(o.use_wall)
+    r.wall_origin, r.wall_normal = F3(*map(float, o.wall_origin)), F3(*map(float, o.wall_normal))
+    r.use_sphere, r.sphere_center, r.sphere_radius = int(o.use_sphere), F3(*map(float, o.sphere_center)), float(o.sphere_radius)
+    return r
+
+
+def mesh_arrays(cloth: ClothData, static_triangles: np.ndarray) -> tuple[NativeMesh, list]:
+    """ABI41 mesh struct plus the arrays it points into (keep them alive)."""
+    keep = [
+        np.ascontiguousarray(cloth.positions_world, np.float32), np.ascontiguousarray(cloth.inv_mass, np.float32),
+        np.ascontiguousarray(cloth.edges, np.int32), np.ascontiguousarray(cloth.edge_rest_lengths, np.float32),
+        np.ascontiguousarray(cloth.edge_color_offsets, np.int32), np.ascontiguousarray(cloth.bends, np.int32),
+        np.ascontiguousarray(cloth.bend_rest_lengths, np.float32), np.ascontiguousarray(cloth.bend_color_offsets, np.int32),
+        np.ascontiguousarray(cloth.lra_edges, np.int32), np.ascontiguousarray(cloth.lra_rest_lengths, np.float32),
+        np.ascontiguousarray(cloth.lra_color_offsets, np.int32), np.ascontiguousarray(cloth.triangles, np.int32),
+        np.ascontiguousarray(np.asarray(static_triangles, np.float32).reshape(-1, 3)),
+    ]
+    m = NativeMesh(_fp(keep[0]), _fp(keep[1]), _ip(keep[2]), _fp(keep[3]), _ip(keep[4]), _ip(keep[5]), _fp(keep[6]),
+                   _ip(keep[7]), _ip(keep[8]), _fp(keep[9]), _ip(keep[10]), _ip(keep[11]), _fp(keep[12]))
+    return m, keep
+
+
+class NativeXpbdSolver:
+    """One cloth on the GPU (the reference's NativeXpbdSolver interface)."""
+
+    def __init__(self, cloth: ClothData, options: SolverOptions, static_triangles: np.ndarray):
+        self._lib = _load_library()
+        caps = capabilities()
+        if options.stretch_optimization_enabled and not caps & _CAP_STRETCH_OPTIMIZATION:
+            raise NativeSolverError("Loaded CUDA solver library does not support hard stretch optimization.")
+        if not caps & _CAP_PIN_WEIGHTS:
+            raise NativeSolverError("Loaded CUDA solver library does not support vertex-group pin weights.")
+        self._vertex_count = len(cloth.positions_world)
+        self._positions_out = np.empty((self._vertex_count, 3), np.float32)
+        self._static_triangle_count = len(static_triangles)
+        cfg = config_from_options(cloth, options, static_triangles)
+        mesh, keep = mesh_arrays(cloth, static_triangles)
+        self._handle = self._lib.ssbl_create_solver(ctypes.byref(cfg), ctypes.byref(mesh))
+        del keep
+        if not self._handle:
+            raise NativeSolverError(_last_error(self._lib))
+        if len(cloth.pin_indices) > 0:
+            self.update_pin_targets(cloth.pin_indices, cloth.pin_targets_world, cloth.pin_weights)
+
+    @classmethod
+    def from_raw(cls, config: NativeConfig, mesh: NativeMesh, pins=None) -> "NativeXpbdSolver":
+        """Create from ABI41 structs directly (the pointers in `mesh` must
+        stay valid for the call)."""
+        self = cls.__new__(cls)
+        self._lib = _load_library()
+        self._vertex_count = int(config.vertex_count)
+        self._positions_out = np.empty((self._vertex_count, 3), np.float32)
+        self._static_triangle_count = int(config.static_triangle_count)
+        self._handle = self._lib.ssbl_create_solver(ctypes.byref(config), ctypes.byref(mesh))
+        if not self._handle:
+            raise NativeSolverError(_last_error(self._lib))
+        if pins is not None and len(pins[0]) > 0:
+            self.update_pin_targets(*pins)
+        return self
+
+    @property
+    def handle(self) -> int:
+        return self._handle
+
+    def close(self) -> None:
+        if getattr(self, "_handle", None):
+            self._lib.ssbl_clear_global_dynamic_scene(self._handle)
+            self._lib.ssbl_destroy_solver(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, ok) -> None:
+        if not ok:
+            raise NativeSolverError(_last_error(self._lib))
+
+    def reset(self) -> None:
+        self._check(self._lib.ssbl_reset_solver(self._handle))
+
+    def update_pin_targets(self, indices, positions, weights=None) -> None:
+        idx = np.ascontiguousarray(indices, np.int32)
+        pos = np.ascontiguousarray(positions, np.float32)
+        w = np.ones(len(idx), np.float32) if weights is None else np.ascontiguousarray(weights, np.float32).reshape(-1)
+        if len(idx) != len(pos) or len(idx) != len(w):
+            raise NativeSolverError("Pin index, target, and weight arrays must have matching lengths.")
+        self._check(self._lib.ssbl_update_pin_targets(self._handle, _ip(idx), _fp(pos), _fp(w), len(idx)))
+
+    def update_runtime_colliders(self, options: SolverOptions) -> None:
+        self._colliders = colliders_from_options(options)
+        self._check(self._lib.ssbl_update_runtime_colliders(self._handle, ctypes.byref(self._colliders)))
+
+    def update_positions(self, positions: np.ndarray) -> None:
+        p = np.ascontiguousarray(positions, np.float32)
+        if p.shape != (self._vertex_count, 3):
+            raise NativeSolverError(f"Position upload expected shape ({self._vertex_count}, 3), got {tuple(p.shape)}.")
+        self._check(self._lib.ssbl_update_positions(self._handle, _fp(p), p.size))
+
+    def update_static_triangles(self, static_triangles: np.ndarray) -> None:
+        n = len(static_triangles)
+        if n <= 0 and self._static_triangle_count <= 0:
+            return
+        t = np.ascontiguousarray(np.asarray(static_triangles, np.float32).reshape(-1, 3))
+        self._check(self._lib.ssbl_update_static_triangles(self._handle, _fp(t), n))
+        self._static_triangle_count = n
+
+    def update_frame_inputs(self, *, pin_indices=None, pin_positions=None, pin_weights=None, update_pin=False,
+                            options: SolverOptions | None = None, static_triangles=None) -> None:
+        fi = NativeFrameInputs()
+        keep = []
+        if update_pin:
+            idx = np.ascontiguousarray(pin_indices, np.int32)
+            pos = np.ascontiguousarray(pin_positions, np.float32)
+            w = np.ones(len(idx), np.float32) if pin_weights is None else np.ascontiguousarray(pin_weights, np.float32)
+            keep += [idx, pos, w]
+            fi.update_pin_targets, fi.pin_indices, fi.pin_positions, fi.pin_weights, fi.pin_count = 1, _ip(idx), _fp(pos), _fp(w), len(idx)
+        if options is not None:
+            fi.update_runtime_colliders = 1
+            fi.runtime_colliders = colliders_from_options(options)
+        if static_triangles is not None:
+            t = np.ascontiguousarray(np.asarray(static_triangles, np.float32).reshape(-1, 3))
+            keep.append(t)
+            fi.update_static_triangles, fi.static_triangles, fi.static_triangle_count = 1, _fp(t), len(t) // 3
+        self._check(self._lib.ssbl_update_frame_inputs(self._handle, ctypes.byref(fi)))
+
+    def step(self, substeps: int, iterations: int, diagnostics: bool = True, synchronize: bool = True) -> None:
+        fetch = 1 if diagnostics else 0
+        sync = 1 if (synchronize or diagnostics) else 0
+        self._check(self._lib.ssbl_step_solver_ex(self._handle, int(substeps), int(iterations), fetch, sync))
+
+    def download_positions(self) -> np.ndarray:
+        out = self._positions_out
+        self._check(self._lib.ssbl_download_positions(self._handle, _fp(out), out.size))
+        return out
+
+    def diagnostics(self) -> dict:
+        raw = NativeDiagnostics()
+        self._check(self._lib.ssbl_get_diagnostics(self._handle, ctypes.byref(raw)))
+        return {name: getattr(raw, name) for name, _ in NativeDiagnostics._fields_}
+
+    # ---- GB300 extensions -------------------------------------------------
+    def build_self_structures(self) -> None:
+        self._check(self._lib.xpbd_gb300_build_self_structures(self._handle))
+
+    def read_buffer(self, buffer_id: int, dtype, count: int) -> np.ndarray:
+        out = np.empty(count, dtype=dtype)
+        n = self._lib.xpbd_gb300_read_buffer(self._handle, int(buffer_id), out.ctypes.data, out.nbytes)
+        if n < 0:
+            raise NativeSolverError(_last_error(self._lib))
+        return out[: n // out.itemsize]
+
+    def hash_info(self) -> np.ndarray:
+        out = np.zeros(6, np.int32)
+        self._check(self._lib.xpbd_gb300_hash_info(self._handle, _ip(out)))
+        return out
+
+    def set_graph_capture(self, enabled: bool) -> None:
+        self._check(self._lib.xpbd_gb300_set_graph_capture(self._handle, 1 if enabled else 0))
+
+    def last_step_launches(self) -> int:
+        return int(self._lib.xpbd_gb300_last_step_launches(self._handle))
+
+    def synchronize(self) -> None:
+        self._check(self._lib.xpbd_gb300_synchronize(self._handle))
+
+    def stream(self) -> int:
+        return int(self._lib.xpbd_gb300_stream(self._handle) or 0)
+
+    KERNEL_KINDS = ("predict", "stretch_pass", "vertex_pass", "bend_color", "vertex_hash", "triangle_hash",
+                    "edge_hash", "neighbors", "vertex_vertex", "vertex_triangle", "edge_edge", "island",
+                    "self_apply", "copy")
+
+    def profile_frame(self, substeps: int, iterations: int) -> dict:
+        n = len(self.KERNEL_KINDS)
+        ms = np.zeros(n, np.float32)
+        cnt = np.zeros(n, np.int64)
+        self._check(self._lib.xpbd_gb300_profile_frame(self._handle, int(substeps), int(iterations), _fp(ms),
+                                                        cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), n))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
