@@ -25,7 +25,6 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_NAME = "libssbl_xpbd_cuda_abi41.so"
-SOURCES = ["xpbd_abi.cu", "xpbd_step.cu", "xpbd_self.cu", "xpbd_sdf.cu", "xpbd_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3",
@@ -72,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     exe = nvcc()
     headers = _headers()
-    sources = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    sources = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
     objects = []
     jobs = []
     for src in sources:

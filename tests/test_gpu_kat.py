@@ -52,7 +52,7 @@ def test_gpu_sdf_diagnostics_and_rebuild(gpu_lib):
     d2 = gpu.diagnostics()
     assert d2["static_sdf_rebuild_count"] > r0 and d2["static_triangle_count"] == 12
     small = np.array([[-0.6, -0.6, 0.2], [0.6, -0.6, 0.2], [-0.6, 0.6, 0.2], [0.6, -0.6, 0.2], [0.6, 0.6, 0.2],
-                      [-0.6, 0.6, 0.2]], np.float32)
+                      [-0.6, 0.6, 0.2]], np.float32).reshape(2, 3, 3)
     gpu.update_static_triangles(small)
     d3 = gpu.diagnostics()
     assert d3["static_sdf_rebuild_count"] > d2["static_sdf_rebuild_count"] and d3["static_triangle_count"] == 2

@@ -92,11 +92,14 @@ def _sorted_buckets(start, ent):
 def test_hash_and_neighbor_tables_bit_exact(gpu_lib, oracle_lib):
     sc = scene.drop_scene(64, 1, seed=3)
     gpu, ora = _pair(sc, oracle_lib)
-    # crumple the cloth so buckets and neighbour lists are populated
+    # fold the cloth onto itself 1.2 mm apart so buckets and neighbour lists
+    # are populated by vertices that are far apart in the rest pose
     rng = np.random.default_rng(7)
     p = sc.cloth.positions_world.copy()
-    p[:, 2] = 0.5 + 0.004 * np.sin(p[:, 0] * 40.0) + rng.uniform(-1e-3, 1e-3, len(p)).astype(np.float32)
-    p[:, 0] *= 0.5
+    right = p[:, 0] > 0.0
+    p[right, 0] = -p[right, 0] + 0.001
+    p[right, 2] += 0.0012
+    p[:, :2] += rng.uniform(-2e-4, 2e-4, (len(p), 2)).astype(np.float32)
     p = p.astype(np.float32)
     gpu.update_positions(p)
     ora.update_positions(p)
