@@ -60,6 +60,24 @@ __attribute__((visibility("default"))) void* xpbd_gb300_stream(void* handle);
 __attribute__((visibility("default"))) int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations,
                                                                      float* kernel_ms, long long* kernel_launches, int kinds);
 
+/* No counterpart in the reference.  Vertex spatial hash that allocates no
+ * device memory, for callers that cannot call cudaMalloc / cudaFree (a host
+ * application whose pool owns all device memory, or a frame loop that cannot
+ * absorb the device synchronisation those calls may cause).  Inputs and
+ * outputs are the caller's device arrays: positions (x y z per vertex),
+ * bucket_start (bucket_count + 1 ints), bucket_entries (vertex_count ints),
+ * cells (4 ints per vertex, may be NULL).  bucket_count must be a power of
+ * two of at most 262144: the bucket counters live in a fixed 1 MiB array
+ * inside the library, one per device, kept until the process exits and
+ * shared by every call, so calls that overlap on the GPU race.  The first
+ * call on a device looks up that array's address; make it before any stream
+ * capture.  Work is queued on `stream` (cudaStream_t, NULL = default).
+ * Returns 1, or 0 with ssbl_last_error() set. */
+__attribute__((visibility("default"))) int xpbd_gb300_vertex_hash_noalloc(const float* positions, int vertex_count,
+                                                                           float cell_size, int bucket_count,
+                                                                           int* bucket_start, int* bucket_entries,
+                                                                           int* cells, void* stream);
+
 /* Wait for the solver's stream. */
 __attribute__((visibility("default"))) int xpbd_gb300_synchronize(void* handle);
 

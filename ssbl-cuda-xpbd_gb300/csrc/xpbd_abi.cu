@@ -717,6 +717,12 @@ Solver* as_solver(void* h) { return reinterpret_cast<Solver*>(h); }
 
 }  // namespace
 
+namespace xg {
+// Lets entry points defined in other translation units report through
+// ssbl_last_error().
+void set_last_error(const std::string& msg) { g_error = msg; }
+}  // namespace xg
+
 // ----------------------------------------------------------- C entry points
 
 extern "C" SSBL_API void* ssbl_create_solver(const SsblXpbdConfig* config, const SsblXpbdMesh* mesh) {

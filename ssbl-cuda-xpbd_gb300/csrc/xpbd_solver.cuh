@@ -16,6 +16,8 @@
 // inverse mass with the position, which the constraint kernels need together.
 #pragma once
 
+#include <string>
+
 #include "xpbd_math.cuh"
 
 namespace xg {
@@ -165,6 +167,9 @@ __device__ __forceinline__ void count_add(unsigned long long* counts, int slot, 
 }
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+
+// Set the message returned by ssbl_last_error() (defined in xpbd_abi.cu).
+void set_last_error(const std::string& msg);
 
 // ---- host launchers (defined in the .cu files) ----
 void launch_predict(const View& v, int V, float dt, cudaStream_t s);
