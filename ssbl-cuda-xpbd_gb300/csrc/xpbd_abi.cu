@@ -208,6 +208,7 @@ struct Solver {
     int *eb_count = nullptr, *eb_start = nullptr, *eb_ent = nullptr;
     int* nb_count = nullptr;
     int* nb_idx = nullptr;
+    int* scan_tmp = nullptr;
     Acc4* acc = nullptr;
 
     // dynamic colliders (accepted, see step)
@@ -261,6 +262,7 @@ struct Solver {
         v.eb_ent = eb_ent;
         v.nb_count = nb_count;
         v.nb_idx = nb_idx;
+        v.scan_tmp = scan_tmp;
         v.acc = acc;
         v.max_delta_bits = max_delta_bits;
         return v;
@@ -282,7 +284,7 @@ void free_solver(Solver* S) {
                     S->bend_rest, S->tris,     S->edges,      S->edge_rest, S->pin_target, S->pin_weight, S->pin_relax,
                     S->counts,    S->max_delta_bits, S->pack, S->sdf,      S->static_tris, S->vcell,    S->vb_count,
                     S->vb_start,  S->vb_ent,   S->tb_count,   S->tb_start, S->tb_ent,    S->eb_count,   S->eb_start,
-                    S->eb_ent,    S->nb_count, S->nb_idx,     S->acc};
+                    S->eb_ent,    S->nb_count, S->nb_idx,     S->acc,      S->scan_tmp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (S->stream) cudaStreamDestroy(S->stream);
@@ -600,19 +602,22 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 flush();
                 View sv = cur_view();
                 if (P.vhash)
-                    timed(kKVertexHash, 4, [&] {
+                    timed(kKVertexHash, 6, [&] {
                         cudaMemsetAsync(S->vb_count, 0, sizeof(int) * P.vbuckets, S->stream);
                         self_build_vertex_hash(sv, V, P.vbuckets, S->stream);
                     });
+                // strict queries with a 32-candidate budget do not depend on
+                // the order of buckets of <= 32 members
+                const bool order = fast || std::min(std::max(c.max_self_collision_neighbors, 1), 32) < 32;
                 if (P.thash)
-                    timed(kKTriangleHash, 4, [&] {
+                    timed(kKTriangleHash, 6, [&] {
                         cudaMemsetAsync(S->tb_count, 0, sizeof(int) * P.tbuckets, S->stream);
-                        self_build_triangle_hash(sv, T, P.tbuckets, S->stream);
+                        self_build_triangle_hash(sv, T, P.tbuckets, order, S->stream);
                     });
                 if (P.ehash)
-                    timed(kKEdgeHash, 4, [&] {
+                    timed(kKEdgeHash, 6, [&] {
                         cudaMemsetAsync(S->eb_count, 0, sizeof(int) * P.ebuckets, S->stream);
-                        self_build_edge_hash(sv, E, P.ebuckets, S->stream);
+                        self_build_edge_hash(sv, E, P.ebuckets, order, S->stream);
                     });
                 if (fast) {
                     timed(kKNeighbors, 1, [&] { self_neighbors(sv, V, P.vhash != 0, S->stream); });
@@ -621,9 +626,9 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 }
                 for (int pass = 0; pass < passes; ++pass) {
                     if (!fast) timed(kKNeighbors, 1, [&] { self_neighbors(sv, V, P.vhash != 0, S->stream); });
-                    timed(kKVertexVertex, 1, [&] { self_vv(sv, V, S->stream); });
-                    if (T > 0) timed(kKVertexTriangle, 1, [&] { self_vt(sv, V, P.thash != 0, S->stream); });
-                    if (E > 0) timed(kKEdgeEdge, 1, [&] { self_ee(sv, E, P.ehash != 0, S->stream); });
+                    timed(kKVertexVertex, 1, [&] { self_vv(sv, V, !fast, S->stream); });
+                    if (T > 0) timed(kKVertexTriangle, 1, [&] { self_vt(sv, V, P.thash != 0, !fast, S->stream); });
+                    if (E > 0) timed(kKEdgeEdge, 1, [&] { self_ee(sv, E, P.ehash != 0, !fast, S->stream); });
                     if (pass == passes - 1 && fast && T > 0 && P.thash) timed(kKIsland, 1, [&] { self_island(sv, V, S->stream); });
                     timed(kKSelfApply, 1, [&] { self_apply(sv, V, S->stream); });
                 }
@@ -872,7 +877,9 @@ extern "C" SSBL_API void* ssbl_create_solver(const SsblXpbdConfig* config, const
     if (ok && S->self_on && radius > 0.0f) {
         ok = dalloc(&S->nb_count, V, "self collision count allocation") &&
              dalloc(&S->nb_idx, (size_t)V * kNeighborSlots, "self collision index allocation") &&
-             dalloc(&S->acc, V, "self accumulation allocation");
+             dalloc(&S->acc, V, "self accumulation allocation") &&
+             dalloc(&S->scan_tmp, (size_t)std::max(std::max(P.vbuckets, P.tbuckets), P.ebuckets) / 4096 + 2,
+                    "bucket scan allocation");
         if (ok && P.vhash)
             ok = dalloc(&S->vcell, V, "self collision cell allocation") &&
                  dalloc(&S->vb_count, P.vbuckets, "self collision hash count allocation") &&
@@ -1131,11 +1138,11 @@ extern "C" __attribute__((visibility("default"))) int xpbd_gb300_build_self_stru
     }
     if (P.thash) {
         cudaMemsetAsync(S->tb_count, 0, sizeof(int) * P.tbuckets, S->stream);
-        self_build_triangle_hash(v, P.T, P.tbuckets, S->stream);
+        self_build_triangle_hash(v, P.T, P.tbuckets, true, S->stream);
     }
     if (P.ehash) {
         cudaMemsetAsync(S->eb_count, 0, sizeof(int) * P.ebuckets, S->stream);
-        self_build_edge_hash(v, P.E, P.ebuckets, S->stream);
+        self_build_edge_hash(v, P.E, P.ebuckets, true, S->stream);
     }
     self_neighbors(v, P.V, P.vhash != 0, S->stream);
     return (cuda_ok(cudaGetLastError(), "build self structures") && cuda_ok(cudaStreamSynchronize(S->stream), "build self structures")) ? 1 : 0;

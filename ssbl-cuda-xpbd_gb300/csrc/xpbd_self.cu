@@ -192,99 +192,150 @@ __global__ void k_vhash_scatter(View v) {
     v.vb_ent[atomicAdd(&v.vb_count[b], 1)] = i;
 }
 
-// `scatter` = false: count entries per bucket; true: write them.
+// Sixteen threads per primitive: thread c of primitive k handles cells c,
+// c + 16, ... of its cell box (at most 64 cells, z, y, x order).  `scatter`
+// = false counts entries per bucket; true writes them through the cursors
+// left by the scan.
+constexpr int kPrimLanes = 16;
+
 template <bool kTri>
-__global__ void k_prim_hash(View v, bool scatter) {
+__global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     const Params& P = *v.P;
     const int n = kTri ? P.T : P.E;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (int)(t / kPrimLanes), c0 = (int)(t % kPrimLanes);
     if (k >= n) return;
     bool ok = false;
-    CellRange r = kTri ? tri_cells(v, k, &ok, !scatter) : edge_cells(v, k, &ok, !scatter);
+    const CellRange r = kTri ? tri_cells(v, k, &ok, !scatter && c0 == 0) : edge_cells(v, k, &ok, !scatter && c0 == 0);
     if (!ok) return;
+    const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
+    if (nx <= 0 || ny <= 0 || nz <= 0) return;
+    const int cells = nx * ny * nz;
     int* cnt = kTri ? v.tb_count : v.eb_count;
     int* ent = kTri ? v.tb_ent : v.eb_ent;
     const int nb = kTri ? P.tbuckets : P.ebuckets;
-    for (int z = r.z0; z <= r.z1; ++z)
-        for (int y = r.y0; y <= r.y1; ++y)
-            for (int x = r.x0; x <= r.x1; ++x) {
-                const int b = (int)bucket_of(x, y, z, nb);
-                const int slot = atomicAdd(&cnt[b], 1);
-                if (scatter)
-                    ent[slot] = k;
-                else if (slot >= kBucketSlots)
-                    count1(v.counts, kCntSelfOverflow);
-            }
+    for (int c = c0; c < cells; c += kPrimLanes) {
+        const int x = r.x0 + c % nx, y = r.y0 + (c / nx) % ny, z = r.z0 + c / (nx * ny);
+        const int slot = atomicAdd(&cnt[(int)bucket_of(x, y, z, nb)], 1);
+        if (scatter)
+            ent[slot] = k;
+        else if (slot >= kBucketSlots)
+            count1(v.counts, kCntSelfOverflow);
+    }
 }
 
-// Exclusive scan of counts[0..n) into start[0..n]; counts is overwritten
-// with the starts so it can serve as the scatter cursor.  One block,
-// 4096-element tiles with a running carry.
-__global__ void __launch_bounds__(1024) k_scan(int* counts, int* start, int n) {
-    __shared__ int warp_sums[32];
-    __shared__ int carry_s;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) carry_s = 0;
+// Exclusive scan of counts[0..n) into start[0..n] in three launches: block
+// sums of 4096-count tiles, a scan of the block sums, then each tile's local
+// scan plus its offset.  counts is overwritten with the starts so it serves
+// as the scatter cursor.
+constexpr int kScanTile = 4096;
+
+__device__ __forceinline__ int block_exclusive_scan4(int (&vals)[4], int* warp_sums, int* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int local = vals[0] + vals[1] + vals[2] + vals[3];
+    int incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
     __syncthreads();
-    for (int base = 0; base < n; base += 4096) {
-        int vals[4];
-        int local = 0;
-        for (int k = 0; k < 4; ++k) {
-            const int idx = base + tid * 4 + k;
-            vals[k] = idx < n ? counts[idx] : 0;
-            local += vals[k];
-        }
-        int incl = local;
+    if (wid == 0) {
+        int w = lane < nw ? warp_sums[lane] : 0;
         for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+            const int t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
         }
-        if (lane == 31) warp_sums[wid] = incl;
-        __syncthreads();
-        if (wid == 0) {
-            int w = warp_sums[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += t;
-            }
-            warp_sums[lane] = w;
-        }
-        __syncthreads();
-        const int carry = carry_s;
-        int run = carry + (wid > 0 ? warp_sums[wid - 1] : 0) + incl - local;
+        if (lane < nw) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    *total = warp_sums[nw - 1];
+    const int before = (wid > 0 ? warp_sums[wid - 1] : 0) + incl - local;
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_reduce(const int* counts, int n, int* block_sums) {
+    __shared__ int ws[32];
+    int vals[4];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
+    for (int k = 0; k < 4; ++k) vals[k] = base + k < n ? counts[base + k] : 0;
+    int total;
+    block_exclusive_scan4(vals, ws, &total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of the block sums in place (one block, any count).
+__global__ void __launch_bounds__(1024) k_scan_sums(int* sums, int n) {
+    __shared__ int ws[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += kScanTile) {
+        int vals[4];
+        const int i0 = base + threadIdx.x * 4;
+        for (int k = 0; k < 4; ++k) vals[k] = i0 + k < n ? sums[i0 + k] : 0;
+        int total;
+        int run = carry + block_exclusive_scan4(vals, ws, &total);
         for (int k = 0; k < 4; ++k) {
-            const int idx = base + tid * 4 + k;
-            if (idx < n) {
-                start[idx] = run;
-                counts[idx] = run;
-            }
+            if (i0 + k < n) sums[i0 + k] = run;
             run += vals[k];
         }
         __syncthreads();
-        if (tid == 1023) carry_s = run;
+        if (threadIdx.x == 0) carry += total;
         __syncthreads();
     }
-    if (tid == 0) start[n] = carry_s;
 }
 
-// Order each bucket's members: full insertion sort up to 32 members, else a
-// selection of the 32 smallest ids to the front (queries read no further).
-__global__ void k_bucket_sort(const int* start, int* ent, int nbuckets) {
+__global__ void __launch_bounds__(1024) k_scan_down(int* counts, int* start, int n, const int* block_offsets) {
+    __shared__ int ws[32];
+    int vals[4];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
+    for (int k = 0; k < 4; ++k) vals[k] = base + k < n ? counts[base + k] : 0;
+    int total;
+    int run = block_offsets[blockIdx.x] + block_exclusive_scan4(vals, ws, &total);
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) {
+            start[base + k] = run;
+            counts[base + k] = run;
+        }
+        run += vals[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) start[n] = run;
+}
+
+void scan_counts(int* counts, int* start, int n, int* block_sums, cudaStream_t s) {
+    const int blocks = (n + kScanTile - 1) / kScanTile;
+    k_scan_reduce<<<blocks, 1024, 0, s>>>(counts, n, block_sums);
+    k_scan_sums<<<1, 1024, 0, s>>>(block_sums, blocks);
+    k_scan_down<<<blocks, 1024, 0, s>>>(counts, start, n, block_sums);
+}
+
+// Order each bucket's members: buckets of up to 32 are copied to a local
+// array, insertion-sorted and written back; larger ones get the 32 smallest
+// ids moved to the front in order (queries read no further).
+// With `full` = false buckets of up to 32 members keep their scatter order:
+// a strict-mode query with a 32-candidate budget reads all of them and sums
+// their pushes in fixed point, so their order cannot change the result.
+__global__ void k_bucket_sort(const int* start, int* ent, int nbuckets, bool full) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbuckets) return;
     const int s = start[b], n = start[b + 1] - s;
     int* e = ent + s;
     if (n <= 1) return;
     if (n <= kBucketSlots) {
-        for (int i = 1; i < n; ++i) {
+        if (!full) return;
+        int tmp[kBucketSlots];
+        for (int i = 0; i < n; ++i) {
             const int key = e[i];
             int j = i - 1;
-            while (j >= 0 && e[j] > key) {
-                e[j + 1] = e[j];
+            while (j >= 0 && tmp[j] > key) {
+                tmp[j + 1] = tmp[j];
                 --j;
             }
-            e[j + 1] = key;
+            tmp[j + 1] = key;
         }
+        for (int i = 0; i < n; ++i) e[i] = tmp[i];
         return;
     }
     for (int i = 0; i < kBucketSlots; ++i) {
@@ -725,6 +776,370 @@ __global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
     }
 }
 
+// ------------------------------------------- warp-per-item strict queries --
+// Strict mode has no order-dependent filter, so each candidate can be tested
+// by its own lane: one warp per vertex (or edge), one lane per cell or
+// candidate slot.  Lane order equals the reference loop order, a ballot
+// prefix gives each accepted candidate its rank, and the neighbour budget
+// keeps the first `budget` accepted candidates exactly as the serial loop
+// does.  Fixed-point sums make the accumulation order irrelevant.
+
+__device__ __forceinline__ int warp_global_id() { return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); }
+
+__device__ __forceinline__ int warp_exclusive_sum(int v, int lane) {
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    return incl - v;
+}
+
+__device__ __forceinline__ long long warp_sum64(long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// VV neighbour table: lane l < 27 scans cell (dz, dy, dx) = (l/9-1, l/3%3-1,
+// l%3-1), the reference's nested-loop order (abi41.cu:4756-4781).
+__global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v) {
+    const Params& P = *v.P;
+    const int src = warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if (src >= P.V) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) {
+        if (lane == 0) v.nb_count[src] = 0;
+        return;
+    }
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const float4 p = v.pos[src];
+    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
+    int found[kNeighborSlots];
+    int nfound = 0;
+    if (lane < 27) {
+        const int qx = cx + lane % 3 - 1, qy = cy + (lane / 3) % 3 - 1, qz = cz + lane / 9 - 1;
+        const int b = (int)bucket_of(qx, qy, qz, P.vbuckets);
+        const int st = v.vb_start[b];
+        const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
+        for (int k = 0; k < lim; ++k) {
+            const int other = v.vb_ent[st + k];
+            const int4 oc = v.vcell[other];
+            if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
+            found[nfound++] = other;
+        }
+    }
+    const int offset = warp_exclusive_sum(nfound, lane);
+    const int total = __shfl_sync(0xffffffffu, offset + nfound, 31);
+    for (int k = 0; k < nfound && offset + k < kNeighborSlots; ++k) v.nb_idx[src * kNeighborSlots + offset + k] = found[k];
+    if (lane == 0) {
+        if (total >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
+        v.nb_count[src] = min(total, kNeighborSlots);
+    }
+}
+
+// VV responses (strict): lane n handles neighbour n of the source vertex.
+__global__ void __launch_bounds__(kThreads) k_vv_warp(View v) {
+    const Params& P = *v.P;
+    const int src = warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if (src >= P.V) return;
+    if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
+    const int count = min(v.nb_count[src], kNeighborSlots);
+    if (count == 0) return;
+    long long ax = 0, ay = 0, az = 0;
+    int candidate = 0, contact = 0;
+    if (lane < count) {
+        const int other = v.nb_idx[src * kNeighborSlots + lane];
+        if (other >= 0 && other < P.V && other != src) {
+            candidate = 1;
+            const F3 pc = f3(v.pos[src]), pp = f3(v.prev[src]);
+            const float target = contact_radius(P);
+            const float th = target * 0.5f + target * 0.5f;
+            const F3 qc = f3(v.pos[other]), qp = f3(v.prev[other]);
+            if (th > 0.0f) {
+                const float scale = !(__ldg(&v.inv_mass[other]) > 0.0f) ? 1.0f : 0.5f;
+                F3 resp{0.0f, 0.0f, 0.0f};
+                bool hit = false;
+                const F3 d_ref = pp - qp;
+                const float cc = dot3(d_ref, d_ref) - th * th;
+                const F3 rel = (pc - pp) - (qc - qp);
+                const float a = dot3(rel, rel), b = dot3(d_ref, rel);
+                if (cc >= 0.0f && b < 0.0f && a > 1.0e-5f) {
+                    const float disc = b * b - a * cc;
+                    if (disc >= 0.0f) {
+                        const float t = (-b - sqrtf(disc)) / a;
+                        if (t > 0.0f && t <= 1.0f) {
+                            const float sg = 1.0f - t;
+                            const F3 ph = pp * sg + pc * t, qh = qp * sg + qc * t;
+                            F3 nrm = ph - qh;
+                            const float nl = dot3(nrm, nrm);
+                            if (nl > kEps) {
+                                nrm = nrm * (1.0f / sqrtf(nl));
+                                const float vn = dot3((pc - ph) - (qc - qh), nrm);
+                                if (vn > 0.0f) {
+                                    resp = nrm * (-vn * scale);
+                                    hit = true;
+                                }
+                            }
+                        }
+                    }
+                }
+                bool skip = false;
+                if (!hit) {
+                    const F3 delta = pc - qc;
+                    const float dsq = dot3(delta, delta);
+                    if (dsq >= th * th) {
+                        skip = true;
+                    } else {
+                        F3 nrm{0.0f, 0.0f, 1.0f};
+                        float dist = sqrtf(fmaxf(dsq, kEps));
+                        if (dsq > kEps) {
+                            nrm = delta * (1.0f / dist);
+                        } else {
+                            const F3 rd = f3(ld4(&v.rest[src])) - f3(ld4(&v.rest[other]));
+                            const float rl = dot3(rd, rd);
+                            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+                            dist = 0.0f;
+                        }
+                        resp = nrm * fminf((th - dist) * scale, th * 0.35f);
+                        hit = true;
+                    }
+                }
+                if (!skip && hit && dot3(resp, resp) > kEps) {
+                    const float max_len = fmaxf(th * 0.35f, 1.0e-4f);
+                    const float rl = len3(resp);
+                    if (rl > max_len) resp = resp * (max_len / rl);
+                    ax = to_fix(resp.x);
+                    ay = to_fix(resp.y);
+                    az = to_fix(resp.z);
+                    contact = 1;
+                }
+            }
+        }
+    }
+    const unsigned cand_mask = __ballot_sync(0xffffffffu, candidate);
+    const unsigned hit_mask = __ballot_sync(0xffffffffu, contact);
+    ax = warp_sum64(ax);
+    ay = warp_sum64(ay);
+    az = warp_sum64(az);
+    if (lane == 0) {
+        if (cand_mask) count_add(v.counts, kCntSelfCandidates, __popc(cand_mask));
+        if (hit_mask) {
+            count_add(v.counts, kCntExactImpulseContacts, __popc(hit_mask));
+            unsigned long long* acc = reinterpret_cast<unsigned long long*>(&v.acc[src]);
+            atomicAdd(acc + 0, (unsigned long long)ax);
+            atomicAdd(acc + 1, (unsigned long long)ay);
+            atomicAdd(acc + 2, (unsigned long long)az);
+            atomicAdd(acc + 3, (unsigned long long)__popc(hit_mask));
+        }
+    }
+}
+
+// A soft push of up to four vertices decided by one lane, applied after the
+// budget check.
+struct SoftPush {
+    F3 delta;
+    int idx[4];
+    float w[4];
+    bool apply;  // push > 0 and total > 0
+};
+
+// Strict-mode vertex-triangle pair up to the accept decision
+// (abi41.cu:4990-5107 without the fast-mode filter).  The current-distance
+// test runs before the rest-pose test: both only reject, and strict mode
+// counts neither, so the outcome is the same.
+__device__ bool vt_eval(const View& v, int vertex, int tri, float target, float onset, SoftPush* out) {
+    const Params& P = *v.P;
+    if (tri < 0 || tri >= P.T) return false;
+    const int4 t = __ldg(&v.tris[tri]);
+    if (!tri_valid(P, t)) return false;
+    if (vertex == t.x || vertex == t.y || vertex == t.z) return false;
+    const F3 p = f3(v.pos[vertex]), a = f3(v.pos[t.x]), b = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
+    const F3 q = closest_on_triangle(p, a, b, c);
+    const F3 d = p - q;
+    const float dsq = dot3(d, d);
+    float dist = sqrtf(fmaxf(dsq, kEps));
+    if (dist >= onset) return false;
+    if (rest_vt_neighbor(v, vertex, t, target, onset)) return false;
+    F3 nrm{0.0f, 0.0f, 1.0f};
+    if (dsq > kEps) {
+        nrm = d * (1.0f / dist);
+    } else {
+        nrm = cross3(b - a, c - a);
+        const float nl = dot3(nrm, nrm);
+        if (nl > kEps) {
+            nrm = nrm * (1.0f / sqrtf(nl));
+        } else {
+            const F3 rv = f3(ld4(&v.rest[vertex]));
+            const F3 rd = rv - closest_on_triangle(rv, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])), f3(ld4(&v.rest[t.z])));
+            const float rl = dot3(rd, rd);
+            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+        }
+        dist = 0.0f;
+    }
+    float wa, wb, wc;
+    barycentric(q, a, b, c, &wa, &wb, &wc);
+    const float pen = target - dist;
+    float push;
+    if (pen > 0.0f) {
+        push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    } else {
+        const float x = 1.0f - fminf(dist / onset, 1.0f);
+        push = fminf(x * x * target * 0.06f, target * 0.04f);
+    }
+    const float wv = __ldg(&v.inv_mass[vertex]);
+    const float wta = __ldg(&v.inv_mass[t.x]) * wa, wtb = __ldg(&v.inv_mass[t.y]) * wb, wtc = __ldg(&v.inv_mass[t.z]) * wc;
+    const float total = wv + wta + wtb + wtc;
+    out->apply = push > 0.0f && total > 0.0f;
+    if (out->apply) {
+        out->delta = nrm * (push / total);
+        out->idx[0] = vertex;
+        out->idx[1] = t.x;
+        out->idx[2] = t.y;
+        out->idx[3] = t.z;
+        out->w[0] = wv;
+        out->w[1] = -wta;
+        out->w[2] = -wtb;
+        out->w[3] = -wtc;
+    }
+    return true;
+}
+
+// Strict-mode edge-edge pair up to the accept decision (abi41.cu:5595-5722
+// without the fast-mode filter; current distance tested before the rest
+// pose, as above).
+__device__ bool ee_eval(const View& v, int ia, int ib, float target, float onset, SoftPush* out) {
+    const Params& P = *v.P;
+    if (ib <= ia || ia < 0 || ib < 0 || ia >= P.E || ib >= P.E) return false;
+    const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
+    if (!edge_valid(P, ea) || !edge_valid(P, eb)) return false;
+    if (ea.x == eb.x || ea.x == eb.y || ea.y == eb.x || ea.y == eb.y) return false;
+    const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
+    float s, t;
+    segment_params(a0, a1, b0, b1, &s, &t);
+    const F3 pa = a0 + (a1 - a0) * s;
+    const F3 pb = b0 + (b1 - b0) * t;
+    const F3 d = pa - pb;
+    const float dsq = dot3(d, d);
+    float dist = sqrtf(fmaxf(dsq, kEps));
+    if (dist >= onset) return false;
+    if (rest_ee_neighbor(v, ea, eb, target, onset)) return false;
+    F3 nrm{0.0f, 0.0f, 1.0f};
+    if (dsq > kEps) {
+        nrm = d * (1.0f / dist);
+    } else {
+        nrm = cross3(a1 - a0, b1 - b0);
+        const float nl = dot3(nrm, nrm);
+        if (nl > kEps) {
+            nrm = nrm * (1.0f / sqrtf(nl));
+        } else {
+            const F3 r0 = f3(ld4(&v.rest[ea.x])), r1 = f3(ld4(&v.rest[ea.y]));
+            const F3 r2 = f3(ld4(&v.rest[eb.x])), r3 = f3(ld4(&v.rest[eb.y]));
+            float rs, rt;
+            segment_params(r0, r1, r2, r3, &rs, &rt);
+            const F3 rd = (r0 + (r1 - r0) * rs) - (r2 + (r3 - r2) * rt);
+            const float rl = dot3(rd, rd);
+            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+        }
+        dist = 0.0f;
+    }
+    const float pen = target - dist;
+    float push;
+    if (pen > 0.0f) {
+        push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    } else {
+        const float x = 1.0f - fminf(dist / onset, 1.0f);
+        push = fminf(x * x * target * 0.06f, target * 0.04f);
+    }
+    const float ma0 = __ldg(&v.inv_mass[ea.x]), ma1 = __ldg(&v.inv_mass[ea.y]);
+    const float mb0 = __ldg(&v.inv_mass[eb.x]), mb1 = __ldg(&v.inv_mass[eb.y]);
+    const float ws0 = 1.0f - s, ws1 = s, wt0 = 1.0f - t, wt1 = t;
+    const float total = ma0 * ws0 * ws0 + ma1 * ws1 * ws1 + mb0 * wt0 * wt0 + mb1 * wt1 * wt1;
+    out->apply = push > 0.0f && total > 0.0f;
+    if (out->apply) {
+        out->delta = nrm * (push / total);
+        out->idx[0] = ea.x;
+        out->idx[1] = ea.y;
+        out->idx[2] = eb.x;
+        out->idx[3] = eb.y;
+        out->w[0] = ma0 * ws0;
+        out->w[1] = ma1 * ws1;
+        out->w[2] = -(mb0 * wt0);
+        out->w[3] = -(mb1 * wt1);
+    }
+    return true;
+}
+
+// Commit the accepted pairs within the budget: candidate counter for each,
+// and the push for those that have one.
+__device__ __forceinline__ void commit_pushes(const View& v, bool accepted, const SoftPush& sp, int budget, int lane,
+                                              int contact_slot) {
+    const unsigned acc_mask = __ballot_sync(0xffffffffu, accepted);
+    const int rank = __popc(acc_mask & ((1u << lane) - 1u));
+    const bool take = accepted && rank < budget;
+    const bool push = take && sp.apply;
+    const unsigned take_mask = __ballot_sync(0xffffffffu, take);
+    const unsigned push_mask = __ballot_sync(0xffffffffu, push);
+    if (lane == 0) {
+        if (take_mask) count_add(v.counts, kCntSelfCandidates, __popc(take_mask));
+        if (push_mask) count_add(v.counts, contact_slot, __popc(push_mask));
+    }
+    if (push) {
+        for (int k = 0; k < 4; ++k) {
+            // the reference skips a vertex whose share is not positive (w > 0,
+            // or -w > 0 for the far side); the sign was folded into w
+            const float w = sp.w[k];
+            const bool far = (contact_slot == kCntSoftContacts) ? (k > 0) : (k > 1);
+            if ((far ? -w : w) > 0.0f) accumulate(v, sp.idx[k], sp.delta * w);
+        }
+    }
+}
+
+// Strict VT: one warp per vertex, lane k = slot k of the vertex's own cell
+// bucket (abi41.cu:5129-5143).
+__global__ void __launch_bounds__(kThreads) k_vt_warp(View v) {
+    const Params& P = *v.P;
+    const int vertex = warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if (vertex >= P.V) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const float4 p = v.pos[vertex];
+    const int b = (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
+    const int st = v.tb_start[b];
+    const int lim = min(v.tb_start[b + 1] - st, kBucketSlots);
+    if (lim == 0) return;
+    SoftPush sp;
+    sp.apply = false;
+    const bool accepted = lane < lim && vt_eval(v, vertex, v.tb_ent[st + lane], target, onset, &sp);
+    commit_pushes(v, accepted, sp, neighbor_budget(P), lane, kCntSoftContacts);
+}
+
+// Strict EE: one warp per edge, lane k = slot k of the midpoint's cell
+// bucket (abi41.cu:5724-5758).
+__global__ void __launch_bounds__(kThreads) k_ee_warp(View v) {
+    const Params& P = *v.P;
+    const int e = warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if (e >= P.E) return;
+    const int2 ed = __ldg(&v.edges[e]);
+    if (!edge_valid(P, ed)) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) return;
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
+    const int b = (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
+    const int st = v.eb_start[b];
+    const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
+    if (lim == 0) return;
+    SoftPush sp;
+    sp.apply = false;
+    const bool accepted = lane < lim && ee_eval(v, e, v.eb_ent[st + lane], target, onset, &sp);
+    commit_pushes(v, accepted, sp, neighbor_budget(P), lane, kCntEdgeEdgeContacts);
+}
+
 // ------------------------------------------------- fast overlap islands --
 // Fast mode, final pass: aggregate push for a vertex buried in >= 3 nearby
 // triangles of the 27-cell neighbourhood (abi41.cu:5226-5439).
@@ -881,53 +1296,60 @@ __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
 struct SelfLaunch {
     static void vhash(const View& v, int V, int nb, cudaStream_t s) {
         k_vhash_count<<<blocks_for(V), kThreads, 0, s>>>(v);
-        k_scan<<<1, 1024, 0, s>>>(v.vb_count, v.vb_start, nb);
+        scan_counts(v.vb_count, v.vb_start, nb, v.scan_tmp, s);
         k_vhash_scatter<<<blocks_for(V), kThreads, 0, s>>>(v);
-        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.vb_start, v.vb_ent, nb);
+        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.vb_start, v.vb_ent, nb, true);
     }
-    static void thash(const View& v, int T, int nb, cudaStream_t s) {
-        k_prim_hash<true><<<blocks_for(T), kThreads, 0, s>>>(v, false);
-        k_scan<<<1, 1024, 0, s>>>(v.tb_count, v.tb_start, nb);
-        k_prim_hash<true><<<blocks_for(T), kThreads, 0, s>>>(v, true);
-        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.tb_start, v.tb_ent, nb);
-    }
-    static void ehash(const View& v, int E, int nb, cudaStream_t s) {
-        k_prim_hash<false><<<blocks_for(E), kThreads, 0, s>>>(v, false);
-        k_scan<<<1, 1024, 0, s>>>(v.eb_count, v.eb_start, nb);
-        k_prim_hash<false><<<blocks_for(E), kThreads, 0, s>>>(v, true);
-        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.eb_start, v.eb_ent, nb);
+    template <bool kTri>
+    static void phash(const View& v, int n, int* count, int* start, int* ent, int nb, bool order, cudaStream_t s) {
+        const long long threads = (long long)n * kPrimLanes;
+        const int blocks = (int)((threads + kThreads - 1) / kThreads);
+        k_prim_hash<kTri><<<blocks, kThreads, 0, s>>>(v, false);
+        scan_counts(count, start, nb, v.scan_tmp, s);
+        k_prim_hash<kTri><<<blocks, kThreads, 0, s>>>(v, true);
+        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(start, ent, nb, order);
     }
 };
 
 void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s) {
     if (V > 0) SelfLaunch::vhash(v, V, nb, s);
 }
-void self_build_triangle_hash(const View& v, int T, int nb, cudaStream_t s) {
-    if (T > 0) SelfLaunch::thash(v, T, nb, s);
+void self_build_triangle_hash(const View& v, int T, int nb, bool order, cudaStream_t s) {
+    if (T > 0) SelfLaunch::phash<true>(v, T, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
 }
-void self_build_edge_hash(const View& v, int E, int nb, cudaStream_t s) {
-    if (E > 0) SelfLaunch::ehash(v, E, nb, s);
+void self_build_edge_hash(const View& v, int E, int nb, bool order, cudaStream_t s) {
+    if (E > 0) SelfLaunch::phash<false>(v, E, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
 }
+inline int warp_blocks(long long items) { return (int)((items * 32 + kThreads - 1) / kThreads); }
+
 void self_neighbors(const View& v, int V, bool hashed, cudaStream_t s) {
     if (V <= 0) return;
     if (hashed)
-        k_neighbors_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
+        k_neighbors_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
     else
         k_neighbors_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
 }
-void self_vv(const View& v, int V, cudaStream_t s) {
-    if (V > 0) k_vv<<<blocks_for(V), kThreads, 0, s>>>(v);
-}
-void self_vt(const View& v, int V, bool hashed, cudaStream_t s) {
+void self_vv(const View& v, int V, bool strict, cudaStream_t s) {
     if (V <= 0) return;
-    if (hashed)
+    if (strict)
+        k_vv_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
+    else
+        k_vv<<<blocks_for(V), kThreads, 0, s>>>(v);
+}
+void self_vt(const View& v, int V, bool hashed, bool strict, cudaStream_t s) {
+    if (V <= 0) return;
+    if (hashed && strict)
+        k_vt_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
+    else if (hashed)
         k_vt_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
     else
         k_vt_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
 }
-void self_ee(const View& v, int E, bool hashed, cudaStream_t s) {
+void self_ee(const View& v, int E, bool hashed, bool strict, cudaStream_t s) {
     if (E <= 0) return;
-    if (hashed)
+    if (hashed && strict)
+        k_ee_warp<<<warp_blocks(E), kThreads, 0, s>>>(v);
+    else if (hashed)
         k_ee_hash<<<blocks_for(E), kThreads, 0, s>>>(v);
     else
         k_ee_brute<<<blocks_for(E), kThreads, 0, s>>>(v);

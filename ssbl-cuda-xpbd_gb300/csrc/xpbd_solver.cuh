@@ -147,6 +147,7 @@ struct View {
     int* eb_count;
     int* eb_start;
     int* eb_ent;
+    int* scan_tmp;          // block sums of the bucket scans
     int tb_capacity, eb_capacity;
     int* nb_count;          // [V]
     int* nb_idx;            // [V * 32]
@@ -192,12 +193,15 @@ void launch_sdf_build(const View& v, int voxels, cudaStream_t s);
 
 // self collision (bucket counts must be zeroed before each hash build)
 void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s);
-void self_build_triangle_hash(const View& v, int T, int nb, cudaStream_t s);
-void self_build_edge_hash(const View& v, int E, int nb, cudaStream_t s);
+// `order` = false leaves buckets of <= 32 members in scatter order (valid
+// only for strict queries with a 32-candidate budget)
+void self_build_triangle_hash(const View& v, int T, int nb, bool order, cudaStream_t s);
+void self_build_edge_hash(const View& v, int E, int nb, bool order, cudaStream_t s);
 void self_neighbors(const View& v, int V, bool hashed, cudaStream_t s);
-void self_vv(const View& v, int V, cudaStream_t s);
-void self_vt(const View& v, int V, bool hashed, cudaStream_t s);
-void self_ee(const View& v, int E, bool hashed, cudaStream_t s);
+// `strict` selects the warp-per-item kernels (no order-dependent filters)
+void self_vv(const View& v, int V, bool strict, cudaStream_t s);
+void self_vt(const View& v, int V, bool hashed, bool strict, cudaStream_t s);
+void self_ee(const View& v, int E, bool hashed, bool strict, cudaStream_t s);
 void self_island(const View& v, int V, cudaStream_t s);
 void self_apply(const View& v, int V, cudaStream_t s);
 
