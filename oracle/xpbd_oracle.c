@@ -160,8 +160,15 @@ struct OracleSolver {
     long long* acc;
     unsigned long long counts[N_COUNTS];
     float max_delta;
+    /* hard-stretch optimisation */
+    int pcg_on; float strength;
+    float *diag, *pinv; V3 *r, *z, *d, *q; float* off; /* off: 4 floats per stretch-CSR entry */
+    V3* avg_sum; float* avg_cnt;
+    float red[8]; unsigned long long pcg_guard; float pcg_max_delta;
+    int* cap_edges; float* cap_rest; int* cap_colors; int n_cap_colors;
 };
 
+enum { R_DAD = 0, R_RZ = 1, R_RZN = 2, R_STATUS = 3, R_INIT = 4, R_ITER = 5 };
 static void cnt(OracleSolver* s, int slot) {
 #pragma omp atomic
     s->counts[slot] += 1ull;
@@ -1270,13 +1277,355 @@ static void self_collision(OracleSolver* s) {
     }
 }
 
+
+/* ------------------------------------------------ hard-stretch solve -- */
+typedef struct { float m11, m12, m13, m22, m23, m33; } Sym;
+static Sym sym_ld(const float* a, int i) { const float* m = a + 6 * (size_t)i; Sym r = {m[0], m[1], m[2], m[3], m[4], m[5]}; return r; }
+static void sym_st(float* a, int i, Sym m) { float* o = a + 6 * (size_t)i; o[0] = m.m11; o[1] = m.m12; o[2] = m.m13; o[3] = m.m22; o[4] = m.m23; o[5] = m.m33; }
+/* abi41.cu:1125-1131 */
+static V3 sym_madd(Sym m, V3 v, V3 a) {
+    return v3(fmaf(m.m13, v.z, fmaf(m.m12, v.y, fmaf(m.m11, v.x, a.x))), fmaf(m.m23, v.z, fmaf(m.m22, v.y, fmaf(m.m12, v.x, a.y))),
+              fmaf(m.m33, v.z, fmaf(m.m23, v.y, fmaf(m.m13, v.x, a.z))));
+}
+static Sym sym_outer(V3 n, float s) { Sym r = {n.x * n.x * s, n.x * n.y * s, n.x * n.z * s, n.y * n.y * s, n.y * n.z * s, n.z * n.z * s}; return r; }
+static Sym sym_add(Sym a, Sym b) { Sym r = {a.m11 + b.m11, a.m12 + b.m12, a.m13 + b.m13, a.m22 + b.m22, a.m23 + b.m23, a.m33 + b.m33}; return r; }
+/* abi41.cu:1158-1189 */
+static Sym sym_inv(OracleSolver* s, Sym m) {
+    float a = m.m11, b = m.m12, c = m.m13, d = m.m22, e = m.m23, f = m.m33;
+    float df_ee = fmaf(d, f, -e * e), bf_ce = fmaf(b, f, -c * e), be_cd = fmaf(b, e, -c * d);
+    float det = fmaf(c, be_cd, fmaf(-b, bf_ce, a * df_ee));
+    if (isfinite(det) && fabsf(det) > 1.0e-12f) {
+        float inv = 1.0f / det;
+        Sym r = {df_ee * inv, fmaf(c, e, -b * f) * inv, be_cd * inv, fmaf(a, f, -c * c) * inv, fmaf(b, c, -a * e) * inv, fmaf(a, d, -b * b) * inv};
+        return r;
+    }
+#pragma omp atomic
+    s->pcg_guard += 1;
+    Sym r = {1.0f / fmaxf(fabsf(a), 1.0e-4f), 0, 0, 1.0f / fmaxf(fabsf(d), 1.0e-4f), 0, 1.0f / fmaxf(fabsf(f), 1.0e-4f)};
+    return r;
+}
+/* abi41.cu:1070-1104 */
+static float proj_limit(const OracleSolver* s, float rest) {
+    float th = s->cfg.cloth_thickness;
+    float base = fmaxf(1.0e-5f, fminf(fmaxf(rest, th) * 0.5f, 0.25f));
+    if (s->strength < 0.95f || !isfinite(th) || th <= K_EPS) return base;
+    return fminf(base, fmaxf(1.0e-5f, fminf(fmaxf(rest * 0.18f, th * 0.06f), 0.0035f)));
+}
+static float writeback_limit(const OracleSolver* s) {
+    float th = s->cfg.cloth_thickness;
+    if (s->strength < 0.95f || !isfinite(th) || th <= K_EPS) return 0.25f;
+    return fmaxf(2.5e-4f, fminf(th * 0.035f, 9.0e-4f));
+}
+
+/* Sum of per-vertex values in the GPU's fixed order: a shuffle-down tree
+ * per 32-vertex warp over a grid of ceil(V / 256) * 256 threads, then lane l
+ * adds warp partials l, l + 32, ... and a final shuffle-down tree. */
+static float warp_tree32(const float* x) {
+    float a[32];
+    memcpy(a, x, sizeof(a));
+    for (int o = 16; o > 0; o >>= 1) {
+        float b[32];
+        for (int l = 0; l < 32; ++l) b[l] = a[l] + (l + o < 32 ? a[l + o] : a[l]);
+        memcpy(a, b, sizeof(a));
+    }
+    return a[0];
+}
+static float fixed_sum(const float* vals, int V) {
+    int nw = ((V + 255) / 256) * 8;
+    float* part = (float*)calloc((size_t)nw + 1, sizeof(float));
+    for (int w = 0; w < nw; ++w) {
+        float x[32];
+        for (int l = 0; l < 32; ++l) { int i = w * 32 + l; x[l] = i < V ? vals[i] : 0.0f; }
+        part[w] = warp_tree32(x);
+    }
+    float lanes[32];
+    for (int l = 0; l < 32; ++l) { float acc = 0.0f; for (int k = l; k < nw; k += 32) acc += part[k]; lanes[l] = acc; }
+    free(part);
+    return warp_tree32(lanes);
+}
+
+/* Assembly (abi41.cu:3085-3186) gathered per vertex in edge order, with
+ * the preconditioner and initial residual (abi41.cu:3188-3226). */
+static void pcg_build(OracleSolver* s, float* tmp) {
+    const float strength = clamp01(s->strength * 2.5f);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s->V; ++i) {
+        Sym dg = {1, 0, 0, 1, 0, 1};
+        V3 rhs = v3(0, 0, 0);
+        for (int k = s->sp_off[i]; k < s->sp_off[i + 1]; ++k) {
+            int o = s->sp_other[k], is_j = s->sp_side[k];
+            int a = is_j ? o : i, b = is_j ? i : o;
+            float wi = s->w[a], wj = s->w[b], weight = wi + wj, rest = s->sp_rest[k];
+            int ai = wi > 0.0f, aj = wj > 0.0f;
+            float* off = s->off + 4 * (size_t)k;
+            off[0] = off[1] = off[2] = off[3] = 0.0f;
+            V3 pi = s->pos[a], pj = s->pos[b];
+            if (!(isfinite(weight) && weight > 0.0f && isfinite(rest) && rest > K_EPS && vfinite(pi) && vfinite(pj))) continue;
+            V3 delta = vsub(pj, pi);
+            float lsq = vdot(delta, delta);
+            if (!isfinite(lsq) || lsq <= K_EPS) continue;
+            float len = sqrtf(lsq), err = len - rest;
+            if (!isfinite(err) || fabsf(err) <= 1.0e-6f || strength <= 0.0f) continue;
+            float lim = proj_limit(s, rest);
+            float projected = fmaxf(-lim, fminf(err * strength, lim));
+            if (!isfinite(projected) || fabsf(projected) <= 1.0e-7f) continue;
+            V3 n = vmul(delta, 1.0f / len);
+            V3 desired = vmul(n, projected / weight);
+            float stiff = fmaxf(strength, 1.0e-3f);
+            if (is_j ? aj : ai) {
+                rhs = vadd(rhs, is_j ? vmul(desired, -wj) : vmul(desired, wi));
+                dg = sym_add(dg, sym_outer(n, stiff));
+            }
+            if (ai && aj) { off[0] = n.x; off[1] = n.y; off[2] = n.z; off[3] = stiff; }
+        }
+        sym_st(s->diag, i, dg);
+        if (!(s->w[i] > 0.0f)) {
+            s->r[i] = s->z[i] = s->d[i] = v3(0, 0, 0);
+            Sym id = {1, 0, 0, 1, 0, 1};
+            sym_st(s->pinv, i, id);
+            tmp[i] = 0.0f;
+        } else {
+            Sym inv = sym_inv(s, dg);
+            V3 z = sym_madd(inv, rhs, v3(0, 0, 0));
+            sym_st(s->pinv, i, inv);
+            s->r[i] = rhs; s->z[i] = z; s->d[i] = z;
+            tmp[i] = vdot(rhs, z);
+        }
+    }
+    float total = fixed_sum(tmp, s->V);
+    s->red[R_RZ] = total; s->red[R_INIT] = total; s->red[R_ITER] = 0.0f; s->red[R_DAD] = 0.0f; s->red[R_RZN] = 0.0f;
+    s->red[R_STATUS] = 0.0f;
+}
+
+/* Eight CG iterations with device alpha / beta and the incremental write-back
+ * (abi41.cu:3228-3464, 7655-7674). */
+static void pcg_iterate(OracleSolver* s, float* tmp) {
+    for (int it = 0; it < 8; ++it) {
+        /* q = A d */
+        int status_ok = s->red[R_STATUS] == 0.0f;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < s->V; ++i) {
+            tmp[i] = 0.0f;
+            if (!status_ok) continue;
+            if (!(s->w[i] > 0.0f)) { s->q[i] = v3(0, 0, 0); continue; }
+            V3 qv = sym_madd(sym_ld(s->diag, i), s->d[i], v3(0, 0, 0));
+            for (int k = s->sp_off[i]; k < s->sp_off[i + 1]; ++k) {
+                const float* o = s->off + 4 * (size_t)k;
+                Sym nb = {0, 0, 0, 0, 0, 0};
+                if (o[3] != 0.0f) {
+                    Sym b = sym_outer(v3(o[0], o[1], o[2]), o[3]);
+                    Sym m = {-b.m11, -b.m12, -b.m13, -b.m22, -b.m23, -b.m33};
+                    nb = m;
+                }
+                qv = sym_madd(nb, s->d[s->sp_other[k]], qv);
+            }
+            s->q[i] = qv;
+            tmp[i] = vdot(s->d[i], qv);
+        }
+        s->red[R_DAD] = s->red[R_DAD] + fixed_sum(tmp, s->V);
+        /* update */
+        float rz_old = s->red[R_RZ], dad = s->red[R_DAD], status = 0.0f, alpha = 0.0f;
+        if (!isfinite(rz_old) || rz_old < 0.0f) status = 1.0f;
+        else if (rz_old <= 1.0e-14f) status = 2.0f;
+        else if (!isfinite(dad) || dad <= 1.0e-14f) status = 3.0f;
+        else { alpha = rz_old / dad; if (!isfinite(alpha)) status = 4.0f; }
+        if (status != 0.0f) {
+            s->red[R_STATUS] = status;
+            if (status != 2.0f) s->pcg_guard += 1;
+        } else {
+            const float mdl = writeback_limit(s);
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < s->V; ++i) {
+                tmp[i] = 0.0f;
+                if (!(s->w[i] > 0.0f)) { s->r[i] = s->z[i] = v3(0, 0, 0); continue; }
+                V3 di = s->d[i], qi = s->q[i], ri = s->r[i];
+                V3 res = v3(fmaf(qi.x, -alpha, ri.x), fmaf(qi.y, -alpha, ri.y), fmaf(qi.z, -alpha, ri.z));
+                if (!vfinite(res)) res = v3(0, 0, 0);
+                V3 z = sym_madd(sym_ld(s->pinv, i), res, v3(0, 0, 0));
+                s->r[i] = res; s->z[i] = z;
+                tmp[i] = vdot(res, z);
+                V3 delta = vmul(di, alpha);
+                float len = vlen(delta);
+                if (len > mdl) { delta = vmul(delta, mdl / fmaxf(len, K_EPS)); cnt(s, C_HARD); }
+                s->pos[i] = vadd(s->pos[i], delta);
+                s->prev[i] = vadd(s->prev[i], vmul(delta, 0.08f));
+                float dl = vlen(delta);
+#pragma omp critical
+                if (dl > s->pcg_max_delta) s->pcg_max_delta = dl;
+            }
+            s->red[R_RZN] = s->red[R_RZN] + fixed_sum(tmp, s->V);
+            s->red[R_ITER] = s->red[R_ITER] + 1.0f;
+        }
+        if (it + 1 >= 8) break;
+        /* direction and advance */
+        float st = s->red[R_STATUS], ro = s->red[R_RZ], rn = s->red[R_RZN];
+        int ok = st == 0.0f && isfinite(ro) && isfinite(rn) && ro > 1.0e-14f && rn >= 0.0f;
+        float beta = ok ? rn / ro : 0.0f;
+        if (ok && isfinite(beta)) {
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < s->V; ++i) {
+                if (!(s->w[i] > 0.0f)) { s->d[i] = v3(0, 0, 0); continue; }
+                V3 dd = s->d[i], zz = s->z[i];
+                s->d[i] = v3(fmaf(dd.x, beta, zz.x), fmaf(dd.y, beta, zz.y), fmaf(dd.z, beta, zz.z));
+            }
+        }
+        if (st == 0.0f && isfinite(rn) && rn >= 0.0f) {
+            s->red[R_RZ] = rn; s->red[R_DAD] = 0.0f; s->red[R_RZN] = 0.0f; s->red[R_STATUS] = 0.0f;
+        }
+    }
+}
+
+/* Averaged polish / tiny corrections of one vertex's edges
+ * (abi41.cu:1995-2112, 2399-2494). */
+static int avg_delta(OracleSolver* s, int tiny, int a, int b, float rest, int is_j, V3* out) {
+    float wi = s->w[a], wj = s->w[b], weight = wi + wj;
+    if (!isfinite(weight) || weight <= 0.0f) return 0;
+    V3 pi = s->pos[a], pj = s->pos[b];
+    if (tiny) {
+        if (!isfinite(rest) || rest <= K_EPS || rest > 7.5e-4f) return 0;
+        if (!vfinite(pi) || !vfinite(pj)) return 0;
+    } else {
+        if (!isfinite(rest) || rest <= K_EPS) return 0;
+        if (!vfinite(pi) || !vfinite(pj) || !vfinite(s->prev[a]) || !vfinite(s->prev[b])) return 0;
+    }
+    V3 edge = vsub(pj, pi);
+    float lsq = vdot(edge, edge);
+    if (!isfinite(lsq) || lsq <= 1.0e-14f) return 0;
+    float len = sqrtf(lsq), target, relax, md;
+    if (tiny) { target = rest * 1.06f; relax = 1.0f; md = fminf(fmaxf(rest * 3.0f, 2.5e-4f), 8.0e-4f); }
+    else {
+        target = rest * (s->strength >= 0.95f ? 1.08f : 1.18f); relax = 0.90f;
+        md = fmaxf(5.0e-4f, fminf(fmaxf(rest * 2.0f, s->cfg.cloth_thickness * 0.25f), 0.008f));
+    }
+    float excess = len - target;
+    if (!isfinite(excess) || excess <= 0.0f) return 0;
+    V3 corr = vmul(edge, -relax * excess / fmaxf(weight * len, K_EPS));
+    if (!vfinite(corr)) return 0;
+    float cl = vlen(corr);
+    if (!isfinite(cl) || cl <= 1.0e-20f) return 0;
+    float w = is_j ? wj : wi;
+    if (!(w > 0.0f)) return 0;
+    V3 d = limit_delta(is_j ? vmul(corr, wj) : vmul(corr, -wi), md);
+    if (!vfinite(d) || !(vlen(d) > 0.0f)) return 0;
+    *out = d;
+    return 1;
+}
+static void averaged_pass(OracleSolver* s, int tiny) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s->V; ++i) {
+        V3 sum = v3(0, 0, 0);
+        float count = 0.0f;
+        for (int k = s->sp_off[i]; k < s->sp_off[i + 1]; ++k) {
+            int o = s->sp_other[k], is_j = s->sp_side[k];
+            V3 d;
+            if (avg_delta(s, tiny, is_j ? o : i, is_j ? i : o, s->sp_rest[k], is_j, &d)) { sum = vadd(sum, d); count += 1.0f; }
+        }
+        s->avg_sum[i] = sum; s->avg_cnt[i] = count;
+    }
+    const float th = s->cfg.cloth_thickness;
+    const float md = tiny ? fminf(fmaxf(th * 0.015f, 2.5e-4f), 9.0e-4f) : fmaxf(5.0e-4f, fminf(fmaxf(th * 0.20f, 1.0e-3f), 0.005f));
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s->V; ++i) {
+        if (!(s->w[i] > 0.0f)) continue;
+        float count = s->avg_cnt[i];
+        if (!isfinite(count) || count <= 0.0f) continue;
+        V3 delta = vmul(s->avg_sum[i], 1.0f / count);
+        if (!vfinite(delta)) { cnt(s, C_HARD); continue; }
+        delta = limit_delta(delta, md);
+        if (!vfinite(delta) || !(vlen(delta) > 0.0f)) continue;
+        s->pos[i] = vadd(s->pos[i], delta);
+        s->prev[i] = vadd(s->prev[i], vmul(delta, tiny ? 0.24f : 0.16f));
+    }
+}
+
+/* Ratio caps in place one colour at a time: kind 0 normal
+ * (abi41.cu:2249-2362), 1 tiny (2496-2601), 2 extreme (2603-2708). */
+static void cap_range(OracleSolver* s, int start, int count, float dt, int kind) {
+#pragma omp parallel for schedule(static)
+    for (int l = 0; l < count; ++l) {
+        int e = start + l;
+        if (e < 0 || e >= s->E) continue;
+        float rest = s->cap_rest[e];
+        if (!isfinite(rest) || rest <= K_EPS) continue;
+        if (kind == 1 ? rest > 7.5e-4f : rest <= 7.5e-4f) continue;
+        int i = s->cap_edges[2 * e], j = s->cap_edges[2 * e + 1];
+        if (i < 0 || j < 0 || i >= s->V || j >= s->V || i == j) continue;
+        float wi = s->w[i], wj = s->w[j], weight = wi + wj;
+        if (!isfinite(weight) || weight <= 0.0f) continue;
+        V3 pi = s->pos[i], pj = s->pos[j], qi = s->prev[i], qj = s->prev[j];
+        if (!vfinite(pi) || !vfinite(pj) || !vfinite(qi) || !vfinite(qj)) continue;
+        V3 edge = vsub(pj, pi);
+        float lsq = vdot(edge, edge);
+        if (!isfinite(lsq) || lsq <= 1.0e-14f) continue;
+        float len = sqrtf(lsq);
+        int high = s->strength >= 0.95f;
+        float sr, tr, md, ps;
+        float th = s->cfg.cloth_thickness;
+        if (kind == 0) { sr = high ? 1.12f : 1.32f; tr = high ? 1.04f : 1.22f; md = fminf(fmaxf(rest * 0.60f, th * 0.10f), 0.010f); ps = 0.08f; }
+        else if (kind == 1) { sr = 1.35f; tr = 1.12f; md = fminf(fmaxf(rest * 6.0f, 5.0e-4f), 1.5e-3f); ps = 1.0f; }
+        else { sr = 1.24f; tr = 1.10f; md = fminf(fmaxf(rest * 1.25f, th * 0.10f), 0.006f); ps = 0.30f; }
+        if (!isfinite(len) || len <= rest * sr) continue;
+        float excess = len - rest * tr;
+        if (!isfinite(excess) || excess <= 0.0f) continue;
+        V3 corr = vmul(edge, -excess / fmaxf(weight * len, K_EPS));
+        if (!vfinite(corr) || vlen(corr) <= 1.0e-20f) continue;
+        V3 pdi = v3(0, 0, 0), pdj = v3(0, 0, 0);
+        V3 n = vmul(edge, 1.0f / fmaxf(len, K_EPS));
+        float sdt = kind == 0 ? fmaxf(dt, K_EPS) : dt;
+        if (isfinite(sdt) && sdt > K_EPS) {
+            float inv_dt = 1.0f / sdt;
+            V3 vi = vmul(vsub(pi, qi), inv_dt), vj = vmul(vsub(pj, qj), inv_dt);
+            float sep = vdot(vsub(vj, vi), n);
+            if (isfinite(sep) && sep > 0.0f) {
+                float trim = sep * sdt * 1.0f / weight;
+                if (wi > 0.0f) pdi = vadd(pdi, vmul(n, -wi * trim));
+                if (wj > 0.0f) pdj = vadd(pdj, vmul(n, wj * trim));
+            }
+        }
+        if (wi > 0.0f) {
+            V3 d = limit_delta(vmul(corr, -wi), md);
+            if (vfinite(d) && vlen(d) > 0.0f) { pdi = vadd(pdi, vmul(d, ps)); s->pos[i] = vadd(pi, d); s->prev[i] = vadd(qi, pdi); }
+        }
+        if (wj > 0.0f) {
+            V3 d = limit_delta(vmul(corr, wj), md);
+            if (vfinite(d) && vlen(d) > 0.0f) { pdj = vadd(pdj, vmul(d, ps)); s->pos[j] = vadd(pj, d); s->prev[j] = vadd(qj, pdj); }
+        }
+    }
+}
+static void caps(OracleSolver* s, float dt, int kind, int passes, int both) {
+    for (int p = 0; p < passes; ++p) {
+        for (int k = 0; k < s->n_cap_colors; ++k) cap_range(s, s->cap_colors[k], s->cap_colors[k + 1] - s->cap_colors[k], dt, kind);
+        if (both)
+            for (int k = s->n_cap_colors - 1; k >= 0; --k) cap_range(s, s->cap_colors[k], s->cap_colors[k + 1] - s->cap_colors[k], dt, kind);
+    }
+}
+/* PCG solve + polish + extreme caps of one substep (abi41.cu:9183-9201) */
+static void hard_stretch(OracleSolver* s, float dt) {
+    float* tmp = (float*)calloc((size_t)s->V + 1, sizeof(float));
+    pcg_build(s, tmp);
+    pcg_iterate(s, tmp);
+    free(tmp);
+    if (s->strength >= 0.95f) {
+        for (int polish = 0; polish < 2; ++polish) {
+            averaged_pass(s, 0);
+            caps(s, dt, 0, 2, 1);
+            for (int tiny = 0; tiny < 2; ++tiny) {
+                averaged_pass(s, 1);
+                caps(s, dt, 1, 3, 0);
+            }
+        }
+        caps(s, dt, 2, 3, 0);
+    }
+}
+
 /* ----------------------------------------------------------- lifecycle -- */
 void oracle_destroy(OracleSolver* s) {
     if (!s) return;
     void* p[] = {s->pos, s->snap, s->prev, s->vel, s->rest, s->w, s->inv, s->sp_off, s->sp_other, s->sp_side, s->sp_rest,
                  s->te_off, s->te_other, s->te_side, s->te_rest, s->bj_off, s->bj_other, s->bj_side, s->bj_rest, s->bends,
                  s->bend_rest, s->bend_colors, s->tris, s->edges, s->pin_w, s->pin_t, s->pin_relax, s->sdf, s->stris,
-                 s->vcell, s->vb_start, s->vb_ent, s->tb_start, s->tb_ent, s->eb_start, s->eb_ent, s->nb_count, s->nb_idx, s->acc};
+                 s->vcell, s->vb_start, s->vb_ent, s->tb_start, s->tb_ent, s->eb_start, s->eb_ent, s->nb_count, s->nb_idx, s->acc,
+                 s->diag, s->pinv, s->r, s->z, s->d, s->q, s->off, s->avg_sum, s->avg_cnt, s->cap_edges, s->cap_rest, s->cap_colors};
     for (size_t k = 0; k < sizeof(p) / sizeof(p[0]); ++k) free(p[k]);
     free(s);
 }
@@ -1300,7 +1649,6 @@ OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* me
     if (!isfinite(c->stretch_optimization_strength)) c->stretch_optimization_strength = 0.0f;
     c->stretch_optimization_strength = clamp01(c->stretch_optimization_strength);
     c->stretch_optimization_enabled = (c->edge_count > 0 && c->stretch_optimization_enabled && c->stretch_optimization_strength > 0.0f);
-    if (c->stretch_optimization_enabled) { set_err("oracle: stretch optimization not restated"); oracle_destroy(s); return NULL; }
     const int V = c->vertex_count, E = c->edge_count, B = c->bend_count, L = c->lra_count, T = c->triangle_count;
     s->V = V; s->E = E; s->B = B; s->L = L; s->T = T;
     if (B > 0 && (!mesh->bends || !mesh->bend_rest_lengths)) { set_err("ABI41 bend constraints require bend pairs and rest lengths"); oracle_destroy(s); return NULL; }
@@ -1334,6 +1682,47 @@ OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* me
         s->edges[2 * e] = sp[2 * e]; s->edges[2 * e + 1] = sp[2 * e + 1];
     }
     build_csr(V, sp, spr, E, &s->sp_off, &s->sp_other, &s->sp_side, &s->sp_rest);
+    s->pcg_on = c->stretch_optimization_enabled;
+    s->strength = c->stretch_optimization_strength;
+    if (s->pcg_on) {
+        if (s->sp_off[V] == 0) { free(sp); free(spr); set_err("PCG stretch optimization found no valid CSR edges"); oracle_destroy(s); return NULL; }
+        s->diag = (float*)calloc(nv * 6, sizeof(float)); s->pinv = (float*)calloc(nv * 6, sizeof(float));
+        s->r = (V3*)calloc(nv, sizeof(V3)); s->z = (V3*)calloc(nv, sizeof(V3)); s->d = (V3*)calloc(nv, sizeof(V3)); s->q = (V3*)calloc(nv, sizeof(V3));
+        s->off = (float*)calloc((size_t)s->sp_off[V] * 4 + 4, sizeof(float));
+        s->avg_sum = (V3*)calloc(nv, sizeof(V3)); s->avg_cnt = (float*)calloc(nv, sizeof(float));
+        s->cap_edges = (int*)xcalloc((size_t)E * 2, sizeof(int)); s->cap_rest = (float*)xcalloc((size_t)E, sizeof(float));
+        if (c->edge_color_count > 0 && mesh->edge_color_offsets) {
+            s->n_cap_colors = c->edge_color_count;
+            s->cap_colors = (int*)malloc(sizeof(int) * (size_t)(s->n_cap_colors + 1));
+            memcpy(s->cap_colors, mesh->edge_color_offsets, sizeof(int) * (size_t)(s->n_cap_colors + 1));
+            memcpy(s->cap_edges, sp, sizeof(int) * 2 * (size_t)E); memcpy(s->cap_rest, spr, sizeof(float) * (size_t)E);
+        } else {
+            /* greedy first-fit colouring in edge order, stable grouping */
+            int* color = (int*)calloc((size_t)E + 1, sizeof(int));
+            int ncol = 0;
+            unsigned char* used = (unsigned char*)calloc(nv * 64, 1);
+            for (int e = 0; e < E; ++e) {
+                int a = sp[2 * e], b = sp[2 * e + 1], k = 0;
+                while (k < 64 && ((a < V && used[(size_t)a * 64 + k]) || (b < V && used[(size_t)b * 64 + k]))) ++k;
+                color[e] = k;
+                if (a < V && k < 64) used[(size_t)a * 64 + k] = 1;
+                if (b < V && k < 64) used[(size_t)b * 64 + k] = 1;
+                if (k + 1 > ncol) ncol = k + 1;
+            }
+            free(used);
+            s->n_cap_colors = ncol;
+            s->cap_colors = (int*)calloc((size_t)ncol + 1, sizeof(int));
+            for (int e = 0; e < E; ++e) s->cap_colors[color[e] + 1]++;
+            for (int k = 0; k < ncol; ++k) s->cap_colors[k + 1] += s->cap_colors[k];
+            int* cur = (int*)malloc(sizeof(int) * (size_t)(ncol + 1));
+            memcpy(cur, s->cap_colors, sizeof(int) * (size_t)(ncol + 1));
+            for (int e = 0; e < E; ++e) {
+                int at = cur[color[e]]++;
+                s->cap_edges[2 * at] = sp[2 * e]; s->cap_edges[2 * at + 1] = sp[2 * e + 1]; s->cap_rest[at] = spr[e];
+            }
+            free(cur); free(color);
+        }
+    }
     free(sp); free(spr);
     build_csr(V, L > 0 ? mesh->lra_edges : NULL, L > 0 ? mesh->lra_rest_lengths : NULL, L, &s->te_off, &s->te_other, &s->te_side, &s->te_rest);
     s->bends = (int*)xcalloc((size_t)B * 2, sizeof(int));
@@ -1422,6 +1811,9 @@ int oracle_step(OracleSolver* s, int substeps, int iterations) {
     if (iterations < 1) iterations = 1;
     memset(s->counts, 0, sizeof(s->counts));
     s->max_delta = 0.0f;
+    s->pcg_guard = 0;
+    s->pcg_max_delta = 0.0f;
+    memset(s->red, 0, sizeof(s->red));
     if (s->pin_relax_iter != iterations) {
         float ex = 1.0f / (float)(iterations + 1 > 1 ? iterations + 1 : 1);
         for (int i = 0; i < s->V; ++i) s->pin_relax[i] = soft_relax(s->pin_w[i], ex);
@@ -1436,7 +1828,8 @@ int oracle_step(OracleSolver* s, int substeps, int iterations) {
         pin_all(s, dt);
         for (int it = 0; it < iterations; ++it) {
             int last = it == iterations - 1, final_c = st == substeps - 1 && last;
-            if (s->E > 0) spring_all(s, dt);
+            if (s->E > 0 && !s->pcg_on) spring_all(s, dt);
+            if (s->pcg_on && last) hard_stretch(s, dt);
             if (final_c && s->L > 0) tether_all(s, dt);
             if (final_c && s->B > 0) { if (s->n_bend_colors > 0) bends_by_color(s, dt); else bends_jacobi(s, dt); }
             pin_all(s, dt);
@@ -1445,6 +1838,11 @@ int oracle_step(OracleSolver* s, int substeps, int iterations) {
             int self_run = s->self_on && s->cfg.self_collision && last && (((st + 1) % interval) == 0 || st == substeps - 1) &&
                            s->V > 0 && s->radius > 0.0f;
             if (self_run) self_collision(s);
+            if (s->pcg_on && final_c && s->strength >= 0.95f) {
+                caps(s, dt, 0, 2, 1);
+                caps(s, dt, 2, 3, 0);
+                caps(s, dt, 1, 3, 0);
+            }
             if (analytic || sdf || last || self_run) pin_all(s, dt);
         }
         velocity_all(s, dt);

@@ -150,6 +150,7 @@ struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
     long long cache_hits = 0, cache_misses = 0;
+    long long pcg_solves = 0;
 };
 
 struct Solver {
@@ -219,6 +220,15 @@ struct Solver {
 
     int wing_count = 0;  // triangle pairs sharing an edge (bending wings)
 
+    // hard-stretch optimisation (CG solve and caps)
+    bool pcg_on = false;
+    PcgView pcg{};
+    int2* cap_edges = nullptr;   // edges sorted by colour for the caps
+    float* cap_rest = nullptr;
+    std::vector<int> cap_colors; // colour offsets into cap_edges
+    int pcg_nnz = 0;
+    long long pcg_iterations = 0;
+
     std::map<GraphKey, GraphEntry> graphs;
     bool use_graphs = true;
     long long last_launches = 0;
@@ -284,7 +294,9 @@ void free_solver(Solver* S) {
                     S->bend_rest, S->tris,     S->edges,      S->edge_rest, S->pin_target, S->pin_weight, S->pin_relax,
                     S->counts,    S->max_delta_bits, S->pack, S->sdf,      S->static_tris, S->vcell,    S->vb_count,
                     S->vb_start,  S->vb_ent,   S->tb_count,   S->tb_start, S->tb_ent,    S->eb_count,   S->eb_start,
-                    S->eb_ent,    S->nb_count, S->nb_idx,     S->acc,      S->scan_tmp};
+                    S->eb_ent,    S->nb_count, S->nb_idx,     S->acc,      S->scan_tmp,  S->pcg.diag,   S->pcg.pinv,
+                    S->pcg.r,     S->pcg.z,    S->pcg.d,      S->pcg.q,    S->pcg.offdiag, S->pcg.avg,  S->pcg.red,
+                    S->pcg.partials, S->pcg.ticket, S->pcg.guard, S->pcg.max_delta_bits, S->cap_edges, S->cap_rest};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (S->stream) cudaStreamDestroy(S->stream);
@@ -504,12 +516,15 @@ enum KernelKind {
     kKIsland = 11,
     kKSelfApply = 12,
     kKCopy = 13,
-    kKinds = 14
+    kKPcg = 14,          // CG solve (build + 8 iterations)
+    kKStretchCaps = 15,  // averaged polish and colour-range ratio caps
+    kKinds = 16
 };
 
 struct FrameStats {
     long long launches = 0;
     long long cache_hits = 0, cache_misses = 0;
+    long long pcg_solves = 0;
 };
 
 // Optional per-launch event pairs, recorded when profiling a frame.
@@ -529,7 +544,9 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
     const float dt = c.dt / (float)substeps;
     const bool analytic = P.use_ground || P.use_wall || P.use_sphere;
     const bool sdf = P.sdf_ready != 0;
-    const bool spring = E > 0;
+    const bool pcg = S->pcg_on;
+    const bool spring = E > 0 && !pcg;
+    const bool hard = pcg && P.stretch_strength >= 0.95f;
     View base = S->view();
     int cur = 0;
     unsigned pending = 0;
@@ -565,6 +582,40 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         v.pos = S->pos[cur];
         return v;
     };
+    // colour-range caps over the colour-sorted edge arrays
+    auto caps = [&](int kind, int passes, bool both_ways) {
+        View cv = base;
+        cv.pos_in = S->pos[cur];
+        cv.pos = S->pos[cur];
+        cv.edges = S->cap_edges;
+        cv.edge_rest = S->cap_rest;
+        const int ncol = (int)S->cap_colors.size() - 1;
+        timed(kKStretchCaps, 0, [&] {
+            for (int p = 0; p < passes; ++p) {
+                for (int k = 0; k < ncol; ++k) {
+                    const int n = S->cap_colors[k + 1] - S->cap_colors[k];
+                    if (n > 0) {
+                        pcg_cap_range(cv, S->cap_colors[k], n, dt, kind, S->stream);
+                        st->launches += 1;
+                    }
+                }
+                if (both_ways)
+                    for (int k = ncol - 1; k >= 0; --k) {
+                        const int n = S->cap_colors[k + 1] - S->cap_colors[k];
+                        if (n > 0) {
+                            pcg_cap_range(cv, S->cap_colors[k], n, dt, kind, S->stream);
+                            st->launches += 1;
+                        }
+                    }
+            }
+        });
+    };
+    auto averaged = [&](bool tiny) {
+        View av = base;
+        av.pos_in = S->pos[cur];
+        av.pos = S->pos[cur];
+        timed(kKStretchCaps, 2, [&] { pcg_averaged_pass(av, S->pcg, V, tiny, S->stream); });
+    };
     const bool self_enabled = S->self_on && c.self_collision && V > 0 && P.self_radius > 0.0f;
     const int interval = std::max(c.self_collision_interval, 1);
     const int passes = std::max(1, std::min(c.fast_self_collision_passes, 8));
@@ -577,6 +628,25 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
             const bool final_c = (s == substeps - 1) && last_it;
             flush();
             if (spring) gather = 1;
+            if (pcg && last_it) {
+                // CG stretch solve, then (hardness >= 0.95) the averaged
+                // polish with normal and tiny caps, and the extreme caps
+                // (abi41.cu:9183-9201, 7806-7857, 7974-7995)
+                View gv = cur_view();
+                timed(kKPcg, 0, [&] { pcg_solve(gv, S->pcg, V, S->stream, &st->launches); });
+                st->pcg_solves += 1;
+                if (hard) {
+                    for (int polish = 0; polish < 2; ++polish) {
+                        averaged(false);
+                        caps(0, 2, true);
+                        for (int tiny = 0; tiny < 2; ++tiny) {
+                            averaged(true);
+                            caps(1, 3, false);
+                        }
+                    }
+                    caps(2, 3, false);
+                }
+            }
             if (final_c && L > 0) {
                 flush();
                 gather = 2;
@@ -633,6 +703,13 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                     timed(kKSelfApply, 1, [&] { self_apply(sv, V, S->stream); });
                 }
             }
+            // final ratio caps after the contacts (abi41.cu:9346-9350, 7997-8027)
+            if (pcg && final_c && hard) {
+                flush();
+                caps(0, 2, true);
+                caps(2, 3, false);
+                caps(1, 3, false);
+            }
             // Final pin polish whenever a contact stage ran (the dynamic
             // collider stage counts as running on every last iteration).
             if (analytic || sdf || last_it || self_run) pending |= kPassPinPolish;
@@ -665,11 +742,13 @@ bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st) {
         g.launches = cst.launches;
         g.cache_hits = cst.cache_hits;
         g.cache_misses = cst.cache_misses;
+        g.pcg_solves = cst.pcg_solves;
         it = S->graphs.emplace(key, g).first;
     }
     st->launches += it->second.launches;
     st->cache_hits += it->second.cache_hits;
     st->cache_misses += it->second.cache_misses;
+    st->pcg_solves += it->second.pcg_solves;
     return cuda_ok(cudaGraphLaunch(it->second.exec, S->stream), "launch frame graph");
 }
 
@@ -715,6 +794,34 @@ bool fetch_counts(Solver* S, const FrameStats& st) {
     d.self_filter_cache_misses = S->cfg.self_collision_mode == 1 ? st.cache_misses : 0;
     d.self_cluster_count = (long long)c[kCntClusterCount];
     d.self_cluster_owned_contacts = (long long)c[kCntClusterOwnedContacts];
+    if (S->pcg_on) {
+        // residual diagnostics from the scalar slots (abi41.cu:7586-7624)
+        float red[kRedSlots];
+        unsigned long long guard = 0;
+        unsigned mbits = 0;
+        if (!cuda_ok(cudaMemcpyAsync(red, S->pcg.red, sizeof(red), cudaMemcpyDeviceToHost, S->stream), "fetch PCG reductions") ||
+            !cuda_ok(cudaMemcpyAsync(&guard, S->pcg.guard, sizeof(guard), cudaMemcpyDeviceToHost, S->stream), "fetch PCG guard count") ||
+            !cuda_ok(cudaMemcpyAsync(&mbits, S->pcg.max_delta_bits, 4, cudaMemcpyDeviceToHost, S->stream), "fetch PCG max delta") ||
+            !cuda_ok(cudaStreamSynchronize(S->stream), "fetch PCG diagnostics"))
+            return false;
+        d.abi41_pcg_csr_nnz = S->pcg_nnz;
+        d.abi41_pcg_texture_ready = 1;
+        d.abi41_pcg_iterations = S->pcg_iterations;
+        float initial = red[kRedInitialRZ];
+        if ((!std::isfinite(initial) || initial <= 0.0f) && std::isfinite(red[kRedRZ]) && red[kRedRZ] >= 0.0f) initial = red[kRedRZ];
+        if (std::isfinite(initial) && initial >= 0.0f) {
+            d.abi41_pcg_initial_residual = std::sqrt(std::max(initial, 0.0f));
+            d.abi41_pcg_final_residual = d.abi41_pcg_initial_residual;
+        }
+        const float status = red[kRedStatus];
+        const float final_rz = status == 2.0f ? red[kRedRZ] : red[kRedRZNext];
+        if ((status == 0.0f || status == 2.0f) && std::isfinite(final_rz) && final_rz >= 0.0f)
+            d.abi41_pcg_final_residual = std::sqrt(std::max(final_rz, 0.0f));
+        else if (status != 0.0f && status != 2.0f)
+            d.abi41_pcg_guarded += 1;
+        d.abi41_pcg_guarded += (long long)guard;
+        std::memcpy(&d.abi41_pcg_max_delta, &mbits, 4);
+    }
     return true;
 }
 
@@ -758,8 +865,6 @@ extern "C" SSBL_API void* ssbl_create_solver(const SsblXpbdConfig* config, const
         free_solver(S);
         return nullptr;
     };
-    if (c.stretch_optimization_enabled)
-        return bail("stretch optimization (PCG hard stretch) is not supported by this build of the GB300 solver");
     if (c.use_volume_pressure && c.pressure_strength > 0.0f)
         return bail("volume pressure is not supported by this build of the GB300 solver");
     if (B > 0 && (!mesh->bends || !mesh->bend_rest_lengths))
@@ -847,6 +952,8 @@ extern "C" SSBL_API void* ssbl_create_solver(const SsblXpbdConfig* config, const
     P.self_radius = radius;
     P.self_mode = c.self_collision_mode;
     P.max_neighbors = c.max_self_collision_neighbors;
+    P.stretch_strength = c.stretch_optimization_strength;
+    S->pcg_on = c.stretch_optimization_enabled != 0;
     S->self_on = c.self_collision != 0;
     if (S->self_on && radius > 0.0f) {
         const float cell = std::max(radius * 1.8f, 1.0e-3f);
@@ -894,6 +1001,57 @@ extern "C" SSBL_API void* ssbl_create_solver(const SsblXpbdConfig* config, const
                  dalloc(&S->eb_start, P.ebuckets + 1, "self edge hash start allocation") &&
                  dalloc(&S->eb_ent, (size_t)E * kMaxPrimitiveCells, "self edge hash index allocation");
     }
+    // hard-stretch buffers; caps need edges grouped by colour: the caller's
+    // colouring when given (edges already sorted by colour), else a greedy
+    // first-fit colouring in edge order
+    std::vector<int2> cap_edges;
+    std::vector<float> cap_rest;
+    if (ok && S->pcg_on) {
+        S->pcg_nnz = (int)sp_ent.size();
+        if (S->pcg_nnz == 0) return bail("PCG stretch optimization found no valid CSR edges");
+        if (!S->edge_colors.empty()) {
+            cap_edges = springs;
+            cap_rest = spring_rest;
+            S->cap_colors = S->edge_colors;
+        } else {
+            std::vector<int> color(E, 0);
+            std::vector<std::vector<int>> used(V);
+            int ncol = 0;
+            for (int e = 0; e < E; ++e) {
+                const int a = springs[e].x, b = springs[e].y;
+                int k = 0;
+                auto taken = [&](int v, int col) {
+                    return v >= 0 && v < V && std::find(used[v].begin(), used[v].end(), col) != used[v].end();
+                };
+                while (taken(a, k) || taken(b, k)) ++k;
+                color[e] = k;
+                if (a >= 0 && a < V) used[a].push_back(k);
+                if (b >= 0 && b < V) used[b].push_back(k);
+                ncol = std::max(ncol, k + 1);
+            }
+            S->cap_colors.assign(ncol + 1, 0);
+            for (int e = 0; e < E; ++e) S->cap_colors[color[e] + 1]++;
+            for (int k = 0; k < ncol; ++k) S->cap_colors[k + 1] += S->cap_colors[k];
+            std::vector<int> cursor(S->cap_colors.begin(), S->cap_colors.end() - 1);
+            cap_edges.resize(E);
+            cap_rest.resize(E);
+            for (int e = 0; e < E; ++e) {
+                const int at = cursor[color[e]]++;
+                cap_edges[at] = springs[e];
+                cap_rest[at] = spring_rest[e];
+            }
+        }
+        PcgView& g = S->pcg;
+        ok = dalloc(&g.diag, 2 * (size_t)V, "PCG diagonal block allocation") &&
+             dalloc(&g.pinv, 2 * (size_t)V, "PCG preconditioner allocation") && dalloc(&g.r, V, "PCG residual allocation") &&
+             dalloc(&g.z, V, "PCG preconditioned residual allocation") && dalloc(&g.d, V, "PCG search direction allocation") &&
+             dalloc(&g.q, V, "PCG A*d allocation") && dalloc(&g.offdiag, sp_ent.size(), "PCG offdiagonal allocation") &&
+             dalloc(&g.avg, V, "stretch cap accumulation allocation") && dalloc(&g.red, kRedSlots, "PCG reduction allocation") &&
+             dalloc(&g.partials, pcg_warp_partials(V), "PCG partial sum allocation") &&
+             dalloc(&g.ticket, 1, "PCG ticket allocation") && dalloc(&g.guard, 1, "PCG guard counter allocation") &&
+             dalloc(&g.max_delta_bits, 1, "PCG max delta allocation") && dalloc(&S->cap_edges, E, "cap edge allocation") &&
+             dalloc(&S->cap_rest, E, "cap rest allocation");
+    }
     if (!ok) return bail(nullptr);
     cudaStream_t st = S->stream;
     ok = dupload(S->pos[0], rest4.data(), V, st, "position upload") && dupload(S->pos[1], rest4.data(), V, st, "position upload") &&
@@ -917,6 +1075,12 @@ extern "C" SSBL_API void* ssbl_create_solver(const SsblXpbdConfig* config, const
          (!S->acc || cuda_ok(cudaMemsetAsync(S->acc, 0, sizeof(Acc4) * V, st), "reset self accumulation")) &&
          (!S->nb_count || cuda_ok(cudaMemsetAsync(S->nb_count, 0, sizeof(int) * V, st), "reset neighbor table")) &&
          sync_params(S) && cuda_ok(cudaStreamSynchronize(st), "solver upload");
+    if (ok && S->pcg_on)
+        ok = dupload(S->cap_edges, cap_edges.data(), E, st, "cap edge upload") &&
+             dupload(S->cap_rest, cap_rest.data(), E, st, "cap rest upload") &&
+             cuda_ok(cudaMemsetAsync(S->pcg.ticket, 0, sizeof(unsigned), st), "reset PCG ticket") &&
+             cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots, st), "reset PCG reductions") &&
+             cuda_ok(cudaStreamSynchronize(st), "PCG buffer upload");
     if (!ok) return bail(nullptr);
     S->diag.finite_flag = 1;
     S->diag.abi41_bending_wing_count = S->wing_count;
@@ -1032,9 +1196,15 @@ extern "C" SSBL_API int ssbl_step_solver_ex(void* handle, int substeps, int iter
         !cuda_ok(cudaMemsetAsync(S->max_delta_bits, 0, sizeof(unsigned), S->stream), "reset self max smoothed delta") ||
         !upload_pin_relax(S, iterations) || !sync_params(S))
         return 0;
+    if (S->pcg_on &&
+        (!cuda_ok(cudaMemsetAsync(S->pcg.guard, 0, sizeof(unsigned long long), S->stream), "reset PCG guard count") ||
+         !cuda_ok(cudaMemsetAsync(S->pcg.max_delta_bits, 0, sizeof(unsigned), S->stream), "reset PCG max delta") ||
+         !cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots, S->stream), "reset PCG reductions")))
+        return 0;
     FrameStats st;
     if (!run_frame(S, substeps, iterations, &st)) return 0;
     S->last_launches = st.launches;
+    S->pcg_iterations = st.pcg_solves * 8;
     if (force_sync || fetch_diagnostics) {
         const auto ts = std::chrono::high_resolution_clock::now();
         if (!cuda_ok(cudaStreamSynchronize(S->stream), "ABI41 solver step")) return 0;

@@ -68,6 +68,9 @@ enum Counter {
     kCntSlots = 38
 };
 
+// Scalar slots of the CG solve (same roles as abi41.cu:158-164).
+enum PcgSlot { kRedDAD = 0, kRedRZ = 1, kRedRZNext = 2, kRedStatus = 3, kRedInitialRZ = 4, kRedIterations = 5, kRedSlots = 8 };
+
 // Values that can change between frames without changing the launch
 // sequence.  They live in device memory so a captured CUDA graph stays valid
 // when the caller moves a collider or the pins.
@@ -104,6 +107,24 @@ struct Params {
     float vcell, tcell, ecell;
     int vbuckets, tbuckets, ebuckets;
     int vhash, thash, ehash;  // hash in use (else brute force)
+    float stretch_strength;   // clamp01(stretch_optimization_strength)
+};
+
+// Buffers of the hard-stretch CG solve and the averaged caps.
+struct PcgView {
+    float4* diag;        // 2 rows per vertex: symmetric 3x3 block
+    float4* pinv;        // 2 rows per vertex: block-Jacobi inverse
+    float4* r;
+    float4* z;
+    float4* d;
+    float4* q;
+    float4* offdiag;     // per stretch-CSR entry: edge normal xyz, stiffness
+    float4* avg;         // averaged caps: sum xyz, count
+    float* red;          // kRedSlots scalars
+    float* partials;     // one per warp of the solve grid
+    unsigned* ticket;    // last-block ticket
+    unsigned long long* guard;
+    unsigned* max_delta_bits;
 };
 
 // Device pointers of one solver, passed by value to each kernel.
@@ -173,6 +194,11 @@ __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 void set_last_error(const std::string& msg);
 
 // ---- host launchers (defined in the .cu files) ----
+int pcg_warp_partials(int V);
+void pcg_solve(const View& v, const PcgView& g, int V, cudaStream_t s, long long* launches);
+void pcg_averaged_pass(const View& v, const PcgView& g, int V, bool tiny, cudaStream_t s);
+// kind: 0 normal cap, 1 tiny cap, 2 extreme cap
+void pcg_cap_range(const View& v, int start, int count, float dt, int kind, cudaStream_t s);
 void launch_predict(const View& v, int V, float dt, cudaStream_t s);
 // pass flags for launch_vertex_pass
 enum PassFlags : unsigned {

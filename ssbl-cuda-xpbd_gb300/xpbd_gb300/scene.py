@@ -352,3 +352,23 @@ def drop_scene(n: int = 100, frames: int = 200, seed: int = 0, self_mode: int = 
                         max_self_collision_neighbors=64 if self_mode == 2 else 32, fast_self_collision_passes=4,
                         contact_friction=0.3, static_sdf_max_resolution=64)
     return Scene(f"drop-{n}", cloth, opt, collider_meshes(), 10, 2, frames, 1.0)
+
+
+def hardness_grid_scene(n: int = 32, hardness: float = 0.4, frames: int = 60) -> Scene:
+    """The plain grid with the add-on's hardness mapping: compliances from the
+    hardness slider, the hard-stretch (CG) path at strength = hardness, and
+    hidden tethers to the pins when hardness >= 0.5 (xpbd_core.py:213-244)."""
+    base = plain_grid_scene(n, frames)
+    h = derive_hardness(hardness)
+    w = np.zeros(len(base.cloth.positions_world), np.float32)
+    w[base.cloth.pin_indices] = 1.0
+    cloth = build_cloth(base.cloth.positions_world, base.cloth.triangles, 0.2, w,
+                        tether_slack=h["hidden_tether_slack"] if h["hidden_tether_enabled"] else None)
+    opt = base.options
+    opt.stretch_compliance = h["stretch_compliance"]
+    opt.bend_compliance = h["bend_compliance"]
+    opt.stretch_optimization_enabled = h["stretch_optimization_enabled"]
+    opt.stretch_optimization_strength = h["stretch_optimization_strength"]
+    opt.lra_compliance = h["hidden_tether_compliance"] if h["hidden_tether_enabled"] else 0.0
+    opt.cloth_thickness = 0.02
+    return Scene(f"hardness-{hardness}-grid-{n}", cloth, opt, base.static_triangles, 10, 2, frames, 1.0)

@@ -290,3 +290,66 @@ def pinned_square():
 
 ALL = [static_sdf_plane, static_sdf_box, self_vv, self_vt, self_ee, tether_static, tether_animated, bend_hinge,
        pin_weights, pinned_square]
+
+
+def _hard_stretch_case(rest, inv, start, enabled):
+    """abi41_smoke.cpp:599-652: one edge of rest 1 m, soft springs, PCG on or
+    off at full strength, stepped 1 x 1 from `start`."""
+    cfg = _cfg(vertex_count=2, edge_count=1, dt=1 / 60, damping=1.0, gravity=(0, 0, 0), stretch_compliance=1.0e6,
+               stretch_optimization_enabled=1 if enabled else 0, stretch_optimization_strength=1.0)
+    m, keep = _mesh(positions=np.asarray(rest, np.float32), inv_mass=inv, edges=[[0, 1]], edge_rest_lengths=[1.0])
+    start = np.asarray(start, np.float32)
+
+    def run(solver):
+        solver.update_positions(start)
+        solver.step(1, 1)
+        out = solver.download_positions().copy()
+        assert np.isfinite(out).all()
+        return out
+
+    return Case("hard_stretch", cfg, m, keep), run
+
+
+def _chain_case():
+    """abi41_smoke.cpp:654-742: a pinned 4-vertex chain with its end pulled
+    2 m out; the PCG pass pulls the end back by more than 2 cm."""
+    rest = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [3, 0, 0]], np.float32)
+    start = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [5, 0, 0]], np.float32)
+    cfg = _cfg(vertex_count=4, edge_count=3, dt=1 / 60, damping=1.0, stretch_compliance=1.0e6,
+               stretch_optimization_enabled=1, stretch_optimization_strength=1.0)
+    m, keep = _mesh(positions=rest, inv_mass=[0, 1, 1, 1], edges=[[0, 1], [1, 2], [2, 3]], edge_rest_lengths=[1, 1, 1])
+
+    def run(solver):
+        solver.update_positions(start)
+        solver.step(1, 1)
+        out = solver.download_positions().copy()
+        assert np.isfinite(out).all()
+        assert out[3, 0] < start[3, 0] - 0.02
+        return out
+
+    return Case("chain", cfg, m, keep), run
+
+
+def hard_stretch_suite(make_solver):
+    """abi41_smoke.cpp:744-876 with `make_solver(case)` building the backend:
+    returns the outputs so callers can compare backends."""
+    rest = [[0, 0, 0], [1, 0, 0]]
+    stretched = [[0, 0, 0], [2.5, 0, 0]]
+    outs = {}
+    for name, args in {
+        "off": (rest, [1.0, 1.0], stretched, False),
+        "on": (rest, [1.0, 1.0], stretched, True),
+        "pinned": (rest, [0.0, 1.0], stretched, True),
+        "both_pinned": ([[0, 0, 0], [2.5, 0, 0]], [0.0, 0.0], [[0, 0, 0], [2.5, 0, 0]], True),
+        "zero": (rest, [1.0, 1.0], [[0, 0, 0], [0, 0, 0]], True),
+    }.items():
+        case, run = _hard_stretch_case(*args)
+        outs[name] = run(make_solver(case))
+    off_d = float(np.linalg.norm(outs["off"][1] - outs["off"][0]))
+    on_d = float(np.linalg.norm(outs["on"][1] - outs["on"][0]))
+    assert on_d < off_d - 0.05, (off_d, on_d)
+    assert abs(outs["pinned"][0, 0]) <= 1e-5 and outs["pinned"][1, 0] < 2.5 - 0.05
+    assert abs(float(np.linalg.norm(outs["both_pinned"][1] - outs["both_pinned"][0])) - 2.5) <= 1e-4
+    case, run = _chain_case()
+    outs["chain"] = run(make_solver(case))
+    return outs

@@ -65,3 +65,28 @@ def test_gpu_bend_wing_diagnostics(gpu_lib):
     run(gpu)
     d = gpu.diagnostics()
     assert d["abi41_bending_texture_ready"] == 1 and d["abi41_bending_wing_count"] > 0
+
+
+def test_gpu_hard_stretch_known_answers_and_parity(gpu_lib, oracle_lib):
+    """abi41_smoke.cpp:599-876: PCG shrinks a stretched edge more than the
+    soft springs, keeps pins, CSR nnz 2 / 6, residual decreases; outputs
+    bit-identical to the oracle."""
+    diags = {}
+
+    def make_gpu(c):
+        s = gpu_lib.NativeXpbdSolver.from_raw(c.cfg, c.mesh, c.pins)
+        diags[len(diags)] = s
+        return s
+
+    g = kat_cases.hard_stretch_suite(make_gpu)
+    o = kat_cases.hard_stretch_suite(lambda c: oracle_lib.OracleSolver(c.cfg, c.mesh, c.keep, c.pins))
+    for k in g:
+        assert np.array_equal(g[k], o[k]), (k, g[k], o[k])
+    on = diags[1].diagnostics()
+    assert on["abi41_pcg_csr_nnz"] == 2 and on["abi41_pcg_texture_ready"] == 1 and on["abi41_pcg_iterations"] > 0
+    assert on["abi41_pcg_initial_residual"] > 0.0
+    assert on["abi41_pcg_final_residual"] < on["abi41_pcg_initial_residual"]
+    assert on["abi41_pcg_max_delta"] > 0.0
+    chain = diags[5].diagnostics()
+    assert chain["abi41_pcg_csr_nnz"] == 6 and chain["abi41_pcg_iterations"] > 0
+    assert chain["abi41_pcg_final_residual"] < chain["abi41_pcg_initial_residual"]

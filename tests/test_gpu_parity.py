@@ -50,6 +50,15 @@ def test_plain_grid_with_tethers_and_graph_off(gpu_lib, oracle_lib):
     _run_and_compare(sc, gpu, ora, 6)
 
 
+@pytest.mark.parametrize("hardness", [0.4, 1.0])
+def test_hard_stretch_grid_parity(hardness, gpu_lib, oracle_lib):
+    """CG stretch path (hardness 0.4) and CG + averaged polish + ratio caps +
+    tethers (hardness 1.0) against the oracle."""
+    sc = scene.hardness_grid_scene(24, hardness, 8)
+    gpu, ora = _pair(sc, oracle_lib)
+    _run_and_compare(sc, gpu, ora, 8)
+
+
 @pytest.mark.parametrize("mode", [2, 1], ids=["strict", "fast"])
 def test_drop_scene_parity(mode, gpu_lib, oracle_lib):
     sc = scene.drop_scene(48, 8, seed=0, self_mode=mode)

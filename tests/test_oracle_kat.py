@@ -22,3 +22,8 @@ def test_oracle_self_counters(oracle_lib):
     counts = solver.read_buffer(13, np.uint64, 38)
     assert counts[0] + counts[1] > 0  # soft + exact-impulse contacts
     assert counts[9] > 0  # candidates
+
+
+def test_oracle_hard_stretch_known_answers(oracle_lib):
+    """abi41_smoke.cpp:599-876 (PCG hard stretch) on the oracle."""
+    kat_cases.hard_stretch_suite(lambda c: oracle_lib.OracleSolver(c.cfg, c.mesh, c.keep, c.pins))
