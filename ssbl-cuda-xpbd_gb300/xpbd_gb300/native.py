@@ -462,7 +462,7 @@ class NativeXpbdSolver:
 
     KERNEL_KINDS = ("predict", "stretch_pass", "vertex_pass", "bend_color", "vertex_hash", "triangle_hash",
                     "edge_hash", "neighbors", "vertex_vertex", "vertex_triangle", "edge_edge", "island",
-                    "self_apply", "copy")
+                    "self_apply", "copy", "pcg", "stretch_caps")
 
     def profile_frame(self, substeps: int, iterations: int) -> dict:
         n = len(self.KERNEL_KINDS)
