@@ -53,10 +53,10 @@ __attribute__((visibility("default"))) long long xpbd_gb300_last_step_launches(v
 __attribute__((visibility("default"))) void* xpbd_gb300_stream(void* handle);
 
 /* Run one frame without graph capture, timing every launch with CUDA events
- * on the solver's stream; per kernel kind (14 kinds: predict, stretch pass,
+ * on the solver's stream; per kernel kind (16 kinds: predict, stretch pass,
  * other vertex pass, bend colour, vertex / triangle / edge hash, neighbour
- * table, VV, VT, EE, island, self apply, copy) write the summed milliseconds
- * and the launch count.  Advances the simulation by that frame. */
+ * table, VV, VT, EE, island, self apply, copy, CG solve, stretch caps) write
+ * the summed milliseconds and the launch count.  Advances the simulation by that frame. */
 __attribute__((visibility("default"))) int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations,
                                                                      float* kernel_ms, long long* kernel_launches, int kinds);
 
@@ -77,6 +77,45 @@ __attribute__((visibility("default"))) int xpbd_gb300_vertex_hash_noalloc(const 
                                                                            float cell_size, int bucket_count,
                                                                            int* bucket_start, int* bucket_entries,
                                                                            int* cells, void* stream);
+
+/* ---- Batched form (no counterpart in the reference) ----------------------
+ * One solver for `cloth_count` independent cloths, stepped together by
+ * ssbl_step_solver_ex: every launch of a frame covers all cloths and the
+ * frame is captured as one CUDA graph.  configs[k] / meshes[k] have the
+ * meaning of ssbl_create_solver's arguments (abi41.cu:8791); each cloth keeps
+ * its own parameters, pins, colliders and static SDF, and its results are
+ * the same bits as when it runs alone.  Hard stretch optimisation (the CG
+ * path) is accepted only for cloth_count == 1.  The handle is accepted by
+ * every ABI41 entry point, which then addresses all cloths: positions are
+ * concatenated in cloth order, pin indices run over the concatenated
+ * vertices, colliders and static triangles apply to every cloth, and the
+ * diagnostics are sums over the cloths.  Destroy with ssbl_destroy_solver. */
+__attribute__((visibility("default"))) void* xpbd_gb300_batch_create(const SsblXpbdConfig* configs,
+                                                                      const SsblXpbdMesh* meshes, int cloth_count);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_cloth_count(void* handle);
+/* out4 = first vertex, vertex count, first edge, edge count of the cloth. */
+__attribute__((visibility("default"))) int xpbd_gb300_batch_cloth_range(void* handle, int cloth, int* out4);
+/* Per-cloth forms of ssbl_update_pin_targets (indices local to the cloth),
+ * ssbl_update_runtime_colliders, ssbl_update_static_triangles,
+ * ssbl_update_frame_inputs, ssbl_update_positions, ssbl_download_positions
+ * and ssbl_reset_solver. */
+__attribute__((visibility("default"))) int xpbd_gb300_batch_update_pin_targets(void* handle, int cloth, const int* indices,
+                                                                                const float* positions, const float* weights,
+                                                                                int count);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_update_runtime_colliders(void* handle, int cloth,
+                                                                                      const SsblXpbdRuntimeColliders* colliders);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_update_static_triangles(void* handle, int cloth,
+                                                                                     const float* triangles, int triangle_count);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_update_frame_inputs(void* handle, int cloth,
+                                                                                 const SsblXpbdFrameInputs* inputs);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_update_positions(void* handle, int cloth, const float* positions,
+                                                                              int max_floats);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_download_positions(void* handle, int cloth, float* out,
+                                                                                int max_floats);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_reset_cloth(void* handle, int cloth);
+/* An inactive cloth is skipped by every kernel (its state stays as it is)
+ * until it is activated again. */
+__attribute__((visibility("default"))) int xpbd_gb300_batch_set_active(void* handle, int cloth, int active);
 
 /* Wait for the solver's stream. */
 __attribute__((visibility("default"))) int xpbd_gb300_synchronize(void* handle);

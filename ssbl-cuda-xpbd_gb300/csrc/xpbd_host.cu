@@ -1,0 +1,1331 @@
+// Solver creation (CSR builds, hash sizing, static SDF), cloth-level
+// updates and the per-frame launch schedule of the GB300 XPBD library.
+//
+// A solver holds one or more cloths concatenated in its device arrays (the
+// layout is described in xpbd_host.cuh).  The schedule below is the
+// reference's single-cloth schedule (native/src/ssbl_xpbd_cuda_abi41.cu:
+// 9165-9376); every kernel reads the parameters of the cloth its item belongs
+// to, so a cloth stepped inside a batch follows exactly the sequence of
+// per-vertex operations it follows alone and its results are the same bits.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+
+#include "xpbd_host.cuh"
+
+namespace xg {
+namespace host {
+
+thread_local std::string g_error;
+
+namespace {
+
+constexpr int kInvalid = -1;  // index outside its cloth: invalid in every kernel
+
+// Vertex -> constraint CSR: for each vertex the incident constraints in
+// increasing constraint index, tagged with the vertex's side (bit 31 set when
+// the vertex is the constraint's second endpoint).
+void build_pair_csr(int V, const std::vector<int2>& pairs, const std::vector<float>& rest, std::vector<int>* off,
+                    std::vector<int2>* ent) {
+    off->assign(V + 1, 0);
+    for (const int2& p : pairs) {
+        if (p.x < 0 || p.y < 0 || p.x >= V || p.y >= V || p.x == p.y) continue;
+        (*off)[p.x + 1]++;
+        (*off)[p.y + 1]++;
+    }
+    for (int i = 0; i < V; ++i) (*off)[i + 1] += (*off)[i];
+    ent->assign((*off)[V], make_int2(0, 0));
+    std::vector<int> cur(off->begin(), off->end() - 1);
+    for (size_t k = 0; k < pairs.size(); ++k) {
+        const int2 p = pairs[k];
+        if (p.x < 0 || p.y < 0 || p.x >= V || p.y >= V || p.x == p.y) continue;
+        int bits;
+        std::memcpy(&bits, &rest[k], 4);
+        (*ent)[cur[p.x]++] = make_int2(p.y, bits);
+        (*ent)[cur[p.y]++] = make_int2(p.x | kSideBit, bits);
+    }
+}
+
+// Closed-mesh test for the SDF sign: weld vertices on a 1e-6 grid and require
+// every undirected edge to have exactly two incident triangles
+// (abi41.cu:6026-6063).
+struct QKey {
+    long long x, y, z;
+    bool operator==(const QKey& o) const { return x == o.x && y == o.y && z == o.z; }
+};
+struct QKeyHash {
+    size_t operator()(const QKey& k) const {
+        uint64_t h = (uint64_t)k.x * 0x9E3779B97F4A7C15ull;
+        h ^= (uint64_t)k.y + 0x632BE59BD9B4E019ull + (h << 6) + (h >> 2);
+        h ^= (uint64_t)k.z + 0x85EBCA77C2B2AE63ull + (h << 6) + (h >> 2);
+        return (size_t)h;
+    }
+};
+
+bool mesh_is_closed(const float* tris, int count) {
+    if (!tris || count <= 0) return false;
+    std::unordered_map<QKey, int, QKeyHash> ids;
+    std::unordered_map<uint64_t, int> edges;
+    auto vid = [&](const float* v) {
+        const QKey k{std::llround((double)v[0] * 1000000.0), std::llround((double)v[1] * 1000000.0),
+                     std::llround((double)v[2] * 1000000.0)};
+        auto it = ids.find(k);
+        if (it != ids.end()) return it->second;
+        const int id = (int)ids.size();
+        ids.emplace(k, id);
+        return id;
+    };
+    auto ekey = [](int a, int b) {
+        const unsigned lo = (unsigned)std::min(a, b), hi = (unsigned)std::max(a, b);
+        return ((uint64_t)lo << 32) | hi;
+    };
+    for (int t = 0; t < count; ++t) {
+        const float* p = tris + t * 9;
+        for (int k = 0; k < 9; ++k)
+            if (!std::isfinite(p[k])) return false;
+        const int a = vid(p), b = vid(p + 3), c = vid(p + 6);
+        if (a == b || b == c || c == a) continue;
+        edges[ekey(a, b)] += 1;
+        edges[ekey(b, c)] += 1;
+        edges[ekey(c, a)] += 1;
+    }
+    if (edges.empty()) return false;
+    for (const auto& e : edges)
+        if (e.second != 2) return false;
+    return true;
+}
+
+// Number of bending wings: triangle pairs on an edge with distinct opposite
+// vertices (abi41.cu:7193-7302).  Reported in the diagnostics only.
+int count_wings(int V, const std::vector<int4>& tris, size_t begin, size_t end) {
+    std::unordered_map<uint64_t, int> first_opposite;
+    int wings = 0;
+    for (size_t k = begin; k < end; ++k) {
+        const int4 t = tris[k];
+        const int ids[3] = {t.x, t.y, t.z};
+        if (t.x >= V || t.y >= V || t.z >= V) continue;
+        for (int e = 0; e < 3; ++e) {
+            const int x = ids[e], y = ids[(e + 1) % 3], opp = ids[(e + 2) % 3];
+            const uint64_t key = ((uint64_t)(unsigned)std::min(x, y) << 32) | (unsigned)std::max(x, y);
+            auto it = first_opposite.find(key);
+            if (it == first_opposite.end()) {
+                first_opposite.emplace(key, opp);
+            } else if (it->second != opp) {
+                ++wings;
+            }
+        }
+    }
+    return wings;
+}
+
+float self_radius(const SsblXpbdConfig& c) {
+    const float req = std::max(c.self_collision_distance, 0.0f);
+    if (req > 0.0f) return req;
+    return std::max(std::max(c.cloth_thickness, c.collision_margin), 0.0f);
+}
+
+// Soft-pin relaxation 1 - (1 - clamp(w / 0.75))^(1/(I+1)) (abi41.cu:3466-3477).
+float pin_soft_relaxation(float weight, float exponent) {
+    if (!std::isfinite(weight) || weight < 0.05f) return 0.0f;
+    const float total = std::min(std::max(weight / 0.75f, 0.0f), 1.0f);
+    if (total >= 1.0f) return 1.0f;
+    const float remaining = std::max(1.0f - total, 0.0f);
+    const float relax = 1.0f - std::pow(remaining, std::max(exponent, 1.0e-4f));
+    return std::isfinite(relax) ? std::min(std::max(relax, 0.0f), 1.0f) : total;
+}
+
+// Config sanitising of ssbl_create_solver (abi41.cu:8791-8840).
+void sanitize(SsblXpbdConfig& c) {
+    c.vertex_count = std::max(c.vertex_count, 0);
+    c.edge_count = std::max(c.edge_count, 0);
+    c.bend_count = std::max(c.bend_count, 0);
+    c.lra_count = std::max(c.lra_count, 0);
+    c.triangle_count = std::max(c.triangle_count, 0);
+    c.damping = std::isfinite(c.damping) ? std::max(0.0f, std::min(c.damping, 1.0f)) : 1.0f;
+    if (!std::isfinite(c.bend_compliance) || c.bend_compliance < 0.0f) c.bend_compliance = 0.0f;
+    if (!std::isfinite(c.lra_compliance) || c.lra_compliance < 0.0f) c.lra_compliance = 0.0f;
+    if (!std::isfinite(c.stretch_optimization_strength)) c.stretch_optimization_strength = 0.0f;
+    c.stretch_optimization_strength = std::min(std::max(c.stretch_optimization_strength, 0.0f), 1.0f);
+    c.stretch_optimization_enabled =
+        (c.edge_count > 0 && c.stretch_optimization_enabled && c.stretch_optimization_strength > 0.0f) ? 1 : 0;
+}
+
+void load_colliders(Params& P, const SsblXpbdRuntimeColliders& c) {
+    P.use_ground = c.use_ground;
+    P.ground_height = c.ground_height;
+    P.use_wall = c.use_wall;
+    std::memcpy(P.wall_origin, c.wall_origin, sizeof(P.wall_origin));
+    std::memcpy(P.wall_normal, c.wall_normal, sizeof(P.wall_normal));
+    P.use_sphere = c.use_sphere;
+    std::memcpy(P.sphere_center, c.sphere_center, sizeof(P.sphere_center));
+    P.sphere_radius = c.sphere_radius;
+}
+
+// Greedy first-fit edge colouring in edge order (used for the hard-stretch
+// caps when the caller gives no colouring).
+void greedy_edge_colors(int V, const std::vector<int2>& springs, std::vector<int>* offsets, std::vector<int>* order) {
+    const int E = (int)springs.size();
+    std::vector<int> color(E, 0);
+    std::vector<std::vector<int>> used(V);
+    int ncol = 0;
+    for (int e = 0; e < E; ++e) {
+        const int a = springs[e].x, b = springs[e].y;
+        int k = 0;
+        auto taken = [&](int v, int col) {
+            return v >= 0 && v < V && std::find(used[v].begin(), used[v].end(), col) != used[v].end();
+        };
+        while (taken(a, k) || taken(b, k)) ++k;
+        color[e] = k;
+        if (a >= 0 && a < V) used[a].push_back(k);
+        if (b >= 0 && b < V) used[b].push_back(k);
+        ncol = std::max(ncol, k + 1);
+    }
+    offsets->assign(ncol + 1, 0);
+    for (int e = 0; e < E; ++e) (*offsets)[color[e] + 1]++;
+    for (int k = 0; k < ncol; ++k) (*offsets)[k + 1] += (*offsets)[k];
+    std::vector<int> cursor(offsets->begin(), offsets->end() - 1);
+    order->assign(E, 0);
+    for (int e = 0; e < E; ++e) (*order)[cursor[color[e]]++] = e;
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+View Solver::view() const {
+    View v{};
+    v.P = dp;
+    v.vcloth = vcloth;
+    v.ecloth = ecloth;
+    v.tcloth = tcloth;
+    v.nV = nV;
+    v.nE = nE;
+    v.nT = nT;
+    v.nB = bend_colors.empty() ? 0 : bend_colors.back();
+    v.K = K;
+    v.substep = 0;
+    v.substeps = 1;
+    v.pass = -1;
+    v.last_it = 1;
+    v.pos_in = pos[0];
+    v.pos = pos[0];
+    v.prev = prev;
+    v.vel = vel;
+    v.rest = rest;
+    v.inv_mass = inv_mass;
+    v.sp_off = sp_off;
+    v.sp_ent = sp_ent;
+    v.te_off = te_off;
+    v.te_ent = te_ent;
+    v.bj_off = bj_off;
+    v.bj_ent = bj_ent;
+    v.bends = bends;
+    v.bend_rest = bend_rest;
+    v.tris = tris;
+    v.edges = edges;
+    v.edge_rest = edge_rest;
+    v.pin_target = pin_target;
+    v.pin_weight = pin_weight;
+    v.pin_relax = pin_relax;
+    v.counts = counts;
+    v.vcell = vcell;
+    v.vb_count = vb_count;
+    v.vb_start = vb_start;
+    v.vb_ent = vb_ent;
+    v.tb_count = tb_count;
+    v.tb_start = tb_start;
+    v.tb_ent = tb_ent;
+    v.eb_count = eb_count;
+    v.eb_start = eb_start;
+    v.eb_ent = eb_ent;
+    v.nb_count = nb_count;
+    v.nb_idx = nb_idx;
+    v.scan_tmp = scan_tmp;
+    v.acc = acc;
+    v.max_delta_bits = max_delta_bits;
+    return v;
+}
+
+void Solver::drop_graphs() {
+    for (auto& g : graphs)
+        if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    graphs.clear();
+}
+
+void free_solver(Solver* S) {
+    if (!S) return;
+    if (S->stream) cudaStreamSynchronize(S->stream);
+    S->drop_graphs();
+    for (Cloth& c : S->cl) {
+        dfree(c.sdf);
+        dfree(c.static_tris);
+    }
+    dfree(S->dp);
+    dfree(S->vcloth);
+    dfree(S->ecloth);
+    dfree(S->tcloth);
+    dfree(S->pos[0]);
+    dfree(S->pos[1]);
+    dfree(S->prev);
+    dfree(S->vel);
+    dfree(S->rest);
+    dfree(S->inv_mass);
+    dfree(S->sp_off);
+    dfree(S->sp_ent);
+    dfree(S->te_off);
+    dfree(S->te_ent);
+    dfree(S->bj_off);
+    dfree(S->bj_ent);
+    dfree(S->bends);
+    dfree(S->bend_rest);
+    dfree(S->tris);
+    dfree(S->edges);
+    dfree(S->edge_rest);
+    dfree(S->pin_target);
+    dfree(S->pin_weight);
+    dfree(S->pin_relax);
+    dfree(S->counts);
+    dfree(S->max_delta_bits);
+    dfree(S->pack);
+    dfree(S->vcell);
+    dfree(S->vb_count);
+    dfree(S->vb_start);
+    dfree(S->vb_ent);
+    dfree(S->tb_count);
+    dfree(S->tb_start);
+    dfree(S->tb_ent);
+    dfree(S->eb_count);
+    dfree(S->eb_start);
+    dfree(S->eb_ent);
+    dfree(S->nb_count);
+    dfree(S->nb_idx);
+    dfree(S->acc);
+    dfree(S->scan_tmp);
+    PcgView& g = S->pcg;
+    dfree(g.diag);
+    dfree(g.pinv);
+    dfree(g.r);
+    dfree(g.z);
+    dfree(g.d);
+    dfree(g.q);
+    dfree(g.offdiag);
+    dfree(g.avg);
+    dfree(g.red);
+    dfree(g.partials);
+    dfree(g.ticket);
+    dfree(g.guard);
+    dfree(g.max_delta_bits);
+    dfree(S->cap_edges);
+    dfree(S->cap_rest);
+    if (S->stream) cudaStreamDestroy(S->stream);
+    delete S;
+}
+
+bool sync_params(Solver* S) {
+    if (!S->params_dirty) return true;
+    if (!cuda_ok(cudaMemcpyAsync(S->dp, S->hp.data(), sizeof(Params) * S->K, cudaMemcpyHostToDevice, S->stream),
+                 "upload solver parameters"))
+        return false;
+    S->params_dirty = false;
+    return true;
+}
+
+namespace {
+
+bool upload_pin_relax(Solver* S, int iterations) {
+    if (S->pin_relax_iterations == iterations) return true;
+    const float exponent = 1.0f / (float)std::max(iterations + 1, 1);
+    for (int i = 0; i < S->nV; ++i) S->h_pin_relax[i] = pin_soft_relaxation(S->h_pin_weight[i], exponent);
+    if (!dupload(S->pin_relax, S->h_pin_relax.data(), S->nV, S->stream, "pin relaxation upload")) return false;
+    S->pin_relax_iterations = iterations;
+    return true;
+}
+
+// Static SDF of one cloth: grid sizing (abi41.cu:6123-6218) and the device
+// build.
+bool build_static_sdf(Solver* S, int k, const float* tris, int count) {
+    Params& P = S->hp[k];
+    Cloth& C = S->cl[k];
+    P.sdf_ready = 0;
+    P.sdf_dim[0] = P.sdf_dim[1] = P.sdf_dim[2] = 0;
+    P.sdf_origin[0] = P.sdf_origin[1] = P.sdf_origin[2] = 0.0f;
+    P.sdf_voxel = 0.0f;
+    P.sdf_signed = 0;
+    P.static_tri_count = std::max(count, 0);
+    S->params_dirty = true;
+    C.sdf_build_ms = 0.0f;
+    if (count <= 0) return true;
+    if (!tris) return fail("static triangle data is required for SDF build");
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int q = 0; q < count * 3; ++q) {
+        const float* v = tris + q * 3;
+        if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2]))
+            return fail("static triangle data contains non-finite coordinates");
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], v[a]);
+            hi[a] = std::max(hi[a], v[a]);
+        }
+    }
+    const SsblXpbdConfig& c = C.cfg;
+    float voxel = (std::isfinite(c.static_sdf_voxel_size) && c.static_sdf_voxel_size > 0.0f)
+                      ? c.static_sdf_voxel_size
+                      : std::max(std::max(c.collision_margin, 0.0f) * 0.5f, 0.002f);
+    const int band = std::max(c.static_sdf_band_voxels > 0 ? c.static_sdf_band_voxels : 4, 1);
+    const int max_res = std::max(c.static_sdf_max_resolution > 0 ? c.static_sdf_max_resolution : 160, 16);
+    const float margin = std::max(c.collision_margin, 0.0f);
+    const float expand = margin + (float)band * voxel + voxel * 2.0f;
+    float ext[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = lo[a] - expand;
+        hi[a] = hi[a] + expand;
+        ext[a] = std::max(hi[a] - lo[a], voxel);
+    }
+    const float largest = std::max(ext[0], std::max(ext[1], ext[2]));
+    if (largest / voxel + 1.0f > (float)max_res) voxel = largest / (float)std::max(max_res - 1, 1);
+    voxel = std::max(voxel, 1.0e-5f);
+    int dim[3];
+    for (int a = 0; a < 3; ++a) dim[a] = std::min(std::max((int)std::ceil(ext[a] / voxel) + 1, 2), max_res);
+    const long long voxels_ll = (long long)dim[0] * dim[1] * dim[2];
+    if (voxels_ll <= 0 || voxels_ll > 0x7fffffffll) return fail("static SDF grid is too large");
+    const int voxels = (int)voxels_ll;
+    if (voxels > C.sdf_capacity) {
+        if (!cuda_ok(cudaStreamSynchronize(S->stream), "static SDF reallocation")) return false;
+        dfree(C.sdf);
+        C.sdf_capacity = 0;
+        if (!dalloc(&C.sdf, voxels, "static SDF allocation")) return false;
+        C.sdf_capacity = voxels;
+    }
+    if (count > C.static_capacity) {
+        if (!cuda_ok(cudaStreamSynchronize(S->stream), "static triangle reallocation")) return false;
+        dfree(C.static_tris);
+        C.static_capacity = 0;
+        if (!dalloc(&C.static_tris, (size_t)count * 3, "static triangle upload")) return false;
+        C.static_capacity = count;
+    }
+    std::vector<float4> t4((size_t)count * 3);
+    for (int q = 0; q < count * 3; ++q) t4[q] = make_float4(tris[q * 3], tris[q * 3 + 1], tris[q * 3 + 2], 0.0f);
+    if (!dupload(C.static_tris, t4.data(), t4.size(), S->stream, "static triangle upload")) return false;
+    for (int a = 0; a < 3; ++a) {
+        P.sdf_dim[a] = dim[a];
+        P.sdf_origin[a] = lo[a];
+    }
+    P.sdf_voxel = voxel;
+    P.sdf = C.sdf;
+    P.static_tris = C.static_tris;
+    P.sdf_signed = mesh_is_closed(tris, count) ? 1 : 0;
+    if (!P.sdf_signed) C.sdf_unsigned += 1;
+    if (!sync_params(S)) return false;
+    launch_sdf_build(S->view(), k, voxels, S->stream);
+    if (!cuda_ok(cudaGetLastError(), "build static SDF") || !cuda_ok(cudaStreamSynchronize(S->stream), "sync static SDF build"))
+        return false;
+    P.sdf_ready = 1;
+    S->params_dirty = true;
+    C.sdf_rebuilds += 1;
+    C.sdf_build_ms = (float)ms_since(t0);
+    return true;
+}
+
+struct Range {
+    int lo, hi;
+};
+
+Range cloth_range(const Solver* S, int cloth) {
+    if (cloth < 0) return Range{0, S->nV};
+    return Range{S->hp[cloth].vstart, S->hp[cloth].vstart + S->hp[cloth].V};
+}
+
+bool valid_cloth(const Solver* S, int cloth) { return S && cloth < S->K; }
+
+}  // namespace
+
+// Static SDF fields of the diagnostics block (abi41.cu:6105-6121), summed
+// over the cloths; the grid shape is the first cloth's with a grid.
+void sdf_diagnostics(Solver* S) {
+    SsblXpbdDiagnostics& d = S->diag;
+    d.static_triangle_count = 0;
+    d.static_sdf_rebuild_count = 0;
+    d.static_sdf_unsigned_fallback_count = 0;
+    d.static_sdf_build_ms = 0.0f;
+    d.static_sdf_grid_x = d.static_sdf_grid_y = d.static_sdf_grid_z = 0;
+    d.static_sdf_voxel_count = 0;
+    bool shaped = false;
+    for (int k = 0; k < S->K; ++k) {
+        const Params& P = S->hp[k];
+        const Cloth& C = S->cl[k];
+        d.static_triangle_count += P.static_tri_count;
+        d.static_sdf_rebuild_count += C.sdf_rebuilds;
+        d.static_sdf_unsigned_fallback_count += C.sdf_unsigned;
+        d.static_sdf_build_ms += C.sdf_build_ms;
+        if (!shaped && (P.sdf_ready || k == S->K - 1)) {
+            d.static_sdf_grid_x = P.sdf_dim[0];
+            d.static_sdf_grid_y = P.sdf_dim[1];
+            d.static_sdf_grid_z = P.sdf_dim[2];
+            shaped = P.sdf_ready != 0;
+        }
+        d.static_sdf_voxel_count += P.sdf_ready ? (long long)P.sdf_dim[0] * P.sdf_dim[1] * P.sdf_dim[2] : 0;
+    }
+    if (!shaped && S->K > 0) {
+        d.static_sdf_grid_x = S->hp[0].sdf_dim[0];
+        d.static_sdf_grid_y = S->hp[0].sdf_dim[1];
+        d.static_sdf_grid_z = S->hp[0].sdf_dim[2];
+    }
+}
+
+bool upload_static(Solver* S, int cloth, const float* tris, int count) {
+    if (!valid_cloth(S, cloth)) return fail("invalid static triangle update");
+    count = std::max(count, 0);
+    if (count > 0 && !tris) return fail("static triangle data is required when triangle count is nonzero");
+    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
+    bool ok = true;
+    for (int k = k0; k < k1 && ok; ++k) {
+        S->cl[k].cfg.static_triangle_count = count;
+        ok = build_static_sdf(S, k, tris, count);
+    }
+    sdf_diagnostics(S);
+    return ok;
+}
+
+bool upload_pins(Solver* S, int cloth, const int* indices, const float* positions, const float* weights, int count) {
+    if (!valid_cloth(S, cloth)) return fail("invalid solver handle");
+    if (count < 0) return fail("invalid pin count");
+    if (count > 0 && (!indices || !positions)) return fail("pin arrays are required when pin count is nonzero");
+    const Range r = cloth_range(S, cloth);
+    std::fill(S->h_pin_weight.begin() + r.lo, S->h_pin_weight.begin() + r.hi, -1.0f);
+    for (int k = 0; k < count; ++k) {
+        const int i = r.lo + indices[k];
+        if (indices[k] < 0 || i >= r.hi) continue;
+        S->h_pin_weight[i] = weights ? weights[k] : 1.0f;
+        S->h_pin_target[i] = make_float4(positions[k * 3 + 0], positions[k * 3 + 1], positions[k * 3 + 2], 0.0f);
+    }
+    if (cloth >= 0)
+        S->cl[cloth].pin_count = count;
+    else if (S->K == 1)
+        S->cl[0].pin_count = count;
+    S->pin_relax_iterations = -1;
+    const int n = r.hi - r.lo;
+    return dupload(S->pin_weight + r.lo, S->h_pin_weight.data() + r.lo, n, S->stream, "pin weight upload") &&
+           dupload(S->pin_target + r.lo, S->h_pin_target.data() + r.lo, n, S->stream, "pin target upload") &&
+           cuda_ok(cudaStreamSynchronize(S->stream), "pin upload");
+}
+
+bool set_colliders(Solver* S, int cloth, const SsblXpbdRuntimeColliders& c) {
+    if (!valid_cloth(S, cloth)) return fail("invalid runtime collider update");
+    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
+    for (int k = k0; k < k1; ++k) {
+        S->cl[k].colliders = c;
+        load_colliders(S->hp[k], c);
+    }
+    S->params_dirty = true;
+    return true;
+}
+
+bool upload_positions(Solver* S, int cloth, const float* positions, int max_floats) {
+    if (!valid_cloth(S, cloth) || !positions) return fail("invalid position upload");
+    const Range r = cloth_range(S, cloth);
+    const int n = r.hi - r.lo;
+    if (max_floats < n * 3) return fail("invalid position upload");
+    std::vector<float4> p4(n);
+    for (int i = 0; i < n; ++i)
+        p4[i] = make_float4(positions[i * 3], positions[i * 3 + 1], positions[i * 3 + 2], S->h_w[r.lo + i]);
+    return dupload(S->pos[0] + r.lo, p4.data(), n, S->stream, "upload positions") &&
+           dupload(S->prev + r.lo, p4.data(), n, S->stream, "upload previous positions") &&
+           cuda_ok(cudaStreamSynchronize(S->stream), "upload positions");
+}
+
+bool download_positions(Solver* S, int cloth, float* out, int max_floats) {
+    if (!valid_cloth(S, cloth) || !out) return fail("invalid position download");
+    const Range r = cloth_range(S, cloth);
+    const int n = r.hi - r.lo;
+    if (max_floats < n * 3) return fail("invalid position download");
+    launch_pack_positions(S->pack + 3ll * r.lo, S->pos[0] + r.lo, n, S->stream);
+    return cuda_ok(cudaGetLastError(), "pack positions") &&
+           cuda_ok(cudaMemcpyAsync(out, S->pack + 3ll * r.lo, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, S->stream),
+                   "download ABI41 positions") &&
+           cuda_ok(cudaStreamSynchronize(S->stream), "download ABI41 positions");
+}
+
+bool reset_cloths(Solver* S, int cloth) {
+    if (!valid_cloth(S, cloth)) return fail("invalid solver handle");
+    const Range r = cloth_range(S, cloth);
+    const size_t n = (size_t)(r.hi - r.lo);
+    if (!cuda_ok(cudaMemcpyAsync(S->pos[0] + r.lo, S->rest + r.lo, sizeof(float4) * n, cudaMemcpyDeviceToDevice, S->stream),
+                 "reset positions") ||
+        !cuda_ok(cudaMemcpyAsync(S->prev + r.lo, S->rest + r.lo, sizeof(float4) * n, cudaMemcpyDeviceToDevice, S->stream),
+                 "reset previous positions") ||
+        !cuda_ok(cudaMemsetAsync(S->vel + r.lo, 0, sizeof(float4) * n, S->stream), "reset velocities") ||
+        !cuda_ok(cudaMemsetAsync(S->counts, 0, sizeof(unsigned long long) * kCntSlots, S->stream), "reset ABI41 diagnostics") ||
+        !cuda_ok(cudaStreamSynchronize(S->stream), "reset solver"))
+        return false;
+    S->diag = SsblXpbdDiagnostics{};
+    S->diag.finite_flag = 1;
+    return true;
+}
+
+bool set_active(Solver* S, int cloth, bool active) {
+    if (!valid_cloth(S, cloth)) return fail("invalid cloth index");
+    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
+    for (int k = k0; k < k1; ++k) S->hp[k].active = active ? 1 : 0;
+    S->params_dirty = true;
+    return true;
+}
+
+// ------------------------------------------------------------ creation --
+
+Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes, int K) {
+    if (!configs || !meshes || K < 1) {
+        fail("invalid ABI41 solver create request");
+        return nullptr;
+    }
+    Solver* S = new Solver();
+    S->K = K;
+    S->cl.resize(K);
+    S->hp.assign(K, Params{});
+    auto bail = [&](int k, const std::string& msg) -> Solver* {
+        if (!msg.empty()) fail(K > 1 ? "batch cloth " + std::to_string(k) + ": " + msg : msg);
+        free_solver(S);
+        return nullptr;
+    };
+
+    // Per-cloth validation and ranges in the concatenated arrays.
+    long long tv = 0, te = 0, tt = 0, tl = 0;
+    for (int k = 0; k < K; ++k) {
+        const SsblXpbdConfig* config = &configs[k];
+        const SsblXpbdMesh* mesh = &meshes[k];
+        if (config->vertex_count < 0 || config->edge_count < 0 || config->triangle_count < 0 || !std::isfinite(config->dt) ||
+            !(config->dt > 0.0f) || !mesh->positions || !mesh->inv_mass)
+            return bail(k, "invalid ABI41 solver create request");
+        Cloth& C = S->cl[k];
+        SsblXpbdConfig& c = C.cfg;
+        c = *config;
+        sanitize(c);
+        if (c.use_volume_pressure && c.pressure_strength > 0.0f)
+            return bail(k, "volume pressure is not supported by this build of the GB300 solver");
+        if (K > 1 && c.stretch_optimization_enabled)
+            return bail(k, "hard stretch optimization runs on one-cloth solvers only");
+        if (c.bend_count > 0 && (!mesh->bends || !mesh->bend_rest_lengths))
+            return bail(k, "ABI41 bend constraints require bend pairs and rest lengths");
+        if (c.lra_count > 0 && (!mesh->lra_edges || !mesh->lra_rest_lengths))
+            return bail(k, "ABI41 LRA constraints require edge pairs and rest lengths");
+        if (c.edge_color_count > 0) {
+            if (!mesh->edge_color_offsets) return bail(k, "ABI41 edge color offsets are required");
+            C.edge_colors.assign(mesh->edge_color_offsets, mesh->edge_color_offsets + c.edge_color_count + 1);
+        }
+        if (c.bend_color_count > 0) {
+            if (!mesh->bend_color_offsets) return bail(k, "ABI41 bend color offsets are required");
+            C.bend_colors.assign(mesh->bend_color_offsets, mesh->bend_color_offsets + c.bend_color_count + 1);
+        }
+        C.colliders.use_ground = c.use_ground;
+        C.colliders.ground_height = c.ground_height;
+        C.colliders.use_wall = c.use_wall;
+        std::memcpy(C.colliders.wall_origin, c.wall_origin, sizeof(c.wall_origin));
+        std::memcpy(C.colliders.wall_normal, c.wall_normal, sizeof(c.wall_normal));
+        C.colliders.use_sphere = c.use_sphere;
+        std::memcpy(C.colliders.sphere_center, c.sphere_center, sizeof(c.sphere_center));
+        C.colliders.sphere_radius = c.sphere_radius;
+        Params& P = S->hp[k];
+        P.vstart = (int)tv;
+        P.estart = (int)te;
+        P.tstart = (int)tt;
+        P.V = c.vertex_count;
+        P.E = c.edge_count;
+        P.T = c.triangle_count;
+        P.B = c.bend_count;
+        P.L = c.lra_count;
+        tv += P.V;
+        te += P.E;
+        tt += P.T;
+        tl += P.L;
+    }
+    if (tv > (1 << 30) || te > (1 << 30) || tt > (1 << 30) || tl > (1 << 30)) return bail(0, "batch is too large");
+    S->nV = (int)tv;
+    S->nE = (int)te;
+    S->nT = (int)tt;
+    S->nL = (int)tl;
+    const int nV = S->nV, nE = S->nE, nT = S->nT;
+
+    if (!cuda_ok(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking), "create solver stream")) return bail(0, "");
+
+    // Concatenated host arrays; indices outside their cloth become -1.
+    S->h_inv.resize(nV);
+    S->h_w.resize(nV);
+    std::vector<float4> rest4(nV), zero4(nV, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    std::vector<int2> springs(nE), tethers(S->nL), jbends;
+    std::vector<float> spring_rest(nE), tether_rest(S->nL), jbend_rest;
+    std::vector<int4> tris(nT);
+    std::vector<int> vmap, emap, tmap;
+    if (K > 1) {
+        vmap.resize(nV);
+        emap.resize(nE);
+        tmap.resize(nT);
+    }
+    int max_colors = 0;
+    for (int k = 0; k < K; ++k) max_colors = std::max(max_colors, (int)S->cl[k].bend_colors.size() - 1);
+    std::vector<std::vector<int2>> color_bends(std::max(max_colors, 0));
+    std::vector<std::vector<float>> color_rest(std::max(max_colors, 0));
+    int lpos = 0;
+    for (int k = 0; k < K; ++k) {
+        const SsblXpbdMesh* mesh = &meshes[k];
+        Cloth& C = S->cl[k];
+        const SsblXpbdConfig& c = C.cfg;
+        const Params& P = S->hp[k];
+        const int V = P.V, E = P.E, T = P.T, B = P.B, L = P.L, vs = P.vstart;
+        auto gidx = [&](int i) { return (i >= 0 && i < V) ? vs + i : kInvalid; };
+        for (int i = 0; i < V; ++i) {
+            const float im = mesh->inv_mass[i];
+            S->h_inv[vs + i] = im;
+            S->h_w[vs + i] = im > 0.0f ? im : 0.0f;
+            rest4[vs + i] = make_float4(mesh->positions[i * 3], mesh->positions[i * 3 + 1], mesh->positions[i * 3 + 2], S->h_w[vs + i]);
+            if (K > 1) vmap[vs + i] = k;
+        }
+        for (int e = 0; e < E; ++e) {
+            const int i = mesh->edges ? mesh->edges[e * 2] : 0, j = mesh->edges ? mesh->edges[e * 2 + 1] : 0;
+            springs[P.estart + e] = make_int2(gidx(std::max(i, 0)), gidx(std::max(j, 0)));
+            spring_rest[P.estart + e] = mesh->edge_rest_lengths ? mesh->edge_rest_lengths[e] : 0.0f;
+            if (K > 1) emap[P.estart + e] = k;
+        }
+        for (int q = 0; q < L; ++q) {
+            tethers[lpos + q] = make_int2(gidx(mesh->lra_edges[q * 2]), gidx(mesh->lra_edges[q * 2 + 1]));
+            tether_rest[lpos + q] = mesh->lra_rest_lengths[q];
+        }
+        lpos += L;
+        if (B > 0 && C.bend_colors.empty()) {
+            for (int q = 0; q < B; ++q) {
+                jbends.push_back(make_int2(gidx(mesh->bends[q * 2]), gidx(mesh->bends[q * 2 + 1])));
+                jbend_rest.push_back(mesh->bend_rest_lengths[q]);
+            }
+            S->jacobi_bends = true;
+        } else if (B > 0) {
+            // bends of colour j: the caller's range [off_j, off_j+1), clipped
+            // to the cloth's bends
+            for (size_t j = 0; j + 1 < C.bend_colors.size(); ++j) {
+                const int b0 = std::max(C.bend_colors[j], 0), b1 = std::min(C.bend_colors[j + 1], B);
+                for (int q = b0; q < b1; ++q) {
+                    color_bends[j].push_back(make_int2(gidx(mesh->bends[q * 2]), gidx(mesh->bends[q * 2 + 1])));
+                    color_rest[j].push_back(mesh->bend_rest_lengths[q]);
+                }
+            }
+        }
+        for (int t = 0; t < T; ++t) {
+            const int* tr = mesh->triangles ? mesh->triangles + t * 3 : nullptr;
+            const int a = tr ? std::max(tr[0], 0) : 0, b = tr ? std::max(tr[1], 0) : 0, cc = tr ? std::max(tr[2], 0) : 0;
+            tris[P.tstart + t] = make_int4(a, b, cc, 0);  // local for the wing count
+            if (K > 1) tmap[P.tstart + t] = k;
+        }
+        C.wing_count = T > 1 ? count_wings(V, tris, P.tstart, P.tstart + T) : 0;
+        for (int t = 0; t < T; ++t) {
+            int4& tr = tris[P.tstart + t];
+            tr = make_int4(gidx(tr.x), gidx(tr.y), gidx(tr.z), 0);
+        }
+        (void)c;
+    }
+    std::vector<int2> cbends;
+    std::vector<float> cbend_rest;
+    S->bend_colors.assign(1, 0);
+    for (int j = 0; j < max_colors; ++j) {
+        cbends.insert(cbends.end(), color_bends[j].begin(), color_bends[j].end());
+        cbend_rest.insert(cbend_rest.end(), color_rest[j].begin(), color_rest[j].end());
+        S->bend_colors.push_back((int)cbends.size());
+    }
+    if (cbends.empty()) S->bend_colors.clear();
+    S->nB = (int)cbends.size();
+
+    std::vector<int> sp_off, te_off, bj_off;
+    std::vector<int2> sp_ent, te_ent, bj_ent;
+    build_pair_csr(nV, springs, spring_rest, &sp_off, &sp_ent);
+    build_pair_csr(nV, tethers, tether_rest, &te_off, &te_ent);
+    if (S->jacobi_bends) build_pair_csr(nV, jbends, jbend_rest, &bj_off, &bj_ent);
+    S->h_pin_weight.assign(nV, -1.0f);
+    S->h_pin_target.assign(nV, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    S->h_pin_relax.assign(nV, 0.0f);
+
+    // Parameters and self-collision table sizes.
+    int wings = 0;
+    for (int k = 0; k < K; ++k) {
+        Cloth& C = S->cl[k];
+        const SsblXpbdConfig& c = C.cfg;
+        Params& P = S->hp[k];
+        P.active = 1;
+        P.sub_dt = c.dt;
+        P.damping = c.damping;
+        for (int a = 0; a < 3; ++a) P.gravity[a] = c.gravity[a];
+        P.stretch_compliance = c.stretch_compliance;
+        P.bend_compliance = c.bend_compliance;
+        P.lra_compliance = c.lra_compliance;
+        P.margin = c.collision_margin;
+        P.thickness = c.cloth_thickness;
+        P.friction = c.contact_friction;
+        P.tangent_damping = c.contact_tangent_damping;
+        load_colliders(P, C.colliders);
+        const float radius = self_radius(c);
+        P.self_radius = radius;
+        P.self_mode = c.self_collision_mode;
+        P.max_neighbors = c.max_self_collision_neighbors;
+        P.stretch_strength = c.stretch_optimization_strength;
+        C.self_enabled = c.self_collision != 0 && radius > 0.0f && P.V > 0;
+        C.interval = std::max(c.self_collision_interval, 1);
+        C.passes = std::max(1, std::min(c.fast_self_collision_passes, 8));
+        C.fast = c.self_collision_mode == 1;
+        C.order_buckets = C.fast || std::min(std::max(c.max_self_collision_neighbors, 1), 32) < 32;
+        P.self_on = C.self_enabled ? 1 : 0;
+        P.self_interval = C.interval;
+        P.self_passes = C.passes;
+        if (C.self_enabled) {
+            S->self_any = true;
+            const float cell = std::max(radius * 1.8f, 1.0e-3f);
+            P.vcell = P.tcell = P.ecell = cell;
+            P.vhash = P.V >= 128;
+            P.thash = P.T >= 64;
+            P.ehash = P.E >= 64;
+            P.vbuckets = P.vhash ? next_pow2(std::max(1024, P.V * 4)) : 0;
+            P.tbuckets = P.thash ? next_pow2(std::max(1024, P.T * 4)) : 0;
+            P.ebuckets = P.ehash ? next_pow2(std::max(1024, P.E * 4)) : 0;
+            if ((long long)S->nVB + P.vbuckets > (1ll << 30) || (long long)S->nTB + P.tbuckets > (1ll << 30) ||
+                (long long)S->nEB + P.ebuckets > (1ll << 30))
+                return bail(k, "self collision tables are too large");
+            P.vbase = S->nVB;
+            P.tbase = S->nTB;
+            P.ebase = S->nEB;
+            S->nVB += P.vbuckets;
+            S->nTB += P.tbuckets;
+            S->nEB += P.ebuckets;
+        }
+        wings += C.wing_count;
+    }
+    long long tri_entries = 0, edge_entries = 0;
+    for (int k = 0; k < K; ++k) {
+        if (S->hp[k].thash) tri_entries += (long long)S->hp[k].T * kMaxPrimitiveCells;
+        if (S->hp[k].ehash) edge_entries += (long long)S->hp[k].E * kMaxPrimitiveCells;
+    }
+    S->pcg_on = K == 1 && S->cl[0].cfg.stretch_optimization_enabled != 0;
+
+    bool ok = dalloc(&S->dp, K, "parameter allocation") && dalloc(&S->pos[0], nV, "position allocation") &&
+              dalloc(&S->pos[1], nV, "position allocation") && dalloc(&S->prev, nV, "previous position allocation") &&
+              dalloc(&S->vel, nV, "velocity allocation") && dalloc(&S->rest, nV, "rest position allocation") &&
+              dalloc(&S->inv_mass, nV, "inverse mass allocation") && dalloc(&S->sp_off, nV + 1, "spring CSR allocation") &&
+              dalloc(&S->sp_ent, sp_ent.size(), "spring CSR allocation") &&
+              dalloc(&S->te_off, nV + 1, "tether CSR allocation") && dalloc(&S->te_ent, te_ent.size(), "tether CSR allocation") &&
+              dalloc(&S->bends, cbends.size(), "bend pair allocation") &&
+              dalloc(&S->bend_rest, cbend_rest.size(), "bend rest allocation") && dalloc(&S->tris, nT, "triangle allocation") &&
+              dalloc(&S->edges, nE, "edge allocation") && dalloc(&S->edge_rest, nE, "edge rest allocation") &&
+              dalloc(&S->pin_target, nV, "pin target allocation") && dalloc(&S->pin_weight, nV, "pin weight allocation") &&
+              dalloc(&S->pin_relax, nV, "pin relaxation allocation") &&
+              dalloc(&S->counts, kCntSlots, "ABI41 diagnostic allocation") &&
+              dalloc(&S->max_delta_bits, 1, "self max smoothed delta allocation") &&
+              dalloc(&S->pack, (size_t)nV * 3, "download staging allocation");
+    if (ok && K > 1)
+        ok = dalloc(&S->vcloth, nV, "cloth map allocation") && dalloc(&S->ecloth, nE, "cloth map allocation") &&
+             dalloc(&S->tcloth, nT, "cloth map allocation");
+    if (ok && S->jacobi_bends)
+        ok = dalloc(&S->bj_off, nV + 1, "bend CSR allocation") && dalloc(&S->bj_ent, bj_ent.size(), "bend CSR allocation");
+    if (ok && S->self_any) {
+        ok = dalloc(&S->nb_count, nV, "self collision count allocation") &&
+             dalloc(&S->nb_idx, (size_t)nV * kNeighborSlots, "self collision index allocation") &&
+             dalloc(&S->acc, nV, "self accumulation allocation") &&
+             dalloc(&S->scan_tmp, (size_t)std::max(std::max(S->nVB, S->nTB), S->nEB) / 4096 + 2, "bucket scan allocation");
+        if (ok && S->nVB > 0)
+            ok = dalloc(&S->vcell, nV, "self collision cell allocation") &&
+                 dalloc(&S->vb_count, S->nVB, "self collision hash count allocation") &&
+                 dalloc(&S->vb_start, S->nVB + 1, "self collision hash start allocation") &&
+                 dalloc(&S->vb_ent, nV, "self collision hash index allocation");
+        if (ok && S->nTB > 0)
+            ok = dalloc(&S->tb_count, S->nTB, "self triangle hash count allocation") &&
+                 dalloc(&S->tb_start, S->nTB + 1, "self triangle hash start allocation") &&
+                 dalloc(&S->tb_ent, (size_t)tri_entries, "self triangle hash index allocation");
+        if (ok && S->nEB > 0)
+            ok = dalloc(&S->eb_count, S->nEB, "self edge hash count allocation") &&
+                 dalloc(&S->eb_start, S->nEB + 1, "self edge hash start allocation") &&
+                 dalloc(&S->eb_ent, (size_t)edge_entries, "self edge hash index allocation");
+    }
+    // Hard-stretch buffers (one-cloth solvers); the caps need edges grouped
+    // by colour: the caller's colouring when given (edges already sorted by
+    // colour), else a greedy first-fit colouring in edge order.
+    std::vector<int2> cap_edges;
+    std::vector<float> cap_rest;
+    if (ok && S->pcg_on) {
+        S->pcg_nnz = (int)sp_ent.size();
+        if (S->pcg_nnz == 0) return bail(0, "PCG stretch optimization found no valid CSR edges");
+        if (!S->cl[0].edge_colors.empty()) {
+            cap_edges = springs;
+            cap_rest = spring_rest;
+            S->cap_colors = S->cl[0].edge_colors;
+        } else {
+            std::vector<int> order;
+            greedy_edge_colors(nV, springs, &S->cap_colors, &order);
+            cap_edges.resize(nE);
+            cap_rest.resize(nE);
+            for (int e = 0; e < nE; ++e) {
+                cap_edges[e] = springs[order[e]];
+                cap_rest[e] = spring_rest[order[e]];
+            }
+        }
+        PcgView& g = S->pcg;
+        ok = dalloc(&g.diag, 2 * (size_t)nV, "PCG diagonal block allocation") &&
+             dalloc(&g.pinv, 2 * (size_t)nV, "PCG preconditioner allocation") && dalloc(&g.r, nV, "PCG residual allocation") &&
+             dalloc(&g.z, nV, "PCG preconditioned residual allocation") && dalloc(&g.d, nV, "PCG search direction allocation") &&
+             dalloc(&g.q, nV, "PCG A*d allocation") && dalloc(&g.offdiag, sp_ent.size(), "PCG offdiagonal allocation") &&
+             dalloc(&g.avg, nV, "stretch cap accumulation allocation") && dalloc(&g.red, kRedSlots, "PCG reduction allocation") &&
+             dalloc(&g.partials, pcg_warp_partials(nV), "PCG partial sum allocation") &&
+             dalloc(&g.ticket, 1, "PCG ticket allocation") && dalloc(&g.guard, 1, "PCG guard counter allocation") &&
+             dalloc(&g.max_delta_bits, 1, "PCG max delta allocation") && dalloc(&S->cap_edges, nE, "cap edge allocation") &&
+             dalloc(&S->cap_rest, nE, "cap rest allocation");
+    }
+    if (!ok) return bail(0, "");
+    cudaStream_t st = S->stream;
+    ok = dupload(S->pos[0], rest4.data(), nV, st, "position upload") && dupload(S->pos[1], rest4.data(), nV, st, "position upload") &&
+         dupload(S->prev, rest4.data(), nV, st, "previous position upload") &&
+         dupload(S->vel, zero4.data(), nV, st, "velocity upload") && dupload(S->rest, rest4.data(), nV, st, "rest position upload") &&
+         dupload(S->inv_mass, S->h_inv.data(), nV, st, "inverse mass upload") &&
+         dupload(S->sp_off, sp_off.data(), sp_off.size(), st, "spring CSR upload") &&
+         dupload(S->sp_ent, sp_ent.data(), sp_ent.size(), st, "spring CSR upload") &&
+         dupload(S->te_off, te_off.data(), te_off.size(), st, "tether CSR upload") &&
+         dupload(S->te_ent, te_ent.data(), te_ent.size(), st, "tether CSR upload") &&
+         dupload(S->bj_off, bj_off.data(), bj_off.size(), st, "bend CSR upload") &&
+         dupload(S->bj_ent, bj_ent.data(), bj_ent.size(), st, "bend CSR upload") &&
+         dupload(S->bends, cbends.data(), cbends.size(), st, "bend pair upload") &&
+         dupload(S->bend_rest, cbend_rest.data(), cbend_rest.size(), st, "bend rest upload") &&
+         dupload(S->tris, tris.data(), nT, st, "triangle upload") && dupload(S->edges, springs.data(), nE, st, "edge upload") &&
+         dupload(S->edge_rest, spring_rest.data(), nE, st, "edge rest upload") &&
+         dupload(S->pin_weight, S->h_pin_weight.data(), nV, st, "pin weight upload") &&
+         dupload(S->pin_target, S->h_pin_target.data(), nV, st, "pin target upload") &&
+         dupload(S->pin_relax, S->h_pin_relax.data(), nV, st, "pin relaxation upload") &&
+         dupload(S->vcloth, vmap.data(), vmap.size(), st, "cloth map upload") &&
+         dupload(S->ecloth, emap.data(), emap.size(), st, "cloth map upload") &&
+         dupload(S->tcloth, tmap.data(), tmap.size(), st, "cloth map upload") &&
+         cuda_ok(cudaMemsetAsync(S->counts, 0, sizeof(unsigned long long) * kCntSlots, st), "reset ABI41 diagnostics") &&
+         cuda_ok(cudaMemsetAsync(S->max_delta_bits, 0, sizeof(unsigned), st), "reset self max smoothed delta") &&
+         (!S->acc || cuda_ok(cudaMemsetAsync(S->acc, 0, sizeof(Acc4) * nV, st), "reset self accumulation")) &&
+         (!S->nb_count || cuda_ok(cudaMemsetAsync(S->nb_count, 0, sizeof(int) * nV, st), "reset neighbor table")) &&
+         sync_params(S) && cuda_ok(cudaStreamSynchronize(st), "solver upload");
+    if (ok && S->pcg_on)
+        ok = dupload(S->cap_edges, cap_edges.data(), nE, st, "cap edge upload") &&
+             dupload(S->cap_rest, cap_rest.data(), nE, st, "cap rest upload") &&
+             cuda_ok(cudaMemsetAsync(S->pcg.ticket, 0, sizeof(unsigned), st), "reset PCG ticket") &&
+             cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots, st), "reset PCG reductions") &&
+             cuda_ok(cudaStreamSynchronize(st), "PCG buffer upload");
+    if (!ok) return bail(0, "");
+    S->diag.finite_flag = 1;
+    S->diag.abi41_bending_wing_count = wings;
+    S->diag.abi41_bending_texture_ready = wings > 0 ? 1 : 0;
+    for (int k = 0; k < K; ++k)
+        if (!upload_static(S, k, meshes[k].static_triangles, std::max(configs[k].static_triangle_count, 0))) return bail(k, "");
+    return S;
+}
+
+// ------------------------------------------------------------ the frame --
+
+namespace {
+
+// Self-collision work of one substep: which cloths run it and which kernel
+// variants they need.
+struct SelfPlan {
+    bool run = false;
+    int passes = 0;
+    bool vhash = false, thash = false, ehash = false, order = false, any_t = false, any_e = false, island = false;
+    SelfVariants sv{};
+    long long hits = 0, misses = 0;
+};
+
+SelfPlan plan_self(const Solver* S, int s, int substeps) {
+    SelfPlan p;
+    for (int k = 0; k < S->K; ++k) {
+        const Cloth& C = S->cl[k];
+        const Params& P = S->hp[k];
+        if (!C.self_enabled || !P.active) continue;
+        if (!(((s + 1) % C.interval) == 0 || s == substeps - 1)) continue;
+        p.run = true;
+        p.passes = std::max(p.passes, C.passes);
+        p.vhash |= P.vhash != 0;
+        p.thash |= P.thash != 0;
+        p.ehash |= P.ehash != 0;
+        p.order |= C.order_buckets;
+        p.any_t |= P.T > 0;
+        p.any_e |= P.E > 0;
+        p.sv.fast |= C.fast;
+        p.sv.strict |= !C.fast;
+        p.sv.hashed_v |= P.vhash != 0;
+        p.sv.brute_v |= P.vhash == 0;
+        p.sv.hashed_t |= P.thash != 0 && P.T > 0;
+        p.sv.brute_t |= P.thash == 0 && P.T > 0;
+        p.sv.hashed_e |= P.ehash != 0 && P.E > 0;
+        p.sv.brute_e |= P.ehash == 0 && P.E > 0;
+        p.island |= C.fast && P.T > 0 && P.thash != 0;
+        if (C.fast) {
+            p.hits += (long long)P.V * (C.passes > 1 ? C.passes - 1 : 0);
+            p.misses += (long long)P.V;
+        }
+    }
+    return p;
+}
+
+}  // namespace
+
+// Issue one frame: `substeps` substeps of `iterations` iterations, following
+// the reference schedule (abi41.cu:9165-9376).  Per-vertex stages of an
+// iteration are fused into one pass; a pass starts at every stretch /
+// tether / Jacobi-bend gather and around the work that needs all vertices
+// (bends by colour, self collision).
+void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof) {
+    const int nV = S->nV, nE = S->nE;
+    bool analytic = false, sdf = false;
+    for (const Params& P : S->hp) {
+        analytic |= P.use_ground || P.use_wall || P.use_sphere;
+        sdf |= P.sdf_ready != 0;
+    }
+    const bool pcg = S->pcg_on;
+    const bool spring = nE > 0 && !pcg;
+    const bool hard = pcg && S->hp[0].stretch_strength >= 0.95f;
+    const float cap_dt = S->hp[0].sub_dt;
+    const bool colored_bends = !S->bend_colors.empty();
+    View base = S->view();
+    base.substeps = substeps;
+    int cur = 0;
+    unsigned pending = 0;
+    int pending_last = 0;  // last_it of the iteration that queued `pending`
+    int gather = 0;        // 0 none, 1 stretch, 2 tethers, 3 bends without colours
+    auto timed = [&](int kind, int launches, auto&& fn) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (prof) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, S->stream);
+        }
+        fn();
+        if (prof) {
+            cudaEventRecord(b, S->stream);
+            prof->marks.push_back({kind, {a, b}});
+        }
+        st->launches += launches;
+    };
+    auto flush = [&]() {
+        if (!pending && !gather) return;
+        View v = base;
+        v.last_it = pending_last;
+        v.pos_in = S->pos[cur];
+        const unsigned gflag = gather == 1 ? kPassSpring : (gather == 2 ? kPassTether : (gather == 3 ? kPassBend : 0u));
+        v.pos = gather ? S->pos[cur ^ 1] : S->pos[cur];
+        timed(gather == 1 ? kKStretchPass : kKVertexPass, 1, [&] { launch_vertex_pass(v, nV, gflag | pending, S->stream); });
+        if (gather) cur ^= 1;
+        pending = 0;
+        gather = 0;
+    };
+    auto cur_view = [&]() {
+        View v = base;
+        v.pos_in = S->pos[cur];
+        v.pos = S->pos[cur];
+        return v;
+    };
+    // colour-range caps over the colour-sorted edge arrays
+    auto caps = [&](int kind, int passes, bool both_ways) {
+        View cv = cur_view();
+        cv.edges = S->cap_edges;
+        cv.edge_rest = S->cap_rest;
+        const int ncol = (int)S->cap_colors.size() - 1;
+        timed(kKStretchCaps, 0, [&] {
+            for (int p = 0; p < passes; ++p) {
+                for (int k = 0; k < ncol; ++k) {
+                    const int n = S->cap_colors[k + 1] - S->cap_colors[k];
+                    if (n > 0) {
+                        pcg_cap_range(cv, S->cap_colors[k], n, cap_dt, kind, S->stream);
+                        st->launches += 1;
+                    }
+                }
+                if (both_ways)
+                    for (int k = ncol - 1; k >= 0; --k) {
+                        const int n = S->cap_colors[k + 1] - S->cap_colors[k];
+                        if (n > 0) {
+                            pcg_cap_range(cv, S->cap_colors[k], n, cap_dt, kind, S->stream);
+                            st->launches += 1;
+                        }
+                    }
+            }
+        });
+    };
+    auto averaged = [&](bool tiny) {
+        View av = cur_view();
+        timed(kKStretchCaps, 2, [&] { pcg_averaged_pass(av, S->pcg, nV, tiny, S->stream); });
+    };
+    for (int s = 0; s < substeps; ++s) {
+        base.substep = s;
+        const SelfPlan sp = plan_self(S, s, substeps);
+        View pv = cur_view();
+        timed(kKPredict, 1, [&] { launch_predict(pv, nV, S->stream); });
+        for (int it = 0; it < iterations; ++it) {
+            const bool last_it = it == iterations - 1;
+            const bool final_c = (s == substeps - 1) && last_it;
+            flush();
+            base.last_it = last_it ? 1 : 0;
+            if (spring) gather = 1;
+            if (pcg && last_it) {
+                // CG stretch solve, then (hardness >= 0.95) the averaged
+                // polish with normal and tiny caps, and the extreme caps
+                // (abi41.cu:9183-9201, 7806-7857, 7974-7995)
+                View gv = cur_view();
+                timed(kKPcg, 0, [&] { pcg_solve(gv, S->pcg, nV, S->stream, &st->launches); });
+                st->pcg_solves += 1;
+                if (hard) {
+                    for (int polish = 0; polish < 2; ++polish) {
+                        averaged(false);
+                        caps(0, 2, true);
+                        for (int tiny = 0; tiny < 2; ++tiny) {
+                            averaged(true);
+                            caps(1, 3, false);
+                        }
+                    }
+                    caps(2, 3, false);
+                }
+            }
+            if (final_c && S->nL > 0) {
+                flush();
+                gather = 2;
+            }
+            if (final_c && colored_bends) {
+                flush();
+                View bv = cur_view();
+                for (size_t k = 0; k + 1 < S->bend_colors.size(); ++k) {
+                    const int start = S->bend_colors[k], n = S->bend_colors[k + 1] - start;
+                    if (n > 0) timed(kKBendColor, 1, [&] { launch_bend_color(bv, start, n, S->stream); });
+                }
+            }
+            if (final_c && S->jacobi_bends) {
+                flush();
+                gather = 3;
+            }
+            pending |= kPassPin;
+            if (analytic) pending |= kPassAnalytic;
+            if (sdf) pending |= kPassSdf;
+            pending_last = base.last_it;
+            const bool self_run = last_it && sp.run;
+            if (self_run) {
+                flush();
+                View sv = cur_view();
+                if (sp.vhash)
+                    timed(kKVertexHash, 6, [&] {
+                        cudaMemsetAsync(S->vb_count, 0, sizeof(int) * S->nVB, S->stream);
+                        self_build_vertex_hash(sv, nV, S->nVB, S->stream);
+                    });
+                // strict queries with a 32-candidate budget do not depend on
+                // the order of buckets of <= 32 members
+                if (sp.thash)
+                    timed(kKTriangleHash, 6, [&] {
+                        cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, S->stream);
+                        self_build_triangle_hash(sv, S->nT, S->nTB, sp.order, S->stream);
+                    });
+                if (sp.ehash)
+                    timed(kKEdgeHash, 6, [&] {
+                        cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, S->stream);
+                        self_build_edge_hash(sv, nE, S->nEB, sp.order, S->stream);
+                    });
+                if (sp.sv.fast) {
+                    timed(kKNeighbors, 1, [&] { self_neighbors(sv, nV, 1, sp.sv, S->stream); });
+                    st->cache_hits += sp.hits;
+                    st->cache_misses += sp.misses;
+                }
+                for (int pass = 0; pass < sp.passes; ++pass) {
+                    View pv2 = sv;
+                    pv2.pass = pass;
+                    if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, nV, 2, sp.sv, S->stream); });
+                    timed(kKVertexVertex, 1, [&] { self_vv(pv2, nV, sp.sv, S->stream); });
+                    if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, nV, sp.sv, S->stream); });
+                    if (sp.any_e) timed(kKEdgeEdge, 1, [&] { self_ee(pv2, nE, sp.sv, S->stream); });
+                    if (sp.island) timed(kKIsland, 1, [&] { self_island(pv2, nV, S->stream); });
+                    timed(kKSelfApply, 1, [&] { self_apply(pv2, nV, S->stream); });
+                }
+            }
+            // final ratio caps after the contacts (abi41.cu:9346-9350, 7997-8027)
+            if (pcg && final_c && hard) {
+                flush();
+                caps(0, 2, true);
+                caps(2, 3, false);
+                caps(1, 3, false);
+            }
+            // Final pin polish whenever a contact stage ran: analytic
+            // colliders, the SDF, or any last iteration (the dynamic
+            // collider stage counts as running on every last iteration);
+            // the pass applies it per cloth.
+            if (analytic || sdf || last_it) pending |= kPassPinPolish;
+        }
+        pending |= kPassVelocity;
+        flush();
+    }
+    if (cur != 0) timed(kKCopy, 1, [&] { launch_copy_pos(S->pos[0], S->pos[1], nV, S->stream); });
+}
+
+bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st) {
+    if (!S->use_graphs) {
+        enqueue_frame(S, substeps, iterations, st);
+        return cuda_ok(cudaGetLastError(), "launch GB300 XPBD frame");
+    }
+    int analytic = 0, sdf = 0;
+    for (const Params& P : S->hp) {
+        analytic |= (P.use_ground || P.use_wall || P.use_sphere) ? 1 : 0;
+        sdf |= P.sdf_ready ? 1 : 0;
+    }
+    const GraphKey key{substeps, iterations, analytic, sdf};
+    auto it = S->graphs.find(key);
+    if (it == S->graphs.end()) {
+        GraphEntry g;
+        FrameStats cst;
+        if (!cuda_ok(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal), "begin frame capture"))
+            return false;
+        enqueue_frame(S, substeps, iterations, &cst);
+        cudaGraph_t graph = nullptr;
+        if (!cuda_ok(cudaStreamEndCapture(S->stream, &graph), "end frame capture")) return false;
+        const cudaError_t err = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (!cuda_ok(err, "instantiate frame graph")) return false;
+        g.launches = cst.launches;
+        g.cache_hits = cst.cache_hits;
+        g.cache_misses = cst.cache_misses;
+        g.pcg_solves = cst.pcg_solves;
+        it = S->graphs.emplace(key, g).first;
+    }
+    st->launches += it->second.launches;
+    st->cache_hits += it->second.cache_hits;
+    st->cache_misses += it->second.cache_misses;
+    st->pcg_solves += it->second.pcg_solves;
+    return cuda_ok(cudaGraphLaunch(it->second.exec, S->stream), "launch frame graph");
+}
+
+bool fetch_counts(Solver* S, const FrameStats& st) {
+    unsigned long long c[kCntSlots];
+    unsigned mbits = 0;
+    if (!cuda_ok(cudaMemcpyAsync(c, S->counts, sizeof(c), cudaMemcpyDeviceToHost, S->stream), "fetch ABI41 diagnostics") ||
+        !cuda_ok(cudaMemcpyAsync(&mbits, S->max_delta_bits, sizeof(unsigned), cudaMemcpyDeviceToHost, S->stream),
+                 "fetch self max smoothed delta") ||
+        !cuda_ok(cudaStreamSynchronize(S->stream), "fetch diagnostics"))
+        return false;
+    int wings = 0;
+    for (const Cloth& C : S->cl) wings += C.wing_count;
+    SsblXpbdDiagnostics& d = S->diag;
+    d.abi41_soft_contact_count = (long long)c[kCntSoftContacts];
+    d.abi41_exact_impulse_contact_count = (long long)c[kCntExactImpulseContacts];
+    d.abi41_edge_edge_contact_count = (long long)c[kCntEdgeEdgeContacts];
+    d.abi41_hard_projection_fallbacks = (long long)c[kCntHardFallbacks];
+    std::memcpy(&d.abi41_max_smoothed_delta, &mbits, 4);
+    d.fast_soft_repulsion_candidates = (long long)c[kCntSelfCandidates];
+    d.fast_soft_repulsion_applied = (long long)c[kCntSoftContacts];
+    d.external_friction_corrections = (long long)c[kCntFrictionCorrections];
+    d.self_candidate_count = (long long)c[kCntSelfCandidates];
+    d.static_sdf_contact_count = (long long)c[kCntStaticSdfContacts];
+    d.candidate_count = (long long)(c[kCntSelfCandidates] + c[kCntStaticSdfContacts]);
+    d.abi41_lra_tack_count = (long long)c[kCntLraTacks];
+    d.abi41_bending_wing_count = c[kCntBendingWings] > 0 ? (long long)c[kCntBendingWings] : (long long)wings;
+    d.abi41_bending_texture_ready = wings > 0 ? 1 : 0;
+    d.abi41_tack_jitter_guarded = (long long)c[kCntTackGuards];
+    d.abi41_bending_guarded = (long long)c[kCntBendingGuards];
+    d.fast_overlap_island_candidates = (long long)c[kCntIslandCandidates];
+    d.fast_overlap_island_clusters = (long long)c[kCntIslandClusters];
+    d.fast_overlap_island_vertex_refs = (long long)c[kCntIslandVertexRefs];
+    d.fast_overlap_island_applied_vertices = (long long)c[kCntIslandAppliedVertices];
+    d.fast_overlap_island_guarded = (long long)c[kCntIslandGuarded];
+    d.fast_overlap_island_max_delta = (float)c[kCntIslandMaxDeltaMicro] * 1.0e-6f;
+    d.self_filter_seen = (long long)c[kCntFilterSeen];
+    d.self_filter_accepted_vv = (long long)c[kCntFilterAcceptedVv];
+    d.self_filter_accepted_vt = (long long)c[kCntFilterAcceptedVt];
+    d.self_filter_accepted_ee = (long long)c[kCntFilterAcceptedEe];
+    d.self_filter_rejected_rest = (long long)c[kCntFilterRejectedRest];
+    d.self_filter_rejected_duplicate = (long long)c[kCntFilterRejectedDuplicate];
+    d.self_filter_rejected_ownership = (long long)c[kCntFilterRejectedOwnership];
+    d.self_filter_cache_hits = st.cache_hits;      // counted for fast-mode cloths only
+    d.self_filter_cache_misses = st.cache_misses;
+    d.self_cluster_count = (long long)c[kCntClusterCount];
+    d.self_cluster_owned_contacts = (long long)c[kCntClusterOwnedContacts];
+    if (S->pcg_on) {
+        // residual diagnostics from the scalar slots (abi41.cu:7586-7624)
+        float red[kRedSlots];
+        unsigned long long guard = 0;
+        unsigned pbits = 0;
+        if (!cuda_ok(cudaMemcpyAsync(red, S->pcg.red, sizeof(red), cudaMemcpyDeviceToHost, S->stream), "fetch PCG reductions") ||
+            !cuda_ok(cudaMemcpyAsync(&guard, S->pcg.guard, sizeof(guard), cudaMemcpyDeviceToHost, S->stream), "fetch PCG guard count") ||
+            !cuda_ok(cudaMemcpyAsync(&pbits, S->pcg.max_delta_bits, 4, cudaMemcpyDeviceToHost, S->stream), "fetch PCG max delta") ||
+            !cuda_ok(cudaStreamSynchronize(S->stream), "fetch PCG diagnostics"))
+            return false;
+        d.abi41_pcg_csr_nnz = S->pcg_nnz;
+        d.abi41_pcg_texture_ready = 1;
+        d.abi41_pcg_iterations = S->pcg_iterations;
+        float initial = red[kRedInitialRZ];
+        if ((!std::isfinite(initial) || initial <= 0.0f) && std::isfinite(red[kRedRZ]) && red[kRedRZ] >= 0.0f) initial = red[kRedRZ];
+        if (std::isfinite(initial) && initial >= 0.0f) {
+            d.abi41_pcg_initial_residual = std::sqrt(std::max(initial, 0.0f));
+            d.abi41_pcg_final_residual = d.abi41_pcg_initial_residual;
+        }
+        const float status = red[kRedStatus];
+        const float final_rz = status == 2.0f ? red[kRedRZ] : red[kRedRZNext];
+        if ((status == 0.0f || status == 2.0f) && std::isfinite(final_rz) && final_rz >= 0.0f)
+            d.abi41_pcg_final_residual = std::sqrt(std::max(final_rz, 0.0f));
+        else if (status != 0.0f && status != 2.0f)
+            d.abi41_pcg_guarded += 1;
+        d.abi41_pcg_guarded += (long long)guard;
+        std::memcpy(&d.abi41_pcg_max_delta, &pbits, 4);
+    }
+    return true;
+}
+
+// Per-step preparation: sub-step length of each cloth, pin relaxation for
+// this iteration count, parameter upload and counter resets.
+bool prepare_step(Solver* S, int substeps, int iterations) {
+    for (int k = 0; k < S->K; ++k) {
+        const float sub_dt = S->cl[k].cfg.dt / (float)substeps;
+        if (S->hp[k].sub_dt != sub_dt) {
+            S->hp[k].sub_dt = sub_dt;
+            S->params_dirty = true;
+        }
+    }
+    if (!cuda_ok(cudaMemsetAsync(S->counts, 0, sizeof(unsigned long long) * kCntSlots, S->stream), "reset ABI41 diagnostics") ||
+        !cuda_ok(cudaMemsetAsync(S->max_delta_bits, 0, sizeof(unsigned), S->stream), "reset self max smoothed delta") ||
+        !upload_pin_relax(S, iterations) || !sync_params(S))
+        return false;
+    if (S->pcg_on &&
+        (!cuda_ok(cudaMemsetAsync(S->pcg.guard, 0, sizeof(unsigned long long), S->stream), "reset PCG guard count") ||
+         !cuda_ok(cudaMemsetAsync(S->pcg.max_delta_bits, 0, sizeof(unsigned), S->stream), "reset PCG max delta") ||
+         !cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots, S->stream), "reset PCG reductions")))
+        return false;
+    return true;
+}
+
+bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int force_sync) {
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    int ff = 0, uff = 0;
+    for (const Cloth& C : S->cl) {
+        ff += C.force_field_count;
+        uff += C.unsupported_force_field_count;
+    }
+    S->diag = SsblXpbdDiagnostics{};
+    S->diag.finite_flag = 1;
+    S->diag.force_field_count = ff;
+    S->diag.unsupported_force_field_count = uff;
+    sdf_diagnostics(S);
+    substeps = std::max(substeps, 1);
+    iterations = std::max(iterations, 1);
+    if (!prepare_step(S, substeps, iterations)) return false;
+    FrameStats st;
+    if (!run_frame(S, substeps, iterations, &st)) return false;
+    S->last_launches = st.launches;
+    S->pcg_iterations = st.pcg_solves * 8;
+    if (force_sync || fetch_diagnostics) {
+        const auto ts = std::chrono::high_resolution_clock::now();
+        if (!cuda_ok(cudaStreamSynchronize(S->stream), "ABI41 solver step")) return false;
+        S->diag.sync_ms = (float)ms_since(ts);
+    }
+    if (fetch_diagnostics && !fetch_counts(S, st)) return false;
+    S->diag.step_ms = (float)ms_since(t0);
+    S->diag.constraints_ms = S->diag.step_ms;
+    S->diag.resolved_contacts = S->diag.abi41_soft_contact_count + S->diag.abi41_exact_impulse_contact_count +
+                                S->diag.abi41_edge_edge_contact_count + S->diag.static_sdf_contact_count;
+    return true;
+}
+
+}  // namespace host
+
+// Lets entry points defined in other translation units report through
+// ssbl_last_error().
+void set_last_error(const std::string& msg) { host::g_error = msg; }
+
+}  // namespace xg

@@ -1,0 +1,232 @@
+// Host-side solver object shared by the C entry points (xpbd_abi.cu) and the
+// solver implementation (xpbd_host.cu).
+//
+// One Solver holds K >= 1 independent cloths concatenated in every device
+// array: cloth k owns vertices [vstart, vstart + V), edges, triangles, bends
+// and tethers likewise, and its own ranges of the self-collision bucket
+// tables.  An ABI41 handle is a solver of one cloth; the batch entry points
+// create solvers of many.  Every cloth of a solver steps with the same
+// substeps / iterations, in one launch sequence captured as one CUDA graph.
+#pragma once
+
+#include <chrono>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/ssbl_xpbd_cuda.h"
+#include "../../include/xpbd_gb300.h"
+#include "xpbd_solver.cuh"
+
+namespace xg {
+namespace host {
+
+extern thread_local std::string g_error;
+
+inline bool fail(const std::string& msg) {
+    g_error = msg.empty() ? std::string("unknown GB300 XPBD error") : msg;
+    return false;
+}
+
+inline bool cuda_ok(cudaError_t err, const char* what) {
+    if (err == cudaSuccess) return true;
+    g_error = std::string(what) + ": " + cudaGetErrorString(err);
+    return false;
+}
+
+template <class T>
+bool dalloc(T** p, size_t n, const char* what) {
+    *p = nullptr;
+    if (n == 0) return true;
+    return cuda_ok(cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * n), what);
+}
+
+template <class T>
+bool dupload(T* dst, const T* src, size_t n, cudaStream_t s, const char* what) {
+    if (n == 0) return true;
+    return cuda_ok(cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice, s), what);
+}
+
+inline int next_pow2(int value) {
+    int r = 1;
+    value = value < 1 ? 1 : value;
+    while (r < value && r < (1 << 30)) r <<= 1;
+    return r;
+}
+
+inline double ms_since(std::chrono::high_resolution_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::high_resolution_clock::now() - t0).count();
+}
+
+// Kernel kinds of the per-kernel profile (xpbd_gb300_profile_frame).
+enum KernelKind {
+    kKPredict = 0,
+    kKStretchPass = 1,   // stretch gather + per-vertex contact stages
+    kKVertexPass = 2,    // tether / Jacobi-bend gather or stages only
+    kKBendColor = 3,
+    kKVertexHash = 4,
+    kKTriangleHash = 5,
+    kKEdgeHash = 6,
+    kKNeighbors = 7,
+    kKVertexVertex = 8,
+    kKVertexTriangle = 9,
+    kKEdgeEdge = 10,
+    kKIsland = 11,
+    kKSelfApply = 12,
+    kKCopy = 13,
+    kKPcg = 14,          // CG solve (build + 8 iterations)
+    kKStretchCaps = 15,  // averaged polish and colour-range ratio caps
+    kKinds = 16
+};
+
+struct GraphKey {
+    int substeps, iterations, analytic, sdf;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(substeps, iterations, analytic, sdf) < std::tie(o.substeps, o.iterations, o.analytic, o.sdf);
+    }
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+    long long cache_hits = 0, cache_misses = 0;
+    long long pcg_solves = 0;
+};
+
+struct FrameStats {
+    long long launches = 0;
+    long long cache_hits = 0, cache_misses = 0;
+    long long pcg_solves = 0;
+};
+
+// Optional per-launch event pairs, recorded when profiling a frame.
+struct Profile {
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+};
+
+// Host-side state of one cloth of a solver.
+struct Cloth {
+    SsblXpbdConfig cfg{};               // sanitised copy of the caller's config
+    SsblXpbdRuntimeColliders colliders{};
+    std::vector<int> bend_colors;       // caller's colour offsets (local)
+    std::vector<int> edge_colors;
+    bool self_enabled = false;          // self collision on with a positive radius
+    int interval = 1, passes = 1;       // self-collision schedule
+    bool fast = false;
+    bool order_buckets = true;          // queries depend on bucket member order
+    // static SDF of this cloth's collider
+    float* sdf = nullptr;
+    int sdf_capacity = 0;
+    float4* static_tris = nullptr;
+    int static_capacity = 0;
+    long long sdf_rebuilds = 0, sdf_unsigned = 0;
+    float sdf_build_ms = 0.0f;
+    int pin_count = 0;
+    int wing_count = 0;
+    int force_field_count = 0;
+    int unsupported_force_field_count = 0;
+};
+
+struct Solver {
+    int K = 0;
+    std::vector<Cloth> cl;
+    std::vector<Params> hp;     // one per cloth
+    Params* dp = nullptr;
+    bool params_dirty = true;
+    float params_dt_substeps = -1.0f;  // substeps the sub_dt fields were set for
+    cudaStream_t stream = nullptr;
+
+    int nV = 0, nE = 0, nT = 0, nB = 0, nL = 0;   // totals over the cloths
+    int nVB = 0, nTB = 0, nEB = 0;                // total bucket counts
+    int* vcloth = nullptr;                        // cloth maps (K > 1 only)
+    int* ecloth = nullptr;
+    int* tcloth = nullptr;
+
+    float4* pos[2] = {nullptr, nullptr};
+    float4* prev = nullptr;
+    float4* vel = nullptr;
+    float4* rest = nullptr;  // .w = effective inverse mass
+    float* inv_mass = nullptr;
+    int* sp_off = nullptr;
+    int2* sp_ent = nullptr;
+    int* te_off = nullptr;
+    int2* te_ent = nullptr;
+    int* bj_off = nullptr;  // bends as a Jacobi gather (cloths without colours)
+    int2* bj_ent = nullptr;
+    int2* bends = nullptr;  // coloured bends merged by (colour, cloth)
+    float* bend_rest = nullptr;
+    int4* tris = nullptr;
+    int2* edges = nullptr;
+    float* edge_rest = nullptr;
+    float4* pin_target = nullptr;
+    float* pin_weight = nullptr;
+    float* pin_relax = nullptr;
+    unsigned long long* counts = nullptr;
+    unsigned* max_delta_bits = nullptr;
+    float* pack = nullptr;
+
+    std::vector<float> h_w;      // effective inverse mass per vertex
+    std::vector<float> h_inv;    // inverse mass as given
+    std::vector<float> h_pin_weight;
+    std::vector<float4> h_pin_target;
+    std::vector<float> h_pin_relax;
+    int pin_relax_iterations = -1;
+    std::vector<int> bend_colors;   // merged colour offsets into `bends`
+    bool jacobi_bends = false;      // some cloth gathers its bends
+
+    // self collision
+    bool self_any = false;
+    int4* vcell = nullptr;
+    int *vb_count = nullptr, *vb_start = nullptr, *vb_ent = nullptr;
+    int *tb_count = nullptr, *tb_start = nullptr, *tb_ent = nullptr;
+    int *eb_count = nullptr, *eb_start = nullptr, *eb_ent = nullptr;
+    int* nb_count = nullptr;
+    int* nb_idx = nullptr;
+    int* scan_tmp = nullptr;
+    Acc4* acc = nullptr;
+
+    // hard-stretch optimisation (one-cloth solvers only)
+    bool pcg_on = false;
+    PcgView pcg{};
+    int2* cap_edges = nullptr;   // edges sorted by colour for the caps
+    float* cap_rest = nullptr;
+    std::vector<int> cap_colors; // colour offsets into cap_edges
+    int pcg_nnz = 0;
+    long long pcg_iterations = 0;
+
+    std::map<GraphKey, GraphEntry> graphs;
+    bool use_graphs = true;
+    long long last_launches = 0;
+    SsblXpbdDiagnostics diag{};
+
+    View view() const;
+    void drop_graphs();
+};
+
+// Creation of a solver for `count` cloths (count == 1: the ABI41 handle).
+// Returns nullptr with g_error set on failure.
+Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes, int count);
+void free_solver(Solver* S);
+
+// Cloth-level updates; cloth < 0 applies to every cloth (pins then take
+// indices over the concatenated vertices).
+bool upload_pins(Solver* S, int cloth, const int* indices, const float* positions, const float* weights, int count);
+bool set_colliders(Solver* S, int cloth, const SsblXpbdRuntimeColliders& c);
+bool upload_static(Solver* S, int cloth, const float* tris, int count);
+bool upload_positions(Solver* S, int cloth, const float* positions, int max_floats);
+bool download_positions(Solver* S, int cloth, float* out, int max_floats);
+bool reset_cloths(Solver* S, int cloth);
+bool set_active(Solver* S, int cloth, bool active);
+void sdf_diagnostics(Solver* S);
+
+// One frame: prepare parameters, launch (graph or direct), optionally fetch.
+bool prepare_step(Solver* S, int substeps, int iterations);
+bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st);
+void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof = nullptr);
+bool fetch_counts(Solver* S, const FrameStats& st);
+bool sync_params(Solver* S);
+bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int force_sync);
+
+}  // namespace host
+}  // namespace xg

@@ -118,10 +118,10 @@ __device__ __forceinline__ float4 z4() { return make_float4(0.0f, 0.0f, 0.0f, 0.
 // preconditioner / initial residual (abi41.cu:3188-3226) and the iteration
 // set-up (abi41.cu:3071-3083).
 __global__ void __launch_bounds__(kThreads) k_pcg_build(View v, PcgView g) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float rz = 0.0f;
-    if (i < P.V) {
+    if (i < v.nV) {
         const float4 p4 = v.pos[i];
         const float wi_self = p4.w;
         Sym diag{1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f};
@@ -198,11 +198,11 @@ __global__ void __launch_bounds__(kThreads) k_pcg_build(View v, PcgView g) {
 
 // q = A d, partial d.q (abi41.cu:3228-3267); the last block publishes dAd.
 __global__ void __launch_bounds__(kThreads) k_pcg_ad(View v, PcgView g) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool status_ok = g.red[kRedStatus] == kStatusOk;
     float dq = 0.0f;
-    if (status_ok && i < P.V) {
+    if (status_ok && i < v.nV) {
         if (!(v.pos[i].w > 0.0f)) {
             g.q[i] = z4();
         } else {
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_ad(View v, PcgView g) {
 // Device alpha, solution / residual / preconditioned residual update with the
 // incremental position write-back, partial r.z (abi41.cu:3320-3405).
 __global__ void __launch_bounds__(kThreads) k_pcg_update(View v, PcgView g) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float rz_old = g.red[kRedRZ], dad = g.red[kRedDAD];
     float status = kStatusOk, alpha = 0.0f;
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(View v, PcgView g) {
         if (!isfinite(alpha)) status = kStatusBadAlpha;
     }
     float rz = 0.0f;
-    if (status == kStatusOk && i < P.V) {
+    if (status == kStatusOk && i < v.nV) {
         const float4 p4 = v.pos[i];
         if (!(p4.w > 0.0f)) {
             g.r[i] = z4();
@@ -292,12 +292,12 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(View v, PcgView g) {
 // Device beta and d = z + beta d (abi41.cu:3421-3450); the last block then
 // advances the scalar slots (abi41.cu:3452-3464).
 __global__ void __launch_bounds__(kThreads) k_pcg_dir(View v, PcgView g) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float status = g.red[kRedStatus], rz_old = g.red[kRedRZ], rz_new = g.red[kRedRZNext];
     const bool ok = status == kStatusOk && isfinite(rz_old) && isfinite(rz_new) && rz_old > 1.0e-14f && rz_new >= 0.0f;
     const float beta = ok ? rz_new / rz_old : 0.0f;
-    if (ok && isfinite(beta) && i < P.V) {
+    if (ok && isfinite(beta) && i < v.nV) {
         if (!(v.pos[i].w > 0.0f)) {
             g.d[i] = z4();
         } else {
@@ -363,9 +363,9 @@ __device__ bool averaged_delta(const Params& P, bool tiny, float4 pi, float4 pj,
 
 // Gather of the averaged corrections of a vertex's edges into sum / count.
 __global__ void __launch_bounds__(kThreads) k_avg_gather(View v, PcgView g, int tiny) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.V) return;
+    if (i >= v.nV) return;
     const float4 p4 = v.pos[i];
     const F3 prev_self = f3(v.prev[i]);
     F3 sum{0.0f, 0.0f, 0.0f};
@@ -389,9 +389,9 @@ __global__ void __launch_bounds__(kThreads) k_avg_gather(View v, PcgView g, int 
 
 // Apply the averaged corrections (abi41.cu:2084-2112, 2469-2494).
 __global__ void __launch_bounds__(kThreads) k_avg_apply(View v, PcgView g, int tiny) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.V) return;
+    if (i >= v.nV) return;
     const float4 p4 = v.pos[i];
     if (!(p4.w > 0.0f)) return;
     const float4 a = g.avg[i];
@@ -415,18 +415,18 @@ __global__ void __launch_bounds__(kThreads) k_avg_apply(View v, PcgView g, int t
 // colour share a vertex): normal (abi41.cu:2249-2362), tiny (2496-2601) and
 // extreme (2603-2708).
 __global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int count, float dt, int kind) {
-    const Params& P = *v.P;
+    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int local = blockIdx.x * blockDim.x + threadIdx.x;
     if (local >= count) return;
     const int s = start + local;
-    if (s < 0 || s >= P.E) return;
+    if (s < 0 || s >= v.nE) return;
     const float rest = __ldg(&v.edge_rest[s]);
     const bool tiny = kind == 1;
     if (!isfinite(rest) || rest <= kEps) return;
     if (tiny ? rest > 7.5e-4f : rest <= 7.5e-4f) return;
     const int2 ed = __ldg(&v.edges[s]);
     const int i = ed.x, j = ed.y;
-    if (i < 0 || j < 0 || i >= P.V || j >= P.V || i == j) return;
+    if (i < 0 || j < 0 || i >= v.nV || j >= v.nV || i == j) return;
     const float4 pi4 = v.pos[i], pj4 = v.pos[j];
     const float wi = pi4.w, wj = pj4.w, weight = wi + wj;
     if (!isfinite(weight) || weight <= 0.0f) return;

@@ -34,9 +34,9 @@ __device__ bool ray_x_hits(F3 p, F3 a, F3 b, F3 c) {
     return t > 1.0e-6f;
 }
 
-__global__ void __launch_bounds__(kThreads) k_sdf_build(View v, int voxels) {
+__global__ void __launch_bounds__(kThreads) k_sdf_build(View v, int cloth, int voxels) {
     __shared__ float4 tile[kSdfTile * 3];
-    const Params& P = *v.P;
+    const Params& P = v.P[cloth];
     const int voxel = blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = P.sdf_dim[0], ny = P.sdf_dim[1];
     const int x = voxel % nx, y = (voxel / nx) % ny, z = voxel / (nx * ny);
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kThreads) k_sdf_build(View v, int voxels) {
     for (int base = 0; base < T; base += kSdfTile) {
         const int n = min(kSdfTile, T - base);
         __syncthreads();
-        for (int k = threadIdx.x; k < n * 3; k += blockDim.x) tile[k] = ld4(&v.static_tris[base * 3 + k]);
+        for (int k = threadIdx.x; k < n * 3; k += blockDim.x) tile[k] = ld4(&P.static_tris[base * 3 + k]);
         __syncthreads();
         if (voxel < voxels) {
             for (int t = 0; t < n; ++t) {
@@ -64,13 +64,13 @@ __global__ void __launch_bounds__(kThreads) k_sdf_build(View v, int voxels) {
     if (voxel >= voxels) return;
     float dist = sqrtf(fmaxf(best, 0.0f));
     if (is_signed && parity) dist = -dist;
-    const_cast<float*>(v.sdf)[voxel] = dist;
+    const_cast<float*>(P.sdf)[voxel] = dist;
 }
 
 }  // namespace
 
-void launch_sdf_build(const View& v, int voxels, cudaStream_t s) {
-    if (voxels > 0) k_sdf_build<<<(voxels + kThreads - 1) / kThreads, kThreads, 0, s>>>(v, voxels);
+void launch_sdf_build(const View& v, int cloth, int voxels, cudaStream_t s) {
+    if (voxels > 0) k_sdf_build<<<(voxels + kThreads - 1) / kThreads, kThreads, 0, s>>>(v, cloth, voxels);
 }
 
 }  // namespace xg

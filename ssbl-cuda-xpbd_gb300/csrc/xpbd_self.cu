@@ -30,8 +30,7 @@ __device__ __forceinline__ float contact_radius(const Params& P) { return P.self
 __device__ __forceinline__ bool fast_mode(const Params& P) { return P.self_mode == 1; }
 
 __device__ __forceinline__ void accumulate(const View& v, int i, F3 d) {
-    const Params& P = *v.P;
-    if (i < 0 || i >= P.V || !(__ldg(&v.inv_mass[i]) > 0.0f)) return;
+    if (i < 0 || i >= v.nV || !(__ldg(&v.inv_mass[i]) > 0.0f)) return;
     unsigned long long* a = reinterpret_cast<unsigned long long*>(&v.acc[i]);
     atomicAdd(a + 0, (unsigned long long)to_fix(d.x));
     atomicAdd(a + 1, (unsigned long long)to_fix(d.y));
@@ -63,8 +62,8 @@ __device__ int accept_slot(int pair_type) {
     return pair_type == 0 ? kCntFilterAcceptedVv : (pair_type == 1 ? kCntFilterAcceptedVt : kCntFilterAcceptedEe);
 }
 
-__device__ bool try_local_accept(const View& v, int pair_type, unsigned key, Clusters* cl) {
-    if (!fast_mode(*v.P)) return true;
+__device__ bool try_local_accept(const View& v, const Params& P, int pair_type, unsigned key, Clusters* cl) {
+    if (!fast_mode(P)) return true;
     if (cl) {
         const int n = cl->n < 16 ? cl->n : 16;
         for (int i = 0; i < n; ++i) {
@@ -98,8 +97,8 @@ struct Seen {
     int n;
 };
 
-__device__ bool try_note_seen(const View& v, int key, Seen* seen) {
-    if (!fast_mode(*v.P)) return true;
+__device__ bool try_note_seen(const View& v, const Params& P, int key, Seen* seen) {
+    if (!fast_mode(P)) return true;
     count1(v.counts, kCntFilterSeen);
     if (!seen) return true;
     const int lim = seen->n < 64 ? seen->n : 64;
@@ -118,8 +117,8 @@ __device__ bool try_note_seen(const View& v, int key, Seen* seen) {
     return true;
 }
 
-__device__ __forceinline__ void filter_count(const View& v, int slot) {
-    if (fast_mode(*v.P)) count1(v.counts, slot);
+__device__ __forceinline__ void filter_count(const View& v, const Params& P, int slot) {
+    if (fast_mode(P)) count1(v.counts, slot);
 }
 
 // ------------------------------------------------------------- hash build --
@@ -140,17 +139,15 @@ __device__ CellRange primitive_cells(const View& v, F3 lo, F3 hi, F3 fallback, f
     return CellRange{fx, fx, fy, fy, fz, fz};
 }
 
-__device__ bool tri_valid(const Params& P, int4 t) {
-    return t.x >= 0 && t.y >= 0 && t.z >= 0 && t.x < P.V && t.y < P.V && t.z < P.V && t.x != t.y && t.y != t.z &&
-           t.x != t.z;
+__device__ bool tri_valid(int nV, int4 t) {
+    return t.x >= 0 && t.y >= 0 && t.z >= 0 && t.x < nV && t.y < nV && t.z < nV && t.x != t.y && t.y != t.z && t.x != t.z;
 }
 
-__device__ bool edge_valid(const Params& P, int2 e) { return e.x >= 0 && e.y >= 0 && e.x < P.V && e.y < P.V && e.x != e.y; }
+__device__ bool edge_valid(int nV, int2 e) { return e.x >= 0 && e.y >= 0 && e.x < nV && e.y < nV && e.x != e.y; }
 
-__device__ CellRange tri_cells(const View& v, int t, bool* ok, bool count_guard) {
-    const Params& P = *v.P;
+__device__ CellRange tri_cells(const View& v, const Params& P, int t, bool* ok, bool count_guard) {
     const int4 tr = __ldg(&v.tris[t]);
-    *ok = tri_valid(P, tr);
+    *ok = tri_valid(v.nV, tr);
     if (!*ok) return CellRange{0, -1, 0, -1, 0, -1};
     const F3 a = f3(v.pos[tr.x]), b = f3(v.pos[tr.y]), c = f3(v.pos[tr.z]);
     const float m = contact_radius(P) * 1.8f;
@@ -160,10 +157,9 @@ __device__ CellRange tri_cells(const View& v, int t, bool* ok, bool count_guard)
     return primitive_cells(v, lo, hi, centroid, P.tcell, count_guard);
 }
 
-__device__ CellRange edge_cells(const View& v, int e, bool* ok, bool count_guard) {
-    const Params& P = *v.P;
+__device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok, bool count_guard) {
     const int2 ed = __ldg(&v.edges[e]);
-    *ok = edge_valid(P, ed);
+    *ok = edge_valid(v.nV, ed);
     if (!*ok) return CellRange{0, -1, 0, -1, 0, -1};
     const F3 a = f3(v.pos[ed.x]), b = f3(v.pos[ed.y]);
     const float m = contact_radius(P) * 1.8f;
@@ -174,12 +170,13 @@ __device__ CellRange edge_cells(const View& v, int e, bool* ok, bool count_guard
 }
 
 __global__ void k_vhash_count(View v) {
-    const Params& P = *v.P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.V) return;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.vhash || !self_scheduled(P, v)) return;
     const float4 p = v.pos[i];
     const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
-    const int b = (int)bucket_of(cx, cy, cz, P.vbuckets);
+    const int b = P.vbase + (int)bucket_of(cx, cy, cz, P.vbuckets);
     v.vcell[i] = make_int4(cx, cy, cz, b);
     const int slot = atomicAdd(&v.vb_count[b], 1);
     if (slot >= kBucketSlots) count1(v.counts, kCntSelfOverflow);
@@ -187,7 +184,9 @@ __global__ void k_vhash_count(View v) {
 
 __global__ void k_vhash_scatter(View v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.P->V) return;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.vhash || !self_scheduled(P, v)) return;
     const int b = v.vcell[i].w;
     v.vb_ent[atomicAdd(&v.vb_count[b], 1)] = i;
 }
@@ -200,13 +199,14 @@ constexpr int kPrimLanes = 16;
 
 template <bool kTri>
 __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
-    const Params& P = *v.P;
-    const int n = kTri ? P.T : P.E;
+    const int n = kTri ? v.nT : v.nE;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = (int)(t / kPrimLanes), c0 = (int)(t % kPrimLanes);
     if (k >= n) return;
+    const Params& P = kTri ? params_t(v, k) : params_e(v, k);
+    if (!(kTri ? P.thash : P.ehash) || !self_scheduled(P, v)) return;
     bool ok = false;
-    const CellRange r = kTri ? tri_cells(v, k, &ok, !scatter && c0 == 0) : edge_cells(v, k, &ok, !scatter && c0 == 0);
+    const CellRange r = kTri ? tri_cells(v, P, k, &ok, !scatter && c0 == 0) : edge_cells(v, P, k, &ok, !scatter && c0 == 0);
     if (!ok) return;
     const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
     if (nx <= 0 || ny <= 0 || nz <= 0) return;
@@ -214,9 +214,10 @@ __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     int* cnt = kTri ? v.tb_count : v.eb_count;
     int* ent = kTri ? v.tb_ent : v.eb_ent;
     const int nb = kTri ? P.tbuckets : P.ebuckets;
+    const int base = kTri ? P.tbase : P.ebase;
     for (int c = c0; c < cells; c += kPrimLanes) {
         const int x = r.x0 + c % nx, y = r.y0 + (c / nx) % ny, z = r.z0 + c / (nx * ny);
-        const int slot = atomicAdd(&cnt[(int)bucket_of(x, y, z, nb)], 1);
+        const int slot = atomicAdd(&cnt[base + (int)bucket_of(x, y, z, nb)], 1);
         if (scatter)
             ent[slot] = k;
         else if (slot >= kBucketSlots)
@@ -352,8 +353,7 @@ __global__ void k_bucket_sort(const int* start, int* ent, int nbuckets, bool ful
 // Rest-distance exclusion plus onset test on the current or previous
 // positions (abi41.cu:4696-4717).
 __device__ bool vv_valid(const View& v, int src, int other, float target, float onset) {
-    const Params& P = *v.P;
-    if (src < 0 || other < 0 || src >= P.V || other >= P.V || src == other || target <= 0.0f || onset <= target ||
+    if (src < 0 || other < 0 || src >= v.nV || other >= v.nV || src == other || target <= 0.0f || onset <= target ||
         !(__ldg(&v.inv_mass[src]) > 0.0f))
         return false;
     const F3 rd = f3(ld4(&v.rest[src])) - f3(ld4(&v.rest[other]));
@@ -364,41 +364,13 @@ __device__ bool vv_valid(const View& v, int src, int other, float target, float 
     return dot3(cd, cd) < onset * onset || dot3(pd, pd) < onset * onset;
 }
 
-__global__ void k_neighbors_hash(View v) {
-    const Params& P = *v.P;
+// Neighbour table without the vertex hash (cloths under 128 vertices): every
+// vertex of the cloth in index order (abi41.cu:4790-4814).
+__global__ void k_neighbors_brute(View v, int mode) {
     const int src = blockIdx.x * blockDim.x + threadIdx.x;
-    if (src >= P.V) return;
-    const float target = contact_radius(P);
-    if (target <= 0.0f) {
-        v.nb_count[src] = 0;
-        return;
-    }
-    const float onset = fmaxf(target * 1.8f, target + kEps);
-    const float4 p = v.pos[src];
-    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
-    int accepted = 0;
-    for (int dz = -1; dz <= 1 && accepted < kNeighborSlots; ++dz)
-        for (int dy = -1; dy <= 1 && accepted < kNeighborSlots; ++dy)
-            for (int dx = -1; dx <= 1 && accepted < kNeighborSlots; ++dx) {
-                const int qx = cx + dx, qy = cy + dy, qz = cz + dz;
-                const int b = (int)bucket_of(qx, qy, qz, P.vbuckets);
-                const int s = v.vb_start[b];
-                const int lim = min(v.vb_start[b + 1] - s, kBucketSlots);
-                for (int k = 0; k < lim && accepted < kNeighborSlots; ++k) {
-                    const int other = v.vb_ent[s + k];
-                    const int4 oc = v.vcell[other];
-                    if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
-                    v.nb_idx[src * kNeighborSlots + accepted++] = other;
-                }
-            }
-    if (accepted >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
-    v.nb_count[src] = accepted;
-}
-
-__global__ void k_neighbors_brute(View v) {
-    const Params& P = *v.P;
-    const int src = blockIdx.x * blockDim.x + threadIdx.x;
-    if (src >= P.V) return;
+    if (src >= v.nV) return;
+    const Params& P = params_v(v, src);
+    if (P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) {
         v.nb_count[src] = 0;
@@ -406,7 +378,7 @@ __global__ void k_neighbors_brute(View v) {
     }
     const float onset = fmaxf(target * 1.8f, target + kEps);
     int accepted = 0;
-    for (int other = 0; other < P.V && accepted < kNeighborSlots; ++other) {
+    for (int other = P.vstart; other < P.vstart + P.V && accepted < kNeighborSlots; ++other) {
         if (!vv_valid(v, src, other, target, onset)) continue;
         v.nb_idx[src * kNeighborSlots + accepted++] = other;
     }
@@ -419,9 +391,10 @@ __global__ void k_neighbors_brute(View v) {
 // else an overlap push; responses clamped to 0.35 thickness
 // (abi41.cu:4816-4951).
 __global__ void __launch_bounds__(kThreads) k_vv(View v) {
-    const Params& P = *v.P;
     const int src = blockIdx.x * blockDim.x + threadIdx.x;
-    if (src >= P.V) return;
+    if (src >= v.nV) return;
+    const Params& P = params_v(v, src);
+    if (!fast_mode(P) || !self_scheduled(P, v)) return;
     if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
     const int count = v.nb_count[src];
     if (count == 0) return;
@@ -435,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) k_vv(View v) {
     long long ax = 0, ay = 0, az = 0, aw = 0;
     for (int n = 0; n < lim; ++n) {
         const int other = v.nb_idx[src * kNeighborSlots + n];
-        if (other < 0 || other >= P.V || other == src) continue;
+        if (other < 0 || other >= v.nV || other == src) continue;
         if (fast)
             count1(v.counts, kCntFilterSeen);
         else
@@ -498,7 +471,7 @@ __global__ void __launch_bounds__(kThreads) k_vv(View v) {
                 const F3 nrm = resp * (1.0f / fmaxf(len3(resp), kEps));
                 const F3 mid = (pc + qc) * 0.5f;
                 const unsigned key = cluster_key(0, mid, nrm, fmaxf(th * 2.5f, 1.0e-3f));
-                if (!try_local_accept(v, 0, key, &cl)) continue;
+                if (!try_local_accept(v, P, 0, key, &cl)) continue;
                 count1(v.counts, kCntSelfCandidates);
             }
             ax += to_fix(resp.x);
@@ -529,13 +502,12 @@ __device__ bool rest_vt_neighbor(const View& v, int vertex, int4 t, float target
 
 // Soft vertex-triangle push with barycentric split (abi41.cu:4990-5107).
 // Returns whether the pair counts toward the vertex's neighbour budget.
-__device__ bool vt_pair(const View& v, int vertex, int tri, float target, float onset, Clusters* cl) {
-    const Params& P = *v.P;
-    if (tri < 0 || tri >= P.T || target <= 0.0f || onset <= target) return false;
+__device__ bool vt_pair(const View& v, const Params& P, int vertex, int tri, float target, float onset, Clusters* cl) {
+    if (tri < 0 || tri >= v.nT || target <= 0.0f || onset <= target) return false;
     const int4 t = __ldg(&v.tris[tri]);
-    if (!tri_valid(P, t)) return false;
+    if (!tri_valid(v.nV, t)) return false;
     if (rest_vt_neighbor(v, vertex, t, target, onset)) {
-        filter_count(v, kCntFilterRejectedRest);
+        filter_count(v, P, kCntFilterRejectedRest);
         return false;
     }
     const F3 p = f3(v.pos[vertex]), a = f3(v.pos[t.x]), b = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
@@ -563,7 +535,7 @@ __device__ bool vt_pair(const View& v, int vertex, int tri, float target, float 
     }
     if (fast_mode(P)) {
         const unsigned key = cluster_key(1, q, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
-        if (!try_local_accept(v, 1, key, cl)) return true;
+        if (!try_local_accept(v, P, 1, key, cl)) return true;
     }
     count1(v.counts, kCntSelfCandidates);
     float wa, wb, wc;
@@ -602,38 +574,37 @@ __device__ int neighbor_budget(const Params& P) {
 // Vertex-triangle query over the vertex's own cell bucket only
 // (abi41.cu:5109-5182).
 __global__ void __launch_bounds__(kThreads) k_vt_hash(View v) {
-    const Params& P = *v.P;
     const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vertex >= P.V) return;
+    if (vertex >= v.nV) return;
+    const Params& P = params_v(v, vertex);
+    if (!P.thash || !fast_mode(P) || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const int budget = neighbor_budget(P);
     const float4 p = v.pos[vertex];
-    const int b = (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
+    const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
     const int s = v.tb_start[b];
     const int lim = min(v.tb_start[b + 1] - s, kBucketSlots);
     int accepted = 0;
-    if (!fast_mode(P)) {
-        for (int k = 0; k < lim && accepted < budget; ++k)
-            if (vt_pair(v, vertex, v.tb_ent[s + k], target, onset, nullptr)) ++accepted;
-        return;
-    }
     Seen seen;
     seen.n = 0;
     Clusters cl;
     cl.n = 0;
     for (int k = 0; k < lim && accepted < budget; ++k) {
         const int tri = v.tb_ent[s + k];
-        if (!try_note_seen(v, tri, &seen)) continue;
-        if (vt_pair(v, vertex, tri, target, onset, &cl)) ++accepted;
+        if (!try_note_seen(v, P, tri, &seen)) continue;
+        if (vt_pair(v, P, vertex, tri, target, onset, &cl)) ++accepted;
     }
 }
 
+// Vertex-triangle query without the triangle hash (cloths under 64
+// triangles): every triangle of the cloth (abi41.cu:5184-5224).
 __global__ void __launch_bounds__(kThreads) k_vt_brute(View v) {
-    const Params& P = *v.P;
     const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vertex >= P.V) return;
+    if (vertex >= v.nV) return;
+    const Params& P = params_v(v, vertex);
+    if (P.thash || P.T <= 0 || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
@@ -641,9 +612,9 @@ __global__ void __launch_bounds__(kThreads) k_vt_brute(View v) {
     Clusters cl;
     cl.n = 0;
     int accepted = 0;
-    for (int tri = 0; tri < P.T && accepted < budget; ++tri) {
-        if (!try_note_seen(v, tri, nullptr)) continue;
-        if (vt_pair(v, vertex, tri, target, onset, &cl)) ++accepted;
+    for (int tri = P.tstart; tri < P.tstart + P.T && accepted < budget; ++tri) {
+        if (!try_note_seen(v, P, tri, nullptr)) continue;
+        if (vt_pair(v, P, vertex, tri, target, onset, &cl)) ++accepted;
     }
 }
 
@@ -661,13 +632,12 @@ __device__ bool rest_ee_neighbor(const View& v, int2 ea, int2 eb, float target, 
 
 // Soft edge-edge push split by the closest-point parameters
 // (abi41.cu:5595-5722).
-__device__ bool ee_pair(const View& v, int ia, int ib, float target, float onset, Clusters* cl) {
-    const Params& P = *v.P;
-    if (ib <= ia || ia < 0 || ib < 0 || ia >= P.E || ib >= P.E || target <= 0.0f || onset <= target) return false;
+__device__ bool ee_pair(const View& v, const Params& P, int ia, int ib, float target, float onset, Clusters* cl) {
+    if (ib <= ia || ia < 0 || ib < 0 || ia >= v.nE || ib >= v.nE || target <= 0.0f || onset <= target) return false;
     const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
-    if (!edge_valid(P, ea) || !edge_valid(P, eb)) return false;
+    if (!edge_valid(v.nV, ea) || !edge_valid(v.nV, eb)) return false;
     if (rest_ee_neighbor(v, ea, eb, target, onset)) {
-        filter_count(v, kCntFilterRejectedRest);
+        filter_count(v, P, kCntFilterRejectedRest);
         return false;
     }
     const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
@@ -700,7 +670,7 @@ __device__ bool ee_pair(const View& v, int ia, int ib, float target, float onset
     }
     if (fast_mode(P)) {
         const unsigned key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
-        if (!try_local_accept(v, 2, key, cl)) return true;
+        if (!try_local_accept(v, P, 2, key, cl)) return true;
     }
     count1(v.counts, kCntSelfCandidates);
     const float pen = target - dist;
@@ -729,40 +699,39 @@ __device__ bool ee_pair(const View& v, int ia, int ib, float target, float onset
 // Edge-edge query over the bucket of the edge midpoint's cell
 // (abi41.cu:5724-5802).
 __global__ void __launch_bounds__(kThreads) k_ee_hash(View v) {
-    const Params& P = *v.P;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= P.E) return;
+    if (e >= v.nE) return;
+    const Params& P = params_e(v, e);
+    if (!P.ehash || !fast_mode(P) || !self_scheduled(P, v)) return;
     const int2 ed = __ldg(&v.edges[e]);
-    if (!edge_valid(P, ed)) return;
+    if (!edge_valid(v.nV, ed)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const int budget = neighbor_budget(P);
     const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
-    const int b = (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
+    const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
     const int s = v.eb_start[b];
     const int lim = min(v.eb_start[b + 1] - s, kBucketSlots);
     int accepted = 0;
-    if (!fast_mode(P)) {
-        for (int k = 0; k < lim && accepted < budget; ++k)
-            if (ee_pair(v, e, v.eb_ent[s + k], target, onset, nullptr)) ++accepted;
-        return;
-    }
     Seen seen;
     seen.n = 0;
     Clusters cl;
     cl.n = 0;
     for (int k = 0; k < lim && accepted < budget; ++k) {
         const int other = v.eb_ent[s + k];
-        if (!try_note_seen(v, other, &seen)) continue;
-        if (ee_pair(v, e, other, target, onset, &cl)) ++accepted;
+        if (!try_note_seen(v, P, other, &seen)) continue;
+        if (ee_pair(v, P, e, other, target, onset, &cl)) ++accepted;
     }
 }
 
+// Edge-edge query without the edge hash (cloths under 64 edges): later edges
+// of the cloth (abi41.cu:5804-5844).
 __global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
-    const Params& P = *v.P;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= P.E) return;
+    if (e >= v.nE) return;
+    const Params& P = params_e(v, e);
+    if (P.ehash || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
@@ -770,9 +739,9 @@ __global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
     Clusters cl;
     cl.n = 0;
     int accepted = 0;
-    for (int other = e + 1; other < P.E && accepted < budget; ++other) {
-        if (!try_note_seen(v, other, nullptr)) continue;
-        if (ee_pair(v, e, other, target, onset, &cl)) ++accepted;
+    for (int other = e + 1; other < P.estart + P.E && accepted < budget; ++other) {
+        if (!try_note_seen(v, P, other, nullptr)) continue;
+        if (ee_pair(v, P, e, other, target, onset, &cl)) ++accepted;
     }
 }
 
@@ -802,11 +771,12 @@ __device__ __forceinline__ long long warp_sum64(long long v) {
 
 // VV neighbour table: lane l < 27 scans cell (dz, dy, dx) = (l/9-1, l/3%3-1,
 // l%3-1), the reference's nested-loop order (abi41.cu:4756-4781).
-__global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v) {
-    const Params& P = *v.P;
+__global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v, int mode) {
     const int src = warp_global_id();
     const int lane = threadIdx.x & 31;
-    if (src >= P.V) return;
+    if (src >= v.nV) return;
+    const Params& P = params_v(v, src);
+    if (!P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) {
         if (lane == 0) v.nb_count[src] = 0;
@@ -819,7 +789,7 @@ __global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v) {
     int nfound = 0;
     if (lane < 27) {
         const int qx = cx + lane % 3 - 1, qy = cy + (lane / 3) % 3 - 1, qz = cz + lane / 9 - 1;
-        const int b = (int)bucket_of(qx, qy, qz, P.vbuckets);
+        const int b = P.vbase + (int)bucket_of(qx, qy, qz, P.vbuckets);
         const int st = v.vb_start[b];
         const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
         for (int k = 0; k < lim; ++k) {
@@ -840,10 +810,11 @@ __global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v) {
 
 // VV responses (strict): lane n handles neighbour n of the source vertex.
 __global__ void __launch_bounds__(kThreads) k_vv_warp(View v) {
-    const Params& P = *v.P;
     const int src = warp_global_id();
     const int lane = threadIdx.x & 31;
-    if (src >= P.V) return;
+    if (src >= v.nV) return;
+    const Params& P = params_v(v, src);
+    if (fast_mode(P) || !self_scheduled(P, v)) return;
     if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
     const int count = min(v.nb_count[src], kNeighborSlots);
     if (count == 0) return;
@@ -851,7 +822,7 @@ __global__ void __launch_bounds__(kThreads) k_vv_warp(View v) {
     int candidate = 0, contact = 0;
     if (lane < count) {
         const int other = v.nb_idx[src * kNeighborSlots + lane];
-        if (other >= 0 && other < P.V && other != src) {
+        if (other >= 0 && other < v.nV && other != src) {
             candidate = 1;
             const F3 pc = f3(v.pos[src]), pp = f3(v.prev[src]);
             const float target = contact_radius(P);
@@ -950,10 +921,9 @@ struct SoftPush {
 // test runs before the rest-pose test: both only reject, and strict mode
 // counts neither, so the outcome is the same.
 __device__ bool vt_eval(const View& v, int vertex, int tri, float target, float onset, SoftPush* out) {
-    const Params& P = *v.P;
-    if (tri < 0 || tri >= P.T) return false;
+    if (tri < 0 || tri >= v.nT) return false;
     const int4 t = __ldg(&v.tris[tri]);
-    if (!tri_valid(P, t)) return false;
+    if (!tri_valid(v.nV, t)) return false;
     if (vertex == t.x || vertex == t.y || vertex == t.z) return false;
     const F3 p = f3(v.pos[vertex]), a = f3(v.pos[t.x]), b = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
     const F3 q = closest_on_triangle(p, a, b, c);
@@ -1010,10 +980,9 @@ __device__ bool vt_eval(const View& v, int vertex, int tri, float target, float 
 // without the fast-mode filter; current distance tested before the rest
 // pose, as above).
 __device__ bool ee_eval(const View& v, int ia, int ib, float target, float onset, SoftPush* out) {
-    const Params& P = *v.P;
-    if (ib <= ia || ia < 0 || ib < 0 || ia >= P.E || ib >= P.E) return false;
+    if (ib <= ia || ia < 0 || ib < 0 || ia >= v.nE || ib >= v.nE) return false;
     const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
-    if (!edge_valid(P, ea) || !edge_valid(P, eb)) return false;
+    if (!edge_valid(v.nV, ea) || !edge_valid(v.nV, eb)) return false;
     if (ea.x == eb.x || ea.x == eb.y || ea.y == eb.x || ea.y == eb.y) return false;
     const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
     float s, t;
@@ -1099,15 +1068,16 @@ __device__ __forceinline__ void commit_pushes(const View& v, bool accepted, cons
 // Strict VT: one warp per vertex, lane k = slot k of the vertex's own cell
 // bucket (abi41.cu:5129-5143).
 __global__ void __launch_bounds__(kThreads) k_vt_warp(View v) {
-    const Params& P = *v.P;
     const int vertex = warp_global_id();
     const int lane = threadIdx.x & 31;
-    if (vertex >= P.V) return;
+    if (vertex >= v.nV) return;
+    const Params& P = params_v(v, vertex);
+    if (!P.thash || fast_mode(P) || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const float4 p = v.pos[vertex];
-    const int b = (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
+    const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
     const int st = v.tb_start[b];
     const int lim = min(v.tb_start[b + 1] - st, kBucketSlots);
     if (lim == 0) return;
@@ -1120,17 +1090,18 @@ __global__ void __launch_bounds__(kThreads) k_vt_warp(View v) {
 // Strict EE: one warp per edge, lane k = slot k of the midpoint's cell
 // bucket (abi41.cu:5724-5758).
 __global__ void __launch_bounds__(kThreads) k_ee_warp(View v) {
-    const Params& P = *v.P;
     const int e = warp_global_id();
     const int lane = threadIdx.x & 31;
-    if (e >= P.E) return;
+    if (e >= v.nE) return;
+    const Params& P = params_e(v, e);
+    if (!P.ehash || fast_mode(P) || !self_scheduled(P, v)) return;
     const int2 ed = __ldg(&v.edges[e]);
-    if (!edge_valid(P, ed)) return;
+    if (!edge_valid(v.nV, ed)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
-    const int b = (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
+    const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
     const int st = v.eb_start[b];
     const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     if (lim == 0) return;
@@ -1144,9 +1115,10 @@ __global__ void __launch_bounds__(kThreads) k_ee_warp(View v) {
 // Fast mode, final pass: aggregate push for a vertex buried in >= 3 nearby
 // triangles of the 27-cell neighbourhood (abi41.cu:5226-5439).
 __global__ void __launch_bounds__(kThreads) k_island(View v) {
-    const Params& P = *v.P;
     const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vertex >= P.V) return;
+    if (vertex >= v.nV) return;
+    const Params& P = params_v(v, vertex);
+    if (!fast_mode(P) || !P.thash || P.T <= 0 || !self_scheduled(P, v) || v.pass != P.self_passes - 1) return;
     if (!(__ldg(&v.inv_mass[vertex]) > 0.0f)) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
@@ -1169,7 +1141,7 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
     for (int dz = -1; dz <= 1 && contacts < max_contacts && scanned < scan_limit; ++dz)
         for (int dy = -1; dy <= 1 && contacts < max_contacts && scanned < scan_limit; ++dy)
             for (int dx = -1; dx <= 1 && contacts < max_contacts && scanned < scan_limit; ++dx) {
-                const int b = (int)bucket_of(cx + dx, cy + dy, cz + dz, P.tbuckets);
+                const int b = P.tbase + (int)bucket_of(cx + dx, cy + dy, cz + dz, P.tbuckets);
                 const int s = v.tb_start[b];
                 const int lim = min(v.tb_start[b + 1] - s, kBucketSlots);
                 for (int k = 0; k < lim && contacts < max_contacts && scanned < scan_limit; ++k) {
@@ -1182,12 +1154,12 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
                             break;
                         }
                     if (dup) continue;
-                    if (tri < 0 || tri >= P.T) {
+                    if (tri < 0 || tri >= v.nT) {
                         count1(v.counts, kCntIslandGuarded);
                         continue;
                     }
                     const int4 t = __ldg(&v.tris[tri]);
-                    if (!tri_valid(P, t) || rest_vt_neighbor(v, vertex, t, target, onset)) continue;
+                    if (!tri_valid(v.nV, t) || rest_vt_neighbor(v, vertex, t, target, onset)) continue;
                     const F3 a = f3(v.pos[t.x]), b2 = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
                     const F3 ap = f3(v.prev[t.x]), bp = f3(v.prev[t.y]), cp = f3(v.prev[t.z]);
                     if (!finite3(a) || !finite3(b2) || !finite3(c) || !finite3(ap) || !finite3(bp) || !finite3(cp)) {
@@ -1273,9 +1245,10 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
 // Average the accumulated pushes, clamp to 0.35 r, apply with a 0.55 prev
 // shift, and clear the accumulators for the next pass (abi41.cu:4953-4988).
 __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
-    const Params& P = *v.P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.V) return;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!self_scheduled(P, v)) return;
     const Acc4 a = v.acc[i];
     v.acc[i] = Acc4{0, 0, 0, 0};
     if (!(__ldg(&v.inv_mass[i]) > 0.0f) || a.w <= 0) return;
@@ -1322,37 +1295,27 @@ void self_build_edge_hash(const View& v, int E, int nb, bool order, cudaStream_t
 }
 inline int warp_blocks(long long items) { return (int)((items * 32 + kThreads - 1) / kThreads); }
 
-void self_neighbors(const View& v, int V, bool hashed, cudaStream_t s) {
+void self_neighbors(const View& v, int V, int mode, const SelfVariants& sv, cudaStream_t s) {
     if (V <= 0) return;
-    if (hashed)
-        k_neighbors_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
-    else
-        k_neighbors_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
+    if (sv.hashed_v) k_neighbors_warp<<<warp_blocks(V), kThreads, 0, s>>>(v, mode);
+    if (sv.brute_v) k_neighbors_brute<<<blocks_for(V), kThreads, 0, s>>>(v, mode);
 }
-void self_vv(const View& v, int V, bool strict, cudaStream_t s) {
+void self_vv(const View& v, int V, const SelfVariants& sv, cudaStream_t s) {
     if (V <= 0) return;
-    if (strict)
-        k_vv_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
-    else
-        k_vv<<<blocks_for(V), kThreads, 0, s>>>(v);
+    if (sv.strict) k_vv_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
+    if (sv.fast) k_vv<<<blocks_for(V), kThreads, 0, s>>>(v);
 }
-void self_vt(const View& v, int V, bool hashed, bool strict, cudaStream_t s) {
+void self_vt(const View& v, int V, const SelfVariants& sv, cudaStream_t s) {
     if (V <= 0) return;
-    if (hashed && strict)
-        k_vt_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
-    else if (hashed)
-        k_vt_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
-    else
-        k_vt_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
+    if (sv.hashed_t && sv.strict) k_vt_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
+    if (sv.hashed_t && sv.fast) k_vt_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
+    if (sv.brute_t) k_vt_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
 }
-void self_ee(const View& v, int E, bool hashed, bool strict, cudaStream_t s) {
+void self_ee(const View& v, int E, const SelfVariants& sv, cudaStream_t s) {
     if (E <= 0) return;
-    if (hashed && strict)
-        k_ee_warp<<<warp_blocks(E), kThreads, 0, s>>>(v);
-    else if (hashed)
-        k_ee_hash<<<blocks_for(E), kThreads, 0, s>>>(v);
-    else
-        k_ee_brute<<<blocks_for(E), kThreads, 0, s>>>(v);
+    if (sv.hashed_e && sv.strict) k_ee_warp<<<warp_blocks(E), kThreads, 0, s>>>(v);
+    if (sv.hashed_e && sv.fast) k_ee_hash<<<blocks_for(E), kThreads, 0, s>>>(v);
+    if (sv.brute_e) k_ee_brute<<<blocks_for(E), kThreads, 0, s>>>(v);
 }
 void self_island(const View& v, int V, cudaStream_t s) {
     if (V > 0) k_island<<<blocks_for(V), kThreads, 0, s>>>(v);

@@ -71,11 +71,16 @@ enum Counter {
 // Scalar slots of the CG solve (same roles as abi41.cu:158-164).
 enum PcgSlot { kRedDAD = 0, kRedRZ = 1, kRedRZNext = 2, kRedStatus = 3, kRedInitialRZ = 4, kRedIterations = 5, kRedSlots = 8 };
 
-// Values that can change between frames without changing the launch
-// sequence.  They live in device memory so a captured CUDA graph stays valid
-// when the caller moves a collider or the pins.
+// Parameters of one cloth.  A solver holds one or more cloths concatenated
+// in every per-vertex / per-constraint array (a batch); each kernel reads the
+// parameters of the cloth its item belongs to.  They live in device memory so
+// a captured CUDA graph stays valid when the caller moves a collider, the
+// pins or the static SDF of a cloth.
 struct Params {
-    int V, E, T, B, L;
+    // this cloth's ranges in the concatenated arrays
+    int vstart, V, estart, E, tstart, T, B, L;
+    int active;      // 0: every kernel skips this cloth's items
+    float sub_dt;    // frame dt / substeps of the current step
     float damping;
     float gravity[3];
     float stretch_compliance;
@@ -93,21 +98,27 @@ struct Params {
     int use_sphere;
     float sphere_center[3];
     float sphere_radius;
-    // static SDF
+    // static SDF of this cloth's collider
     int sdf_ready;
     int sdf_signed;
     int sdf_dim[3];
     float sdf_origin[3];
     float sdf_voxel;
     int static_tri_count;
+    const float* sdf;
+    const float4* static_tris;  // 3 per triangle
     // self collision
+    int self_on;           // enabled with a positive contact distance
+    int self_interval;
+    int self_passes;
     float self_radius;     // contact target distance r
     int self_mode;         // 1 fast, 2 strict
-    int max_neighbors;     // clamp of cfg.max_self_collision_neighbors
+    int max_neighbors;     // cfg.max_self_collision_neighbors as given
     float vcell, tcell, ecell;
-    int vbuckets, tbuckets, ebuckets;
-    int vhash, thash, ehash;  // hash in use (else brute force)
-    float stretch_strength;   // clamp01(stretch_optimization_strength)
+    int vbuckets, tbuckets, ebuckets;  // this cloth's table sizes
+    int vbase, tbase, ebase;           // offsets of its tables in the shared bucket arrays
+    int vhash, thash, ehash;           // hash in use (else brute force)
+    float stretch_strength;            // clamp01(stretch_optimization_strength)
 };
 
 // Buffers of the hard-stretch CG solve and the averaged caps.
@@ -127,9 +138,17 @@ struct PcgView {
     unsigned* max_delta_bits;
 };
 
-// Device pointers of one solver, passed by value to each kernel.
+// Device pointers of one solver, passed by value to each kernel, plus the
+// launch context of the frame schedule.
 struct View {
-    const Params* P;
+    const Params* P;      // one per cloth
+    const int* vcloth;    // cloth of each vertex / edge / triangle (null for one cloth)
+    const int* ecloth;
+    const int* tcloth;
+    int nV, nE, nT, nB, K;  // totals over all cloths
+    int substep, substeps;  // position in the frame schedule
+    int pass;               // self-collision pass (-1 outside the passes)
+    int last_it;            // launch belongs to the last iteration
     float4* pos_in;       // snapshot read by gathers
     float4* pos;          // position written by this kernel / in place
     float4* prev;
@@ -150,31 +169,37 @@ struct View {
     const float4* pin_target;  // per vertex
     const float* pin_weight;   // per vertex; -1 = no pin
     const float* pin_relax;    // per vertex soft-pin relaxation
-    const int* tri_off;   // vertex -> incident triangles (for normals)
-    const int* tri_inc;
     unsigned long long* counts;
-    // static SDF
-    const float* sdf;
-    const float4* static_tris;  // 3 per triangle
     // self collision
-    int4* vcell;            // cx, cy, cz, bucket per vertex
-    int* vb_count;          // [vbuckets]
-    int* vb_start;          // [vbuckets + 1]
-    int* vb_ent;            // [V]
+    int4* vcell;            // cx, cy, cz, global bucket per vertex
+    int* vb_count;          // [all cloths' vertex buckets]
+    int* vb_start;          // [+1]
+    int* vb_ent;            // [nV]
     int* tb_count;
     int* tb_start;
     int* tb_ent;
-    int* ecount;            // per-primitive cell-entry counts scratch
     int* eb_count;
     int* eb_start;
     int* eb_ent;
     int* scan_tmp;          // block sums of the bucket scans
-    int tb_capacity, eb_capacity;
-    int* nb_count;          // [V]
-    int* nb_idx;            // [V * 32]
-    Acc4* acc;         // fixed-point delta xyz + contact weight
+    int* nb_count;          // [nV]
+    int* nb_idx;            // [nV * 32]
+    Acc4* acc;              // fixed-point delta xyz + contact weight
     unsigned* max_delta_bits;
 };
+
+__device__ __forceinline__ int cloth_of(const int* map, int i) { return map ? __ldg(&map[i]) : 0; }
+__device__ __forceinline__ const Params& params_v(const View& v, int i) { return v.P[cloth_of(v.vcloth, i)]; }
+__device__ __forceinline__ const Params& params_e(const View& v, int e) { return v.P[cloth_of(v.ecloth, e)]; }
+__device__ __forceinline__ const Params& params_t(const View& v, int t) { return v.P[cloth_of(v.tcloth, t)]; }
+
+// Whether a cloth runs self collision in this substep (and, inside the
+// passes, in this pass) (abi41.cu:9255-9262, 9291).
+__device__ __forceinline__ bool self_scheduled(const Params& P, const View& v) {
+    if (!P.active || !P.self_on) return false;
+    if (!(((v.substep + 1) % P.self_interval) == 0 || v.substep == v.substeps - 1)) return false;
+    return v.pass < 0 || v.pass < P.self_passes;
+}
 
 // Warp-aggregated counter increment: one atomic per warp, lane count from the
 // active mask.
@@ -199,7 +224,7 @@ void pcg_solve(const View& v, const PcgView& g, int V, cudaStream_t s, long long
 void pcg_averaged_pass(const View& v, const PcgView& g, int V, bool tiny, cudaStream_t s);
 // kind: 0 normal cap, 1 tiny cap, 2 extreme cap
 void pcg_cap_range(const View& v, int start, int count, float dt, int kind, cudaStream_t s);
-void launch_predict(const View& v, int V, float dt, cudaStream_t s);
+void launch_predict(const View& v, int V, cudaStream_t s);
 // pass flags for launch_vertex_pass
 enum PassFlags : unsigned {
     kPassSpring = 1u,
@@ -211,23 +236,29 @@ enum PassFlags : unsigned {
     kPassTether = 64u,
     kPassBend = 128u,
 };
-void launch_vertex_pass(const View& v, int V, float dt, unsigned flags, cudaStream_t s);
-void launch_bend_color(const View& v, int start, int count, float dt, cudaStream_t s);
+void launch_vertex_pass(const View& v, int V, unsigned flags, cudaStream_t s);
+void launch_bend_color(const View& v, int start, int count, cudaStream_t s);
 void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s);
 void launch_pack_positions(float* dst, const float4* src, int V, cudaStream_t s);
-void launch_sdf_build(const View& v, int voxels, cudaStream_t s);
+void launch_sdf_build(const View& v, int cloth, int voxels, cudaStream_t s);
 
-// self collision (bucket counts must be zeroed before each hash build)
+// self collision (bucket counts must be zeroed before each hash build; nb =
+// total buckets over all cloths)
 void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s);
 // `order` = false leaves buckets of <= 32 members in scatter order (valid
 // only for strict queries with a 32-candidate budget)
 void self_build_triangle_hash(const View& v, int T, int nb, bool order, cudaStream_t s);
 void self_build_edge_hash(const View& v, int E, int nb, bool order, cudaStream_t s);
-void self_neighbors(const View& v, int V, bool hashed, cudaStream_t s);
-// `strict` selects the warp-per-item kernels (no order-dependent filters)
-void self_vv(const View& v, int V, bool strict, cudaStream_t s);
-void self_vt(const View& v, int V, bool hashed, bool strict, cudaStream_t s);
-void self_ee(const View& v, int E, bool hashed, bool strict, cudaStream_t s);
+// Each launcher runs the kernel variants that some cloth needs; every item
+// skips cloths of another mode / table kind.  `mode`: 1 fast cloths only,
+// 2 strict only, 0 both.
+struct SelfVariants {
+    bool fast, strict, hashed_v, brute_v, hashed_t, brute_t, hashed_e, brute_e;
+};
+void self_neighbors(const View& v, int V, int mode, const SelfVariants& sv, cudaStream_t s);
+void self_vv(const View& v, int V, const SelfVariants& sv, cudaStream_t s);
+void self_vt(const View& v, int V, const SelfVariants& sv, cudaStream_t s);
+void self_ee(const View& v, int E, const SelfVariants& sv, cudaStream_t s);
 void self_island(const View& v, int V, cudaStream_t s);
 void self_apply(const View& v, int V, cudaStream_t s);
 

@@ -211,8 +211,8 @@ __device__ void sdf_stage(const View& v, const Params& P, float inv_mass, float 
     const float margin = fmaxf(P.margin, 0.0f);
     if (margin <= 0.0f) return;
     float d = 0.0f;
-    if (!sdf_sample(P, v.sdf, s->p, &d) || d >= margin) return;
-    const F3 n = sdf_normal(P, v.sdf, v.static_tris, s->p);
+    if (!sdf_sample(P, P.sdf, s->p, &d) || d >= margin) return;
+    const F3 n = sdf_normal(P, P.sdf, P.static_tris, s->p);
     if (!finite3(n)) return;
     const float pen = margin - d;
     if (!isfinite(pen) || pen <= 0.0f) return;
@@ -408,10 +408,12 @@ __device__ __forceinline__ void bend_term(const Params& P, unsigned long long* c
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_predict(View v, float dt) {
-    const Params& P = *v.P;
+__global__ void __launch_bounds__(kThreads) k_predict(View v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.V) return;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.active) return;
+    const float dt = P.sub_dt;
     const float4 p4 = v.pos[i];
     const float inv_mass = __ldg(&v.inv_mass[i]);
     VState s;
@@ -433,11 +435,16 @@ __global__ void __launch_bounds__(kThreads) k_predict(View v, float dt) {
     v.vel[i] = f4(s.vel, 0.0f);
 }
 
-__global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, float dt, unsigned flags) {
-    const Params& P = *v.P;
+__global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, unsigned flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.V) return;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    const float dt = P.sub_dt;
     const float4 p4 = v.pos_in[i];
+    if (!P.active) {
+        if (v.pos != v.pos_in) v.pos[i] = p4;  // keep the ping-pong buffers in step
+        return;
+    }
     VState s;
     s.w = p4.w;
     s.p = f3(p4);
@@ -470,7 +477,11 @@ __global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, float dt, unsi
     if (flags & kPassPin) pin_stage(v, i, inv_mass, dt, &s);
     if (flags & kPassAnalytic) analytic_stage(P, v.counts, inv_mass, dt, &s);
     if (flags & kPassSdf) sdf_stage(v, P, inv_mass, dt, &s);
-    if (flags & kPassPinPolish) pin_stage(v, i, inv_mass, dt, &s);
+    // final pin polish when this cloth ran a contact stage in this iteration
+    // (analytic colliders, SDF, or any last iteration; abi41.cu:9360-9369)
+    if ((flags & kPassPinPolish) &&
+        (v.last_it || P.use_ground || P.use_wall || P.use_sphere || P.sdf_ready))
+        pin_stage(v, i, inv_mass, dt, &s);
     if (flags & kPassVelocity) velocity_stage(P, dt, &s);
     v.pos[i] = f4(s.p, s.w);
     v.prev[i] = f4(s.prev, 0.0f);
@@ -479,21 +490,23 @@ __global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, float dt, unsi
 
 // Bend constraints of one colour, applied in place: no two bends of a colour
 // share a vertex (abi41.cu:2886-2970).
-__global__ void __launch_bounds__(kThreads) k_bend_color(View v, int start, int count, float dt) {
-    const Params& P = *v.P;
+__global__ void __launch_bounds__(kThreads) k_bend_color(View v, int start, int count) {
     const int local = blockIdx.x * blockDim.x + threadIdx.x;
     if (local >= count) return;
     const int b = start + local;
-    if (b < 0 || b >= P.B) {
+    if (b < 0 || b >= v.nB) {
         count1(v.counts, kCntBendingGuards);
         return;
     }
     const int2 pr = __ldg(&v.bends[b]);
     const int i = pr.x, j = pr.y;
-    if (i < 0 || j < 0 || i >= P.V || j >= P.V || i == j) {
+    if (i < 0 || j < 0 || i >= v.nV || j >= v.nV || i == j) {
         count1(v.counts, kCntBendingGuards);
         return;
     }
+    const Params& P = params_v(v, i);
+    if (!P.active) return;
+    const float dt = P.sub_dt;
     const float4 pi4 = v.pos[i], pj4 = v.pos[j];
     F3 corr;
     bool guard;
@@ -536,16 +549,16 @@ inline int vblocks_for(int n) { return (n + kVertexThreads - 1) / kVertexThreads
 
 }  // namespace
 
-void launch_predict(const View& v, int V, float dt, cudaStream_t s) {
-    if (V > 0) k_predict<<<vblocks_for(V), kVertexThreads, 0, s>>>(v, dt);
+void launch_predict(const View& v, int V, cudaStream_t s) {
+    if (V > 0) k_predict<<<vblocks_for(V), kVertexThreads, 0, s>>>(v);
 }
 
-void launch_vertex_pass(const View& v, int V, float dt, unsigned flags, cudaStream_t s) {
-    if (V > 0) k_vertex_pass<<<vblocks_for(V), kVertexThreads, 0, s>>>(v, dt, flags);
+void launch_vertex_pass(const View& v, int V, unsigned flags, cudaStream_t s) {
+    if (V > 0) k_vertex_pass<<<vblocks_for(V), kVertexThreads, 0, s>>>(v, flags);
 }
 
-void launch_bend_color(const View& v, int start, int count, float dt, cudaStream_t s) {
-    if (count > 0) k_bend_color<<<blocks_for(count), kThreads, 0, s>>>(v, start, count, dt);
+void launch_bend_color(const View& v, int start, int count, cudaStream_t s) {
+    if (count > 0) k_bend_color<<<blocks_for(count), kThreads, 0, s>>>(v, start, count);
 }
 
 void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s) {

@@ -222,6 +222,17 @@ def _load_library():
         "xpbd_gb300_stream": (vp, [vp]),
         "xpbd_gb300_profile_frame": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _PF,
                                                     ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+        "xpbd_gb300_batch_create": (vp, [ctypes.POINTER(NativeConfig), ctypes.POINTER(NativeMesh), ctypes.c_int]),
+        "xpbd_gb300_batch_cloth_count": (ctypes.c_int, [vp]),
+        "xpbd_gb300_batch_cloth_range": (ctypes.c_int, [vp, ctypes.c_int, _PI]),
+        "xpbd_gb300_batch_update_pin_targets": (ctypes.c_int, [vp, ctypes.c_int, _PI, _PF, _PF, ctypes.c_int]),
+        "xpbd_gb300_batch_update_runtime_colliders": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(NativeRuntimeColliders)]),
+        "xpbd_gb300_batch_update_static_triangles": (ctypes.c_int, [vp, ctypes.c_int, _PF, ctypes.c_int]),
+        "xpbd_gb300_batch_update_frame_inputs": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(NativeFrameInputs)]),
+        "xpbd_gb300_batch_update_positions": (ctypes.c_int, [vp, ctypes.c_int, _PF, ctypes.c_int]),
+        "xpbd_gb300_batch_download_positions": (ctypes.c_int, [vp, ctypes.c_int, _PF, ctypes.c_int]),
+        "xpbd_gb300_batch_reset_cloth": (ctypes.c_int, [vp, ctypes.c_int]),
+        "xpbd_gb300_batch_set_active": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):
@@ -471,3 +482,84 @@ class NativeXpbdSolver:
         self._check(self._lib.xpbd_gb300_profile_frame(self._handle, int(substeps), int(iterations), _fp(ms),
                                                         cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), n))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
+
+class NativeXpbdBatch(NativeXpbdSolver):
+    """Many independent cloths in one solver, stepped together: one launch
+    sequence (one CUDA graph per frame) covers every cloth.  Each cloth's
+    result is the same as when it runs alone.  ABI41 calls on the handle
+    address all cloths (positions concatenated in cloth order); the per-cloth
+    methods address one."""
+
+    def __init__(self, items):
+        """`items`: sequence of (ClothData, SolverOptions, static_triangles)."""
+        self._lib = _load_library()
+        items = list(items)
+        if not items:
+            raise NativeSolverError("A batch needs at least one cloth.")
+        n = len(items)
+        cfgs = (NativeConfig * n)()
+        meshes = (NativeMesh * n)()
+        keep = []
+        for k, (cloth, options, static) in enumerate(items):
+            cfgs[k] = config_from_options(cloth, options, static)
+            meshes[k], kk = mesh_arrays(cloth, static)
+            keep.append(kk)
+        self._handle = self._lib.xpbd_gb300_batch_create(cfgs, meshes, n)
+        del keep
+        if not self._handle:
+            raise NativeSolverError(_last_error(self._lib))
+        self._cloth_count = n
+        self._ranges = np.zeros((n, 4), np.int32)
+        for k in range(n):
+            self._check(self._lib.xpbd_gb300_batch_cloth_range(self._handle, k, _ip(self._ranges[k])))
+        self._vertex_count = int(self._ranges[:, 1].sum())
+        self._positions_out = np.empty((self._vertex_count, 3), np.float32)
+        self._static_triangle_count = max(len(it[2]) for it in items)
+        for k, (cloth, _, _) in enumerate(items):
+            if len(cloth.pin_indices) > 0:
+                self.update_cloth_pin_targets(k, cloth.pin_indices, cloth.pin_targets_world, cloth.pin_weights)
+
+    @property
+    def cloth_count(self) -> int:
+        return self._cloth_count
+
+    def cloth_vertices(self, cloth: int) -> tuple[int, int]:
+        """(first vertex, vertex count) of a cloth in the concatenated arrays."""
+        return int(self._ranges[cloth, 0]), int(self._ranges[cloth, 1])
+
+    def update_cloth_pin_targets(self, cloth: int, indices, positions, weights=None) -> None:
+        idx = np.ascontiguousarray(indices, np.int32)
+        pos = np.ascontiguousarray(positions, np.float32)
+        w = np.ones(len(idx), np.float32) if weights is None else np.ascontiguousarray(weights, np.float32).reshape(-1)
+        if len(idx) != len(pos) or len(idx) != len(w):
+            raise NativeSolverError("Pin index, target, and weight arrays must have matching lengths.")
+        self._check(self._lib.xpbd_gb300_batch_update_pin_targets(self._handle, int(cloth), _ip(idx), _fp(pos), _fp(w), len(idx)))
+
+    def update_cloth_colliders(self, cloth: int, options: SolverOptions) -> None:
+        c = colliders_from_options(options)
+        self._check(self._lib.xpbd_gb300_batch_update_runtime_colliders(self._handle, int(cloth), ctypes.byref(c)))
+
+    def update_cloth_static_triangles(self, cloth: int, static_triangles: np.ndarray) -> None:
+        t = np.ascontiguousarray(np.asarray(static_triangles, np.float32).reshape(-1, 3))
+        self._check(self._lib.xpbd_gb300_batch_update_static_triangles(self._handle, int(cloth), _fp(t), len(t) // 3))
+
+    def update_cloth_positions(self, cloth: int, positions: np.ndarray) -> None:
+        p = np.ascontiguousarray(positions, np.float32)
+        self._check(self._lib.xpbd_gb300_batch_update_positions(self._handle, int(cloth), _fp(p), p.size))
+
+    def download_cloth_positions(self, cloth: int) -> np.ndarray:
+        n = int(self._ranges[cloth, 1])
+        out = np.empty((n, 3), np.float32)
+        self._check(self._lib.xpbd_gb300_batch_download_positions(self._handle, int(cloth), _fp(out), out.size))
+        return out
+
+    def reset_cloth(self, cloth: int) -> None:
+        self._check(self._lib.xpbd_gb300_batch_reset_cloth(self._handle, int(cloth)))
+
+    def set_cloth_active(self, cloth: int, active: bool) -> None:
+        self._check(self._lib.xpbd_gb300_batch_set_active(self._handle, int(cloth), 1 if active else 0))
+
+    def split_positions(self, positions: np.ndarray) -> list[np.ndarray]:
+        """Per-cloth views of concatenated positions."""
+        return [positions[s:s + n] for s, n in ((int(r[0]), int(r[1])) for r in self._ranges)]

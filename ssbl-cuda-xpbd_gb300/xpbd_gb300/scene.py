@@ -372,3 +372,54 @@ def hardness_grid_scene(n: int = 32, hardness: float = 0.4, frames: int = 60) ->
     opt.lra_compliance = h["hidden_tether_compliance"] if h["hidden_tether_enabled"] else 0.0
     opt.cloth_thickness = 0.02
     return Scene(f"hardness-{hardness}-grid-{n}", cloth, opt, base.static_triangles, 10, 2, frames, 1.0)
+
+
+_GRID_CACHE: dict[tuple[int, float], ClothData] = {}
+
+
+def _unpinned_grid(n: int, z: float) -> ClothData:
+    """Constraint inputs of an unpinned n x n grid (cached: every cloth of a
+    batch with the same side shares its topology and rest state)."""
+    key = (n, z)
+    if key not in _GRID_CACHE:
+        pos, tris = grid_mesh(n, 1.0, z)
+        _GRID_CACHE[key] = build_cloth(pos, tris, 0.2, np.zeros(n * n, np.float32))
+    return _GRID_CACHE[key]
+
+
+def batched_scenes(count: int = 256, seed: int = 0, frames: int = 120, side_range: tuple = (16, 128)) -> list[Scene]:
+    """Independent cloths of uneven sizes for the batched form: side drawn
+    uniformly from `side_range` vertices (1 m cloths at z = 0.5), stretch and
+    bend compliance each log-uniform in [1e-8, 1e-4], 2-8 random hard pins,
+    self collision fast or strict with probability 0.5 (2 mm thickness), a
+    sphere (r = 0.3 m) below and the ground at z = -1; 10 substeps x 2
+    iterations."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(rng.integers(side_range[0], side_range[1] + 1))
+        base = _unpinned_grid(n, 0.5)
+        V = n * n
+        pins = np.sort(rng.choice(V, size=int(rng.integers(2, 9)), replace=False)).astype(np.int32)
+        inv = base.inv_mass.copy()
+        inv[pins] = 0.0
+        cloth = ClothData(
+            positions_world=base.positions_world, inv_mass=np.ascontiguousarray(inv, np.float32),
+            triangles=base.triangles, edges=base.edges, edge_rest_lengths=base.edge_rest_lengths,
+            edge_color_offsets=base.edge_color_offsets, bends=base.bends, bend_rest_lengths=base.bend_rest_lengths,
+            bend_color_offsets=base.bend_color_offsets, lra_edges=base.lra_edges, lra_rest_lengths=base.lra_rest_lengths,
+            lra_color_offsets=base.lra_color_offsets, pin_indices=pins,
+            pin_targets_world=np.ascontiguousarray(base.positions_world[pins], np.float32),
+            pin_weights=np.ones(len(pins), np.float32))
+        stretch = float(10.0 ** rng.uniform(-8.0, -4.0))
+        bend = float(10.0 ** rng.uniform(-8.0, -4.0))
+        fast = bool(rng.random() < 0.5)
+        opt = SolverOptions(dt=1.0 / 60.0, damping=0.99, stretch_compliance=stretch, bend_compliance=bend,
+                            collision_margin=0.002, cloth_thickness=0.002, use_sphere=True,
+                            sphere_center=(0.0, 0.0, 0.0), sphere_radius=0.3, use_ground=True, ground_height=-1.0,
+                            self_collision=True, self_collision_mode=1 if fast else 2,
+                            self_collision_interval=2 if fast else 1, max_self_collision_neighbors=32 if fast else 64,
+                            fast_self_collision_passes=4, contact_friction=0.3)
+        out.append(Scene(f"batch-{k}-grid-{n}", cloth, opt, np.empty((0, 3, 3), np.float32), 10, 2, frames, 1.0,
+                         {"side": n, "fast": fast}))
+    return out
