@@ -311,11 +311,11 @@ XG_EXPORT int xpbd_gb300_build_self_structures(void* handle) {
     }
     if (S->nTB > 0) {
         cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, S->stream);
-        self_build_triangle_hash(v, S->nT, S->nTB, true, S->stream);
+        self_build_triangle_hash(v, S->nT, S->nTB, 1, S->stream);
     }
     if (S->nEB > 0) {
         cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, S->stream);
-        self_build_edge_hash(v, S->nE, S->nEB, true, S->stream);
+        self_build_edge_hash(v, S->nE, S->nEB, 1, S->stream);
     }
     self_neighbors(v, S->nV, 0, sv, S->stream);
     return (cuda_ok(cudaGetLastError(), "build self structures") && cuda_ok(cudaStreamSynchronize(S->stream), "build self structures")) ? 1 : 0;

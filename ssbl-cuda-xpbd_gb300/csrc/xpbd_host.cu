@@ -323,6 +323,11 @@ void free_solver(Solver* S) {
     dfree(g.max_delta_bits);
     dfree(S->cap_edges);
     dfree(S->cap_rest);
+    for (int k = 0; k < 3; ++k) {
+        if (S->aux[k]) cudaStreamDestroy(S->aux[k]);
+        if (S->ev_join[k]) cudaEventDestroy(S->ev_join[k]);
+    }
+    if (S->ev_fork) cudaEventDestroy(S->ev_fork);
     if (S->stream) cudaStreamDestroy(S->stream);
     delete S;
 }
@@ -651,6 +656,11 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
     const int nV = S->nV, nE = S->nE, nT = S->nT;
 
     if (!cuda_ok(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking), "create solver stream")) return bail(0, "");
+    for (int k = 0; k < 3; ++k)
+        if (!cuda_ok(cudaStreamCreateWithFlags(&S->aux[k], cudaStreamNonBlocking), "create solver stream") ||
+            !cuda_ok(cudaEventCreateWithFlags(&S->ev_join[k], cudaEventDisableTiming), "create solver event"))
+            return bail(0, "");
+    if (!cuda_ok(cudaEventCreateWithFlags(&S->ev_fork, cudaEventDisableTiming), "create solver event")) return bail(0, "");
 
     // Concatenated host arrays; indices outside their cloth become -1.
     S->h_inv.resize(nV);
@@ -828,7 +838,8 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
         ok = dalloc(&S->nb_count, nV, "self collision count allocation") &&
              dalloc(&S->nb_idx, (size_t)nV * kNeighborSlots, "self collision index allocation") &&
              dalloc(&S->acc, nV, "self accumulation allocation") &&
-             dalloc(&S->scan_tmp, (size_t)std::max(std::max(S->nVB, S->nTB), S->nEB) / 4096 + 2, "bucket scan allocation");
+             dalloc(&S->scan_tmp, 3 * ((size_t)std::max(std::max(S->nVB, S->nTB), S->nEB) / 4096 + 2), "bucket scan allocation");
+        S->scan_seg = std::max(std::max(S->nVB, S->nTB), S->nEB) / 4096 + 2;
         if (ok && S->nVB > 0)
             ok = dalloc(&S->vcell, nV, "self collision cell allocation") &&
                  dalloc(&S->vb_count, S->nVB, "self collision hash count allocation") &&
@@ -927,7 +938,8 @@ namespace {
 struct SelfPlan {
     bool run = false;
     int passes = 0;
-    bool vhash = false, thash = false, ehash = false, order = false, any_t = false, any_e = false, island = false;
+    bool vhash = false, thash = false, ehash = false, any_t = false, any_e = false, island = false;
+    bool t_order = false, t_plain = false, e_order = false, e_plain = false;  // bucket order needs
     SelfVariants sv{};
     long long hits = 0, misses = 0;
 };
@@ -944,7 +956,8 @@ SelfPlan plan_self(const Solver* S, int s, int substeps) {
         p.vhash |= P.vhash != 0;
         p.thash |= P.thash != 0;
         p.ehash |= P.ehash != 0;
-        p.order |= C.order_buckets;
+        if (P.thash) (C.order_buckets ? p.t_order : p.t_plain) = true;
+        if (P.ehash) (C.order_buckets ? p.e_order : p.e_plain) = true;
         p.any_t |= P.T > 0;
         p.any_e |= P.E > 0;
         p.sv.fast |= C.fast;
@@ -963,6 +976,10 @@ SelfPlan plan_self(const Solver* S, int s, int substeps) {
     }
     return p;
 }
+
+// Bucket ordering mode of a hash build: 1 every bucket, 0 only buckets past
+// the 32 query slots, 2 decided per bucket from its cloth.
+int order_mode(bool need, bool plain) { return need ? (plain ? 2 : 1) : 0; }
 
 }  // namespace
 
@@ -1104,24 +1121,46 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
             const bool self_run = last_it && sp.run;
             if (self_run) {
                 flush();
+                // Independent self-collision work runs on side streams: the
+                // three hash builds, then in each pass the VV, VT and EE
+                // queries (and the fast-mode islands).  They only add to the
+                // integer accumulators and counters, so the result does not
+                // depend on their interleaving.  A profiled frame keeps
+                // everything on the solver stream so each kind is timed alone.
+                const bool par = prof == nullptr;
+                auto lane_stream = [&](int k) { return par ? S->aux[k] : S->stream; };
+                auto fork = [&]() {
+                    if (!par) return;
+                    cudaEventRecord(S->ev_fork, S->stream);
+                    for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(S->aux[k], S->ev_fork, 0);
+                };
+                auto join = [&]() {
+                    if (!par) return;
+                    for (int k = 0; k < 3; ++k) {
+                        cudaEventRecord(S->ev_join[k], S->aux[k]);
+                        cudaStreamWaitEvent(S->stream, S->ev_join[k], 0);
+                    }
+                };
                 View sv = cur_view();
+                View hv[3] = {sv, sv, sv};
+                for (int k = 0; k < 3; ++k) hv[k].scan_tmp = S->scan_tmp + (size_t)k * S->scan_seg;
+                fork();
                 if (sp.vhash)
                     timed(kKVertexHash, 6, [&] {
-                        cudaMemsetAsync(S->vb_count, 0, sizeof(int) * S->nVB, S->stream);
-                        self_build_vertex_hash(sv, nV, S->nVB, S->stream);
+                        cudaMemsetAsync(S->vb_count, 0, sizeof(int) * S->nVB, lane_stream(0));
+                        self_build_vertex_hash(hv[0], nV, S->nVB, lane_stream(0));
                     });
-                // strict queries with a 32-candidate budget do not depend on
-                // the order of buckets of <= 32 members
                 if (sp.thash)
                     timed(kKTriangleHash, 6, [&] {
-                        cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, S->stream);
-                        self_build_triangle_hash(sv, S->nT, S->nTB, sp.order, S->stream);
+                        cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, lane_stream(1));
+                        self_build_triangle_hash(hv[1], S->nT, S->nTB, order_mode(sp.t_order, sp.t_plain), lane_stream(1));
                     });
                 if (sp.ehash)
                     timed(kKEdgeHash, 6, [&] {
-                        cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, S->stream);
-                        self_build_edge_hash(sv, nE, S->nEB, sp.order, S->stream);
+                        cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, lane_stream(2));
+                        self_build_edge_hash(hv[2], nE, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
                     });
+                join();
                 if (sp.sv.fast) {
                     timed(kKNeighbors, 1, [&] { self_neighbors(sv, nV, 1, sp.sv, S->stream); });
                     st->cache_hits += sp.hits;
@@ -1130,11 +1169,13 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 for (int pass = 0; pass < sp.passes; ++pass) {
                     View pv2 = sv;
                     pv2.pass = pass;
-                    if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, nV, 2, sp.sv, S->stream); });
-                    timed(kKVertexVertex, 1, [&] { self_vv(pv2, nV, sp.sv, S->stream); });
-                    if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, nV, sp.sv, S->stream); });
-                    if (sp.any_e) timed(kKEdgeEdge, 1, [&] { self_ee(pv2, nE, sp.sv, S->stream); });
-                    if (sp.island) timed(kKIsland, 1, [&] { self_island(pv2, nV, S->stream); });
+                    fork();
+                    if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, nV, 2, sp.sv, lane_stream(0)); });
+                    timed(kKVertexVertex, 1, [&] { self_vv(pv2, nV, sp.sv, lane_stream(0)); });
+                    if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, nV, sp.sv, lane_stream(1)); });
+                    if (sp.island) timed(kKIsland, 1, [&] { self_island(pv2, nV, lane_stream(1)); });
+                    if (sp.any_e) timed(kKEdgeEdge, 1, [&] { self_ee(pv2, nE, sp.sv, lane_stream(2)); });
+                    join();
                     timed(kKSelfApply, 1, [&] { self_apply(pv2, nV, S->stream); });
                 }
             }

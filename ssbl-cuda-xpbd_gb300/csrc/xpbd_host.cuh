@@ -134,8 +134,12 @@ struct Solver {
     std::vector<Params> hp;     // one per cloth
     Params* dp = nullptr;
     bool params_dirty = true;
-    float params_dt_substeps = -1.0f;  // substeps the sub_dt fields were set for
     cudaStream_t stream = nullptr;
+    // side streams for independent self-collision work (captured into the
+    // frame graph as parallel branches), with fork / join events
+    cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[3] = {nullptr, nullptr, nullptr};
 
     int nV = 0, nE = 0, nT = 0, nB = 0, nL = 0;   // totals over the cloths
     int nVB = 0, nTB = 0, nEB = 0;                // total bucket counts
@@ -183,7 +187,8 @@ struct Solver {
     int *eb_count = nullptr, *eb_start = nullptr, *eb_ent = nullptr;
     int* nb_count = nullptr;
     int* nb_idx = nullptr;
-    int* scan_tmp = nullptr;
+    int* scan_tmp = nullptr;  // three segments: vertex, triangle, edge hash scans
+    int scan_seg = 0;
     Acc4* acc = nullptr;
 
     // hard-stretch optimisation (one-cloth solvers only)

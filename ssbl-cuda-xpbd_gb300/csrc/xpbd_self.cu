@@ -178,8 +178,7 @@ __global__ void k_vhash_count(View v) {
     const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
     const int b = P.vbase + (int)bucket_of(cx, cy, cz, P.vbuckets);
     v.vcell[i] = make_int4(cx, cy, cz, b);
-    const int slot = atomicAdd(&v.vb_count[b], 1);
-    if (slot >= kBucketSlots) count1(v.counts, kCntSelfOverflow);
+    atomicAdd(&v.vb_count[b], 1);  // overflow past 32 slots is counted from the totals in the scan
 }
 
 __global__ void k_vhash_scatter(View v) {
@@ -191,37 +190,40 @@ __global__ void k_vhash_scatter(View v) {
     v.vb_ent[atomicAdd(&v.vb_count[b], 1)] = i;
 }
 
-// Sixteen threads per primitive: thread c of primitive k handles cells c,
-// c + 16, ... of its cell box (at most 64 cells, z, y, x order).  `scatter`
-// = false counts entries per bucket; true writes them through the cursors
-// left by the scan.
-constexpr int kPrimLanes = 16;
+// Eight threads per primitive: thread r of primitive k walks the x rows
+// r, r + 8, ... of its cell box (at most 64 cells; rows indexed over (y, z)),
+// so the cell coordinates come from one division per row rather than per
+// cell.  `scatter` = false counts entries per bucket; true writes them
+// through the cursors left by the scan.  Entry order within a bucket is
+// fixed afterwards by k_bucket_sort.
+constexpr int kPrimLanes = 8;
 
 template <bool kTri>
 __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     const int n = kTri ? v.nT : v.nE;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = (int)(t / kPrimLanes), c0 = (int)(t % kPrimLanes);
+    const int k = (int)(t / kPrimLanes), r0 = (int)(t % kPrimLanes);
     if (k >= n) return;
     const Params& P = kTri ? params_t(v, k) : params_e(v, k);
     if (!(kTri ? P.thash : P.ehash) || !self_scheduled(P, v)) return;
     bool ok = false;
-    const CellRange r = kTri ? tri_cells(v, P, k, &ok, !scatter && c0 == 0) : edge_cells(v, P, k, &ok, !scatter && c0 == 0);
+    const CellRange r = kTri ? tri_cells(v, P, k, &ok, !scatter && r0 == 0) : edge_cells(v, P, k, &ok, !scatter && r0 == 0);
     if (!ok) return;
     const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
     if (nx <= 0 || ny <= 0 || nz <= 0) return;
-    const int cells = nx * ny * nz;
     int* cnt = kTri ? v.tb_count : v.eb_count;
     int* ent = kTri ? v.tb_ent : v.eb_ent;
     const int nb = kTri ? P.tbuckets : P.ebuckets;
     const int base = kTri ? P.tbase : P.ebase;
-    for (int c = c0; c < cells; c += kPrimLanes) {
-        const int x = r.x0 + c % nx, y = r.y0 + (c / nx) % ny, z = r.z0 + c / (nx * ny);
-        const int slot = atomicAdd(&cnt[base + (int)bucket_of(x, y, z, nb)], 1);
-        if (scatter)
-            ent[slot] = k;
-        else if (slot >= kBucketSlots)
-            count1(v.counts, kCntSelfOverflow);
+    for (int row = r0; row < ny * nz; row += kPrimLanes) {
+        const int y = r.y0 + row % ny, z = r.z0 + row / ny;
+        for (int x = r.x0; x <= r.x1; ++x) {
+            int* slot_counter = &cnt[base + (int)bucket_of(x, y, z, nb)];
+            if (scatter)
+                ent[atomicAdd(slot_counter, 1)] = k;
+            else
+                atomicAdd(slot_counter, 1);  // no return value needed: a reduction
+        }
     }
 }
 
@@ -256,11 +258,21 @@ __device__ __forceinline__ int block_exclusive_scan4(int (&vals)[4], int* warp_s
     return before;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_reduce(const int* counts, int n, int* block_sums) {
+// Also adds the number of insertions past each bucket's 32 query slots,
+// sum(max(0, count - 32)), to the overflow counter (the reference counts an
+// overflow for every insertion that finds its bucket full, abi41.cu:4569).
+__global__ void __launch_bounds__(1024) k_scan_reduce(const int* counts, int n, int* block_sums,
+                                                      unsigned long long* overflow) {
     __shared__ int ws[32];
     int vals[4];
     const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
-    for (int k = 0; k < 4; ++k) vals[k] = base + k < n ? counts[base + k] : 0;
+    int over = 0;
+    for (int k = 0; k < 4; ++k) {
+        vals[k] = base + k < n ? counts[base + k] : 0;
+        over += vals[k] > kBucketSlots ? vals[k] - kBucketSlots : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) over += __shfl_down_sync(0xffffffffu, over, o);
+    if (overflow && (threadIdx.x & 31) == 0 && over > 0) atomicAdd(overflow, (unsigned long long)over);
     int total;
     block_exclusive_scan4(vals, ws, &total);
     if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
@@ -305,47 +317,99 @@ __global__ void __launch_bounds__(1024) k_scan_down(int* counts, int* start, int
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) start[n] = run;
 }
 
-void scan_counts(int* counts, int* start, int n, int* block_sums, cudaStream_t s) {
+void scan_counts(int* counts, int* start, int n, int* block_sums, unsigned long long* overflow, cudaStream_t s) {
     const int blocks = (n + kScanTile - 1) / kScanTile;
-    k_scan_reduce<<<blocks, 1024, 0, s>>>(counts, n, block_sums);
+    k_scan_reduce<<<blocks, 1024, 0, s>>>(counts, n, block_sums, overflow);
     k_scan_sums<<<1, 1024, 0, s>>>(block_sums, blocks);
     k_scan_down<<<blocks, 1024, 0, s>>>(counts, start, n, block_sums);
 }
 
-// Order each bucket's members: buckets of up to 32 are copied to a local
-// array, insertion-sorted and written back; larger ones get the 32 smallest
-// ids moved to the front in order (queries read no further).
-// With `full` = false buckets of up to 32 members keep their scatter order:
-// a strict-mode query with a 32-candidate budget reads all of them and sums
-// their pushes in fixed point, so their order cannot change the result.
-__global__ void k_bucket_sort(const int* start, int* ent, int nbuckets, bool full) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbuckets) return;
-    const int s = start[b], n = start[b + 1] - s;
-    int* e = ent + s;
-    if (n <= 1) return;
-    if (n <= kBucketSlots) {
-        if (!full) return;
-        int tmp[kBucketSlots];
-        for (int i = 0; i < n; ++i) {
-            const int key = e[i];
-            int j = i - 1;
-            while (j >= 0 && tmp[j] > key) {
-                tmp[j + 1] = tmp[j];
-                --j;
-            }
-            tmp[j + 1] = key;
-        }
-        for (int i = 0; i < n; ++i) e[i] = tmp[i];
-        return;
+__device__ __forceinline__ int warp_global_id() { return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); }
+
+// Whether a cloth's queries depend on the order of a bucket's members: fast
+// mode (order-dependent filters) or a candidate budget under 32.  Strict
+// queries with a 32-candidate budget read every member of a bucket of up to
+// 32 and sum their pushes in fixed point, so its order cannot change them.
+__device__ __forceinline__ bool bucket_order_needed(const Params& P) {
+    const int budget = min(max(P.max_neighbors, 1), kBucketSlots);
+    return fast_mode(P) || budget < kBucketSlots;
+}
+
+// Order bucket members by primitive id.  One warp per 32 consecutive buckets:
+// each lane sorts its own bucket of up to 8 members in registers (odd-even
+// transposition network); a bucket of 9-32 members is sorted by the whole
+// warp (each lane ranks one member against all others with shuffles); a
+// larger one gets its 32 smallest ids moved to the front in order (queries
+// read no further).
+// `mode`: 0 order only buckets of more than 32, 1 order every bucket, 2 ask
+// the cloth of the bucket's first member (bucket_order_needed).  `kind`:
+// 1 triangle, 2 edge buckets (for mode 2).
+__global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* start, int* ent, int nbuckets, int kind,
+                                                          int mode) {
+    const int warp = warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if ((long long)warp * 32 >= nbuckets) return;
+    const int b = warp * 32 + lane;
+    int s = 0, n = 0;
+    if (b < nbuckets) {
+        s = start[b];
+        n = start[b + 1] - s;
     }
-    for (int i = 0; i < kBucketSlots; ++i) {
-        int best = i;
-        for (int j = i + 1; j < n; ++j)
-            if (e[j] < e[best]) best = j;
-        const int t = e[i];
-        e[i] = e[best];
-        e[best] = t;
+    bool need = n > kBucketSlots;
+    if (n >= 2 && n <= kBucketSlots) {
+        if (mode == 1) {
+            need = true;
+        } else if (mode == 2) {
+            const int first = ent[s];
+            need = bucket_order_needed(kind == 1 ? params_t(v, first) : params_e(v, first));
+        }
+    }
+    constexpr int kSmall = 8;
+    if (need && n <= kSmall) {
+        int r[kSmall];
+        int* e = ent + s;
+#pragma unroll
+        for (int k = 0; k < kSmall; ++k) r[k] = k < n ? e[k] : 0x7fffffff;
+#pragma unroll
+        for (int round = 0; round < kSmall; ++round) {
+#pragma unroll
+            for (int k = round & 1; k + 1 < kSmall; k += 2) {
+                const int lo = min(r[k], r[k + 1]), hi = max(r[k], r[k + 1]);
+                r[k] = lo;
+                r[k + 1] = hi;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kSmall; ++k)
+            if (k < n) e[k] = r[k];
+        need = false;
+    }
+    unsigned mask = __ballot_sync(0xffffffffu, need);
+    while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int sj = __shfl_sync(0xffffffffu, s, j), nj = __shfl_sync(0xffffffffu, n, j);
+        int* e = ent + sj;
+        if (nj <= kBucketSlots) {
+            const int key = lane < nj ? e[lane] : 0x7fffffff;
+            int rank = 0;
+            for (int k = 0; k < 32; ++k) {
+                const int o = __shfl_sync(0xffffffffu, key, k);
+                rank += (o < key || (o == key && k < lane)) ? 1 : 0;
+            }
+            __syncwarp();
+            if (lane < nj) e[rank] = key;
+        } else if (lane == 0) {
+            for (int i = 0; i < kBucketSlots; ++i) {
+                int best = i;
+                for (int q = i + 1; q < nj; ++q)
+                    if (e[q] < e[best]) best = q;
+                const int t = e[i];
+                e[i] = e[best];
+                e[best] = t;
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -696,34 +760,6 @@ __device__ bool ee_pair(const View& v, const Params& P, int ia, int ib, float ta
     return true;
 }
 
-// Edge-edge query over the bucket of the edge midpoint's cell
-// (abi41.cu:5724-5802).
-__global__ void __launch_bounds__(kThreads) k_ee_hash(View v) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= v.nE) return;
-    const Params& P = params_e(v, e);
-    if (!P.ehash || !fast_mode(P) || !self_scheduled(P, v)) return;
-    const int2 ed = __ldg(&v.edges[e]);
-    if (!edge_valid(v.nV, ed)) return;
-    const float target = contact_radius(P);
-    if (target <= 0.0f) return;
-    const float onset = fmaxf(target * 1.8f, target + kEps);
-    const int budget = neighbor_budget(P);
-    const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
-    const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
-    const int s = v.eb_start[b];
-    const int lim = min(v.eb_start[b + 1] - s, kBucketSlots);
-    int accepted = 0;
-    Seen seen;
-    seen.n = 0;
-    Clusters cl;
-    cl.n = 0;
-    for (int k = 0; k < lim && accepted < budget; ++k) {
-        const int other = v.eb_ent[s + k];
-        if (!try_note_seen(v, P, other, &seen)) continue;
-        if (ee_pair(v, P, e, other, target, onset, &cl)) ++accepted;
-    }
-}
 
 // Edge-edge query without the edge hash (cloths under 64 edges): later edges
 // of the cloth (abi41.cu:5804-5844).
@@ -753,7 +789,6 @@ __global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
 // keeps the first `budget` accepted candidates exactly as the serial loop
 // does.  Fixed-point sums make the accumulation order irrelevant.
 
-__device__ __forceinline__ int warp_global_id() { return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); }
 
 __device__ __forceinline__ int warp_exclusive_sum(int v, int lane) {
     int incl = v;
@@ -1040,17 +1075,35 @@ __device__ bool ee_eval(const View& v, int ia, int ib, float target, float onset
     return true;
 }
 
-// Commit the accepted pairs within the budget: candidate counter for each,
-// and the push for those that have one.
-__device__ __forceinline__ void commit_pushes(const View& v, bool accepted, const SoftPush& sp, int budget, int lane,
-                                              int contact_slot) {
-    const unsigned acc_mask = __ballot_sync(0xffffffffu, accepted);
-    const int rank = __popc(acc_mask & ((1u << lane) - 1u));
+// Strict VT / EE queries: a group of kQueryLanes lanes per query item walks
+// the item's bucket slots in chunks of kQueryLanes, lane k of a chunk taking
+// slot base + k.  Accepted pairs are ranked in slot order across the chunks
+// and the first `budget` of them are taken, as when one thread walks the
+// slots in order (abi41.cu:5129-5143, 5724-5758); evaluation has no side
+// effects, so the walk stops once the budget is reached.  Groups of 8 keep
+// most lanes busy for the typical 1-16 occupied slots and put four items'
+// dependent load chains in flight per warp.
+constexpr int kQueryLanes = 8;
+
+__device__ __forceinline__ unsigned group_mask() {
+    const int lane = threadIdx.x & 31;
+    return ((1u << kQueryLanes) - 1u) << (lane & ~(kQueryLanes - 1));
+}
+
+// Take the accepted pairs of one chunk whose rank (after `prior` earlier
+// acceptances) is within the budget: candidate counter for each, the push for
+// those that have one.  Returns the group's acceptances in this chunk.
+__device__ __forceinline__ int commit_chunk(const View& v, bool accepted, const SoftPush& sp, int prior, int budget,
+                                           int contact_slot) {
+    const unsigned gm = group_mask();
+    const int lane = threadIdx.x & 31;
+    const unsigned acc_mask = __ballot_sync(gm, accepted) & gm;
+    const int rank = prior + __popc(acc_mask & ((1u << lane) - 1u));
     const bool take = accepted && rank < budget;
     const bool push = take && sp.apply;
-    const unsigned take_mask = __ballot_sync(0xffffffffu, take);
-    const unsigned push_mask = __ballot_sync(0xffffffffu, push);
-    if (lane == 0) {
+    const unsigned take_mask = __ballot_sync(gm, take) & gm;
+    const unsigned push_mask = __ballot_sync(gm, push) & gm;
+    if ((lane & (kQueryLanes - 1)) == 0) {
         if (take_mask) count_add(v.counts, kCntSelfCandidates, __popc(take_mask));
         if (push_mask) count_add(v.counts, contact_slot, __popc(push_mask));
     }
@@ -1063,13 +1116,17 @@ __device__ __forceinline__ void commit_pushes(const View& v, bool accepted, cons
             if ((far ? -w : w) > 0.0f) accumulate(v, sp.idx[k], sp.delta * w);
         }
     }
+    return __popc(acc_mask);
 }
 
-// Strict VT: one warp per vertex, lane k = slot k of the vertex's own cell
-// bucket (abi41.cu:5129-5143).
-__global__ void __launch_bounds__(kThreads) k_vt_warp(View v) {
-    const int vertex = warp_global_id();
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ int group_item() {
+    return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / kQueryLanes);
+}
+
+// Strict VT: the vertex's own cell bucket (abi41.cu:5129-5143).
+__global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
+    const int vertex = group_item();
+    const int gl = threadIdx.x & (kQueryLanes - 1);
     if (vertex >= v.nV) return;
     const Params& P = params_v(v, vertex);
     if (!P.thash || fast_mode(P) || !self_scheduled(P, v)) return;
@@ -1080,18 +1137,21 @@ __global__ void __launch_bounds__(kThreads) k_vt_warp(View v) {
     const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
     const int st = v.tb_start[b];
     const int lim = min(v.tb_start[b + 1] - st, kBucketSlots);
-    if (lim == 0) return;
-    SoftPush sp;
-    sp.apply = false;
-    const bool accepted = lane < lim && vt_eval(v, vertex, v.tb_ent[st + lane], target, onset, &sp);
-    commit_pushes(v, accepted, sp, neighbor_budget(P), lane, kCntSoftContacts);
+    const int budget = neighbor_budget(P);
+    int prior = 0;
+    for (int base = 0; base < lim && prior < budget; base += kQueryLanes) {
+        SoftPush sp;
+        sp.apply = false;
+        const int slot = base + gl;
+        const bool accepted = slot < lim && vt_eval(v, vertex, v.tb_ent[st + slot], target, onset, &sp);
+        prior += commit_chunk(v, accepted, sp, prior, budget, kCntSoftContacts);
+    }
 }
 
-// Strict EE: one warp per edge, lane k = slot k of the midpoint's cell
-// bucket (abi41.cu:5724-5758).
-__global__ void __launch_bounds__(kThreads) k_ee_warp(View v) {
-    const int e = warp_global_id();
-    const int lane = threadIdx.x & 31;
+// Strict EE: the bucket of the edge midpoint's cell (abi41.cu:5724-5758).
+__global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
+    const int e = group_item();
+    const int gl = threadIdx.x & (kQueryLanes - 1);
     if (e >= v.nE) return;
     const Params& P = params_e(v, e);
     if (!P.ehash || fast_mode(P) || !self_scheduled(P, v)) return;
@@ -1104,11 +1164,213 @@ __global__ void __launch_bounds__(kThreads) k_ee_warp(View v) {
     const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
     const int st = v.eb_start[b];
     const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
-    if (lim == 0) return;
-    SoftPush sp;
-    sp.apply = false;
-    const bool accepted = lane < lim && ee_eval(v, e, v.eb_ent[st + lane], target, onset, &sp);
-    commit_pushes(v, accepted, sp, neighbor_budget(P), lane, kCntEdgeEdgeContacts);
+    const int budget = neighbor_budget(P);
+    int prior = 0;
+    for (int base = 0; base < lim && prior < budget; base += kQueryLanes) {
+        SoftPush sp;
+        sp.apply = false;
+        const int slot = base + gl;
+        const bool accepted = slot < lim && ee_eval(v, e, v.eb_ent[st + slot], target, onset, &sp);
+        prior += commit_chunk(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
+    }
+}
+
+// Fast-mode edge-edge pair as ee_pair walks it (rest test first, then the
+// current distance), without the cluster filter.  Returns 0 (no pair),
+// 1 (rejected by the rest pose), 2 (beyond the onset distance) or 3 (a
+// candidate: *key is its cluster key, *out its push).
+__device__ int ee_fast_classify(const View& v, int ia, int ib, float target, float onset, SoftPush* out, unsigned* key) {
+    if (ib <= ia || ia < 0 || ib < 0 || ia >= v.nE || ib >= v.nE || target <= 0.0f || onset <= target) return 0;
+    const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
+    if (!edge_valid(v.nV, ea) || !edge_valid(v.nV, eb)) return 0;
+    if (rest_ee_neighbor(v, ea, eb, target, onset)) return 1;
+    const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
+    float s, t;
+    segment_params(a0, a1, b0, b1, &s, &t);
+    const F3 pa = a0 + (a1 - a0) * s;
+    const F3 pb = b0 + (b1 - b0) * t;
+    const F3 d = pa - pb;
+    const float dsq = dot3(d, d);
+    float dist = sqrtf(fmaxf(dsq, kEps));
+    if (dist >= onset) return 2;
+    F3 nrm{0.0f, 0.0f, 1.0f};
+    if (dsq > kEps) {
+        nrm = d * (1.0f / dist);
+    } else {
+        nrm = cross3(a1 - a0, b1 - b0);
+        const float nl = dot3(nrm, nrm);
+        if (nl > kEps) {
+            nrm = nrm * (1.0f / sqrtf(nl));
+        } else {
+            const F3 r0 = f3(ld4(&v.rest[ea.x])), r1 = f3(ld4(&v.rest[ea.y]));
+            const F3 r2 = f3(ld4(&v.rest[eb.x])), r3 = f3(ld4(&v.rest[eb.y]));
+            float rs, rt;
+            segment_params(r0, r1, r2, r3, &rs, &rt);
+            const F3 rd = (r0 + (r1 - r0) * rs) - (r2 + (r3 - r2) * rt);
+            const float rl = dot3(rd, rd);
+            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+        }
+        dist = 0.0f;
+    }
+    *key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+    const float pen = target - dist;
+    float push;
+    if (pen > 0.0f) {
+        push = fminf(pen * 0.35f + target * 0.01f, target * 0.25f);
+    } else {
+        const float x = 1.0f - fminf(dist / onset, 1.0f);
+        push = fminf(x * x * target * 0.06f, target * 0.04f);
+    }
+    const float ma0 = __ldg(&v.inv_mass[ea.x]), ma1 = __ldg(&v.inv_mass[ea.y]);
+    const float mb0 = __ldg(&v.inv_mass[eb.x]), mb1 = __ldg(&v.inv_mass[eb.y]);
+    const float ws0 = 1.0f - s, ws1 = s, wt0 = 1.0f - t, wt1 = t;
+    const float total = ma0 * ws0 * ws0 + ma1 * ws1 * ws1 + mb0 * wt0 * wt0 + mb1 * wt1 * wt1;
+    out->apply = push > 0.0f && total > 0.0f;
+    if (out->apply) {
+        out->delta = nrm * (push / total);
+        out->idx[0] = ea.x;
+        out->idx[1] = ea.y;
+        out->idx[2] = eb.x;
+        out->idx[3] = eb.y;
+        out->w[0] = ma0 * ws0;
+        out->w[1] = ma1 * ws1;
+        out->w[2] = -(mb0 * wt0);
+        out->w[3] = -(mb1 * wt1);
+    }
+    return 3;
+}
+
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
+    for (int i = 0; i < n; ++i) m &= m - 1;
+    return __ffs(m) - 1;
+}
+
+// Fast-mode EE query in groups of kQueryLanes lanes with the exact outcome of
+// the serial walk of k_ee_hash (abi41.cu:5724-5802 with the filters of
+// 714-832): slots are visited in order until `budget` pairs have passed the
+// distance test; a slot whose edge id appeared at an earlier slot is a
+// duplicate; a passing pair is accepted when its cluster key is new and fewer
+// than 16 keys are held.  Fast-mode buckets are ordered by id (k_bucket_sort
+// orders every bucket of a fast cloth, and the first 32 members of larger
+// ones), so a duplicate is the same id as the slot before it.  The group
+// carries the accepted keys in registers (lane g holds keys g and g + 8).
+// Counters are summed per warp and added once at the end.
+__global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
+    const int e = group_item();
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (kQueryLanes - 1);
+    const int gbase = lane & ~(kQueryLanes - 1);
+    const unsigned gm = group_mask();
+    int c_seen = 0, c_dup = 0, c_rest = 0, c_own = 0, c_acc = 0, c_contact = 0;
+    bool run = e < v.nE;
+    const Params* P = nullptr;
+    if (run) {
+        P = &params_e(v, e);
+        run = P->ehash && fast_mode(*P) && self_scheduled(*P, v);
+    }
+    int2 ed = make_int2(-1, -1);
+    if (run) {
+        ed = __ldg(&v.edges[e]);
+        run = edge_valid(v.nV, ed) && contact_radius(*P) > 0.0f;
+    }
+    int st = 0, lim = 0, budget = 0;
+    float target = 0.0f, onset = 0.0f;
+    if (run) {
+        target = contact_radius(*P);
+        onset = fmaxf(target * 1.8f, target + kEps);
+        budget = neighbor_budget(*P);
+        const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
+        const int b =
+            P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell), cell_of(mid.y, P->ecell), cell_of(mid.z, P->ecell), P->ebuckets);
+        st = v.eb_start[b];
+        lim = min(v.eb_start[b + 1] - st, kBucketSlots);
+    }
+    unsigned keys[2] = {0u, 0u};
+    int nkeys = 0, accepted = 0, last_id = -1;
+    for (int c = 0; c < kBucketSlots / kQueryLanes; ++c) {
+        if (!(run && c * kQueryLanes < lim && accepted < budget)) break;  // uniform within the group
+        {
+            const int slot = c * kQueryLanes + gl;
+            const bool valid = slot < lim;
+            const int id = valid ? v.eb_ent[st + slot] : -1;
+            const int before = __shfl_sync(gm, id, gbase + ((gl + kQueryLanes - 1) & (kQueryLanes - 1)));
+            const bool dup = valid && id == (gl == 0 ? last_id : before);
+            last_id = __shfl_sync(gm, id, gbase + kQueryLanes - 1);
+            SoftPush sp;
+            sp.apply = false;
+            unsigned key = 0u;
+            const int cls = (valid && !dup) ? ee_fast_classify(v, e, id, target, onset, &sp, &key) : 0;
+            const unsigned pass_mask = (__ballot_sync(gm, cls == 3) >> gbase) & 0xffu;
+            const int remaining = budget - accepted;
+            const int cut = __popc(pass_mask) >= remaining ? nth_set_bit(pass_mask, remaining - 1) : kQueryLanes;
+            const bool visited = valid && gl <= cut;
+            c_seen += visited ? 1 : 0;
+            c_dup += (visited && dup) ? 1 : 0;
+            c_rest += (visited && cls == 1) ? 1 : 0;
+            const bool cand = visited && cls == 3;
+            const unsigned cand_mask = (__ballot_sync(gm, cand) >> gbase) & 0xffu;
+            if (cand_mask == 0u) {
+                accepted += __popc(pass_mask & ((cut >= kQueryLanes) ? 0xffu : ((2u << cut) - 1u)));
+                continue;
+            }
+            // cluster filter: new key among the held ones and the earlier
+            // candidates of this chunk, while fewer than 16 keys are held
+            bool first = cand;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const unsigned hk = __shfl_sync(gm, keys[j >> 3], gbase + (j & 7));
+                first = first && !(j < nkeys && hk == key);
+            }
+#pragma unroll
+            for (int j = 0; j < kQueryLanes; ++j) {
+                const unsigned ok = __shfl_sync(gm, key, gbase + j);
+                first = first && !(j < gl && ((cand_mask >> j) & 1u) && ok == key);
+            }
+            const unsigned first_mask = (__ballot_sync(gm, first) >> gbase) & 0xffu;
+            const int rank = __popc(first_mask & ((1u << gl) - 1u));
+            const bool take = first && nkeys + rank < 16;
+            const unsigned take_mask = (__ballot_sync(gm, take) >> gbase) & 0xffu;
+            c_own += (cand && !take) ? 1 : 0;
+            if (take) {
+                c_acc += 1;
+                if (sp.apply) {
+                    c_contact += 1;
+                    for (int k = 0; k < 4; ++k) {
+                        const float w = sp.w[k];
+                        if ((k > 1 ? -w : w) > 0.0f) accumulate(v, sp.idx[k], sp.delta * w);
+                    }
+                }
+            }
+            // append the taken keys in slot order: key position q is held by
+            // lane q % 8 in register q / 8
+            const int ntake = __popc(take_mask);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int q = gl + h * kQueryLanes;
+                const bool mine = q >= nkeys && q < nkeys + ntake;
+                const int src = mine ? nth_set_bit(take_mask, q - nkeys) : gl;
+                const unsigned got = __shfl_sync(gm, key, gbase + src);
+                if (mine) keys[h] = got;
+            }
+            nkeys += ntake;
+            accepted += __popc(pass_mask & ((cut >= kQueryLanes) ? 0xffu : ((2u << cut) - 1u)));
+        }
+    }
+    // one atomic per counter and warp
+    const int sums[6] = {c_seen, c_dup, c_rest, c_own, c_acc, c_contact};
+    const int slots[6] = {kCntFilterSeen, kCntFilterRejectedDuplicate, kCntFilterRejectedRest, kCntFilterRejectedOwnership,
+                          kCntFilterAcceptedEe, kCntEdgeEdgeContacts};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const int total = __reduce_add_sync(0xffffffffu, sums[q]);
+        if (lane == 0 && total > 0) count_add(v.counts, slots[q], (unsigned long long)total);
+    }
+    const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);
+    if (lane == 0 && acc_total > 0) {
+        count_add(v.counts, kCntClusterCount, (unsigned long long)acc_total);
+        count_add(v.counts, kCntClusterOwnedContacts, (unsigned long long)acc_total);
+        count_add(v.counts, kCntSelfCandidates, (unsigned long long)acc_total);
+    }
 }
 
 // ------------------------------------------------- fast overlap islands --
@@ -1266,34 +1528,36 @@ __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
 }  // namespace
 
 // Host-side entry points used by the solver orchestration.
+inline int warp_blocks(long long items) { return (int)((items * 32 + kThreads - 1) / kThreads); }
+inline int group_blocks(long long items) { return (int)((items * kQueryLanes + kThreads - 1) / kThreads); }
+
 struct SelfLaunch {
     static void vhash(const View& v, int V, int nb, cudaStream_t s) {
         k_vhash_count<<<blocks_for(V), kThreads, 0, s>>>(v);
-        scan_counts(v.vb_count, v.vb_start, nb, v.scan_tmp, s);
+        scan_counts(v.vb_count, v.vb_start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
         k_vhash_scatter<<<blocks_for(V), kThreads, 0, s>>>(v);
-        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(v.vb_start, v.vb_ent, nb, true);
+        k_bucket_sort<<<warp_blocks((nb + 31) / 32), kThreads, 0, s>>>(v, v.vb_start, v.vb_ent, nb, 0, 1);
     }
     template <bool kTri>
-    static void phash(const View& v, int n, int* count, int* start, int* ent, int nb, bool order, cudaStream_t s) {
+    static void phash(const View& v, int n, int* count, int* start, int* ent, int nb, int order, cudaStream_t s) {
         const long long threads = (long long)n * kPrimLanes;
         const int blocks = (int)((threads + kThreads - 1) / kThreads);
         k_prim_hash<kTri><<<blocks, kThreads, 0, s>>>(v, false);
-        scan_counts(count, start, nb, v.scan_tmp, s);
+        scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
         k_prim_hash<kTri><<<blocks, kThreads, 0, s>>>(v, true);
-        k_bucket_sort<<<blocks_for(nb), kThreads, 0, s>>>(start, ent, nb, order);
+        k_bucket_sort<<<warp_blocks((nb + 31) / 32), kThreads, 0, s>>>(v, start, ent, nb, kTri ? 1 : 2, order);
     }
 };
 
 void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s) {
     if (V > 0) SelfLaunch::vhash(v, V, nb, s);
 }
-void self_build_triangle_hash(const View& v, int T, int nb, bool order, cudaStream_t s) {
+void self_build_triangle_hash(const View& v, int T, int nb, int order, cudaStream_t s) {
     if (T > 0) SelfLaunch::phash<true>(v, T, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
 }
-void self_build_edge_hash(const View& v, int E, int nb, bool order, cudaStream_t s) {
+void self_build_edge_hash(const View& v, int E, int nb, int order, cudaStream_t s) {
     if (E > 0) SelfLaunch::phash<false>(v, E, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
 }
-inline int warp_blocks(long long items) { return (int)((items * 32 + kThreads - 1) / kThreads); }
 
 void self_neighbors(const View& v, int V, int mode, const SelfVariants& sv, cudaStream_t s) {
     if (V <= 0) return;
@@ -1307,14 +1571,14 @@ void self_vv(const View& v, int V, const SelfVariants& sv, cudaStream_t s) {
 }
 void self_vt(const View& v, int V, const SelfVariants& sv, cudaStream_t s) {
     if (V <= 0) return;
-    if (sv.hashed_t && sv.strict) k_vt_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
+    if (sv.hashed_t && sv.strict) k_vt_warp<<<group_blocks(V), kThreads, 0, s>>>(v);
     if (sv.hashed_t && sv.fast) k_vt_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
     if (sv.brute_t) k_vt_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
 }
 void self_ee(const View& v, int E, const SelfVariants& sv, cudaStream_t s) {
     if (E <= 0) return;
-    if (sv.hashed_e && sv.strict) k_ee_warp<<<warp_blocks(E), kThreads, 0, s>>>(v);
-    if (sv.hashed_e && sv.fast) k_ee_hash<<<blocks_for(E), kThreads, 0, s>>>(v);
+    if (sv.hashed_e && sv.strict) k_ee_warp<<<group_blocks(E), kThreads, 0, s>>>(v);
+    if (sv.hashed_e && sv.fast) k_ee_fast<<<group_blocks(E), kThreads, 0, s>>>(v);
     if (sv.brute_e) k_ee_brute<<<blocks_for(E), kThreads, 0, s>>>(v);
 }
 void self_island(const View& v, int V, cudaStream_t s) {

@@ -245,10 +245,11 @@ void launch_sdf_build(const View& v, int cloth, int voxels, cudaStream_t s);
 // self collision (bucket counts must be zeroed before each hash build; nb =
 // total buckets over all cloths)
 void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s);
-// `order` = false leaves buckets of <= 32 members in scatter order (valid
-// only for strict queries with a 32-candidate budget)
-void self_build_triangle_hash(const View& v, int T, int nb, bool order, cudaStream_t s);
-void self_build_edge_hash(const View& v, int E, int nb, bool order, cudaStream_t s);
+// `order`: 0 orders only buckets of more than 32 members (enough for strict
+// queries with a 32-candidate budget), 1 orders every bucket, 2 asks each
+// bucket's cloth
+void self_build_triangle_hash(const View& v, int T, int nb, int order, cudaStream_t s);
+void self_build_edge_hash(const View& v, int E, int nb, int order, cudaStream_t s);
 // Each launcher runs the kernel variants that some cloth needs; every item
 // skips cloths of another mode / table kind.  `mode`: 1 fast cloths only,
 // 2 strict only, 0 both.
