@@ -1,25 +1,37 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 XPBD cloth step (vertex-substeps/s).
 
-Workload (default ``drop10k``): a 100 x 100 cloth (10,000 vertices, 19,602
-triangles) with seeded +-1 mm jitter dropped onto a sphere (r = 0.3 m) and a
-64^3 static SDF of a box and a torus, strict spatial-hash self collision with
-2 mm thickness, friction 0.3; 10 substeps x 2 iterations per frame.  A
-"step" is one frame.  Inputs are seeded synthetic (no dataset exists).
+Workloads (a "step" is one frame of 10 substeps x 2 iterations):
+
+* ``batch256`` (default): 256 independent cloths, sides drawn uniformly from
+  16-128 vertices (1,589,788 vertices in all), stretch and bend compliance
+  log-uniform in [1e-8, 1e-4], 2-8 random hard pins per cloth, fast or
+  strict self collision (2 mm) with probability 0.5, a sphere and the ground;
+  all cloths run in one batched solver (one launch sequence per frame,
+  captured as one CUDA graph).  The same cloths are also run the plain way,
+  one ABI41 handle per cloth stepped back to back, and reported as ``plain``.
+* ``drop10k``: a 100 x 100 cloth (10,000 vertices) with seeded +-1 mm jitter
+  dropped onto a sphere (r = 0.3 m) and a 64^3 static SDF of a box and a
+  torus, strict self collision with 2 mm thickness, friction 0.3.
+* ``plain32``: 32 x 32 grid, two pinned corners, ground plane.
+
+Inputs are seeded synthetic (the reference uses no dataset).
 
 Timing: W untimed warm-up frames, then K frames, each bracketed by CUDA
 events on the solver's own stream; before every timed frame a 256 MiB buffer
-is written on that stream so L2 (129 MB) starts cold (the cloth's state is
-far smaller than L2).  ``value`` = vertices x substeps x K x N / time.
+is written on that stream so L2 (129 MB) starts cold.  ``value`` = vertices x
+substeps x K x N / time.
 
-Also reported: ``e2e`` through the C-ABI with host buffers (frame inputs
-uploaded, positions downloaded every frame), the per-kernel profile and the
-roofline of the dominant kernel, SM clocks sampled during the timed region,
-and the CPU oracle timed on a bounded sample of the same workload.
+Also reported: ``e2e`` through the C-ABI with host buffers (pin targets
+uploaded, positions downloaded every frame), the per-kernel profile of one
+un-graphed frame and the roofline of the dominant kernel kind, SM clocks
+sampled during the timed region, and the CPU oracle timed on a bounded
+sample of the same workload.
 
 ``--impl reference``: the reference's step has no CPU implementation and its
 CUDA solver cannot be carried to the GPU machine, so that arm times the CPU
-restatement of the reference's algorithm (oracle/) with all host threads.
+restatement of the reference's algorithm (oracle/) with all host threads, on
+a bounded sample of the workload's cloths per step.
 """
 from __future__ import annotations
 
@@ -42,31 +54,47 @@ from xpbd_gb300 import scene  # noqa: E402
 
 METRIC = "vertex-substeps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+F3 = 12  # bytes of a position / velocity row read or written (x, y, z f32)
 
-# Compulsory bytes per launch of each kernel kind: state rows read and
-# written once (16-byte rows, 4-byte scalars), constraint streams read once.
-# Candidate gathers of the self-collision queries are not counted, so these
-# are lower bounds for those kinds.
-def kernel_bytes(kind: str, V: int, E: int, T: int) -> float | None:
-    table = {
-        "predict": V * (16 * 2 + 16 * 3 + 4),        # R pos vel, W pos prev vel, R pin weight
-        "stretch_pass": V * (16 * 3 * 2 + 4 + 4 + 4) + 2 * E * 8,  # R/W pos prev vel, pin, inv, CSR off; 2E entries
-        "vertex_pass": V * (16 * 3 * 2 + 4 + 4),
-        "neighbors": V * (16 + 16 + 4) + V * 4,        # pos, cell, count
-        "vertex_vertex": V * (4 + 16 + 16 + 4 + 32),   # count, pos, prev, inv, acc
-        "vertex_triangle": V * (16 + 8),               # pos, bucket range
-        "edge_edge": E * (8 + 32 + 8),                 # edge, endpoints, bucket range
-        "self_apply": V * (32 * 2 + 16 * 2 * 2 + 4),   # acc R/W, pos prev R/W, inv
-    }
-    return table.get(kind)
+DESCRIPTIONS = {
+    "batch256": "256 independent cloths, side U{16..128} verts (1,589,788 verts), compliance log-uniform 1e-8..1e-4, "
+                "2-8 hard pins each, fast/strict self collision (2 mm, p=0.5), sphere + ground, one batched solver "
+                "(one CUDA graph per frame), 10 substeps x 2 iterations per frame",
+    "drop10k": "10k cloth (100x100 grid, 19,602 tris) dropped on a sphere + 64^3 box/torus SDF, strict self "
+               "collision 2 mm, friction 0.3, 10 substeps x 2 iterations per frame",
+    "plain32": "plain 32x32 grid (1,024 verts), two pinned corners, ground, 10 substeps x 2 iterations",
+}
 
 
-def workload(name: str):
+def workload(name: str) -> list:
+    if name == "batch256":
+        return scene.batched_scenes(256, seed=0, frames=120)
     if name == "drop10k":
-        return scene.drop_scene(100, 200, seed=0, self_mode=2)
+        return [scene.drop_scene(100, 200, seed=0, self_mode=2)]
     if name == "plain32":
-        return scene.plain_grid_scene(32, 120)
+        return [scene.plain_grid_scene(32, 120)]
     raise SystemExit(f"unknown workload {name}")
+
+
+def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict) -> float | None:
+    """Compulsory bytes of one launch of a kernel kind (x, v rows of 12 B,
+    constraint entries of 12 B: two indices and a rest length).  The query
+    kinds count what a query must read: its own item, its bucket range, and
+    per bucket slot evaluated the candidate id, indices and positions (slot
+    counts measured in the profiled frame)."""
+    if kind == "predict":
+        return 52.0 * V                                   # R x v w, W x prev
+    if kind == "stretch_pass":
+        return 12.0 * E + 24.0 * V + 36.0 * V             # constraint stream, x R/W, contact stages R x v W x
+    if kind == "vertex_pass":
+        return 52.0 * V                                   # velocity update R x prev W v x
+    if kind == "bend_color":
+        return 12.0 * B + 48.0 * B                        # constraint stream, 2 endpoints R/W
+    if kind == "edge_edge" and counters.get("ee_items"):
+        return (8 + 2 * F3 + 8) * counters["ee_items"] + (4 + 8 + 2 * F3) * counters["ee_slots"]
+    if kind == "vertex_triangle" and counters.get("vt_items"):
+        return (F3 + 8) * counters["vt_items"] + (4 + 12 + 3 * F3) * counters["vt_slots"]
+    return None
 
 
 def peaks() -> tuple[float, str]:
@@ -139,73 +167,124 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_oracle_rate(sc, budget_s: float, warm: int = 1) -> tuple[float, int, str]:
+def oracle_sample(scs: list, target_vertices: int) -> list:
+    """The first cloths of the workload, up to about `target_vertices`."""
+    out, v = [], 0
+    for sc in scs:
+        out.append(sc)
+        v += len(sc.cloth.positions_world)
+        if v >= target_vertices:
+            break
+    return out
+
+
+def cpu_oracle_rate(scs: list, budget_s: float) -> tuple[float, int, str]:
+    """The oracle (all host threads) stepping cloths of the workload one
+    frame each, in workload order, for about `budget_s` seconds."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import xpbd_oracle
 
     threads = xpbd_oracle.set_threads(os.cpu_count() or 1)
-    o = xpbd_oracle.OracleSolver.from_scene(sc.cloth, sc.options, sc.static_triangles)
-    for _ in range(warm):
-        o.step(sc.substeps, sc.iterations)
-    frames, t0 = 0, time.perf_counter()
-    while True:
-        o.step(sc.substeps, sc.iterations)
-        frames += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or frames >= 400:
+    work, elapsed, cloths, frames_per = 0, 0.0, 0, 1 if len(scs) > 1 else 400
+    for sc in scs:
+        o = xpbd_oracle.OracleSolver.from_scene(sc.cloth, sc.options, sc.static_triangles)
+        o.step(sc.substeps, sc.iterations)  # warm-up frame
+        V = len(sc.cloth.positions_world)
+        t0 = time.perf_counter()
+        n = 0
+        while n < frames_per:
+            o.step(sc.substeps, sc.iterations)
+            n += 1
+            if elapsed + time.perf_counter() - t0 >= budget_s:
+                break
+        elapsed += time.perf_counter() - t0
+        work += V * sc.substeps * n
+        cloths += 1
+        if elapsed >= budget_s:
             break
-    V = len(sc.cloth.positions_world)
-    return V * sc.substeps * frames / el, threads, f"{frames} frames after {warm} warm-up, {el:.1f} s"
+    if len(scs) > 1:
+        what = f"first {cloths} cloths of the workload, one warm-up frame then one timed frame each, {elapsed:.1f} s"
+    else:
+        what = f"{n} frames after one warm-up frame, {elapsed:.1f} s"
+    return work / elapsed, threads, what
 
 
-def run_reference(args, sc, world, rank):
+def run_reference(args, scs, world, rank):
+    """Reference arm: the CPU restatement on a bounded sample per step."""
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import xpbd_oracle
 
     threads = xpbd_oracle.set_threads(os.cpu_count() or 1)
-    o = xpbd_oracle.OracleSolver.from_scene(sc.cloth, sc.options, sc.static_triangles)
+    sample = oracle_sample(scs, 60000) if len(scs) > 1 else scs
+    solvers = [xpbd_oracle.OracleSolver.from_scene(s.cloth, s.options, s.static_triangles) for s in sample]
+    V = sum(len(s.cloth.positions_world) for s in sample)
+    S, I = sample[0].substeps, sample[0].iterations
     for _ in range(args.warmup):
-        o.step(sc.substeps, sc.iterations)
+        for o in solvers:
+            o.step(S, I)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        o.step(sc.substeps, sc.iterations)
+        for o in solvers:
+            o.step(S, I)
     el = time.perf_counter() - t0
-    V = len(sc.cloth.positions_world)
-    value = V * sc.substeps * args.steps / el
+    value = V * S * args.steps / el
+    what = (f"first {len(sample)} of the workload's {len(scs)} cloths ({V} vertices) per step, one frame each"
+            if len(scs) > 1 else "the whole workload, one frame per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload_desc, "vertices": V, "substeps": sc.substeps, "iterations": sc.iterations},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} frames of the same workload after {args.warmup} warm-up frames"},
+        "config": {"workload": DESCRIPTIONS[args.workload], "vertices_per_step": V, "substeps": S, "iterations": I},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": what},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's step exists only as CUDA code; this arm is the C restatement of its algorithm on the host cores",
     }
     print(json.dumps(line), flush=True)
 
 
+def time_plain(native, scs, frames: int) -> dict:
+    """The plain drop-in: one ABI41 handle per cloth, stepped back to back
+    (no per-handle sync) with one wait per frame, like the reference add-on
+    steps its cloths."""
+    solvers = [native.NativeXpbdSolver(s.cloth, s.options, s.static_triangles) for s in scs]
+    S, I = scs[0].substeps, scs[0].iterations
+    V = sum(len(s.cloth.positions_world) for s in scs)
+    for _ in range(2):
+        for s in solvers:
+            s.step(S, I, diagnostics=False, synchronize=False)
+        for s in solvers:
+            s.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        for s in solvers:
+            s.step(S, I, diagnostics=False, synchronize=False)
+        for s in solvers:
+            s.synchronize()
+    el = time.perf_counter() - t0
+    launches = sum(s.last_step_launches() for s in solvers)
+    for s in solvers:
+        s.close()
+    return {"value": V * S * frames / el, "unit": METRIC, "ms_per_step": 1000.0 * el / frames, "frames": frames,
+            "handles": len(scs), "launches_per_step": launches}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="drop10k", choices=["drop10k", "plain32"])
+    ap.add_argument("--workload", default="batch256", choices=sorted(DESCRIPTIONS))
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--plain-frames", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
-    sc = workload(args.workload)
-    args.workload_desc = {
-        "drop10k": "10k cloth (100x100 grid, 19,602 tris) dropped on a sphere + 64^3 box/torus SDF, strict self "
-                   "collision 2 mm, friction 0.3, 10 substeps x 2 iterations per frame",
-        "plain32": "plain 32x32 grid (1,024 verts), two pinned corners, ground, 10 substeps x 2 iterations",
-    }[args.workload]
+    scs = workload(args.workload)
     if args.impl == "reference":
-        run_reference(args, sc, world, rank)
+        run_reference(args, scs, world, rank)
         return
 
     import torch
@@ -219,11 +298,16 @@ def main():
     from xpbd_gb300 import build, native
 
     build.build()
-    V = len(sc.cloth.positions_world)
-    E = len(sc.cloth.edges)
-    T = len(sc.cloth.triangles)
-    S, I = sc.substeps, sc.iterations
-    solver = native.NativeXpbdSolver(sc.cloth, sc.options, sc.static_triangles)
+    V = sum(len(s.cloth.positions_world) for s in scs)
+    E = sum(len(s.cloth.edges) for s in scs)
+    T = sum(len(s.cloth.triangles) for s in scs)
+    B = sum(len(s.cloth.bends) for s in scs)
+    S, I = scs[0].substeps, scs[0].iterations
+    batched = len(scs) > 1
+    if batched:
+        solver = native.NativeXpbdBatch([(s.cloth, s.options, s.static_triangles) for s in scs])
+    else:
+        solver = native.NativeXpbdSolver(scs[0].cloth, scs[0].options, scs[0].static_triangles)
     for _ in range(args.warmup):
         solver.step(S, I, diagnostics=False, synchronize=False)
     solver.synchronize()
@@ -250,67 +334,90 @@ def main():
     launches_per_step = solver.last_step_launches()
     value = V * S * args.steps * world / (total_ms / 1000.0)
 
-    # per-kernel profile of one un-graphed frame (events around each launch)
-    prof = {}
-    for _ in range(3):
+    # per-kernel profile of un-graphed frames (events around each launch on
+    # the solver stream) and the work counters of the query kernels
+    prof, counters = {}, {}
+    reps = 2
+    for _ in range(reps):
         p = solver.profile_frame(S, I)
         for k, (ms, n) in p.items():
             a = prof.setdefault(k, [0.0, 0])
             a[0] += ms
             a[1] += n
+        for k, c in solver.profile_counters().items():
+            counters[k] = counters.get(k, 0) + c
     dominant = max(prof.items(), key=lambda kv: kv[1][0])[0]
     dom_ms, dom_n = prof[dominant]
     avg_ms = dom_ms / max(dom_n, 1)
     peak, peak_kind = peaks()
-    alg = kernel_bytes(dominant, V, E, T)
+    alg_total = algorithmic_bytes(dominant, V, E, T, B, counters)
     roof = None
-    if alg is not None and avg_ms > 0:
-        achieved = alg / (avg_ms / 1000.0) / 1e9
+    if alg_total is not None and avg_ms > 0:
+        # counters and launches cover all profiled frames; bytes per launch
+        per_launch = alg_total / max(dom_n, 1) if dominant in ("edge_edge", "vertex_triangle") else alg_total
+        achieved = per_launch / (avg_ms / 1000.0) / 1e9
         roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": None,
-                "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": alg}
-    profile_summary = {k: {"ms_per_frame": v[0] / 3.0, "launches_per_frame": v[1] / 3.0} for k, v in prof.items() if v[1]}
+                "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch}
+    profile_summary = {k: {"ms_per_frame": v[0] / reps, "launches_per_frame": v[1] / reps} for k, v in prof.items() if v[1]}
 
-    # end to end through the C-ABI with host buffers
+    # end to end through the C-ABI with host buffers: every frame the pin
+    # targets of all cloths go up and all positions come back
     lib = native._load_library()
     out = torch.empty((V, 3), dtype=torch.float32).pin_memory().numpy()
-    colliders = native.colliders_from_options(sc.options)
-    fi = native.NativeFrameInputs()
-    fi.update_runtime_colliders = 1
-    fi.runtime_colliders = colliders
-    h2d = ctypes.sizeof(native.NativeRuntimeColliders)
+    pin_idx, pin_pos, pin_w = [], [], []
+    base = 0
+    for s in scs:
+        pin_idx.append(s.cloth.pin_indices.astype(np.int32) + base)
+        pin_pos.append(s.cloth.pin_targets_world)
+        pin_w.append(s.cloth.pin_weights)
+        base += len(s.cloth.positions_world)
+    pin_idx = torch.from_numpy(np.concatenate(pin_idx)).pin_memory().numpy()
+    pin_pos = torch.from_numpy(np.ascontiguousarray(np.concatenate(pin_pos), np.float32)).pin_memory().numpy()
+    pin_w = torch.from_numpy(np.ascontiguousarray(np.concatenate(pin_w), np.float32)).pin_memory().numpy()
+    ip = pin_idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    pp = pin_pos.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    wp = pin_w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    h2d = pin_idx.nbytes + pin_pos.nbytes + pin_w.nbytes
     d2h = out.nbytes
     h = solver.handle
     fp = out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
-    for _ in range(2):
-        lib.ssbl_update_frame_inputs(h, ctypes.byref(fi))
-        lib.ssbl_step_solver_ex(h, S, I, 0, 0)
-        lib.ssbl_download_positions(h, fp, out.size)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ok = lib.ssbl_update_frame_inputs(h, ctypes.byref(fi)) and lib.ssbl_step_solver_ex(h, S, I, 0, 0) and \
+
+    def e2e_frame():
+        ok = lib.ssbl_update_pin_targets(h, ip, pp, wp, len(pin_idx)) and lib.ssbl_step_solver_ex(h, S, I, 0, 0) and \
             lib.ssbl_download_positions(h, fp, out.size)
         if not ok:
             raise RuntimeError(native._last_error(lib))
+
+    for _ in range(2):
+        e2e_frame()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_frame()
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": V * S * args.steps * world / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s / args.steps}
+    e2e = {"value": V * S * args.steps * world / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s / args.steps}
     assert np.isfinite(out).all()
+
+    plain = time_plain(native, scs, args.plain_frames) if batched else None
 
     if rank != 0:
         return
-    cpu_value, cores, sample = cpu_oracle_rate(sc, args.cpu_budget)
+    cpu_value, cores, sample = cpu_oracle_rate(scs, args.cpu_budget)
+    config = {"workload": DESCRIPTIONS[args.workload], "cloths": len(scs), "vertices": V, "edges": E, "triangles": T,
+              "substeps": S, "iterations": I, "frames_per_step": 1,
+              "l2": "256 MiB buffer written before every timed step", "parallelism": f"replicas x{world}"}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded grid cloth, box/torus collider)",
-        "config": {"workload": args.workload_desc, "vertices": V, "edges": E, "triangles": T, "substeps": S,
-                   "iterations": I, "frames_per_step": 1, "l2": "256 MiB buffer written before every timed step",
-                   "parallelism": f"replicas x{world}"},
+        "dtype": "f32", "data": "synthetic (seeded grid cloths, box/torus collider)", "config": config,
         "e2e": e2e, "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks.summary(),
-        "roofline": roof, "kernel_profile": profile_summary,
+        "roofline": roof, "kernel_profile": profile_summary, "work_counters_per_frame": {k: c / reps for k, c in counters.items()},
         "cpu_baseline": {"value": cpu_value, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
     }
+    if plain is not None:
+        line["plain"] = plain
+        line["batched_over_plain"] = value / plain["value"]
     print(json.dumps(line), flush=True)
 
 

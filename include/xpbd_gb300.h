@@ -60,6 +60,11 @@ __attribute__((visibility("default"))) void* xpbd_gb300_stream(void* handle);
 __attribute__((visibility("default"))) int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations,
                                                                      float* kernel_ms, long long* kernel_launches, int kinds);
 
+/* Work counters of the last xpbd_gb300_profile_frame: out4 = EE query items,
+ * EE bucket slots evaluated, VT query items (strict cloths), VT slots
+ * evaluated.  They size the algorithmic bytes of the query kernels. */
+__attribute__((visibility("default"))) int xpbd_gb300_profile_counters(void* handle, long long* out4);
+
 /* No counterpart in the reference.  Vertex spatial hash that allocates no
  * device memory, for callers that cannot call cudaMalloc / cudaFree (a host
  * application whose pool owns all device memory, or a frame loop that cannot

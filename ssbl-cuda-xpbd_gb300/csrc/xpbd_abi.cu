@@ -433,6 +433,18 @@ XG_EXPORT int xpbd_gb300_profile_frame(void* handle, int substeps, int iteration
     return 1;
 }
 
+XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out4) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S || !out4) return fail("invalid profile counter request") ? 1 : 0;
+    unsigned long long c[kPerfSlots];
+    if (!cuda_ok(cudaMemcpyAsync(c, S->perf, sizeof(c), cudaMemcpyDeviceToHost, S->stream), "read work counters") ||
+        !cuda_ok(cudaStreamSynchronize(S->stream), "read work counters"))
+        return 0;
+    for (int k = 0; k < kPerfSlots; ++k) out4[k] = (long long)c[k];
+    return 1;
+}
+
 XG_EXPORT int xpbd_gb300_synchronize(void* handle) {
     g_error.clear();
     Solver* S = as_solver(handle);

@@ -291,6 +291,7 @@ void free_solver(Solver* S) {
     dfree(S->pin_weight);
     dfree(S->pin_relax);
     dfree(S->counts);
+    dfree(S->perf);
     dfree(S->max_delta_bits);
     dfree(S->pack);
     dfree(S->vcell);
@@ -323,6 +324,10 @@ void free_solver(Solver* S) {
     dfree(g.max_delta_bits);
     dfree(S->cap_edges);
     dfree(S->cap_rest);
+    dfree(S->stage_idx);
+    dfree(S->stage_target);
+    dfree(S->stage_weight);
+    dfree(S->stage_relax);
     for (int k = 0; k < 3; ++k) {
         if (S->aux[k]) cudaStreamDestroy(S->aux[k]);
         if (S->ev_join[k]) cudaEventDestroy(S->ev_join[k]);
@@ -497,27 +502,84 @@ bool upload_static(Solver* S, int cloth, const float* tris, int count) {
     return ok;
 }
 
+// Pin update: the new set replaces the cloth's (or, for cloth < 0, every
+// cloth's) pins; a vertex listed twice keeps its last entry.  Only the
+// vertices whose pin changes (old pins cleared, new pins set) travel to the
+// device, as a compact list scattered by a kernel.
 bool upload_pins(Solver* S, int cloth, const int* indices, const float* positions, const float* weights, int count) {
     if (!valid_cloth(S, cloth)) return fail("invalid solver handle");
     if (count < 0) return fail("invalid pin count");
     if (count > 0 && (!indices || !positions)) return fail("pin arrays are required when pin count is nonzero");
     const Range r = cloth_range(S, cloth);
-    std::fill(S->h_pin_weight.begin() + r.lo, S->h_pin_weight.begin() + r.hi, -1.0f);
+    std::vector<int>& mod = S->pin_changed;
+    mod.clear();
+    auto mark = [&](int i) {
+        if (S->pin_mark[i] != S->pin_epoch) {
+            S->pin_mark[i] = S->pin_epoch;
+            mod.push_back(i);
+        }
+    };
+    ++S->pin_epoch;
+    std::vector<int> keep;
+    keep.reserve(S->pin_set.size());
+    for (int i : S->pin_set) {
+        if (i >= r.lo && i < r.hi) {
+            S->h_pin_weight[i] = -1.0f;
+            mark(i);
+        } else {
+            keep.push_back(i);
+        }
+    }
     for (int k = 0; k < count; ++k) {
         const int i = r.lo + indices[k];
         if (indices[k] < 0 || i >= r.hi) continue;
         S->h_pin_weight[i] = weights ? weights[k] : 1.0f;
         S->h_pin_target[i] = make_float4(positions[k * 3 + 0], positions[k * 3 + 1], positions[k * 3 + 2], 0.0f);
+        mark(i);
+        if (S->pin_kept[i] != S->pin_epoch) {
+            S->pin_kept[i] = S->pin_epoch;
+            keep.push_back(i);
+        }
     }
+    S->pin_set.swap(keep);
     if (cloth >= 0)
         S->cl[cloth].pin_count = count;
     else if (S->K == 1)
         S->cl[0].pin_count = count;
-    S->pin_relax_iterations = -1;
-    const int n = r.hi - r.lo;
-    return dupload(S->pin_weight + r.lo, S->h_pin_weight.data() + r.lo, n, S->stream, "pin weight upload") &&
-           dupload(S->pin_target + r.lo, S->h_pin_target.data() + r.lo, n, S->stream, "pin target upload") &&
-           cuda_ok(cudaStreamSynchronize(S->stream), "pin upload");
+    const int n = (int)mod.size();
+    if (n == 0) return true;
+    const float exponent = 1.0f / (float)std::max(S->pin_relax_iterations + 1, 1);
+    S->h_stage_target.resize(n);
+    S->h_stage_weight.resize(n);
+    S->h_stage_relax.resize(n);
+    for (int k = 0; k < n; ++k) {
+        const int i = mod[k];
+        S->h_stage_target[k] = S->h_pin_target[i];
+        S->h_stage_weight[k] = S->h_pin_weight[i];
+        S->h_pin_relax[i] = S->pin_relax_iterations >= 0 ? pin_soft_relaxation(S->h_pin_weight[i], exponent) : 0.0f;
+        S->h_stage_relax[k] = S->h_pin_relax[i];
+    }
+    if (n > S->stage_capacity) {
+        if (!cuda_ok(cudaStreamSynchronize(S->stream), "pin staging reallocation")) return false;
+        dfree(S->stage_idx);
+        dfree(S->stage_target);
+        dfree(S->stage_weight);
+        dfree(S->stage_relax);
+        S->stage_capacity = 0;
+        const int cap = std::max(n, 256);
+        if (!dalloc(&S->stage_idx, cap, "pin staging allocation") || !dalloc(&S->stage_target, cap, "pin staging allocation") ||
+            !dalloc(&S->stage_weight, cap, "pin staging allocation") || !dalloc(&S->stage_relax, cap, "pin staging allocation"))
+            return false;
+        S->stage_capacity = cap;
+    }
+    if (!dupload(S->stage_idx, mod.data(), n, S->stream, "pin index upload") ||
+        !dupload(S->stage_target, S->h_stage_target.data(), n, S->stream, "pin target upload") ||
+        !dupload(S->stage_weight, S->h_stage_weight.data(), n, S->stream, "pin weight upload") ||
+        !dupload(S->stage_relax, S->h_stage_relax.data(), n, S->stream, "pin relaxation upload"))
+        return false;
+    launch_pin_scatter(S->stage_idx, S->stage_target, S->stage_weight, S->stage_relax, n, S->pin_target, S->pin_weight,
+                       S->pin_relax, S->nV, S->stream);
+    return cuda_ok(cudaGetLastError(), "pin upload");
 }
 
 bool set_colliders(Solver* S, int cloth, const SsblXpbdRuntimeColliders& c) {
@@ -754,6 +816,8 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
     S->h_pin_weight.assign(nV, -1.0f);
     S->h_pin_target.assign(nV, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     S->h_pin_relax.assign(nV, 0.0f);
+    S->pin_mark.assign(nV, 0);
+    S->pin_kept.assign(nV, 0);
 
     // Parameters and self-collision table sizes.
     int wings = 0;
@@ -826,7 +890,7 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
               dalloc(&S->edges, nE, "edge allocation") && dalloc(&S->edge_rest, nE, "edge rest allocation") &&
               dalloc(&S->pin_target, nV, "pin target allocation") && dalloc(&S->pin_weight, nV, "pin weight allocation") &&
               dalloc(&S->pin_relax, nV, "pin relaxation allocation") &&
-              dalloc(&S->counts, kCntSlots, "ABI41 diagnostic allocation") &&
+              dalloc(&S->counts, kCntSlots, "ABI41 diagnostic allocation") && dalloc(&S->perf, kPerfSlots, "work counter allocation") &&
               dalloc(&S->max_delta_bits, 1, "self max smoothed delta allocation") &&
               dalloc(&S->pack, (size_t)nV * 3, "download staging allocation");
     if (ok && K > 1)
@@ -1002,6 +1066,10 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
     const bool colored_bends = !S->bend_colors.empty();
     View base = S->view();
     base.substeps = substeps;
+    if (prof) {
+        base.perf = S->perf;
+        cudaMemsetAsync(S->perf, 0, sizeof(unsigned long long) * kPerfSlots, S->stream);
+    }
     int cur = 0;
     unsigned pending = 0;
     int pending_last = 0;  // last_it of the iteration that queued `pending`

@@ -176,6 +176,16 @@ struct Solver {
     std::vector<float4> h_pin_target;
     std::vector<float> h_pin_relax;
     int pin_relax_iterations = -1;
+    // pin updates: current pinned vertices, change marks, device staging
+    std::vector<int> pin_set, pin_changed, pin_mark, pin_kept;
+    int pin_epoch = 0;
+    std::vector<float4> h_stage_target;
+    std::vector<float> h_stage_weight, h_stage_relax;
+    int* stage_idx = nullptr;
+    float4* stage_target = nullptr;
+    float* stage_weight = nullptr;
+    float* stage_relax = nullptr;
+    int stage_capacity = 0;
     std::vector<int> bend_colors;   // merged colour offsets into `bends`
     bool jacobi_bends = false;      // some cloth gathers its bends
 
@@ -190,6 +200,7 @@ struct Solver {
     int* scan_tmp = nullptr;  // three segments: vertex, triangle, edge hash scans
     int scan_seg = 0;
     Acc4* acc = nullptr;
+    unsigned long long* perf = nullptr;  // kPerfSlots work counters of a profiled frame
 
     // hard-stretch optimisation (one-cloth solvers only)
     bool pcg_on = false;

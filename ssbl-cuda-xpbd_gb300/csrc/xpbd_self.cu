@@ -1138,13 +1138,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
     const int st = v.tb_start[b];
     const int lim = min(v.tb_start[b + 1] - st, kBucketSlots);
     const int budget = neighbor_budget(P);
-    int prior = 0;
+    int prior = 0, evaluated = 0;
     for (int base = 0; base < lim && prior < budget; base += kQueryLanes) {
         SoftPush sp;
         sp.apply = false;
         const int slot = base + gl;
+        evaluated += min(lim - base, kQueryLanes);
         const bool accepted = slot < lim && vt_eval(v, vertex, v.tb_ent[st + slot], target, onset, &sp);
         prior += commit_chunk(v, accepted, sp, prior, budget, kCntSoftContacts);
+    }
+    if (v.perf && gl == 0) {
+        atomicAdd(&v.perf[kPerfVtItems], 1ull);
+        atomicAdd(&v.perf[kPerfVtSlots], (unsigned long long)evaluated);
     }
 }
 
@@ -1165,13 +1170,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     const int st = v.eb_start[b];
     const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     const int budget = neighbor_budget(P);
-    int prior = 0;
+    int prior = 0, evaluated = 0;
     for (int base = 0; base < lim && prior < budget; base += kQueryLanes) {
         SoftPush sp;
         sp.apply = false;
         const int slot = base + gl;
+        evaluated += min(lim - base, kQueryLanes);
         const bool accepted = slot < lim && ee_eval(v, e, v.eb_ent[st + slot], target, onset, &sp);
         prior += commit_chunk(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
+    }
+    if (v.perf && gl == 0) {
+        atomicAdd(&v.perf[kPerfEeItems], 1ull);
+        atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)evaluated);
     }
 }
 
@@ -1286,12 +1296,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
         lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     }
     unsigned keys[2] = {0u, 0u};
-    int nkeys = 0, accepted = 0, last_id = -1;
+    int nkeys = 0, accepted = 0, last_id = -1, evaluated = 0;
     for (int c = 0; c < kBucketSlots / kQueryLanes; ++c) {
         if (!(run && c * kQueryLanes < lim && accepted < budget)) break;  // uniform within the group
         {
             const int slot = c * kQueryLanes + gl;
             const bool valid = slot < lim;
+            evaluated += valid ? 1 : 0;
             const int id = valid ? v.eb_ent[st + slot] : -1;
             const int before = __shfl_sync(gm, id, gbase + ((gl + kQueryLanes - 1) & (kQueryLanes - 1)));
             const bool dup = valid && id == (gl == 0 ? last_id : before);
@@ -1364,6 +1375,14 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
     for (int q = 0; q < 6; ++q) {
         const int total = __reduce_add_sync(0xffffffffu, sums[q]);
         if (lane == 0 && total > 0) count_add(v.counts, slots[q], (unsigned long long)total);
+    }
+    if (v.perf) {
+        const int items = __reduce_add_sync(0xffffffffu, (run && gl == 0) ? 1 : 0);
+        const int slots_total = __reduce_add_sync(0xffffffffu, evaluated);
+        if (lane == 0) {
+            atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
+            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)slots_total);
+        }
     }
     const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);
     if (lane == 0 && acc_total > 0) {

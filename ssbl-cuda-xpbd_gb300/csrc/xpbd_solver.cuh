@@ -186,7 +186,12 @@ struct View {
     int* nb_idx;            // [nV * 32]
     Acc4* acc;              // fixed-point delta xyz + contact weight
     unsigned* max_delta_bits;
+    // work counters of a profiled frame (null otherwise): query items and
+    // bucket slots evaluated by the EE and VT queries
+    unsigned long long* perf;
 };
+
+enum PerfSlot { kPerfEeItems = 0, kPerfEeSlots = 1, kPerfVtItems = 2, kPerfVtSlots = 3, kPerfSlots = 4 };
 
 __device__ __forceinline__ int cloth_of(const int* map, int i) { return map ? __ldg(&map[i]) : 0; }
 __device__ __forceinline__ const Params& params_v(const View& v, int i) { return v.P[cloth_of(v.vcloth, i)]; }
@@ -239,6 +244,8 @@ enum PassFlags : unsigned {
 void launch_vertex_pass(const View& v, int V, unsigned flags, cudaStream_t s);
 void launch_bend_color(const View& v, int start, int count, cudaStream_t s);
 void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s);
+void launch_pin_scatter(const int* idx, const float4* target, const float* weight, const float* relax, int n,
+                        float4* pin_target, float* pin_weight, float* pin_relax, int nV, cudaStream_t s);
 void launch_pack_positions(float* dst, const float4* src, int V, cudaStream_t s);
 void launch_sdf_build(const View& v, int cloth, int voxels, cudaStream_t s);
 

@@ -540,6 +540,18 @@ __global__ void k_pack_positions(float* dst, const float4* src, int n) {
     dst[i * 3 + 2] = p.z;
 }
 
+// Scatter of changed pin entries (vertices whose pin was set or cleared).
+__global__ void k_pin_scatter(const int* idx, const float4* target, const float* weight, const float* relax, int n,
+                              float4* pin_target, float* pin_weight, float* pin_relax, int nV) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = idx[k];
+    if (i < 0 || i >= nV) return;
+    pin_target[i] = target[k];
+    pin_weight[i] = weight[k];
+    pin_relax[i] = relax[k];
+}
+
 inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 // The per-vertex passes are latency bound (gathers of neighbours): 128-thread
@@ -559,6 +571,11 @@ void launch_vertex_pass(const View& v, int V, unsigned flags, cudaStream_t s) {
 
 void launch_bend_color(const View& v, int start, int count, cudaStream_t s) {
     if (count > 0) k_bend_color<<<blocks_for(count), kThreads, 0, s>>>(v, start, count);
+}
+
+void launch_pin_scatter(const int* idx, const float4* target, const float* weight, const float* relax, int n,
+                        float4* pin_target, float* pin_weight, float* pin_relax, int nV, cudaStream_t s) {
+    if (n > 0) k_pin_scatter<<<blocks_for(n), kThreads, 0, s>>>(idx, target, weight, relax, n, pin_target, pin_weight, pin_relax, nV);
 }
 
 void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s) {

@@ -222,6 +222,7 @@ def _load_library():
         "xpbd_gb300_stream": (vp, [vp]),
         "xpbd_gb300_profile_frame": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _PF,
                                                     ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+        "xpbd_gb300_profile_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
         "xpbd_gb300_batch_create": (vp, [ctypes.POINTER(NativeConfig), ctypes.POINTER(NativeMesh), ctypes.c_int]),
         "xpbd_gb300_batch_cloth_count": (ctypes.c_int, [vp]),
         "xpbd_gb300_batch_cloth_range": (ctypes.c_int, [vp, ctypes.c_int, _PI]),
@@ -482,6 +483,13 @@ class NativeXpbdSolver:
         self._check(self._lib.xpbd_gb300_profile_frame(self._handle, int(substeps), int(iterations), _fp(ms),
                                                         cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), n))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
+    def profile_counters(self) -> dict:
+        """Work counters of the last profile_frame (EE / VT query items and
+        bucket slots evaluated)."""
+        out = np.zeros(4, np.int64)
+        self._check(self._lib.xpbd_gb300_profile_counters(self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
+        return {"ee_items": int(out[0]), "ee_slots": int(out[1]), "vt_items": int(out[2]), "vt_slots": int(out[3])}
 
 
 class NativeXpbdBatch(NativeXpbdSolver):

@@ -122,7 +122,38 @@ def edge_constraints(triangles: np.ndarray, rest: np.ndarray) -> tuple[np.ndarra
     return pairs, np.maximum(np.linalg.norm(delta, axis=1), _EPS)
 
 
-def bend_constraints(triangles: np.ndarray, rest: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+def _native_prep():
+    """The library's host-side preprocessing entry points, when it is built
+    (same results as the Python loops below, which remain the restatement)."""
+    global _PREP
+    if _PREP is None:
+        try:
+            import ctypes
+            import os
+
+            from .build import library_path
+
+            path = os.environ.get("SSBL_NATIVE_DLL_PATH") or library_path()
+            lib = ctypes.CDLL(path) if os.path.exists(path) else None
+            if lib is not None and hasattr(lib, "xpbd_gb300_greedy_color"):
+                pi = ctypes.POINTER(ctypes.c_int)
+                lib.xpbd_gb300_greedy_color.argtypes = [pi, ctypes.c_int, ctypes.c_int, pi]
+                lib.xpbd_gb300_greedy_color.restype = ctypes.c_int
+                lib.xpbd_gb300_bend_pairs.argtypes = [pi, ctypes.c_int, pi, ctypes.c_int]
+                lib.xpbd_gb300_bend_pairs.restype = ctypes.c_int
+                _PREP = lib
+            else:
+                _PREP = False
+        except Exception:
+            _PREP = False
+    return _PREP or None
+
+
+_PREP = None
+
+
+def bend_pairs_py(triangles: np.ndarray) -> np.ndarray:
+    """Bend pairs by the Python walk of xpbd_core.py:730-747."""
     first_opposite: dict[tuple[int, int], int] = {}
     pairs: set[tuple[int, int]] = set()
     for tri in np.asarray(triangles, dtype=np.int64):
@@ -134,7 +165,26 @@ def bend_constraints(triangles: np.ndarray, rest: np.ndarray) -> tuple[np.ndarra
                 first_opposite[key] = opp
             elif prev != opp:
                 pairs.add((prev, opp) if prev < opp else (opp, prev))
-    arr = np.asarray(sorted(pairs), dtype=np.int32).reshape(-1, 2)
+    return np.asarray(sorted(pairs), dtype=np.int32).reshape(-1, 2)
+
+
+def bend_pairs(triangles: np.ndarray) -> np.ndarray:
+    lib = _native_prep()
+    tris = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+    if lib is None or len(tris) == 0:
+        return bend_pairs_py(tris)
+    import ctypes
+
+    out = np.empty((3 * len(tris), 2), np.int32)
+    pi = ctypes.POINTER(ctypes.c_int)
+    n = lib.xpbd_gb300_bend_pairs(tris.ctypes.data_as(pi), len(tris), out.ctypes.data_as(pi), len(out))
+    if n < 0:
+        return bend_pairs_py(tris)
+    return np.ascontiguousarray(out[:n])
+
+
+def bend_constraints(triangles: np.ndarray, rest: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    arr = bend_pairs(triangles)
     if len(arr) == 0:
         return arr, np.empty(0, np.float32)
     delta = rest[arr[:, 1]] - rest[arr[:, 0]]
@@ -146,6 +196,29 @@ def color_constraints(pairs: np.ndarray, rest: np.ndarray, vertex_count: int):
     colour; returns (pairs, rest, offsets)."""
     if len(pairs) == 0:
         return pairs.reshape(0, 2), np.asarray(rest, np.float32), np.asarray([0], np.int32)
+    colors = greedy_colors(pairs, vertex_count)
+    order = np.argsort(colors, kind="stable")
+    counts = np.bincount(colors[order], minlength=int(colors.max()) + 1).astype(np.int32)
+    offsets = np.concatenate(([0], np.cumsum(counts))).astype(np.int32)
+    return (np.ascontiguousarray(pairs[order], np.int32), np.ascontiguousarray(np.asarray(rest)[order], np.float32), offsets)
+
+
+def greedy_colors(pairs: np.ndarray, vertex_count: int) -> np.ndarray:
+    """Greedy first-fit colour of each pair in order (native when built)."""
+    lib = _native_prep()
+    p = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    if lib is not None:
+        import ctypes
+
+        pi = ctypes.POINTER(ctypes.c_int)
+        out = np.empty(len(p), np.int32)
+        if lib.xpbd_gb300_greedy_color(p.ctypes.data_as(pi), len(p), int(vertex_count), out.ctypes.data_as(pi)) >= 0:
+            return out
+    return greedy_colors_py(p, vertex_count)
+
+
+def greedy_colors_py(pairs: np.ndarray, vertex_count: int) -> np.ndarray:
+    """Greedy first-fit colouring by the Python loop of xpbd_core.py:828-859."""
     used = [0] * vertex_count  # bitmask of colours per vertex
     colors = np.empty(len(pairs), dtype=np.int32)
     for k, (a, b) in enumerate(np.asarray(pairs, dtype=np.int64)):
@@ -163,10 +236,7 @@ def color_constraints(pairs: np.ndarray, rest: np.ndarray, vertex_count: int):
             used[a] |= bit
         if 0 <= b < vertex_count:
             used[b] |= bit
-    order = np.argsort(colors, kind="stable")
-    counts = np.bincount(colors[order], minlength=int(colors.max()) + 1).astype(np.int32)
-    offsets = np.concatenate(([0], np.cumsum(counts))).astype(np.int32)
-    return (np.ascontiguousarray(pairs[order], np.int32), np.ascontiguousarray(np.asarray(rest)[order], np.float32), offsets)
+    return colors
 
 
 def vertex_inverse_mass(rest: np.ndarray, triangles: np.ndarray, density: float, pin_mask: np.ndarray) -> np.ndarray:
