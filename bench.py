@@ -63,6 +63,9 @@ DESCRIPTIONS = {
     "drop10k": "10k cloth (100x100 grid, 19,602 tris) dropped on a sphere + 64^3 box/torus SDF, strict self "
                "collision 2 mm, friction 0.3, 10 substeps x 2 iterations per frame",
     "plain32": "plain 32x32 grid (1,024 verts), two pinned corners, ground, 10 substeps x 2 iterations",
+    "serve": "serving: Poisson arrivals 200/s of cloth solves, V log-uniform 1k-250k (16 grid sizes), horizons "
+             "30-240 frames, random sphere and/or box/torus SDF, strict self collision 2 mm, admitted by a "
+             "device-memory budget, resident until done, one frame per resident request per tick",
 }
 
 
@@ -73,6 +76,8 @@ def workload(name: str) -> list:
         return [scene.drop_scene(100, 200, seed=0, self_mode=2)]
     if name == "plain32":
         return [scene.plain_grid_scene(32, 120)]
+    if name == "serve":
+        return []
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -270,6 +275,54 @@ def time_plain(native, scs, frames: int) -> dict:
             "handles": len(scs), "launches_per_step": launches}
 
 
+def run_serving(args, world, rank, local):
+    """Serving form: the request loop for --serve-seconds of Poisson
+    arrivals; a "step" is one tick (every resident request advances one
+    frame).  Each rank serves its own arrival stream (replicas)."""
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop; its CPU "
+                              "restatement is timed by the batch256 / drop10k workloads"}), flush=True)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    from xpbd_gb300 import build
+    from xpbd_gb300.serving import ServingEngine
+
+    build.build()
+    reqs = scene.serving_requests(rate=200.0, duration=args.serve_seconds, seed=rank)
+    # warm-up: a few small requests through a separate engine (module load, first graph capture)
+    warm = ServingEngine(hbm_budget_bytes=int(8e9))
+    warm.run(scene.serving_requests(rate=50.0, duration=0.1, seed=99, v_range=(1000, 4000), horizon=(3, 5),
+                                    max_requests=args.warmup), duration=None, drain=True)
+    warm.close()
+    torch.cuda.synchronize()
+    eng = ServingEngine(hbm_budget_bytes=int(args.serve_budget_gb * 1e9))
+    with ClockSampler(local) as clocks:
+        st = eng.run(reqs, duration=args.serve_seconds)
+        eng.close()  # waits for solvers still being built (their graph captures) before any device-wide sync
+        torch.cuda.synchronize()
+    results = st.pop("results")
+    d2h = sum(r.positions.nbytes for r in results)
+    value = st["throughput"] * world
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": st["ticks"], "warmup": args.warmup,
+        "ms_per_step": 1000.0 * st["elapsed_s"] / max(st["ticks"], 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request stream)",
+        "config": {"workload": DESCRIPTIONS["serve"], "seconds": args.serve_seconds, "offered_requests": len(reqs),
+                   "budget_gb": args.serve_budget_gb, "parallelism": f"replicas x{world}"},
+        "serving": {k: v for k, v in st.items()},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": d2h / max(st["ticks"], 1),
+                "note": "the loop is end to end: requests enter from host arrays and results return to host memory"},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -279,9 +332,14 @@ def main():
     ap.add_argument("--workload", default="batch256", choices=sorted(DESCRIPTIONS))
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--plain-frames", type=int, default=3)
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
+    if args.workload == "serve":
+        run_serving(args, world, rank, local)
+        return
     scs = workload(args.workload)
     if args.impl == "reference":
         run_reference(args, scs, world, rank)

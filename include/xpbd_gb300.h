@@ -122,6 +122,16 @@ __attribute__((visibility("default"))) int xpbd_gb300_batch_reset_cloth(void* ha
  * until it is activated again. */
 __attribute__((visibility("default"))) int xpbd_gb300_batch_set_active(void* handle, int cloth, int active);
 
+/* Capture and instantiate the frame graph for (substeps, iterations) and the
+ * current collider kinds without running a frame, so the first step does
+ * not pay for the capture (the serving loop prepares new solvers off the
+ * stepping thread). */
+__attribute__((visibility("default"))) int xpbd_gb300_prepare_graph(void* handle, int substeps, int iterations);
+
+/* Device memory held by the solver (bytes of all its allocations), for
+ * admission by a device-memory budget. */
+__attribute__((visibility("default"))) long long xpbd_gb300_device_bytes(void* handle);
+
 /* Wait for the solver's stream. */
 __attribute__((visibility("default"))) int xpbd_gb300_synchronize(void* handle);
 

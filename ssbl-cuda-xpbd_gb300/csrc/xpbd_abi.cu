@@ -355,16 +355,17 @@ XG_EXPORT long long xpbd_gb300_read_buffer(void* handle, int id, void* out, long
         case XPBD_BUF_NEIGHBOR_COUNTS: src = S->nb_count; bytes = 4ll * S->nV; break;
         case XPBD_BUF_NEIGHBOR_INDICES: src = S->nb_idx; bytes = 4ll * S->nV * kNeighborSlots; break;
         case XPBD_BUF_STATIC_SDF:
-            src = S->cl[0].sdf;
+            src = S->cl[0].grid ? S->cl[0].grid->sdf : nullptr;
             bytes = P0.sdf_ready ? 4ll * P0.sdf_dim[0] * P0.sdf_dim[1] * P0.sdf_dim[2] : 0;
             break;
         case XPBD_BUF_COUNTERS: src = S->counts; bytes = 8ll * kCntSlots; break;
         default: fail("unknown buffer id"); return -1;
     }
-    if (!src) {
+    if (!src && bytes > 0) {
         fail("buffer is not allocated for this solver");
         return -1;
     }
+    if (!src) return 0;
     if (bytes > max_bytes) {
         fail("output buffer too small");
         return -1;
@@ -443,6 +444,18 @@ XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out4) {
         return 0;
     for (int k = 0; k < kPerfSlots; ++k) out4[k] = (long long)c[k];
     return 1;
+}
+
+XG_EXPORT int xpbd_gb300_prepare_graph(void* handle, int substeps, int iterations) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S) return fail("invalid solver handle") ? 1 : 0;
+    return ok_or_zero(prepare_graph(S, std::max(substeps, 1), std::max(iterations, 1)));
+}
+
+XG_EXPORT long long xpbd_gb300_device_bytes(void* handle) {
+    Solver* S = as_solver(handle);
+    return S ? S->device_bytes : -1;
 }
 
 XG_EXPORT int xpbd_gb300_synchronize(void* handle) {

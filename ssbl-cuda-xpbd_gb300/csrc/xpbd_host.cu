@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <unordered_map>
 
 #include "xpbd_host.cuh"
@@ -19,6 +20,7 @@ namespace xg {
 namespace host {
 
 thread_local std::string g_error;
+thread_local long long* g_alloc_account = nullptr;
 
 namespace {
 
@@ -196,6 +198,23 @@ void dfree(T*& p) {
     p = nullptr;
 }
 
+std::mutex g_sdf_mutex;
+std::vector<SdfGrid*> g_sdf_cache;
+
+// Drop a cloth's reference to its SDF grid; the last reference frees it.
+void release_grid(Solver* S, Cloth& c) {
+    if (!c.grid) return;
+    std::lock_guard<std::mutex> lock(g_sdf_mutex);
+    SdfGrid* g = c.grid;
+    c.grid = nullptr;
+    S->device_bytes -= g->bytes;
+    if (--g->refs > 0) return;
+    g_sdf_cache.erase(std::remove(g_sdf_cache.begin(), g_sdf_cache.end(), g), g_sdf_cache.end());
+    dfree(g->sdf);
+    dfree(g->tris_dev);
+    delete g;
+}
+
 }  // namespace
 
 View Solver::view() const {
@@ -262,10 +281,7 @@ void free_solver(Solver* S) {
     if (!S) return;
     if (S->stream) cudaStreamSynchronize(S->stream);
     S->drop_graphs();
-    for (Cloth& c : S->cl) {
-        dfree(c.sdf);
-        dfree(c.static_tris);
-    }
+    for (Cloth& c : S->cl) release_grid(S, c);
     dfree(S->dp);
     dfree(S->vcloth);
     dfree(S->ecloth);
@@ -405,36 +421,86 @@ bool build_static_sdf(Solver* S, int k, const float* tris, int count) {
     const long long voxels_ll = (long long)dim[0] * dim[1] * dim[2];
     if (voxels_ll <= 0 || voxels_ll > 0x7fffffffll) return fail("static SDF grid is too large");
     const int voxels = (int)voxels_ll;
-    if (voxels > C.sdf_capacity) {
-        if (!cuda_ok(cudaStreamSynchronize(S->stream), "static SDF reallocation")) return false;
-        dfree(C.sdf);
-        C.sdf_capacity = 0;
-        if (!dalloc(&C.sdf, voxels, "static SDF allocation")) return false;
-        C.sdf_capacity = voxels;
+    int device = 0;
+    cudaGetDevice(&device);
+    std::unique_lock<std::mutex> lock(g_sdf_mutex);
+    SdfGrid* grid = nullptr;
+    for (SdfGrid* g : g_sdf_cache)
+        if (g->device == device && g->voxel_setting == c.static_sdf_voxel_size && g->band == band &&
+            g->max_res == max_res && g->margin == margin && g->tris.size() == (size_t)count * 9 &&
+            std::memcmp(g->tris.data(), tris, sizeof(float) * 9 * (size_t)count) == 0) {
+            grid = g;
+            break;
+        }
+    if (grid) {
+        grid->refs += 1;
+    } else {
+        grid = new SdfGrid();
+        grid->device = device;
+        grid->tris.assign(tris, tris + (size_t)count * 9);
+        grid->voxel_setting = c.static_sdf_voxel_size;
+        grid->band = band;
+        grid->max_res = max_res;
+        grid->margin = margin;
+        long long bytes = 0;
+        {
+            AllocAccount account(&bytes);
+            if (!dalloc(&grid->sdf, voxels, "static SDF allocation") ||
+                !dalloc(&grid->tris_dev, (size_t)count * 3, "static triangle upload")) {
+                dfree(grid->sdf);
+                delete grid;
+                return false;
+            }
+        }
+        grid->bytes = bytes;
+        std::vector<float4> t4((size_t)count * 3);
+        for (int q = 0; q < count * 3; ++q) t4[q] = make_float4(tris[q * 3], tris[q * 3 + 1], tris[q * 3 + 2], 0.0f);
+        for (int a = 0; a < 3; ++a) {
+            grid->dim[a] = dim[a];
+            grid->origin[a] = lo[a];
+        }
+        grid->voxel = voxel;
+        grid->is_signed = mesh_is_closed(tris, count) ? 1 : 0;
+        // build it with this cloth's parameters pointing at the new grid
+        for (int a = 0; a < 3; ++a) {
+            P.sdf_dim[a] = dim[a];
+            P.sdf_origin[a] = lo[a];
+        }
+        P.sdf_voxel = voxel;
+        P.sdf = grid->sdf;
+        P.static_tris = grid->tris_dev;
+        P.sdf_signed = grid->is_signed;
+        S->params_dirty = true;
+        if (!dupload(grid->tris_dev, t4.data(), t4.size(), S->stream, "static triangle upload") || !sync_params(S)) {
+            dfree(grid->sdf);
+            dfree(grid->tris_dev);
+            delete grid;
+            return false;
+        }
+        launch_sdf_build(S->view(), k, voxels, S->stream);
+        if (!cuda_ok(cudaGetLastError(), "build static SDF") ||
+            !cuda_ok(cudaStreamSynchronize(S->stream), "sync static SDF build")) {
+            dfree(grid->sdf);
+            dfree(grid->tris_dev);
+            delete grid;
+            return false;
+        }
+        grid->refs = 1;
+        g_sdf_cache.push_back(grid);
     }
-    if (count > C.static_capacity) {
-        if (!cuda_ok(cudaStreamSynchronize(S->stream), "static triangle reallocation")) return false;
-        dfree(C.static_tris);
-        C.static_capacity = 0;
-        if (!dalloc(&C.static_tris, (size_t)count * 3, "static triangle upload")) return false;
-        C.static_capacity = count;
-    }
-    std::vector<float4> t4((size_t)count * 3);
-    for (int q = 0; q < count * 3; ++q) t4[q] = make_float4(tris[q * 3], tris[q * 3 + 1], tris[q * 3 + 2], 0.0f);
-    if (!dupload(C.static_tris, t4.data(), t4.size(), S->stream, "static triangle upload")) return false;
+    lock.unlock();
+    release_grid(S, C);
+    C.grid = grid;
+    S->device_bytes += grid->bytes;
     for (int a = 0; a < 3; ++a) {
-        P.sdf_dim[a] = dim[a];
-        P.sdf_origin[a] = lo[a];
+        P.sdf_dim[a] = grid->dim[a];
+        P.sdf_origin[a] = grid->origin[a];
     }
-    P.sdf_voxel = voxel;
-    P.sdf = C.sdf;
-    P.static_tris = C.static_tris;
-    P.sdf_signed = mesh_is_closed(tris, count) ? 1 : 0;
+    P.sdf_voxel = grid->voxel;
+    P.sdf = grid->sdf;
+    P.static_tris = grid->tris_dev;
+    P.sdf_signed = grid->is_signed;
     if (!P.sdf_signed) C.sdf_unsigned += 1;
-    if (!sync_params(S)) return false;
-    launch_sdf_build(S->view(), k, voxels, S->stream);
-    if (!cuda_ok(cudaGetLastError(), "build static SDF") || !cuda_ok(cudaStreamSynchronize(S->stream), "sync static SDF build"))
-        return false;
     P.sdf_ready = 1;
     S->params_dirty = true;
     C.sdf_rebuilds += 1;
@@ -559,8 +625,10 @@ bool upload_pins(Solver* S, int cloth, const int* indices, const float* position
         S->h_pin_relax[i] = S->pin_relax_iterations >= 0 ? pin_soft_relaxation(S->h_pin_weight[i], exponent) : 0.0f;
         S->h_stage_relax[k] = S->h_pin_relax[i];
     }
+    AllocAccount account(&S->device_bytes);
     if (n > S->stage_capacity) {
         if (!cuda_ok(cudaStreamSynchronize(S->stream), "pin staging reallocation")) return false;
+        S->device_bytes -= (long long)(sizeof(int) + sizeof(float4) + 2 * sizeof(float)) * S->stage_capacity;
         dfree(S->stage_idx);
         dfree(S->stage_target);
         dfree(S->stage_weight);
@@ -651,6 +719,7 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
         return nullptr;
     }
     Solver* S = new Solver();
+    AllocAccount account(&S->device_bytes);
     S->K = K;
     S->cl.resize(K);
     S->hp.assign(K, Params{});
@@ -1266,11 +1335,11 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
     if (cur != 0) timed(kKCopy, 1, [&] { launch_copy_pos(S->pos[0], S->pos[1], nV, S->stream); });
 }
 
-bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st) {
-    if (!S->use_graphs) {
-        enqueue_frame(S, substeps, iterations, st);
-        return cuda_ok(cudaGetLastError(), "launch GB300 XPBD frame");
-    }
+namespace {
+
+// The frame graph for (substeps, iterations) and the current collider kinds,
+// captured and instantiated on first use.
+GraphEntry* ensure_graph(Solver* S, int substeps, int iterations) {
     int analytic = 0, sdf = 0;
     for (const Params& P : S->hp) {
         analytic |= (P.use_ground || P.use_wall || P.use_sphere) ? 1 : 0;
@@ -1282,24 +1351,41 @@ bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st) {
         GraphEntry g;
         FrameStats cst;
         if (!cuda_ok(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal), "begin frame capture"))
-            return false;
+            return nullptr;
         enqueue_frame(S, substeps, iterations, &cst);
         cudaGraph_t graph = nullptr;
-        if (!cuda_ok(cudaStreamEndCapture(S->stream, &graph), "end frame capture")) return false;
+        if (!cuda_ok(cudaStreamEndCapture(S->stream, &graph), "end frame capture")) return nullptr;
         const cudaError_t err = cudaGraphInstantiate(&g.exec, graph, 0);
         cudaGraphDestroy(graph);
-        if (!cuda_ok(err, "instantiate frame graph")) return false;
+        if (!cuda_ok(err, "instantiate frame graph")) return nullptr;
         g.launches = cst.launches;
         g.cache_hits = cst.cache_hits;
         g.cache_misses = cst.cache_misses;
         g.pcg_solves = cst.pcg_solves;
         it = S->graphs.emplace(key, g).first;
     }
-    st->launches += it->second.launches;
-    st->cache_hits += it->second.cache_hits;
-    st->cache_misses += it->second.cache_misses;
-    st->pcg_solves += it->second.pcg_solves;
-    return cuda_ok(cudaGraphLaunch(it->second.exec, S->stream), "launch frame graph");
+    return &it->second;
+}
+
+}  // namespace
+
+bool prepare_graph(Solver* S, int substeps, int iterations) {
+    if (!S->use_graphs) return true;
+    return ensure_graph(S, substeps, iterations) != nullptr;
+}
+
+bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st) {
+    if (!S->use_graphs) {
+        enqueue_frame(S, substeps, iterations, st);
+        return cuda_ok(cudaGetLastError(), "launch GB300 XPBD frame");
+    }
+    GraphEntry* g = ensure_graph(S, substeps, iterations);
+    if (!g) return false;
+    st->launches += g->launches;
+    st->cache_hits += g->cache_hits;
+    st->cache_misses += g->cache_misses;
+    st->pcg_solves += g->pcg_solves;
+    return cuda_ok(cudaGraphLaunch(g->exec, S->stream), "launch frame graph");
 }
 
 bool fetch_counts(Solver* S, const FrameStats& st) {

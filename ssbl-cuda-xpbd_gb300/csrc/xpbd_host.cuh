@@ -23,6 +23,15 @@ namespace xg {
 namespace host {
 
 extern thread_local std::string g_error;
+// Device bytes of the solver being built or updated on this thread: every
+// successful dalloc adds to it while an AllocAccount is in scope.
+extern thread_local long long* g_alloc_account;
+
+struct AllocAccount {
+    long long* prev;
+    explicit AllocAccount(long long* target) : prev(g_alloc_account) { g_alloc_account = target; }
+    ~AllocAccount() { g_alloc_account = prev; }
+};
 
 inline bool fail(const std::string& msg) {
     g_error = msg.empty() ? std::string("unknown GB300 XPBD error") : msg;
@@ -39,7 +48,9 @@ template <class T>
 bool dalloc(T** p, size_t n, const char* what) {
     *p = nullptr;
     if (n == 0) return true;
-    return cuda_ok(cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * n), what);
+    if (!cuda_ok(cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * n), what)) return false;
+    if (g_alloc_account) *g_alloc_account += (long long)(sizeof(T) * n);
+    return true;
 }
 
 template <class T>
@@ -105,6 +116,25 @@ struct Profile {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
 };
 
+// A static SDF grid on the device, shared by every cloth whose collider
+// triangles and SDF settings are identical (serving many requests against
+// the same collider builds its grid once).  Reference counted.
+struct SdfGrid {
+    int device = 0;
+    std::vector<float> tris;      // the collider triangles it was built from
+    float voxel_setting = 0.0f;   // config values that size the grid
+    int band = 0, max_res = 0;
+    float margin = 0.0f;
+    float* sdf = nullptr;
+    float4* tris_dev = nullptr;
+    int dim[3] = {0, 0, 0};
+    float origin[3] = {0.0f, 0.0f, 0.0f};
+    float voxel = 0.0f;
+    int is_signed = 0;
+    long long bytes = 0;
+    int refs = 0;
+};
+
 // Host-side state of one cloth of a solver.
 struct Cloth {
     SsblXpbdConfig cfg{};               // sanitised copy of the caller's config
@@ -115,11 +145,8 @@ struct Cloth {
     int interval = 1, passes = 1;       // self-collision schedule
     bool fast = false;
     bool order_buckets = true;          // queries depend on bucket member order
-    // static SDF of this cloth's collider
-    float* sdf = nullptr;
-    int sdf_capacity = 0;
-    float4* static_tris = nullptr;
-    int static_capacity = 0;
+    // static SDF of this cloth's collider (shared grid, null when none)
+    SdfGrid* grid = nullptr;
     long long sdf_rebuilds = 0, sdf_unsigned = 0;
     float sdf_build_ms = 0.0f;
     int pin_count = 0;
@@ -211,6 +238,7 @@ struct Solver {
     int pcg_nnz = 0;
     long long pcg_iterations = 0;
 
+    long long device_bytes = 0;  // sum of the solver's device allocations
     std::map<GraphKey, GraphEntry> graphs;
     bool use_graphs = true;
     long long last_launches = 0;
@@ -239,6 +267,7 @@ void sdf_diagnostics(Solver* S);
 // One frame: prepare parameters, launch (graph or direct), optionally fetch.
 bool prepare_step(Solver* S, int substeps, int iterations);
 bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st);
+bool prepare_graph(Solver* S, int substeps, int iterations);  // capture without launching
 void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof = nullptr);
 bool fetch_counts(Solver* S, const FrameStats& st);
 bool sync_params(Solver* S);

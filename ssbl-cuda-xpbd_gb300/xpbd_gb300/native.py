@@ -223,6 +223,8 @@ def _load_library():
         "xpbd_gb300_profile_frame": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _PF,
                                                     ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "xpbd_gb300_profile_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
+        "xpbd_gb300_device_bytes": (ctypes.c_longlong, [vp]),
+        "xpbd_gb300_prepare_graph": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "xpbd_gb300_batch_create": (vp, [ctypes.POINTER(NativeConfig), ctypes.POINTER(NativeMesh), ctypes.c_int]),
         "xpbd_gb300_batch_cloth_count": (ctypes.c_int, [vp]),
         "xpbd_gb300_batch_cloth_range": (ctypes.c_int, [vp, ctypes.c_int, _PI]),
@@ -468,6 +470,14 @@ class NativeXpbdSolver:
 
     def synchronize(self) -> None:
         self._check(self._lib.xpbd_gb300_synchronize(self._handle))
+
+    def prepare_graph(self, substeps: int, iterations: int) -> None:
+        """Capture the frame graph now (no frame is run)."""
+        self._check(self._lib.xpbd_gb300_prepare_graph(self._handle, int(substeps), int(iterations)))
+
+    def device_bytes(self) -> int:
+        """Device memory held by this solver."""
+        return int(self._lib.xpbd_gb300_device_bytes(self._handle))
 
     def stream(self) -> int:
         return int(self._lib.xpbd_gb300_stream(self._handle) or 0)

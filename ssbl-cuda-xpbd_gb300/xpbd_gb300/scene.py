@@ -444,15 +444,15 @@ def hardness_grid_scene(n: int = 32, hardness: float = 0.4, frames: int = 60) ->
     return Scene(f"hardness-{hardness}-grid-{n}", cloth, opt, base.static_triangles, 10, 2, frames, 1.0)
 
 
-_GRID_CACHE: dict[tuple[int, float], ClothData] = {}
+_GRID_CACHE: dict[tuple, ClothData] = {}
 
 
-def _unpinned_grid(n: int, z: float) -> ClothData:
+def _unpinned_grid(n: int, z: float, side: float = 1.0) -> ClothData:
     """Constraint inputs of an unpinned n x n grid (cached: every cloth of a
     batch with the same side shares its topology and rest state)."""
-    key = (n, z)
+    key = (n, z, side)
     if key not in _GRID_CACHE:
-        pos, tris = grid_mesh(n, 1.0, z)
+        pos, tris = grid_mesh(n, side, z)
         _GRID_CACHE[key] = build_cloth(pos, tris, 0.2, np.zeros(n * n, np.float32))
     return _GRID_CACHE[key]
 
@@ -492,4 +492,44 @@ def batched_scenes(count: int = 256, seed: int = 0, frames: int = 120, side_rang
                             fast_self_collision_passes=4, contact_friction=0.3)
         out.append(Scene(f"batch-{k}-grid-{n}", cloth, opt, np.empty((0, 3, 3), np.float32), 10, 2, frames, 1.0,
                          {"side": n, "fast": fast}))
+    return out
+
+
+def serving_requests(rate: float = 200.0, duration: float = 60.0, seed: int = 0, v_range: tuple = (1000, 250000),
+                     horizon: tuple = (30, 240), classes: int = 16, max_requests: int | None = None) -> list:
+    """Cloth solve requests for the serving form: Poisson arrivals at `rate`
+    per second over `duration` seconds, vertex counts log-uniform in
+    `v_range` (snapped to `classes` geometric grid sizes so cloths of one
+    size share their topology), horizons uniform in `horizon` frames, a
+    random sphere (r in [0.1, 0.5] m) and / or a static SDF collider (box,
+    torus or both); strict self collision with 2 mm thickness as in the 10k
+    drop scene; 10 substeps x 2 iterations.  Cloths keep a 1 cm vertex
+    spacing, so a larger request is a larger cloth (0.3 m to 5 m), not a
+    finer one."""
+    from .serving import ClothRequest
+
+    rng = np.random.default_rng(seed)
+    lo, hi = math.sqrt(v_range[0]), math.sqrt(v_range[1])
+    sides = sorted({int(round(lo * (hi / lo) ** (k / max(classes - 1, 1)))) for k in range(classes)})
+    sdfs = [box_triangles((0.55, 0.0, -0.55), (0.25, 0.25, 0.25)), torus_triangles((-0.45, 0.1, -0.35), 0.22, 0.07, 32, 16)]
+    sdfs.append(np.concatenate(sdfs).astype(np.float32))
+    out, t = [], 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > duration or (max_requests is not None and len(out) >= max_requests):
+            break
+        v = math.exp(rng.uniform(math.log(v_range[0]), math.log(v_range[1])))
+        n = min(sides, key=lambda s: abs(math.log(s * s) - math.log(v)))
+        cloth = _unpinned_grid(n, 0.5, (n - 1) * 0.01)
+        kind = int(rng.integers(0, 3))  # 0 sphere, 1 SDF, 2 both
+        use_sphere = kind in (0, 2)
+        static = sdfs[int(rng.integers(0, 3))] if kind in (1, 2) else np.empty((0, 3, 3), np.float32)
+        opt = SolverOptions(dt=1.0 / 60.0, damping=0.99, stretch_compliance=1.0e-7, bend_compliance=1.0e-4,
+                            collision_margin=0.002, cloth_thickness=0.002, use_sphere=use_sphere,
+                            sphere_center=(0.0, 0.0, 0.0), sphere_radius=float(rng.uniform(0.1, 0.5)), use_ground=True,
+                            ground_height=-1.0, self_collision=True, self_collision_mode=2, self_collision_interval=1,
+                            max_self_collision_neighbors=64, fast_self_collision_passes=4, contact_friction=0.3,
+                            static_sdf_max_resolution=64)
+        frames = int(rng.integers(horizon[0], horizon[1] + 1))
+        out.append(ClothRequest(cloth, opt, static, frames, 10, 2, len(out), t))
     return out
