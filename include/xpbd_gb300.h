@@ -132,6 +132,36 @@ __attribute__((visibility("default"))) int xpbd_gb300_prepare_graph(void* handle
  * admission by a device-memory budget. */
 __attribute__((visibility("default"))) long long xpbd_gb300_device_bytes(void* handle);
 
+/* ---- Differentiable form (no counterpart in the reference) ---------------
+ * A contact-free cloth (stretch and bend constraints, hard pins; no
+ * colliders, self collision, tethers or hard-stretch path) rolled out from
+ * its rest state with one compliance per edge and per bend, and the adjoint
+ * of that rollout.  Array arguments of rollout / backward are DEVICE
+ * pointers (float32): compliances of E and B values, positions and their
+ * gradient of 3V values.  The rollout keeps every frame's starting state;
+ * backward re-runs one frame at a time from those checkpoints. */
+__attribute__((visibility("default"))) void* xpbd_gb300_diff_create(const SsblXpbdConfig* config, const SsblXpbdMesh* mesh);
+__attribute__((visibility("default"))) int xpbd_gb300_diff_destroy(void* handle);
+/* Hard pins only (weight >= 0.75); softer pins are refused. */
+__attribute__((visibility("default"))) int xpbd_gb300_diff_update_pin_targets(void* handle, const int* indices,
+                                                                               const float* positions, const float* weights,
+                                                                               int count);
+__attribute__((visibility("default"))) int xpbd_gb300_diff_rollout(void* handle, const float* stretch_compliance,
+                                                                    const float* bend_compliance, int frames, int substeps,
+                                                                    int iterations, float* final_positions);
+/* dL/d(compliance) of the last rollout for dL/d(final positions). */
+__attribute__((visibility("default"))) int xpbd_gb300_diff_backward(void* handle, const float* grad_positions,
+                                                                     float* grad_stretch, float* grad_bend);
+__attribute__((visibility("default"))) void* xpbd_gb300_diff_stream(void* handle);
+
+/* Host-side input preprocessing of the cloth builders (no device work):
+ * greedy first-fit colouring of constraint pairs in order (writes a colour
+ * per pair, returns the colour count or -1) and the bend pairs of a triangle
+ * mesh in increasing order (returns their count or -1). */
+__attribute__((visibility("default"))) int xpbd_gb300_greedy_color(const int* pairs, int count, int vertex_count, int* colors);
+__attribute__((visibility("default"))) int xpbd_gb300_bend_pairs(const int* triangles, int triangle_count, int* pairs,
+                                                                  int max_pairs);
+
 /* Wait for the solver's stream. */
 __attribute__((visibility("default"))) int xpbd_gb300_synchronize(void* handle);
 

@@ -12,6 +12,7 @@
 // the incident constraints in constraint order: the same snapshot-Jacobi
 // update as the reference's atomics, without float atomics, and therefore
 // deterministic.
+#include "xpbd_constraint.cuh"
 #include "xpbd_solver.cuh"
 
 namespace xg {
@@ -227,29 +228,9 @@ __device__ void sdf_stage(const View& v, const Params& P, float inv_mass, float 
 }
 
 // v = v + feedback(measured - v) with the aligned-feedback clamp
-// (abi41.cu:5846-5884).
+// (abi41.cu:5846-5884); the arithmetic is velocity_update.
 __device__ void velocity_stage(const Params& P, float dt, VState* s) {
-    if (s->w <= 0.0f) {
-        s->vel = F3{0.0f, 0.0f, 0.0f};
-        return;
-    }
-    const float sdt = fmaxf(dt, kEps);
-    const F3 measured = (s->p - s->prev) * (1.0f / sdt);
-    const F3 base = s->vel;
-    if (!finite3(measured) || !finite3(base)) {
-        s->vel = F3{0.0f, 0.0f, 0.0f};
-        return;
-    }
-    const F3 proj = measured - base;
-    const float pdb = dot3(proj, base);
-    const float scale = (isfinite(pdb) && pdb > 0.0f) ? 0.9f : 1.0f;
-    const float max_delta = fmaxf(2.0e-4f, fmaxf(P.thickness, 0.0f) * 0.35f);
-    const float max_speed = max_delta / sdt;
-    F3 fb = proj * scale;
-    const float fspeed = len3(fb);
-    if (scale < 1.0f && isfinite(fspeed) && fspeed > max_speed && fspeed > kEps) fb = fb * (max_speed / fspeed);
-    if (!finite3(fb)) fb = F3{0.0f, 0.0f, 0.0f};
-    s->vel = base + fb;
+    s->vel = velocity_update(s->p, s->prev, s->vel, s->w, P.thickness, dt);
 }
 
 // Stretch constraint of edge (i, j) seen from one of its endpoints
@@ -257,21 +238,12 @@ __device__ void velocity_stage(const Params& P, float dt, VState* s) {
 // orientation so both endpoints get bit-identical values.
 __device__ __forceinline__ void spring_term(const Params& P, unsigned long long* counts, float dt, float4 pi, float4 pj,
                                             float rest, bool self_is_j, F3* dp, F3* dprev) {
+    F3 corr;
+    float c;
+    bool clamped;
+    if (!stretch_correction(pi, pj, rest, P.stretch_compliance, dt, &corr, &c, &clamped)) return;
+    if (clamped && !self_is_j) count1(counts, kCntHardFallbacks);
     const float wi = pi.w, wj = pj.w;
-    const float weight = wi + wj;
-    if (weight <= 0.0f) return;
-    const F3 delta = f3(pj) - f3(pi);
-    const float len = sqrtf(fmaxf(dot3(delta, delta), kEps));
-    const float c = len - rest;
-    const float alpha = fmaxf(P.stretch_compliance, 0.0f) / fmaxf(dt * dt, kEps);
-    const float dlambda = -c / (weight + alpha);
-    F3 corr = delta * (0.18f * dlambda / fmaxf(len, kEps));
-    const float corr_len = sqrtf(fmaxf(dot3(corr, corr), 0.0f));
-    const float max_corr = fmaxf(0.0025f, fminf(fmaxf(rest, 0.0f) * 0.10f, 0.025f));
-    if (corr_len > max_corr) {
-        corr = corr * (max_corr / fmaxf(corr_len, kEps));
-        if (!self_is_j) count1(counts, kCntHardFallbacks);
-    }
     const float wself = self_is_j ? wj : wi;
     if (wself > 0.0f) {
         const F3 d = self_is_j ? corr * wj : corr * (-wi);
@@ -349,45 +321,8 @@ __device__ __forceinline__ void tether_term(const Params& P, unsigned long long*
 // skipped; `guard` is set when the reference would count a guard.
 __device__ __forceinline__ bool bend_correction(const Params& P, float dt, float4 pi4, float4 pj4, float rest, F3* corr_out,
                                                 bool* guard) {
-    *guard = false;
-    const float wi = pi4.w, wj = pj4.w;
-    const float weight = wi + wj;
-    if (!isfinite(weight) || weight <= 0.0f) return false;
-    if (!isfinite(rest) || rest <= kEps) {
-        *guard = true;
-        return false;
-    }
-    const F3 pi = f3(pi4), pj = f3(pj4);
-    if (!finite3(pi) || !finite3(pj)) {
-        *guard = true;
-        return false;
-    }
-    const F3 delta = pj - pi;
-    const float len_sq = len_sq_xyz(delta);
-    if (!isfinite(len_sq) || len_sq <= 1.0e-10f) {
-        *guard = true;
-        return false;
-    }
-    const float inv_len = 1.0f / sqrtf(len_sq);
-    const float len = len_sq * inv_len;
-    const float c = len - rest;
-    if (!isfinite(c) || fabsf(c) <= 1.0e-6f) return false;
-    const float alpha = fmaxf(P.bend_compliance, 0.0f) / fmaxf(dt * dt, kEps);
-    const float dlambda = -c / fmaxf(weight + alpha, kEps);
-    F3 corr = delta * (0.10f * dlambda * inv_len);
-    if (!finite3(corr)) {
-        *guard = true;
-        return false;
-    }
-    const float corr_len = len3(corr);
-    const float max_corr = fmaxf(2.5e-4f, fminf(fmaxf(rest, P.thickness) * 0.08f, 0.020f));
-    if (!isfinite(corr_len) || corr_len <= 0.0f) return false;
-    if (corr_len > max_corr) {
-        corr = corr * (max_corr / fmaxf(corr_len, kEps));
-        *guard = true;
-    }
-    *corr_out = corr;
-    return true;
+    bool clamped;
+    return bend_correction_k(pi4, pj4, rest, P.bend_compliance, P.thickness, dt, corr_out, guard, &clamped);
 }
 
 __device__ __forceinline__ void bend_term(const Params& P, unsigned long long* counts, float dt, float4 pi, float4 pj,

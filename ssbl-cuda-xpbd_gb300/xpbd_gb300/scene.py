@@ -533,3 +533,24 @@ def serving_requests(rate: float = 200.0, duration: float = 60.0, seed: int = 0,
         frames = int(rng.integers(horizon[0], horizon[1] + 1))
         out.append(ClothRequest(cloth, opt, static, frames, 10, 2, len(out), t))
     return out
+
+
+def diff_scene(n: int = 64, frames: int = 60, stretch: float = 1.0e-7, bend: float = 1.0e-4) -> Scene:
+    """Contact-free cloth for the differentiable form: n x n grid (1 m), the
+    two corners of the y = +0.5 edge hard-pinned, 0.2 kg/m^2, damping 0.99
+    per substep, gravity -9.81, no colliders; 10 substeps x 2 iterations."""
+    pos, tris = grid_mesh(n, 1.0, 0.0)
+    w = np.zeros(n * n, np.float32)
+    w[(n - 1) * n] = 1.0
+    w[n * n - 1] = 1.0
+    cloth = build_cloth(pos, tris, 0.2, w)
+    opt = SolverOptions(dt=1.0 / 60.0, damping=0.99, gravity=(0.0, 0.0, -9.81), stretch_compliance=stretch,
+                        bend_compliance=bend, collision_margin=0.005)
+    return Scene(f"diff-grid-{n}", cloth, opt, np.empty((0, 3, 3), np.float32), 10, 2, frames, 1.0)
+
+
+def compliance_field(count: int, center: float, decades: float, seed: int) -> np.ndarray:
+    """Seeded per-constraint compliances, log-uniform within +-`decades`
+    around `center`."""
+    rng = np.random.default_rng(seed)
+    return (center * 10.0 ** rng.uniform(-decades, decades, count)).astype(np.float32)
