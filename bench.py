@@ -69,9 +69,9 @@ DESCRIPTIONS = {
 }
 
 
-def workload(name: str) -> list:
+def workload(name: str, cloths: int = 256) -> list:
     if name == "batch256":
-        return scene.batched_scenes(256, seed=0, frames=120)
+        return scene.batched_scenes(cloths, seed=0, frames=120)
     if name == "drop10k":
         return [scene.drop_scene(100, 200, seed=0, self_mode=2)]
     if name == "plain32":
@@ -323,6 +323,27 @@ def run_serving(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def time_plain_serial(native, scs, frames: int = 1) -> dict:
+    """One ABI41 handle per cloth, each frame waited for before the next
+    cloth steps: the order in which the reference add-on's handles run when
+    every launch goes to one device stream (the reference launches its
+    kernels on the legacy default stream, native/src/ssbl_xpbd_cuda_abi41.cu:
+    4527, 6204 and most other launches)."""
+    S, I = scs[0].substeps, scs[0].iterations
+    V = sum(len(s.cloth.positions_world) for s in scs)
+    total = 0.0
+    for s in scs:
+        solver = native.NativeXpbdSolver(s.cloth, s.options, s.static_triangles)
+        solver.step(S, I, diagnostics=False, synchronize=True)
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            solver.step(S, I, diagnostics=False, synchronize=True)
+        total += time.perf_counter() - t0
+        solver.close()
+    return {"value": V * S * frames / total, "unit": METRIC, "ms_per_step": 1000.0 * total / frames, "frames": frames,
+            "handles": len(scs), "note": "handles stepped one after another, each frame synchronised"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -331,7 +352,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batch256", choices=sorted(DESCRIPTIONS))
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--plain-frames", type=int, default=3)
+    ap.add_argument("--plain-frames", type=int, default=3, help="frames of the plain comparison (0 skips it)")
+    ap.add_argument("--batch-cloths", type=int, default=256, help="cloths of the batch256 workload (smaller for profiling)")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     args = ap.parse_args()
@@ -340,7 +362,11 @@ def main():
     if args.workload == "serve":
         run_serving(args, world, rank, local)
         return
-    scs = workload(args.workload)
+    scs = workload(args.workload, args.batch_cloths)
+    if args.batch_cloths != 256 and args.workload == "batch256":
+        nv = sum(len(s.cloth.positions_world) for s in scs)
+        DESCRIPTIONS["batch256"] = DESCRIPTIONS["batch256"].replace("256 independent cloths", f"{args.batch_cloths} independent cloths").replace(
+            "1,589,788 verts", f"{nv:,} verts")
     if args.impl == "reference":
         run_reference(args, scs, world, rank)
         return
@@ -457,7 +483,8 @@ def main():
            "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s / args.steps}
     assert np.isfinite(out).all()
 
-    plain = time_plain(native, scs, args.plain_frames) if batched else None
+    plain = time_plain(native, scs, args.plain_frames) if batched and args.plain_frames > 0 else None
+    plain_serial = time_plain_serial(native, scs) if batched and args.plain_frames > 0 else None
 
     if rank != 0:
         return
@@ -476,6 +503,9 @@ def main():
     if plain is not None:
         line["plain"] = plain
         line["batched_over_plain"] = value / plain["value"]
+    if plain_serial is not None:
+        line["plain_serial"] = plain_serial
+        line["batched_over_plain_serial"] = value / plain_serial["value"]
     print(json.dumps(line), flush=True)
 
 
