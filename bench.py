@@ -63,6 +63,9 @@ DESCRIPTIONS = {
     "drop10k": "10k cloth (100x100 grid, 19,602 tris) dropped on a sphere + 64^3 box/torus SDF, strict self "
                "collision 2 mm, friction 0.3, 10 substeps x 2 iterations per frame",
     "plain32": "plain 32x32 grid (1,024 verts), two pinned corners, ground, 10 substeps x 2 iterations",
+    "diff": "differentiable: 64x64 cloth (4,096 verts), per-constraint stretch / bend compliance fields, no contacts, "
+            "60 frames x 10 substeps x 2 iterations; one step = rollout + adjoint (per-frame checkpoints) of L2 to a "
+            "target from another seeded compliance field",
     "serve": "serving: Poisson arrivals 200/s of cloth solves, V log-uniform 1k-250k (16 grid sizes), horizons "
              "30-240 frames, random sphere and/or box/torus SDF, strict self collision 2 mm, admitted by a "
              "device-memory budget, resident until done, one frame per resident request per tick",
@@ -76,7 +79,7 @@ def workload(name: str, cloths: int = 256) -> list:
         return [scene.drop_scene(100, 200, seed=0, self_mode=2)]
     if name == "plain32":
         return [scene.plain_grid_scene(32, 120)]
-    if name == "serve":
+    if name in ("serve", "diff"):
         return []
     raise SystemExit(f"unknown workload {name}")
 
@@ -275,6 +278,66 @@ def time_plain(native, scs, frames: int) -> dict:
             "handles": len(scs), "launches_per_step": launches}
 
 
+def run_diff(args, world, rank, local):
+    """Differentiable form: one step = a 60-frame rollout of the 64 x 64
+    cloth and the adjoint of an L2 loss (vertex-substeps/s of the forward
+    frames; the backward recomputes each frame once more)."""
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable rollout"}), flush=True)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    from xpbd_gb300 import build
+    from xpbd_gb300.diff import DiffCloth
+
+    build.build()
+    sc = scene.diff_scene(64, 60)
+    ks = torch.tensor(scene.compliance_field(len(sc.cloth.edges), 1e-7, 1.0, 0), device="cuda")
+    kb = torch.tensor(scene.compliance_field(len(sc.cloth.bends), 1e-4, 1.0, 1), device="cuda")
+    kts = torch.tensor(scene.compliance_field(len(sc.cloth.edges), 1e-7, 1.0, 2), device="cuda")
+    ktb = torch.tensor(scene.compliance_field(len(sc.cloth.bends), 1e-4, 1.0, 3), device="cuda")
+    dc = DiffCloth(sc.cloth, sc.options)
+    target = dc.rollout(kts, ktb, sc.frames, sc.substeps, sc.iterations).clone()
+
+    def step():
+        x = dc.rollout(ks, kb, sc.frames, sc.substeps, sc.iterations)
+        return dc.backward(2.0 * (x - target))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gs, gb = step()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        dc.rollout(ks, kb, sc.frames, sc.substeps, sc.iterations)
+    torch.cuda.synchronize()
+    fwd = time.perf_counter() - t1
+    V = len(sc.cloth.positions_world)
+    value = V * sc.substeps * sc.frames * args.steps / el
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded compliance fields)",
+        "config": {"workload": DESCRIPTIONS["diff"], "vertices": V, "edges": len(sc.cloth.edges),
+                   "bends": len(sc.cloth.bends), "frames": sc.frames, "substeps": sc.substeps,
+                   "parallelism": f"replicas x{world}"},
+        "forward_only": {"value": V * sc.substeps * sc.frames * args.steps / fwd, "unit": METRIC,
+                         "ms_per_rollout": 1000.0 * fwd / args.steps},
+        "grad_norms": {"stretch": float(gs.norm()), "bend": float(gb.norm())},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "inputs and gradients stay on the device (torch tensors)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_serving(args, world, rank, local):
     """Serving form: the request loop for --serve-seconds of Poisson
     arrivals; a "step" is one tick (every resident request advances one
@@ -361,6 +424,9 @@ def main():
     world, rank, local = dist_setup()
     if args.workload == "serve":
         run_serving(args, world, rank, local)
+        return
+    if args.workload == "diff":
+        run_diff(args, world, rank, local)
         return
     scs = workload(args.workload, args.batch_cloths)
     if args.batch_cloths != 256 and args.workload == "batch256":
