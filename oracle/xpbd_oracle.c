@@ -166,6 +166,11 @@ struct OracleSolver {
     V3* avg_sum; float* avg_cnt;
     float red[8]; unsigned long long pcg_guard; float pcg_max_delta;
     int* cap_edges; float* cap_rest; int* cap_colors; int n_cap_colors;
+    /* prediction extras: incident triangles, volume pressure, force fields */
+    int *vt_off, *vt_tri;
+    int pressure_on; float *p_area, *p_rest;
+    float p_strength, p_accel, p_impulse, p_vrest, p_vlen;
+    SsblXpbdForceField fields[64]; int nfields;
 };
 
 enum { R_DAD = 0, R_RZ = 1, R_RZN = 2, R_STATUS = 3, R_INIT = 4, R_ITER = 5 };
@@ -429,17 +434,208 @@ static int contact_response(OracleSolver* s, V3 n, float proxy, V3* vel) {
     return corrected;
 }
 
-/* abi41.cu:1869-1925 (no force fields / pressure) */
+/* ---- force fields (abi41.cu:1262-1558) ----
+ * Restated kind by kind; turbulence uses the same lattice hash as the GPU
+ * build (an integer mix, not the Blender permutation table). */
+static V3 f3a(const float* a) { return v3(a[0], a[1], a[2]); }
+static float field_noise(V3 p, int seed, float salt) {
+    float x = sinf(p.x * 12.9898f + p.y * 78.233f + p.z * 37.719f + ((float)seed + salt) * 19.191f) * 43758.5453f;
+    return (x - floorf(x)) * 2.0f - 1.0f;
+}
+static int lattice_hash(int i) {
+    unsigned h = (unsigned)i * 0x9E3779B1u;
+    h ^= h >> 15; h *= 0x85EBCA77u; h ^= h >> 13;
+    return (int)(h & 255u);
+}
+static float noise_grad(int h, float x, float y, float z) {
+    h &= 15;
+    float u = h < 8 ? x : y, v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
+    return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+}
+static float nfade(float t) { return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f); }
+static float nlerp(float t, float a, float b) { return a + t * (b - a); }
+static float gradient_noise(float x, float y, float z) {
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    int X = (int)fx & 255, Y = (int)fy & 255, Z = (int)fz & 255;
+    x -= fx; y -= fy; z -= fz;
+    float u = nfade(x), v = nfade(y), w = nfade(z);
+    int A = lattice_hash(X) + Y, Bq = lattice_hash(X + 1) + Y;
+    int AA = lattice_hash(A) + Z, AB = lattice_hash(A + 1) + Z, BA = lattice_hash(Bq) + Z, BB = lattice_hash(Bq + 1) + Z;
+    float x0 = nlerp(u, noise_grad(lattice_hash(AA), x, y, z), noise_grad(lattice_hash(BA), x - 1.0f, y, z));
+    float x1 = nlerp(u, noise_grad(lattice_hash(AB), x, y - 1.0f, z), noise_grad(lattice_hash(BB), x - 1.0f, y - 1.0f, z));
+    float x2 = nlerp(u, noise_grad(lattice_hash(AA + 1), x, y, z - 1.0f), noise_grad(lattice_hash(BA + 1), x - 1.0f, y, z - 1.0f));
+    float x3 = nlerp(u, noise_grad(lattice_hash(AB + 1), x, y - 1.0f, z - 1.0f), noise_grad(lattice_hash(BB + 1), x - 1.0f, y - 1.0f, z - 1.0f));
+    return nlerp(w, nlerp(v, x0, x1), nlerp(v, x2, x3));
+}
+static float turbulence3(float size, float x, float y, float z) {
+    if (size != 0.0f && isfinite(size)) { float inv = 1.0f / size; x *= inv; y *= inv; z *= inv; }
+    float sum = 0.0f, amp = 1.0f, sc = 1.0f;
+    for (int o = 0; o < 3; ++o) { sum += (0.5f + 0.5f * gradient_noise(sc * x, sc * y, sc * z)) * amp; amp *= 0.5f; sc *= 2.0f; }
+    return sum * (4.0f / 7.0f);
+}
+static float field_falloff(const SsblXpbdForceField* f, float dist, float rdist) {
+    if (!isfinite(dist)) return 0.0f;
+    float dmin = fmaxf(f->distance_min, 0.0f), dmax = fmaxf(f->distance_max, 0.0f);
+    float rmin = fmaxf(f->radial_min, 0.0f), rmax = fmaxf(f->radial_max, 0.0f);
+    if (f->use_max_distance && dmax > 0.0f && dist >= dmax) return 0.0f;
+    if (f->use_radial_max && rmax > 0.0f && rdist >= rmax) return 0.0f;
+    float k = 1.0f;
+    if (f->use_max_distance && dmax > dmin && dist > dmin) k *= clamp01((dmax - dist) / fmaxf(dmax - dmin, K_EPS));
+    if (f->use_min_distance && f->falloff_power > 0.0f && dist > dmin) { float r = fmaxf(dmin, 1.0e-4f); k *= powf(r / fmaxf(dist, r), f->falloff_power); }
+    if (f->use_radial_max && rmax > rmin && rdist > rmin) k *= clamp01((rmax - rdist) / fmaxf(rmax - rmin, K_EPS));
+    if (f->use_radial_min && f->radial_falloff > 0.0f && rdist > rmin) { float r = fmaxf(rmin, 1.0e-4f); k *= powf(r / fmaxf(rdist, r), f->radial_falloff); }
+    return isfinite(k) ? k : 0.0f;
+}
+static V3 cap_field(V3 a) {
+    float l = vlen(a);
+    if (!isfinite(l) || l <= 5000.0f) return isfinite(l) ? a : v3(0, 0, 0);
+    return vmul(a, 5000.0f / fmaxf(l, K_EPS));
+}
+static V3 with_flow(const SsblXpbdForceField* f, V3 a, V3 vel, float falloff) {
+    if (f->type != 6 && f->type != 9) {
+        float flow = isfinite(f->flow) ? f->flow : 0.0f;
+        if (fabsf(flow) > 1.0e-6f && falloff != 0.0f) a = vadd(a, vmul(vel, -flow * falloff));
+    }
+    return cap_field(a);
+}
+static V3 field_accel(const SsblXpbdForceField* f, V3 p, V3 vel, V3 nrm, int has_n) {
+    V3 zero = v3(0, 0, 0);
+    if (!isfinite(f->strength) || f->strength == 0.0f || f->apply_to_location == 0) return zero;
+    V3 d = vsub(p, f3a(f->origin));
+    V3 axis = normalize_or(f3a(f->axis), v3(0, 0, 1));
+    V3 rd = f->use_2d_force ? vsub(d, vmul(axis, vdot(d, axis))) : d;
+    float dist = vlen(d), rdist = vlen(rd);
+    float fo = field_falloff(f, dist, rdist);
+    float st = f->strength * fo;
+    if (st == 0.0f || !isfinite(st)) return zero;
+    switch (f->type) {
+    case 1: { /* wind */
+        if (!has_n) return zero;
+        V3 dir = normalize_or(f3a(f->direction), zero);
+        float proj = vdot(dir, nrm);
+        if (!isfinite(proj) || proj <= 0.0f) return zero;
+        float m = st * proj;
+        if (f->noise > 0.0f) m *= fmaxf(0.0f, 1.0f + f->noise * field_noise(p, f->seed, 0.0f));
+        return with_flow(f, vmul(dir, m), vel, fo);
+    }
+    case 2: case 5: { /* force, charge */
+        V3 sd = f->use_2d_force ? rd : d;
+        float sdist = f->use_2d_force ? rdist : dist;
+        if (sdist <= 1.0e-6f) return zero;
+        float k = st / fmaxf(sdist, K_EPS);
+        if (f->type == 5) k /= fmaxf(sdist * sdist, 0.01f);
+        return with_flow(f, vmul(sd, k), vel, fo);
+    }
+    case 3: { /* vortex */
+        V3 radial = vsub(d, vmul(axis, vdot(d, axis)));
+        if (vdot(radial, radial) <= 1.0e-10f) return zero;
+        return with_flow(f, vmul(normalize_or(vcross(axis, radial), zero), st), vel, fo);
+    }
+    case 6: { /* harmonic */
+        float sdist = f->use_2d_force ? rdist : dist;
+        V3 sd = f->use_2d_force ? rd : d;
+        if (sdist <= 1.0e-6f) return zero;
+        V3 u = vmul(sd, 1.0f / fmaxf(sdist, K_EPS));
+        float spring = -st * (sdist - fmaxf(f->rest_length, 0.0f));
+        float damp = -vdot(vel, u) * fmaxf(f->harmonic_damping, 0.0f) * fabsf(st);
+        return with_flow(f, vmul(u, spring + damp), vel, fo);
+    }
+    case 7: { /* Lennard-Jones */
+        if (dist <= 1.0e-6f) return zero;
+        V3 u = vmul(d, 1.0f / fmaxf(dist, K_EPS));
+        float radius = fmaxf(f->rest_length, fmaxf(f->size, 0.1f));
+        float q = fminf(radius / fmaxf(dist, 1.0e-3f), 6.0f);
+        float q2 = q * q, q6 = q2 * q2 * q2;
+        return with_flow(f, vmul(u, st * (q6 * q6 - q6)), vel, fo);
+    }
+    case 8: { /* magnet */
+        V3 ax = normalize_or(f3a(f->direction), zero);
+        return with_flow(f, vmul(vcross(vel, ax), st), vel, fo);
+    }
+    case 9: { /* drag */
+        float speed = vlen(vel);
+        if (speed <= 1.0e-6f) return zero;
+        float lin = fmaxf(f->linear_drag, 0.0f), quad = fmaxf(f->quadratic_drag, 0.0f);
+        if (lin <= 0.0f && quad <= 0.0f) lin = fabsf(st);
+        return with_flow(f, vmul(vel, -(lin + quad * speed)), vel, fo);
+    }
+    case 4: { /* turbulence */
+        V3 q = f->use_global_coords ? p : vadd(d, axis);
+        V3 n = v3(-1.0f + 2.0f * turbulence3(f->size, q.x, q.y, q.z), -1.0f + 2.0f * turbulence3(f->size, q.y, q.z, q.x),
+                  -1.0f + 2.0f * turbulence3(f->size, q.z, q.x, q.y));
+        return with_flow(f, vmul(n, st), vel, fo);
+    }
+    case 10: { /* texture */
+        float freq = fmaxf(fmaxf(f->noise, f->texture_nabla), 0.25f);
+        if (f->size > 1.0e-6f) freq = fmaxf(freq, 1.0f / f->size);
+        V3 q = vmul(d, freq);
+        V3 n = v3(field_noise(q, f->seed, 0.0f), field_noise(q, f->seed, 7.0f), field_noise(q, f->seed, 13.0f));
+        return with_flow(f, vmul(n, st), vel, fo);
+    }
+    default: return zero;
+    }
+}
+
+/* Vertex normal from the incident triangles at the substep-start positions
+ * (abi41.cu:1213-1261; IEEE 1/sqrt). */
+static int vertex_normal(const OracleSolver* s, int i, const V3* x, V3* out) {
+    if (!s->vt_off) return 0;
+    int b = s->vt_off[i], e = s->vt_off[i + 1];
+    if (e <= b) return 0;
+    V3 acc = v3(0, 0, 0);
+    for (int k = b; k < e; ++k) {
+        int t = s->vt_tri[k];
+        if (t < 0 || t >= s->T) continue;
+        const int* tr = s->tris + 3 * t;
+        if (tr[0] < 0 || tr[1] < 0 || tr[2] < 0 || tr[0] >= s->V || tr[1] >= s->V || tr[2] >= s->V) continue;
+        V3 n = vcross(vsub(x[tr[1]], x[tr[0]]), vsub(x[tr[2]], x[tr[0]]));
+        float l2 = vdot(n, n);
+        if (!isfinite(l2) || l2 <= 1.0e-10f) continue;
+        acc = vadd(acc, vmul(n, 1.0f / sqrtf(l2)));
+    }
+    float a2 = vdot(acc, acc);
+    if (!isfinite(a2) || a2 <= 1.0e-10f) return 0;
+    *out = vmul(acc, 1.0f / sqrtf(a2));
+    return 1;
+}
+
+/* abi41.cu:1869-1925: gravity, volume pressure, force fields, damping,
+ * pressure speed trims; normals from the substep-start positions. */
 static void integrate_all(OracleSolver* s, float dt) {
+    const int needs_normal = s->pressure_on || s->nfields > 0;
+#pragma omp parallel for
+    for (int i = 0; i < s->V; ++i) s->prev[i] = s->pos[i];
 #pragma omp parallel for
     for (int i = 0; i < s->V; ++i) {
-        s->prev[i] = s->pos[i];
         if (!(s->w[i] > 0.0f)) { s->vel[i] = v3(0, 0, 0); s->pos[i] = s->rest[i]; continue; }
+        V3 nrm = v3(0, 0, 0);
+        int has_n = needs_normal && vertex_normal(s, i, s->prev, &nrm);
         V3 a = vadd(v3(s->cfg.gravity[0], s->cfg.gravity[1], s->cfg.gravity[2]), v3(0, 0, 0));
+        int pressure = s->pressure_on && has_n;
+        float area = pressure ? s->p_area[i] : 0.0f;
+        if (pressure && isfinite(area) && area > 0.0f) a = vadd(a, vmul(nrm, s->p_strength * s->p_accel * area * s->inv[i]));
+        if (s->nfields > 0) {
+            V3 fa = v3(0, 0, 0);
+            for (int k = 0; k < s->nfields; ++k) fa = vadd(fa, field_accel(&s->fields[k], s->prev[i], s->vel[i], nrm, has_n));
+            a = vadd(a, cap_field(fa));
+        }
         V3 vel = vadd(s->vel[i], vmul(a, dt));
         vel = vmul(vel, s->cfg.damping);
+        if (pressure) {
+            float rest = s->p_rest[i];
+            if (isfinite(rest) && rest > K_EPS && isfinite(dt) && dt > K_EPS) {
+                float pa = fmaxf(s->p_strength, 0.0f) * fmaxf(s->p_accel, 0.0f) * fmaxf(area, 0.0f) * fmaxf(s->inv[i], 0.0f);
+                float maxd = fmaxf(rest * fmaxf(s->p_impulse, 0.0f), 1.0e-7f);
+                float del = pa * dt * dt;
+                if (isfinite(del) && del > maxd) vel = vsub(vel, vmul(nrm, (del - maxd) / dt));
+                float vr = fmaxf(rest, fmaxf(s->p_vlen, 0.0f));
+                float maxo = fmaxf(vr * fmaxf(s->p_vrest, 0.0f) / dt, 1.0e-6f);
+                float out = vdot(vel, nrm);
+                if (isfinite(out) && out > maxo) vel = vsub(vel, vmul(nrm, out - maxo));
+            }
+        }
         s->vel[i] = vel;
-        s->pos[i] = vadd(s->pos[i], vmul(vel, dt));
+        s->pos[i] = vadd(s->prev[i], vmul(vel, dt));
     }
 }
 
@@ -1625,12 +1821,113 @@ void oracle_destroy(OracleSolver* s) {
                  s->te_off, s->te_other, s->te_side, s->te_rest, s->bj_off, s->bj_other, s->bj_side, s->bj_rest, s->bends,
                  s->bend_rest, s->bend_colors, s->tris, s->edges, s->pin_w, s->pin_t, s->pin_relax, s->sdf, s->stris,
                  s->vcell, s->vb_start, s->vb_ent, s->tb_start, s->tb_ent, s->eb_start, s->eb_ent, s->nb_count, s->nb_idx, s->acc,
-                 s->diag, s->pinv, s->r, s->z, s->d, s->q, s->off, s->avg_sum, s->avg_cnt, s->cap_edges, s->cap_rest, s->cap_colors};
+                 s->diag, s->pinv, s->r, s->z, s->d, s->q, s->off, s->avg_sum, s->avg_cnt, s->cap_edges, s->cap_rest, s->cap_colors,
+                 s->vt_off, s->vt_tri, s->p_area, s->p_rest};
     for (size_t k = 0; k < sizeof(p) / sizeof(p[0]); ++k) free(p[k]);
     free(s);
 }
 
 /* Creation and sanitising as abi41.cu:8791-8967 (without PCG / pressure). */
+static float env_scale(const char* name, float value, float lo, float hi) {
+    const char* raw = getenv(name);
+    if (raw && raw[0]) {
+        char* end = NULL;
+        float v = strtof(raw, &end);
+        if (end != raw && isfinite(v)) value = v;
+    }
+    return fmaxf(lo, fminf(value, hi));
+}
+
+/* Area shares (a third of each incident rest triangle, capped at 16 x the
+ * mean), rest scales (mean incident rest length, else sqrt(area), clamped to
+ * [0.02, 16] x the mean) and the outward-speed length scale. */
+static void pressure_prep(OracleSolver* s, const SsblXpbdMesh* mesh, float object_scale) {
+    const int V = s->V, T = s->T, E = s->E;
+    const float* pos = mesh->positions;
+    double total = 0.0;
+    int valid = 0;
+    for (int t = 0; t < T; ++t) {
+        const int* tr = s->tris + 3 * t;
+        if (tr[0] < 0 || tr[1] < 0 || tr[2] < 0 || tr[0] >= V || tr[1] >= V || tr[2] >= V) continue;
+        V3 a = v3(pos[3 * tr[0]], pos[3 * tr[0] + 1], pos[3 * tr[0] + 2]);
+        V3 b = v3(pos[3 * tr[1]], pos[3 * tr[1] + 1], pos[3 * tr[1] + 2]);
+        V3 cc = v3(pos[3 * tr[2]], pos[3 * tr[2] + 1], pos[3 * tr[2] + 2]);
+        V3 n = vcross(vsub(b, a), vsub(cc, a));
+        float sq4 = vdot(n, n);
+        if (!isfinite(sq4) || sq4 <= 0.0f) continue;
+        float area = 0.5f * sqrtf(sq4);
+        if (!isfinite(area) || area <= 0.0f) continue;
+        float share = area / 3.0f;
+        s->p_area[tr[0]] += share; s->p_area[tr[1]] += share; s->p_area[tr[2]] += share;
+        total += (double)area;
+        ++valid;
+    }
+    if (valid <= 0 || !(total > 0.0) || !isfinite(total)) {
+        for (int i = 0; i < V; ++i) s->p_area[i] = 0.0f;
+    } else {
+        float mean = (float)(total / (double)(V > 1 ? V : 1));
+        float cap = fmaxf(mean * 16.0f, 1.0e-12f);
+        for (int i = 0; i < V; ++i) s->p_area[i] = (!isfinite(s->p_area[i]) || s->p_area[i] <= 0.0f) ? 0.0f : fminf(s->p_area[i], cap);
+    }
+    double* sum = (double*)calloc((size_t)(V > 0 ? V : 1), sizeof(double));
+    int* cnt = (int*)calloc((size_t)(V > 0 ? V : 1), sizeof(int));
+    for (int e = 0; e < E; ++e) {
+        int i = mesh->edges ? mesh->edges[2 * e] : 0, j = mesh->edges ? mesh->edges[2 * e + 1] : 0;
+        if (i < 0) i = 0;
+        if (j < 0) j = 0;
+        float r = mesh->edge_rest_lengths ? mesh->edge_rest_lengths[e] : 0.0f;
+        if (i >= V || j >= V || !isfinite(r) || r <= 0.0f) continue;
+        sum[i] += (double)r; sum[j] += (double)r; cnt[i] += 1; cnt[j] += 1;
+    }
+    double tot = 0.0;
+    int nval = 0;
+    for (int i = 0; i < V; ++i) {
+        float x = 0.0f;
+        if (cnt[i] > 0) x = (float)(sum[i] / (double)cnt[i]);
+        else if (isfinite(s->p_area[i]) && s->p_area[i] > 0.0f) x = sqrtf(s->p_area[i]);
+        if (isfinite(x) && x > 0.0f) { s->p_rest[i] = x; tot += (double)x; ++nval; }
+    }
+    free(sum); free(cnt);
+    float mean = nval > 0 ? (float)(tot / (double)nval) : 1.0f;
+    float lo = fmaxf(mean * 0.02f, 1.0e-7f), hi = fmaxf(mean * 16.0f, lo);
+    for (int i = 0; i < V; ++i) {
+        float x = s->p_rest[i];
+        if (!isfinite(x) || x <= 0.0f) x = mean;
+        s->p_rest[i] = fmaxf(lo, fminf(x, hi));
+    }
+    /* velocity length scale */
+    float ms = 0.0f;
+    int mc = 0;
+    for (int i = 0; i < V; ++i) if (isfinite(s->p_rest[i]) && s->p_rest[i] > 0.0f) { ms += s->p_rest[i]; ++mc; }
+    ms = mc > 0 ? ms / (float)mc : 1.0f;
+    int any = 0;
+    V3 lo3 = v3(0, 0, 0), hi3 = v3(0, 0, 0);
+    for (int i = 0; i < V; ++i) {
+        V3 p = v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        if (!vfinite(p)) continue;
+        if (!any) { lo3 = hi3 = p; any = 1; }
+        else {
+            lo3 = v3(fminf(lo3.x, p.x), fminf(lo3.y, p.y), fminf(lo3.z, p.z));
+            hi3 = v3(fmaxf(hi3.x, p.x), fmaxf(hi3.y, p.y), fmaxf(hi3.z, p.z));
+        }
+    }
+    if (!any) { s->p_vlen = fmaxf(ms, 1.0e-6f); return; }
+    V3 span = vsub(hi3, lo3);
+    float diag = sqrtf(fmaxf(vdot(span, span), 0.0f));
+    if (!isfinite(diag) || diag <= 0.0f) { s->p_vlen = fmaxf(ms, 1.0e-6f); return; }
+    float obj = isfinite(object_scale) && object_scale > 0.0f ? object_scale : 0.08f;
+    s->p_vlen = fmaxf(diag * obj, ms * 4.0f);
+}
+
+int oracle_update_force_fields(OracleSolver* s, const SsblXpbdForceField* fields, int count) {
+    if (!s) return set_err("invalid force field update");
+    if (count < 0 || count > 64) return set_err("force field count exceeds SSBL maximum");
+    if (count > 0 && !fields) return set_err("missing force field data");
+    if (count > 0) memcpy(s->fields, fields, sizeof(SsblXpbdForceField) * (size_t)count);
+    s->nfields = count;
+    return 1;
+}
+
 OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* mesh) {
     if (!config || config->vertex_count < 0 || config->edge_count < 0 || config->triangle_count < 0 || !isfinite(config->dt) ||
         !(config->dt > 0.0f) || !mesh || !mesh->positions || !mesh->inv_mass) {
@@ -1754,6 +2051,31 @@ OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* me
         if (s->vhash) { s->vcell = (int*)calloc(nv * 4, sizeof(int)); s->vb_start = (int*)calloc((size_t)s->nvb + 1, sizeof(int)); s->vb_ent = (int*)calloc(nv, sizeof(int)); }
         if (s->thash) { s->tb_start = (int*)calloc((size_t)s->ntb + 1, sizeof(int)); s->tb_ent = (int*)calloc((size_t)T * MAX_PRIM_CELLS, sizeof(int)); }
         if (s->ehash) { s->eb_start = (int*)calloc((size_t)s->neb + 1, sizeof(int)); s->eb_ent = (int*)calloc((size_t)E * MAX_PRIM_CELLS, sizeof(int)); }
+    }
+    /* vertex -> incident triangles in triangle order */
+    s->vt_off = (int*)calloc(nv + 1, sizeof(int));
+    for (int t = 0; t < T; ++t)
+        for (int a = 0; a < 3; ++a) { int id = s->tris[3 * t + a]; if (id >= 0 && id < V) s->vt_off[id + 1]++; }
+    for (int i = 0; i < V; ++i) s->vt_off[i + 1] += s->vt_off[i];
+    s->vt_tri = (int*)xcalloc((size_t)s->vt_off[V] + 1, sizeof(int));
+    {
+        int* cur = (int*)calloc(nv + 1, sizeof(int));
+        memcpy(cur, s->vt_off, sizeof(int) * (size_t)V);
+        for (int t = 0; t < T; ++t)
+            for (int a = 0; a < 3; ++a) { int id = s->tris[3 * t + a]; if (id >= 0 && id < V) s->vt_tri[cur[id]++] = t; }
+        free(cur);
+    }
+    /* volume pressure (abi41.cu:7413-7584, 8816-8903) */
+    s->pressure_on = c->use_volume_pressure && c->pressure_strength > 0.0f && isfinite(c->pressure_strength);
+    s->p_strength = fmaxf(c->pressure_strength, 0.0f);
+    s->p_accel = env_scale("SSBL_ABI41_PRESSURE_UI_ACCEL_SCALE", 1792.0f, 1.0f, 8192.0f);
+    s->p_impulse = env_scale("SSBL_ABI41_PRESSURE_IMPULSE_REST_SCALE", 0.85f, 0.05f, 8.0f);
+    s->p_vrest = env_scale("SSBL_ABI41_PRESSURE_VELOCITY_REST_SCALE", 2.25f, 0.10f, 16.0f);
+    if (s->pressure_on) {
+        float objs = env_scale("SSBL_ABI41_PRESSURE_VELOCITY_OBJECT_SCALE", 0.08f, 0.005f, 1.0f);
+        s->p_area = (float*)calloc(nv, sizeof(float));
+        s->p_rest = (float*)calloc(nv, sizeof(float));
+        pressure_prep(s, mesh, objs);
     }
     int nst = config->static_triangle_count > 0 ? config->static_triangle_count : 0;
     if (!build_sdf(s, mesh->static_triangles, nst)) { oracle_destroy(s); return NULL; }

@@ -38,6 +38,8 @@ int oracle_update_pin_targets(OracleSolver* s, const int* indices, const float* 
 int oracle_update_runtime_colliders(OracleSolver* s, const SsblXpbdRuntimeColliders* c);
 int oracle_update_positions(OracleSolver* s, const float* positions, int max_floats);
 int oracle_update_static_triangles(OracleSolver* s, const float* triangles, int count);
+/* Force fields (at most 64) applied by the prediction from the next step. */
+int oracle_update_force_fields(OracleSolver* s, const SsblXpbdForceField* fields, int count);
 int oracle_step(OracleSolver* s, int substeps, int iterations);
 int oracle_download_positions(OracleSolver* s, float* out, int max_floats);
 int oracle_download_state(OracleSolver* s, float* pos3, float* prev3, float* vel3);

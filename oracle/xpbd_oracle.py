@@ -40,6 +40,7 @@ def load():
         "oracle_update_runtime_colliders": (ci, [vp, vp]),
         "oracle_update_positions": (ci, [vp, pf, ci]),
         "oracle_update_static_triangles": (ci, [vp, pf, ci]),
+        "oracle_update_force_fields": (ci, [vp, vp, ci]),
         "oracle_step": (ci, [vp, ci, ci]),
         "oracle_download_positions": (ci, [vp, pf, ci]),
         "oracle_download_state": (ci, [vp, pf, pf, pf]),
@@ -124,6 +125,11 @@ class OracleSolver:
     def update_static_triangles(self, tris):
         t = np.ascontiguousarray(np.asarray(tris, np.float32).reshape(-1, 3))
         self._check(self._lib.oracle_update_static_triangles(self._h, _fp(t), len(t) // 3))
+
+    def update_force_fields(self, fields):
+        """`fields`: a ctypes array of NativeForceField records."""
+        n = len(fields)
+        self._check(self._lib.oracle_update_force_fields(self._h, ctypes.addressof(fields) if n else None, n))
 
     def step(self, substeps, iterations):
         self._check(self._lib.oracle_step(self._h, int(substeps), int(iterations)))

@@ -42,15 +42,9 @@ bool frame_inputs(Solver* S, int cloth, const SsblXpbdFrameInputs* in) {
     if (in->update_dynamic_particles && in->dynamic_particle_count > 0)
         return fail("dynamic particle colliders are not supported by this build of the GB300 solver");
     if (in->update_static_triangles && !upload_static(S, cloth, in->static_triangles, in->static_triangle_count)) return false;
-    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
-    if (in->update_force_fields) {
-        if (in->force_field_count < 0 || in->force_field_count > 64) return fail("force field count exceeds SSBL maximum");
-        if (in->force_field_count > 0) return fail("force fields are not supported by this build of the GB300 solver");
-        for (int k = k0; k < k1; ++k) {
-            S->cl[k].force_field_count = 0;
-            S->cl[k].unsupported_force_field_count = std::max(in->unsupported_force_field_count, 0);
-        }
-    }
+    if (in->update_force_fields &&
+        !upload_fields(S, cloth, in->force_fields, in->force_field_count, in->unsupported_force_field_count))
+        return false;
     int ff = 0, uff = 0;
     for (const Cloth& C : S->cl) {
         ff += C.force_field_count;

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cstdlib>
 #include <mutex>
 #include <unordered_map>
 
@@ -120,6 +121,121 @@ int count_wings(int V, const std::vector<int4>& tris, size_t begin, size_t end) 
         }
     }
     return wings;
+}
+
+// ---- volume pressure preprocessing (abi41.cu:7413-7584, 8816-8903) ----
+
+// A tuning constant of the pressure model, overridable from the environment
+// under the reference's variable names, clamped to its range.
+float env_scale(const char* name, float value, float lo, float hi) {
+    const char* raw = std::getenv(name);
+    if (raw && raw[0]) {
+        char* end = nullptr;
+        const float v = std::strtof(raw, &end);
+        if (end != raw && std::isfinite(v)) value = v;
+    }
+    return std::max(lo, std::min(value, hi));
+}
+
+// Area share of each vertex: a third of every incident triangle's rest area,
+// capped at 16 x the mean vertex area; all zero without a valid triangle.
+std::vector<float> pressure_area_shares(int V, const std::vector<int4>& tris, size_t t0, size_t t1, const float* pos) {
+    std::vector<float> shares(V, 0.0f);
+    double total = 0.0;
+    int valid = 0;
+    for (size_t k = t0; k < t1; ++k) {
+        const int4 t = tris[k];
+        if (t.x < 0 || t.y < 0 || t.z < 0 || t.x >= V || t.y >= V || t.z >= V) continue;
+        const F3 a = F3{pos[3 * t.x], pos[3 * t.x + 1], pos[3 * t.x + 2]};
+        const F3 b = F3{pos[3 * t.y], pos[3 * t.y + 1], pos[3 * t.y + 2]};
+        const F3 c = F3{pos[3 * t.z], pos[3 * t.z + 1], pos[3 * t.z + 2]};
+        const F3 n = cross3(b - a, c - a);
+        const float sq4 = dot3(n, n);
+        if (!std::isfinite(sq4) || sq4 <= 0.0f) continue;
+        const float area = 0.5f * std::sqrt(sq4);
+        if (!std::isfinite(area) || area <= 0.0f) continue;
+        const float share = area / 3.0f;
+        shares[t.x] += share;
+        shares[t.y] += share;
+        shares[t.z] += share;
+        total += (double)area;
+        ++valid;
+    }
+    if (valid <= 0 || !(total > 0.0) || !std::isfinite(total)) return std::vector<float>(V, 0.0f);
+    const float mean = (float)(total / (double)std::max(V, 1));
+    const float cap = std::max(mean * 16.0f, 1.0e-12f);
+    for (float& x : shares) x = (!std::isfinite(x) || x <= 0.0f) ? 0.0f : std::min(x, cap);
+    return shares;
+}
+
+// Rest length scale of each vertex: the mean rest length of its edges (else
+// the square root of its area share), clamped to [0.02, 16] x the mean.
+std::vector<float> pressure_rest_scales(int V, const int* edges, const float* rest, int E, const std::vector<float>& shares) {
+    std::vector<float> scales(V, 0.0f);
+    std::vector<double> sum(V, 0.0);
+    std::vector<int> cnt(V, 0);
+    for (int e = 0; e < E; ++e) {
+        const int i = std::max(edges ? edges[2 * e] : 0, 0), j = std::max(edges ? edges[2 * e + 1] : 0, 0);
+        const float r = rest ? rest[e] : 0.0f;
+        if (i >= V || j >= V || !std::isfinite(r) || r <= 0.0f) continue;
+        sum[i] += (double)r;
+        sum[j] += (double)r;
+        cnt[i] += 1;
+        cnt[j] += 1;
+    }
+    double total = 0.0;
+    int valid = 0;
+    for (int i = 0; i < V; ++i) {
+        float x = 0.0f;
+        if (cnt[i] > 0)
+            x = (float)(sum[i] / (double)cnt[i]);
+        else if (std::isfinite(shares[i]) && shares[i] > 0.0f)
+            x = std::sqrt(shares[i]);
+        if (std::isfinite(x) && x > 0.0f) {
+            scales[i] = x;
+            total += (double)x;
+            ++valid;
+        }
+    }
+    const float mean = valid > 0 ? (float)(total / (double)valid) : 1.0f;
+    const float lo = std::max(mean * 0.02f, 1.0e-7f), hi = std::max(mean * 16.0f, lo);
+    for (float& x : scales) {
+        if (!std::isfinite(x) || x <= 0.0f) x = mean;
+        x = std::max(lo, std::min(x, hi));
+    }
+    return scales;
+}
+
+// Length scale of the outward-speed trim: max(bounding-box diagonal x object
+// scale, 4 x the mean rest scale).
+float pressure_velocity_length(int V, const float* pos, const std::vector<float>& scales, float object_scale) {
+    float mean = 0.0f;
+    int n = 0;
+    for (float x : scales)
+        if (std::isfinite(x) && x > 0.0f) {
+            mean += x;
+            ++n;
+        }
+    mean = n > 0 ? mean / (float)n : 1.0f;
+    bool any = false;
+    F3 lo{0.0f, 0.0f, 0.0f}, hi{0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < V; ++i) {
+        const F3 p{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        if (!finite3(p)) continue;
+        if (!any) {
+            lo = hi = p;
+            any = true;
+        } else {
+            lo = F3{std::min(lo.x, p.x), std::min(lo.y, p.y), std::min(lo.z, p.z)};
+            hi = F3{std::max(hi.x, p.x), std::max(hi.y, p.y), std::max(hi.z, p.z)};
+        }
+    }
+    if (!any) return std::max(mean, 1.0e-6f);
+    const F3 span = hi - lo;
+    const float diag = std::sqrt(std::max(dot3(span, span), 0.0f));
+    if (!std::isfinite(diag) || diag <= 0.0f) return std::max(mean, 1.0e-6f);
+    const float obj = std::isfinite(object_scale) && object_scale > 0.0f ? object_scale : 0.08f;
+    return std::max(diag * obj, mean * 4.0f);
 }
 
 float self_radius(const SsblXpbdConfig& c) {
@@ -252,6 +368,10 @@ View Solver::view() const {
     v.pin_target = pin_target;
     v.pin_weight = pin_weight;
     v.pin_relax = pin_relax;
+    v.vt_off = vt_off;
+    v.vt_tri = vt_tri;
+    v.p_area = p_area;
+    v.p_rest = p_rest;
     v.counts = counts;
     v.vcell = vcell;
     v.vb_count = vb_count;
@@ -281,7 +401,14 @@ void free_solver(Solver* S) {
     if (!S) return;
     if (S->stream) cudaStreamSynchronize(S->stream);
     S->drop_graphs();
-    for (Cloth& c : S->cl) release_grid(S, c);
+    for (Cloth& c : S->cl) {
+        release_grid(S, c);
+        dfree(c.fields_dev);
+    }
+    dfree(S->vt_off);
+    dfree(S->vt_tri);
+    dfree(S->p_area);
+    dfree(S->p_rest);
     dfree(S->dp);
     dfree(S->vcloth);
     dfree(S->ecloth);
@@ -661,6 +788,36 @@ bool set_colliders(Solver* S, int cloth, const SsblXpbdRuntimeColliders& c) {
     return true;
 }
 
+// Force fields of a cloth (cloth < 0: every cloth), at most 64
+// (abi41.cu:5920-5960).
+bool upload_fields(Solver* S, int cloth, const SsblXpbdForceField* fields, int count, int unsupported) {
+    if (!valid_cloth(S, cloth)) return fail("invalid force field update");
+    if (count < 0 || count > kMaxFieldRecords) return fail("force field count exceeds SSBL maximum");
+    if (count > 0 && !fields) return fail("missing force field data");
+    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
+    AllocAccount account(&S->device_bytes);
+    for (int k = k0; k < k1; ++k) {
+        Cloth& C = S->cl[k];
+        C.unsupported_force_field_count = std::max(unsupported, 0);
+        if (count > C.fields_capacity) {
+            if (!cuda_ok(cudaStreamSynchronize(S->stream), "force field reallocation")) return false;
+            S->device_bytes -= (long long)sizeof(SsblXpbdForceField) * C.fields_capacity;
+            dfree(C.fields_dev);
+            C.fields_capacity = 0;
+            if (!dalloc(&C.fields_dev, count, "force field allocation")) return false;
+            C.fields_capacity = count;
+        }
+        if (count > 0 && !dupload(C.fields_dev, fields, count, S->stream, "upload force fields")) return false;
+        C.force_field_count = count;
+        Params& P = S->hp[k];
+        P.fields = C.fields_dev;
+        P.field_count = count;
+        P.needs_normal = (P.pressure_on || count > 0) ? 1 : 0;
+    }
+    S->params_dirty = true;
+    return cuda_ok(cudaStreamSynchronize(S->stream), "upload force fields");
+}
+
 bool upload_positions(Solver* S, int cloth, const float* positions, int max_floats) {
     if (!valid_cloth(S, cloth) || !positions) return fail("invalid position upload");
     const Range r = cloth_range(S, cloth);
@@ -741,8 +898,6 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
         SsblXpbdConfig& c = C.cfg;
         c = *config;
         sanitize(c);
-        if (c.use_volume_pressure && c.pressure_strength > 0.0f)
-            return bail(k, "volume pressure is not supported by this build of the GB300 solver");
         if (K > 1 && c.stretch_optimization_enabled)
             return bail(k, "hard stretch optimization runs on one-cloth solvers only");
         if (c.bend_count > 0 && (!mesh->bends || !mesh->bend_rest_lengths))
@@ -885,6 +1040,56 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
     S->h_pin_weight.assign(nV, -1.0f);
     S->h_pin_target.assign(nV, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     S->h_pin_relax.assign(nV, 0.0f);
+    // vertex -> incident triangles in triangle order (vertex normals)
+    std::vector<int> vt_off(nV + 1, 0), vt_tri;
+    for (int t = 0; t < nT; ++t) {
+        const int4 tr = tris[t];
+        const int ids[3] = {tr.x, tr.y, tr.z};
+        for (int a = 0; a < 3; ++a)
+            if (ids[a] >= 0 && ids[a] < nV) vt_off[ids[a] + 1]++;
+    }
+    for (int i = 0; i < nV; ++i) vt_off[i + 1] += vt_off[i];
+    vt_tri.assign(vt_off[nV], -1);
+    {
+        std::vector<int> cur(vt_off.begin(), vt_off.end() - 1);
+        for (int t = 0; t < nT; ++t) {
+            const int4 tr = tris[t];
+            const int ids[3] = {tr.x, tr.y, tr.z};
+            for (int a = 0; a < 3; ++a)
+                if (ids[a] >= 0 && ids[a] < nV) vt_tri[cur[ids[a]]++] = t;
+        }
+    }
+    // volume pressure shares and scales per cloth
+    const float accel_scale = env_scale("SSBL_ABI41_PRESSURE_UI_ACCEL_SCALE", 1792.0f, 1.0f, 8192.0f);
+    const float impulse_scale = env_scale("SSBL_ABI41_PRESSURE_IMPULSE_REST_SCALE", 0.85f, 0.05f, 8.0f);
+    const float velocity_scale = env_scale("SSBL_ABI41_PRESSURE_VELOCITY_REST_SCALE", 2.25f, 0.10f, 16.0f);
+    const float object_scale = env_scale("SSBL_ABI41_PRESSURE_VELOCITY_OBJECT_SCALE", 0.08f, 0.005f, 1.0f);
+    std::vector<float> p_area, p_rest;
+    bool any_pressure = false;
+    for (int k = 0; k < K; ++k) {
+        const SsblXpbdConfig& c = S->cl[k].cfg;
+        S->cl[k].pressure_on = c.use_volume_pressure && c.pressure_strength > 0.0f && std::isfinite(c.pressure_strength);
+        any_pressure |= S->cl[k].pressure_on;
+    }
+    if (any_pressure) {
+        p_area.assign(nV, 0.0f);
+        p_rest.assign(nV, 0.0f);
+        for (int k = 0; k < K; ++k) {
+            Params& P = S->hp[k];
+            const SsblXpbdMesh* mesh = &meshes[k];
+            // local triangle indices (negative indices clamped to 0 as at create)
+            std::vector<int4> lt(P.T);
+            for (int t = 0; t < P.T; ++t) {
+                const int* tr = mesh->triangles ? mesh->triangles + 3 * t : nullptr;
+                lt[t] = make_int4(tr ? std::max(tr[0], 0) : 0, tr ? std::max(tr[1], 0) : 0, tr ? std::max(tr[2], 0) : 0, 0);
+            }
+            const std::vector<float> a = pressure_area_shares(P.V, lt, 0, lt.size(), mesh->positions);
+            const std::vector<float> r = pressure_rest_scales(P.V, mesh->edges, mesh->edge_rest_lengths, P.E, a);
+            std::copy(a.begin(), a.end(), p_area.begin() + P.vstart);
+            std::copy(r.begin(), r.end(), p_rest.begin() + P.vstart);
+            P.pressure_velocity_length_scale = pressure_velocity_length(P.V, mesh->positions, r, object_scale);
+        }
+    }
     S->pin_mark.assign(nV, 0);
     S->pin_kept.assign(nV, 0);
 
@@ -911,6 +1116,14 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
         P.self_mode = c.self_collision_mode;
         P.max_neighbors = c.max_self_collision_neighbors;
         P.stretch_strength = c.stretch_optimization_strength;
+        P.pressure_on = C.pressure_on ? 1 : 0;
+        P.pressure_strength = std::max(c.pressure_strength, 0.0f);
+        P.pressure_accel_scale = accel_scale;
+        P.pressure_impulse_rest_scale = impulse_scale;
+        P.pressure_velocity_rest_scale = velocity_scale;
+        P.needs_normal = P.pressure_on;
+        P.fields = nullptr;
+        P.field_count = 0;
         C.self_enabled = c.self_collision != 0 && radius > 0.0f && P.V > 0;
         C.interval = std::max(c.self_collision_interval, 1);
         C.passes = std::max(1, std::min(c.fast_self_collision_passes, 8));
@@ -967,6 +1180,11 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
              dalloc(&S->tcloth, nT, "cloth map allocation");
     if (ok && S->jacobi_bends)
         ok = dalloc(&S->bj_off, nV + 1, "bend CSR allocation") && dalloc(&S->bj_ent, bj_ent.size(), "bend CSR allocation");
+    if (ok && nT > 0)
+        ok = dalloc(&S->vt_off, nV + 1, "incident triangle allocation") &&
+             dalloc(&S->vt_tri, vt_tri.size(), "incident triangle allocation");
+    if (ok && any_pressure)
+        ok = dalloc(&S->p_area, nV, "pressure area allocation") && dalloc(&S->p_rest, nV, "pressure scale allocation");
     if (ok && S->self_any) {
         ok = dalloc(&S->nb_count, nV, "self collision count allocation") &&
              dalloc(&S->nb_idx, (size_t)nV * kNeighborSlots, "self collision index allocation") &&
@@ -1039,6 +1257,10 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
          dupload(S->pin_weight, S->h_pin_weight.data(), nV, st, "pin weight upload") &&
          dupload(S->pin_target, S->h_pin_target.data(), nV, st, "pin target upload") &&
          dupload(S->pin_relax, S->h_pin_relax.data(), nV, st, "pin relaxation upload") &&
+         (!S->vt_off || (dupload(S->vt_off, vt_off.data(), vt_off.size(), st, "incident triangle upload") &&
+                         dupload(S->vt_tri, vt_tri.data(), vt_tri.size(), st, "incident triangle upload"))) &&
+         dupload(S->p_area, p_area.data(), p_area.size(), st, "pressure area upload") &&
+         dupload(S->p_rest, p_rest.data(), p_rest.size(), st, "pressure scale upload") &&
          dupload(S->vcloth, vmap.data(), vmap.size(), st, "cloth map upload") &&
          dupload(S->ecloth, emap.data(), emap.size(), st, "cloth map upload") &&
          dupload(S->tcloth, tmap.data(), tmap.size(), st, "cloth map upload") &&
@@ -1123,10 +1345,11 @@ int order_mode(bool need, bool plain) { return need ? (plain ? 2 : 1) : 0; }
 // (bends by colour, self collision).
 void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof) {
     const int nV = S->nV, nE = S->nE;
-    bool analytic = false, sdf = false;
+    bool analytic = false, sdf = false, normals = false;
     for (const Params& P : S->hp) {
         analytic |= P.use_ground || P.use_wall || P.use_sphere;
         sdf |= P.sdf_ready != 0;
+        normals |= P.needs_normal != 0;
     }
     const bool pcg = S->pcg_on;
     const bool spring = nE > 0 && !pcg;
@@ -1209,7 +1432,9 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         base.substep = s;
         const SelfPlan sp = plan_self(S, s, substeps);
         View pv = cur_view();
+        if (normals) pv.pos = S->pos[cur ^ 1];  // vertex normals read the snapshot
         timed(kKPredict, 1, [&] { launch_predict(pv, nV, S->stream); });
+        if (normals) cur ^= 1;
         for (int it = 0; it < iterations; ++it) {
             const bool last_it = it == iterations - 1;
             const bool final_c = (s == substeps - 1) && last_it;
@@ -1340,12 +1565,13 @@ namespace {
 // The frame graph for (substeps, iterations) and the current collider kinds,
 // captured and instantiated on first use.
 GraphEntry* ensure_graph(Solver* S, int substeps, int iterations) {
-    int analytic = 0, sdf = 0;
+    int analytic = 0, sdf = 0, normals = 0;
     for (const Params& P : S->hp) {
         analytic |= (P.use_ground || P.use_wall || P.use_sphere) ? 1 : 0;
         sdf |= P.sdf_ready ? 1 : 0;
+        normals |= P.needs_normal ? 1 : 0;
     }
-    const GraphKey key{substeps, iterations, analytic, sdf};
+    const GraphKey key{substeps, iterations, analytic, sdf, normals};
     auto it = S->graphs.find(key);
     if (it == S->graphs.end()) {
         GraphEntry g;

@@ -22,6 +22,8 @@
 namespace xg {
 namespace host {
 
+constexpr int kMaxFieldRecords = 64;  // force fields per cloth (abi41.cu:166)
+
 extern thread_local std::string g_error;
 // Device bytes of the solver being built or updated on this thread: every
 // successful dalloc adds to it while an AllocAccount is in scope.
@@ -92,9 +94,10 @@ enum KernelKind {
 };
 
 struct GraphKey {
-    int substeps, iterations, analytic, sdf;
+    int substeps, iterations, analytic, sdf, normals;
     bool operator<(const GraphKey& o) const {
-        return std::tie(substeps, iterations, analytic, sdf) < std::tie(o.substeps, o.iterations, o.analytic, o.sdf);
+        return std::tie(substeps, iterations, analytic, sdf, normals) <
+               std::tie(o.substeps, o.iterations, o.analytic, o.sdf, o.normals);
     }
 };
 
@@ -153,6 +156,9 @@ struct Cloth {
     int wing_count = 0;
     int force_field_count = 0;
     int unsupported_force_field_count = 0;
+    SsblXpbdForceField* fields_dev = nullptr;  // device copy of the cloth's force fields
+    int fields_capacity = 0;
+    bool pressure_on = false;
 };
 
 struct Solver {
@@ -183,6 +189,10 @@ struct Solver {
     int2* sp_ent = nullptr;
     int* te_off = nullptr;
     int2* te_ent = nullptr;
+    int* vt_off = nullptr;  // vertex -> incident triangles (normals for pressure / fields)
+    int* vt_tri = nullptr;
+    float* p_area = nullptr;  // volume pressure per vertex (any cloth with pressure)
+    float* p_rest = nullptr;
     int* bj_off = nullptr;  // bends as a Jacobi gather (cloths without colours)
     int2* bj_ent = nullptr;
     int2* bends = nullptr;  // coloured bends merged by (colour, cloth)
@@ -258,6 +268,7 @@ void free_solver(Solver* S);
 bool upload_pins(Solver* S, int cloth, const int* indices, const float* positions, const float* weights, int count);
 bool set_colliders(Solver* S, int cloth, const SsblXpbdRuntimeColliders& c);
 bool upload_static(Solver* S, int cloth, const float* tris, int count);
+bool upload_fields(Solver* S, int cloth, const SsblXpbdForceField* fields, int count, int unsupported);
 bool upload_positions(Solver* S, int cloth, const float* positions, int max_floats);
 bool download_positions(Solver* S, int cloth, float* out, int max_floats);
 bool reset_cloths(Solver* S, int cloth);

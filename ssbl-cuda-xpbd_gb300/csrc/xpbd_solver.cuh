@@ -18,6 +18,7 @@
 
 #include <string>
 
+#include "../../include/ssbl_xpbd_cuda.h"
 #include "xpbd_math.cuh"
 
 namespace xg {
@@ -119,6 +120,16 @@ struct Params {
     int vbase, tbase, ebase;           // offsets of its tables in the shared bucket arrays
     int vhash, thash, ehash;           // hash in use (else brute force)
     float stretch_strength;            // clamp01(stretch_optimization_strength)
+    // external accelerations of the prediction (force fields, volume pressure)
+    const SsblXpbdForceField* fields;  // field_count records (device)
+    int field_count;
+    int pressure_on;                   // use_volume_pressure with a positive strength
+    float pressure_strength;
+    float pressure_accel_scale;
+    float pressure_impulse_rest_scale;
+    float pressure_velocity_rest_scale;
+    float pressure_velocity_length_scale;
+    int needs_normal;                  // pressure or fields: vertex normals are gathered
 };
 
 // Buffers of the hard-stretch CG solve and the averaged caps.
@@ -169,6 +180,10 @@ struct View {
     const float4* pin_target;  // per vertex
     const float* pin_weight;   // per vertex; -1 = no pin
     const float* pin_relax;    // per vertex soft-pin relaxation
+    const int* vt_off;         // vertex -> incident triangles (triangle order)
+    const int* vt_tri;
+    const float* p_area;       // volume pressure: area share and rest scale per vertex
+    const float* p_rest;
     unsigned long long* counts;
     // self collision
     int4* vcell;            // cx, cy, cz, global bucket per vertex

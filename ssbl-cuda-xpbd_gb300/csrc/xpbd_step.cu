@@ -13,6 +13,7 @@
 // update as the reference's atomics, without float atomics, and therefore
 // deterministic.
 #include "xpbd_constraint.cuh"
+#include "xpbd_fields.cuh"
 #include "xpbd_solver.cuh"
 
 namespace xg {
@@ -343,13 +344,44 @@ __device__ __forceinline__ void bend_term(const Params& P, unsigned long long* c
     }
 }
 
+// Area-weighted normal of a vertex from its incident triangles in the
+// snapshot positions (abi41.cu:1213-1261; 1/sqrt in IEEE arithmetic).
+__device__ bool vertex_normal(const View& v, int i, F3* out) {
+    if (!v.vt_off) return false;
+    const int begin = __ldg(&v.vt_off[i]), end = __ldg(&v.vt_off[i + 1]);
+    if (end <= begin) return false;
+    F3 acc{0.0f, 0.0f, 0.0f};
+    for (int k = begin; k < end; ++k) {
+        const int t = __ldg(&v.vt_tri[k]);
+        if (t < 0 || t >= v.nT) continue;
+        const int4 tr = __ldg(&v.tris[t]);
+        if (tr.x < 0 || tr.y < 0 || tr.z < 0 || tr.x >= v.nV || tr.y >= v.nV || tr.z >= v.nV) continue;
+        const F3 p0 = f3(v.pos_in[tr.x]), p1 = f3(v.pos_in[tr.y]), p2 = f3(v.pos_in[tr.z]);
+        const F3 n = cross3(p1 - p0, p2 - p0);
+        const float l2 = dot3(n, n);
+        if (!isfinite(l2) || l2 <= 1.0e-10f) continue;
+        acc = acc + n * (1.0f / sqrtf(l2));
+    }
+    const float a2 = dot3(acc, acc);
+    if (!isfinite(a2) || a2 <= 1.0e-10f) return false;
+    *out = acc * (1.0f / sqrtf(a2));
+    return true;
+}
+
+// Integrate (abi41.cu:1869-1925): gravity, volume pressure along the vertex
+// normal, force fields, damping, pressure speed trims; fixed vertices return
+// to rest.  Reads the snapshot `pos_in` and writes `pos` (the same buffer
+// unless vertex normals are gathered).
 __global__ void __launch_bounds__(kThreads) k_predict(View v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nV) return;
     const Params& P = params_v(v, i);
-    if (!P.active) return;
+    const float4 p4 = v.pos_in[i];
+    if (!P.active) {
+        if (v.pos != v.pos_in) v.pos[i] = p4;
+        return;
+    }
     const float dt = P.sub_dt;
-    const float4 p4 = v.pos[i];
     const float inv_mass = __ldg(&v.inv_mass[i]);
     VState s;
     s.w = p4.w;
@@ -358,9 +390,36 @@ __global__ void __launch_bounds__(kThreads) k_predict(View v) {
         s.vel = F3{0.0f, 0.0f, 0.0f};
         s.p = f3(ld4(&v.rest[i]));
     } else {
-        const F3 accel = F3{P.gravity[0], P.gravity[1], P.gravity[2]} + F3{0.0f, 0.0f, 0.0f};
+        F3 normal{0.0f, 0.0f, 0.0f};
+        const bool has_normal = P.needs_normal && vertex_normal(v, i, &normal);
+        F3 accel = F3{P.gravity[0], P.gravity[1], P.gravity[2]} + F3{0.0f, 0.0f, 0.0f};
+        const bool pressure = P.pressure_on && has_normal;
+        const float area = pressure ? __ldg(&v.p_area[i]) : 0.0f;
+        if (pressure && isfinite(area) && area > 0.0f)
+            accel = accel + normal * (P.pressure_strength * P.pressure_accel_scale * area * inv_mass);
+        if (P.field_count > 0) {
+            F3 fa{0.0f, 0.0f, 0.0f};
+            const F3 vel0 = f3(v.vel[i]);
+            const int n = min(P.field_count, kMaxFields);
+            for (int k = 0; k < n; ++k) fa = fa + field_accel(P.fields[k], f3(p4), vel0, normal, has_normal);
+            accel = accel + cap_field_accel(fa);
+        }
         F3 vel = f3(v.vel[i]) + accel * dt;
         vel = vel * P.damping;
+        if (pressure) {
+            const float rest = __ldg(&v.p_rest[i]);
+            if (isfinite(rest) && rest > kEps && isfinite(dt) && dt > kEps) {
+                const float pa = fmaxf(P.pressure_strength, 0.0f) * fmaxf(P.pressure_accel_scale, 0.0f) * fmaxf(area, 0.0f) *
+                                 fmaxf(inv_mass, 0.0f);
+                const float max_delta = fmaxf(rest * fmaxf(P.pressure_impulse_rest_scale, 0.0f), 1.0e-7f);
+                const float delta = pa * dt * dt;
+                if (isfinite(delta) && delta > max_delta) vel = vel - normal * ((delta - max_delta) / dt);
+                const float vrest = fmaxf(rest, fmaxf(P.pressure_velocity_length_scale, 0.0f));
+                const float max_out = fmaxf(vrest * fmaxf(P.pressure_velocity_rest_scale, 0.0f) / dt, 1.0e-6f);
+                const float out = dot3(vel, normal);
+                if (isfinite(out) && out > max_out) vel = vel - normal * (out - max_out);
+            }
+        }
         s.vel = vel;
         s.p = f3(p4) + vel * dt;
     }

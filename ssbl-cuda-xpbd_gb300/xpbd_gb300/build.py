@@ -35,7 +35,7 @@ NVCC_FLAGS = [
     "-prec-sqrt=true",
     "-ftz=false",
     "-Xcompiler",
-    "-fPIC,-fvisibility=hidden",
+    "-fPIC,-fvisibility=hidden,-ffp-contract=off",
     "-I" + os.path.join(REPO_ROOT, "include"),
 ]
 

@@ -431,6 +431,17 @@ class NativeXpbdSolver:
             fi.update_static_triangles, fi.static_triangles, fi.static_triangle_count = 1, _fp(t), len(t) // 3
         self._check(self._lib.ssbl_update_frame_inputs(self._handle, ctypes.byref(fi)))
 
+    def update_force_fields(self, fields, unsupported: int = 0) -> None:
+        """Replace the force fields (a sequence of NativeForceField, at most
+        64) through ssbl_update_frame_inputs."""
+        arr = (NativeForceField * max(len(fields), 1))(*fields)
+        fi = NativeFrameInputs()
+        fi.update_force_fields = 1
+        fi.force_fields = ctypes.cast(arr, ctypes.POINTER(NativeForceField)) if len(fields) else None
+        fi.force_field_count = len(fields)
+        fi.unsupported_force_field_count = int(unsupported)
+        self._check(self._lib.ssbl_update_frame_inputs(self._handle, ctypes.byref(fi)))
+
     def step(self, substeps: int, iterations: int, diagnostics: bool = True, synchronize: bool = True) -> None:
         fetch = 1 if diagnostics else 0
         sync = 1 if (synchronize or diagnostics) else 0
@@ -571,6 +582,15 @@ class NativeXpbdBatch(NativeXpbdSolver):
         out = np.empty((n, 3), np.float32)
         self._check(self._lib.xpbd_gb300_batch_download_positions(self._handle, int(cloth), _fp(out), out.size))
         return out
+
+    def update_cloth_force_fields(self, cloth: int, fields, unsupported: int = 0) -> None:
+        arr = (NativeForceField * max(len(fields), 1))(*fields)
+        fi = NativeFrameInputs()
+        fi.update_force_fields = 1
+        fi.force_fields = ctypes.cast(arr, ctypes.POINTER(NativeForceField)) if len(fields) else None
+        fi.force_field_count = len(fields)
+        fi.unsupported_force_field_count = int(unsupported)
+        self._check(self._lib.xpbd_gb300_batch_update_frame_inputs(self._handle, int(cloth), ctypes.byref(fi)))
 
     def reset_cloth(self, cloth: int) -> None:
         self._check(self._lib.xpbd_gb300_batch_reset_cloth(self._handle, int(cloth)))
