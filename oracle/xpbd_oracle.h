@@ -9,7 +9,8 @@
  * Semantics restated (each function in xpbd_oracle.c cites its reference
  * lines): prediction, weighted pins, snapshot-Jacobi stretch, tethers, bends
  * by colour, ground / sphere / wall contacts with friction, the static SDF
- * (build, trilinear sampling, contact), self collision (vertex / triangle /
+ * (build, trilinear sampling, contact), dynamic triangle / particle
+ * colliders (hashes, unsigned and signed responses), self collision (vertex / triangle /
  * edge spatial hashes, neighbour table, VV / VT / EE responses, fast-mode
  * filters and overlap islands, averaging) and the velocity update, in the
  * reference's kernel order (abi41.cu:9165-9376).
@@ -40,6 +41,13 @@ int oracle_update_positions(OracleSolver* s, const float* positions, int max_flo
 int oracle_update_static_triangles(OracleSolver* s, const float* triangles, int count);
 /* Force fields (at most 64) applied by the prediction from the next step. */
 int oracle_update_force_fields(OracleSolver* s, const SsblXpbdForceField* fields, int count);
+/* Dynamic colliders, replaced on each call (count 0 clears): plain
+ * triangles (9 floats each, unsigned response), an indexed closed mesh
+ * (signed response) and particles with radii. */
+int oracle_update_dynamic_triangles(OracleSolver* s, const float* triangles, int count);
+int oracle_update_dynamic_indexed(OracleSolver* s, const float* vertices, int vertex_count, const int* indices, int count,
+                                  int topology_changed);
+int oracle_update_dynamic_particles(OracleSolver* s, const float* positions, const float* radii, int count);
 int oracle_step(OracleSolver* s, int substeps, int iterations);
 int oracle_download_positions(OracleSolver* s, float* out, int max_floats);
 int oracle_download_state(OracleSolver* s, float* pos3, float* prev3, float* vel3);
@@ -52,6 +60,9 @@ int oracle_build_self_structures(OracleSolver* s);
  * 12 static SDF (float), 13 counters (uint64 x 38).  Returns bytes or -1. */
 long long oracle_read_buffer(OracleSolver* s, int which, void* out, long long max_bytes);
 int oracle_hash_info(OracleSolver* s, int* out6);
+/* Dynamic colliders: triangles, large triangles, largest bucket, triangle
+ * hash built, particles, particle hash built. */
+int oracle_dynamic_info(OracleSolver* s, int* out6);
 /* Threads used by the parallel loops (OpenMP builds); returns the count. */
 int oracle_set_threads(int n);
 

@@ -41,12 +41,16 @@ def load():
         "oracle_update_positions": (ci, [vp, pf, ci]),
         "oracle_update_static_triangles": (ci, [vp, pf, ci]),
         "oracle_update_force_fields": (ci, [vp, vp, ci]),
+        "oracle_update_dynamic_triangles": (ci, [vp, pf, ci]),
+        "oracle_update_dynamic_indexed": (ci, [vp, pf, ci, pi, ci, ci]),
+        "oracle_update_dynamic_particles": (ci, [vp, pf, pf, ci]),
         "oracle_step": (ci, [vp, ci, ci]),
         "oracle_download_positions": (ci, [vp, pf, ci]),
         "oracle_download_state": (ci, [vp, pf, pf, pf]),
         "oracle_build_self_structures": (ci, [vp]),
         "oracle_read_buffer": (ctypes.c_longlong, [vp, ci, vp, ctypes.c_longlong]),
         "oracle_hash_info": (ci, [vp, pi]),
+        "oracle_dynamic_info": (ci, [vp, pi]),
         "oracle_set_threads": (ci, [ci]),
     }
     for name, (res, args) in sig.items():
@@ -131,6 +135,22 @@ class OracleSolver:
         n = len(fields)
         self._check(self._lib.oracle_update_force_fields(self._h, ctypes.addressof(fields) if n else None, n))
 
+    def update_dynamic_colliders(self, *, triangles=None, indexed=None, particles=None):
+        """Same arguments as NativeXpbdSolver.update_dynamic_colliders."""
+        if triangles is not None:
+            t = np.ascontiguousarray(np.asarray(triangles, np.float32).reshape(-1, 9))
+            self._check(self._lib.oracle_update_dynamic_triangles(self._h, _fp(t), len(t)))
+        if indexed is not None:
+            verts, idx, changed = indexed
+            v = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, 3))
+            ix = np.ascontiguousarray(np.asarray(idx, np.int32).reshape(-1, 3))
+            self._check(self._lib.oracle_update_dynamic_indexed(self._h, _fp(v), len(v), _ip(ix), len(ix), 1 if changed else 0))
+        if particles is not None:
+            pos, rad = particles
+            p = np.ascontiguousarray(np.asarray(pos, np.float32).reshape(-1, 3))
+            r = np.ascontiguousarray(np.asarray(rad, np.float32).reshape(-1))
+            self._check(self._lib.oracle_update_dynamic_particles(self._h, _fp(p), _fp(r), len(p)))
+
     def step(self, substeps, iterations):
         self._check(self._lib.oracle_step(self._h, int(substeps), int(iterations)))
 
@@ -158,6 +178,13 @@ class OracleSolver:
         out = np.zeros(6, np.int32)
         self._check(self._lib.oracle_hash_info(self._h, _ip(out)))
         return out
+
+
+    def dynamic_info(self):
+        out = np.zeros(6, np.int32)
+        self._check(self._lib.oracle_dynamic_info(self._h, _ip(out)))
+        return {"triangles": int(out[0]), "large": int(out[1]), "max_occupancy": int(out[2]), "tri_hashed": bool(out[3]),
+                "particles": int(out[4]), "par_hashed": bool(out[5])}
 
 
 def set_threads(n: int) -> int:

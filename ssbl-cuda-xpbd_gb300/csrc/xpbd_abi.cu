@@ -35,12 +35,16 @@ bool frame_inputs(Solver* S, int cloth, const SsblXpbdFrameInputs* in) {
     if (in->update_pin_targets && !upload_pins(S, cloth, in->pin_indices, in->pin_positions, in->pin_weights, in->pin_count))
         return false;
     if (in->update_runtime_colliders && !set_colliders(S, cloth, in->runtime_colliders)) return false;
-    if (in->update_dynamic_triangles && in->dynamic_triangle_count > 0)
-        return fail("dynamic triangle colliders are not supported by this build of the GB300 solver");
-    if (in->update_dynamic_indexed_triangles && in->dynamic_indexed_triangle_count > 0)
-        return fail("dynamic triangle colliders are not supported by this build of the GB300 solver");
-    if (in->update_dynamic_particles && in->dynamic_particle_count > 0)
-        return fail("dynamic particle colliders are not supported by this build of the GB300 solver");
+    if (in->update_dynamic_triangles && !upload_dynamic_triangles(S, cloth, in->dynamic_triangles, in->dynamic_triangle_count))
+        return false;
+    if (in->update_dynamic_indexed_triangles &&
+        !upload_dynamic_indexed(S, cloth, in->dynamic_triangle_vertices, in->dynamic_triangle_vertex_count,
+                                in->dynamic_triangle_indices, in->dynamic_indexed_triangle_count,
+                                in->dynamic_triangle_topology_changed != 0))
+        return false;
+    if (in->update_dynamic_particles &&
+        !upload_dynamic_particles(S, cloth, in->dynamic_particle_positions, in->dynamic_particle_radii, in->dynamic_particle_count))
+        return false;
     if (in->update_static_triangles && !upload_static(S, cloth, in->static_triangles, in->static_triangle_count)) return false;
     if (in->update_force_fields &&
         !upload_fields(S, cloth, in->force_fields, in->force_field_count, in->unsupported_force_field_count))
@@ -113,8 +117,7 @@ extern "C" SSBL_API int ssbl_update_dynamic_triangles(void* handle, const float*
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S) return fail("invalid dynamic triangle update") ? 1 : 0;
-    if (triangle_count > 0 && triangles) return fail("dynamic triangle colliders are not supported by this build of the GB300 solver") ? 1 : 0;
-    return 1;
+    return ok_or_zero(upload_dynamic_triangles(S, -1, triangles, triangle_count));
 }
 
 extern "C" SSBL_API int ssbl_update_frame_inputs(void* handle, const SsblXpbdFrameInputs* in) {

@@ -404,6 +404,7 @@ void free_solver(Solver* S) {
     for (Cloth& c : S->cl) {
         release_grid(S, c);
         dfree(c.fields_dev);
+        free_dynamic(c);
     }
     dfree(S->vt_off);
     dfree(S->vt_tri);
@@ -1101,6 +1102,7 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
         Params& P = S->hp[k];
         P.active = 1;
         P.sub_dt = c.dt;
+        P.frame_dt = c.dt;
         P.damping = c.damping;
         for (int a = 0; a < 3; ++a) P.gravity[a] = c.gravity[a];
         P.stretch_compliance = c.stretch_compliance;
@@ -1343,8 +1345,20 @@ int order_mode(bool need, bool plain) { return need ? (plain ? 2 : 1) : 0; }
 // iteration are fused into one pass; a pass starts at every stretch /
 // tether / Jacobi-bend gather and around the work that needs all vertices
 // (bends by colour, self collision).
+// Kinds of dynamic colliders present: bit 0 unsigned (plain triangles and
+// particles), bit 1 signed (indexed meshes, with their particles).
+int dynamic_kinds(const Solver* S) {
+    int kinds = 0;
+    for (int k = 0; k < S->K; ++k) {
+        if (!S->hp[k].dyn) continue;
+        kinds |= S->cl[k].dyn.h.signed_mode ? 2 : 1;
+    }
+    return kinds;
+}
+
 void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof) {
     const int nV = S->nV, nE = S->nE;
+    const int dyn = dynamic_kinds(S);
     bool analytic = false, sdf = false, normals = false;
     for (const Params& P : S->hp) {
         analytic |= P.use_ground || P.use_wall || P.use_sphere;
@@ -1480,6 +1494,13 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
             if (analytic) pending |= kPassAnalytic;
             if (sdf) pending |= kPassSdf;
             pending_last = base.last_it;
+            // unsigned dynamic colliders after the static contacts of the
+            // last iteration (abi41.cu:9234-9254)
+            if (last_it && (dyn & 1)) {
+                flush();
+                View dv = cur_view();
+                timed(kKDynamic, 1, [&] { launch_dynamic_collision(dv, nV, 0, S->stream); });
+            }
             const bool self_run = last_it && sp.run;
             if (self_run) {
                 flush();
@@ -1541,12 +1562,25 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                     timed(kKSelfApply, 1, [&] { self_apply(pv2, nV, S->stream); });
                 }
             }
+            // signed dynamic colliders after self collision (abi41.cu:9340-9345)
+            if (last_it && (dyn & 2)) {
+                flush();
+                View dv = cur_view();
+                timed(kKDynamic, 1, [&] { launch_dynamic_collision(dv, nV, 1, S->stream); });
+            }
             // final ratio caps after the contacts (abi41.cu:9346-9350, 7997-8027)
             if (pcg && final_c && hard) {
                 flush();
                 caps(0, 2, true);
                 caps(2, 3, false);
                 caps(1, 3, false);
+            }
+            // inside-only signed passes at the final constraints (abi41.cu:9351-9360)
+            if (final_c && (dyn & 2)) {
+                flush();
+                View dv = cur_view();
+                for (int pass = 0; pass < kSignedInsidePasses; ++pass)
+                    timed(kKDynamic, 1, [&] { launch_dynamic_collision(dv, nV, 2, S->stream); });
             }
             // Final pin polish whenever a contact stage ran: analytic
             // colliders, the SDF, or any last iteration (the dynamic
@@ -1571,7 +1605,7 @@ GraphEntry* ensure_graph(Solver* S, int substeps, int iterations) {
         sdf |= P.sdf_ready ? 1 : 0;
         normals |= P.needs_normal ? 1 : 0;
     }
-    const GraphKey key{substeps, iterations, analytic, sdf, normals};
+    const GraphKey key{substeps, iterations, analytic, sdf, normals, dynamic_kinds(S)};
     auto it = S->graphs.find(key);
     if (it == S->graphs.end()) {
         GraphEntry g;
@@ -1635,7 +1669,28 @@ bool fetch_counts(Solver* S, const FrameStats& st) {
     d.external_friction_corrections = (long long)c[kCntFrictionCorrections];
     d.self_candidate_count = (long long)c[kCntSelfCandidates];
     d.static_sdf_contact_count = (long long)c[kCntStaticSdfContacts];
-    d.candidate_count = (long long)(c[kCntSelfCandidates] + c[kCntStaticSdfContacts]);
+    d.candidate_count = (long long)(c[kCntDynParCandidates] + c[kCntDynTriCandidates] + c[kCntSelfCandidates] +
+                                   c[kCntStaticSdfContacts]);
+    // dynamic colliders (abi41.cu:8078-8117): the hashes are built at upload,
+    // so the per-build figures (large triangles, largest bucket) come from
+    // the host copies
+    d.dynamic_particle_candidate_count = (long long)c[kCntDynParCandidates];
+    d.dynamic_particle_contacts = (long long)c[kCntDynParContacts];
+    d.dynamic_particle_overflow = 0;
+    d.dynamic_triangle_candidate_count = (long long)c[kCntDynTriCandidates];
+    d.dynamic_triangle_bucket_overflow = (long long)c[kCntDynTriOverflow];
+    d.dynamic_triangle_aabb_reject_count = (long long)c[kCntDynTriAabbRejects];
+    long long large = 0, occupancy = 0;
+    for (const Cloth& C : S->cl) {
+        if (!C.dyn.h.tri_hashed || C.dyn.h.tri_count <= 0) continue;
+        large += C.dyn.large_count;
+        occupancy = std::max(occupancy, (long long)C.dyn.max_occupancy);
+    }
+    d.dynamic_triangle_large_primitive_count = large;
+    d.dynamic_triangle_max_bucket_occupancy = occupancy;
+    d.fast_triangle_pair_candidates = d.dynamic_triangle_candidate_count;
+    d.fast_triangle_pair_contacts = (long long)c[kCntTrianglePairs];
+    d.fast_triangle_pair_skipped_rest = d.dynamic_triangle_aabb_reject_count;
     d.abi41_lra_tack_count = (long long)c[kCntLraTacks];
     d.abi41_bending_wing_count = c[kCntBendingWings] > 0 ? (long long)c[kCntBendingWings] : (long long)wings;
     d.abi41_bending_texture_ready = wings > 0 ? 1 : 0;
@@ -1722,6 +1777,10 @@ bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int fo
     S->diag.finite_flag = 1;
     S->diag.force_field_count = ff;
     S->diag.unsupported_force_field_count = uff;
+    for (const Cloth& C : S->cl) {
+        S->diag.dynamic_triangle_count += C.dyn.h.tri_count;
+        S->diag.dynamic_particle_count += C.dyn.h.par_count;
+    }
     sdf_diagnostics(S);
     substeps = std::max(substeps, 1);
     iterations = std::max(iterations, 1);

@@ -90,14 +90,16 @@ enum KernelKind {
     kKCopy = 13,
     kKPcg = 14,          // CG solve (build + 8 iterations)
     kKStretchCaps = 15,  // averaged polish and colour-range ratio caps
-    kKinds = 16
+    kKDynamic = 16,      // dynamic-collider contacts
+    kKinds = 17
 };
 
 struct GraphKey {
     int substeps, iterations, analytic, sdf, normals;
+    int dyn;  // bit 0: some cloth has unsigned dynamic colliders, bit 1: signed
     bool operator<(const GraphKey& o) const {
-        return std::tie(substeps, iterations, analytic, sdf, normals) <
-               std::tie(o.substeps, o.iterations, o.analytic, o.sdf, o.normals);
+        return std::tie(substeps, iterations, analytic, sdf, normals, dyn) <
+               std::tie(o.substeps, o.iterations, o.analytic, o.sdf, o.normals, o.dyn);
     }
 };
 
@@ -138,6 +140,35 @@ struct SdfGrid {
     int refs = 0;
 };
 
+// Dynamic colliders of one cloth: device buffers (grown, never shrunk) and
+// the descriptor the kernels read.
+struct DynHost {
+    DynSet h{};                   // host copy of the descriptor
+    DynSet* dev = nullptr;        // device copy (Params.dyn)
+    float4* tris = nullptr;       // 3 rows per triangle
+    float4* verts = nullptr;      // indexed mesh vertices
+    int* idx = nullptr;           // indexed mesh triples
+    float4 *amin = nullptr, *amax = nullptr, *center = nullptr, *prev_center = nullptr;
+    float* radius = nullptr;
+    int4 *cmin = nullptr, *cmax = nullptr;
+    int* large = nullptr;
+    int *lflag = nullptr, *lpos = nullptr;  // large flags and their scan
+    int *tcount = nullptr, *tstart = nullptr, *tent = nullptr, *scan_tmp = nullptr;
+    int* small = nullptr;         // large count, max bucket occupancy
+    float4 *ppos = nullptr, *pprev = nullptr;
+    float* prad = nullptr;
+    int4* pcell = nullptr;
+    int *pcount = nullptr, *pstart = nullptr, *pent = nullptr, *pscan = nullptr;
+    int tris_cap = 0, verts_cap = 0, idx_cap = 0, bounds_cap = 0, tb_cap = 0, tent_cap = 0;
+    int par_cap = 0, pb_cap = 0;
+    int tri_upload_count = 0;     // triangles of the last upload (motion continuity)
+    int topology_count = -1;      // triangles of the uploaded index buffer
+    int par_upload_count = 0;
+    unsigned long long radius_signature = 0;
+    int large_count = 0;          // triangles spanning more than 64 cells
+    int max_occupancy = 0;        // largest bucket of the triangle hash
+};
+
 // Host-side state of one cloth of a solver.
 struct Cloth {
     SsblXpbdConfig cfg{};               // sanitised copy of the caller's config
@@ -159,6 +190,7 @@ struct Cloth {
     SsblXpbdForceField* fields_dev = nullptr;  // device copy of the cloth's force fields
     int fields_capacity = 0;
     bool pressure_on = false;
+    DynHost dyn;
 };
 
 struct Solver {
@@ -273,6 +305,13 @@ bool upload_positions(Solver* S, int cloth, const float* positions, int max_floa
 bool download_positions(Solver* S, int cloth, float* out, int max_floats);
 bool reset_cloths(Solver* S, int cloth);
 bool set_active(Solver* S, int cloth, bool active);
+// Dynamic colliders of a cloth (cloth < 0: every cloth), replaced on each
+// upload; defined in xpbd_dynamic.cu.
+bool upload_dynamic_triangles(Solver* S, int cloth, const float* tris, int count);
+bool upload_dynamic_indexed(Solver* S, int cloth, const float* verts, int vcount, const int* idx, int count,
+                            bool topology_changed);
+bool upload_dynamic_particles(Solver* S, int cloth, const float* pos, const float* radii, int count);
+void free_dynamic(Cloth& C);
 void sdf_diagnostics(Solver* S);
 
 // One frame: prepare parameters, launch (graph or direct), optionally fetch.

@@ -1568,6 +1568,10 @@ struct SelfLaunch {
     }
 };
 
+void scan_bucket_counts(int* counts, int* start, int n, int* block_sums, cudaStream_t s) {
+    if (n > 0) scan_counts(counts, start, n, block_sums, nullptr, s);
+}
+
 void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s) {
     if (V > 0) SelfLaunch::vhash(v, V, nb, s);
 }

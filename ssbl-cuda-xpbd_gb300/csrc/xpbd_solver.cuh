@@ -41,6 +41,10 @@ enum Counter {
     kCntExactImpulseContacts = 1,
     kCntEdgeEdgeContacts = 2,
     kCntHardFallbacks = 3,
+    kCntDynParCandidates = 4,
+    kCntDynParContacts = 5,
+    kCntDynParOverflow = 6,
+    kCntTrianglePairs = 7,
     kCntSelfCandidates = 9,
     kCntSelfOverflow = 10,
     kCntStaticSdfContacts = 11,
@@ -66,11 +70,52 @@ enum Counter {
     kCntClusterCount = 31,
     kCntClusterOwnedContacts = 32,
     kCntFrictionCorrections = 33,
+    kCntDynTriCandidates = 34,
+    kCntDynTriOverflow = 35,
+    kCntDynTriLarge = 36,
+    kCntDynTriAabbRejects = 37,
     kCntSlots = 38
 };
 
 // Scalar slots of the CG solve (same roles as abi41.cu:158-164).
 enum PcgSlot { kRedDAD = 0, kRedRZ = 1, kRedRZNext = 2, kRedStatus = 3, kRedInitialRZ = 4, kRedIterations = 5, kRedSlots = 8 };
+
+// Dynamic colliders of one cloth (moving triangle meshes and particles,
+// uploaded every frame): geometry, per-triangle bounds, and the spatial
+// hashes built at upload (bucket members in increasing id order).
+struct DynSet {
+    // triangles
+    int tri_count;
+    int signed_mode;      // 1 for indexed (closed, animated) meshes
+    int motion_valid;     // previous centres belong to the same triangles
+    int tri_hashed;       // hash built (>= 64 triangles), else brute force
+    float tri_cell;
+    int tri_buckets;
+    const float4* tris;   // 3 rows per triangle
+    const float4* amin;   // bounds per triangle
+    const float4* amax;
+    const float4* center;
+    const float4* prev_center;
+    const float* radius;
+    const int4* cmin;     // cell span per triangle (hash margin = collision margin)
+    const int4* cmax;
+    const int* tstart;    // [tri_buckets + 1]
+    const int* tent;
+    const int* large;     // triangles spanning more than 64 cells, increasing id
+    int large_count;
+    // particles
+    int par_count;
+    int par_motion_valid;
+    int par_hashed;       // hash built (>= 128 particles), else brute force
+    float par_cell;
+    int par_buckets;
+    const float4* par_pos;
+    const float4* par_prev;
+    const float* par_radius;
+    const int4* par_cellc;
+    const int* pstart;    // [par_buckets + 1]
+    const int* pent;      // first 16 members of a bucket are queried
+};
 
 // Parameters of one cloth.  A solver holds one or more cloths concatenated
 // in every per-vertex / per-constraint array (a batch); each kernel reads the
@@ -82,6 +127,7 @@ struct Params {
     int vstart, V, estart, E, tstart, T, B, L;
     int active;      // 0: every kernel skips this cloth's items
     float sub_dt;    // frame dt / substeps of the current step
+    float frame_dt;  // collider motion interval: cfg.dt when positive, else sub_dt
     float damping;
     float gravity[3];
     float stretch_compliance;
@@ -130,6 +176,7 @@ struct Params {
     float pressure_velocity_rest_scale;
     float pressure_velocity_length_scale;
     int needs_normal;                  // pressure or fields: vertex normals are gathered
+    const DynSet* dyn;                 // dynamic colliders (device), null when none
 };
 
 // Buffers of the hard-stretch CG solve and the averaged caps.
@@ -263,6 +310,15 @@ void launch_pin_scatter(const int* idx, const float4* target, const float* weigh
                         float4* pin_target, float* pin_weight, float* pin_relax, int nV, cudaStream_t s);
 void launch_pack_positions(float* dst, const float4* src, int V, cudaStream_t s);
 void launch_sdf_build(const View& v, int cloth, int voxels, cudaStream_t s);
+
+// dynamic colliders: collision passes over all vertices (cloths without
+// colliders of the kind skip); `which` 0 unsigned triangles + particles
+// (cloths in unsigned mode), 1 signed triangles + particles, 2 signed
+// triangles inside-only
+void launch_dynamic_collision(const View& v, int V, int which, cudaStream_t s);
+constexpr int kSignedInsidePasses = 6;  // inside-only passes at the final constraints (abi41.cu:80)
+// exclusive scan of bucket counts into starts (counts become cursors)
+void scan_bucket_counts(int* counts, int* start, int n, int* block_sums, cudaStream_t s);
 
 // self collision (bucket counts must be zeroed before each hash build; nb =
 // total buckets over all cloths)

@@ -325,6 +325,34 @@ def mesh_arrays(cloth: ClothData, static_triangles: np.ndarray) -> tuple[NativeM
     return m, keep
 
 
+def _dynamic_frame_inputs(triangles, indexed, particles):
+    fi = NativeFrameInputs()
+    keep = []
+    if triangles is not None:
+        t = np.ascontiguousarray(np.asarray(triangles, np.float32).reshape(-1, 9))
+        keep.append(t)
+        fi.update_dynamic_triangles, fi.dynamic_triangles, fi.dynamic_triangle_count = 1, _fp(t), len(t)
+    if indexed is not None:
+        verts, idx, changed = indexed
+        v = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, 3))
+        ix = np.ascontiguousarray(np.asarray(idx, np.int32).reshape(-1, 3))
+        keep += [v, ix]
+        fi.update_dynamic_indexed_triangles = 1
+        fi.dynamic_triangle_vertices, fi.dynamic_triangle_vertex_count = _fp(v), len(v)
+        fi.dynamic_triangle_indices, fi.dynamic_indexed_triangle_count = _ip(ix), len(ix)
+        fi.dynamic_triangle_topology_changed = 1 if changed else 0
+    if particles is not None:
+        pos, rad = particles
+        p = np.ascontiguousarray(np.asarray(pos, np.float32).reshape(-1, 3))
+        r = np.ascontiguousarray(np.asarray(rad, np.float32).reshape(-1))
+        if len(r) != len(p):
+            raise ValueError("one radius per dynamic particle")
+        keep += [p, r]
+        fi.update_dynamic_particles = 1
+        fi.dynamic_particle_positions, fi.dynamic_particle_radii, fi.dynamic_particle_count = _fp(p), _fp(r), len(p)
+    return fi, keep
+
+
 class NativeXpbdSolver:
     """One cloth on the GPU (the reference's NativeXpbdSolver interface)."""
 
@@ -442,6 +470,17 @@ class NativeXpbdSolver:
         fi.unsupported_force_field_count = int(unsupported)
         self._check(self._lib.ssbl_update_frame_inputs(self._handle, ctypes.byref(fi)))
 
+    def update_dynamic_colliders(self, *, triangles=None, indexed=None, particles=None) -> None:
+        """Replace dynamic colliders through ssbl_update_frame_inputs.
+
+        triangles: (T, 3, 3) plain triangles (unsigned response);
+        indexed: (vertices (N, 3), indices (T, 3), topology_changed) of a
+        closed mesh (signed response); particles: (positions (P, 3), radii
+        (P,)).  An empty array clears that kind; None leaves it unchanged."""
+        fi, keep = _dynamic_frame_inputs(triangles, indexed, particles)
+        self._check(self._lib.ssbl_update_frame_inputs(self._handle, ctypes.byref(fi)))
+        del keep
+
     def step(self, substeps: int, iterations: int, diagnostics: bool = True, synchronize: bool = True) -> None:
         fetch = 1 if diagnostics else 0
         sync = 1 if (synchronize or diagnostics) else 0
@@ -495,7 +534,7 @@ class NativeXpbdSolver:
 
     KERNEL_KINDS = ("predict", "stretch_pass", "vertex_pass", "bend_color", "vertex_hash", "triangle_hash",
                     "edge_hash", "neighbors", "vertex_vertex", "vertex_triangle", "edge_edge", "island",
-                    "self_apply", "copy", "pcg", "stretch_caps")
+                    "self_apply", "copy", "pcg", "stretch_caps", "dynamic")
 
     def profile_frame(self, substeps: int, iterations: int) -> dict:
         n = len(self.KERNEL_KINDS)
@@ -591,6 +630,12 @@ class NativeXpbdBatch(NativeXpbdSolver):
         fi.force_field_count = len(fields)
         fi.unsupported_force_field_count = int(unsupported)
         self._check(self._lib.xpbd_gb300_batch_update_frame_inputs(self._handle, int(cloth), ctypes.byref(fi)))
+
+    def update_cloth_dynamic_colliders(self, cloth: int, *, triangles=None, indexed=None, particles=None) -> None:
+        """update_dynamic_colliders for one cloth of the batch."""
+        fi, keep = _dynamic_frame_inputs(triangles, indexed, particles)
+        self._check(self._lib.xpbd_gb300_batch_update_frame_inputs(self._handle, int(cloth), ctypes.byref(fi)))
+        del keep
 
     def reset_cloth(self, cloth: int) -> None:
         self._check(self._lib.xpbd_gb300_batch_reset_cloth(self._handle, int(cloth)))

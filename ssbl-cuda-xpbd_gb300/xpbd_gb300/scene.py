@@ -371,6 +371,55 @@ def torus_triangles(center, major: float, minor: float, nu: int = 32, nv: int = 
     return pts[faces].astype(np.float32)
 
 
+def icosphere(center, radius: float, subdivisions: int = 2) -> tuple[np.ndarray, np.ndarray]:
+    """Closed, outward-wound sphere mesh: (vertices (N, 3) f32, indices
+    (20 * 4^subdivisions, 3) i32)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+             (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+             (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    v = np.array(verts) * radius + np.asarray(center, np.float64)
+    return v.astype(np.float32), np.array(faces, np.int32)
+
+
+def ramp_triangles(center, size: float, n: int, tilt: float) -> np.ndarray:
+    """Open n x n grid of 2 n^2 triangles (size m square, tilted by `tilt`
+    radians about x), (2 n^2, 3, 3) f32, facing +z."""
+    pos, tris = grid_mesh(n + 1, size, 0.0)
+    c, s = math.cos(tilt), math.sin(tilt)
+    y, z = pos[:, 1].astype(np.float64), pos[:, 2].astype(np.float64)
+    rot = np.stack([pos[:, 0], c * y - s * z, s * y + c * z], axis=1) + np.asarray(center, np.float64)
+    return rot[tris].astype(np.float32)
+
+
+def particle_stream(count: int, center, spread: float, radius: float, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """Seeded particles (positions (count, 3), radii (count,)) in a slab
+    of half-width `spread` around `center`, radii in [0.5, 1] x radius."""
+    rng = np.random.default_rng(seed)
+    p = np.asarray(center, np.float64) + rng.uniform(-spread, spread, size=(count, 3)) * np.array([1.0, 1.0, 0.25])
+    r = rng.uniform(0.5, 1.0, size=count) * radius
+    return p.astype(np.float32), r.astype(np.float32)
+
+
 # --------------------------------------------------------- named scenes ---
 @dataclass
 class Scene:
@@ -533,6 +582,17 @@ def serving_requests(rate: float = 200.0, duration: float = 60.0, seed: int = 0,
         frames = int(rng.integers(horizon[0], horizon[1] + 1))
         out.append(ClothRequest(cloth, opt, static, frames, 10, 2, len(out), t))
     return out
+
+
+def dynamic_scene(n: int = 32, frames: int = 60) -> Scene:
+    """Cloth for the dynamic colliders: an unpinned n x n grid (1 m) at
+    z = 0 with 2 mm thickness and 5 mm margin, friction 0.2, falling onto
+    colliders that the caller moves every frame."""
+    cloth = _unpinned_grid(n, 0.0)
+    opt = SolverOptions(dt=1.0 / 60.0, damping=0.99, stretch_compliance=1.0e-7, bend_compliance=1.0e-4,
+                        collision_margin=0.005, cloth_thickness=0.002, contact_friction=0.2, use_ground=True,
+                        ground_height=-1.0)
+    return Scene(f"dynamic-{n}", cloth, opt, np.empty((0, 3, 3), np.float32), 10, 2, frames, 1.0)
 
 
 def diff_scene(n: int = 64, frames: int = 60, stretch: float = 1.0e-7, bend: float = 1.0e-4) -> Scene:
