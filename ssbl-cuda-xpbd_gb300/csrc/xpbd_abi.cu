@@ -220,10 +220,13 @@ XG_EXPORT int xpbd_gb300_batch_cloth_range(void* handle, int cloth, int* out4) {
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || !out4 || cloth < 0 || cloth >= S->K) return fail("invalid cloth index") ? 1 : 0;
-    const Params& P = S->hp[cloth];
-    out4[0] = P.vstart;
+    // offsets in the caller's cloth order (the order of whole-handle transfers)
+    int estart = 0;
+    for (int k = 0; k < cloth; ++k) estart += S->hp[S->ext2int[k]].E;
+    const Params& P = S->hp[S->ext2int[cloth]];
+    out4[0] = S->ext_vstart[cloth];
     out4[1] = P.V;
-    out4[2] = P.estart;
+    out4[2] = estart;
     out4[3] = P.E;
     return 1;
 }
@@ -233,6 +236,7 @@ XG_EXPORT int xpbd_gb300_batch_update_pin_targets(void* handle, int cloth, const
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid cloth index") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(upload_pins(S, cloth, indices, positions, weights, count));
 }
 
@@ -240,6 +244,7 @@ XG_EXPORT int xpbd_gb300_batch_update_runtime_colliders(void* handle, int cloth,
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || !inputs || cloth < 0 || cloth >= S->K) return fail("invalid runtime collider update") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(set_colliders(S, cloth, *inputs));
 }
 
@@ -247,6 +252,7 @@ XG_EXPORT int xpbd_gb300_batch_update_static_triangles(void* handle, int cloth, 
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid static triangle update") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(upload_static(S, cloth, triangles, triangle_count));
 }
 
@@ -254,6 +260,7 @@ XG_EXPORT int xpbd_gb300_batch_update_frame_inputs(void* handle, int cloth, cons
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid frame input update") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(frame_inputs(S, cloth, in));
 }
 
@@ -261,6 +268,7 @@ XG_EXPORT int xpbd_gb300_batch_update_positions(void* handle, int cloth, const f
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid position upload") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(upload_positions(S, cloth, positions, max_floats));
 }
 
@@ -268,6 +276,7 @@ XG_EXPORT int xpbd_gb300_batch_download_positions(void* handle, int cloth, float
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid position download") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(download_positions(S, cloth, out, max_floats));
 }
 
@@ -275,6 +284,7 @@ XG_EXPORT int xpbd_gb300_batch_reset_cloth(void* handle, int cloth) {
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid cloth index") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(reset_cloths(S, cloth));
 }
 
@@ -282,6 +292,7 @@ XG_EXPORT int xpbd_gb300_batch_set_active(void* handle, int cloth, int active) {
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid cloth index") ? 1 : 0;
+    cloth = S->ext2int[cloth];
     return ok_or_zero(set_active(S, cloth, active != 0));
 }
 
@@ -300,21 +311,22 @@ XG_EXPORT int xpbd_gb300_build_self_structures(void* handle) {
         if (!P.self_on) continue;
         sv.hashed_v |= P.vhash != 0;
         sv.brute_v |= P.vhash == 0;
+        sv.add_cloth(P, S->cl[k].fast);
     }
     const View v = S->view();
     if (S->nVB > 0) {
         cudaMemsetAsync(S->vb_count, 0, sizeof(int) * S->nVB, S->stream);
-        self_build_vertex_hash(v, S->nV, S->nVB, S->stream);
+        self_build_vertex_hash(v, sv, S->nVB, S->stream);
     }
     if (S->nTB > 0) {
         cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, S->stream);
-        self_build_triangle_hash(v, S->nT, S->nTB, 1, S->stream);
+        self_build_triangle_hash(v, sv, S->nTB, 1, S->stream);
     }
     if (S->nEB > 0) {
         cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, S->stream);
-        self_build_edge_hash(v, S->nE, S->nEB, 1, S->stream);
+        self_build_edge_hash(v, sv, S->nEB, 1, S->stream);
     }
-    self_neighbors(v, S->nV, 0, sv, S->stream);
+    self_neighbors(v, 0, sv, S->stream);
     return (cuda_ok(cudaGetLastError(), "build self structures") && cuda_ok(cudaStreamSynchronize(S->stream), "build self structures")) ? 1 : 0;
 }
 

@@ -647,6 +647,24 @@ Range cloth_range(const Solver* S, int cloth) {
 
 bool valid_cloth(const Solver* S, int cloth) { return S && cloth < S->K; }
 
+// Vertex index over the caller-ordered concatenation -> stored index (-1
+// outside).
+int internal_vertex(const Solver* S, int i) {
+    if (i < 0 || i >= S->ext_vstart[S->K]) return -1;
+    const int k = (int)(std::upper_bound(S->ext_vstart.begin(), S->ext_vstart.end(), i) - S->ext_vstart.begin()) - 1;
+    return S->hp[S->ext2int[k]].vstart + (i - S->ext_vstart[k]);
+}
+
+// Stored vertex index -> index over the caller-ordered concatenation.
+int external_vertex(const Solver* S, int i) {
+    int lo = 0, hi = S->K - 1;  // last cloth whose vstart <= i
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (S->hp[mid].vstart <= i) lo = mid; else hi = mid - 1;
+    }
+    return S->ext_vstart[S->int2ext[lo]] + (i - S->hp[lo].vstart);
+}
+
 }  // namespace
 
 // Static SDF fields of the diagnostics block (abi41.cu:6105-6121), summed
@@ -660,14 +678,16 @@ void sdf_diagnostics(Solver* S) {
     d.static_sdf_grid_x = d.static_sdf_grid_y = d.static_sdf_grid_z = 0;
     d.static_sdf_voxel_count = 0;
     bool shaped = false;
-    for (int k = 0; k < S->K; ++k) {
+    for (int e = 0; e < S->K; ++e) {  // the caller's cloth order
+        const int k = S->ext2int.empty() ? e : S->ext2int[e];
+        const bool last = e == S->K - 1;
         const Params& P = S->hp[k];
         const Cloth& C = S->cl[k];
         d.static_triangle_count += P.static_tri_count;
         d.static_sdf_rebuild_count += C.sdf_rebuilds;
         d.static_sdf_unsigned_fallback_count += C.sdf_unsigned;
         d.static_sdf_build_ms += C.sdf_build_ms;
-        if (!shaped && (P.sdf_ready || k == S->K - 1)) {
+        if (!shaped && (P.sdf_ready || last)) {
             d.static_sdf_grid_x = P.sdf_dim[0];
             d.static_sdf_grid_y = P.sdf_dim[1];
             d.static_sdf_grid_z = P.sdf_dim[2];
@@ -676,9 +696,10 @@ void sdf_diagnostics(Solver* S) {
         d.static_sdf_voxel_count += P.sdf_ready ? (long long)P.sdf_dim[0] * P.sdf_dim[1] * P.sdf_dim[2] : 0;
     }
     if (!shaped && S->K > 0) {
-        d.static_sdf_grid_x = S->hp[0].sdf_dim[0];
-        d.static_sdf_grid_y = S->hp[0].sdf_dim[1];
-        d.static_sdf_grid_z = S->hp[0].sdf_dim[2];
+        const Params& P0 = S->hp[S->ext2int.empty() ? 0 : S->ext2int[0]];
+        d.static_sdf_grid_x = P0.sdf_dim[0];
+        d.static_sdf_grid_y = P0.sdf_dim[1];
+        d.static_sdf_grid_z = P0.sdf_dim[2];
     }
 }
 
@@ -725,8 +746,8 @@ bool upload_pins(Solver* S, int cloth, const int* indices, const float* position
         }
     }
     for (int k = 0; k < count; ++k) {
-        const int i = r.lo + indices[k];
-        if (indices[k] < 0 || i >= r.hi) continue;
+        const int i = (cloth < 0 && S->permuted) ? internal_vertex(S, indices[k]) : r.lo + indices[k];
+        if (indices[k] < 0 || i < r.lo || i >= r.hi) continue;
         S->h_pin_weight[i] = weights ? weights[k] : 1.0f;
         S->h_pin_target[i] = make_float4(positions[k * 3 + 0], positions[k * 3 + 1], positions[k * 3 + 2], 0.0f);
         mark(i);
@@ -825,8 +846,11 @@ bool upload_positions(Solver* S, int cloth, const float* positions, int max_floa
     const int n = r.hi - r.lo;
     if (max_floats < n * 3) return fail("invalid position upload");
     std::vector<float4> p4(n);
-    for (int i = 0; i < n; ++i)
-        p4[i] = make_float4(positions[i * 3], positions[i * 3 + 1], positions[i * 3 + 2], S->h_w[r.lo + i]);
+    for (int i = 0; i < n; ++i) {
+        // a whole-handle upload lists the cloths in the caller's order
+        const int src = (cloth < 0 && S->permuted) ? external_vertex(S, i) : i;
+        p4[i] = make_float4(positions[src * 3], positions[src * 3 + 1], positions[src * 3 + 2], S->h_w[r.lo + i]);
+    }
     return dupload(S->pos[0] + r.lo, p4.data(), n, S->stream, "upload positions") &&
            dupload(S->prev + r.lo, p4.data(), n, S->stream, "upload previous positions") &&
            cuda_ok(cudaStreamSynchronize(S->stream), "upload positions");
@@ -838,6 +862,18 @@ bool download_positions(Solver* S, int cloth, float* out, int max_floats) {
     const int n = r.hi - r.lo;
     if (max_floats < n * 3) return fail("invalid position download");
     launch_pack_positions(S->pack + 3ll * r.lo, S->pos[0] + r.lo, n, S->stream);
+    if (cloth < 0 && S->permuted) {
+        // whole handle: each cloth's block goes to its place in the caller's order
+        if (!cuda_ok(cudaGetLastError(), "pack positions")) return false;
+        for (int k = 0; k < S->K; ++k) {
+            const Params& P = S->hp[S->ext2int[k]];
+            if (P.V > 0 && !cuda_ok(cudaMemcpyAsync(out + 3ll * S->ext_vstart[k], S->pack + 3ll * P.vstart, sizeof(float) * 3 * P.V,
+                                                    cudaMemcpyDeviceToHost, S->stream),
+                                    "download ABI41 positions"))
+                return false;
+        }
+        return cuda_ok(cudaStreamSynchronize(S->stream), "download ABI41 positions");
+    }
     return cuda_ok(cudaGetLastError(), "pack positions") &&
            cuda_ok(cudaMemcpyAsync(out, S->pack + 3ll * r.lo, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, S->stream),
                    "download ABI41 positions") &&
@@ -871,8 +907,8 @@ bool set_active(Solver* S, int cloth, bool active) {
 
 // ------------------------------------------------------------ creation --
 
-Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes, int K) {
-    if (!configs || !meshes || K < 1) {
+Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_meshes, int K) {
+    if (!in_configs || !in_meshes || K < 1) {
         fail("invalid ABI41 solver create request");
         return nullptr;
     }
@@ -881,8 +917,30 @@ Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes,
     S->K = K;
     S->cl.resize(K);
     S->hp.assign(K, Params{});
+    // internal order: grouped by self-collision mode, stable within a group
+    S->int2ext.resize(K);
+    for (int k = 0; k < K; ++k) S->int2ext[k] = k;
+    auto mode_key = [&](int k) {
+        const SsblXpbdConfig& c = in_configs[k];
+        if (!c.self_collision) return 0;
+        return c.self_collision_mode == 1 ? 1 : 2;
+    };
+    std::stable_sort(S->int2ext.begin(), S->int2ext.end(), [&](int a, int b) { return mode_key(a) < mode_key(b); });
+    S->ext2int.resize(K);
+    S->ext_vstart.assign(K + 1, 0);
+    std::vector<SsblXpbdConfig> cfg_sorted(K);
+    std::vector<SsblXpbdMesh> mesh_sorted(K);
+    for (int k = 0; k < K; ++k) {
+        S->ext2int[S->int2ext[k]] = k;
+        S->permuted |= S->int2ext[k] != k;
+        cfg_sorted[k] = in_configs[S->int2ext[k]];
+        mesh_sorted[k] = in_meshes[S->int2ext[k]];
+    }
+    for (int k = 0; k < K; ++k) S->ext_vstart[k + 1] = S->ext_vstart[k] + std::max(in_configs[k].vertex_count, 0);
+    const SsblXpbdConfig* configs = cfg_sorted.data();
+    const SsblXpbdMesh* meshes = mesh_sorted.data();
     auto bail = [&](int k, const std::string& msg) -> Solver* {
-        if (!msg.empty()) fail(K > 1 ? "batch cloth " + std::to_string(k) + ": " + msg : msg);
+        if (!msg.empty()) fail(K > 1 ? "batch cloth " + std::to_string(S->int2ext[k]) + ": " + msg : msg);
         free_solver(S);
         return nullptr;
     };
@@ -1319,6 +1377,7 @@ SelfPlan plan_self(const Solver* S, int s, int substeps) {
         p.any_e |= P.E > 0;
         p.sv.fast |= C.fast;
         p.sv.strict |= !C.fast;
+        p.sv.add_cloth(P, C.fast);
         p.sv.hashed_v |= P.vhash != 0;
         p.sv.brute_v |= P.vhash == 0;
         p.sv.hashed_t |= P.thash != 0 && P.T > 0;
@@ -1531,21 +1590,21 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 if (sp.vhash)
                     timed(kKVertexHash, 6, [&] {
                         cudaMemsetAsync(S->vb_count, 0, sizeof(int) * S->nVB, lane_stream(0));
-                        self_build_vertex_hash(hv[0], nV, S->nVB, lane_stream(0));
+                        self_build_vertex_hash(hv[0], sp.sv, S->nVB, lane_stream(0));
                     });
                 if (sp.thash)
                     timed(kKTriangleHash, 6, [&] {
                         cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, lane_stream(1));
-                        self_build_triangle_hash(hv[1], S->nT, S->nTB, order_mode(sp.t_order, sp.t_plain), lane_stream(1));
+                        self_build_triangle_hash(hv[1], sp.sv, S->nTB, order_mode(sp.t_order, sp.t_plain), lane_stream(1));
                     });
                 if (sp.ehash)
                     timed(kKEdgeHash, 6, [&] {
                         cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, lane_stream(2));
-                        self_build_edge_hash(hv[2], nE, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
+                        self_build_edge_hash(hv[2], sp.sv, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
                     });
                 join();
                 if (sp.sv.fast) {
-                    timed(kKNeighbors, 1, [&] { self_neighbors(sv, nV, 1, sp.sv, S->stream); });
+                    timed(kKNeighbors, 1, [&] { self_neighbors(sv, 1, sp.sv, S->stream); });
                     st->cache_hits += sp.hits;
                     st->cache_misses += sp.misses;
                 }
@@ -1553,13 +1612,13 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                     View pv2 = sv;
                     pv2.pass = pass;
                     fork();
-                    if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, nV, 2, sp.sv, lane_stream(0)); });
-                    timed(kKVertexVertex, 1, [&] { self_vv(pv2, nV, sp.sv, lane_stream(0)); });
-                    if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, nV, sp.sv, lane_stream(1)); });
-                    if (sp.island) timed(kKIsland, 1, [&] { self_island(pv2, nV, lane_stream(1)); });
-                    if (sp.any_e) timed(kKEdgeEdge, 1, [&] { self_ee(pv2, nE, sp.sv, lane_stream(2)); });
+                    if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, 2, sp.sv, lane_stream(0)); });
+                    timed(kKVertexVertex, 1, [&] { self_vv(pv2, sp.sv, lane_stream(0)); });
+                    if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, sp.sv, lane_stream(1)); });
+                    if (sp.island) timed(kKIsland, 1, [&] { self_island(pv2, sp.sv, lane_stream(1)); });
+                    if (sp.any_e) timed(kKEdgeEdge, 1, [&] { self_ee(pv2, sp.sv, lane_stream(2)); });
                     join();
-                    timed(kKSelfApply, 1, [&] { self_apply(pv2, nV, S->stream); });
+                    timed(kKSelfApply, 1, [&] { self_apply(pv2, sp.sv, S->stream); });
                 }
             }
             // signed dynamic colliders after self collision (abi41.cu:9340-9345)

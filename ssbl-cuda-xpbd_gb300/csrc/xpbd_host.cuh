@@ -195,6 +195,13 @@ struct Cloth {
 
 struct Solver {
     int K = 0;
+    // Cloths are stored grouped by self-collision mode (none, fast, strict;
+    // caller order within a group) so that each mode-specific kernel covers
+    // contiguous items.  The batch entry points take the caller's cloth
+    // index (ext2int maps it); concatenated whole-handle transfers use the
+    // caller's order (ext_vstart: vertex offsets in that order).
+    bool permuted = false;
+    std::vector<int> ext2int, int2ext, ext_vstart;
     std::vector<Cloth> cl;
     std::vector<Params> hp;     // one per cloth
     Params* dp = nullptr;

@@ -170,8 +170,8 @@ __device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok,
 }
 
 __global__ void k_vhash_count(View v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nV) return;
+    const int i = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= v.hi) return;
     const Params& P = params_v(v, i);
     if (!P.vhash || !self_scheduled(P, v)) return;
     const float4 p = v.pos[i];
@@ -182,8 +182,8 @@ __global__ void k_vhash_count(View v) {
 }
 
 __global__ void k_vhash_scatter(View v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nV) return;
+    const int i = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= v.hi) return;
     const Params& P = params_v(v, i);
     if (!P.vhash || !self_scheduled(P, v)) return;
     const int b = v.vcell[i].w;
@@ -200,10 +200,9 @@ constexpr int kPrimLanes = 8;
 
 template <bool kTri>
 __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
-    const int n = kTri ? v.nT : v.nE;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = (int)(t / kPrimLanes), r0 = (int)(t % kPrimLanes);
-    if (k >= n) return;
+    const int k = v.lo + (int)(t / kPrimLanes), r0 = (int)(t % kPrimLanes);
+    if (k >= v.hi) return;
     const Params& P = kTri ? params_t(v, k) : params_e(v, k);
     if (!(kTri ? P.thash : P.ehash) || !self_scheduled(P, v)) return;
     bool ok = false;
@@ -348,10 +347,10 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
                                                           int mode) {
     const int warp = warp_global_id();
     const int lane = threadIdx.x & 31;
-    if ((long long)warp * 32 >= nbuckets) return;
-    const int b = warp * 32 + lane;
+    if (v.lo + (long long)warp * 32 >= v.hi || v.hi > nbuckets) return;
+    const int b = v.lo + warp * 32 + lane;
     int s = 0, n = 0;
-    if (b < nbuckets) {
+    if (b < v.hi) {
         s = start[b];
         n = start[b + 1] - s;
     }
@@ -431,8 +430,8 @@ __device__ bool vv_valid(const View& v, int src, int other, float target, float 
 // Neighbour table without the vertex hash (cloths under 128 vertices): every
 // vertex of the cloth in index order (abi41.cu:4790-4814).
 __global__ void k_neighbors_brute(View v, int mode) {
-    const int src = blockIdx.x * blockDim.x + threadIdx.x;
-    if (src >= v.nV) return;
+    const int src = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (src >= v.hi) return;
     const Params& P = params_v(v, src);
     if (P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
     const float target = contact_radius(P);
@@ -455,8 +454,8 @@ __global__ void k_neighbors_brute(View v, int mode) {
 // else an overlap push; responses clamped to 0.35 thickness
 // (abi41.cu:4816-4951).
 __global__ void __launch_bounds__(kThreads) k_vv(View v) {
-    const int src = blockIdx.x * blockDim.x + threadIdx.x;
-    if (src >= v.nV) return;
+    const int src = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (src >= v.hi) return;
     const Params& P = params_v(v, src);
     if (!fast_mode(P) || !self_scheduled(P, v)) return;
     if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
@@ -638,8 +637,8 @@ __device__ int neighbor_budget(const Params& P) {
 // Vertex-triangle query over the vertex's own cell bucket only
 // (abi41.cu:5109-5182).
 __global__ void __launch_bounds__(kThreads) k_vt_hash(View v) {
-    const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vertex >= v.nV) return;
+    const int vertex = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
     if (!P.thash || !fast_mode(P) || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
@@ -665,8 +664,8 @@ __global__ void __launch_bounds__(kThreads) k_vt_hash(View v) {
 // Vertex-triangle query without the triangle hash (cloths under 64
 // triangles): every triangle of the cloth (abi41.cu:5184-5224).
 __global__ void __launch_bounds__(kThreads) k_vt_brute(View v) {
-    const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vertex >= v.nV) return;
+    const int vertex = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
     if (P.thash || P.T <= 0 || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
@@ -764,8 +763,8 @@ __device__ bool ee_pair(const View& v, const Params& P, int ia, int ib, float ta
 // Edge-edge query without the edge hash (cloths under 64 edges): later edges
 // of the cloth (abi41.cu:5804-5844).
 __global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= v.nE) return;
+    const int e = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (e >= v.hi) return;
     const Params& P = params_e(v, e);
     if (P.ehash || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
@@ -807,9 +806,9 @@ __device__ __forceinline__ long long warp_sum64(long long v) {
 // VV neighbour table: lane l < 27 scans cell (dz, dy, dx) = (l/9-1, l/3%3-1,
 // l%3-1), the reference's nested-loop order (abi41.cu:4756-4781).
 __global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v, int mode) {
-    const int src = warp_global_id();
+    const int src = v.lo + warp_global_id();
     const int lane = threadIdx.x & 31;
-    if (src >= v.nV) return;
+    if (src >= v.hi) return;
     const Params& P = params_v(v, src);
     if (!P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
     const float target = contact_radius(P);
@@ -845,9 +844,9 @@ __global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v, int mode) {
 
 // VV responses (strict): lane n handles neighbour n of the source vertex.
 __global__ void __launch_bounds__(kThreads) k_vv_warp(View v) {
-    const int src = warp_global_id();
+    const int src = v.lo + warp_global_id();
     const int lane = threadIdx.x & 31;
-    if (src >= v.nV) return;
+    if (src >= v.hi) return;
     const Params& P = params_v(v, src);
     if (fast_mode(P) || !self_scheduled(P, v)) return;
     if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
@@ -1125,9 +1124,9 @@ __device__ __forceinline__ int group_item() {
 
 // Strict VT: the vertex's own cell bucket (abi41.cu:5129-5143).
 __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
-    const int vertex = group_item();
+    const int vertex = v.lo + group_item();
     const int gl = threadIdx.x & (kQueryLanes - 1);
-    if (vertex >= v.nV) return;
+    if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
     if (!P.thash || fast_mode(P) || !self_scheduled(P, v)) return;
     const float target = contact_radius(P);
@@ -1155,9 +1154,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
 
 // Strict EE: the bucket of the edge midpoint's cell (abi41.cu:5724-5758).
 __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
-    const int e = group_item();
+    const int e = v.lo + group_item();
     const int gl = threadIdx.x & (kQueryLanes - 1);
-    if (e >= v.nE) return;
+    if (e >= v.hi) return;
     const Params& P = params_e(v, e);
     if (!P.ehash || fast_mode(P) || !self_scheduled(P, v)) return;
     const int2 ed = __ldg(&v.edges[e]);
@@ -1266,13 +1265,13 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
 // carries the accepted keys in registers (lane g holds keys g and g + 8).
 // Counters are summed per warp and added once at the end.
 __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
-    const int e = group_item();
+    const int e = v.lo + group_item();
     const int lane = threadIdx.x & 31;
     const int gl = lane & (kQueryLanes - 1);
     const int gbase = lane & ~(kQueryLanes - 1);
     const unsigned gm = group_mask();
     int c_seen = 0, c_dup = 0, c_rest = 0, c_own = 0, c_acc = 0, c_contact = 0;
-    bool run = e < v.nE;
+    bool run = e < v.hi;
     const Params* P = nullptr;
     if (run) {
         P = &params_e(v, e);
@@ -1396,8 +1395,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
 // Fast mode, final pass: aggregate push for a vertex buried in >= 3 nearby
 // triangles of the 27-cell neighbourhood (abi41.cu:5226-5439).
 __global__ void __launch_bounds__(kThreads) k_island(View v) {
-    const int vertex = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vertex >= v.nV) return;
+    const int vertex = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
     if (!fast_mode(P) || !P.thash || P.T <= 0 || !self_scheduled(P, v) || v.pass != P.self_passes - 1) return;
     if (!(__ldg(&v.inv_mass[vertex]) > 0.0f)) return;
@@ -1526,8 +1525,8 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
 // Average the accumulated pushes, clamp to 0.35 r, apply with a 0.55 prev
 // shift, and clear the accumulators for the next pass (abi41.cu:4953-4988).
 __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nV) return;
+    const int i = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= v.hi) return;
     const Params& P = params_v(v, i);
     if (!self_scheduled(P, v)) return;
     const Acc4 a = v.acc[i];
@@ -1550,65 +1549,87 @@ __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
 inline int warp_blocks(long long items) { return (int)((items * 32 + kThreads - 1) / kThreads); }
 inline int group_blocks(long long items) { return (int)((items * kQueryLanes + kThreads - 1) / kThreads); }
 
-struct SelfLaunch {
-    static void vhash(const View& v, int V, int nb, cudaStream_t s) {
-        k_vhash_count<<<blocks_for(V), kThreads, 0, s>>>(v);
-        scan_counts(v.vb_count, v.vb_start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
-        k_vhash_scatter<<<blocks_for(V), kThreads, 0, s>>>(v);
-        k_bucket_sort<<<warp_blocks((nb + 31) / 32), kThreads, 0, s>>>(v, v.vb_start, v.vb_ent, nb, 0, 1);
-    }
-    template <bool kTri>
-    static void phash(const View& v, int n, int* count, int* start, int* ent, int nb, int order, cudaStream_t s) {
-        const long long threads = (long long)n * kPrimLanes;
-        const int blocks = (int)((threads + kThreads - 1) / kThreads);
-        k_prim_hash<kTri><<<blocks, kThreads, 0, s>>>(v, false);
-        scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
-        k_prim_hash<kTri><<<blocks, kThreads, 0, s>>>(v, true);
-        k_bucket_sort<<<warp_blocks((nb + 31) / 32), kThreads, 0, s>>>(v, start, ent, nb, kTri ? 1 : 2, order);
-    }
-};
+namespace {
+
+View ranged(const View& v, const ItemRange& r) {
+    View out = v;
+    out.lo = r.lo;
+    out.hi = r.hi;
+    return out;
+}
+
+void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange& buckets, int* count, int* start, int* ent,
+               int nb, int order, cudaStream_t s) {
+    if (items.size() == 0) return;
+    const View iv = ranged(v, items);
+    const long long threads = (long long)items.size() * kPrimLanes;
+    const int blocks = (int)((threads + kThreads - 1) / kThreads);
+    if (tri)
+        k_prim_hash<true><<<blocks, kThreads, 0, s>>>(iv, false);
+    else
+        k_prim_hash<false><<<blocks, kThreads, 0, s>>>(iv, false);
+    scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
+    if (tri)
+        k_prim_hash<true><<<blocks, kThreads, 0, s>>>(iv, true);
+    else
+        k_prim_hash<false><<<blocks, kThreads, 0, s>>>(iv, true);
+    if (buckets.size() > 0)
+        k_bucket_sort<<<warp_blocks((buckets.size() + 31) / 32), kThreads, 0, s>>>(ranged(v, buckets), start, ent, nb,
+                                                                                  tri ? 1 : 2, order);
+}
+
+}  // namespace
 
 void scan_bucket_counts(int* counts, int* start, int n, int* block_sums, cudaStream_t s) {
     if (n > 0) scan_counts(counts, start, n, block_sums, nullptr, s);
 }
 
-void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s) {
-    if (V > 0) SelfLaunch::vhash(v, V, nb, s);
+void self_build_vertex_hash(const View& v, const SelfVariants& sv, int nb, cudaStream_t s) {
+    const ItemRange& r = sv.v_all;
+    if (r.size() == 0) return;
+    const View iv = ranged(v, r);
+    k_vhash_count<<<blocks_for(r.size()), kThreads, 0, s>>>(iv);
+    scan_counts(v.vb_count, v.vb_start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
+    k_vhash_scatter<<<blocks_for(r.size()), kThreads, 0, s>>>(iv);
+    if (sv.vb.size() > 0)
+        k_bucket_sort<<<warp_blocks((sv.vb.size() + 31) / 32), kThreads, 0, s>>>(ranged(v, sv.vb), v.vb_start, v.vb_ent, nb, 0, 1);
 }
-void self_build_triangle_hash(const View& v, int T, int nb, int order, cudaStream_t s) {
-    if (T > 0) SelfLaunch::phash<true>(v, T, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
+void self_build_triangle_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
+    prim_hash(v, true, sv.t_all, sv.tb, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
 }
-void self_build_edge_hash(const View& v, int E, int nb, int order, cudaStream_t s) {
-    if (E > 0) SelfLaunch::phash<false>(v, E, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
+void self_build_edge_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
+    prim_hash(v, false, sv.e_all, sv.eb, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
 }
 
-void self_neighbors(const View& v, int V, int mode, const SelfVariants& sv, cudaStream_t s) {
-    if (V <= 0) return;
-    if (sv.hashed_v) k_neighbors_warp<<<warp_blocks(V), kThreads, 0, s>>>(v, mode);
-    if (sv.brute_v) k_neighbors_brute<<<blocks_for(V), kThreads, 0, s>>>(v, mode);
+void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_t s) {
+    const ItemRange& r = mode == 1 ? sv.v_fast : (mode == 2 ? sv.v_strict : sv.v_all);
+    if (r.size() == 0) return;
+    if (sv.hashed_v) k_neighbors_warp<<<warp_blocks(r.size()), kThreads, 0, s>>>(ranged(v, r), mode);
+    if (sv.brute_v) k_neighbors_brute<<<blocks_for(r.size()), kThreads, 0, s>>>(ranged(v, r), mode);
 }
-void self_vv(const View& v, int V, const SelfVariants& sv, cudaStream_t s) {
-    if (V <= 0) return;
-    if (sv.strict) k_vv_warp<<<warp_blocks(V), kThreads, 0, s>>>(v);
-    if (sv.fast) k_vv<<<blocks_for(V), kThreads, 0, s>>>(v);
+void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    if (sv.strict && sv.v_strict.size() > 0) k_vv_warp<<<warp_blocks(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
+    if (sv.fast && sv.v_fast.size() > 0) k_vv<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
 }
-void self_vt(const View& v, int V, const SelfVariants& sv, cudaStream_t s) {
-    if (V <= 0) return;
-    if (sv.hashed_t && sv.strict) k_vt_warp<<<group_blocks(V), kThreads, 0, s>>>(v);
-    if (sv.hashed_t && sv.fast) k_vt_hash<<<blocks_for(V), kThreads, 0, s>>>(v);
-    if (sv.brute_t) k_vt_brute<<<blocks_for(V), kThreads, 0, s>>>(v);
+void self_vt(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    if (sv.hashed_t && sv.strict && sv.v_strict.size() > 0)
+        k_vt_warp<<<group_blocks(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
+    if (sv.hashed_t && sv.fast && sv.v_fast.size() > 0)
+        k_vt_hash<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
+    if (sv.brute_t && sv.v_all.size() > 0) k_vt_brute<<<blocks_for(sv.v_all.size()), kThreads, 0, s>>>(ranged(v, sv.v_all));
 }
-void self_ee(const View& v, int E, const SelfVariants& sv, cudaStream_t s) {
-    if (E <= 0) return;
-    if (sv.hashed_e && sv.strict) k_ee_warp<<<group_blocks(E), kThreads, 0, s>>>(v);
-    if (sv.hashed_e && sv.fast) k_ee_fast<<<group_blocks(E), kThreads, 0, s>>>(v);
-    if (sv.brute_e) k_ee_brute<<<blocks_for(E), kThreads, 0, s>>>(v);
+void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    if (sv.hashed_e && sv.strict && sv.e_strict.size() > 0)
+        k_ee_warp<<<group_blocks(sv.e_strict.size()), kThreads, 0, s>>>(ranged(v, sv.e_strict));
+    if (sv.hashed_e && sv.fast && sv.e_fast.size() > 0)
+        k_ee_fast<<<group_blocks(sv.e_fast.size()), kThreads, 0, s>>>(ranged(v, sv.e_fast));
+    if (sv.brute_e && sv.e_all.size() > 0) k_ee_brute<<<blocks_for(sv.e_all.size()), kThreads, 0, s>>>(ranged(v, sv.e_all));
 }
-void self_island(const View& v, int V, cudaStream_t s) {
-    if (V > 0) k_island<<<blocks_for(V), kThreads, 0, s>>>(v);
+void self_island(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    if (sv.v_fast.size() > 0) k_island<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
 }
-void self_apply(const View& v, int V, cudaStream_t s) {
-    if (V > 0) k_self_apply<<<blocks_for(V), kThreads, 0, s>>>(v);
+void self_apply(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    if (sv.v_all.size() > 0) k_self_apply<<<blocks_for(sv.v_all.size()), kThreads, 0, s>>>(ranged(v, sv.v_all));
 }
 
 }  // namespace xg

@@ -251,6 +251,9 @@ struct View {
     // work counters of a profiled frame (null otherwise): query items and
     // bucket slots evaluated by the EE and VT queries
     unsigned long long* perf;
+    // item range [lo, hi) of a self-collision launch (vertices, edges,
+    // triangles or buckets, by kernel); set by the launchers
+    int lo, hi;
 };
 
 enum PerfSlot { kPerfEeItems = 0, kPerfEeSlots = 1, kPerfVtItems = 2, kPerfVtSlots = 3, kPerfSlots = 4 };
@@ -320,25 +323,56 @@ constexpr int kSignedInsidePasses = 6;  // inside-only passes at the final const
 // exclusive scan of bucket counts into starts (counts become cursors)
 void scan_bucket_counts(int* counts, int* start, int n, int* block_sums, cudaStream_t s);
 
+// Contiguous item range covering the cloths added to it.
+struct ItemRange {
+    int lo = 0, hi = 0;
+    void add(int start, int n) {
+        if (n <= 0) return;
+        if (hi <= lo) {
+            lo = start;
+            hi = start + n;
+        } else {
+            lo = lo < start ? lo : start;
+            hi = hi > start + n ? hi : start + n;
+        }
+    }
+    int size() const { return hi > lo ? hi - lo : 0; }
+};
+
+// The kernel variants some scheduled cloth needs and the item ranges of the
+// scheduled cloths.  Cloths are stored grouped by self-collision mode, so a
+// mode's range holds no items of the other mode's cloths.
+struct SelfVariants {
+    bool fast, strict, hashed_v, brute_v, hashed_t, brute_t, hashed_e, brute_e;
+    ItemRange v_all, v_fast, v_strict, e_all, e_fast, e_strict, t_all, vb, tb, eb;
+    void add_cloth(const Params& P, bool is_fast) {
+        v_all.add(P.vstart, P.V);
+        (is_fast ? v_fast : v_strict).add(P.vstart, P.V);
+        e_all.add(P.estart, P.E);
+        (is_fast ? e_fast : e_strict).add(P.estart, P.E);
+        t_all.add(P.tstart, P.T);
+        if (P.vhash) vb.add(P.vbase, P.vbuckets);
+        if (P.thash) tb.add(P.tbase, P.tbuckets);
+        if (P.ehash) eb.add(P.ebase, P.ebuckets);
+    }
+};
+
 // self collision (bucket counts must be zeroed before each hash build; nb =
-// total buckets over all cloths)
-void self_build_vertex_hash(const View& v, int V, int nb, cudaStream_t s);
+// total buckets over all cloths).  Each launcher runs the kernel variants
+// that some cloth needs, over the item range of that variant's cloths;
+// every item still skips cloths of another mode / table kind.
+void self_build_vertex_hash(const View& v, const SelfVariants& sv, int nb, cudaStream_t s);
 // `order`: 0 orders only buckets of more than 32 members (enough for strict
 // queries with a 32-candidate budget), 1 orders every bucket, 2 asks each
 // bucket's cloth
-void self_build_triangle_hash(const View& v, int T, int nb, int order, cudaStream_t s);
-void self_build_edge_hash(const View& v, int E, int nb, int order, cudaStream_t s);
-// Each launcher runs the kernel variants that some cloth needs; every item
-// skips cloths of another mode / table kind.  `mode`: 1 fast cloths only,
-// 2 strict only, 0 both.
-struct SelfVariants {
-    bool fast, strict, hashed_v, brute_v, hashed_t, brute_t, hashed_e, brute_e;
-};
-void self_neighbors(const View& v, int V, int mode, const SelfVariants& sv, cudaStream_t s);
-void self_vv(const View& v, int V, const SelfVariants& sv, cudaStream_t s);
-void self_vt(const View& v, int V, const SelfVariants& sv, cudaStream_t s);
-void self_ee(const View& v, int E, const SelfVariants& sv, cudaStream_t s);
-void self_island(const View& v, int V, cudaStream_t s);
-void self_apply(const View& v, int V, cudaStream_t s);
+void self_build_triangle_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s);
+void self_build_edge_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s);
+// `mode`: 1 fast cloths only, 2 strict only, 0 both
+void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_t s);
+void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s);
+void self_vt(const View& v, const SelfVariants& sv, cudaStream_t s);
+void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s);
+void self_island(const View& v, const SelfVariants& sv, cudaStream_t s);
+void self_apply(const View& v, const SelfVariants& sv, cudaStream_t s);
 
 }  // namespace xg

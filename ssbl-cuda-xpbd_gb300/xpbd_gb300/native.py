@@ -643,6 +643,11 @@ class NativeXpbdBatch(NativeXpbdSolver):
     def set_cloth_active(self, cloth: int, active: bool) -> None:
         self._check(self._lib.xpbd_gb300_batch_set_active(self._handle, int(cloth), 1 if active else 0))
 
+    def cloth_range(self, cloth: int) -> tuple:
+        """(first vertex, vertices, first edge, edges) of a cloth in the
+        concatenation used by whole-handle transfers (the caller's order)."""
+        return tuple(int(x) for x in self._ranges[cloth])
+
     def split_positions(self, positions: np.ndarray) -> list[np.ndarray]:
         """Per-cloth views of concatenated positions."""
         return [positions[s:s + n] for s, n in ((int(r[0]), int(r[1])) for r in self._ranges)]

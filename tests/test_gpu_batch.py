@@ -135,3 +135,36 @@ def test_batch_rejects_hard_stretch(gpu_lib):
     scs[1].options.stretch_optimization_strength = 0.5
     with pytest.raises(NativeSolverError, match="batch cloth 1: hard stretch optimization runs on one-cloth solvers only"):
         NativeXpbdBatch(_items(scs))
+
+
+def test_whole_handle_transfers_use_the_callers_cloth_order(gpu_lib, oracle_lib):
+    """The batch stores its cloths grouped by self-collision mode; ABI41
+    calls on the batch handle (whole-handle positions and pins, indices over
+    the concatenation in the caller's order) still address the caller's
+    cloths, and the cloth ranges describe that order."""
+    scs = _mixed_scenes()
+    order = [s.options.self_collision_mode if s.options.self_collision else 0 for s in scs]
+    assert order != sorted(order)  # the mix is stored in another order
+    batch = NativeXpbdBatch(_items(scs))
+    oras = _oracles(scs, oracle_lib)
+    sizes = [len(s.cloth.positions_world) for s in scs]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    for k in range(len(scs)):
+        assert batch.cloth_range(k)[:2] == (int(offs[k]), sizes[k])
+    # whole-handle position upload: cloth k lifted by 1 cm x (k + 1)
+    allpos = np.concatenate([s.cloth.positions_world + np.float32(0.01 * (k + 1)) for k, s in enumerate(scs)])
+    batch.update_positions(allpos)
+    # whole-handle pins: one pin per cloth at its local vertex 3, indices over the concatenation
+    idx = (offs[:-1] + 3).astype(np.int32)
+    tgt = allpos[idx] + np.float32(0.02)
+    batch.update_pin_targets(idx, tgt, np.ones(len(idx), np.float32))
+    for k, o in enumerate(oras):
+        o.update_positions(allpos[offs[k]:offs[k + 1]])
+        o.update_pin_targets(np.array([3], np.int32), tgt[k:k + 1], np.ones(1, np.float32))
+    for _ in range(2):
+        batch.step(10, 2, diagnostics=False, synchronize=True)
+        got = batch.download_positions()
+        for k, o in enumerate(oras):
+            o.step(10, 2)
+            assert np.array_equal(got[offs[k]:offs[k + 1]], o.download_positions()), k
+            assert np.array_equal(batch.download_cloth_positions(k), o.download_positions()), k
