@@ -1377,6 +1377,7 @@ SelfPlan plan_self(const Solver* S, int s, int substeps) {
         p.any_e |= P.E > 0;
         p.sv.fast |= C.fast;
         p.sv.strict |= !C.fast;
+        if (!C.fast) (std::min(std::max(P.max_neighbors, 1), kBucketSlots) >= kBucketSlots ? p.sv.strict_wide : p.sv.strict_narrow) = true;
         p.sv.add_cloth(P, C.fast);
         p.sv.hashed_v |= P.vhash != 0;
         p.sv.brute_v |= P.vhash == 0;

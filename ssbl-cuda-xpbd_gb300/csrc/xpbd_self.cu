@@ -1128,7 +1128,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
     const int gl = threadIdx.x & (kQueryLanes - 1);
     if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
-    if (!P.thash || fast_mode(P) || !self_scheduled(P, v)) return;
+    if (!P.thash || fast_mode(P) || !self_scheduled(P, v) || neighbor_budget(P) >= kBucketSlots) return;
     const float target = contact_radius(P);
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
@@ -1158,7 +1158,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     const int gl = threadIdx.x & (kQueryLanes - 1);
     if (e >= v.hi) return;
     const Params& P = params_e(v, e);
-    if (!P.ehash || fast_mode(P) || !self_scheduled(P, v)) return;
+    if (!P.ehash || fast_mode(P) || !self_scheduled(P, v) || neighbor_budget(P) >= kBucketSlots) return;
     const int2 ed = __ldg(&v.edges[e]);
     if (!edge_valid(v.nV, ed)) return;
     const float target = contact_radius(P);
@@ -1181,6 +1181,93 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     if (v.perf && gl == 0) {
         atomicAdd(&v.perf[kPerfEeItems], 1ull);
         atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)evaluated);
+    }
+}
+
+// Strict VT / EE queries whose candidate budget is at least the 32 query
+// slots: every accepted pair of an item's slots is taken, so the pairs are
+// independent and their order does not matter (pushes are summed in fixed
+// point).  One warp per 32 consecutive query items lays the items' bucket
+// slots end to end and evaluates 32 (item, slot) pairs per round, so the
+// lanes stay busy however the slot counts vary.  The same pairs, counters
+// and pushes as the 8-lane group kernels, which keep the cloths with a
+// smaller budget.
+template <bool kEdge>
+__global__ void __launch_bounds__(kThreads, 4) k_flat_query(View v) {
+    const int lane = threadIdx.x & 31;
+    const int item = v.lo + warp_global_id() * 32 + lane;
+    int st = 0, lim = 0;
+    float target = 0.0f, onset = 0.0f;
+    bool counted = false;
+    if (item < v.hi) {
+        const Params& P = kEdge ? params_e(v, item) : params_v(v, item);
+        bool want = (kEdge ? P.ehash : P.thash) && !fast_mode(P) && self_scheduled(P, v) && neighbor_budget(P) >= kBucketSlots;
+        F3 q{0.0f, 0.0f, 0.0f};
+        if (want && kEdge) {
+            const int2 ed = __ldg(&v.edges[item]);
+            want = edge_valid(v.nV, ed);
+            if (want) q = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
+        } else if (want) {
+            q = f3(v.pos[item]);
+        }
+        if (want) target = contact_radius(P);
+        if (want && target > 0.0f) {
+            onset = fmaxf(target * 1.8f, target + kEps);
+            const float cell = kEdge ? P.ecell : P.tcell;
+            const int b = (kEdge ? P.ebase : P.tbase) +
+                          (int)bucket_of(cell_of(q.x, cell), cell_of(q.y, cell), cell_of(q.z, cell), kEdge ? P.ebuckets : P.tbuckets);
+            const int* start = kEdge ? v.eb_start : v.tb_start;
+            st = start[b];
+            lim = min(start[b + 1] - st, kBucketSlots);
+            counted = true;
+        }
+    }
+    int incl = lim;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - lim;
+    const int* ent = kEdge ? v.eb_ent : v.tb_ent;
+    constexpr int contact_slot = kEdge ? kCntEdgeEdgeContacts : kCntSoftContacts;
+    unsigned takes = 0, pushes = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int w = base + lane;
+        int j = 0;  // owner: the first lane whose inclusive slot count exceeds w
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
+        const int o_item = __shfl_sync(0xffffffffu, item, j);
+        const int o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
+        const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
+        SoftPush sp;
+        sp.apply = false;
+        bool accepted = false;
+        if (w < total) {
+            const int other = ent[o_first + w];
+            accepted = kEdge ? ee_eval(v, o_item, other, o_target, o_onset, &sp) : vt_eval(v, o_item, other, o_target, o_onset, &sp);
+        }
+        const bool push = accepted && sp.apply;
+        takes += __popc(__ballot_sync(0xffffffffu, accepted));
+        pushes += __popc(__ballot_sync(0xffffffffu, push));
+        if (push) {
+            for (int k = 0; k < 4; ++k) {
+                const float wk = sp.w[k];
+                const bool far = kEdge ? (k > 1) : (k > 0);
+                if ((far ? -wk : wk) > 0.0f) accumulate(v, sp.idx[k], sp.delta * wk);
+            }
+        }
+    }
+    const unsigned items = __popc(__ballot_sync(0xffffffffu, counted));
+    if (lane == 0) {
+        count_add(v.counts, kCntSelfCandidates, takes);
+        count_add(v.counts, contact_slot, pushes);
+        if (v.perf && items) {
+            atomicAdd(&v.perf[kEdge ? kPerfEeItems : kPerfVtItems], (unsigned long long)items);
+            atomicAdd(&v.perf[kEdge ? kPerfEeSlots : kPerfVtSlots], (unsigned long long)total);
+        }
     }
 }
 
@@ -1612,14 +1699,18 @@ void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s) {
     if (sv.fast && sv.v_fast.size() > 0) k_vv<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
 }
 void self_vt(const View& v, const SelfVariants& sv, cudaStream_t s) {
-    if (sv.hashed_t && sv.strict && sv.v_strict.size() > 0)
+    if (sv.hashed_t && sv.strict_wide && sv.v_strict.size() > 0)
+        k_flat_query<false><<<blocks_for(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
+    if (sv.hashed_t && sv.strict_narrow && sv.v_strict.size() > 0)
         k_vt_warp<<<group_blocks(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
     if (sv.hashed_t && sv.fast && sv.v_fast.size() > 0)
         k_vt_hash<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
     if (sv.brute_t && sv.v_all.size() > 0) k_vt_brute<<<blocks_for(sv.v_all.size()), kThreads, 0, s>>>(ranged(v, sv.v_all));
 }
 void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
-    if (sv.hashed_e && sv.strict && sv.e_strict.size() > 0)
+    if (sv.hashed_e && sv.strict_wide && sv.e_strict.size() > 0)
+        k_flat_query<true><<<blocks_for(sv.e_strict.size()), kThreads, 0, s>>>(ranged(v, sv.e_strict));
+    if (sv.hashed_e && sv.strict_narrow && sv.e_strict.size() > 0)
         k_ee_warp<<<group_blocks(sv.e_strict.size()), kThreads, 0, s>>>(ranged(v, sv.e_strict));
     if (sv.hashed_e && sv.fast && sv.e_fast.size() > 0)
         k_ee_fast<<<group_blocks(sv.e_fast.size()), kThreads, 0, s>>>(ranged(v, sv.e_fast));

@@ -344,6 +344,7 @@ struct ItemRange {
 // mode's range holds no items of the other mode's cloths.
 struct SelfVariants {
     bool fast, strict, hashed_v, brute_v, hashed_t, brute_t, hashed_e, brute_e;
+    bool strict_wide, strict_narrow;  // strict cloths with a candidate budget of >= 32 / < 32 slots
     ItemRange v_all, v_fast, v_strict, e_all, e_fast, e_strict, t_all, vb, tb, eb;
     void add_cloth(const Params& P, bool is_fast) {
         v_all.add(P.vstart, P.V);

@@ -21,6 +21,10 @@ def _mixed_scenes():
     scs.append(scene.drop_scene(18, 6, seed=1))
     # fast self collision on the drop scene
     scs.append(scene.drop_scene(14, 6, seed=2, self_mode=1))
+    # strict with a candidate budget under the 32 query slots (group queries)
+    sc = scene.drop_scene(16, 6, seed=4)
+    sc.options.max_self_collision_neighbors = 5
+    scs.append(sc)
     # plain grid, tethers to the pins, bends gathered (no colouring)
     sc = scene.plain_grid_scene(12, 6)
     w = np.zeros(len(sc.cloth.positions_world), np.float32)

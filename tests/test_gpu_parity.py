@@ -131,13 +131,16 @@ def test_hash_and_neighbor_tables_bit_exact(gpu_lib, oracle_lib):
     assert g["nbcount"].sum() > 0
 
 
-@pytest.mark.parametrize("mode", [2, 1], ids=["strict", "fast"])
-def test_folded_cloth_self_contact_parity(mode, gpu_lib, oracle_lib):
+@pytest.mark.parametrize("mode,budget", [(2, 64), (2, 6), (1, 32)], ids=["strict", "strict-budget6", "fast"])
+def test_folded_cloth_self_contact_parity(mode, budget, gpu_lib, oracle_lib):
     """A cloth folded onto itself 1.2 mm apart (inside the 2 mm contact
     distance): every self-collision query finds real contacts, so the budget
     cut, the duplicate / rest / ownership filters and the pushes all run.
+    Strict mode with a budget of 32 slots or more runs the flattened queries,
+    with a smaller budget the 8-lane group queries and their budget cut.
     Positions and all 38 counters must match the oracle bit for bit."""
     sc = scene.drop_scene(40, 4, seed=3, self_mode=mode)
+    sc.options.max_self_collision_neighbors = budget
     gpu, ora = _pair(sc, oracle_lib)
     rng = np.random.default_rng(11)
     p = sc.cloth.positions_world.copy()
