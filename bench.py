@@ -419,6 +419,7 @@ def main():
     ap.add_argument("--batch-cloths", type=int, default=256, help="cloths of the batch256 workload (smaller for profiling)")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--autotune", type=int, default=1, help="1: launch configuration from the autotuner (default); 0: built-in defaults")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -458,6 +459,9 @@ def main():
         solver = native.NativeXpbdBatch([(s.cloth, s.options, s.static_triangles) for s in scs])
     else:
         solver = native.NativeXpbdSolver(scs[0].cloth, scs[0].options, scs[0].static_triangles)
+    # launch configuration from the autotuner (cached per device and
+    # workload; measured from the initial state, which it restores)
+    tuned = solver.autotune(S, I, rounds=2) if args.autotune else None
     for _ in range(args.warmup):
         solver.step(S, I, diagnostics=False, synchronize=False)
     solver.synchronize()
@@ -565,6 +569,7 @@ def main():
         "e2e": e2e, "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks.summary(),
         "roofline": roof, "kernel_profile": profile_summary, "work_counters_per_frame": {k: c / reps for k, c in counters.items()},
         "cpu_baseline": {"value": cpu_value, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+        "launch_config": {"config": solver.launch_config(), "autotune": tuned},
     }
     if plain is not None:
         line["plain"] = plain

@@ -53,12 +53,37 @@ __attribute__((visibility("default"))) long long xpbd_gb300_last_step_launches(v
 __attribute__((visibility("default"))) void* xpbd_gb300_stream(void* handle);
 
 /* Run one frame without graph capture, timing every launch with CUDA events
- * on the solver's stream; per kernel kind (16 kinds: predict, stretch pass,
+ * on the solver's stream; per kernel kind (17 kinds: predict, stretch pass,
  * other vertex pass, bend colour, vertex / triangle / edge hash, neighbour
- * table, VV, VT, EE, island, self apply, copy, CG solve, stretch caps) write
- * the summed milliseconds and the launch count.  Advances the simulation by that frame. */
+ * table, VV, VT, EE, island, self apply, copy, CG solve, stretch caps,
+ * dynamic colliders) write the summed milliseconds and the launch count
+ * (kinds >= 17).  Advances the simulation by that frame. */
 __attribute__((visibility("default"))) int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations,
                                                                      float* kernel_ms, long long* kernel_launches, int kinds);
+
+/* Launch configuration (no counterpart in the reference): 8 slots, in order
+ * block size of the per-vertex passes (default 128), of the hash count /
+ * scatter kernels (256), lanes per primitive of the triangle / edge hash
+ * (4, 8 or 16; default 8), block size of the warp-per-item kernels (256), of
+ * the thread-per-item queries (256), lanes per item of the strict group
+ * queries (4, 8 or 16; default 8), block size of the group queries (256) and
+ * of the dynamic-collider pass (128).  Block sizes are multiples of 32 up to
+ * 256; 0 selects the default.  No value changes a result.  Setting drops the
+ * captured frame graphs. */
+__attribute__((visibility("default"))) int xpbd_gb300_set_launch_config(void* handle, const int* values, int count);
+__attribute__((visibility("default"))) int xpbd_gb300_get_launch_config(void* handle, int* out, int count);
+
+/* Workload summary: out8 = cloths, vertices, edges, triangles, cloths with
+ * fast self collision, with strict self collision, with dynamic colliders,
+ * with a static SDF (the autotuner cache keys on it). */
+__attribute__((visibility("default"))) int xpbd_gb300_solver_info(void* handle, long long* out8);
+
+/* Autotuner: from the current state, time profiled frames (the fastest of
+ * `rounds` per candidate, state restored before each) for each candidate of
+ * each slot in turn, keep the fastest configuration and restore the state.
+ * ms_out2 = {tuned frame ms, default frame ms} (summed kernel times). */
+__attribute__((visibility("default"))) int xpbd_gb300_autotune(void* handle, int substeps, int iterations, int rounds,
+                                                               float* ms_out2);
 
 /* Work counters of the last xpbd_gb300_profile_frame: out4 = EE query items,
  * EE bucket slots evaluated, VT query items (strict cloths), VT slots

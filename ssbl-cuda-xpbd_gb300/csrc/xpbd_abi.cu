@@ -419,28 +419,46 @@ XG_EXPORT void* xpbd_gb300_stream(void* handle) {
 XG_EXPORT int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations, float* kernel_ms,
                                        long long* kernel_launches, int kinds) {
     g_error.clear();
+    return ok_or_zero(profile_frame(as_solver(handle), substeps, iterations, kernel_ms, kernel_launches, kinds));
+}
+
+XG_EXPORT int xpbd_gb300_set_launch_config(void* handle, const int* values, int count) {
+    g_error.clear();
+    return ok_or_zero(set_launch_config(as_solver(handle), values, count));
+}
+
+XG_EXPORT int xpbd_gb300_get_launch_config(void* handle, int* out, int count) {
+    g_error.clear();
     Solver* S = as_solver(handle);
-    if (!S || !kernel_ms || !kernel_launches || kinds < kKinds) return fail("invalid profile request") ? 1 : 0;
-    substeps = std::max(substeps, 1);
-    iterations = std::max(iterations, 1);
-    if (!prepare_step(S, substeps, iterations)) return 0;
-    for (int k = 0; k < kinds; ++k) {
-        kernel_ms[k] = 0.0f;
-        kernel_launches[k] = 0;
-    }
-    FrameStats st;
-    Profile prof;
-    enqueue_frame(S, substeps, iterations, &st, &prof);
-    if (!cuda_ok(cudaGetLastError(), "profile frame") || !cuda_ok(cudaStreamSynchronize(S->stream), "profile frame")) return 0;
-    for (auto& m : prof.marks) {
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, m.second.first, m.second.second);
-        kernel_ms[m.first] += ms;
-        kernel_launches[m.first] += 1;
-        cudaEventDestroy(m.second.first);
-        cudaEventDestroy(m.second.second);
-    }
+    if (!S || !out || count < 0) return fail("invalid launch configuration request") ? 1 : 0;
+    for (int k = 0; k < count; ++k) out[k] = k < kTuneSlots ? tune_of(S->tune, k) : 0;
     return 1;
+}
+
+XG_EXPORT int xpbd_gb300_solver_info(void* handle, long long* out8) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S || !out8) return fail("invalid solver info request") ? 1 : 0;
+    long long fast = 0, strict = 0, dyn = 0, sdf = 0;
+    for (int k = 0; k < S->K; ++k) {
+        if (S->cl[k].self_enabled) (S->cl[k].fast ? fast : strict) += 1;
+        dyn += S->hp[k].dyn ? 1 : 0;
+        sdf += S->hp[k].sdf_ready ? 1 : 0;
+    }
+    out8[0] = S->K;
+    out8[1] = S->nV;
+    out8[2] = S->nE;
+    out8[3] = S->nT;
+    out8[4] = fast;
+    out8[5] = strict;
+    out8[6] = dyn;
+    out8[7] = sdf;
+    return 1;
+}
+
+XG_EXPORT int xpbd_gb300_autotune(void* handle, int substeps, int iterations, int rounds, float* ms_out2) {
+    g_error.clear();
+    return ok_or_zero(autotune(as_solver(handle), std::max(substeps, 1), std::max(iterations, 1), rounds, ms_out2));
 }
 
 XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out4) {

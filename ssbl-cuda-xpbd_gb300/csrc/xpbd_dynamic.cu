@@ -421,7 +421,7 @@ __device__ void dyn_particles(const View& v, const Params& P, const DynSet& D, i
 
 // which: 0 unsigned meshes (triangles then particles), 1 signed meshes
 // (triangles then particles, outside contacts), 2 signed meshes inside-only.
-__global__ void __launch_bounds__(kThreadsDyn) k_dynamic(View v, int which) {
+__global__ void __launch_bounds__(kMaxBlock) k_dynamic(View v, int which) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nV) return;
     const Params& P = params_v(v, i);
@@ -436,7 +436,8 @@ __global__ void __launch_bounds__(kThreadsDyn) k_dynamic(View v, int which) {
 }  // namespace
 
 void launch_dynamic_collision(const View& v, int V, int which, cudaStream_t s) {
-    if (V > 0) k_dynamic<<<dyn_blocks(V), kThreadsDyn, 0, s>>>(v, which);
+    const int b = tune_of(v.tune, kTuneDynamicBlock);
+    if (V > 0) k_dynamic<<<grid_for(V, b), b, 0, s>>>(v, which);
 }
 
 namespace host {

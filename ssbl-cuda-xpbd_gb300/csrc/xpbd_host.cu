@@ -335,6 +335,7 @@ void release_grid(Solver* S, Cloth& c) {
 
 View Solver::view() const {
     View v{};
+    v.tune = tune;
     v.P = dp;
     v.vcloth = vcloth;
     v.ecloth = ecloth;
@@ -1860,6 +1861,144 @@ bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int fo
     S->diag.resolved_contacts = S->diag.abi41_soft_contact_count + S->diag.abi41_exact_impulse_contact_count +
                                 S->diag.abi41_edge_edge_contact_count + S->diag.static_sdf_contact_count;
     return true;
+}
+
+bool profile_frame(Solver* S, int substeps, int iterations, float* kernel_ms, long long* kernel_launches, int kinds) {
+    if (!S || !kernel_ms || !kernel_launches || kinds < kKinds) return fail("invalid profile request");
+    substeps = std::max(substeps, 1);
+    iterations = std::max(iterations, 1);
+    if (!prepare_step(S, substeps, iterations)) return false;
+    for (int k = 0; k < kinds; ++k) {
+        kernel_ms[k] = 0.0f;
+        kernel_launches[k] = 0;
+    }
+    FrameStats st;
+    Profile prof;
+    enqueue_frame(S, substeps, iterations, &st, &prof);
+    const bool ok = cuda_ok(cudaGetLastError(), "profile frame") && cuda_ok(cudaStreamSynchronize(S->stream), "profile frame");
+    for (auto& m : prof.marks) {
+        float ms = 0.0f;
+        if (ok) cudaEventElapsedTime(&ms, m.second.first, m.second.second);
+        kernel_ms[m.first] += ms;
+        kernel_launches[m.first] += 1;
+        cudaEventDestroy(m.second.first);
+        cudaEventDestroy(m.second.second);
+    }
+    return ok;
+}
+
+namespace {
+
+bool tune_value_ok(int slot, int v) {
+    if (v == 0) return true;
+    if (slot == kTunePrimLanes || slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
+    return v >= 32 && v <= kMaxBlock && v % 32 == 0;
+}
+
+}  // namespace
+
+bool set_launch_config(Solver* S, const int* values, int n) {
+    if (!S || (!values && n > 0) || n < 0 || n > kTuneSlots) return fail("invalid launch configuration");
+    LaunchTune t = S->tune;
+    for (int k = 0; k < n; ++k) {
+        if (!tune_value_ok(k, values[k])) return fail("invalid launch configuration value for slot " + std::to_string(k));
+        t.v[k] = (short)values[k];
+    }
+    if (std::memcmp(&t, &S->tune, sizeof(t)) != 0) {
+        if (!cuda_ok(cudaStreamSynchronize(S->stream), "launch configuration")) return false;
+        S->tune = t;
+        S->drop_graphs();
+    }
+    return true;
+}
+
+// Coordinate descent over the slots, one sweep, each candidate timed as the
+// fastest of `rounds` profiled frames from the same saved state.
+bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out) {
+    if (!S) return fail("invalid solver handle");
+    rounds = std::max(rounds, 1);
+    const size_t n = (size_t)std::max(S->nV, 1);
+    float4 *spos = nullptr, *sprev = nullptr, *svel = nullptr;
+    {
+        AllocAccount none(nullptr);
+        if (!dalloc(&spos, n, "autotune state") || !dalloc(&sprev, n, "autotune state") || !dalloc(&svel, n, "autotune state")) {
+            cudaFree(spos);
+            cudaFree(sprev);
+            return false;
+        }
+    }
+    auto copy = [&](float4* dst, const float4* src) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, sizeof(float4) * (size_t)S->nV, cudaMemcpyDeviceToDevice, S->stream), "autotune state");
+    };
+    bool ok = cuda_ok(cudaStreamSynchronize(S->stream), "autotune") && copy(spos, S->pos[0]) && copy(sprev, S->prev) &&
+              copy(svel, S->vel);
+    std::vector<float> kms(kKinds);
+    std::vector<long long> kn(kKinds);
+    auto measure = [&](float* out) {
+        float best = 0.0f;
+        for (int r = 0; r < rounds && ok; ++r) {
+            ok = copy(S->pos[0], spos) && copy(S->prev, sprev) && copy(S->vel, svel) &&
+                 profile_frame(S, substeps, iterations, kms.data(), kn.data(), kKinds);
+            float total = 0.0f;
+            for (float x : kms) total += x;
+            if (r == 0 || total < best) best = total;
+        }
+        *out = best;
+        return ok;
+    };
+    int dyn = 0, narrow = 0;
+    for (int k = 0; k < S->K; ++k) {
+        dyn |= S->hp[k].dyn ? 1 : 0;
+        narrow |= (S->cl[k].self_enabled && !S->cl[k].fast && std::min(std::max(S->hp[k].max_neighbors, 1), kBucketSlots) < kBucketSlots) ? 1 : 0;
+    }
+    const std::vector<std::vector<short>> cand = {
+        {64, 128, 256},   // vertex passes
+        {128, 256},       // hash count / scatter
+        {4, 8, 16},       // lanes per primitive
+        {128, 256},       // warp kernels
+        {64, 128, 256},   // thread-per-item queries
+        {4, 8, 16},       // group lanes
+        {128, 256},       // group block
+        {64, 128, 256},   // dynamic colliders
+    };
+    const LaunchTune start = S->tune;
+    LaunchTune best = start;
+    for (int k = 0; k < kTuneSlots; ++k) best.v[k] = (short)tune_of(start, k);
+    S->tune = best;
+    S->drop_graphs();
+    float best_ms = 0.0f, default_ms = 0.0f;
+    if (ok) ok = measure(&default_ms);
+    best_ms = default_ms;
+    for (int slot = 0; slot < kTuneSlots && ok; ++slot) {
+        if (slot == kTuneDynamicBlock && !dyn) continue;
+        if ((slot == kTuneGroupLanes || slot == kTuneGroupBlock) && !narrow && !S->self_any) continue;
+        for (short c : cand[slot]) {
+            if (c == best.v[slot]) continue;
+            LaunchTune t = best;
+            t.v[slot] = c;
+            S->tune = t;
+            float ms = 0.0f;
+            if (!measure(&ms)) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
+    }
+    S->tune = ok ? best : start;
+    S->drop_graphs();
+    const bool restored = copy(S->pos[0], spos) && copy(S->prev, sprev) && copy(S->vel, svel) &&
+                          cuda_ok(cudaStreamSynchronize(S->stream), "autotune restore");
+    cudaFree(spos);
+    cudaFree(sprev);
+    cudaFree(svel);
+    S->diag = SsblXpbdDiagnostics{};
+    S->diag.finite_flag = 1;
+    if (ms_out) {
+        ms_out[0] = best_ms;
+        ms_out[1] = default_ms;
+    }
+    return ok && restored;
 }
 
 }  // namespace host

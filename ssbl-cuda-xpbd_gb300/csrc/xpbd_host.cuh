@@ -287,6 +287,7 @@ struct Solver {
     int pcg_nnz = 0;
     long long pcg_iterations = 0;
 
+    LaunchTune tune{};           // launch configuration (0 = default per slot)
     long long device_bytes = 0;  // sum of the solver's device allocations
     std::map<GraphKey, GraphEntry> graphs;
     bool use_graphs = true;
@@ -329,6 +330,15 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
 bool fetch_counts(Solver* S, const FrameStats& st);
 bool sync_params(Solver* S);
 bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int force_sync);
+
+// Launch configuration: set (validated; captured graphs are dropped) and the
+// autotuner, which measures profiled frames from the current state (restored
+// after every trial and at the end, so tuning changes no result) and keeps
+// the configuration with the shortest frame.  ms_out: {tuned, default}.
+bool set_launch_config(Solver* S, const int* values, int n);
+bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out);
+// One profiled frame: per-kind milliseconds and launches (kinds >= kKinds).
+bool profile_frame(Solver* S, int substeps, int iterations, float* kernel_ms, long long* kernel_launches, int kinds);
 
 }  // namespace host
 }  // namespace xg

@@ -23,7 +23,6 @@ namespace xg {
 
 namespace {
 
-inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 __device__ __forceinline__ float contact_radius(const Params& P) { return P.self_radius; }
 
@@ -190,18 +189,19 @@ __global__ void k_vhash_scatter(View v) {
     v.vb_ent[atomicAdd(&v.vb_count[b], 1)] = i;
 }
 
-// Eight threads per primitive: thread r of primitive k walks the x rows
-// r, r + 8, ... of its cell box (at most 64 cells; rows indexed over (y, z)),
+// L threads per primitive (4, 8 or 16, a tile choice of the autotuner;
+// default 8): thread r of primitive k walks the x rows r, r + L, ... of its
+// cell box (at most 64 cells; rows indexed over (y, z)),
 // so the cell coordinates come from one division per row rather than per
 // cell.  `scatter` = false counts entries per bucket; true writes them
 // through the cursors left by the scan.  Entry order within a bucket is
 // fixed afterwards by k_bucket_sort.
-constexpr int kPrimLanes = 8;
 
-template <bool kTri>
+
+template <bool kTri, int L>
 __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = v.lo + (int)(t / kPrimLanes), r0 = (int)(t % kPrimLanes);
+    const int k = v.lo + (int)(t / L), r0 = (int)(t % L);
     if (k >= v.hi) return;
     const Params& P = kTri ? params_t(v, k) : params_e(v, k);
     if (!(kTri ? P.thash : P.ehash) || !self_scheduled(P, v)) return;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     int* ent = kTri ? v.tb_ent : v.eb_ent;
     const int nb = kTri ? P.tbuckets : P.ebuckets;
     const int base = kTri ? P.tbase : P.ebase;
-    for (int row = r0; row < ny * nz; row += kPrimLanes) {
+    for (int row = r0; row < ny * nz; row += L) {
         const int y = r.y0 + row % ny, z = r.z0 + row / ny;
         for (int x = r.x0; x <= r.x1; ++x) {
             int* slot_counter = &cnt[base + (int)bucket_of(x, y, z, nb)];
@@ -1082,19 +1082,24 @@ __device__ bool ee_eval(const View& v, int ia, int ib, float target, float onset
 // effects, so the walk stops once the budget is reached.  Groups of 8 keep
 // most lanes busy for the typical 1-16 occupied slots and put four items'
 // dependent load chains in flight per warp.
+// The lanes per item (4, 8 or 16) are a tile choice of the autotuner: the
+// ranking in slot order makes the outcome independent of it.  The fast EE
+// query keeps groups of 8.
 constexpr int kQueryLanes = 8;
 
+template <int L = kQueryLanes>
 __device__ __forceinline__ unsigned group_mask() {
     const int lane = threadIdx.x & 31;
-    return ((1u << kQueryLanes) - 1u) << (lane & ~(kQueryLanes - 1));
+    return ((1u << L) - 1u) << (lane & ~(L - 1));
 }
 
 // Take the accepted pairs of one chunk whose rank (after `prior` earlier
 // acceptances) is within the budget: candidate counter for each, the push for
 // those that have one.  Returns the group's acceptances in this chunk.
+template <int L = kQueryLanes>
 __device__ __forceinline__ int commit_chunk(const View& v, bool accepted, const SoftPush& sp, int prior, int budget,
                                            int contact_slot) {
-    const unsigned gm = group_mask();
+    const unsigned gm = group_mask<L>();
     const int lane = threadIdx.x & 31;
     const unsigned acc_mask = __ballot_sync(gm, accepted) & gm;
     const int rank = prior + __popc(acc_mask & ((1u << lane) - 1u));
@@ -1102,7 +1107,7 @@ __device__ __forceinline__ int commit_chunk(const View& v, bool accepted, const 
     const bool push = take && sp.apply;
     const unsigned take_mask = __ballot_sync(gm, take) & gm;
     const unsigned push_mask = __ballot_sync(gm, push) & gm;
-    if ((lane & (kQueryLanes - 1)) == 0) {
+    if ((lane & (L - 1)) == 0) {
         if (take_mask) count_add(v.counts, kCntSelfCandidates, __popc(take_mask));
         if (push_mask) count_add(v.counts, contact_slot, __popc(push_mask));
     }
@@ -1118,14 +1123,16 @@ __device__ __forceinline__ int commit_chunk(const View& v, bool accepted, const 
     return __popc(acc_mask);
 }
 
+template <int L = kQueryLanes>
 __device__ __forceinline__ int group_item() {
-    return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / kQueryLanes);
+    return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
 }
 
 // Strict VT: the vertex's own cell bucket (abi41.cu:5129-5143).
+template <int L>
 __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
-    const int vertex = v.lo + group_item();
-    const int gl = threadIdx.x & (kQueryLanes - 1);
+    const int vertex = v.lo + group_item<L>();
+    const int gl = threadIdx.x & (L - 1);
     if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
     if (!P.thash || fast_mode(P) || !self_scheduled(P, v) || neighbor_budget(P) >= kBucketSlots) return;
@@ -1138,13 +1145,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
     const int lim = min(v.tb_start[b + 1] - st, kBucketSlots);
     const int budget = neighbor_budget(P);
     int prior = 0, evaluated = 0;
-    for (int base = 0; base < lim && prior < budget; base += kQueryLanes) {
+    for (int base = 0; base < lim && prior < budget; base += L) {
         SoftPush sp;
         sp.apply = false;
         const int slot = base + gl;
-        evaluated += min(lim - base, kQueryLanes);
+        evaluated += min(lim - base, L);
         const bool accepted = slot < lim && vt_eval(v, vertex, v.tb_ent[st + slot], target, onset, &sp);
-        prior += commit_chunk(v, accepted, sp, prior, budget, kCntSoftContacts);
+        prior += commit_chunk<L>(v, accepted, sp, prior, budget, kCntSoftContacts);
     }
     if (v.perf && gl == 0) {
         atomicAdd(&v.perf[kPerfVtItems], 1ull);
@@ -1153,9 +1160,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
 }
 
 // Strict EE: the bucket of the edge midpoint's cell (abi41.cu:5724-5758).
+template <int L>
 __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
-    const int e = v.lo + group_item();
-    const int gl = threadIdx.x & (kQueryLanes - 1);
+    const int e = v.lo + group_item<L>();
+    const int gl = threadIdx.x & (L - 1);
     if (e >= v.hi) return;
     const Params& P = params_e(v, e);
     if (!P.ehash || fast_mode(P) || !self_scheduled(P, v) || neighbor_budget(P) >= kBucketSlots) return;
@@ -1170,13 +1178,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     const int budget = neighbor_budget(P);
     int prior = 0, evaluated = 0;
-    for (int base = 0; base < lim && prior < budget; base += kQueryLanes) {
+    for (int base = 0; base < lim && prior < budget; base += L) {
         SoftPush sp;
         sp.apply = false;
         const int slot = base + gl;
-        evaluated += min(lim - base, kQueryLanes);
+        evaluated += min(lim - base, L);
         const bool accepted = slot < lim && ee_eval(v, e, v.eb_ent[st + slot], target, onset, &sp);
-        prior += commit_chunk(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
+        prior += commit_chunk<L>(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
     }
     if (v.perf && gl == 0) {
         atomicAdd(&v.perf[kPerfEeItems], 1ull);
@@ -1633,9 +1641,6 @@ __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
 }  // namespace
 
 // Host-side entry points used by the solver orchestration.
-inline int warp_blocks(long long items) { return (int)((items * 32 + kThreads - 1) / kThreads); }
-inline int group_blocks(long long items) { return (int)((items * kQueryLanes + kThreads - 1) / kThreads); }
-
 namespace {
 
 View ranged(const View& v, const ItemRange& r) {
@@ -1645,24 +1650,62 @@ View ranged(const View& v, const ItemRange& r) {
     return out;
 }
 
+// Threads of a launch over `items` with `per_item` lanes each, in blocks of b.
+inline int grid(long long items, int per_item, int b) { return grid_for(items * per_item, b); }
+
+template <bool kTri, int L>
+void prim_pass(const View& iv, int blocks, int b, bool scatter, cudaStream_t s) {
+    k_prim_hash<kTri, L><<<blocks, b, 0, s>>>(iv, scatter);
+}
+
+template <bool kTri>
+void prim_pass_lanes(const View& iv, long long items, int lanes, int b, bool scatter, cudaStream_t s) {
+    switch (lanes) {
+        case 4: prim_pass<kTri, 4>(iv, grid(items, 4, b), b, scatter, s); break;
+        case 16: prim_pass<kTri, 16>(iv, grid(items, 16, b), b, scatter, s); break;
+        default: prim_pass<kTri, 8>(iv, grid(items, 8, b), b, scatter, s); break;
+    }
+}
+
+void bucket_order(const View& v, const ItemRange& buckets, const int* start, int* ent, int nb, int kind, int mode,
+                  cudaStream_t s) {
+    if (buckets.size() == 0) return;
+    const int b = tune_of(v.tune, kTuneWarpBlock);
+    k_bucket_sort<<<grid((buckets.size() + 31) / 32, 32, b), b, 0, s>>>(ranged(v, buckets), start, ent, nb, kind, mode);
+}
+
 void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange& buckets, int* count, int* start, int* ent,
                int nb, int order, cudaStream_t s) {
     if (items.size() == 0) return;
     const View iv = ranged(v, items);
-    const long long threads = (long long)items.size() * kPrimLanes;
-    const int blocks = (int)((threads + kThreads - 1) / kThreads);
+    const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, kTunePrimLanes);
     if (tri)
-        k_prim_hash<true><<<blocks, kThreads, 0, s>>>(iv, false);
+        prim_pass_lanes<true>(iv, items.size(), lanes, b, false, s);
     else
-        k_prim_hash<false><<<blocks, kThreads, 0, s>>>(iv, false);
+        prim_pass_lanes<false>(iv, items.size(), lanes, b, false, s);
     scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
     if (tri)
-        k_prim_hash<true><<<blocks, kThreads, 0, s>>>(iv, true);
+        prim_pass_lanes<true>(iv, items.size(), lanes, b, true, s);
     else
-        k_prim_hash<false><<<blocks, kThreads, 0, s>>>(iv, true);
-    if (buckets.size() > 0)
-        k_bucket_sort<<<warp_blocks((buckets.size() + 31) / 32), kThreads, 0, s>>>(ranged(v, buckets), start, ent, nb,
-                                                                                  tri ? 1 : 2, order);
+        prim_pass_lanes<false>(iv, items.size(), lanes, b, true, s);
+    bucket_order(v, buckets, start, ent, nb, tri ? 1 : 2, order, s);
+}
+
+template <int L>
+void group_queries(const View& v, const SelfVariants& sv, int b, cudaStream_t s, bool edges) {
+    if (edges)
+        k_ee_warp<L><<<grid(sv.e_strict.size(), L, b), b, 0, s>>>(ranged(v, sv.e_strict));
+    else
+        k_vt_warp<L><<<grid(sv.v_strict.size(), L, b), b, 0, s>>>(ranged(v, sv.v_strict));
+}
+
+void group_queries_lanes(const View& v, const SelfVariants& sv, cudaStream_t s, bool edges) {
+    const int b = tune_of(v.tune, kTuneGroupBlock);
+    switch (tune_of(v.tune, kTuneGroupLanes)) {
+        case 4: group_queries<4>(v, sv, b, s, edges); break;
+        case 16: group_queries<16>(v, sv, b, s, edges); break;
+        default: group_queries<8>(v, sv, b, s, edges); break;
+    }
 }
 
 }  // namespace
@@ -1675,11 +1718,11 @@ void self_build_vertex_hash(const View& v, const SelfVariants& sv, int nb, cudaS
     const ItemRange& r = sv.v_all;
     if (r.size() == 0) return;
     const View iv = ranged(v, r);
-    k_vhash_count<<<blocks_for(r.size()), kThreads, 0, s>>>(iv);
+    const int b = tune_of(v.tune, kTuneHashBlock);
+    k_vhash_count<<<grid(r.size(), 1, b), b, 0, s>>>(iv);
     scan_counts(v.vb_count, v.vb_start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
-    k_vhash_scatter<<<blocks_for(r.size()), kThreads, 0, s>>>(iv);
-    if (sv.vb.size() > 0)
-        k_bucket_sort<<<warp_blocks((sv.vb.size() + 31) / 32), kThreads, 0, s>>>(ranged(v, sv.vb), v.vb_start, v.vb_ent, nb, 0, 1);
+    k_vhash_scatter<<<grid(r.size(), 1, b), b, 0, s>>>(iv);
+    bucket_order(v, sv.vb, v.vb_start, v.vb_ent, nb, 0, 1, s);
 }
 void self_build_triangle_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
     prim_hash(v, true, sv.t_all, sv.tb, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
@@ -1691,36 +1734,41 @@ void self_build_edge_hash(const View& v, const SelfVariants& sv, int nb, int ord
 void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_t s) {
     const ItemRange& r = mode == 1 ? sv.v_fast : (mode == 2 ? sv.v_strict : sv.v_all);
     if (r.size() == 0) return;
-    if (sv.hashed_v) k_neighbors_warp<<<warp_blocks(r.size()), kThreads, 0, s>>>(ranged(v, r), mode);
-    if (sv.brute_v) k_neighbors_brute<<<blocks_for(r.size()), kThreads, 0, s>>>(ranged(v, r), mode);
+    const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
+    if (sv.hashed_v) k_neighbors_warp<<<grid(r.size(), 32, wb), wb, 0, s>>>(ranged(v, r), mode);
+    if (sv.brute_v) k_neighbors_brute<<<grid(r.size(), 1, qb), qb, 0, s>>>(ranged(v, r), mode);
 }
 void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s) {
-    if (sv.strict && sv.v_strict.size() > 0) k_vv_warp<<<warp_blocks(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
-    if (sv.fast && sv.v_fast.size() > 0) k_vv<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
+    const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
+    if (sv.strict && sv.v_strict.size() > 0) k_vv_warp<<<grid(sv.v_strict.size(), 32, wb), wb, 0, s>>>(ranged(v, sv.v_strict));
+    if (sv.fast && sv.v_fast.size() > 0) k_vv<<<grid(sv.v_fast.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_fast));
 }
 void self_vt(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
     if (sv.hashed_t && sv.strict_wide && sv.v_strict.size() > 0)
-        k_flat_query<false><<<blocks_for(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
-    if (sv.hashed_t && sv.strict_narrow && sv.v_strict.size() > 0)
-        k_vt_warp<<<group_blocks(sv.v_strict.size()), kThreads, 0, s>>>(ranged(v, sv.v_strict));
+        k_flat_query<false><<<grid(sv.v_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.v_strict));
+    if (sv.hashed_t && sv.strict_narrow && sv.v_strict.size() > 0) group_queries_lanes(v, sv, s, false);
     if (sv.hashed_t && sv.fast && sv.v_fast.size() > 0)
-        k_vt_hash<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
-    if (sv.brute_t && sv.v_all.size() > 0) k_vt_brute<<<blocks_for(sv.v_all.size()), kThreads, 0, s>>>(ranged(v, sv.v_all));
+        k_vt_hash<<<grid(sv.v_fast.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_fast));
+    if (sv.brute_t && sv.v_all.size() > 0) k_vt_brute<<<grid(sv.v_all.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_all));
 }
 void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
+    const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
+    const int gb = tune_of(v.tune, kTuneGroupBlock);
     if (sv.hashed_e && sv.strict_wide && sv.e_strict.size() > 0)
-        k_flat_query<true><<<blocks_for(sv.e_strict.size()), kThreads, 0, s>>>(ranged(v, sv.e_strict));
-    if (sv.hashed_e && sv.strict_narrow && sv.e_strict.size() > 0)
-        k_ee_warp<<<group_blocks(sv.e_strict.size()), kThreads, 0, s>>>(ranged(v, sv.e_strict));
+        k_flat_query<true><<<grid(sv.e_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.e_strict));
+    if (sv.hashed_e && sv.strict_narrow && sv.e_strict.size() > 0) group_queries_lanes(v, sv, s, true);
     if (sv.hashed_e && sv.fast && sv.e_fast.size() > 0)
-        k_ee_fast<<<group_blocks(sv.e_fast.size()), kThreads, 0, s>>>(ranged(v, sv.e_fast));
-    if (sv.brute_e && sv.e_all.size() > 0) k_ee_brute<<<blocks_for(sv.e_all.size()), kThreads, 0, s>>>(ranged(v, sv.e_all));
+        k_ee_fast<<<grid(sv.e_fast.size(), kQueryLanes, gb), gb, 0, s>>>(ranged(v, sv.e_fast));
+    if (sv.brute_e && sv.e_all.size() > 0) k_ee_brute<<<grid(sv.e_all.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.e_all));
 }
 void self_island(const View& v, const SelfVariants& sv, cudaStream_t s) {
-    if (sv.v_fast.size() > 0) k_island<<<blocks_for(sv.v_fast.size()), kThreads, 0, s>>>(ranged(v, sv.v_fast));
+    const int qb = tune_of(v.tune, kTuneQueryBlock);
+    if (sv.v_fast.size() > 0) k_island<<<grid(sv.v_fast.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_fast));
 }
 void self_apply(const View& v, const SelfVariants& sv, cudaStream_t s) {
-    if (sv.v_all.size() > 0) k_self_apply<<<blocks_for(sv.v_all.size()), kThreads, 0, s>>>(ranged(v, sv.v_all));
+    const int qb = tune_of(v.tune, kTuneQueryBlock);
+    if (sv.v_all.size() > 0) k_self_apply<<<grid(sv.v_all.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_all));
 }
 
 }  // namespace xg

@@ -196,6 +196,29 @@ struct PcgView {
     unsigned* max_delta_bits;
 };
 
+// Launch configuration of the kernel classes (block sizes and tiles), chosen
+// by the autotuner; 0 selects the built-in default.  None of them changes a
+// result: every kernel's per-item arithmetic and its fixed-point sums are the
+// same for any block size, lanes per primitive or lanes per query item.
+enum TuneSlot {
+    kTuneVertexBlock = 0,  // per-vertex constraint passes and prediction (default 128)
+    kTuneHashBlock,        // hash count / scatter kernels (256)
+    kTunePrimLanes,        // lanes per primitive of the triangle / edge hash: 4, 8, 16 (8)
+    kTuneWarpBlock,        // warp-per-item kernels: neighbour table, strict VV, flat queries, bucket order (256)
+    kTuneQueryBlock,       // thread-per-item queries: fast VV / VT, brute queries, islands, apply (256)
+    kTuneGroupLanes,       // lanes per item of the strict group queries: 4, 8, 16 (8)
+    kTuneGroupBlock,       // group query kernels (256)
+    kTuneDynamicBlock,     // dynamic colliders (128)
+    kTuneSlots
+};
+struct LaunchTune {
+    short v[kTuneSlots];
+};
+constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128};
+constexpr int kMaxBlock = 256;  // the kernels' launch bounds
+inline int tune_of(const LaunchTune& t, int slot) { return t.v[slot] > 0 ? t.v[slot] : kTuneDefault[slot]; }
+inline int grid_for(long long threads, int block) { return (int)((threads + block - 1) / block); }
+
 // Device pointers of one solver, passed by value to each kernel, plus the
 // launch context of the frame schedule.
 struct View {
@@ -254,6 +277,7 @@ struct View {
     // item range [lo, hi) of a self-collision launch (vertices, edges,
     // triangles or buckets, by kernel); set by the launchers
     int lo, hi;
+    LaunchTune tune;  // read by the launchers only
 };
 
 enum PerfSlot { kPerfEeItems = 0, kPerfEeSlots = 1, kPerfVtItems = 2, kPerfVtSlots = 3, kPerfSlots = 4 };

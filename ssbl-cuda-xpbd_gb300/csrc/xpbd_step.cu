@@ -520,23 +520,23 @@ __global__ void k_pin_scatter(const int* idx, const float4* target, const float*
 
 inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
-// The per-vertex passes are latency bound (gathers of neighbours): 128-thread
-// blocks spread a 10k-vertex cloth over twice as many SMs.
-constexpr int kVertexThreads = 128;
-inline int vblocks_for(int n) { return (n + kVertexThreads - 1) / kVertexThreads; }
-
 }  // namespace
 
+// The per-vertex passes are latency bound (gathers of neighbours): by default
+// 128-thread blocks spread a 10k-vertex cloth over twice as many SMs.
 void launch_predict(const View& v, int V, cudaStream_t s) {
-    if (V > 0) k_predict<<<vblocks_for(V), kVertexThreads, 0, s>>>(v);
+    const int b = tune_of(v.tune, kTuneVertexBlock);
+    if (V > 0) k_predict<<<grid_for(V, b), b, 0, s>>>(v);
 }
 
 void launch_vertex_pass(const View& v, int V, unsigned flags, cudaStream_t s) {
-    if (V > 0) k_vertex_pass<<<vblocks_for(V), kVertexThreads, 0, s>>>(v, flags);
+    const int b = tune_of(v.tune, kTuneVertexBlock);
+    if (V > 0) k_vertex_pass<<<grid_for(V, b), b, 0, s>>>(v, flags);
 }
 
 void launch_bend_color(const View& v, int start, int count, cudaStream_t s) {
-    if (count > 0) k_bend_color<<<blocks_for(count), kThreads, 0, s>>>(v, start, count);
+    const int b = tune_of(v.tune, kTuneVertexBlock);
+    if (count > 0) k_bend_color<<<grid_for(count, b), b, 0, s>>>(v, start, count);
 }
 
 void launch_pin_scatter(const int* idx, const float4* target, const float* weight, const float* relax, int n,

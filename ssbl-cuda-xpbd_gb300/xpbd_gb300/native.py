@@ -224,6 +224,10 @@ def _load_library():
                                                     ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "xpbd_gb300_profile_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
         "xpbd_gb300_device_bytes": (ctypes.c_longlong, [vp]),
+        "xpbd_gb300_set_launch_config": (ctypes.c_int, [vp, _PI, ctypes.c_int]),
+        "xpbd_gb300_get_launch_config": (ctypes.c_int, [vp, _PI, ctypes.c_int]),
+        "xpbd_gb300_solver_info": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
+        "xpbd_gb300_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _PF]),
         "xpbd_gb300_prepare_graph": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "xpbd_gb300_batch_create": (vp, [ctypes.POINTER(NativeConfig), ctypes.POINTER(NativeMesh), ctypes.c_int]),
         "xpbd_gb300_batch_cloth_count": (ctypes.c_int, [vp]),
@@ -528,6 +532,49 @@ class NativeXpbdSolver:
     def device_bytes(self) -> int:
         """Device memory held by this solver."""
         return int(self._lib.xpbd_gb300_device_bytes(self._handle))
+
+    LAUNCH_SLOTS = ("vertex_block", "hash_block", "prim_lanes", "warp_block", "query_block", "group_lanes",
+                    "group_block", "dynamic_block")
+
+    def launch_config(self) -> dict:
+        """Effective launch configuration (block sizes and tiles) by slot."""
+        out = np.zeros(len(self.LAUNCH_SLOTS), np.int32)
+        self._check(self._lib.xpbd_gb300_get_launch_config(self._handle, _ip(out), len(out)))
+        return {k: int(v) for k, v in zip(self.LAUNCH_SLOTS, out)}
+
+    def set_launch_config(self, config) -> None:
+        """Set slots from a dict (missing slots unchanged) or a sequence in
+        LAUNCH_SLOTS order (0 = default).  Results do not depend on it."""
+        cur = self.launch_config()
+        if isinstance(config, dict):
+            unknown = set(config) - set(self.LAUNCH_SLOTS)
+            if unknown:
+                raise NativeSolverError(f"unknown launch configuration slots: {sorted(unknown)}")
+            cur.update({k: int(v) for k, v in config.items()})
+            vals = [cur[k] for k in self.LAUNCH_SLOTS]
+        else:
+            vals = [int(x) for x in config]
+        arr = np.ascontiguousarray(vals, np.int32)
+        self._check(self._lib.xpbd_gb300_set_launch_config(self._handle, _ip(arr), len(arr)))
+
+    def solver_info(self) -> dict:
+        out = (ctypes.c_longlong * 8)()
+        self._check(self._lib.xpbd_gb300_solver_info(self._handle, out))
+        keys = ("cloths", "vertices", "edges", "triangles", "fast", "strict", "dynamic", "sdf")
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    def autotune(self, substeps: int, iterations: int, rounds: int = 2, cache: bool = True) -> dict:
+        """Pick the launch configuration for this workload (cached per device
+        and workload, see xpbd_gb300.autotune).  The solver's state is
+        unchanged."""
+        from . import autotune as _tune
+
+        return _tune.tune(self, int(substeps), int(iterations), rounds=rounds, use_cache=cache)
+
+    def _autotune_native(self, substeps: int, iterations: int, rounds: int) -> tuple:
+        ms = np.zeros(2, np.float32)
+        self._check(self._lib.xpbd_gb300_autotune(self._handle, int(substeps), int(iterations), int(rounds), _fp(ms)))
+        return float(ms[0]), float(ms[1])
 
     def stream(self) -> int:
         return int(self._lib.xpbd_gb300_stream(self._handle) or 0)
