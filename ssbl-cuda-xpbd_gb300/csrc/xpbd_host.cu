@@ -1356,6 +1356,7 @@ struct SelfPlan {
     int passes = 0;
     bool vhash = false, thash = false, ehash = false, any_t = false, any_e = false, island = false;
     bool t_order = false, t_plain = false, e_order = false, e_plain = false;  // bucket order needs
+    unsigned island_passes = 0;  // passes in which some cloth runs its overlap islands
     SelfVariants sv{};
     long long hits = 0, misses = 0;
 };
@@ -1386,7 +1387,10 @@ SelfPlan plan_self(const Solver* S, int s, int substeps) {
         p.sv.brute_t |= P.thash == 0 && P.T > 0;
         p.sv.hashed_e |= P.ehash != 0 && P.E > 0;
         p.sv.brute_e |= P.ehash == 0 && P.E > 0;
-        p.island |= C.fast && P.T > 0 && P.thash != 0;
+        if (C.fast && P.T > 0 && P.thash != 0) {
+            p.island = true;
+            p.island_passes |= 1u << (std::min(std::max(P.self_passes, 1), 31) - 1);  // islands run in a cloth's final pass
+        }
         if (C.fast) {
             p.hits += (long long)P.V * (C.passes > 1 ? C.passes - 1 : 0);
             p.misses += (long long)P.V;
@@ -1617,7 +1621,8 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                     if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, 2, sp.sv, lane_stream(0)); });
                     timed(kKVertexVertex, 1, [&] { self_vv(pv2, sp.sv, lane_stream(0)); });
                     if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, sp.sv, lane_stream(1)); });
-                    if (sp.island) timed(kKIsland, 1, [&] { self_island(pv2, sp.sv, lane_stream(1)); });
+                    if (sp.island && ((sp.island_passes >> pass) & 1u))
+                        timed(kKIsland, 1, [&] { self_island(pv2, sp.sv, lane_stream(1)); });
                     if (sp.any_e) timed(kKEdgeEdge, 1, [&] { self_ee(pv2, sp.sv, lane_stream(2)); });
                     join();
                     timed(kKSelfApply, 1, [&] { self_apply(pv2, sp.sv, S->stream); });

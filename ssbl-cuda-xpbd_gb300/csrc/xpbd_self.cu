@@ -195,7 +195,7 @@ __global__ void k_vhash_scatter(View v) {
 // so the cell coordinates come from one division per row rather than per
 // cell.  `scatter` = false counts entries per bucket; true writes them
 // through the cursors left by the scan.  Entry order within a bucket is
-// fixed afterwards by k_bucket_sort.
+// fixed afterwards by k_bucket_sort where a query depends on it.
 
 
 template <bool kTri, int L>
@@ -1534,18 +1534,31 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
                         continue;
                     }
                     const int4 t = __ldg(&v.tris[tri]);
-                    if (!tri_valid(v.nV, t) || rest_vt_neighbor(v, vertex, t, target, onset)) continue;
+                    if (!tri_valid(v.nV, t)) continue;
+                    // The reference tests the rest pose, then finiteness, then
+                    // the current distance.  Both the rest and the distance
+                    // test only skip the candidate, so for finite positions
+                    // the (cheaper, usually failing) distance test runs
+                    // first; non-finite positions keep the reference order,
+                    // which decides the guard count.
                     const F3 a = f3(v.pos[t.x]), b2 = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
                     const F3 ap = f3(v.prev[t.x]), bp = f3(v.prev[t.y]), cp = f3(v.prev[t.z]);
-                    if (!finite3(a) || !finite3(b2) || !finite3(c) || !finite3(ap) || !finite3(bp) || !finite3(cp)) {
+                    const bool finite = finite3(a) && finite3(b2) && finite3(c) && finite3(ap) && finite3(bp) && finite3(cp);
+                    F3 q{0.0f, 0.0f, 0.0f};
+                    float dsq = 0.0f, dist = 0.0f;
+                    if (finite) {
+                        q = closest_on_triangle(p, a, b2, c);
+                        const F3 d0 = p - q;
+                        dsq = dot3(d0, d0);
+                        dist = sqrtf(fmaxf(dsq, kEps));
+                        if (dist >= target) continue;
+                    }
+                    if (rest_vt_neighbor(v, vertex, t, target, onset)) continue;
+                    if (!finite) {
                         count1(v.counts, kCntIslandGuarded);
                         continue;
                     }
-                    const F3 q = closest_on_triangle(p, a, b2, c);
                     F3 delta = p - q;
-                    const float dsq = dot3(delta, delta);
-                    float dist = sqrtf(fmaxf(dsq, kEps));
-                    if (dist >= target) continue;
                     F3 nrm{0.0f, 0.0f, 1.0f};
                     if (dsq > kEps) {
                         nrm = delta * (1.0f / dist);
