@@ -156,6 +156,43 @@ XG_HD void segment_params(F3 p1, F3 q1, F3 p2, F3 q2, float* s, float* t) {
     }
 }
 
+// Early rejection that cannot change a result.  The closest points computed
+// by closest_on_triangle / segment_params are convex combinations of the
+// corners, so their exact distance is at least the largest per-axis gap
+// between the primitives' boxes; the float computation deviates from it by
+// a few units in the last place of the largest coordinate magnitude.  When
+// the gap exceeds `limit` by a relative 1e-5 plus 4e-6 x that magnitude
+// (well above the rounding), the computed distance is not below `limit`, so
+// a test "distance < limit" would fail anyway.  Non-finite input never takes
+// the shortcut.
+XG_HD float abs_max4(F3 a, F3 b, F3 c, F3 d) {
+    const float ma = fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z)));
+    const float mb = fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z)));
+    const float mc = fmaxf(fabsf(c.x), fmaxf(fabsf(c.y), fabsf(c.z)));
+    const float md = fmaxf(fabsf(d.x), fmaxf(fabsf(d.y), fabsf(d.z)));
+    return fmaxf(fmaxf(ma, mb), fmaxf(mc, md));
+}
+
+XG_HD bool gap_proves_far(float gap, float magnitude, bool finite, float limit) {
+    return finite && gap > limit * 1.00001f + magnitude * 4.0e-6f;
+}
+
+XG_HD bool segments_far(F3 a0, F3 a1, F3 b0, F3 b1, float limit) {
+    const float gx = fmaxf(fminf(b0.x, b1.x) - fmaxf(a0.x, a1.x), fminf(a0.x, a1.x) - fmaxf(b0.x, b1.x));
+    const float gy = fmaxf(fminf(b0.y, b1.y) - fmaxf(a0.y, a1.y), fminf(a0.y, a1.y) - fmaxf(b0.y, b1.y));
+    const float gz = fmaxf(fminf(b0.z, b1.z) - fmaxf(a0.z, a1.z), fminf(a0.z, a1.z) - fmaxf(b0.z, b1.z));
+    const bool finite = finite3(a0) && finite3(a1) && finite3(b0) && finite3(b1);
+    return gap_proves_far(fmaxf(gx, fmaxf(gy, gz)), abs_max4(a0, a1, b0, b1), finite, limit);
+}
+
+XG_HD bool point_triangle_far(F3 p, F3 a, F3 b, F3 c, float limit) {
+    const float gx = fmaxf(fminf(a.x, fminf(b.x, c.x)) - p.x, p.x - fmaxf(a.x, fmaxf(b.x, c.x)));
+    const float gy = fmaxf(fminf(a.y, fminf(b.y, c.y)) - p.y, p.y - fmaxf(a.y, fmaxf(b.y, c.y)));
+    const float gz = fmaxf(fminf(a.z, fminf(b.z, c.z)) - p.z, p.z - fmaxf(a.z, fmaxf(b.z, c.z)));
+    const bool finite = finite3(p) && finite3(a) && finite3(b) && finite3(c);
+    return gap_proves_far(fmaxf(gx, fmaxf(gy, gz)), abs_max4(p, a, b, c), finite, limit);
+}
+
 // Fixed-point accumulation of position deltas: 2^32 units per metre.  Integer
 // addition is associative, so scatter sums come out the same whatever order
 // the atomics land in; the CPU oracle quantises the same way.

@@ -557,9 +557,10 @@ __global__ void __launch_bounds__(kThreads) k_vv(View v) {
 __device__ bool rest_vt_neighbor(const View& v, int vertex, int4 t, float target, float onset) {
     if (vertex == t.x || vertex == t.y || vertex == t.z) return true;
     const F3 rp = f3(ld4(&v.rest[vertex]));
-    const F3 rq = closest_on_triangle(rp, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])), f3(ld4(&v.rest[t.z])));
-    const F3 rd = rp - rq;
+    const F3 ra = f3(ld4(&v.rest[t.x])), rb = f3(ld4(&v.rest[t.y])), rc = f3(ld4(&v.rest[t.z]));
     const float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    if (point_triangle_far(rp, ra, rb, rc, skip)) return false;
+    const F3 rd = rp - closest_on_triangle(rp, ra, rb, rc);
     return dot3(rd, rd) < skip * skip;
 }
 
@@ -574,6 +575,7 @@ __device__ bool vt_pair(const View& v, const Params& P, int vertex, int tri, flo
         return false;
     }
     const F3 p = f3(v.pos[vertex]), a = f3(v.pos[t.x]), b = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
+    if (point_triangle_far(p, a, b, c, onset)) return false;
     const F3 q = closest_on_triangle(p, a, b, c);
     F3 d = p - q;
     const float dsq = dot3(d, d);
@@ -686,10 +688,11 @@ __device__ bool rest_ee_neighbor(const View& v, int2 ea, int2 eb, float target, 
     if (ea.x == eb.x || ea.x == eb.y || ea.y == eb.x || ea.y == eb.y) return true;
     const F3 a0 = f3(ld4(&v.rest[ea.x])), a1 = f3(ld4(&v.rest[ea.y]));
     const F3 b0 = f3(ld4(&v.rest[eb.x])), b1 = f3(ld4(&v.rest[eb.y]));
+    const float skip = fmaxf(onset * 1.25f, target * 2.5f);
+    if (segments_far(a0, a1, b0, b1, skip)) return false;
     float s, t;
     segment_params(a0, a1, b0, b1, &s, &t);
     const F3 d = (a0 + (a1 - a0) * s) - (b0 + (b1 - b0) * t);
-    const float skip = fmaxf(onset * 1.25f, target * 2.5f);
     return dot3(d, d) < skip * skip;
 }
 
@@ -704,6 +707,7 @@ __device__ bool ee_pair(const View& v, const Params& P, int ia, int ib, float ta
         return false;
     }
     const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
+    if (segments_far(a0, a1, b0, b1, onset)) return false;
     float s, t;
     segment_params(a0, a1, b0, b1, &s, &t);
     const F3 pa = a0 + (a1 - a0) * s;
@@ -960,6 +964,7 @@ __device__ bool vt_eval(const View& v, int vertex, int tri, float target, float 
     if (!tri_valid(v.nV, t)) return false;
     if (vertex == t.x || vertex == t.y || vertex == t.z) return false;
     const F3 p = f3(v.pos[vertex]), a = f3(v.pos[t.x]), b = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
+    if (point_triangle_far(p, a, b, c, onset)) return false;
     const F3 q = closest_on_triangle(p, a, b, c);
     const F3 d = p - q;
     const float dsq = dot3(d, d);
@@ -1019,6 +1024,7 @@ __device__ bool ee_eval(const View& v, int ia, int ib, float target, float onset
     if (!edge_valid(v.nV, ea) || !edge_valid(v.nV, eb)) return false;
     if (ea.x == eb.x || ea.x == eb.y || ea.y == eb.x || ea.y == eb.y) return false;
     const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
+    if (segments_far(a0, a1, b0, b1, onset)) return false;
     float s, t;
     segment_params(a0, a1, b0, b1, &s, &t);
     const F3 pa = a0 + (a1 - a0) * s;
@@ -1289,6 +1295,7 @@ __device__ int ee_fast_classify(const View& v, int ia, int ib, float target, flo
     if (!edge_valid(v.nV, ea) || !edge_valid(v.nV, eb)) return 0;
     if (rest_ee_neighbor(v, ea, eb, target, onset)) return 1;
     const F3 a0 = f3(v.pos[ea.x]), a1 = f3(v.pos[ea.y]), b0 = f3(v.pos[eb.x]), b1 = f3(v.pos[eb.y]);
+    if (segments_far(a0, a1, b0, b1, onset)) return 2;
     float s, t;
     segment_params(a0, a1, b0, b1, &s, &t);
     const F3 pa = a0 + (a1 - a0) * s;
@@ -1547,6 +1554,7 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
                     F3 q{0.0f, 0.0f, 0.0f};
                     float dsq = 0.0f, dist = 0.0f;
                     if (finite) {
+                        if (point_triangle_far(p, a, b2, c, target)) continue;
                         q = closest_on_triangle(p, a, b2, c);
                         const F3 d0 = p - q;
                         dsq = dot3(d0, d0);
