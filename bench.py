@@ -543,7 +543,11 @@ def main():
         if not ok:
             raise RuntimeError(native._last_error(lib))
 
-    for _ in range(2):
+    # the same frames as the device-timed region: from the initial state,
+    # W warm-up frames, then K timed frames
+    if not lib.ssbl_reset_solver(h):
+        raise RuntimeError(native._last_error(lib))
+    for _ in range(args.warmup):
         e2e_frame()
     t0 = time.perf_counter()
     for _ in range(args.steps):

@@ -61,6 +61,17 @@ __attribute__((visibility("default"))) void* xpbd_gb300_stream(void* handle);
 __attribute__((visibility("default"))) int xpbd_gb300_profile_frame(void* handle, int substeps, int iterations,
                                                                      float* kernel_ms, long long* kernel_launches, int kinds);
 
+/* Shared dynamic scene for one cloth of a batch (ssbl_attach_global_dynamic_scene
+ * attaches every cloth of a handle): the cloth's unsigned dynamic-collider
+ * stage reads the scene's colliders except those of `target_source_id` (and,
+ * with mode 2, those of layers not below `target_collision_layer`); mode 0
+ * keeps it on its own colliders.  clear detaches the cloth. */
+__attribute__((visibility("default"))) int xpbd_gb300_batch_attach_global_dynamic_scene(void* handle, int cloth, void* scene,
+                                                                                        int target_source_id,
+                                                                                        int target_collision_layer,
+                                                                                        int collision_mode);
+__attribute__((visibility("default"))) int xpbd_gb300_batch_clear_global_dynamic_scene(void* handle, int cloth);
+
 /* Launch configuration (no counterpart in the reference): 8 slots, in order
  * block size of the per-vertex passes (default 128), of the hash count /
  * scatter kernels (256), lanes per primitive of the triangle / edge hash

@@ -138,6 +138,20 @@ static inline long long to_fix(float v) {
 static inline float from_fix(long long v) { return (float)v * (1.0f / 4294967296.0f); }
 
 /* ------------------------------------------------------------- solver -- */
+/* One set of dynamic colliders: a cloth's own (OracleSolver.own) or a shared
+ * scene's (OracleScene.d, with source ids and layers per primitive). */
+typedef struct ODyn ODyn;
+struct ODyn {
+    int dt_n, dt_signed, dt_motion, dt_hashed, dt_nb, dt_large_n, dt_upload, dt_max_occ;
+    float dt_cell;
+    V3 *dt_tri, *dt_min, *dt_max, *dt_center, *dt_prev_center; float* dt_radius;
+    int *dt_cmin, *dt_cmax, *dt_start, *dt_ent, *dt_large, *dt_idx; int dt_idx_n;
+    int dp_n, dp_motion, dp_hashed, dp_nb, dp_upload;
+    float dp_cell; unsigned long long dp_sig;
+    V3 *dp_pos, *dp_prev; float* dp_rad; int *dp_cellc, *dp_start, *dp_ent;
+    int *tri_src, *tri_layer, *par_src, *par_layer;
+};
+
 struct OracleSolver {
     SsblXpbdConfig cfg;
     SsblXpbdRuntimeColliders col;
@@ -171,15 +185,10 @@ struct OracleSolver {
     int pressure_on; float *p_area, *p_rest;
     float p_strength, p_accel, p_impulse, p_vrest, p_vlen;
     SsblXpbdForceField fields[64]; int nfields;
-    /* dynamic colliders: triangles (bounds, cell spans, hash with bucket
-     * members in increasing id order, large list) and particles */
-    int dt_n, dt_signed, dt_motion, dt_hashed, dt_nb, dt_large_n, dt_upload, dt_topo, dt_max_occ;
-    float dt_cell;
-    V3 *dt_tri, *dt_min, *dt_max, *dt_center, *dt_prev_center; float* dt_radius;
-    int *dt_cmin, *dt_cmax, *dt_start, *dt_ent, *dt_large, *dt_idx; int dt_idx_n;
-    int dp_n, dp_motion, dp_hashed, dp_nb, dp_upload;
-    float dp_cell; unsigned long long dp_sig;
-    V3 *dp_pos, *dp_prev; float* dp_rad; int *dp_cellc, *dp_start, *dp_ent;
+    /* dynamic colliders: the cloth's own, and an attached shared scene with
+     * its source filter */
+    ODyn own;
+    OracleScene* scene; int gd_mode, gd_src, gd_layer;
     float dyn_sub_dt;
 };
 
@@ -1825,6 +1834,8 @@ static void hard_stretch(OracleSolver* s, float dt) {
 }
 
 /* ----------------------------------------------------------- lifecycle -- */
+static void odyn_free(ODyn* d);
+
 void oracle_destroy(OracleSolver* s) {
     if (!s) return;
     void* p[] = {s->pos, s->snap, s->prev, s->vel, s->rest, s->w, s->inv, s->sp_off, s->sp_other, s->sp_side, s->sp_rest,
@@ -1832,10 +1843,9 @@ void oracle_destroy(OracleSolver* s) {
                  s->bend_rest, s->bend_colors, s->tris, s->edges, s->pin_w, s->pin_t, s->pin_relax, s->sdf, s->stris,
                  s->vcell, s->vb_start, s->vb_ent, s->tb_start, s->tb_ent, s->eb_start, s->eb_ent, s->nb_count, s->nb_idx, s->acc,
                  s->diag, s->pinv, s->r, s->z, s->d, s->q, s->off, s->avg_sum, s->avg_cnt, s->cap_edges, s->cap_rest, s->cap_colors,
-                 s->vt_off, s->vt_tri, s->p_area, s->p_rest, s->dt_tri, s->dt_min, s->dt_max, s->dt_center, s->dt_prev_center,
-                 s->dt_radius, s->dt_cmin, s->dt_cmax, s->dt_start, s->dt_ent, s->dt_large, s->dt_idx, s->dp_pos, s->dp_prev,
-                 s->dp_rad, s->dp_cellc, s->dp_start, s->dp_ent};
+                 s->vt_off, s->vt_tri, s->p_area, s->p_rest};
     for (size_t k = 0; k < sizeof(p) / sizeof(p[0]); ++k) free(p[k]);
+    odyn_free(&s->own);
     free(s);
 }
 
@@ -2129,27 +2139,41 @@ int oracle_update_static_triangles(OracleSolver* s, const float* tris, int count
 }
 
 /* ------------------------------------------------- dynamic colliders -- */
+struct OracleScene {
+    ODyn d;
+    float margin, thickness;
+    long long overflow;
+};
+
+static void odyn_free(ODyn* d) {
+    void* p[] = {d->dt_tri, d->dt_min, d->dt_max, d->dt_center, d->dt_prev_center, d->dt_radius, d->dt_cmin, d->dt_cmax,
+                 d->dt_start, d->dt_ent, d->dt_large, d->dt_idx, d->dp_pos, d->dp_prev, d->dp_rad, d->dp_cellc, d->dp_start,
+                 d->dp_ent, d->tri_src, d->tri_layer, d->par_src, d->par_layer};
+    for (size_t k = 0; k < sizeof(p) / sizeof(p[0]); ++k) free(p[k]);
+    memset(d, 0, sizeof(*d));
+}
+
 /* Triangle rows, bounds, centres, radii and cell spans grown by the collision
  * margin (abi41.cu:3686-3760); hash with members in increasing id order and
  * the large list (spans over 64 cells) in id order (abi41.cu:3763-3930,
  * 6220-6392). */
-static void dyn_tri_finish(OracleSolver* s, int T, int signed_mode, int motion, float cell) {
+static void dyn_tri_finish(ODyn* d, float margin_in, int T, int signed_mode, int motion, float cell) {
     size_t n = (size_t)T;
-    if (motion) memcpy(s->dt_prev_center, s->dt_center, sizeof(V3) * n);
-    s->dt_min = (V3*)realloc(s->dt_min, sizeof(V3) * n); s->dt_max = (V3*)realloc(s->dt_max, sizeof(V3) * n);
-    s->dt_center = (V3*)realloc(s->dt_center, sizeof(V3) * n); s->dt_radius = (float*)realloc(s->dt_radius, sizeof(float) * n);
-    if (!motion) s->dt_prev_center = (V3*)realloc(s->dt_prev_center, sizeof(V3) * n);
-    s->dt_cmin = (int*)realloc(s->dt_cmin, sizeof(int) * 3 * n); s->dt_cmax = (int*)realloc(s->dt_cmax, sizeof(int) * 3 * n);
+    if (motion) memcpy(d->dt_prev_center, d->dt_center, sizeof(V3) * n);
+    d->dt_min = (V3*)realloc(d->dt_min, sizeof(V3) * n); d->dt_max = (V3*)realloc(d->dt_max, sizeof(V3) * n);
+    d->dt_center = (V3*)realloc(d->dt_center, sizeof(V3) * n); d->dt_radius = (float*)realloc(d->dt_radius, sizeof(float) * n);
+    if (!motion) d->dt_prev_center = (V3*)realloc(d->dt_prev_center, sizeof(V3) * n);
+    d->dt_cmin = (int*)realloc(d->dt_cmin, sizeof(int) * 3 * n); d->dt_cmax = (int*)realloc(d->dt_cmax, sizeof(int) * 3 * n);
     const int hashed = T >= 64;
-    const float margin = fmaxf(s->cfg.collision_margin, 0.0f);
+    const float margin = fmaxf(margin_in, 0.0f);
     for (int t = 0; t < T; ++t) {
-        V3 a = s->dt_tri[3 * t], b = s->dt_tri[3 * t + 1], c = s->dt_tri[3 * t + 2];
+        V3 a = d->dt_tri[3 * t], b = d->dt_tri[3 * t + 1], c = d->dt_tri[3 * t + 2];
         V3 lo = v3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
         V3 hi = v3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
         V3 ce = vmul(vadd(vadd(a, b), c), 1.0f / 3.0f);
         V3 da = vsub(a, ce), db = vsub(b, ce), dc = vsub(c, ce);
-        s->dt_min[t] = lo; s->dt_max[t] = hi; s->dt_center[t] = ce;
-        s->dt_radius[t] = sqrtf(fmaxf(fmaxf(vdot(da, da), vdot(db, db)), vdot(dc, dc)));
+        d->dt_min[t] = lo; d->dt_max[t] = hi; d->dt_center[t] = ce;
+        d->dt_radius[t] = sqrtf(fmaxf(fmaxf(vdot(da, da), vdot(db, db)), vdot(dc, dc)));
         if (!hashed) continue;
         float cs = fmaxf(cell, 1.0e-3f);
         int x0 = cell_of(lo.x - margin, cs), y0 = cell_of(lo.y - margin, cs), z0 = cell_of(lo.z - margin, cs);
@@ -2158,26 +2182,26 @@ static void dyn_tri_finish(OracleSolver* s, int T, int signed_mode, int motion, 
         if (!(sx > 0 && sy > 0 && sz > 0)) {
             x0 = x1 = cell_of(ce.x, cs); y0 = y1 = cell_of(ce.y, cs); z0 = z1 = cell_of(ce.z, cs);
         }
-        int* m0 = s->dt_cmin + 3 * t; int* m1 = s->dt_cmax + 3 * t;
+        int* m0 = d->dt_cmin + 3 * t; int* m1 = d->dt_cmax + 3 * t;
         m0[0] = x0; m0[1] = y0; m0[2] = z0; m1[0] = x1; m1[1] = y1; m1[2] = z1;
     }
-    if (!motion) memcpy(s->dt_prev_center, s->dt_center, sizeof(V3) * n);
-    s->dt_n = T; s->dt_signed = signed_mode; s->dt_motion = motion; s->dt_hashed = hashed; s->dt_cell = cell;
-    s->dt_large_n = 0; s->dt_max_occ = 0; s->dt_nb = 0;
+    if (!motion) memcpy(d->dt_prev_center, d->dt_center, sizeof(V3) * n);
+    d->dt_n = T; d->dt_signed = signed_mode; d->dt_motion = motion; d->dt_hashed = hashed; d->dt_cell = cell;
+    d->dt_large_n = 0; d->dt_max_occ = 0; d->dt_nb = 0;
     if (!hashed) return;
     const int nb = next_pow2(T * 4 > 1024 ? T * 4 : 1024);
-    s->dt_nb = nb;
-    s->dt_start = (int*)realloc(s->dt_start, sizeof(int) * ((size_t)nb + 1));
-    s->dt_large = (int*)realloc(s->dt_large, sizeof(int) * n);
+    d->dt_nb = nb;
+    d->dt_start = (int*)realloc(d->dt_start, sizeof(int) * ((size_t)nb + 1));
+    d->dt_large = (int*)realloc(d->dt_large, sizeof(int) * n);
     int* count = (int*)calloc((size_t)nb, sizeof(int));
     for (int pass = 0; pass < 2; ++pass) {
         for (int t = 0; t < T; ++t) {
-            const int* m0 = s->dt_cmin + 3 * t; const int* m1 = s->dt_cmax + 3 * t;
+            const int* m0 = d->dt_cmin + 3 * t; const int* m1 = d->dt_cmax + 3 * t;
             long long sx = (long long)m1[0] - m0[0] + 1, sy = (long long)m1[1] - m0[1] + 1, sz = (long long)m1[2] - m0[2] + 1;
             long long cells = (sx > 0 && sy > 0 && sz > 0) ? sx * sy * sz : 0;
             if (cells <= 0) continue;
             if (cells > MAX_PRIM_CELLS) {
-                if (pass == 0) s->dt_large[s->dt_large_n++] = t;
+                if (pass == 0) d->dt_large[d->dt_large_n++] = t;
                 continue;
             }
             for (int z = m0[2]; z <= m1[2]; ++z)
@@ -2185,24 +2209,24 @@ static void dyn_tri_finish(OracleSolver* s, int T, int signed_mode, int motion, 
                     for (int x = m0[0]; x <= m1[0]; ++x) {
                         unsigned b = bucket_of(x, y, z, nb);
                         if (pass == 0) count[b]++;
-                        else s->dt_ent[count[b]++] = t;
+                        else d->dt_ent[count[b]++] = t;
                     }
         }
         if (pass == 0) {
             int total = 0;
             for (int b = 0; b < nb; ++b) {
-                if (count[b] > s->dt_max_occ) s->dt_max_occ = count[b];
-                s->dt_start[b] = total; total += count[b]; count[b] = s->dt_start[b];
+                if (count[b] > d->dt_max_occ) d->dt_max_occ = count[b];
+                d->dt_start[b] = total; total += count[b]; count[b] = d->dt_start[b];
             }
-            s->dt_start[nb] = total;
-            s->dt_ent = (int*)realloc(s->dt_ent, sizeof(int) * (size_t)(total > 0 ? total : 1));
+            d->dt_start[nb] = total;
+            d->dt_ent = (int*)realloc(d->dt_ent, sizeof(int) * (size_t)(total > 0 ? total : 1));
         }
     }
     free(count);
 }
 
-static float dyn_tri_cell(const OracleSolver* s, float max_extent, int indexed) {
-    float margin = fmaxf(s->cfg.collision_margin, 0.0f), thick = fmaxf(s->cfg.cloth_thickness, 0.0f);
+static float dyn_tri_cell(float margin_in, float thick_in, float max_extent, int indexed) {
+    float margin = fmaxf(margin_in, 0.0f), thick = fmaxf(thick_in, 0.0f);
     float ext = fmaxf(fmaxf(max_extent + margin * 2.0f, thick), 1.0e-3f);
     if (!indexed) return ext;
     float fine = fmaxf(fmaxf(thick * 1.5f, margin * 4.0f), 0.02f);
@@ -2216,35 +2240,46 @@ static float tri_extent3(V3 a, V3 b, V3 c) {
     return e;
 }
 
-static void dyn_tri_clear(OracleSolver* s) {
-    s->dt_n = 0; s->dt_signed = 0; s->dt_motion = 0; s->dt_hashed = 0; s->dt_upload = 0; s->dt_large_n = 0; s->dt_max_occ = 0;
+static void dyn_tri_clear(ODyn* d) {
+    d->dt_n = 0; d->dt_signed = 0; d->dt_motion = 0; d->dt_hashed = 0; d->dt_upload = 0; d->dt_large_n = 0; d->dt_max_occ = 0;
 }
 
 /* abi41.cu:8333-8413 */
-int oracle_update_dynamic_triangles(OracleSolver* s, const float* tris, int count) {
-    if (!s) return set_err("invalid dynamic triangle update");
-    if (count < 0) count = 0;
-    if (count == 0) { dyn_tri_clear(s); return 1; }
-    if (!tris) return set_err("dynamic triangle data is required when triangle count is nonzero");
+static float rows_extent(const float* tris, int count) {
     float max_extent = 0.0f;
     for (int t = 0; t < count; ++t) {
         float e = tri_extent3(f3a(tris + 9 * t), f3a(tris + 9 * t + 3), f3a(tris + 9 * t + 6));
         if (isfinite(e) && e >= 0.0f) max_extent = fmaxf(max_extent, e);
     }
-    int motion = s->dt_upload == count;
-    s->dt_tri = (V3*)realloc(s->dt_tri, sizeof(V3) * 3 * (size_t)count);
-    for (int q = 0; q < 3 * count; ++q) s->dt_tri[q] = f3a(tris + 3 * q);
-    dyn_tri_finish(s, count, 0, motion, dyn_tri_cell(s, max_extent, 0));
-    s->dt_upload = count;
+    return max_extent;
+}
+
+static void dyn_put_rows(ODyn* d, const float* tris, int count) {
+    d->dt_tri = (V3*)realloc(d->dt_tri, sizeof(V3) * 3 * (size_t)count);
+    for (int q = 0; q < 3 * count; ++q) d->dt_tri[q] = f3a(tris + 3 * q);
+}
+
+int oracle_update_dynamic_triangles(OracleSolver* s, const float* tris, int count) {
+    if (!s) return set_err("invalid dynamic triangle update");
+    ODyn* d = &s->own;
+    if (count < 0) count = 0;
+    if (count == 0) { dyn_tri_clear(d); return 1; }
+    if (!tris) return set_err("dynamic triangle data is required when triangle count is nonzero");
+    float max_extent = rows_extent(tris, count);
+    int motion = d->dt_upload == count;
+    dyn_put_rows(d, tris, count);
+    dyn_tri_finish(d, s->cfg.collision_margin, count, 0, motion, dyn_tri_cell(s->cfg.collision_margin, s->cfg.cloth_thickness, max_extent, 0));
+    d->dt_upload = count;
     return 1;
 }
 
 /* abi41.cu:8415-8564, rows from indices 3663-3684 */
 int oracle_update_dynamic_indexed(OracleSolver* s, const float* verts, int vcount, const int* idx, int count, int topology_changed) {
     if (!s) return set_err("invalid dynamic indexed triangle update");
+    ODyn* d = &s->own;
     if (vcount < 0) vcount = 0;
     if (count < 0) count = 0;
-    if (vcount == 0 || count == 0) { dyn_tri_clear(s); return 1; }
+    if (vcount == 0 || count == 0) { dyn_tri_clear(d); return 1; }
     if (!verts || !idx) return set_err("dynamic indexed triangle positions and indices are required when count is nonzero");
     float max_extent = 0.0f;
     for (int t = 0; t < count; ++t) {
@@ -2253,32 +2288,32 @@ int oracle_update_dynamic_indexed(OracleSolver* s, const float* verts, int vcoun
         float e = tri_extent3(f3a(verts + 3 * a), f3a(verts + 3 * b), f3a(verts + 3 * c));
         if (isfinite(e) && e >= 0.0f) max_extent = fmaxf(max_extent, e);
     }
-    if (topology_changed || count != s->dt_idx_n || !s->dt_idx) {
-        s->dt_idx = (int*)realloc(s->dt_idx, sizeof(int) * 3 * (size_t)count);
-        memcpy(s->dt_idx, idx, sizeof(int) * 3 * (size_t)count);
-        s->dt_idx_n = count;
+    if (topology_changed || count != d->dt_idx_n || !d->dt_idx) {
+        d->dt_idx = (int*)realloc(d->dt_idx, sizeof(int) * 3 * (size_t)count);
+        memcpy(d->dt_idx, idx, sizeof(int) * 3 * (size_t)count);
+        d->dt_idx_n = count;
     }
-    int motion = !topology_changed && s->dt_upload == count;
-    s->dt_tri = (V3*)realloc(s->dt_tri, sizeof(V3) * 3 * (size_t)count);
+    int motion = !topology_changed && d->dt_upload == count;
+    d->dt_tri = (V3*)realloc(d->dt_tri, sizeof(V3) * 3 * (size_t)count);
     for (int t = 0; t < count; ++t) {
-        int a = s->dt_idx[3 * t], b = s->dt_idx[3 * t + 1], c = s->dt_idx[3 * t + 2];
+        int a = d->dt_idx[3 * t], b = d->dt_idx[3 * t + 1], c = d->dt_idx[3 * t + 2];
         if (a < 0 || b < 0 || c < 0 || a >= vcount || b >= vcount || c >= vcount) {
-            s->dt_tri[3 * t] = s->dt_tri[3 * t + 1] = s->dt_tri[3 * t + 2] = v3(0.0f, 0.0f, 0.0f);
+            d->dt_tri[3 * t] = d->dt_tri[3 * t + 1] = d->dt_tri[3 * t + 2] = v3(0.0f, 0.0f, 0.0f);
             continue;
         }
-        s->dt_tri[3 * t] = f3a(verts + 3 * a); s->dt_tri[3 * t + 1] = f3a(verts + 3 * b); s->dt_tri[3 * t + 2] = f3a(verts + 3 * c);
+        d->dt_tri[3 * t] = f3a(verts + 3 * a); d->dt_tri[3 * t + 1] = f3a(verts + 3 * b); d->dt_tri[3 * t + 2] = f3a(verts + 3 * c);
     }
-    dyn_tri_finish(s, count, 1, motion, dyn_tri_cell(s, max_extent, 1));
-    s->dt_upload = count;
+    dyn_tri_finish(d, s->cfg.collision_margin, count, 1, motion, dyn_tri_cell(s->cfg.collision_margin, s->cfg.cloth_thickness, max_extent, 1));
+    d->dt_upload = count;
     return 1;
 }
 
-/* abi41.cu:584-603 (radius signature), 8566-8696, hash 6395-6449 */
-int oracle_update_dynamic_particles(OracleSolver* s, const float* pos, const float* radii, int count) {
-    if (!s) return set_err("invalid dynamic particle update");
-    if (count < 0) count = 0;
-    if (count == 0) { s->dp_n = 0; s->dp_motion = 0; s->dp_hashed = 0; s->dp_upload = 0; s->dp_sig = 0; return 1; }
-    if (!pos || !radii) return set_err("dynamic particle position/radius data is required when particle count is nonzero");
+/* abi41.cu:584-603 (radius signature), 8566-8696, hash 6395-6449.  prev:
+ * the caller's previous positions (shared scene) or NULL to keep the last
+ * upload's positions as previous.  Returns the particles past the 16 queried
+ * slots of their buckets. */
+static long long dyn_put_particles(ODyn* d, float margin, float thickness, const float* pos, const float* prev, const float* radii,
+                                   int count) {
     uint64_t sig = 1469598103934665603ull ^ (uint64_t)count;
     float max_r = 0.0f;
     for (int q = 0; q < count; ++q) {
@@ -2288,57 +2323,153 @@ int oracle_update_dynamic_particles(OracleSolver* s, const float* pos, const flo
         uint32_t bits; memcpy(&bits, &r, 4);
         sig ^= (uint64_t)bits; sig *= 1099511628211ull;
     }
-    if (s->dp_cell <= 0.0f || s->dp_sig != sig || s->dp_upload != count) {
-        s->dp_cell = fmaxf(fmaxf(max_r + fmaxf(s->cfg.collision_margin, 0.0f), fmaxf(s->cfg.cloth_thickness, 0.0f)), 1.0e-3f);
-        s->dp_sig = sig;
+    if (d->dp_cell <= 0.0f || d->dp_sig != sig || d->dp_upload != count) {
+        d->dp_cell = fmaxf(fmaxf(max_r + fmaxf(margin, 0.0f), fmaxf(thickness, 0.0f)), 1.0e-3f);
+        d->dp_sig = sig;
     }
-    int motion = s->dp_upload == count;
+    int motion = d->dp_upload == count;
     size_t n = (size_t)count;
-    if (motion) { memcpy(s->dp_prev, s->dp_pos, sizeof(V3) * n); }
-    else s->dp_prev = (V3*)realloc(s->dp_prev, sizeof(V3) * n);
-    s->dp_pos = (V3*)realloc(s->dp_pos, sizeof(V3) * n); s->dp_rad = (float*)realloc(s->dp_rad, sizeof(float) * n);
-    for (int q = 0; q < count; ++q) { s->dp_pos[q] = f3a(pos + 3 * q); s->dp_rad[q] = radii[q]; }
-    if (!motion) memcpy(s->dp_prev, s->dp_pos, sizeof(V3) * n);
-    s->dp_n = count; s->dp_motion = motion; s->dp_hashed = count >= 128; s->dp_nb = 0;
-    if (s->dp_hashed) {
+    if (prev) {
+        d->dp_prev = (V3*)realloc(d->dp_prev, sizeof(V3) * n);
+        for (int q = 0; q < count; ++q) d->dp_prev[q] = f3a(prev + 3 * q);
+    } else if (motion) {
+        memcpy(d->dp_prev, d->dp_pos, sizeof(V3) * n);
+    } else {
+        d->dp_prev = (V3*)realloc(d->dp_prev, sizeof(V3) * n);
+    }
+    d->dp_pos = (V3*)realloc(d->dp_pos, sizeof(V3) * n); d->dp_rad = (float*)realloc(d->dp_rad, sizeof(float) * n);
+    for (int q = 0; q < count; ++q) { d->dp_pos[q] = f3a(pos + 3 * q); d->dp_rad[q] = radii[q]; }
+    if (!prev && !motion) memcpy(d->dp_prev, d->dp_pos, sizeof(V3) * n);
+    d->dp_n = count; d->dp_motion = motion; d->dp_hashed = count >= 128; d->dp_nb = 0;
+    long long overflow = 0;
+    if (d->dp_hashed) {
         int nb = next_pow2(count * 4 > 1024 ? count * 4 : 1024);
-        s->dp_nb = nb;
-        s->dp_cellc = (int*)realloc(s->dp_cellc, sizeof(int) * 3 * n);
-        s->dp_start = (int*)realloc(s->dp_start, sizeof(int) * ((size_t)nb + 1));
-        s->dp_ent = (int*)realloc(s->dp_ent, sizeof(int) * n);
+        d->dp_nb = nb;
+        d->dp_cellc = (int*)realloc(d->dp_cellc, sizeof(int) * 3 * n);
+        d->dp_start = (int*)realloc(d->dp_start, sizeof(int) * ((size_t)nb + 1));
+        d->dp_ent = (int*)realloc(d->dp_ent, sizeof(int) * n);
         int* cntb = (int*)calloc((size_t)nb, sizeof(int));
         unsigned* bk = (unsigned*)malloc(sizeof(unsigned) * n);
         for (int q = 0; q < count; ++q) {
-            int* c = s->dp_cellc + 3 * q;
-            c[0] = cell_of(s->dp_pos[q].x, s->dp_cell); c[1] = cell_of(s->dp_pos[q].y, s->dp_cell); c[2] = cell_of(s->dp_pos[q].z, s->dp_cell);
+            int* c = d->dp_cellc + 3 * q;
+            c[0] = cell_of(d->dp_pos[q].x, d->dp_cell); c[1] = cell_of(d->dp_pos[q].y, d->dp_cell); c[2] = cell_of(d->dp_pos[q].z, d->dp_cell);
             bk[q] = bucket_of(c[0], c[1], c[2], nb);
             cntb[bk[q]]++;
         }
         int total = 0;
-        for (int b = 0; b < nb; ++b) { s->dp_start[b] = total; total += cntb[b]; cntb[b] = s->dp_start[b]; }
-        s->dp_start[nb] = total;
-        for (int q = 0; q < count; ++q) s->dp_ent[cntb[bk[q]]++] = q;
+        for (int b = 0; b < nb; ++b) {
+            if (cntb[b] > 16) overflow += cntb[b] - 16;
+            d->dp_start[b] = total; total += cntb[b]; cntb[b] = d->dp_start[b];
+        }
+        d->dp_start[nb] = total;
+        for (int q = 0; q < count; ++q) d->dp_ent[cntb[bk[q]]++] = q;
         free(bk); free(cntb);
     }
-    s->dp_upload = count;
+    d->dp_upload = count;
+    return overflow;
+}
+
+static void dyn_clear_particles(ODyn* d) { d->dp_n = 0; d->dp_motion = 0; d->dp_hashed = 0; d->dp_upload = 0; d->dp_sig = 0; }
+
+int oracle_update_dynamic_particles(OracleSolver* s, const float* pos, const float* radii, int count) {
+    if (!s) return set_err("invalid dynamic particle update");
+    if (count < 0) count = 0;
+    if (count == 0) { dyn_clear_particles(&s->own); return 1; }
+    if (!pos || !radii) return set_err("dynamic particle position/radius data is required when particle count is nonzero");
+    dyn_put_particles(&s->own, s->cfg.collision_margin, s->cfg.cloth_thickness, pos, NULL, radii, count);
+    return 1;
+}
+
+/* ---- shared scene (abi41.cu:6597-6784, 8733-8789) ---- */
+OracleScene* oracle_scene_create(void) { return (OracleScene*)calloc(1, sizeof(OracleScene)); }
+
+void oracle_scene_destroy(OracleScene* g) {
+    if (!g) return;
+    odyn_free(&g->d);
+    free(g);
+}
+
+static int* copy_ints(int* dst, const int* src, int n) {
+    dst = (int*)realloc(dst, sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (n > 0) memcpy(dst, src, sizeof(int) * (size_t)n);
+    return dst;
+}
+
+int oracle_scene_update(OracleScene* g, const SsblXpbdGlobalDynamicSceneInputs* in) {
+    if (!g || !in) return set_err("invalid global dynamic scene update");
+    int P = in->particle_count > 0 ? in->particle_count : 0, T = in->triangle_count > 0 ? in->triangle_count : 0;
+    if (P > 0 && (!in->particle_positions || !in->particle_radii || !in->particle_source_ids || !in->particle_collision_layers))
+        return set_err("global dynamic particle arrays are incomplete");
+    if (T > 0 && (!in->triangle_vertices || !in->triangle_source_ids || !in->triangle_collision_layers))
+        return set_err("global dynamic triangle arrays are incomplete");
+    g->margin = fmaxf(in->collision_margin, 0.0f);
+    g->thickness = fmaxf(in->cloth_thickness, 0.0f);
+    g->overflow = 0;
+    ODyn* d = &g->d;
+    if (P == 0) {
+        dyn_clear_particles(d);
+    } else {
+        d->par_src = copy_ints(d->par_src, in->particle_source_ids, P);
+        d->par_layer = copy_ints(d->par_layer, in->particle_collision_layers, P);
+        g->overflow += dyn_put_particles(d, g->margin, g->thickness, in->particle_positions,
+                                         in->particle_prev_positions ? in->particle_prev_positions : in->particle_positions,
+                                         in->particle_radii, P);
+    }
+    if (T == 0) {
+        dyn_tri_clear(d);
+    } else {
+        d->tri_src = copy_ints(d->tri_src, in->triangle_source_ids, T);
+        d->tri_layer = copy_ints(d->tri_layer, in->triangle_collision_layers, T);
+        int motion = d->dt_upload == T;
+        dyn_put_rows(d, in->triangle_vertices, T);
+        dyn_tri_finish(d, g->margin, T, 0, motion, dyn_tri_cell(g->margin, g->thickness, rows_extent(in->triangle_vertices, T), 1));
+        d->dt_upload = T;
+    }
+    return 1;
+}
+
+int oracle_scene_attach(OracleSolver* s, OracleScene* g, int target_source_id, int target_collision_layer, int mode) {
+    if (!s || !g) return set_err("invalid global dynamic scene attach");
+    s->scene = g;
+    s->gd_src = target_source_id;
+    s->gd_layer = target_collision_layer;
+    s->gd_mode = mode;
+    return 1;
+}
+
+int oracle_scene_clear(OracleSolver* s) {
+    if (!s) return set_err("invalid global dynamic scene clear");
+    s->scene = NULL;
+    s->gd_src = s->gd_layer = s->gd_mode = 0;
+    return 1;
+}
+
+long long oracle_scene_overflow(const OracleScene* g) { return g ? g->overflow : 0; }
+
+/* abi41.cu:3984-3997 */
+static int source_enabled(const OracleSolver* s, int source, int layer) {
+    if (s->gd_mode == 0) return 1;
+    if (s->gd_src != 0 && source == s->gd_src) return 0;
+    if (s->gd_mode == 2) return layer < s->gd_layer;
     return 1;
 }
 
 typedef struct { V3 delta, vel, acc; float pen, dist, acc_w; } DynBest;
 
 /* abi41.cu:3998-4111 */
-static void dyn_tri_candidate(OracleSolver* s, int t, V3 p, float cdt, int inside, float qm, float cm, DynBest* b, unsigned* cand,
+static void dyn_tri_candidate(OracleSolver* s, const ODyn* ds, int t, V3 p, float cdt, int inside, float qm, float cm, DynBest* b, unsigned* cand,
                               unsigned* rej) {
-    if (t < 0 || t >= s->dt_n) return;
+    if (t < 0 || t >= ds->dt_n) return;
+    if (ds->tri_src && !source_enabled(s, ds->tri_src[t], ds->tri_layer ? ds->tri_layer[t] : 0)) return;
     *cand += 1;
-    V3 lo = s->dt_min[t], hi = s->dt_max[t];
+    V3 lo = ds->dt_min[t], hi = ds->dt_max[t];
     V3 q = v3(fminf(fmaxf(p.x, lo.x), hi.x), fminf(fmaxf(p.y, lo.y), hi.y), fminf(fmaxf(p.z, lo.z), hi.z));
     V3 dq = vsub(p, q);
     if (vdot(dq, dq) > qm * qm) { *rej += 1; return; }
-    V3 dc = vsub(p, s->dt_center[t]);
-    float rr = s->dt_radius[t] + qm;
+    V3 dc = vsub(p, ds->dt_center[t]);
+    float rr = ds->dt_radius[t] + qm;
     if (vdot(dc, dc) > rr * rr) { *rej += 1; return; }
-    V3 a = s->dt_tri[3 * t], bb = s->dt_tri[3 * t + 1], c = s->dt_tri[3 * t + 2];
+    V3 a = ds->dt_tri[3 * t], bb = ds->dt_tri[3 * t + 1], c = ds->dt_tri[3 * t + 2];
     V3 cp = closest_on_tri(p, a, bb, c);
     V3 d = vsub(p, cp);
     float dsq = vdot(d, d), dist = sqrtf(fmaxf(dsq, K_EPS));
@@ -2347,7 +2478,7 @@ static void dyn_tri_candidate(OracleSolver* s, int t, V3 p, float cdt, int insid
     V3 trin = vmul(tn, 1.0f / tl);
     V3 normal = dsq > K_EPS * 4.0f ? vmul(d, 1.0f / fmaxf(dist, K_EPS)) : trin;
     float pen = cm - dist;
-    if (s->dt_signed) {
+    if (ds->dt_signed) {
         float sd = vdot(d, trin);
         if (inside) {
             if (sd >= 0.001f) return;
@@ -2365,7 +2496,7 @@ static void dyn_tri_candidate(OracleSolver* s, int t, V3 p, float cdt, int insid
         }
         if (dist < b->dist) {
             V3 vel = v3(0.0f, 0.0f, 0.0f);
-            if (s->dt_motion && cdt > K_EPS) vel = vmul(vsub(s->dt_center[t], s->dt_prev_center[t]), 1.0f / cdt);
+            if (ds->dt_motion && cdt > K_EPS) vel = vmul(vsub(ds->dt_center[t], ds->dt_prev_center[t]), 1.0f / cdt);
             b->dist = dist; b->pen = pen; b->delta = delta; b->vel = vel;
         }
     } else {
@@ -2424,48 +2555,48 @@ static void dyn_signed_response(OracleSolver* s, int i, V3 p, V3 raw, V3 cvel, f
 }
 
 /* abi41.cu:4114-4323 (query and response of one vertex) */
-static void dyn_triangles(OracleSolver* s, int i, int inside, unsigned* cand, unsigned* rej) {
+static void dyn_triangles(OracleSolver* s, const ODyn* ds, int i, int inside, unsigned* cand, unsigned* rej) {
     const float sub_dt = s->dyn_sub_dt;
     const float cdt = (isfinite(s->cfg.dt) && s->cfg.dt > K_EPS) ? s->cfg.dt : fmaxf(sub_dt, K_EPS);
     float cm = fmaxf(s->cfg.collision_margin, 0.0f);
-    if (s->dt_signed) cm = fmaxf(cm, fmaxf(s->cfg.cloth_thickness, 0.0f) * 0.75f);
+    if (ds->dt_signed) cm = fmaxf(cm, fmaxf(s->cfg.cloth_thickness, 0.0f) * 0.75f);
     float qm = cm;
-    if (s->dt_signed) {
-        float animated = fmaxf(fmaxf(cm * 2.0f, 0.04f), fmaxf(s->dt_cell, 0.0f) * 1.25f);
+    if (ds->dt_signed) {
+        float animated = fmaxf(fmaxf(cm * 2.0f, 0.04f), fmaxf(ds->dt_cell, 0.0f) * 1.25f);
         qm = fminf(fmaxf(animated, cm), 0.08f);
     }
     if (cm <= 0.0f || qm <= 0.0f) return;
     V3 p = s->pos[i];
     DynBest b = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0.0f, 3.402823466e+38f, 0.0f};
-    if (s->dt_hashed) {
-        int cx = cell_of(p.x, s->dt_cell), cy = cell_of(p.y, s->dt_cell), cz = cell_of(p.z, s->dt_cell);
+    if (ds->dt_hashed) {
+        int cx = cell_of(p.x, ds->dt_cell), cy = cell_of(p.y, ds->dt_cell), cz = cell_of(p.z, ds->dt_cell);
         int R = 0;
-        if (s->dt_signed) {
+        if (ds->dt_signed) {
             if (!inside) R = 1;
-            else { float cs = fmaxf(s->dt_cell, 1.0e-3f); R = clampi((int)ceilf(fmaxf(qm, 0.0f) / cs), 1, 4); }
+            else { float cs = fmaxf(ds->dt_cell, 1.0e-3f); R = clampi((int)ceilf(fmaxf(qm, 0.0f) / cs), 1, 4); }
         }
         for (int dz = -R; dz <= R; ++dz)
             for (int dy = -R; dy <= R; ++dy)
                 for (int dx = -R; dx <= R; ++dx) {
                     int qx = cx + dx, qy = cy + dy, qz = cz + dz;
-                    unsigned bk = bucket_of(qx, qy, qz, s->dt_nb);
-                    int s0 = s->dt_start[bk], s1 = s->dt_start[bk + 1];
+                    unsigned bk = bucket_of(qx, qy, qz, ds->dt_nb);
+                    int s0 = ds->dt_start[bk], s1 = ds->dt_start[bk + 1];
                     if (s1 < s0) s1 = s0;
                     for (int k = s0; k < s1; ++k) {
-                        int t = s->dt_ent[k];
-                        if (t < 0 || t >= s->dt_n) continue;
-                        const int* lo = s->dt_cmin + 3 * t; const int* hi = s->dt_cmax + 3 * t;
+                        int t = ds->dt_ent[k];
+                        if (t < 0 || t >= ds->dt_n) continue;
+                        const int* lo = ds->dt_cmin + 3 * t; const int* hi = ds->dt_cmax + 3 * t;
                         if (qx != clampi(cx, lo[0], hi[0]) || qy != clampi(cy, lo[1], hi[1]) || qz != clampi(cz, lo[2], hi[2])) continue;
-                        dyn_tri_candidate(s, t, p, cdt, inside, qm, cm, &b, cand, rej);
+                        dyn_tri_candidate(s, ds, t, p, cdt, inside, qm, cm, &b, cand, rej);
                     }
                 }
-        for (int k = 0; k < s->dt_large_n; ++k) dyn_tri_candidate(s, s->dt_large[k], p, cdt, inside, qm, cm, &b, cand, rej);
+        for (int k = 0; k < ds->dt_large_n; ++k) dyn_tri_candidate(s, ds, ds->dt_large[k], p, cdt, inside, qm, cm, &b, cand, rej);
     } else {
-        for (int t = 0; t < s->dt_n; ++t) dyn_tri_candidate(s, t, p, cdt, inside, qm, cm, &b, cand, rej);
+        for (int t = 0; t < ds->dt_n; ++t) dyn_tri_candidate(s, ds, t, p, cdt, inside, qm, cm, &b, cand, rej);
     }
     if (!(b.pen > 0.0f)) return;
     cnt(s, C_TRI_PAIRS);
-    if (s->dt_signed) {
+    if (ds->dt_signed) {
         dyn_signed_response(s, i, p, dyn_local_average(b.acc, b.acc_w, b.delta), b.vel, b.pen, sub_dt, inside);
     } else {
         V3 applied = vmul(b.delta, 0.5f);
@@ -2484,7 +2615,7 @@ static void dyn_triangles(OracleSolver* s, int i, int inside, unsigned* cand, un
 }
 
 /* abi41.cu:4354-4511 */
-static void dyn_particles(OracleSolver* s, int i, unsigned* cand) {
+static void dyn_particles(OracleSolver* s, const ODyn* ds, int i, unsigned* cand) {
     const float sub_dt = s->dyn_sub_dt;
     const float cdt = (isfinite(s->cfg.dt) && s->cfg.dt > K_EPS) ? s->cfg.dt : fmaxf(sub_dt, K_EPS);
     V3 p = s->pos[i];
@@ -2493,28 +2624,29 @@ static void dyn_particles(OracleSolver* s, int i, unsigned* cand) {
     float best = 0.0f, acc_w = 0.0f;
     int nq = 0;
     int list[27 * 16];
-    if (s->dp_hashed) {
-        int cx = cell_of(p.x, s->dp_cell), cy = cell_of(p.y, s->dp_cell), cz = cell_of(p.z, s->dp_cell);
+    if (ds->dp_hashed) {
+        int cx = cell_of(p.x, ds->dp_cell), cy = cell_of(p.y, ds->dp_cell), cz = cell_of(p.z, ds->dp_cell);
         for (int dz = -1; dz <= 1; ++dz)
             for (int dy = -1; dy <= 1; ++dy)
                 for (int dx = -1; dx <= 1; ++dx) {
                     int qx = cx + dx, qy = cy + dy, qz = cz + dz;
-                    unsigned bk = bucket_of(qx, qy, qz, s->dp_nb);
-                    int s0 = s->dp_start[bk], n = s->dp_start[bk + 1] - s0;
+                    unsigned bk = bucket_of(qx, qy, qz, ds->dp_nb);
+                    int s0 = ds->dp_start[bk], n = ds->dp_start[bk + 1] - s0;
                     if (n > 16) n = 16;
                     for (int k = 0; k < n; ++k) {
-                        int q = s->dp_ent[s0 + k];
-                        const int* c = s->dp_cellc + 3 * q;
+                        int q = ds->dp_ent[s0 + k];
+                        const int* c = ds->dp_cellc + 3 * q;
                         if (c[0] != qx || c[1] != qy || c[2] != qz) continue;
                         list[nq++] = q;
                     }
                 }
     }
-    int total = s->dp_hashed ? nq : s->dp_n;
+    int total = ds->dp_hashed ? nq : ds->dp_n;
     for (int k = 0; k < total; ++k) {
-        int q = s->dp_hashed ? list[k] : k;
-        V3 c = s->dp_pos[q];
-        float r = fmaxf(s->dp_rad[q], 0.0f) + margin;
+        int q = ds->dp_hashed ? list[k] : k;
+        if (ds->par_src && !source_enabled(s, ds->par_src[q], ds->par_layer ? ds->par_layer[q] : 0)) continue;
+        V3 c = ds->dp_pos[q];
+        float r = fmaxf(ds->dp_rad[q], 0.0f) + margin;
         if (r <= 0.0f) continue;
         V3 d = vsub(p, c);
         float dist = sqrtf(fmaxf(vdot(d, d), K_EPS));
@@ -2523,19 +2655,19 @@ static void dyn_particles(OracleSolver* s, int i, unsigned* cand) {
         V3 n = dist > K_EPS ? vmul(d, 1.0f / dist) : v3(0.0f, 0.0f, 1.0f);
         float pen = r - dist;
         V3 delta = vmul(n, pen);
-        if (s->dt_signed && vfinite(delta)) {
+        if (ds->dt_signed && vfinite(delta)) {
             float w = fmaxf(pen, K_EPS);
             acc = vadd(acc, vmul(delta, w));
             acc_w += w;
         }
         if (pen > best) {
             V3 pv = v3(0, 0, 0);
-            if (s->dp_motion && cdt > K_EPS) pv = vmul(vsub(c, s->dp_prev[q]), 1.0f / cdt);
+            if (ds->dp_motion && cdt > K_EPS) pv = vmul(vsub(c, ds->dp_prev[q]), 1.0f / cdt);
             best = pen; bd = delta; bv = pv;
         }
     }
     if (!(best > 0.0f)) return;
-    if (s->dt_signed) dyn_signed_response(s, i, p, dyn_local_average(acc, acc_w, bd), bv, best, sub_dt, 0);
+    if (ds->dt_signed) dyn_signed_response(s, i, p, dyn_local_average(acc, acc_w, bd), bv, best, sub_dt, 0);
     else s->pos[i] = vadd(p, vmul(bd, 0.5f));
     cnt(s, C_EXACT);
     cnt(s, C_DP_CONTACTS);
@@ -2544,15 +2676,27 @@ static void dyn_particles(OracleSolver* s, int i, unsigned* cand) {
 /* One dynamic-collider stage over all vertices: which 0 unsigned triangles
  * and particles, 1 signed triangles and particles, 2 signed inside-only
  * triangles (abi41.cu:4250-4323, 4447-4538, 9234-9360). */
+/* The colliders a stage reads: the unsigned stage the shared scene when one
+ * is attached with a non-zero mode, else the cloth's own unsigned set; the
+ * signed stages the cloth's own indexed mesh (abi41.cu:9234-9360). */
+static const ODyn* stage_set(const OracleSolver* s, int which) {
+    if (which == 0) {
+        if (s->gd_mode != 0 && s->scene) return &s->scene->d;
+        return (s->own.dt_n > 0 || s->own.dp_n > 0) && !s->own.dt_signed ? &s->own : NULL;
+    }
+    return (s->own.dt_n > 0 || s->own.dp_n > 0) && s->own.dt_signed ? &s->own : NULL;
+}
+
 static void dynamic_all(OracleSolver* s, int which) {
-    if ((which == 0) == (s->dt_signed != 0)) return;
+    const ODyn* d = stage_set(s, which);
+    if (!d || (d->dt_n == 0 && d->dp_n == 0)) return;
     unsigned long long tc = 0, tr = 0, pc = 0;
 #pragma omp parallel for schedule(static) reduction(+ : tc, tr, pc)
     for (int i = 0; i < s->V; ++i) {
         if (s->inv[i] <= 0.0f) continue;
         unsigned c = 0, r = 0, q = 0;
-        if (s->dt_n > 0) dyn_triangles(s, i, which == 2, &c, &r);
-        if (which != 2 && s->dp_n > 0) dyn_particles(s, i, &q);
+        if (d->dt_n > 0) dyn_triangles(s, d, i, which == 2, &c, &r);
+        if (which != 2 && d->dp_n > 0) dyn_particles(s, d, i, &q);
         tc += c; tr += r; pc += q;
     }
     s->counts[C_DT_CAND] += tc;
@@ -2602,18 +2746,17 @@ int oracle_step(OracleSolver* s, int substeps, int iterations) {
             pin_all(s, dt);
             if (analytic) analytic_all(s, dt);
             if (sdf) sdf_all(s, dt);
-            const int dyn_any = s->dt_n > 0 || s->dp_n > 0;
-            if (last && dyn_any && !s->dt_signed) dynamic_all(s, 0);
+            if (last) dynamic_all(s, 0);
             int self_run = s->self_on && s->cfg.self_collision && last && (((st + 1) % interval) == 0 || st == substeps - 1) &&
                            s->V > 0 && s->radius > 0.0f;
             if (self_run) self_collision(s);
-            if (last && dyn_any && s->dt_signed) dynamic_all(s, 1);
+            if (last) dynamic_all(s, 1);
             if (s->pcg_on && final_c && s->strength >= 0.95f) {
                 caps(s, dt, 0, 2, 1);
                 caps(s, dt, 2, 3, 0);
                 caps(s, dt, 1, 3, 0);
             }
-            if (final_c && dyn_any && s->dt_signed)
+            if (final_c && stage_set(s, 1))
                 for (int pass = 0; pass < 6; ++pass) dynamic_all(s, 2);
             if (analytic || sdf || last || self_run) pin_all(s, dt);
         }
@@ -2671,8 +2814,9 @@ long long oracle_read_buffer(OracleSolver* s, int which, void* out, long long ma
 
 int oracle_dynamic_info(OracleSolver* s, int* o) {
     if (!s || !o) return set_err("invalid dynamic info request");
-    o[0] = s->dt_n; o[1] = s->dt_hashed ? s->dt_large_n : 0; o[2] = s->dt_hashed ? s->dt_max_occ : 0; o[3] = s->dt_hashed;
-    o[4] = s->dp_n; o[5] = s->dp_hashed;
+    const ODyn* d = &s->own;
+    o[0] = d->dt_n; o[1] = d->dt_hashed ? d->dt_large_n : 0; o[2] = d->dt_hashed ? d->dt_max_occ : 0; o[3] = d->dt_hashed;
+    o[4] = d->dp_n; o[5] = d->dp_hashed;
     return 1;
 }
 

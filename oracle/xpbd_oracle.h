@@ -31,6 +31,7 @@ extern "C" {
 #endif
 
 typedef struct OracleSolver OracleSolver;
+typedef struct OracleScene OracleScene;
 
 OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* mesh);
 void oracle_destroy(OracleSolver* s);
@@ -48,6 +49,16 @@ int oracle_update_dynamic_triangles(OracleSolver* s, const float* triangles, int
 int oracle_update_dynamic_indexed(OracleSolver* s, const float* vertices, int vertex_count, const int* indices, int count,
                                   int topology_changed);
 int oracle_update_dynamic_particles(OracleSolver* s, const float* positions, const float* radii, int count);
+/* Shared dynamic scene: colliders of many sources with source ids and
+ * collision layers; an attached solver's unsigned dynamic stage reads it
+ * through its source filter (mode 0: own colliders, 1: all but its own
+ * source, 2: only lower layers). */
+OracleScene* oracle_scene_create(void);
+void oracle_scene_destroy(OracleScene* g);
+int oracle_scene_update(OracleScene* g, const SsblXpbdGlobalDynamicSceneInputs* inputs);
+int oracle_scene_attach(OracleSolver* s, OracleScene* g, int target_source_id, int target_collision_layer, int mode);
+int oracle_scene_clear(OracleSolver* s);
+long long oracle_scene_overflow(const OracleScene* g);
 int oracle_step(OracleSolver* s, int substeps, int iterations);
 int oracle_download_positions(OracleSolver* s, float* out, int max_floats);
 int oracle_download_state(OracleSolver* s, float* pos3, float* prev3, float* vel3);

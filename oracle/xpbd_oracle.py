@@ -44,6 +44,12 @@ def load():
         "oracle_update_dynamic_triangles": (ci, [vp, pf, ci]),
         "oracle_update_dynamic_indexed": (ci, [vp, pf, ci, pi, ci, ci]),
         "oracle_update_dynamic_particles": (ci, [vp, pf, pf, ci]),
+        "oracle_scene_create": (vp, []),
+        "oracle_scene_destroy": (None, [vp]),
+        "oracle_scene_update": (ci, [vp, vp]),
+        "oracle_scene_attach": (ci, [vp, vp, ci, ci, ci]),
+        "oracle_scene_clear": (ci, [vp]),
+        "oracle_scene_overflow": (ctypes.c_longlong, [vp]),
         "oracle_step": (ci, [vp, ci, ci]),
         "oracle_download_positions": (ci, [vp, pf, ci]),
         "oracle_download_state": (ci, [vp, pf, pf, pf]),
@@ -151,6 +157,14 @@ class OracleSolver:
             r = np.ascontiguousarray(np.asarray(rad, np.float32).reshape(-1))
             self._check(self._lib.oracle_update_dynamic_particles(self._h, _fp(p), _fp(r), len(p)))
 
+    def attach_global_scene(self, scene, target_source_id=0, target_collision_layer=0, mode=1):
+        self._check(self._lib.oracle_scene_attach(self._h, scene._h, int(target_source_id), int(target_collision_layer), int(mode)))
+        self._scene_ref = scene
+
+    def clear_global_scene(self):
+        self._check(self._lib.oracle_scene_clear(self._h))
+        self._scene_ref = None
+
     def step(self, substeps, iterations):
         self._check(self._lib.oracle_step(self._h, int(substeps), int(iterations)))
 
@@ -185,6 +199,42 @@ class OracleSolver:
         self._check(self._lib.oracle_dynamic_info(self._h, _ip(out)))
         return {"triangles": int(out[0]), "large": int(out[1]), "max_occupancy": int(out[2]), "tri_hashed": bool(out[3]),
                 "particles": int(out[4]), "par_hashed": bool(out[5])}
+
+
+class OracleScene:
+    """Shared dynamic scene of the oracle (same arguments as
+    xpbd_gb300.native.GlobalDynamicScene)."""
+
+    def __init__(self):
+        self._lib = load()
+        self._h = self._lib.oracle_scene_create()
+
+    def update(self, triangles=None, particles=None, margin: float = 0.0, thickness: float = 0.0):
+        import sys
+
+        pkg = os.path.join(os.path.dirname(HERE), "ssbl-cuda-xpbd_gb300")
+        if pkg not in sys.path:
+            sys.path.insert(0, pkg)
+        from xpbd_gb300.native import scene_inputs
+
+        fi, keep = scene_inputs(triangles, particles, margin, thickness)
+        if not self._lib.oracle_scene_update(self._h, ctypes.addressof(fi)):
+            raise OracleError(self._lib.oracle_last_error().decode())
+        del keep
+
+    def overflow(self) -> int:
+        return int(self._lib.oracle_scene_overflow(self._h))
+
+    def close(self):
+        if self._h:
+            self._lib.oracle_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def set_threads(n: int) -> int:

@@ -155,47 +155,39 @@ extern "C" SSBL_API unsigned int ssbl_capabilities(void) {
     return SSBL_CAP_STRETCH_OPTIMIZATION | SSBL_CAP_PIN_WEIGHTS | SSBL_CAP_GLOBAL_DYNAMIC_SCENE;
 }
 
-// The global dynamic scene shares dynamic colliders between cloths; this
-// build keeps the handle life cycle and rejects cross-cloth collision modes.
-namespace {
-struct GlobalScene {
-    int particle_count = 0;
-    int triangle_count = 0;
-};
-}  // namespace
-
+// Shared dynamic scene (abi41.cu:6597-6784, 8733-8789): colliders of many
+// sources hashed once and read by every attached cloth through its source
+// filter.  Attaching with mode 0 keeps the cloth on its own colliders.
 extern "C" SSBL_API void* ssbl_create_global_dynamic_scene(void) {
     g_error.clear();
-    return new GlobalScene();
+    return scene_create();
 }
 
 extern "C" SSBL_API int ssbl_destroy_global_dynamic_scene(void* scene) {
     g_error.clear();
-    delete reinterpret_cast<GlobalScene*>(scene);
+    scene_destroy(reinterpret_cast<GlobalScene*>(scene));
     return 1;
 }
 
 extern "C" SSBL_API int ssbl_update_global_dynamic_scene(void* scene, const SsblXpbdGlobalDynamicSceneInputs* in) {
     g_error.clear();
-    GlobalScene* G = reinterpret_cast<GlobalScene*>(scene);
-    if (!G || !in) return fail("invalid global dynamic scene update") ? 1 : 0;
-    G->particle_count = std::max(in->particle_count, 0);
-    G->triangle_count = std::max(in->triangle_count, 0);
-    return 1;
+    return ok_or_zero(scene_update(reinterpret_cast<GlobalScene*>(scene), in));
 }
 
-extern "C" SSBL_API int ssbl_attach_global_dynamic_scene(void* handle, void* scene, int, int, int collision_mode) {
+extern "C" SSBL_API int ssbl_attach_global_dynamic_scene(void* handle, void* scene, int target_source_id, int target_collision_layer,
+                                                         int collision_mode) {
     g_error.clear();
-    if (!handle || !scene) return fail("invalid global dynamic scene attach") ? 1 : 0;
-    GlobalScene* G = reinterpret_cast<GlobalScene*>(scene);
-    if (collision_mode != 0 && (G->particle_count > 0 || G->triangle_count > 0))
-        return fail("cross-cloth collision through the global dynamic scene is not supported by this build of the GB300 solver") ? 1 : 0;
-    return 1;
+    Solver* S = as_solver(handle);
+    if (!S || !scene) return fail("invalid global dynamic scene attach") ? 1 : 0;
+    return ok_or_zero(scene_attach(S, -1, reinterpret_cast<GlobalScene*>(scene), target_source_id, target_collision_layer, collision_mode));
 }
 
 extern "C" SSBL_API int ssbl_clear_global_dynamic_scene(void* handle) {
     g_error.clear();
-    return handle ? 1 : (fail("invalid solver handle") ? 1 : 0);
+    Solver* S = as_solver(handle);
+    if (!S) return fail("invalid global dynamic scene clear") ? 1 : 0;
+    scene_detach(S, -1);
+    return 1;
 }
 
 extern "C" SSBL_API const char* ssbl_last_error(void) { return g_error.c_str(); }
@@ -278,6 +270,23 @@ XG_EXPORT int xpbd_gb300_batch_download_positions(void* handle, int cloth, float
     if (!S || cloth < 0 || cloth >= S->K) return fail("invalid position download") ? 1 : 0;
     cloth = S->ext2int[cloth];
     return ok_or_zero(download_positions(S, cloth, out, max_floats));
+}
+
+XG_EXPORT int xpbd_gb300_batch_attach_global_dynamic_scene(void* handle, int cloth, void* scene, int target_source_id,
+                                                           int target_collision_layer, int collision_mode) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S || !scene || cloth < 0 || cloth >= S->K) return fail("invalid global dynamic scene attach") ? 1 : 0;
+    return ok_or_zero(scene_attach(S, S->ext2int[cloth], reinterpret_cast<GlobalScene*>(scene), target_source_id,
+                                   target_collision_layer, collision_mode));
+}
+
+XG_EXPORT int xpbd_gb300_batch_clear_global_dynamic_scene(void* handle, int cloth) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S || cloth < 0 || cloth >= S->K) return fail("invalid global dynamic scene clear") ? 1 : 0;
+    scene_detach(S, S->ext2int[cloth]);
+    return 1;
 }
 
 XG_EXPORT int xpbd_gb300_batch_reset_cloth(void* handle, int cloth) {

@@ -135,6 +135,15 @@ __global__ void k_dyn_sort_buckets(const int* start, int* ent, int nb) {
         }
 }
 
+// Particles past the 16 queried per bucket (the reference counts one
+// overflow per insertion into a full bucket, abi41.cu:4350).
+__global__ void k_dyn_overflow(const int* start, int nb, unsigned long long* out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int n = start[b + 1] - start[b];
+    if (n > kParSlots) atomicAdd(out, (unsigned long long)(n - kParSlots));
+}
+
 // Indexed mesh: triangle rows from the vertex and index arrays; an index
 // out of range gives a degenerate triangle at the origin (abi41.cu:3663-3684).
 __global__ void k_dyn_from_indices(const float4* verts, int nv, const int* idx, int T, float4* tris) {
@@ -163,10 +172,20 @@ __device__ __forceinline__ float point_box_sq(F3 p, F3 lo, F3 hi) {
     return dot3(d, d);
 }
 
+// Source filter of the shared scene (abi41.cu:3984-3997): the target's own
+// source is skipped, and mode 2 keeps only lower collision layers.
+__device__ __forceinline__ bool source_enabled(const Params& P, int source, int layer) {
+    if (P.gd_mode == 0) return true;
+    if (P.gd_target_source != 0 && source == P.gd_target_source) return false;
+    if (P.gd_mode == 2) return layer < P.gd_target_layer;
+    return true;
+}
+
 // One candidate triangle (abi41.cu:3998-4111).
-__device__ void dyn_tri_candidate(const DynSet& D, int t, F3 p, float collider_dt, bool inside, float qm, float cm, DynBest* b,
-                                  unsigned* candidates, unsigned* rejects) {
+__device__ void dyn_tri_candidate(const Params& P, const DynSet& D, int t, F3 p, float collider_dt, bool inside, float qm, float cm,
+                                  DynBest* b, unsigned* candidates, unsigned* rejects) {
     if (t < 0 || t >= D.tri_count) return;
+    if (D.tri_src && !source_enabled(P, D.tri_src[t], D.tri_layer ? D.tri_layer[t] : 0)) return;
     *candidates += 1;
     if (point_box_sq(p, f3(D.amin[t]), f3(D.amax[t])) > qm * qm) {
         *rejects += 1;
@@ -325,12 +344,12 @@ __device__ void dyn_triangles(const View& v, const Params& P, const DynSet& D, i
                         const int4 lo = D.cmin[t], hi = D.cmax[t];
                         if (qx != min(max(cx, lo.x), hi.x) || qy != min(max(cy, lo.y), hi.y) || qz != min(max(cz, lo.z), hi.z))
                             continue;
-                        dyn_tri_candidate(D, t, p, collider_dt, inside, qm, cm, &b, &candidates, &rejects);
+                        dyn_tri_candidate(P, D, t, p, collider_dt, inside, qm, cm, &b, &candidates, &rejects);
                     }
                 }
-        for (int k = 0; k < D.large_count; ++k) dyn_tri_candidate(D, D.large[k], p, collider_dt, inside, qm, cm, &b, &candidates, &rejects);
+        for (int k = 0; k < D.large_count; ++k) dyn_tri_candidate(P, D, D.large[k], p, collider_dt, inside, qm, cm, &b, &candidates, &rejects);
     } else {
-        for (int t = 0; t < D.tri_count; ++t) dyn_tri_candidate(D, t, p, collider_dt, inside, qm, cm, &b, &candidates, &rejects);
+        for (int t = 0; t < D.tri_count; ++t) dyn_tri_candidate(P, D, t, p, collider_dt, inside, qm, cm, &b, &candidates, &rejects);
     }
     warp_count(v.counts, kCntDynTriCandidates, candidates);
     warp_count(v.counts, kCntDynTriAabbRejects, rejects);
@@ -366,6 +385,7 @@ __device__ void dyn_particles(const View& v, const Params& P, const DynSet& D, i
     unsigned candidates = 0;
     auto consider = [&](int k) {
         if (k < 0 || k >= D.par_count) return;
+        if (D.par_src && !source_enabled(P, D.par_src[k], D.par_layer ? D.par_layer[k] : 0)) return;
         const F3 c = f3(D.par_pos[k]);
         const float r = fmaxf(D.par_radius[k], 0.0f) + margin;
         if (r <= 0.0f) return;
@@ -425,10 +445,18 @@ __global__ void __launch_bounds__(kMaxBlock) k_dynamic(View v, int which) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nV) return;
     const Params& P = params_v(v, i);
-    if (!P.active || !P.dyn) return;
+    if (!P.active) return;
+    // the unsigned stage reads the shared scene when one is attached, else
+    // the cloth's own unsigned colliders; the signed stages read the cloth's
+    // own indexed mesh (abi41.cu:9234-9360)
+    const DynSet* Dp = nullptr;
+    if (which == 0)
+        Dp = (P.gd_mode != 0 && P.gdyn) ? P.gdyn : ((P.dyn && !P.dyn->signed_mode) ? P.dyn : nullptr);
+    else
+        Dp = (P.dyn && P.dyn->signed_mode) ? P.dyn : nullptr;
+    if (!Dp) return;
     if (__ldg(&v.inv_mass[i]) <= 0.0f) return;
-    const DynSet& D = *P.dyn;
-    if ((which == 0) == (D.signed_mode != 0)) return;
+    const DynSet& D = *Dp;
     if (D.tri_count > 0) dyn_triangles(v, P, D, i, which == 2);
     if (which != 2 && D.par_count > 0) dyn_particles(v, P, D, i);
 }
@@ -444,24 +472,40 @@ namespace host {
 
 namespace {
 
+// Where an upload allocates and launches: the owner's stream and device byte
+// account, and the margin / thickness that size the hash cells and spans
+// (the cloth's configuration, or a shared scene's own values).
+struct DynCtx {
+    cudaStream_t st;
+    long long* bytes;
+    float margin;
+    float thickness;
+};
+
+DynCtx cloth_ctx(Solver* S, int k) {
+    const SsblXpbdConfig& c = S->cl[k].cfg;
+    return DynCtx{S->stream, &S->device_bytes, std::max(c.collision_margin, 0.0f), std::max(c.cloth_thickness, 0.0f)};
+}
+
 // (Re)allocate a device array of at least n elements; the old contents are
-// dropped.  Frames in flight are finished first.
+// dropped.  Work in flight on the owner's stream is finished first.
 template <class T>
-bool realloc_dev(Solver* S, T** p, size_t old_n, size_t n, const char* what) {
+bool realloc_dev(const DynCtx& c, T** p, size_t old_n, size_t n, const char* what) {
     if (*p) {
-        if (!cuda_ok(cudaStreamSynchronize(S->stream), what)) return false;
+        if (!cuda_ok(cudaStreamSynchronize(c.st), what)) return false;
         cudaFree(*p);
-        S->device_bytes -= (long long)(sizeof(T) * old_n);
+        *c.bytes -= (long long)(sizeof(T) * old_n);
         *p = nullptr;
     }
     return dalloc(p, std::max<size_t>(n, 1), what);
 }
 
 // Cell size of a triangle source (abi41.cu:8319-8331): the largest triangle
-// extent plus two margins for plain meshes; finer for indexed meshes.
-float tri_cell_size(float max_extent, float margin, float thickness, bool indexed) {
+// extent plus two margins for plain meshes; finer for indexed meshes and the
+// shared scene.
+float tri_cell_size(float max_extent, float margin, float thickness, bool fine_cells) {
     const float extent_cell = std::max(std::max(max_extent + margin * 2.0f, thickness), 1.0e-3f);
-    if (!indexed) return extent_cell;
+    if (!fine_cells) return extent_cell;
     const float fine = std::max(std::max(thickness * 1.5f, margin * 4.0f), 0.02f);
     return std::max(std::min(extent_cell, fine), 1.0e-3f);
 }
@@ -473,22 +517,29 @@ float tri_extent(const float* a, const float* b, const float* c) {
     return std::max(hx - lx, std::max(hy - ly, hz - lz));
 }
 
-// Bounds, cell spans and (>= 64 triangles) the hash of a cloth's triangles
-// after their rows are in D.tris (abi41.cu:3686-3760, 6220-6392).
-bool finish_triangles(Solver* S, int k, int T, bool signed_mode, bool motion_valid, float cell) {
-    Cloth& C = S->cl[k];
-    DynHost& D = C.dyn;
-    cudaStream_t st = S->stream;
+float rows_max_extent(const float* tris, int count) {
+    float m = 0.0f;
+    for (int t = 0; t < count; ++t) {
+        const float e = tri_extent(tris + 9 * t, tris + 9 * t + 3, tris + 9 * t + 6);
+        if (std::isfinite(e) && e >= 0.0f) m = std::max(m, e);
+    }
+    return m;
+}
+
+// Bounds, cell spans and (>= 64 triangles) the hash of the triangles whose
+// rows are in D.tris (abi41.cu:3686-3760, 6220-6392).
+bool finish_triangles(const DynCtx& c, DynHost& D, int T, bool signed_mode, bool motion_valid, float cell) {
+    cudaStream_t st = c.st;
     const bool hashed = T >= kTriHashMin;
     if (T > D.bounds_cap) {
         const size_t o = (size_t)D.bounds_cap, n = (size_t)T;
-        if (!realloc_dev(S, &D.amin, o, n, "dynamic triangle bounds") || !realloc_dev(S, &D.amax, o, n, "dynamic triangle bounds") ||
-            !realloc_dev(S, &D.center, o, n, "dynamic triangle bounds") ||
-            !realloc_dev(S, &D.prev_center, o, n, "dynamic triangle bounds") ||
-            !realloc_dev(S, &D.radius, o, n, "dynamic triangle bounds") || !realloc_dev(S, &D.cmin, o, n, "dynamic triangle cells") ||
-            !realloc_dev(S, &D.cmax, o, n, "dynamic triangle cells") || !realloc_dev(S, &D.large, o, n, "dynamic triangle large list") ||
-            !realloc_dev(S, &D.lflag, o, n, "dynamic triangle large list") ||
-            !realloc_dev(S, &D.lpos, o + 1, n + 1, "dynamic triangle large list"))
+        if (!realloc_dev(c, &D.amin, o, n, "dynamic triangle bounds") || !realloc_dev(c, &D.amax, o, n, "dynamic triangle bounds") ||
+            !realloc_dev(c, &D.center, o, n, "dynamic triangle bounds") ||
+            !realloc_dev(c, &D.prev_center, o, n, "dynamic triangle bounds") ||
+            !realloc_dev(c, &D.radius, o, n, "dynamic triangle bounds") || !realloc_dev(c, &D.cmin, o, n, "dynamic triangle cells") ||
+            !realloc_dev(c, &D.cmax, o, n, "dynamic triangle cells") || !realloc_dev(c, &D.large, o, n, "dynamic triangle large list") ||
+            !realloc_dev(c, &D.lflag, o, n, "dynamic triangle large list") ||
+            !realloc_dev(c, &D.lpos, o + 1, n + 1, "dynamic triangle large list"))
             return false;
         D.bounds_cap = T;
     }
@@ -496,8 +547,8 @@ bool finish_triangles(Solver* S, int k, int T, bool signed_mode, bool motion_val
     if (motion_valid &&
         !cuda_ok(cudaMemcpyAsync(D.prev_center, D.center, sizeof(float4) * T, cudaMemcpyDeviceToDevice, st), "keep dynamic centres"))
         return false;
-    k_dyn_bounds<<<dyn_blocks(T), kThreadsDyn, 0, st>>>(D.tris, T, cell, std::max(C.cfg.collision_margin, 0.0f), hashed, D.amin,
-                                                         D.amax, D.center, D.radius, D.cmin, D.cmax);
+    k_dyn_bounds<<<dyn_blocks(T), kThreadsDyn, 0, st>>>(D.tris, T, cell, c.margin, hashed, D.amin, D.amax, D.center, D.radius,
+                                                         D.cmin, D.cmax);
     if (!motion_valid &&
         !cuda_ok(cudaMemcpyAsync(D.prev_center, D.center, sizeof(float4) * T, cudaMemcpyDeviceToDevice, st), "init dynamic centres"))
         return false;
@@ -515,9 +566,9 @@ bool finish_triangles(Solver* S, int k, int T, bool signed_mode, bool motion_val
         const int nb = next_pow2(std::max(1024, T * 4));
         if (nb > D.tb_cap) {
             const size_t o = (size_t)D.tb_cap;
-            if (!realloc_dev(S, &D.tcount, o, (size_t)nb, "dynamic triangle hash") ||
-                !realloc_dev(S, &D.tstart, o + 1, (size_t)nb + 1, "dynamic triangle hash") ||
-                !realloc_dev(S, &D.scan_tmp, o / 4096 + 2, (size_t)nb / 4096 + 2, "dynamic triangle hash"))
+            if (!realloc_dev(c, &D.tcount, o, (size_t)nb, "dynamic triangle hash") ||
+                !realloc_dev(c, &D.tstart, o + 1, (size_t)nb + 1, "dynamic triangle hash") ||
+                !realloc_dev(c, &D.scan_tmp, o / 4096 + 2, (size_t)nb / 4096 + 2, "dynamic triangle hash"))
                 return false;
             D.tb_cap = nb;
         }
@@ -534,7 +585,7 @@ bool finish_triangles(Solver* S, int k, int T, bool signed_mode, bool motion_val
             !cuda_ok(cudaStreamSynchronize(st), "dynamic triangle hash"))
             return false;
         if (got[0] > D.tent_cap) {
-            if (!realloc_dev(S, &D.tent, (size_t)D.tent_cap, (size_t)got[0], "dynamic triangle hash")) return false;
+            if (!realloc_dev(c, &D.tent, (size_t)D.tent_cap, (size_t)got[0], "dynamic triangle hash")) return false;
             D.tent_cap = got[0];
         }
         k_dyn_tri_hash<<<dyn_blocks(T), kThreadsDyn, 0, st>>>(T, D.cmin, D.cmax, nb, D.tcount, D.tent, true, nullptr, nullptr);
@@ -559,18 +610,15 @@ bool finish_triangles(Solver* S, int k, int T, bool signed_mode, bool motion_val
     return cuda_ok(cudaGetLastError(), "dynamic triangle hash");
 }
 
-// Copy the descriptor to the device and point the cloth's parameters at it
-// (null when the cloth has no dynamic collider).
-bool publish(Solver* S, int k) {
-    DynHost& D = S->cl[k].dyn;
-    if (!D.dev && !dalloc(&D.dev, 1, "dynamic collider descriptor")) return false;
-    if (!dupload(D.dev, &D.h, 1, S->stream, "dynamic collider descriptor") ||
-        !cuda_ok(cudaStreamSynchronize(S->stream), "dynamic collider upload"))
-        return false;
-    const bool any = D.h.tri_count > 0 || D.h.par_count > 0;
-    S->hp[k].dyn = any ? D.dev : nullptr;
-    S->params_dirty = true;
-    return true;
+// Plain triangle rows (9 floats each) into D.tris.
+bool put_rows(const DynCtx& c, DynHost& D, const float* tris, int count) {
+    if (count > D.tris_cap) {
+        if (!realloc_dev(c, &D.tris, (size_t)D.tris_cap * 3, (size_t)count * 3, "dynamic triangle upload")) return false;
+        D.tris_cap = count;
+    }
+    std::vector<float4> rows((size_t)count * 3);
+    for (int q = 0; q < count * 3; ++q) rows[q] = make_float4(tris[3 * q], tris[3 * q + 1], tris[3 * q + 2], 0.0f);
+    return dupload(D.tris, rows.data(), rows.size(), c.st, "dynamic triangle upload");
 }
 
 void clear_triangles(DynHost& D) {
@@ -584,10 +632,111 @@ void clear_triangles(DynHost& D) {
     D.max_occupancy = 0;
 }
 
-}  // namespace
+void clear_particles(DynHost& D) {
+    D.h.par_count = 0;
+    D.h.par_motion_valid = 0;
+    D.h.par_hashed = 0;
+    D.par_upload_count = 0;
+    D.radius_signature = 0;
+}
 
-void free_dynamic(Cloth& C) {
-    DynHost& D = C.dyn;
+// Particles (abi41.cu:8566-8696, 6595-6665 for the shared scene; hash
+// 6395-6449).  prev: the previous positions given by the caller (the shared
+// scene), or null to keep the last upload's positions as previous.
+bool put_particles(const DynCtx& c, DynHost& D, const float* pos, const float* prev, const float* radii, int count,
+                   unsigned long long* overflow_out) {
+    uint64_t sig = 1469598103934665603ull ^ (uint64_t)count;
+    float max_r = 0.0f;
+    std::vector<float4> p4(count), q4;
+    for (int q = 0; q < count; ++q) {
+        float r = std::isfinite(radii[q]) ? radii[q] : 0.0f;
+        r = std::max(r, 0.0f);
+        max_r = std::max(max_r, r);
+        uint32_t bits;
+        std::memcpy(&bits, &r, 4);
+        sig ^= (uint64_t)bits;
+        sig *= 1099511628211ull;
+        p4[q] = make_float4(pos[3 * q], pos[3 * q + 1], pos[3 * q + 2], 0.0f);
+    }
+    DynSet& h = D.h;
+    cudaStream_t st = c.st;
+    if (h.par_cell <= 0.0f || D.radius_signature != sig || D.par_upload_count != count) {
+        h.par_cell = std::max(std::max(max_r + c.margin, c.thickness), 1.0e-3f);
+        D.radius_signature = sig;
+    }
+    const bool motion = D.par_upload_count == count;
+    if (count > D.par_cap) {
+        const size_t o = (size_t)D.par_cap, n = (size_t)count;
+        if (!realloc_dev(c, &D.ppos, o, n, "dynamic particle upload") || !realloc_dev(c, &D.pprev, o, n, "dynamic particle upload") ||
+            !realloc_dev(c, &D.prad, o, n, "dynamic particle upload") || !realloc_dev(c, &D.pcell, o, n, "dynamic particle hash") ||
+            !realloc_dev(c, &D.pent, o, n, "dynamic particle hash"))
+            return false;
+        D.par_cap = count;
+    }
+    if (prev) {
+        q4.resize(count);
+        for (int q = 0; q < count; ++q) q4[q] = make_float4(prev[3 * q], prev[3 * q + 1], prev[3 * q + 2], 0.0f);
+        if (!dupload(D.pprev, q4.data(), (size_t)count, st, "dynamic particle previous upload")) return false;
+    } else if (motion && !cuda_ok(cudaMemcpyAsync(D.pprev, D.ppos, sizeof(float4) * count, cudaMemcpyDeviceToDevice, st),
+                                  "keep dynamic particle positions")) {
+        return false;
+    }
+    if (!dupload(D.ppos, p4.data(), (size_t)count, st, "dynamic particle upload") ||
+        !dupload(D.prad, radii, (size_t)count, st, "dynamic particle radius upload"))
+        return false;
+    if (!prev && !motion &&
+        !cuda_ok(cudaMemcpyAsync(D.pprev, D.ppos, sizeof(float4) * count, cudaMemcpyDeviceToDevice, st), "init dynamic particle positions"))
+        return false;
+    h.par_count = count;
+    h.par_motion_valid = motion ? 1 : 0;
+    h.par_hashed = count >= kParHashMin ? 1 : 0;
+    h.par_buckets = 0;
+    if (h.par_hashed) {
+        const int nb = next_pow2(std::max(1024, count * 4));
+        if (nb > D.pb_cap) {
+            const size_t o = (size_t)D.pb_cap;
+            if (!realloc_dev(c, &D.pcount, o, (size_t)nb, "dynamic particle hash") ||
+                !realloc_dev(c, &D.pstart, o + 1, (size_t)nb + 1, "dynamic particle hash") ||
+                !realloc_dev(c, &D.pscan, o / 4096 + 2, (size_t)nb / 4096 + 2, "dynamic particle hash"))
+                return false;
+            D.pb_cap = nb;
+        }
+        if (!cuda_ok(cudaMemsetAsync(D.pcount, 0, sizeof(int) * nb, st), "reset dynamic particle hash")) return false;
+        k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, D.pcell, D.pcount, nullptr, false);
+        scan_bucket_counts(D.pcount, D.pstart, nb, D.pscan, st);
+        k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, D.pcell, D.pcount, D.pent, true);
+        k_dyn_sort_buckets<<<dyn_blocks(nb), kThreadsDyn, 0, st>>>(D.pstart, D.pent, nb);
+        if (overflow_out) k_dyn_overflow<<<dyn_blocks(nb), kThreadsDyn, 0, st>>>(D.pstart, nb, overflow_out);
+        h.par_buckets = nb;
+    }
+    h.par_pos = D.ppos;
+    h.par_prev = D.pprev;
+    h.par_radius = D.prad;
+    h.par_cellc = D.pcell;
+    h.pstart = D.pstart;
+    h.pent = D.pent;
+    D.par_upload_count = count;
+    return cuda_ok(cudaGetLastError(), "dynamic particle hash");
+}
+
+// Copy the descriptor to the device (allocated on first use).
+bool publish_set(const DynCtx& c, DynHost& D) {
+    if (!D.dev && !dalloc(&D.dev, 1, "dynamic collider descriptor")) return false;
+    return dupload(D.dev, &D.h, 1, c.st, "dynamic collider descriptor") && cuda_ok(cudaStreamSynchronize(c.st), "dynamic collider upload");
+}
+
+// Point the cloth's parameters at its descriptor (null when it has no
+// dynamic collider).
+bool publish(Solver* S, int k) {
+    DynHost& D = S->cl[k].dyn;
+    if (!publish_set(cloth_ctx(S, k), D)) return false;
+    const bool any = D.h.tri_count > 0 || D.h.par_count > 0;
+    S->hp[k].dyn = any ? D.dev : nullptr;
+    S->params_dirty = true;
+    return true;
+}
+
+void free_set(DynHost& D) {
     void* ptrs[] = {D.tris, D.verts, D.idx, D.amin, D.amax, D.center, D.prev_center, D.radius, D.cmin, D.cmax, D.large, D.lflag,
                     D.lpos, D.tcount, D.tstart, D.tent, D.scan_tmp, D.small, D.ppos, D.pprev, D.prad, D.pcell, D.pcount, D.pstart,
                     D.pent, D.pscan, D.dev};
@@ -595,6 +744,10 @@ void free_dynamic(Cloth& C) {
         if (p) cudaFree(p);
     D = DynHost{};
 }
+
+}  // namespace
+
+void free_dynamic(Cloth& C) { free_set(C.dyn); }
 
 // Plain dynamic triangles (unsigned response), 9 floats per triangle
 // (abi41.cu:8333-8413).
@@ -604,13 +757,7 @@ bool upload_dynamic_triangles(Solver* S, int cloth, const float* tris, int count
     if (count > 0 && !tris) return fail("dynamic triangle data is required when triangle count is nonzero");
     const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
     AllocAccount account(&S->device_bytes);
-    float max_extent = 0.0f;
-    for (int t = 0; t < count; ++t) {
-        const float e = tri_extent(tris + 9 * t, tris + 9 * t + 3, tris + 9 * t + 6);
-        if (std::isfinite(e) && e >= 0.0f) max_extent = std::max(max_extent, e);
-    }
-    std::vector<float4> rows((size_t)count * 3);
-    for (int q = 0; q < count * 3; ++q) rows[q] = make_float4(tris[3 * q], tris[3 * q + 1], tris[3 * q + 2], 0.0f);
+    const float max_extent = rows_max_extent(tris, count);
     for (int k = k0; k < k1; ++k) {
         DynHost& D = S->cl[k].dyn;
         if (count == 0) {
@@ -618,15 +765,10 @@ bool upload_dynamic_triangles(Solver* S, int cloth, const float* tris, int count
             if (!publish(S, k)) return false;
             continue;
         }
-        const SsblXpbdConfig& c = S->cl[k].cfg;
-        const float cell = tri_cell_size(max_extent, std::max(c.collision_margin, 0.0f), std::max(c.cloth_thickness, 0.0f), false);
+        const DynCtx c = cloth_ctx(S, k);
         const bool motion = D.tri_upload_count == count;
-        if (count > D.tris_cap) {
-            if (!realloc_dev(S, &D.tris, (size_t)D.tris_cap * 3, (size_t)count * 3, "dynamic triangle upload")) return false;
-            D.tris_cap = count;
-        }
-        if (!dupload(D.tris, rows.data(), rows.size(), S->stream, "dynamic triangle upload") ||
-            !finish_triangles(S, k, count, false, motion, cell))
+        if (!put_rows(c, D, tris, count) ||
+            !finish_triangles(c, D, count, false, motion, tri_cell_size(max_extent, c.margin, c.thickness, false)))
             return false;
         D.tri_upload_count = count;
         if (!publish(S, k)) return false;
@@ -661,122 +803,180 @@ bool upload_dynamic_indexed(Solver* S, int cloth, const float* verts, int vcount
     for (int i = 0; i < vcount; ++i) v4[i] = make_float4(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2], 0.0f);
     for (int k = k0; k < k1; ++k) {
         DynHost& D = S->cl[k].dyn;
-        const SsblXpbdConfig& cf = S->cl[k].cfg;
-        const float cell = tri_cell_size(max_extent, std::max(cf.collision_margin, 0.0f), std::max(cf.cloth_thickness, 0.0f), true);
+        const DynCtx cx = cloth_ctx(S, k);
         if (vcount > D.verts_cap) {
-            if (!realloc_dev(S, &D.verts, (size_t)D.verts_cap, (size_t)vcount, "dynamic triangle vertex upload")) return false;
+            if (!realloc_dev(cx, &D.verts, (size_t)D.verts_cap, (size_t)vcount, "dynamic triangle vertex upload")) return false;
             D.verts_cap = vcount;
         }
         if (!dupload(D.verts, v4.data(), (size_t)vcount, S->stream, "dynamic triangle vertex upload")) return false;
         if (topology_changed || count != D.topology_count || count > D.idx_cap) {
             if (count > D.idx_cap) {
-                if (!realloc_dev(S, &D.idx, (size_t)D.idx_cap * 3, (size_t)count * 3, "dynamic triangle index upload")) return false;
+                if (!realloc_dev(cx, &D.idx, (size_t)D.idx_cap * 3, (size_t)count * 3, "dynamic triangle index upload")) return false;
                 D.idx_cap = count;
             }
             if (!dupload(D.idx, idx, (size_t)3 * count, S->stream, "dynamic triangle index upload")) return false;
             D.topology_count = count;
         }
         if (count > D.tris_cap) {
-            if (!realloc_dev(S, &D.tris, (size_t)D.tris_cap * 3, (size_t)count * 3, "dynamic indexed triangle allocation")) return false;
+            if (!realloc_dev(cx, &D.tris, (size_t)D.tris_cap * 3, (size_t)count * 3, "dynamic indexed triangle allocation")) return false;
             D.tris_cap = count;
         }
         const bool motion = !topology_changed && D.tri_upload_count == count;
         k_dyn_from_indices<<<dyn_blocks(count), kThreadsDyn, 0, S->stream>>>(D.verts, vcount, D.idx, count, D.tris);
-        if (!finish_triangles(S, k, count, true, motion, cell)) return false;
+        if (!finish_triangles(cx, D, count, true, motion, tri_cell_size(max_extent, cx.margin, cx.thickness, true))) return false;
         D.tri_upload_count = count;
         if (!publish(S, k)) return false;
     }
     return true;
 }
 
-// Dynamic particles (abi41.cu:8566-8696, hash 6395-6449).
+// Dynamic particles of a cloth (abi41.cu:8566-8696).
 bool upload_dynamic_particles(Solver* S, int cloth, const float* pos, const float* radii, int count) {
     if (!S || cloth >= S->K) return fail("invalid dynamic particle update");
     count = std::max(count, 0);
     const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
     AllocAccount account(&S->device_bytes);
     if (count > 0 && (!pos || !radii)) return fail("dynamic particle position/radius data is required when particle count is nonzero");
-    // radius signature (FNV-1a over the sanitised radii) and the largest radius
-    uint64_t sig = 1469598103934665603ull ^ (uint64_t)count;
-    float max_r = 0.0f;
-    std::vector<float4> p4(count);
-    for (int q = 0; q < count; ++q) {
-        float r = std::isfinite(radii[q]) ? radii[q] : 0.0f;
-        r = std::max(r, 0.0f);
-        max_r = std::max(max_r, r);
-        uint32_t bits;
-        std::memcpy(&bits, &r, 4);
-        sig ^= (uint64_t)bits;
-        sig *= 1099511628211ull;
-        p4[q] = make_float4(pos[3 * q], pos[3 * q + 1], pos[3 * q + 2], 0.0f);
-    }
     for (int k = k0; k < k1; ++k) {
         DynHost& D = S->cl[k].dyn;
-        DynSet& h = D.h;
-        cudaStream_t st = S->stream;
-        if (count == 0) {
-            h.par_count = 0;
-            h.par_motion_valid = 0;
-            h.par_hashed = 0;
-            D.par_upload_count = 0;
-            D.radius_signature = 0;
-            if (!publish(S, k)) return false;
-            continue;
-        }
-        if (h.par_cell <= 0.0f || D.radius_signature != sig || D.par_upload_count != count) {
-            const SsblXpbdConfig& c = S->cl[k].cfg;
-            h.par_cell = std::max(std::max(max_r + std::max(c.collision_margin, 0.0f), std::max(c.cloth_thickness, 0.0f)), 1.0e-3f);
-            D.radius_signature = sig;
-        }
-        const bool motion = D.par_upload_count == count;
-        if (count > D.par_cap) {
-            const size_t o = (size_t)D.par_cap, n = (size_t)count;
-            if (!realloc_dev(S, &D.ppos, o, n, "dynamic particle upload") || !realloc_dev(S, &D.pprev, o, n, "dynamic particle upload") ||
-                !realloc_dev(S, &D.prad, o, n, "dynamic particle upload") || !realloc_dev(S, &D.pcell, o, n, "dynamic particle hash") ||
-                !realloc_dev(S, &D.pent, o, n, "dynamic particle hash"))
-                return false;
-            D.par_cap = count;
-        }
-        if (motion && !cuda_ok(cudaMemcpyAsync(D.pprev, D.ppos, sizeof(float4) * count, cudaMemcpyDeviceToDevice, st),
-                               "keep dynamic particle positions"))
+        if (count == 0)
+            clear_particles(D);
+        else if (!put_particles(cloth_ctx(S, k), D, pos, nullptr, radii, count, nullptr))
             return false;
-        if (!dupload(D.ppos, p4.data(), (size_t)count, st, "dynamic particle upload") ||
-            !dupload(D.prad, radii, (size_t)count, st, "dynamic particle radius upload"))
-            return false;
-        if (!motion && !cuda_ok(cudaMemcpyAsync(D.pprev, D.ppos, sizeof(float4) * count, cudaMemcpyDeviceToDevice, st),
-                                "init dynamic particle positions"))
-            return false;
-        h.par_count = count;
-        h.par_motion_valid = motion ? 1 : 0;
-        h.par_hashed = count >= kParHashMin ? 1 : 0;
-        h.par_buckets = 0;
-        if (h.par_hashed) {
-            const int nb = next_pow2(std::max(1024, count * 4));
-            if (nb > D.pb_cap) {
-                const size_t o = (size_t)D.pb_cap;
-                if (!realloc_dev(S, &D.pcount, o, (size_t)nb, "dynamic particle hash") ||
-                    !realloc_dev(S, &D.pstart, o + 1, (size_t)nb + 1, "dynamic particle hash") ||
-                    !realloc_dev(S, &D.pscan, o / 4096 + 2, (size_t)nb / 4096 + 2, "dynamic particle hash"))
-                    return false;
-                D.pb_cap = nb;
-            }
-            if (!cuda_ok(cudaMemsetAsync(D.pcount, 0, sizeof(int) * nb, st), "reset dynamic particle hash")) return false;
-            k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, D.pcell, D.pcount, nullptr, false);
-            scan_bucket_counts(D.pcount, D.pstart, nb, D.pscan, st);
-            k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, D.pcell, D.pcount, D.pent, true);
-            k_dyn_sort_buckets<<<dyn_blocks(nb), kThreadsDyn, 0, st>>>(D.pstart, D.pent, nb);
-            h.par_buckets = nb;
-        }
-        h.par_pos = D.ppos;
-        h.par_prev = D.pprev;
-        h.par_radius = D.prad;
-        h.par_cellc = D.pcell;
-        h.pstart = D.pstart;
-        h.pent = D.pent;
-        D.par_upload_count = count;
-        if (!cuda_ok(cudaGetLastError(), "dynamic particle hash") || !publish(S, k)) return false;
+        if (!publish(S, k)) return false;
     }
     return true;
+}
+
+// ------------------------------------------------------ shared scene --
+
+GlobalScene* scene_create() {
+    GlobalScene* G = new GlobalScene();
+    if (!cuda_ok(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking), "global dynamic scene stream")) {
+        delete G;
+        return nullptr;
+    }
+    return G;
+}
+
+void scene_destroy(GlobalScene* G) {
+    if (!G) return;
+    // solvers still attached stop using it before its memory goes
+    for (const auto& a : std::vector<std::pair<Solver*, int>>(G->attached.begin(), G->attached.end())) scene_detach(a.first, a.second);
+    cudaDeviceSynchronize();
+    free_set(G->dyn);
+    void* ptrs[] = {G->tri_src, G->tri_layer, G->par_src, G->par_layer, G->overflow};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (G->stream) cudaStreamDestroy(G->stream);
+    delete G;
+}
+
+// abi41.cu:6597-6784: triangles as plain rows with fine hash cells and the
+// unsigned response, particles with the caller's previous positions, source
+// ids and collision layers per primitive.
+bool scene_update(GlobalScene* G, const SsblXpbdGlobalDynamicSceneInputs* in) {
+    if (!G || !in) return fail("invalid global dynamic scene update");
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    const int P = std::max(in->particle_count, 0), T = std::max(in->triangle_count, 0);
+    if (P > 0 && (!in->particle_positions || !in->particle_radii || !in->particle_source_ids || !in->particle_collision_layers))
+        return fail("global dynamic particle arrays are incomplete");
+    if (T > 0 && (!in->triangle_vertices || !in->triangle_source_ids || !in->triangle_collision_layers))
+        return fail("global dynamic triangle arrays are incomplete");
+    // solvers read the scene from their own streams: let their frames finish
+    if (!cuda_ok(cudaDeviceSynchronize(), "global dynamic scene update")) return false;
+    G->margin = std::max(in->collision_margin, 0.0f);
+    G->thickness = std::max(in->cloth_thickness, 0.0f);
+    G->hash_overflow = 0;
+    AllocAccount account(&G->device_bytes);
+    const DynCtx c{G->stream, &G->device_bytes, G->margin, G->thickness};
+    DynHost& D = G->dyn;
+    if (!G->overflow && !dalloc(&G->overflow, 1, "global dynamic scene counters")) return false;
+    if (!cuda_ok(cudaMemsetAsync(G->overflow, 0, sizeof(unsigned long long), c.st), "global dynamic scene counters")) return false;
+    if (P == 0) {
+        clear_particles(D);
+    } else {
+        if (P > G->par_meta_cap) {
+            if (!realloc_dev(c, &G->par_src, (size_t)G->par_meta_cap, (size_t)P, "global dynamic particle source ids") ||
+                !realloc_dev(c, &G->par_layer, (size_t)G->par_meta_cap, (size_t)P, "global dynamic particle layers"))
+                return false;
+            G->par_meta_cap = P;
+        }
+        if (!dupload(G->par_src, in->particle_source_ids, (size_t)P, c.st, "global dynamic particle source upload") ||
+            !dupload(G->par_layer, in->particle_collision_layers, (size_t)P, c.st, "global dynamic particle layer upload") ||
+            !put_particles(c, D, in->particle_positions, in->particle_prev_positions ? in->particle_prev_positions : in->particle_positions,
+                           in->particle_radii, P, G->overflow))
+            return false;
+    }
+    if (T == 0) {
+        clear_triangles(D);
+    } else {
+        if (T > G->tri_meta_cap) {
+            if (!realloc_dev(c, &G->tri_src, (size_t)G->tri_meta_cap, (size_t)T, "global dynamic triangle source ids") ||
+                !realloc_dev(c, &G->tri_layer, (size_t)G->tri_meta_cap, (size_t)T, "global dynamic triangle layers"))
+                return false;
+            G->tri_meta_cap = T;
+        }
+        const bool motion = D.tri_upload_count == T;
+        if (!dupload(G->tri_src, in->triangle_source_ids, (size_t)T, c.st, "global dynamic triangle source upload") ||
+            !dupload(G->tri_layer, in->triangle_collision_layers, (size_t)T, c.st, "global dynamic triangle layer upload") ||
+            !put_rows(c, D, in->triangle_vertices, T) ||
+            !finish_triangles(c, D, T, false, motion, tri_cell_size(rows_max_extent(in->triangle_vertices, T), c.margin, c.thickness, true)))
+            return false;
+        D.tri_upload_count = T;
+    }
+    D.h.tri_src = T > 0 ? G->tri_src : nullptr;
+    D.h.tri_layer = T > 0 ? G->tri_layer : nullptr;
+    D.h.par_src = P > 0 ? G->par_src : nullptr;
+    D.h.par_layer = P > 0 ? G->par_layer : nullptr;
+    unsigned long long over = 0;
+    if (!publish_set(c, D) ||
+        !cuda_ok(cudaMemcpyAsync(&over, G->overflow, sizeof(over), cudaMemcpyDeviceToHost, c.st), "global dynamic scene counters") ||
+        !cuda_ok(cudaStreamSynchronize(c.st), "global dynamic scene update"))
+        return false;
+    G->hash_overflow = (long long)over;
+    G->upload_ms = (float)ms_since(t0);
+    // attached solvers re-check which stages their frame graph needs
+    for (const auto& a : G->attached) a.first->params_dirty = true;
+    return true;
+}
+
+bool scene_attach(Solver* S, int cloth, GlobalScene* G, int source_id, int layer, int mode) {
+    if (!S || !G || cloth >= S->K) return fail("invalid global dynamic scene attach");
+    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
+    for (int k = k0; k < k1; ++k) {
+        Cloth& C = S->cl[k];
+        if (C.gscene && C.gscene != G) C.gscene->attached.erase({S, k});
+        if (!G->dyn.dev) {
+            AllocAccount account(&G->device_bytes);
+            if (!publish_set(DynCtx{G->stream, &G->device_bytes, G->margin, G->thickness}, G->dyn)) return false;
+        }
+        C.gscene = G;
+        G->attached.insert({S, k});
+        Params& P = S->hp[k];
+        P.gdyn = G->dyn.dev;
+        P.gd_mode = mode;
+        P.gd_target_source = source_id;
+        P.gd_target_layer = layer;
+    }
+    S->params_dirty = true;
+    return true;
+}
+
+void scene_detach(Solver* S, int cloth) {
+    if (!S) return;
+    const int k0 = cloth < 0 ? 0 : cloth, k1 = cloth < 0 ? S->K : cloth + 1;
+    for (int k = k0; k < k1 && k < S->K; ++k) {
+        Cloth& C = S->cl[k];
+        if (C.gscene) C.gscene->attached.erase({S, k});
+        C.gscene = nullptr;
+        Params& P = S->hp[k];
+        P.gdyn = nullptr;
+        P.gd_mode = 0;
+        P.gd_target_source = 0;
+        P.gd_target_layer = 0;
+    }
+    S->params_dirty = true;
 }
 
 }  // namespace host

@@ -402,6 +402,7 @@ void free_solver(Solver* S) {
     if (!S) return;
     if (S->stream) cudaStreamSynchronize(S->stream);
     S->drop_graphs();
+    scene_detach(S, -1);
     for (Cloth& c : S->cl) {
         release_grid(S, c);
         dfree(c.fields_dev);
@@ -1415,8 +1416,17 @@ int order_mode(bool need, bool plain) { return need ? (plain ? 2 : 1) : 0; }
 int dynamic_kinds(const Solver* S) {
     int kinds = 0;
     for (int k = 0; k < S->K; ++k) {
-        if (!S->hp[k].dyn) continue;
-        kinds |= S->cl[k].dyn.h.signed_mode ? 2 : 1;
+        const Params& P = S->hp[k];
+        const GlobalScene* G = S->cl[k].gscene;
+        const bool shared = P.gd_mode != 0 && G && (G->dyn.h.tri_count > 0 || G->dyn.h.par_count > 0);
+        if (shared) kinds |= 1;
+        if (!P.dyn) continue;
+        // own colliders: signed meshes keep their passes; unsigned ones give
+        // way to an attached shared scene (abi41.cu:9239)
+        if (S->cl[k].dyn.h.signed_mode)
+            kinds |= 2;
+        else if (P.gd_mode == 0)
+            kinds |= 1;
     }
     return kinds;
 }
@@ -1843,9 +1853,21 @@ bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int fo
     S->diag.finite_flag = 1;
     S->diag.force_field_count = ff;
     S->diag.unsupported_force_field_count = uff;
-    for (const Cloth& C : S->cl) {
-        S->diag.dynamic_triangle_count += C.dyn.h.tri_count;
-        S->diag.dynamic_particle_count += C.dyn.h.par_count;
+    for (int k = 0; k < S->K; ++k) {
+        const Cloth& C = S->cl[k];
+        const GlobalScene* G = S->hp[k].gd_mode != 0 ? C.gscene : nullptr;
+        if (G) {
+            // a cloth on the shared scene reports the scene (abi41.cu:9109-9122)
+            S->diag.dynamic_triangle_count += G->dyn.h.tri_count;
+            S->diag.dynamic_particle_count += G->dyn.h.par_count;
+            S->diag.global_dynamic_triangle_count += G->dyn.h.tri_count;
+            S->diag.global_dynamic_particle_count += G->dyn.h.par_count;
+            S->diag.global_dynamic_hash_overflow += G->hash_overflow;
+            S->diag.global_dynamic_scene_upload_ms += G->upload_ms;
+        } else {
+            S->diag.dynamic_triangle_count += C.dyn.h.tri_count;
+            S->diag.dynamic_particle_count += C.dyn.h.par_count;
+        }
     }
     sdf_diagnostics(S);
     substeps = std::max(substeps, 1);

@@ -11,6 +11,7 @@
 
 #include <chrono>
 #include <map>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -169,6 +170,25 @@ struct DynHost {
     int max_occupancy = 0;        // largest bucket of the triangle hash
 };
 
+struct Solver;
+
+// Shared dynamic scene: colliders of many sources (other cloths' proxies,
+// props) hashed once, read by every attached cloth with its own source
+// filter.  Updates wait for the device to be idle, so no attached solver's
+// frame reads it while it changes.
+struct GlobalScene {
+    DynHost dyn;
+    int *tri_src = nullptr, *tri_layer = nullptr, *par_src = nullptr, *par_layer = nullptr;
+    int tri_meta_cap = 0, par_meta_cap = 0;
+    unsigned long long* overflow = nullptr;  // particles past the 16 queried slots of a bucket
+    float margin = 0.0f, thickness = 0.0f;
+    long long hash_overflow = 0;
+    float upload_ms = 0.0f;
+    long long device_bytes = 0;
+    cudaStream_t stream = nullptr;
+    std::set<std::pair<Solver*, int>> attached;  // (solver, cloth) pairs reading it
+};
+
 // Host-side state of one cloth of a solver.
 struct Cloth {
     SsblXpbdConfig cfg{};               // sanitised copy of the caller's config
@@ -191,6 +211,7 @@ struct Cloth {
     int fields_capacity = 0;
     bool pressure_on = false;
     DynHost dyn;
+    GlobalScene* gscene = nullptr;      // attached shared scene (may be detached: gd_mode 0)
 };
 
 struct Solver {
@@ -320,6 +341,13 @@ bool upload_dynamic_indexed(Solver* S, int cloth, const float* verts, int vcount
                             bool topology_changed);
 bool upload_dynamic_particles(Solver* S, int cloth, const float* pos, const float* radii, int count);
 void free_dynamic(Cloth& C);
+// Shared dynamic scene (xpbd_dynamic.cu).  cloth < 0 attaches / detaches
+// every cloth of the solver.
+GlobalScene* scene_create();
+void scene_destroy(GlobalScene* G);
+bool scene_update(GlobalScene* G, const SsblXpbdGlobalDynamicSceneInputs* in);
+bool scene_attach(Solver* S, int cloth, GlobalScene* G, int source_id, int layer, int mode);
+void scene_detach(Solver* S, int cloth);
 void sdf_diagnostics(Solver* S);
 
 // One frame: prepare parameters, launch (graph or direct), optionally fetch.

@@ -115,6 +115,11 @@ struct DynSet {
     const int4* par_cellc;
     const int* pstart;    // [par_buckets + 1]
     const int* pent;      // first 16 members of a bucket are queried
+    // shared scene only: source id and collision layer per primitive
+    const int* tri_src;
+    const int* tri_layer;
+    const int* par_src;
+    const int* par_layer;
 };
 
 // Parameters of one cloth.  A solver holds one or more cloths concatenated
@@ -177,6 +182,12 @@ struct Params {
     float pressure_velocity_length_scale;
     int needs_normal;                  // pressure or fields: vertex normals are gathered
     const DynSet* dyn;                 // dynamic colliders (device), null when none
+    // shared dynamic scene (cross-cloth collision, abi41.cu:3984-3997):
+    // with a non-zero mode it replaces the cloth's own unsigned colliders;
+    // primitives of the target source id are skipped, and with mode 2 only
+    // lower collision layers collide
+    const DynSet* gdyn;
+    int gd_mode, gd_target_source, gd_target_layer;
 };
 
 // Buffers of the hard-stretch CG solve and the averaged caps.

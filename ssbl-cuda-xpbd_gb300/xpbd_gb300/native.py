@@ -209,7 +209,7 @@ def _load_library():
         "ssbl_capabilities": (ctypes.c_uint, []),
         "ssbl_create_global_dynamic_scene": (vp, []),
         "ssbl_destroy_global_dynamic_scene": (ctypes.c_int, [vp]),
-        "ssbl_update_global_dynamic_scene": (ctypes.c_int, [vp, vp]),
+        "ssbl_update_global_dynamic_scene": (ctypes.c_int, [vp, ctypes.POINTER(NativeGlobalSceneInputs)]),
         "ssbl_attach_global_dynamic_scene": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
         "ssbl_clear_global_dynamic_scene": (ctypes.c_int, [vp]),
         "ssbl_last_error": (ctypes.c_char_p, []),
@@ -236,6 +236,9 @@ def _load_library():
         "xpbd_gb300_batch_update_runtime_colliders": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(NativeRuntimeColliders)]),
         "xpbd_gb300_batch_update_static_triangles": (ctypes.c_int, [vp, ctypes.c_int, _PF, ctypes.c_int]),
         "xpbd_gb300_batch_update_frame_inputs": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(NativeFrameInputs)]),
+        "xpbd_gb300_batch_attach_global_dynamic_scene": (ctypes.c_int, [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int,
+                                                                         ctypes.c_int]),
+        "xpbd_gb300_batch_clear_global_dynamic_scene": (ctypes.c_int, [vp, ctypes.c_int]),
         "xpbd_gb300_batch_update_positions": (ctypes.c_int, [vp, ctypes.c_int, _PF, ctypes.c_int]),
         "xpbd_gb300_batch_download_positions": (ctypes.c_int, [vp, ctypes.c_int, _PF, ctypes.c_int]),
         "xpbd_gb300_batch_reset_cloth": (ctypes.c_int, [vp, ctypes.c_int]),
@@ -327,6 +330,86 @@ def mesh_arrays(cloth: ClothData, static_triangles: np.ndarray) -> tuple[NativeM
     m = NativeMesh(_fp(keep[0]), _fp(keep[1]), _ip(keep[2]), _fp(keep[3]), _ip(keep[4]), _ip(keep[5]), _fp(keep[6]),
                    _ip(keep[7]), _ip(keep[8]), _fp(keep[9]), _ip(keep[10]), _ip(keep[11]), _fp(keep[12]))
     return m, keep
+
+
+class NativeGlobalSceneInputs(ctypes.Structure):
+    """SsblXpbdGlobalDynamicSceneInputs (native/include/ssbl_xpbd_cuda.h:299-312)."""
+
+    _fields_ = [
+        ("particle_positions", _PF), ("particle_prev_positions", _PF), ("particle_radii", _PF),
+        ("particle_source_ids", _PI), ("particle_collision_layers", _PI), ("particle_count", ctypes.c_int),
+        ("triangle_vertices", _PF), ("triangle_source_ids", _PI), ("triangle_collision_layers", _PI),
+        ("triangle_count", ctypes.c_int), ("collision_margin", ctypes.c_float), ("cloth_thickness", ctypes.c_float),
+    ]
+
+
+def scene_inputs(triangles=None, particles=None, margin: float = 0.0, thickness: float = 0.0):
+    """NativeGlobalSceneInputs (and the arrays it points to) from
+    triangles = (rows (T, 3, 3), source ids (T,), layers (T,)) and
+    particles = (positions (P, 3), previous positions (P, 3) or None,
+    radii (P,), source ids (P,), layers (P,))."""
+    fi = NativeGlobalSceneInputs()
+    keep = []
+    if triangles is not None:
+        rows, src, layer = triangles
+        t = np.ascontiguousarray(np.asarray(rows, np.float32).reshape(-1, 9))
+        ts = np.ascontiguousarray(src, np.int32).reshape(-1)
+        tl = np.ascontiguousarray(layer, np.int32).reshape(-1)
+        if len(ts) != len(t) or len(tl) != len(t):
+            raise ValueError("one source id and one layer per scene triangle")
+        keep += [t, ts, tl]
+        fi.triangle_vertices, fi.triangle_source_ids, fi.triangle_collision_layers = _fp(t), _ip(ts), _ip(tl)
+        fi.triangle_count = len(t)
+    if particles is not None:
+        pos, prev, rad, src, layer = particles
+        p = np.ascontiguousarray(np.asarray(pos, np.float32).reshape(-1, 3))
+        q = None if prev is None else np.ascontiguousarray(np.asarray(prev, np.float32).reshape(-1, 3))
+        r = np.ascontiguousarray(rad, np.float32).reshape(-1)
+        ps = np.ascontiguousarray(src, np.int32).reshape(-1)
+        pl = np.ascontiguousarray(layer, np.int32).reshape(-1)
+        if not (len(r) == len(ps) == len(pl) == len(p)) or (q is not None and len(q) != len(p)):
+            raise ValueError("one previous position, radius, source id and layer per scene particle")
+        keep += [p, r, ps, pl] + ([q] if q is not None else [])
+        fi.particle_positions, fi.particle_radii = _fp(p), _fp(r)
+        fi.particle_prev_positions = _fp(q) if q is not None else _PF()
+        fi.particle_source_ids, fi.particle_collision_layers = _ip(ps), _ip(pl)
+        fi.particle_count = len(p)
+    fi.collision_margin = float(margin)
+    fi.cloth_thickness = float(thickness)
+    return fi, keep
+
+
+class GlobalDynamicScene:
+    """Shared dynamic scene (ssbl_create_global_dynamic_scene): colliders of
+    many sources hashed once on the device; every attached cloth reads them
+    through its source filter."""
+
+    def __init__(self):
+        self._lib = _load_library()
+        self._handle = self._lib.ssbl_create_global_dynamic_scene()
+        if not self._handle:
+            raise NativeSolverError(_last_error(self._lib))
+
+    @property
+    def handle(self) -> int:
+        return self._handle
+
+    def update(self, triangles=None, particles=None, margin: float = 0.0, thickness: float = 0.0) -> None:
+        fi, keep = scene_inputs(triangles, particles, margin, thickness)
+        if not self._lib.ssbl_update_global_dynamic_scene(self._handle, ctypes.byref(fi)):
+            raise NativeSolverError(_last_error(self._lib))
+        del keep
+
+    def close(self) -> None:
+        if getattr(self, "_handle", None):
+            self._lib.ssbl_destroy_global_dynamic_scene(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _dynamic_frame_inputs(triangles, indexed, particles):
@@ -484,6 +567,19 @@ class NativeXpbdSolver:
         fi, keep = _dynamic_frame_inputs(triangles, indexed, particles)
         self._check(self._lib.ssbl_update_frame_inputs(self._handle, ctypes.byref(fi)))
         del keep
+
+    def attach_global_scene(self, scene: "GlobalDynamicScene", target_source_id: int = 0, target_collision_layer: int = 0,
+                            mode: int = 1) -> None:
+        """Read the scene's colliders in the unsigned dynamic stage (mode 1:
+        all but the target source, 2: only layers below the target's; 0:
+        keep the own colliders)."""
+        self._check(self._lib.ssbl_attach_global_dynamic_scene(self._handle, scene.handle, int(target_source_id),
+                                                               int(target_collision_layer), int(mode)))
+        self._scene_ref = scene
+
+    def clear_global_scene(self) -> None:
+        self._check(self._lib.ssbl_clear_global_dynamic_scene(self._handle))
+        self._scene_ref = None
 
     def step(self, substeps: int, iterations: int, diagnostics: bool = True, synchronize: bool = True) -> None:
         fetch = 1 if diagnostics else 0
@@ -683,6 +779,15 @@ class NativeXpbdBatch(NativeXpbdSolver):
         fi, keep = _dynamic_frame_inputs(triangles, indexed, particles)
         self._check(self._lib.xpbd_gb300_batch_update_frame_inputs(self._handle, int(cloth), ctypes.byref(fi)))
         del keep
+
+    def attach_cloth_global_scene(self, cloth: int, scene: "GlobalDynamicScene", target_source_id: int = 0,
+                                  target_collision_layer: int = 0, mode: int = 1) -> None:
+        self._check(self._lib.xpbd_gb300_batch_attach_global_dynamic_scene(
+            self._handle, int(cloth), scene.handle, int(target_source_id), int(target_collision_layer), int(mode)))
+        self._scene_ref = scene
+
+    def clear_cloth_global_scene(self, cloth: int) -> None:
+        self._check(self._lib.xpbd_gb300_batch_clear_global_dynamic_scene(self._handle, int(cloth)))
 
     def reset_cloth(self, cloth: int) -> None:
         self._check(self._lib.xpbd_gb300_batch_reset_cloth(self._handle, int(cloth)))
