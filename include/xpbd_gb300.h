@@ -72,6 +72,19 @@ __attribute__((visibility("default"))) int xpbd_gb300_batch_attach_global_dynami
                                                                                         int collision_mode);
 __attribute__((visibility("default"))) int xpbd_gb300_batch_clear_global_dynamic_scene(void* handle, int cloth);
 
+/* PC2 point-cache writer (the reference's bake / realtime cache format,
+ * session_manager.py:4624-4733): open for one cloth of a solver or batch
+ * (cloth -1: every vertex of the handle in stored order), then one sample per
+ * call from the cloth's current positions in object-local coordinates
+ * (matrix_world_inv16: row-major 4x4, null = identity).  The transform runs
+ * on the solver's stream, the copy to pinned memory on a side stream and the
+ * file write on a writer thread, so stepping continues while samples drain.
+ * close(commit = 1) writes the final header and renames the temporary file
+ * into place; it returns the sample count or -1. */
+__attribute__((visibility("default"))) void* xpbd_gb300_pc2_open(void* handle, int cloth, const char* path, int start_frame);
+__attribute__((visibility("default"))) int xpbd_gb300_pc2_write(void* handle, void* writer, const float* matrix_world_inv16);
+__attribute__((visibility("default"))) long long xpbd_gb300_pc2_close(void* writer, int commit);
+
 /* Launch configuration (no counterpart in the reference): 8 slots, in order
  * block size of the per-vertex passes (default 128), of the hash count /
  * scatter kernels (256), lanes per primitive of the triangle / edge hash

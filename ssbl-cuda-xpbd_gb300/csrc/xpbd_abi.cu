@@ -431,6 +431,26 @@ XG_EXPORT int xpbd_gb300_profile_frame(void* handle, int substeps, int iteration
     return ok_or_zero(profile_frame(as_solver(handle), substeps, iterations, kernel_ms, kernel_launches, kinds));
 }
 
+XG_EXPORT void* xpbd_gb300_pc2_open(void* handle, int cloth, const char* path, int start_frame) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S || cloth >= S->K) {
+        fail("invalid PC2 writer request");
+        return nullptr;
+    }
+    return pc2_open(S, cloth < 0 ? -1 : S->ext2int[cloth], path, start_frame);
+}
+
+XG_EXPORT int xpbd_gb300_pc2_write(void* handle, void* writer, const float* matrix_world_inv16) {
+    g_error.clear();
+    return ok_or_zero(pc2_write(as_solver(handle), writer, matrix_world_inv16));
+}
+
+XG_EXPORT long long xpbd_gb300_pc2_close(void* writer, int commit) {
+    g_error.clear();
+    return pc2_close(writer, commit != 0);
+}
+
 XG_EXPORT int xpbd_gb300_set_launch_config(void* handle, const int* values, int count) {
     g_error.clear();
     return ok_or_zero(set_launch_config(as_solver(handle), values, count));

@@ -359,6 +359,12 @@ bool fetch_counts(Solver* S, const FrameStats& st);
 bool sync_params(Solver* S);
 bool step(Solver* S, int substeps, int iterations, int fetch_diagnostics, int force_sync);
 
+// PC2 point-cache writer of one cloth (cloth < 0: all vertices), in
+// xpbd_pc2.cu.
+void* pc2_open(Solver* S, int cloth, const char* path, int start_frame);
+bool pc2_write(Solver* S, void* writer, const float* matrix16);
+long long pc2_close(void* writer, bool commit);
+
 // Launch configuration: set (validated; captured graphs are dropped) and the
 // autotuner, which measures profiled frames from the current state (restored
 // after every trial and at the end, so tuning changes no result) and keeps
