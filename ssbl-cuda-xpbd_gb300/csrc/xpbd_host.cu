@@ -454,6 +454,8 @@ void free_solver(Solver* S) {
     dfree(S->nb_idx);
     dfree(S->acc);
     dfree(S->scan_tmp);
+    dfree(S->trim_list);
+    dfree(S->trim_count);
     PcgView& g = S->pcg;
     dfree(g.diag);
     dfree(g.pinv);
@@ -922,10 +924,14 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
     // internal order: grouped by self-collision mode, stable within a group
     S->int2ext.resize(K);
     for (int k = 0; k < K; ++k) S->int2ext[k] = k;
+    // none, fast, strict with a budget under 32 slots, strict: the cloths
+    // whose queries depend on bucket order (fast, small-budget strict) form
+    // one contiguous run, and so do the strict ones
     auto mode_key = [&](int k) {
         const SsblXpbdConfig& c = in_configs[k];
         if (!c.self_collision) return 0;
-        return c.self_collision_mode == 1 ? 1 : 2;
+        if (c.self_collision_mode == 1) return 1;
+        return std::min(std::max(c.max_self_collision_neighbors, 1), kBucketSlots) < kBucketSlots ? 2 : 3;
     };
     std::stable_sort(S->int2ext.begin(), S->int2ext.end(), [&](int a, int b) { return mode_key(a) < mode_key(b); });
     S->ext2int.resize(K);
@@ -1258,6 +1264,10 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
                  dalloc(&S->vb_count, S->nVB, "self collision hash count allocation") &&
                  dalloc(&S->vb_start, S->nVB + 1, "self collision hash start allocation") &&
                  dalloc(&S->vb_ent, nV, "self collision hash index allocation");
+        // overflowing buckets (more than 32 members) listed by the scans
+        if (ok)
+            ok = dalloc(&S->trim_list, (size_t)std::max(std::max(S->nVB, S->nTB), S->nEB) * 3, "bucket trim list allocation") &&
+                 dalloc(&S->trim_count, 3, "bucket trim list allocation");
         if (ok && S->nTB > 0)
             ok = dalloc(&S->tb_count, S->nTB, "self triangle hash count allocation") &&
                  dalloc(&S->tb_start, S->nTB + 1, "self triangle hash start allocation") &&
@@ -1376,6 +1386,10 @@ SelfPlan plan_self(const Solver* S, int s, int substeps) {
         p.ehash |= P.ehash != 0;
         if (P.thash) (C.order_buckets ? p.t_order : p.t_plain) = true;
         if (P.ehash) (C.order_buckets ? p.e_order : p.e_plain) = true;
+        if (C.order_buckets) {
+            if (P.thash) p.sv.tb_ord.add(P.tbase, P.tbuckets);
+            if (P.ehash) p.sv.eb_ord.add(P.ebase, P.ebuckets);
+        }
         p.any_t |= P.T > 0;
         p.any_e |= P.E > 0;
         p.sv.fast |= C.fast;
@@ -1601,7 +1615,12 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 };
                 View sv = cur_view();
                 View hv[3] = {sv, sv, sv};
-                for (int k = 0; k < 3; ++k) hv[k].scan_tmp = S->scan_tmp + (size_t)k * S->scan_seg;
+                const size_t trim_seg = (size_t)std::max(std::max(S->nVB, S->nTB), S->nEB);
+                for (int k = 0; k < 3; ++k) {
+                    hv[k].scan_tmp = S->scan_tmp + (size_t)k * S->scan_seg;
+                    hv[k].trim_list = S->trim_list + (size_t)k * trim_seg;
+                    hv[k].trim_count = S->trim_count + k;
+                }
                 fork();
                 if (sp.vhash)
                     timed(kKVertexHash, 6, [&] {
@@ -1611,11 +1630,13 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 if (sp.thash)
                     timed(kKTriangleHash, 6, [&] {
                         cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, lane_stream(1));
+                        cudaMemsetAsync(S->trim_count + 1, 0, sizeof(int), lane_stream(1));
                         self_build_triangle_hash(hv[1], sp.sv, S->nTB, order_mode(sp.t_order, sp.t_plain), lane_stream(1));
                     });
                 if (sp.ehash)
                     timed(kKEdgeHash, 6, [&] {
                         cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, lane_stream(2));
+                        cudaMemsetAsync(S->trim_count + 2, 0, sizeof(int), lane_stream(2));
                         self_build_edge_hash(hv[2], sp.sv, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
                     });
                 join();

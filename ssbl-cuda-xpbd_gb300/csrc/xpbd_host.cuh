@@ -295,6 +295,8 @@ struct Solver {
     int* nb_count = nullptr;
     int* nb_idx = nullptr;
     int* scan_tmp = nullptr;  // three segments: vertex, triangle, edge hash scans
+    int* trim_list = nullptr;  // three segments: buckets of more than 32 members per hash
+    int* trim_count = nullptr; // three list lengths
     int scan_seg = 0;
     Acc4* acc = nullptr;
     unsigned long long* perf = nullptr;  // kPerfSlots work counters of a profiled frame

@@ -260,8 +260,10 @@ __device__ __forceinline__ int block_exclusive_scan4(int (&vals)[4], int* warp_s
 // Also adds the number of insertions past each bucket's 32 query slots,
 // sum(max(0, count - 32)), to the overflow counter (the reference counts an
 // overflow for every insertion that finds its bucket full, abi41.cu:4569).
+// Buckets of more than 32 members are listed in `trim` (when given) for
+// k_bucket_trim.
 __global__ void __launch_bounds__(1024) k_scan_reduce(const int* counts, int n, int* block_sums,
-                                                      unsigned long long* overflow) {
+                                                      unsigned long long* overflow, int* trim, int* trim_count) {
     __shared__ int ws[32];
     int vals[4];
     const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
@@ -269,6 +271,7 @@ __global__ void __launch_bounds__(1024) k_scan_reduce(const int* counts, int n, 
     for (int k = 0; k < 4; ++k) {
         vals[k] = base + k < n ? counts[base + k] : 0;
         over += vals[k] > kBucketSlots ? vals[k] - kBucketSlots : 0;
+        if (trim && vals[k] > kBucketSlots) trim[atomicAdd(trim_count, 1)] = base + k;
     }
     for (int o = 16; o > 0; o >>= 1) over += __shfl_down_sync(0xffffffffu, over, o);
     if (overflow && (threadIdx.x & 31) == 0 && over > 0) atomicAdd(overflow, (unsigned long long)over);
@@ -316,9 +319,10 @@ __global__ void __launch_bounds__(1024) k_scan_down(int* counts, int* start, int
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) start[n] = run;
 }
 
-void scan_counts(int* counts, int* start, int n, int* block_sums, unsigned long long* overflow, cudaStream_t s) {
+void scan_counts(int* counts, int* start, int n, int* block_sums, unsigned long long* overflow, cudaStream_t s,
+                 int* trim = nullptr, int* trim_count = nullptr) {
     const int blocks = (n + kScanTile - 1) / kScanTile;
-    k_scan_reduce<<<blocks, 1024, 0, s>>>(counts, n, block_sums, overflow);
+    k_scan_reduce<<<blocks, 1024, 0, s>>>(counts, n, block_sums, overflow, trim, trim_count);
     k_scan_sums<<<1, 1024, 0, s>>>(block_sums, blocks);
     k_scan_down<<<blocks, 1024, 0, s>>>(counts, start, n, block_sums);
 }
@@ -402,6 +406,52 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
             for (int i = 0; i < kBucketSlots; ++i) {
                 int best = i;
                 for (int q = i + 1; q < nj; ++q)
+                    if (e[q] < e[best]) best = q;
+                const int t = e[i];
+                e[i] = e[best];
+                e[best] = t;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// The listed buckets (more than 32 members) are put in increasing id order,
+// so the 32 slots a query reads hold the bucket's 32 smallest ids.  One warp
+// per bucket over a fixed grid: each lane ranks up to 8 members against all
+// members (ties by position) and the warp writes them back by rank; larger
+// buckets fall back to one lane selecting the 32 smallest.
+constexpr int kTrimPerLane = 8;
+
+__global__ void __launch_bounds__(kThreads) k_bucket_trim(const int* start, int* ent, const int* list, const int* count) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
+    const int total = *count;
+    for (int w = warp_global_id(); w < total; w += warps) {
+        const int b = list[w];
+        const int s = start[b], n = start[b + 1] - s;
+        int* e = ent + s;
+        if (n <= 32 * kTrimPerLane) {
+            int key[kTrimPerLane], rank[kTrimPerLane];
+#pragma unroll
+            for (int q = 0; q < kTrimPerLane; ++q) {
+                const int i = lane + 32 * q;
+                key[q] = i < n ? e[i] : 0;
+                rank[q] = 0;
+                if (i < n)
+                    for (int j = 0; j < n; ++j) {
+                        const int o = e[j];
+                        rank[q] += (o < key[q] || (o == key[q] && j < i)) ? 1 : 0;
+                    }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < kTrimPerLane; ++q)
+                if (lane + 32 * q < n) e[rank[q]] = key[q];
+        } else if (lane == 0) {
+            for (int i = 0; i < kBucketSlots; ++i) {
+                int best = i;
+                for (int q = i + 1; q < n; ++q)
                     if (e[q] < e[best]) best = q;
                 const int t = e[i];
                 e[i] = e[best];
@@ -1674,6 +1724,8 @@ View ranged(const View& v, const ItemRange& r) {
 // Threads of a launch over `items` with `per_item` lanes each, in blocks of b.
 inline int grid(long long items, int per_item, int b) { return grid_for(items * per_item, b); }
 
+constexpr int kTrimBlocks = 152 * 4;  // fixed grid of the trim pass (4 blocks per SM)
+
 template <bool kTri, int L>
 void prim_pass(const View& iv, int blocks, int b, bool scatter, cudaStream_t s) {
     k_prim_hash<kTri, L><<<blocks, b, 0, s>>>(iv, scatter);
@@ -1695,8 +1747,12 @@ void bucket_order(const View& v, const ItemRange& buckets, const int* start, int
     k_bucket_sort<<<grid((buckets.size() + 31) / 32, 32, b), b, 0, s>>>(ranged(v, buckets), start, ent, nb, kind, mode);
 }
 
-void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange& buckets, int* count, int* start, int* ent,
-               int nb, int order, cudaStream_t s) {
+void bucket_trim(const View& v, const int* start, int* ent, cudaStream_t s) {
+    k_bucket_trim<<<kTrimBlocks, kThreads, 0, s>>>(start, ent, v.trim_list, v.trim_count);
+}
+
+void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange& buckets, const ItemRange& ordered, int* count,
+               int* start, int* ent, int nb, int order, cudaStream_t s) {
     if (items.size() == 0) return;
     const View iv = ranged(v, items);
     const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, kTunePrimLanes);
@@ -1704,12 +1760,19 @@ void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange&
         prim_pass_lanes<true>(iv, items.size(), lanes, b, false, s);
     else
         prim_pass_lanes<false>(iv, items.size(), lanes, b, false, s);
-    scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s);
+    scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s, v.trim_list, v.trim_count);
     if (tri)
         prim_pass_lanes<true>(iv, items.size(), lanes, b, true, s);
     else
         prim_pass_lanes<false>(iv, items.size(), lanes, b, true, s);
-    bucket_order(v, buckets, start, ent, nb, tri ? 1 : 2, order, s);
+    if (v.trim_list) {
+        // overflowing buckets of every cloth from the scan's list, then every
+        // bucket of the cloths whose queries follow bucket order
+        bucket_trim(v, start, ent, s);
+        if (order != 0) bucket_order(v, ordered, start, ent, nb, tri ? 1 : 2, 1, s);
+    } else {
+        bucket_order(v, buckets, start, ent, nb, tri ? 1 : 2, order, s);
+    }
 }
 
 template <int L>
@@ -1746,10 +1809,10 @@ void self_build_vertex_hash(const View& v, const SelfVariants& sv, int nb, cudaS
     bucket_order(v, sv.vb, v.vb_start, v.vb_ent, nb, 0, 1, s);
 }
 void self_build_triangle_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
-    prim_hash(v, true, sv.t_all, sv.tb, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
+    prim_hash(v, true, sv.t_all, sv.tb, sv.tb_ord, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
 }
 void self_build_edge_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
-    prim_hash(v, false, sv.e_all, sv.eb, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
+    prim_hash(v, false, sv.e_all, sv.eb, sv.eb_ord, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
 }
 
 void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_t s) {

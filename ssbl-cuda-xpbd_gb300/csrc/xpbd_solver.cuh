@@ -278,6 +278,8 @@ struct View {
     int* eb_start;
     int* eb_ent;
     int* scan_tmp;          // block sums of the bucket scans
+    int* trim_list;         // buckets of more than 32 members found by the scan (null: none kept)
+    int* trim_count;
     int* nb_count;          // [nV]
     int* nb_idx;            // [nV * 32]
     Acc4* acc;              // fixed-point delta xyz + contact weight
@@ -381,6 +383,7 @@ struct SelfVariants {
     bool fast, strict, hashed_v, brute_v, hashed_t, brute_t, hashed_e, brute_e;
     bool strict_wide, strict_narrow;  // strict cloths with a candidate budget of >= 32 / < 32 slots
     ItemRange v_all, v_fast, v_strict, e_all, e_fast, e_strict, t_all, vb, tb, eb;
+    ItemRange tb_ord, eb_ord;  // bucket ranges of cloths whose queries need every bucket ordered
     void add_cloth(const Params& P, bool is_fast) {
         v_all.add(P.vstart, P.V);
         (is_fast ? v_fast : v_strict).add(P.vstart, P.V);
