@@ -1940,6 +1940,7 @@ namespace {
 bool tune_value_ok(int slot, int v) {
     if (v == 0) return true;
     if (slot == kTunePrimLanes || slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
+    if (slot == kTuneFastEeForm) return v == 8 || v == 32;
     return v >= 32 && v <= kMaxBlock && v % 32 == 0;
 }
 
@@ -1994,8 +1995,9 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
         *out = best;
         return ok;
     };
-    int dyn = 0, narrow = 0;
+    int dyn = 0, narrow = 0, fast_any = 0;
     for (int k = 0; k < S->K; ++k) {
+        fast_any |= (S->cl[k].self_enabled && S->cl[k].fast) ? 1 : 0;
         dyn |= S->hp[k].dyn ? 1 : 0;
         narrow |= (S->cl[k].self_enabled && !S->cl[k].fast && std::min(std::max(S->hp[k].max_neighbors, 1), kBucketSlots) < kBucketSlots) ? 1 : 0;
     }
@@ -2008,6 +2010,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
         {4, 8, 16},       // group lanes
         {128, 256},       // group block
         {64, 128, 256},   // dynamic colliders
+        {8, 32},          // fast EE: groups of 8 lanes or flattened warps
     };
     const LaunchTune start = S->tune;
     LaunchTune best = start;
@@ -2020,6 +2023,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
     for (int slot = 0; slot < kTuneSlots && ok; ++slot) {
         if (slot == kTuneDynamicBlock && !dyn) continue;
         if ((slot == kTuneGroupLanes || slot == kTuneGroupBlock) && !narrow && !S->self_any) continue;
+        if (slot == kTuneFastEeForm && !fast_any) continue;
         for (short c : cand[slot]) {
             if (c == best.v[slot]) continue;
             LaunchTune t = best;

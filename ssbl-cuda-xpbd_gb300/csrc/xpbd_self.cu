@@ -1406,6 +1406,143 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
     return __ffs(m) - 1;
 }
 
+// Fast-mode EE query, flattened: the same outcome as k_ee_fast.  Phase 1
+// classifies every (item, slot) pair of a warp's 32 items, 32 pairs per round
+// with the slots of the items laid end to end (duplicate = the same id as the
+// slot before; classify is side-effect free, so pairs past an item's budget
+// cut may be classified for nothing); classes and cluster keys go to shared
+// memory.  Phase 2 gives each lane its item and walks the slots in order:
+// visited / duplicate / rest-pose counts, the budget of passing pairs, the
+// cluster filter on up to 16 held keys, and for each taken pair the push,
+// recomputed by the same classify call, accumulated in fixed point.
+constexpr int kFastWarps = kThreads / 32;
+
+__global__ void __launch_bounds__(kThreads, 3) k_ee_fast_flat(View v) {
+    __shared__ unsigned char cls_s[kFastWarps][32 * kBucketSlots];
+    __shared__ unsigned key_s[kFastWarps][32 * kBucketSlots];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int e = v.lo + warp_global_id() * 32 + lane;
+    bool run = e < v.hi;
+    const Params* P = nullptr;
+    if (run) {
+        P = &params_e(v, e);
+        run = P->ehash && fast_mode(*P) && self_scheduled(*P, v);
+    }
+    int2 ed = make_int2(-1, -1);
+    if (run) {
+        ed = __ldg(&v.edges[e]);
+        run = edge_valid(v.nV, ed) && contact_radius(*P) > 0.0f;
+    }
+    int st = 0, lim = 0, budget = 0;
+    float target = 0.0f, onset = 0.0f;
+    if (run) {
+        target = contact_radius(*P);
+        onset = fmaxf(target * 1.8f, target + kEps);
+        budget = neighbor_budget(*P);
+        const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
+        const int b =
+            P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell), cell_of(mid.y, P->ecell), cell_of(mid.z, P->ecell), P->ebuckets);
+        st = v.eb_start[b];
+        lim = min(v.eb_start[b + 1] - st, kBucketSlots);
+    }
+    int incl = lim;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - lim;
+    unsigned char* cls_w = cls_s[wib];
+    unsigned* key_w = key_s[wib];
+    for (int base = 0; base < total; base += 32) {
+        const int w = base + lane;
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
+        const int o_item = __shfl_sync(0xffffffffu, e, j);
+        const int o_st = __shfl_sync(0xffffffffu, st, j);
+        const int o_excl = __shfl_sync(0xffffffffu, excl, j);
+        const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
+        if (w < total) {
+            const int slot = w - o_excl;
+            const int id = v.eb_ent[o_st + slot];
+            const bool dup = slot > 0 && id == v.eb_ent[o_st + slot - 1];
+            SoftPush sp;
+            sp.apply = false;
+            unsigned key = 0u;
+            const int cls = dup ? 4 : ee_fast_classify(v, o_item, id, o_target, o_onset, &sp, &key);
+            cls_w[j * kBucketSlots + slot] = (unsigned char)cls;
+            key_w[j * kBucketSlots + slot] = key;
+        }
+    }
+    __syncwarp();
+    int c_seen = 0, c_dup = 0, c_rest = 0, c_own = 0, c_acc = 0, c_contact = 0, visited = 0;
+    if (run) {
+        unsigned keys[16];
+        int nkeys = 0, passed = 0;
+        for (int slot = 0; slot < lim && passed < budget; ++slot) {
+            ++visited;
+            ++c_seen;
+            const int cls = cls_w[lane * kBucketSlots + slot];
+            if (cls == 4) {
+                ++c_dup;
+                continue;
+            }
+            if (cls == 1) ++c_rest;
+            if (cls != 3) continue;
+            ++passed;
+            const unsigned key = key_w[lane * kBucketSlots + slot];
+            bool first = true;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) first = first && !(q < nkeys && keys[q] == key);
+            if (!(first && nkeys < 16)) {
+                ++c_own;
+                continue;
+            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                if (q == nkeys) keys[q] = key;
+            ++nkeys;
+            ++c_acc;
+            SoftPush sp;
+            sp.apply = false;
+            unsigned k2 = 0u;
+            ee_fast_classify(v, e, v.eb_ent[st + slot], target, onset, &sp, &k2);
+            if (sp.apply) {
+                ++c_contact;
+                for (int k = 0; k < 4; ++k) {
+                    const float wk = sp.w[k];
+                    if ((k > 1 ? -wk : wk) > 0.0f) accumulate(v, sp.idx[k], sp.delta * wk);
+                }
+            }
+        }
+    }
+    const int sums[6] = {c_seen, c_dup, c_rest, c_own, c_acc, c_contact};
+    const int slots[6] = {kCntFilterSeen, kCntFilterRejectedDuplicate, kCntFilterRejectedRest, kCntFilterRejectedOwnership,
+                          kCntFilterAcceptedEe, kCntEdgeEdgeContacts};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const int t = __reduce_add_sync(0xffffffffu, sums[q]);
+        if (lane == 0 && t > 0) count_add(v.counts, slots[q], (unsigned long long)t);
+    }
+    if (v.perf) {
+        const int items = __reduce_add_sync(0xffffffffu, run ? 1 : 0);
+        const int slots_total = __reduce_add_sync(0xffffffffu, visited);
+        if (lane == 0) {
+            atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
+            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)slots_total);
+        }
+    }
+    const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);
+    if (lane == 0 && acc_total > 0) {
+        count_add(v.counts, kCntClusterCount, (unsigned long long)acc_total);
+        count_add(v.counts, kCntClusterOwnedContacts, (unsigned long long)acc_total);
+        count_add(v.counts, kCntSelfCandidates, (unsigned long long)acc_total);
+    }
+}
+
 // Fast-mode EE query in groups of kQueryLanes lanes with the exact outcome of
 // the serial walk of k_ee_hash (abi41.cu:5724-5802 with the filters of
 // 714-832): slots are visited in order until `budget` pairs have passed the
@@ -1842,8 +1979,14 @@ void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
     if (sv.hashed_e && sv.strict_wide && sv.e_strict.size() > 0)
         k_flat_query<true><<<grid(sv.e_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.e_strict));
     if (sv.hashed_e && sv.strict_narrow && sv.e_strict.size() > 0) group_queries_lanes(v, sv, s, true);
-    if (sv.hashed_e && sv.fast && sv.e_fast.size() > 0)
-        k_ee_fast<<<grid(sv.e_fast.size(), kQueryLanes, gb), gb, 0, s>>>(ranged(v, sv.e_fast));
+    if (sv.hashed_e && sv.fast && sv.e_fast.size() > 0) {
+        if (tune_of(v.tune, kTuneFastEeForm) == 32) {
+            const int fb = min(wb, kThreads);  // the shared arrays hold kThreads / 32 warps
+            k_ee_fast_flat<<<grid(sv.e_fast.size(), 1, fb), fb, 0, s>>>(ranged(v, sv.e_fast));
+        } else {
+            k_ee_fast<<<grid(sv.e_fast.size(), kQueryLanes, gb), gb, 0, s>>>(ranged(v, sv.e_fast));
+        }
+    }
     if (sv.brute_e && sv.e_all.size() > 0) k_ee_brute<<<grid(sv.e_all.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.e_all));
 }
 void self_island(const View& v, const SelfVariants& sv, cudaStream_t s) {

@@ -220,12 +220,13 @@ enum TuneSlot {
     kTuneGroupLanes,       // lanes per item of the strict group queries: 4, 8, 16 (8)
     kTuneGroupBlock,       // group query kernels (256)
     kTuneDynamicBlock,     // dynamic colliders (128)
+    kTuneFastEeForm,       // fast-mode EE query: 8 = groups of 8 lanes, 32 = one warp per 32 items, flattened (32)
     kTuneSlots
 };
 struct LaunchTune {
     short v[kTuneSlots];
 };
-constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128};
+constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32};
 constexpr int kMaxBlock = 256;  // the kernels' launch bounds
 inline int tune_of(const LaunchTune& t, int slot) { return t.v[slot] > 0 ? t.v[slot] : kTuneDefault[slot]; }
 inline int grid_for(long long threads, int block) { return (int)((threads + block - 1) / block); }

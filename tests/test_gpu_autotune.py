@@ -12,9 +12,9 @@ pytestmark = pytest.mark.gpu
 
 CONFIGS = [
     {"vertex_block": 64, "hash_block": 128, "prim_lanes": 4, "warp_block": 128, "query_block": 64, "group_lanes": 4,
-     "group_block": 128, "dynamic_block": 64},
+     "group_block": 128, "dynamic_block": 64, "fast_ee_form": 8},
     {"vertex_block": 256, "hash_block": 256, "prim_lanes": 16, "warp_block": 256, "query_block": 256, "group_lanes": 16,
-     "group_block": 256, "dynamic_block": 256},
+     "group_block": 256, "dynamic_block": 256, "fast_ee_form": 32},
     {"vertex_block": 96, "query_block": 160, "warp_block": 32},
 ]
 
@@ -81,7 +81,8 @@ def test_autotune_restores_state_and_keeps_results(gpu_lib, oracle_lib, tmp_path
     assert r2["cached"] and again.launch_config() == r["config"]
 
 
-@pytest.mark.parametrize("bad", [{"vertex_block": 512}, {"vertex_block": 100}, {"prim_lanes": 32}, {"group_lanes": 2}])
+@pytest.mark.parametrize("bad", [{"vertex_block": 512}, {"vertex_block": 100}, {"prim_lanes": 32}, {"group_lanes": 2},
+                                 {"fast_ee_form": 16}])
 def test_invalid_launch_config_is_refused(bad, gpu_lib):
     sc = scene.plain_grid_scene(8, 1)
     s = NativeXpbdSolver(sc.cloth, sc.options, sc.static_triangles)
