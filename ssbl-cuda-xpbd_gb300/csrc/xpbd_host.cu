@@ -456,6 +456,9 @@ void free_solver(Solver* S) {
     dfree(S->scan_tmp);
     dfree(S->trim_list);
     dfree(S->trim_count);
+    dfree(S->bend_ranges);
+    for (auto& f : S->fused_ops) dfree(f.second.first);
+    S->fused_ops.clear();
     PcgView& g = S->pcg;
     dfree(g.diag);
     dfree(g.pinv);
@@ -1031,6 +1034,7 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
     int max_colors = 0;
     for (int k = 0; k < K; ++k) max_colors = std::max(max_colors, (int)S->cl[k].bend_colors.size() - 1);
     std::vector<std::vector<int2>> color_bends(std::max(max_colors, 0));
+    std::vector<int2> bend_local((size_t)std::max(max_colors, 0) * K, make_int2(0, 0));  // within the colour
     std::vector<std::vector<float>> color_rest(std::max(max_colors, 0));
     int lpos = 0;
     for (int k = 0; k < K; ++k) {
@@ -1069,6 +1073,7 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
             // to the cloth's bends
             for (size_t j = 0; j + 1 < C.bend_colors.size(); ++j) {
                 const int b0 = std::max(C.bend_colors[j], 0), b1 = std::min(C.bend_colors[j + 1], B);
+                bend_local[j * K + k] = make_int2((int)color_bends[j].size(), std::max(b1 - b0, 0));
                 for (int q = b0; q < b1; ++q) {
                     color_bends[j].push_back(make_int2(gidx(mesh->bends[q * 2]), gidx(mesh->bends[q * 2 + 1])));
                     color_rest[j].push_back(mesh->bend_rest_lengths[q]);
@@ -1098,6 +1103,12 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
     }
     if (cbends.empty()) S->bend_colors.clear();
     S->nB = (int)cbends.size();
+    S->h_bend_ranges.assign(bend_local.size(), make_int2(0, 0));
+    for (int j = 0; j < max_colors && !cbends.empty(); ++j)
+        for (int k = 0; k < K; ++k) {
+            const int2 r = bend_local[(size_t)j * K + k];
+            S->h_bend_ranges[(size_t)j * K + k] = make_int2(S->bend_colors[j] + r.x, r.y);
+        }
 
     std::vector<int> sp_off, te_off, bj_off;
     std::vector<int2> sp_ent, te_ent, bj_ent;
@@ -1243,6 +1254,8 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
               dalloc(&S->counts, kCntSlots, "ABI41 diagnostic allocation") && dalloc(&S->perf, kPerfSlots, "work counter allocation") &&
               dalloc(&S->max_delta_bits, 1, "self max smoothed delta allocation") &&
               dalloc(&S->pack, (size_t)nV * 3, "download staging allocation");
+    if (ok && !S->h_bend_ranges.empty())
+        ok = dalloc(&S->bend_ranges, S->h_bend_ranges.size(), "bend range allocation");
     if (ok && K > 1)
         ok = dalloc(&S->vcloth, nV, "cloth map allocation") && dalloc(&S->ecloth, nE, "cloth map allocation") &&
              dalloc(&S->tcloth, nT, "cloth map allocation");
@@ -1323,6 +1336,8 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
          dupload(S->bj_off, bj_off.data(), bj_off.size(), st, "bend CSR upload") &&
          dupload(S->bj_ent, bj_ent.data(), bj_ent.size(), st, "bend CSR upload") &&
          dupload(S->bends, cbends.data(), cbends.size(), st, "bend pair upload") &&
+         (S->h_bend_ranges.empty() ||
+          dupload(S->bend_ranges, S->h_bend_ranges.data(), S->h_bend_ranges.size(), st, "bend range upload")) &&
          dupload(S->bend_rest, cbend_rest.data(), cbend_rest.size(), st, "bend rest upload") &&
          dupload(S->tris, tris.data(), nT, st, "triangle upload") && dupload(S->edges, springs.data(), nE, st, "edge upload") &&
          dupload(S->edge_rest, spring_rest.data(), nE, st, "edge rest upload") &&
@@ -1445,9 +1460,50 @@ int dynamic_kinds(const Solver* S) {
     return kinds;
 }
 
+int buf_index(const Solver* S, const float4* p) { return p == S->pos[0] ? 0 : 1; }
+
+GraphKey frame_key(const Solver* S, int substeps, int iterations) {
+    int analytic = 0, sdf = 0, normals = 0;
+    for (const Params& P : S->hp) {
+        analytic |= (P.use_ground || P.use_wall || P.use_sphere) ? 1 : 0;
+        sdf |= P.sdf_ready ? 1 : 0;
+        normals |= P.needs_normal ? 1 : 0;
+    }
+    return GraphKey{substeps, iterations, analytic, sdf, normals, dynamic_kinds(S)};
+}
+
+// Whether every cloth fits one block and uses only stages the fused frame
+// runs (no self collision, hard stretch or dynamic colliders).
+bool fused_ok(const Solver* S) {
+    if (tune_of(S->tune, kTuneFusedFrame) != 1 || S->pcg_on || S->nV == 0) return false;
+    for (int k = 0; k < S->K; ++k) {
+        const Params& P = S->hp[k];
+        if (P.V > 1024 || S->cl[k].self_enabled || P.dyn || P.gd_mode != 0) return false;
+    }
+    return true;
+}
+
+int fused_block(const Solver* S) {
+    int m = 32;
+    for (const Params& P : S->hp) m = std::max(m, P.V);
+    return std::min((m + 31) / 32 * 32, 1024);
+}
+
 void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof) {
     const int nV = S->nV, nE = S->nE;
     const int dyn = dynamic_kinds(S);
+    if (!prof && !S->rec) {
+        const auto f = S->fused_ops.find(frame_key(S, substeps, iterations));
+        if (f != S->fused_ops.end() && f->second.first && fused_ok(S)) {
+            View v = S->view();
+            v.substeps = substeps;
+            v.pass = -1;
+            launch_frame_fused(v, f->second.first, f->second.second, S->pos[0], S->pos[1], S->bend_ranges, S->K,
+                               fused_block(S), S->stream);
+            st->launches += 1;
+            return;
+        }
+    }
     bool analytic = false, sdf = false, normals = false;
     for (const Params& P : S->hp) {
         analytic |= P.use_ground || P.use_wall || P.use_sphere;
@@ -1490,7 +1546,10 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         v.pos_in = S->pos[cur];
         const unsigned gflag = gather == 1 ? kPassSpring : (gather == 2 ? kPassTether : (gather == 3 ? kPassBend : 0u));
         v.pos = gather ? S->pos[cur ^ 1] : S->pos[cur];
-        timed(gather == 1 ? kKStretchPass : kKVertexPass, 1, [&] { launch_vertex_pass(v, nV, gflag | pending, S->stream); });
+        if (S->rec)
+            S->rec->push_back(FrameOp{1, gflag | pending, buf_index(S, v.pos_in), buf_index(S, v.pos), v.substep, v.last_it, 0});
+        else
+            timed(gather == 1 ? kKStretchPass : kKVertexPass, 1, [&] { launch_vertex_pass(v, nV, gflag | pending, S->stream); });
         if (gather) cur ^= 1;
         pending = 0;
         gather = 0;
@@ -1536,7 +1595,10 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         const SelfPlan sp = plan_self(S, s, substeps);
         View pv = cur_view();
         if (normals) pv.pos = S->pos[cur ^ 1];  // vertex normals read the snapshot
-        timed(kKPredict, 1, [&] { launch_predict(pv, nV, S->stream); });
+        if (S->rec)
+            S->rec->push_back(FrameOp{0, 0u, buf_index(S, pv.pos_in), buf_index(S, pv.pos), s, 0, 0});
+        else
+            timed(kKPredict, 1, [&] { launch_predict(pv, nV, S->stream); });
         if (normals) cur ^= 1;
         for (int it = 0; it < iterations; ++it) {
             const bool last_it = it == iterations - 1;
@@ -1545,6 +1607,7 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
             base.last_it = last_it ? 1 : 0;
             if (spring) gather = 1;
             if (pcg && last_it) {
+                if (S->rec) S->rec_unsupported = true;
                 // CG stretch solve, then (hardness >= 0.95) the averaged
                 // polish with normal and tiny caps, and the extreme caps
                 // (abi41.cu:9183-9201, 7806-7857, 7974-7995)
@@ -1572,7 +1635,10 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 View bv = cur_view();
                 for (size_t k = 0; k + 1 < S->bend_colors.size(); ++k) {
                     const int start = S->bend_colors[k], n = S->bend_colors[k + 1] - start;
-                    if (n > 0) timed(kKBendColor, 1, [&] { launch_bend_color(bv, start, n, S->stream); });
+                    if (n > 0 && S->rec)
+                        S->rec->push_back(FrameOp{2, 0u, buf_index(S, bv.pos_in), buf_index(S, bv.pos), s, 1, (int)k});
+                    else if (n > 0)
+                        timed(kKBendColor, 1, [&] { launch_bend_color(bv, start, n, S->stream); });
                 }
             }
             if (final_c && S->jacobi_bends) {
@@ -1586,12 +1652,14 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
             // unsigned dynamic colliders after the static contacts of the
             // last iteration (abi41.cu:9234-9254)
             if (last_it && (dyn & 1)) {
+                if (S->rec) S->rec_unsupported = true;
                 flush();
                 View dv = cur_view();
                 timed(kKDynamic, 1, [&] { launch_dynamic_collision(dv, nV, 0, S->stream); });
             }
             const bool self_run = last_it && sp.run;
             if (self_run) {
+                if (S->rec) S->rec_unsupported = true;
                 flush();
                 // Independent self-collision work runs on side streams: the
                 // three hash builds, then in each pass the VV, VT and EE
@@ -1688,13 +1756,41 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         pending |= kPassVelocity;
         flush();
     }
-    if (cur != 0) timed(kKCopy, 1, [&] { launch_copy_pos(S->pos[0], S->pos[1], nV, S->stream); });
+    if (cur != 0 && S->rec)
+        S->rec->push_back(FrameOp{3, 0u, 1, 0, 0, 0, 0});
+    else if (cur != 0)
+        timed(kKCopy, 1, [&] { launch_copy_pos(S->pos[0], S->pos[1], nV, S->stream); });
 }
 
 namespace {
 
 // The frame graph for (substeps, iterations) and the current collider kinds,
 // captured and instantiated on first use.
+// Record the frame's operations for the fused form (once per schedule key);
+// outside any stream capture, since it allocates and uploads.
+bool prepare_fused(Solver* S, int substeps, int iterations) {
+    if (!fused_ok(S)) return true;
+    const GraphKey key = frame_key(S, substeps, iterations);
+    if (S->fused_ops.count(key)) return true;
+    std::vector<FrameOp> ops;
+    FrameStats dummy;
+    S->rec = &ops;
+    S->rec_unsupported = false;
+    enqueue_frame(S, substeps, iterations, &dummy, nullptr);
+    S->rec = nullptr;
+    if (S->rec_unsupported || ops.empty()) {
+        S->fused_ops[key] = {nullptr, 0};
+        return true;
+    }
+    AllocAccount account(&S->device_bytes);
+    FrameOp* dev = nullptr;
+    if (!dalloc(&dev, ops.size(), "fused frame allocation") || !dupload(dev, ops.data(), ops.size(), S->stream, "fused frame upload") ||
+        !cuda_ok(cudaStreamSynchronize(S->stream), "fused frame upload"))
+        return false;
+    S->fused_ops[key] = {dev, (int)ops.size()};
+    return true;
+}
+
 GraphEntry* ensure_graph(Solver* S, int substeps, int iterations) {
     int analytic = 0, sdf = 0, normals = 0;
     for (const Params& P : S->hp) {
@@ -1705,6 +1801,7 @@ GraphEntry* ensure_graph(Solver* S, int substeps, int iterations) {
     const GraphKey key{substeps, iterations, analytic, sdf, normals, dynamic_kinds(S)};
     auto it = S->graphs.find(key);
     if (it == S->graphs.end()) {
+        if (!prepare_fused(S, substeps, iterations)) return nullptr;
         GraphEntry g;
         FrameStats cst;
         if (!cuda_ok(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal), "begin frame capture"))
@@ -1733,6 +1830,7 @@ bool prepare_graph(Solver* S, int substeps, int iterations) {
 
 bool run_frame(Solver* S, int substeps, int iterations, FrameStats* st) {
     if (!S->use_graphs) {
+        if (!prepare_fused(S, substeps, iterations)) return false;
         enqueue_frame(S, substeps, iterations, st);
         return cuda_ok(cudaGetLastError(), "launch GB300 XPBD frame");
     }
@@ -1941,6 +2039,7 @@ bool tune_value_ok(int slot, int v) {
     if (v == 0) return true;
     if (slot == kTunePrimLanes || slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
     if (slot == kTuneFastEeForm) return v == 8 || v == 32;
+    if (slot == kTuneFusedFrame) return v == 1 || v == 2;
     return v >= 32 && v <= kMaxBlock && v % 32 == 0;
 }
 
@@ -2011,6 +2110,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
         {128, 256},       // group block
         {64, 128, 256},   // dynamic colliders
         {8, 32},          // fast EE: groups of 8 lanes or flattened warps
+        {1, 2},           // small cloths: fused frame or launched kernels
     };
     const LaunchTune start = S->tune;
     LaunchTune best = start;
@@ -2024,6 +2124,9 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
         if (slot == kTuneDynamicBlock && !dyn) continue;
         if ((slot == kTuneGroupLanes || slot == kTuneGroupBlock) && !narrow && !S->self_any) continue;
         if (slot == kTuneFastEeForm && !fast_any) continue;
+        // profiled frames are never fused, so the fused form is not a
+        // candidate here (it replaces a frame's launches by one)
+        if (slot == kTuneFusedFrame) continue;
         for (short c : cand[slot]) {
             if (c == best.v[slot]) continue;
             LaunchTune t = best;

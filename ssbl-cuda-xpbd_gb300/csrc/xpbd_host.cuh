@@ -311,6 +311,13 @@ struct Solver {
     long long pcg_iterations = 0;
 
     LaunchTune tune{};           // launch configuration (0 = default per slot)
+    // fused frames (cloths small enough for one block each): the recorded
+    // operations per frame schedule, and each cloth's bends per colour
+    std::vector<FrameOp>* rec = nullptr;  // set while recording a frame's operations
+    bool rec_unsupported = false;         // a launch without a fused form was recorded
+    std::map<GraphKey, std::pair<FrameOp*, int>> fused_ops;
+    std::vector<int2> h_bend_ranges;      // [colours x K]: first bend, count
+    int2* bend_ranges = nullptr;
     long long device_bytes = 0;  // sum of the solver's device allocations
     std::map<GraphKey, GraphEntry> graphs;
     bool use_graphs = true;

@@ -221,12 +221,13 @@ enum TuneSlot {
     kTuneGroupBlock,       // group query kernels (256)
     kTuneDynamicBlock,     // dynamic colliders (128)
     kTuneFastEeForm,       // fast-mode EE query: 8 = groups of 8 lanes, 32 = one warp per 32 items, flattened (32)
+    kTuneFusedFrame,       // small cloths: 1 = whole frame in one block per cloth, 2 = launched kernels (1)
     kTuneSlots
 };
 struct LaunchTune {
     short v[kTuneSlots];
 };
-constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32};
+constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 1};
 constexpr int kMaxBlock = 256;  // the kernels' launch bounds
 inline int tune_of(const LaunchTune& t, int slot) { return t.v[slot] > 0 ? t.v[slot] : kTuneDefault[slot]; }
 inline int grid_for(long long threads, int block) { return (int)((threads + block - 1) / block); }
@@ -345,6 +346,25 @@ enum PassFlags : unsigned {
     kPassBend = 128u,
 };
 void launch_vertex_pass(const View& v, int V, unsigned flags, cudaStream_t s);
+
+// One operation of a recorded frame (the launches of the normal schedule):
+// kind 0 prediction, 1 vertex pass (flags), 2 bends of colour `color`,
+// 3 copy of buffer `in_buf` into `out_buf`.  in_buf / out_buf: index of the
+// position buffer read / written.
+struct FrameOp {
+    int kind;
+    unsigned flags;
+    int in_buf, out_buf;
+    int substep, last_it;
+    int color;
+};
+// The whole frame of each cloth in one block (cloths of at most 1024
+// vertices without self collision, hard stretch or dynamic colliders): the
+// recorded operations run in order with a block barrier between them.
+// bend_ranges[color * K + cloth] = {first bend, count} of that cloth's bends
+// of the colour.
+void launch_frame_fused(const View& v, const FrameOp* ops, int nops, float4* buf0, float4* buf1, const int2* bend_ranges,
+                        int K, int block, cudaStream_t s);
 void launch_bend_color(const View& v, int start, int count, cudaStream_t s);
 void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s);
 void launch_pin_scatter(const int* idx, const float4* target, const float* weight, const float* relax, int n,

@@ -344,9 +344,7 @@ __device__ bool vertex_normal(const View& v, int i, F3* out) {
 // normal, force fields, damping, pressure speed trims; fixed vertices return
 // to rest.  Reads the snapshot `pos_in` and writes `pos` (the same buffer
 // unless vertex normals are gathered).
-__global__ void __launch_bounds__(kThreads) k_predict(View v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nV) return;
+__device__ __forceinline__ void predict_item(const View& v, int i) {
     const Params& P = params_v(v, i);
     const float4 p4 = v.pos_in[i];
     if (!P.active) {
@@ -401,9 +399,12 @@ __global__ void __launch_bounds__(kThreads) k_predict(View v) {
     v.vel[i] = f4(s.vel, 0.0f);
 }
 
-__global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, unsigned flags) {
+__global__ void __launch_bounds__(kThreads) k_predict(View v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nV) return;
+    if (i < v.nV) predict_item(v, i);
+}
+
+__device__ __forceinline__ void vertex_pass_item(const View& v, int i, unsigned flags) {
     const Params& P = params_v(v, i);
     const float dt = P.sub_dt;
     const float4 p4 = v.pos_in[i];
@@ -454,12 +455,14 @@ __global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, unsigned flags
     v.vel[i] = f4(s.vel, 0.0f);
 }
 
+__global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, unsigned flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < v.nV) vertex_pass_item(v, i, flags);
+}
+
 // Bend constraints of one colour, applied in place: no two bends of a colour
 // share a vertex (abi41.cu:2886-2970).
-__global__ void __launch_bounds__(kThreads) k_bend_color(View v, int start, int count) {
-    const int local = blockIdx.x * blockDim.x + threadIdx.x;
-    if (local >= count) return;
-    const int b = start + local;
+__device__ __forceinline__ void bend_item(const View& v, int b) {
     if (b < 0 || b >= v.nB) {
         count1(v.counts, kCntBendingGuards);
         return;
@@ -490,6 +493,11 @@ __global__ void __launch_bounds__(kThreads) k_bend_color(View v, int start, int 
         v.prev[j] = f4(f3(v.prev[j]) + d * 0.06f, 0.0f);
     }
     count1(v.counts, kCntBendingWings);
+}
+
+__global__ void __launch_bounds__(kThreads) k_bend_color(View v, int start, int count) {
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local < count) bend_item(v, start + local);
 }
 
 __global__ void k_copy_pos(float4* dst, const float4* src, int n) {
@@ -524,6 +532,74 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 // The per-vertex passes are latency bound (gathers of neighbours): by default
 // 128-thread blocks spread a 10k-vertex cloth over twice as many SMs.
+// One block per cloth; the cloth's positions (both ping-pong buffers),
+// previous positions and velocities live in shared memory for the whole
+// frame, so the neighbour gathers and the per-vertex stages touch no global
+// memory for state.  Every operation of the recorded frame sweeps the cloth's
+// items with the block's threads, then the block synchronises.  The state
+// pointers of the View are offset by the cloth's first vertex, so the item
+// functions index them with global vertex indices as in the launched form.
+__global__ void __launch_bounds__(1024) k_frame_fused(View base, const FrameOp* ops, int nops, float4* buf0,
+                                                       const int2* bend_ranges, int K) {
+    extern __shared__ float4 sm[];
+    const int k = blockIdx.x;
+    if (k >= K) return;
+    const Params& P = base.P[k];
+    const int v0 = P.vstart, n = P.V, v1 = P.vstart + P.V;
+    const int cap = (int)(blockDim.x);  // vertices per state array in shared memory
+    float4* s0 = sm;
+    float4* s1 = sm + cap;
+    float4* sprev = sm + 2 * cap;
+    float4* svel = sm + 3 * cap;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        s0[i] = buf0[v0 + i];
+        sprev[i] = base.prev[v0 + i];
+        svel[i] = base.vel[v0 + i];
+    }
+    __syncthreads();
+    View v = base;
+    v.prev = sprev - v0;
+    v.vel = svel - v0;
+    float4* b0 = s0 - v0;
+    float4* b1 = s1 - v0;
+    for (int o = 0; o < nops; ++o) {
+        const FrameOp op = ops[o];
+        v.pos_in = op.in_buf ? b1 : b0;
+        v.pos = op.out_buf ? b1 : b0;
+        v.substep = op.substep;
+        v.last_it = op.last_it;
+        if (op.kind == 0) {
+            for (int i = v0 + (int)threadIdx.x; i < v1; i += blockDim.x) predict_item(v, i);
+        } else if (op.kind == 1) {
+            for (int i = v0 + (int)threadIdx.x; i < v1; i += blockDim.x) vertex_pass_item(v, i, op.flags);
+        } else if (op.kind == 2) {
+            const int2 r = bend_ranges[op.color * K + k];
+            for (int b = r.x + (int)threadIdx.x; b < r.x + r.y; b += blockDim.x) bend_item(v, b);
+        } else {
+            for (int i = v0 + (int)threadIdx.x; i < v1; i += blockDim.x) v.pos[i] = v.pos_in[i];
+        }
+        __syncthreads();
+    }
+    // a frame ends with its result in buffer 0
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        buf0[v0 + i] = s0[i];
+        base.prev[v0 + i] = sprev[i];
+        base.vel[v0 + i] = svel[i];
+    }
+}
+
+void launch_frame_fused(const View& v, const FrameOp* ops, int nops, float4* buf0, float4* buf1, const int2* bend_ranges,
+                        int K, int block, cudaStream_t s) {
+    (void)buf1;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_frame_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 1024 * (int)sizeof(float4));
+        configured = true;
+    }
+    const size_t smem = (size_t)4 * block * sizeof(float4);
+    if (K > 0) k_frame_fused<<<K, block, smem, s>>>(v, ops, nops, buf0, bend_ranges, K);
+}
+
 void launch_predict(const View& v, int V, cudaStream_t s) {
     const int b = tune_of(v.tune, kTuneVertexBlock);
     if (V > 0) k_predict<<<grid_for(V, b), b, 0, s>>>(v);
