@@ -95,7 +95,9 @@ __attribute__((visibility("default"))) long long xpbd_gb300_pc2_close(void* writ
  * (8: groups of 8 lanes, 32: flattened warps; default 32), and whether
  * solvers whose cloths all fit one block (at most 1024 vertices, no self
  * collision, hard stretch or dynamic colliders) run each frame as one fused
- * launch, a block per cloth (1, default) or as launched kernels (2).  Block sizes
+ * launch, a block per cloth (1, default) or an 8-CTA thread-block cluster per
+ * cloth exchanging through distributed shared memory (8), or as launched
+ * kernels (2).  Block sizes
  * are multiples of 32 up to 256; 0 selects the default.  No value changes a
  * result.  Setting drops the captured frame graphs. */
 __attribute__((visibility("default"))) int xpbd_gb300_set_launch_config(void* handle, const int* values, int count);

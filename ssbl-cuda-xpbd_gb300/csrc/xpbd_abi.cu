@@ -460,7 +460,7 @@ XG_EXPORT int xpbd_gb300_get_launch_config(void* handle, int* out, int count) {
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || !out || count < 0) return fail("invalid launch configuration request") ? 1 : 0;
-    for (int k = 0; k < count; ++k) out[k] = k < kTuneSlots ? tune_of(S->tune, k) : 0;
+    for (int k = 0; k < count; ++k) out[k] = k < kTuneSlots ? effective_tune(S, k) : 0;
     return 1;
 }
 

@@ -379,6 +379,7 @@ long long pc2_close(void* writer, bool commit);
 // after every trial and at the end, so tuning changes no result) and keeps
 // the configuration with the shortest frame.  ms_out: {tuned, default}.
 bool set_launch_config(Solver* S, const int* values, int n);
+int effective_tune(const Solver* S, int slot);
 bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out);
 // One profiled frame: per-kind milliseconds and launches (kinds >= kKinds).
 bool profile_frame(Solver* S, int substeps, int iterations, float* kernel_ms, long long* kernel_launches, int kinds);

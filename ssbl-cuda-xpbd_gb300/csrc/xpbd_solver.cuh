@@ -221,13 +221,14 @@ enum TuneSlot {
     kTuneGroupBlock,       // group query kernels (256)
     kTuneDynamicBlock,     // dynamic colliders (128)
     kTuneFastEeForm,       // fast-mode EE query: 8 = groups of 8 lanes, 32 = one warp per 32 items, flattened (32)
-    kTuneFusedFrame,       // small cloths: 1 = whole frame in one block per cloth, 2 = launched kernels (1)
+    kTuneFusedFrame,       // small cloths: 1 = whole frame in one block per cloth, 8 = in an 8-CTA cluster per cloth,
+                           // 2 = launched kernels (1)
     kTuneSlots
 };
 struct LaunchTune {
     short v[kTuneSlots];
 };
-constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 1};
+constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 0};
 constexpr int kMaxBlock = 256;  // the kernels' launch bounds
 inline int tune_of(const LaunchTune& t, int slot) { return t.v[slot] > 0 ? t.v[slot] : kTuneDefault[slot]; }
 inline int grid_for(long long threads, int block) { return (int)((threads + block - 1) / block); }
@@ -365,6 +366,11 @@ struct FrameOp {
 // of the colour.
 void launch_frame_fused(const View& v, const FrameOp* ops, int nops, float4* buf0, float4* buf1, const int2* bend_ranges,
                         int K, int block, cudaStream_t s);
+// The same with a thread-block cluster of `cluster` CTAs per cloth (each
+// holding a full copy of the state, cap vertices per array) exchanging their
+// slices through distributed shared memory after every operation.
+void launch_frame_cluster(const View& v, const FrameOp* ops, int nops, float4* buf0, const int2* bend_ranges, int K, int cap,
+                          int cluster, int block, cudaStream_t s);
 void launch_bend_color(const View& v, int start, int count, cudaStream_t s);
 void launch_copy_pos(float4* dst, const float4* src, int V, cudaStream_t s);
 void launch_pin_scatter(const int* idx, const float4* target, const float* weight, const float* relax, int n,

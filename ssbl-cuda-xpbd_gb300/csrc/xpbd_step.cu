@@ -13,6 +13,8 @@
 // update as the reference's atomics, without float atomics, and therefore
 // deterministic.
 #include "xpbd_constraint.cuh"
+#include <cooperative_groups.h>
+
 #include "xpbd_contact.cuh"
 #include "xpbd_fields.cuh"
 #include "xpbd_solver.cuh"
@@ -586,6 +588,114 @@ __global__ void __launch_bounds__(1024) k_frame_fused(View base, const FrameOp* 
         base.prev[v0 + i] = sprev[i];
         base.vel[v0 + i] = svel[i];
     }
+}
+
+// Cluster form of the fused frame: a thread-block cluster of C CTAs (C SMs)
+// per cloth.  Each CTA holds a full copy of the cloth's state in its shared
+// memory and computes the vertex operations for its slice of the vertices;
+// after each operation it writes its slice of the arrays the operation wrote
+// into the other CTAs' copies (distributed shared memory), then the cluster
+// synchronises.  Bend colours are computed by every CTA on its own copy
+// (identical work, identical results), so their scattered writes need no
+// exchange.  Within an operation the incoming copies touch only other
+// slices of the arrays being written (gathers read the other buffer; the
+// previous positions and velocities are read for the own vertex only).
+namespace cgx = cooperative_groups;
+
+__global__ void __launch_bounds__(256) k_frame_cluster(View base, const FrameOp* ops, int nops, float4* buf0,
+                                                        const int2* bend_ranges, int K, int cap) {
+    extern __shared__ float4 sm[];
+    cgx::cluster_group cluster = cgx::this_cluster();
+    const int C = (int)cluster.num_blocks();
+    const int r = (int)cluster.block_rank();
+    const int k = (int)(blockIdx.x / C);
+    if (k >= K) return;  // uniform over the cluster
+    const Params& P = base.P[k];
+    const int v0 = P.vstart, n = P.V;
+    const int chunk = (n + C - 1) / C;
+    const int lo = min(r * chunk, n), hi = min(lo + chunk, n);
+    float4* s0 = sm;
+    float4* s1 = sm + cap;
+    float4* sprev = sm + 2 * cap;
+    float4* svel = sm + 3 * cap;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        s0[i] = buf0[v0 + i];
+        sprev[i] = base.prev[v0 + i];
+        svel[i] = base.vel[v0 + i];
+    }
+    cluster.sync();  // every copy is complete before any CTA writes into another
+    View v = base;
+    v.prev = sprev - v0;
+    v.vel = svel - v0;
+    float4* b0 = s0 - v0;
+    float4* b1 = s1 - v0;
+    for (int o = 0; o < nops; ++o) {
+        const FrameOp op = ops[o];
+        v.pos_in = op.in_buf ? b1 : b0;
+        v.pos = op.out_buf ? b1 : b0;
+        v.substep = op.substep;
+        v.last_it = op.last_it;
+        if (op.kind == 2) {
+            // every CTA applies the colour to its copy; one of them counts
+            View bv = v;
+            if (r != 0) bv.counts = nullptr;
+            const int2 rg = bend_ranges[op.color * K + k];
+            for (int b = rg.x + (int)threadIdx.x; b < rg.x + rg.y; b += blockDim.x) bend_item(bv, b);
+        } else {
+            for (int i = v0 + lo + (int)threadIdx.x; i < v0 + hi; i += blockDim.x) {
+                if (op.kind == 0)
+                    predict_item(v, i);
+                else if (op.kind == 1)
+                    vertex_pass_item(v, i, op.flags);
+                else
+                    v.pos[i] = v.pos_in[i];
+            }
+            __syncthreads();
+            // the own slice of the written arrays into every other copy
+            const int out = op.out_buf ? 1 : 0;
+            const bool state = op.kind != 3;
+            for (int q = 1; q < C; ++q) {
+                const int dst = (r + q) % C;
+                float4* rem = cluster.map_shared_rank(sm, dst);
+                for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+                    rem[out * cap + i] = sm[out * cap + i];
+                    if (state) {
+                        rem[2 * cap + i] = sprev[i];
+                        rem[3 * cap + i] = svel[i];
+                    }
+                }
+            }
+        }
+        cluster.sync();
+    }
+    for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+        buf0[v0 + i] = s0[i];
+        base.prev[v0 + i] = sprev[i];
+        base.vel[v0 + i] = svel[i];
+    }
+}
+
+// cluster > 1: one cluster of that many CTAs per cloth (block threads each)
+void launch_frame_cluster(const View& v, const FrameOp* ops, int nops, float4* buf0, const int2* bend_ranges, int K, int cap,
+                          int cluster, int block, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_frame_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 1024 * (int)sizeof(float4));
+        configured = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(K * cluster), 1, 1);
+    cfg.blockDim = dim3((unsigned)block, 1, 1);
+    cfg.dynamicSmemBytes = (size_t)4 * cap * sizeof(float4);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (K > 0) cudaLaunchKernelEx(&cfg, k_frame_cluster, v, ops, nops, buf0, bend_ranges, K, cap);
 }
 
 void launch_frame_fused(const View& v, const FrameOp* ops, int nops, float4* buf0, float4* buf1, const int2* bend_ranges,

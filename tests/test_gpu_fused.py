@@ -35,11 +35,13 @@ def _small_mix():
     return out
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_fused_batch_matches_oracle_and_launched(graphs, gpu_lib, oracle_lib):
+@pytest.mark.parametrize("graphs,mode", [(True, 1), (False, 1), (True, 8)], ids=["block", "block-nographs", "cluster"])
+def test_fused_batch_matches_oracle_and_launched(graphs, mode, gpu_lib, oracle_lib):
     scs = _small_mix()
     items = [(s.cloth, s.options, s.static_triangles) for s in scs]
     fused = NativeXpbdBatch(items)
+    fused.set_launch_config({"fused_frame": mode})
+    assert fused.launch_config()["fused_frame"] == mode
     launched = NativeXpbdBatch(items)
     launched.set_launch_config({"fused_frame": 2})
     for b in (fused, launched):
@@ -65,12 +67,17 @@ def test_fused_single_cloth_with_fields(gpu_lib, oracle_lib):
     sc.options.use_volume_pressure = True
     sc.options.pressure_strength = 2.0
     gpu = NativeXpbdSolver(sc.cloth, sc.options, sc.static_triangles)
+    assert gpu.launch_config()["fused_frame"] == 1  # one block per cloth by default
+    blk = NativeXpbdSolver(sc.cloth, sc.options, sc.static_triangles)
+    blk.set_launch_config({"fused_frame": 8})  # the cluster form
     ora = oracle_lib.OracleSolver.from_scene(sc.cloth, sc.options, sc.static_triangles)
     for frame in range(4):
         gpu.step(10, 2, diagnostics=False, synchronize=True)
+        blk.step(10, 2, diagnostics=False, synchronize=True)
         ora.step(10, 2)
         assert gpu.last_step_launches() == 1
         assert np.array_equal(gpu.download_positions(), ora.download_positions()), frame
+        assert np.array_equal(blk.download_positions(), ora.download_positions()), frame
 
 
 def test_large_or_self_colliding_cloths_are_not_fused(gpu_lib):
