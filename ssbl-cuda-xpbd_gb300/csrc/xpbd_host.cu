@@ -2054,6 +2054,7 @@ bool tune_value_ok(int slot, int v) {
     if (slot == kTunePrimLanes || slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
     if (slot == kTuneFastEeForm) return v == 8 || v == 32;
     if (slot == kTuneFusedFrame) return v == 1 || v == 2 || v == 8;
+    if (slot == kTuneTriLanes) return v == 1 || v == 2 || v == 4 || v == 8 || v == 16;
     return v >= 32 && v <= kMaxBlock && v % 32 == 0;
 }
 
@@ -2127,6 +2128,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
         {64, 128, 256},   // dynamic colliders
         {8, 32},          // fast EE: groups of 8 lanes or flattened warps
         {1, 2, 8},        // small cloths: fused frame (block or cluster per cloth) or launched kernels
+        {1, 2, 4, 16},    // lanes per triangle of the triangle hash
     };
     const LaunchTune start = S->tune;
     LaunchTune best = start;

@@ -1871,6 +1871,8 @@ void prim_pass(const View& iv, int blocks, int b, bool scatter, cudaStream_t s) 
 template <bool kTri>
 void prim_pass_lanes(const View& iv, long long items, int lanes, int b, bool scatter, cudaStream_t s) {
     switch (lanes) {
+        case 1: prim_pass<kTri, 1>(iv, grid(items, 1, b), b, scatter, s); break;
+        case 2: prim_pass<kTri, 2>(iv, grid(items, 2, b), b, scatter, s); break;
         case 4: prim_pass<kTri, 4>(iv, grid(items, 4, b), b, scatter, s); break;
         case 16: prim_pass<kTri, 16>(iv, grid(items, 16, b), b, scatter, s); break;
         default: prim_pass<kTri, 8>(iv, grid(items, 8, b), b, scatter, s); break;
@@ -1892,7 +1894,7 @@ void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange&
                int* start, int* ent, int nb, int order, cudaStream_t s) {
     if (items.size() == 0) return;
     const View iv = ranged(v, items);
-    const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, kTunePrimLanes);
+    const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, tri ? kTuneTriLanes : kTunePrimLanes);
     if (tri)
         prim_pass_lanes<true>(iv, items.size(), lanes, b, false, s);
     else

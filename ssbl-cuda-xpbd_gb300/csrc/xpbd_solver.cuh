@@ -214,7 +214,7 @@ struct PcgView {
 enum TuneSlot {
     kTuneVertexBlock = 0,  // per-vertex constraint passes and prediction (default 128)
     kTuneHashBlock,        // hash count / scatter kernels (256)
-    kTunePrimLanes,        // lanes per primitive of the triangle / edge hash: 4, 8, 16 (8)
+    kTunePrimLanes,        // lanes per primitive of the edge hash: 4, 8, 16 (8)
     kTuneWarpBlock,        // warp-per-item kernels: neighbour table, strict VV, flat queries, bucket order (256)
     kTuneQueryBlock,       // thread-per-item queries: fast VV / VT, brute queries, islands, apply (256)
     kTuneGroupLanes,       // lanes per item of the strict group queries: 4, 8, 16 (8)
@@ -223,12 +223,13 @@ enum TuneSlot {
     kTuneFastEeForm,       // fast-mode EE query: 8 = groups of 8 lanes, 32 = one warp per 32 items, flattened (32)
     kTuneFusedFrame,       // small cloths: 1 = whole frame in one block per cloth, 8 = in an 8-CTA cluster per cloth,
                            // 2 = launched kernels (1)
+    kTuneTriLanes,         // lanes per primitive of the triangle hash: 1, 2, 4, 8, 16 (8)
     kTuneSlots
 };
 struct LaunchTune {
     short v[kTuneSlots];
 };
-constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 0};
+constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 0, 8};
 constexpr int kMaxBlock = 256;  // the kernels' launch bounds
 inline int tune_of(const LaunchTune& t, int slot) { return t.v[slot] > 0 ? t.v[slot] : kTuneDefault[slot]; }
 inline int grid_for(long long threads, int block) { return (int)((threads + block - 1) / block); }

@@ -67,6 +67,7 @@ def estimate_device_bytes(req: ClothRequest) -> int:
     V, E, T = len(c.positions_world), len(c.edges), len(c.triangles)
     B, L = len(c.bends), len(c.lra_edges)
     b = V * (16 * 5 + 4 + 16 + 4 * 2 + 12 + 4 * 2) + E * (8 + 4 + 16) + T * 16 + B * 12 + L * 16 + 4 * 8
+    b += 8 * 64 + 4096  # bend colour ranges and recorded fused-frame operations
     if o.self_collision:
         def pow2(x):
             return 1 << max(int(math.ceil(math.log2(max(x, 1)))), 0)
@@ -75,6 +76,7 @@ def estimate_device_bytes(req: ClothRequest) -> int:
         tb = pow2(max(1024, 4 * T)) if T >= 64 else 0
         eb = pow2(max(1024, 4 * E)) if E >= 64 else 0
         b += V * (4 + 4 * 32 + 32 + 16 + 4) + (vb + tb + eb) * 8 + T * 64 * 4 + E * 64 * 4 + 3 * (max(vb, tb, eb) // 4096 + 2) * 4
+        b += 3 * max(vb, tb, eb) * 4 + 3 * 4  # lists of buckets of more than 32 members
     nst = len(req.static_triangles)
     if nst:
         res = max(o.static_sdf_max_resolution if o.static_sdf_max_resolution > 0 else 160, 16)
