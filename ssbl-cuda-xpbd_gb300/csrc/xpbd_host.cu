@@ -473,6 +473,7 @@ void free_solver(Solver* S) {
     dfree(g.ticket);
     dfree(g.guard);
     dfree(g.max_delta_bits);
+    dfree(S->pcg_blk);
     dfree(S->cap_edges);
     dfree(S->cap_rest);
     dfree(S->stage_idx);
@@ -968,8 +969,6 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
         SsblXpbdConfig& c = C.cfg;
         c = *config;
         sanitize(c);
-        if (K > 1 && c.stretch_optimization_enabled)
-            return bail(k, "hard stretch optimization runs on one-cloth solvers only");
         if (c.bend_count > 0 && (!mesh->bends || !mesh->bend_rest_lengths))
             return bail(k, "ABI41 bend constraints require bend pairs and rest lengths");
         if (c.lra_count > 0 && (!mesh->lra_edges || !mesh->lra_rest_lengths))
@@ -1238,7 +1237,12 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
         if (S->hp[k].thash) tri_entries += (long long)S->hp[k].T * kMaxPrimitiveCells;
         if (S->hp[k].ehash) edge_entries += (long long)S->hp[k].E * kMaxPrimitiveCells;
     }
-    S->pcg_on = K == 1 && S->cl[0].cfg.stretch_optimization_enabled != 0;
+    S->pcg_on = S->spring_any = false;
+    for (int k = 0; k < K; ++k) {
+        const bool on = S->cl[k].cfg.stretch_optimization_enabled != 0;
+        S->pcg_on |= on;
+        S->spring_any |= !on && S->hp[k].E > 0;
+    }
 
     bool ok = dalloc(&S->dp, K, "parameter allocation") && dalloc(&S->pos[0], nV, "position allocation") &&
               dalloc(&S->pos[1], nV, "position allocation") && dalloc(&S->prev, nV, "previous position allocation") &&
@@ -1293,35 +1297,77 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
     // Hard-stretch buffers (one-cloth solvers); the caps need edges grouped
     // by colour: the caller's colouring when given (edges already sorted by
     // colour), else a greedy first-fit colouring in edge order.
+    // In a batch each cloth is coloured on its own and colour c of every
+    // cloth with the hard polish forms cap launch c (cloths share no vertex);
+    // a caller's offsets are clamped to the cloth's edges, which is what the
+    // bounds check of a one-cloth launch does with them.
     std::vector<int2> cap_edges;
     std::vector<float> cap_rest;
+    std::vector<int> blk_cloth;
     if (ok && S->pcg_on) {
-        S->pcg_nnz = (int)sp_ent.size();
-        if (S->pcg_nnz == 0) return bail(0, "PCG stretch optimization found no valid CSR edges");
-        if (!S->cl[0].edge_colors.empty()) {
-            cap_edges = springs;
-            cap_rest = spring_rest;
-            S->cap_colors = S->cl[0].edge_colors;
-        } else {
-            std::vector<int> order;
-            greedy_edge_colors(nV, springs, &S->cap_colors, &order);
-            cap_edges.resize(nE);
-            cap_rest.resize(nE);
-            for (int e = 0; e < nE; ++e) {
-                cap_edges[e] = springs[order[e]];
-                cap_rest[e] = spring_rest[order[e]];
+        S->pcg_nnz = 0;
+        S->pcg_blocks = 0;
+        S->pcg_hard = false;
+        std::vector<std::vector<int>> col_off(K), col_order(K);
+        int ncol = 0;
+        for (int k = 0; k < K; ++k) {
+            Params& P = S->hp[k];
+            P.pcg_on = S->cl[k].cfg.stretch_optimization_enabled != 0 ? 1 : 0;
+            P.pcg_hard = P.pcg_on && P.stretch_strength >= 0.95f ? 1 : 0;
+            P.pcg_block0 = S->pcg_blocks;
+            P.pcg_nblocks = 0;
+            if (!P.pcg_on) continue;
+            const int nnz = sp_off[P.vstart + P.V] - sp_off[P.vstart];
+            if (nnz == 0) return bail(k, "PCG stretch optimization found no valid CSR edges");
+            S->pcg_nnz += nnz;
+            P.pcg_nblocks = pcg_blocks(P.V);
+            S->pcg_blocks += P.pcg_nblocks;
+            blk_cloth.insert(blk_cloth.end(), P.pcg_nblocks, k);
+            if (!P.pcg_hard) continue;
+            S->pcg_hard = true;
+            if (!S->cl[k].edge_colors.empty()) {
+                col_off[k] = S->cl[k].edge_colors;
+                col_order[k].resize(P.E);
+                for (int e = 0; e < P.E; ++e) col_order[k][e] = e;
+            } else {
+                std::vector<int2> local(P.E);
+                for (int e = 0; e < P.E; ++e) {
+                    const int2 g = springs[P.estart + e];
+                    local[e] = make_int2(g.x >= 0 ? g.x - P.vstart : g.x, g.y >= 0 ? g.y - P.vstart : g.y);
+                }
+                greedy_edge_colors(P.V, local, &col_off[k], &col_order[k]);
             }
+            ncol = std::max(ncol, (int)col_off[k].size() - 1);
         }
+        S->cap_colors.assign(1, 0);
+        for (int c = 0; c < ncol; ++c) {
+            for (int k = 0; k < K; ++k) {
+                const Params& P = S->hp[k];
+                if (!P.pcg_hard || c + 1 >= (int)col_off[k].size()) continue;
+                const int lo = std::min(std::max(col_off[k][c], 0), P.E), hi = std::min(std::max(col_off[k][c + 1], 0), P.E);
+                for (int e = lo; e < hi; ++e) {
+                    const int ge = P.estart + col_order[k][e];
+                    cap_edges.push_back(springs[ge]);
+                    cap_rest.push_back(spring_rest[ge]);
+                }
+            }
+            S->cap_colors.push_back((int)cap_edges.size());
+        }
+        S->cap_count = (int)cap_edges.size();
         PcgView& g = S->pcg;
         ok = dalloc(&g.diag, 2 * (size_t)nV, "PCG diagonal block allocation") &&
              dalloc(&g.pinv, 2 * (size_t)nV, "PCG preconditioner allocation") && dalloc(&g.r, nV, "PCG residual allocation") &&
              dalloc(&g.z, nV, "PCG preconditioned residual allocation") && dalloc(&g.d, nV, "PCG search direction allocation") &&
              dalloc(&g.q, nV, "PCG A*d allocation") && dalloc(&g.offdiag, sp_ent.size(), "PCG offdiagonal allocation") &&
-             dalloc(&g.avg, nV, "stretch cap accumulation allocation") && dalloc(&g.red, kRedSlots, "PCG reduction allocation") &&
-             dalloc(&g.partials, pcg_warp_partials(nV), "PCG partial sum allocation") &&
-             dalloc(&g.ticket, 1, "PCG ticket allocation") && dalloc(&g.guard, 1, "PCG guard counter allocation") &&
-             dalloc(&g.max_delta_bits, 1, "PCG max delta allocation") && dalloc(&S->cap_edges, nE, "cap edge allocation") &&
-             dalloc(&S->cap_rest, nE, "cap rest allocation");
+             dalloc(&g.avg, nV, "stretch cap accumulation allocation") &&
+             dalloc(&g.red, (size_t)K * kRedSlots, "PCG reduction allocation") &&
+             dalloc(&g.partials, (size_t)S->pcg_blocks * (kThreads / 32), "PCG partial sum allocation") &&
+             dalloc(&g.ticket, K, "PCG ticket allocation") && dalloc(&g.guard, 1, "PCG guard counter allocation") &&
+             dalloc(&g.max_delta_bits, 1, "PCG max delta allocation") &&
+             dalloc(&S->pcg_blk, S->pcg_blocks, "PCG block map allocation") &&
+             dalloc(&S->cap_edges, std::max(S->cap_count, 1), "cap edge allocation") &&
+             dalloc(&S->cap_rest, std::max(S->cap_count, 1), "cap rest allocation");
+        g.blk_cloth = S->pcg_blk;
     }
     if (!ok) return bail(0, "");
     cudaStream_t st = S->stream;
@@ -1357,10 +1403,11 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
          (!S->nb_count || cuda_ok(cudaMemsetAsync(S->nb_count, 0, sizeof(int) * nV, st), "reset neighbor table")) &&
          sync_params(S) && cuda_ok(cudaStreamSynchronize(st), "solver upload");
     if (ok && S->pcg_on)
-        ok = dupload(S->cap_edges, cap_edges.data(), nE, st, "cap edge upload") &&
-             dupload(S->cap_rest, cap_rest.data(), nE, st, "cap rest upload") &&
-             cuda_ok(cudaMemsetAsync(S->pcg.ticket, 0, sizeof(unsigned), st), "reset PCG ticket") &&
-             cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots, st), "reset PCG reductions") &&
+        ok = (S->cap_count == 0 || (dupload(S->cap_edges, cap_edges.data(), S->cap_count, st, "cap edge upload") &&
+                                    dupload(S->cap_rest, cap_rest.data(), S->cap_count, st, "cap rest upload"))) &&
+             dupload(S->pcg_blk, blk_cloth.data(), blk_cloth.size(), st, "PCG block map upload") &&
+             cuda_ok(cudaMemsetAsync(S->pcg.ticket, 0, sizeof(unsigned) * K, st), "reset PCG ticket") &&
+             cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots * K, st), "reset PCG reductions") &&
              cuda_ok(cudaStreamSynchronize(st), "PCG buffer upload");
     if (!ok) return bail(0, "");
     S->diag.finite_flag = 1;
@@ -1524,10 +1571,11 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         sdf |= P.sdf_ready != 0;
         normals |= P.needs_normal != 0;
     }
+    // cloths with the CG stretch solve skip the spring gather of a pass that
+    // other cloths of the batch need (their vertices pass through unchanged)
     const bool pcg = S->pcg_on;
-    const bool spring = nE > 0 && !pcg;
-    const bool hard = pcg && S->hp[0].stretch_strength >= 0.95f;
-    const float cap_dt = S->hp[0].sub_dt;
+    const bool spring = S->spring_any;
+    const bool hard = S->pcg_hard;
     const bool colored_bends = !S->bend_colors.empty();
     View base = S->view();
     base.substeps = substeps;
@@ -1579,13 +1627,14 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         View cv = cur_view();
         cv.edges = S->cap_edges;
         cv.edge_rest = S->cap_rest;
+        cv.nE = S->cap_count;
         const int ncol = (int)S->cap_colors.size() - 1;
         timed(kKStretchCaps, 0, [&] {
             for (int p = 0; p < passes; ++p) {
                 for (int k = 0; k < ncol; ++k) {
                     const int n = S->cap_colors[k + 1] - S->cap_colors[k];
                     if (n > 0) {
-                        pcg_cap_range(cv, S->cap_colors[k], n, cap_dt, kind, S->stream);
+                        pcg_cap_range(cv, S->cap_colors[k], n, kind, S->stream);
                         st->launches += 1;
                     }
                 }
@@ -1593,7 +1642,7 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                     for (int k = ncol - 1; k >= 0; --k) {
                         const int n = S->cap_colors[k + 1] - S->cap_colors[k];
                         if (n > 0) {
-                            pcg_cap_range(cv, S->cap_colors[k], n, cap_dt, kind, S->stream);
+                            pcg_cap_range(cv, S->cap_colors[k], n, kind, S->stream);
                             st->launches += 1;
                         }
                     }
@@ -1626,7 +1675,7 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                 // polish with normal and tiny caps, and the extreme caps
                 // (abi41.cu:9183-9201, 7806-7857, 7974-7995)
                 View gv = cur_view();
-                timed(kKPcg, 0, [&] { pcg_solve(gv, S->pcg, nV, S->stream, &st->launches); });
+                timed(kKPcg, 0, [&] { pcg_solve(gv, S->pcg, S->pcg_blocks, S->stream, &st->launches); });
                 st->pcg_solves += 1;
                 if (hard) {
                     for (int polish = 0; polish < 2; ++polish) {
@@ -1923,11 +1972,15 @@ bool fetch_counts(Solver* S, const FrameStats& st) {
     d.self_cluster_count = (long long)c[kCntClusterCount];
     d.self_cluster_owned_contacts = (long long)c[kCntClusterOwnedContacts];
     if (S->pcg_on) {
-        // residual diagnostics from the scalar slots (abi41.cu:7586-7624)
-        float red[kRedSlots];
+        // residual diagnostics from the scalar slots (abi41.cu:7586-7624);
+        // in a batch the residuals are those of the stacked systems (square
+        // root of the summed r.z of the solving cloths) and every cloth's
+        // guarded status counts
+        std::vector<float> red((size_t)S->K * kRedSlots);
         unsigned long long guard = 0;
         unsigned pbits = 0;
-        if (!cuda_ok(cudaMemcpyAsync(red, S->pcg.red, sizeof(red), cudaMemcpyDeviceToHost, S->stream), "fetch PCG reductions") ||
+        if (!cuda_ok(cudaMemcpyAsync(red.data(), S->pcg.red, sizeof(float) * red.size(), cudaMemcpyDeviceToHost, S->stream),
+                     "fetch PCG reductions") ||
             !cuda_ok(cudaMemcpyAsync(&guard, S->pcg.guard, sizeof(guard), cudaMemcpyDeviceToHost, S->stream), "fetch PCG guard count") ||
             !cuda_ok(cudaMemcpyAsync(&pbits, S->pcg.max_delta_bits, 4, cudaMemcpyDeviceToHost, S->stream), "fetch PCG max delta") ||
             !cuda_ok(cudaStreamSynchronize(S->stream), "fetch PCG diagnostics"))
@@ -1935,18 +1988,30 @@ bool fetch_counts(Solver* S, const FrameStats& st) {
         d.abi41_pcg_csr_nnz = S->pcg_nnz;
         d.abi41_pcg_texture_ready = 1;
         d.abi41_pcg_iterations = S->pcg_iterations;
-        float initial = red[kRedInitialRZ];
-        if ((!std::isfinite(initial) || initial <= 0.0f) && std::isfinite(red[kRedRZ]) && red[kRedRZ] >= 0.0f) initial = red[kRedRZ];
-        if (std::isfinite(initial) && initial >= 0.0f) {
-            d.abi41_pcg_initial_residual = std::sqrt(std::max(initial, 0.0f));
-            d.abi41_pcg_final_residual = d.abi41_pcg_initial_residual;
+        bool have_initial = false, have_final = false;
+        float initial_sum = 0.0f, final_sum = 0.0f;
+        for (int k = 0; k < S->K; ++k) {
+            if (!S->hp[k].pcg_on) continue;
+            const float* R = red.data() + (size_t)k * kRedSlots;
+            float initial = R[kRedInitialRZ];
+            if ((!std::isfinite(initial) || initial <= 0.0f) && std::isfinite(R[kRedRZ]) && R[kRedRZ] >= 0.0f) initial = R[kRedRZ];
+            const bool init_ok = std::isfinite(initial) && initial >= 0.0f;
+            if (init_ok) {
+                initial_sum += initial;
+                have_initial = true;
+            }
+            const float status = R[kRedStatus];
+            const float final_rz = status == 2.0f ? R[kRedRZ] : R[kRedRZNext];
+            if ((status == 0.0f || status == 2.0f) && std::isfinite(final_rz) && final_rz >= 0.0f) {
+                final_sum += final_rz;
+                have_final = true;
+            } else {
+                if (init_ok) final_sum += initial;  // a cloth without a final value reports its initial one
+                if (status != 0.0f && status != 2.0f) d.abi41_pcg_guarded += 1;
+            }
         }
-        const float status = red[kRedStatus];
-        const float final_rz = status == 2.0f ? red[kRedRZ] : red[kRedRZNext];
-        if ((status == 0.0f || status == 2.0f) && std::isfinite(final_rz) && final_rz >= 0.0f)
-            d.abi41_pcg_final_residual = std::sqrt(std::max(final_rz, 0.0f));
-        else if (status != 0.0f && status != 2.0f)
-            d.abi41_pcg_guarded += 1;
+        if (have_initial) d.abi41_pcg_initial_residual = std::sqrt(std::max(initial_sum, 0.0f));
+        if (have_initial || have_final) d.abi41_pcg_final_residual = std::sqrt(std::max(final_sum, 0.0f));
         d.abi41_pcg_guarded += (long long)guard;
         std::memcpy(&d.abi41_pcg_max_delta, &pbits, 4);
     }
@@ -1970,7 +2035,7 @@ bool prepare_step(Solver* S, int substeps, int iterations) {
     if (S->pcg_on &&
         (!cuda_ok(cudaMemsetAsync(S->pcg.guard, 0, sizeof(unsigned long long), S->stream), "reset PCG guard count") ||
          !cuda_ok(cudaMemsetAsync(S->pcg.max_delta_bits, 0, sizeof(unsigned), S->stream), "reset PCG max delta") ||
-         !cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots, S->stream), "reset PCG reductions")))
+         !cuda_ok(cudaMemsetAsync(S->pcg.red, 0, sizeof(float) * kRedSlots * S->K, S->stream), "reset PCG reductions")))
         return false;
     return true;
 }

@@ -301,11 +301,16 @@ struct Solver {
     Acc4* acc = nullptr;
     unsigned long long* perf = nullptr;  // kPerfSlots work counters of a profiled frame
 
-    // hard-stretch optimisation (one-cloth solvers only)
-    bool pcg_on = false;
+    // hard-stretch optimisation (every cloth that enables it)
+    bool pcg_on = false;         // some cloth runs the CG stretch solve
+    bool pcg_hard = false;       // some cloth runs the averaged polish and caps
+    bool spring_any = false;     // some cloth with edges keeps the spring gather
     PcgView pcg{};
-    int2* cap_edges = nullptr;   // edges sorted by colour for the caps
+    int* pcg_blk = nullptr;      // cloth of each block of the CG grid
+    int pcg_blocks = 0;          // CG grid: the one-cloth grids of those cloths end to end
+    int2* cap_edges = nullptr;   // edges sorted by colour for the caps (colours of all cloths merged)
     float* cap_rest = nullptr;
+    int cap_count = 0;
     std::vector<int> cap_colors; // colour offsets into cap_edges
     int pcg_nnz = 0;
     long long pcg_iterations = 0;

@@ -9,6 +9,12 @@
 // (atomic ticket, no waiting) sums the partials in a fixed order -- lane l
 // adds partials l, l+32, ... then a shuffle-down tree.  The device-side
 // alpha / beta / status logic is the reference's (abi41.cu:3320-3464).
+//
+// In a batch every cloth that enables the optimisation solves its own system:
+// the solve grid is the concatenation of the grids one-cloth solvers of
+// those cloths would launch (a block belongs to one cloth), each cloth has
+// its own partials segment, ticket and scalar slots, so its reductions, its
+// alpha / beta and its status follow exactly the one-cloth sequence.
 #include "xpbd_solver.cuh"
 
 namespace xg {
@@ -85,29 +91,45 @@ __device__ __forceinline__ float warp_tree(float v) {
     return v;
 }
 
-// Store this warp's tree partial; the last block to finish returns true in
-// every thread of its first warp together with the total in `*total`.
-__device__ bool reduce_partials(const PcgView& g, float v, float* total) {
+// The vertex of this thread in the solve grid: the block's cloth, its local
+// vertex index and its global one.
+struct PcgItem {
+    int cloth, local, i;
+    bool valid;
+};
+__device__ __forceinline__ PcgItem pcg_item(const View& v, const PcgView& g) {
+    const int c = __ldg(&g.blk_cloth[blockIdx.x]);
+    const Params& P = v.P[c];
+    const int local = (blockIdx.x - P.pcg_block0) * blockDim.x + threadIdx.x;
+    return PcgItem{c, local, P.vstart + local, local < P.V};
+}
+
+// Store this warp's tree partial; the last block of the cloth to finish
+// returns true in every thread of its first warp together with the cloth's
+// total in `*total`.
+__device__ bool reduce_partials(const PcgView& g, const Params& P, int cloth, float v, float* total) {
     __shared__ bool last;
     const float w = warp_tree(v);
     const int lane = threadIdx.x & 31;
-    const int gw = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int wpb = blockDim.x >> 5;
+    const int gw = blockIdx.x * wpb + (threadIdx.x >> 5);
     if (lane == 0) g.partials[gw] = w;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned ticket = atomicAdd(g.ticket, 1u);
-        last = ticket == gridDim.x - 1;
+        const unsigned ticket = atomicAdd(&g.ticket[cloth], 1u);
+        last = ticket == (unsigned)(P.pcg_nblocks - 1);
     }
     __syncthreads();
     if (!last || threadIdx.x >= 32) return false;
     __threadfence();
-    const int nw = (int)((gridDim.x * (long long)blockDim.x) >> 5);
+    const int nw = P.pcg_nblocks * wpb;
+    const volatile float* part = g.partials + (long long)P.pcg_block0 * wpb;
     float s = 0.0f;
-    for (int k = lane; k < nw; k += 32) s += ((volatile float*)g.partials)[k];
+    for (int k = lane; k < nw; k += 32) s += part[k];
     s = warp_tree(s);
     *total = __shfl_sync(0xffffffffu, s, 0);
-    if (lane == 0) *g.ticket = 0u;
+    if (lane == 0) g.ticket[cloth] = 0u;
     return true;
 }
 
@@ -118,10 +140,11 @@ __device__ __forceinline__ float4 z4() { return make_float4(0.0f, 0.0f, 0.0f, 0.
 // preconditioner / initial residual (abi41.cu:3188-3226) and the iteration
 // set-up (abi41.cu:3071-3083).
 __global__ void __launch_bounds__(kThreads) k_pcg_build(View v, PcgView g) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const PcgItem it = pcg_item(v, g);
+    const Params& P = v.P[it.cloth];
+    const int i = it.i;
     float rz = 0.0f;
-    if (i < v.nV) {
+    if (it.valid) {
         const float4 p4 = v.pos[i];
         const float wi_self = p4.w;
         Sym diag{1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f};
@@ -185,8 +208,8 @@ __global__ void __launch_bounds__(kThreads) k_pcg_build(View v, PcgView g) {
         }
     }
     float total;
-    if (reduce_partials(g, rz, &total) && (threadIdx.x & 31) == 0) {
-        float* R = g.red;
+    if (reduce_partials(g, P, it.cloth, rz, &total) && (threadIdx.x & 31) == 0) {
+        float* R = g.red + it.cloth * kRedSlots;
         R[kRedRZ] = total;
         R[kRedInitialRZ] = total;
         R[kRedIterations] = 0.0f;
@@ -198,11 +221,13 @@ __global__ void __launch_bounds__(kThreads) k_pcg_build(View v, PcgView g) {
 
 // q = A d, partial d.q (abi41.cu:3228-3267); the last block publishes dAd.
 __global__ void __launch_bounds__(kThreads) k_pcg_ad(View v, PcgView g) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool status_ok = g.red[kRedStatus] == kStatusOk;
+    const PcgItem it = pcg_item(v, g);
+    const Params& P = v.P[it.cloth];
+    const int i = it.i;
+    float* R = g.red + it.cloth * kRedSlots;
+    const bool status_ok = R[kRedStatus] == kStatusOk;
     float dq = 0.0f;
-    if (status_ok && i < v.nV) {
+    if (status_ok && it.valid) {
         if (!(v.pos[i].w > 0.0f)) {
             g.q[i] = z4();
         } else {
@@ -226,15 +251,17 @@ __global__ void __launch_bounds__(kThreads) k_pcg_ad(View v, PcgView g) {
         }
     }
     float total;
-    if (reduce_partials(g, dq, &total) && (threadIdx.x & 31) == 0) g.red[kRedDAD] = g.red[kRedDAD] + total;
+    if (reduce_partials(g, P, it.cloth, dq, &total) && (threadIdx.x & 31) == 0) R[kRedDAD] = R[kRedDAD] + total;
 }
 
 // Device alpha, solution / residual / preconditioned residual update with the
 // incremental position write-back, partial r.z (abi41.cu:3320-3405).
 __global__ void __launch_bounds__(kThreads) k_pcg_update(View v, PcgView g) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const float rz_old = g.red[kRedRZ], dad = g.red[kRedDAD];
+    const PcgItem it = pcg_item(v, g);
+    const Params& P = v.P[it.cloth];
+    const int i = it.i;
+    float* R = g.red + it.cloth * kRedSlots;
+    const float rz_old = R[kRedRZ], dad = R[kRedDAD];
     float status = kStatusOk, alpha = 0.0f;
     if (!isfinite(rz_old) || rz_old < 0.0f) {
         status = kStatusBadResidual;
@@ -247,7 +274,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(View v, PcgView g) {
         if (!isfinite(alpha)) status = kStatusBadAlpha;
     }
     float rz = 0.0f;
-    if (status == kStatusOk && i < v.nV) {
+    if (status == kStatusOk && it.valid) {
         const float4 p4 = v.pos[i];
         if (!(p4.w > 0.0f)) {
             g.r[i] = z4();
@@ -276,28 +303,30 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(View v, PcgView g) {
         }
     }
     if (status != kStatusOk) {
-        if (i == 0) {
-            g.red[kRedStatus] = status;
+        if (it.local == 0) {
+            R[kRedStatus] = status;
             if (status != kStatusZeroResidual) atomicAdd(g.guard, 1ull);
         }
         return;
     }
     float total;
-    if (reduce_partials(g, rz, &total) && (threadIdx.x & 31) == 0) {
-        g.red[kRedRZNext] = g.red[kRedRZNext] + total;
-        g.red[kRedIterations] = g.red[kRedIterations] + 1.0f;
+    if (reduce_partials(g, P, it.cloth, rz, &total) && (threadIdx.x & 31) == 0) {
+        R[kRedRZNext] = R[kRedRZNext] + total;
+        R[kRedIterations] = R[kRedIterations] + 1.0f;
     }
 }
 
 // Device beta and d = z + beta d (abi41.cu:3421-3450); the last block then
 // advances the scalar slots (abi41.cu:3452-3464).
 __global__ void __launch_bounds__(kThreads) k_pcg_dir(View v, PcgView g) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const float status = g.red[kRedStatus], rz_old = g.red[kRedRZ], rz_new = g.red[kRedRZNext];
+    const PcgItem it = pcg_item(v, g);
+    const Params& P = v.P[it.cloth];
+    const int i = it.i;
+    float* R = g.red + it.cloth * kRedSlots;
+    const float status = R[kRedStatus], rz_old = R[kRedRZ], rz_new = R[kRedRZNext];
     const bool ok = status == kStatusOk && isfinite(rz_old) && isfinite(rz_new) && rz_old > 1.0e-14f && rz_new >= 0.0f;
     const float beta = ok ? rz_new / rz_old : 0.0f;
-    if (ok && isfinite(beta) && i < v.nV) {
+    if (ok && isfinite(beta) && it.valid) {
         if (!(v.pos[i].w > 0.0f)) {
             g.d[i] = z4();
         } else {
@@ -306,12 +335,12 @@ __global__ void __launch_bounds__(kThreads) k_pcg_dir(View v, PcgView g) {
         }
     }
     float total;
-    if (reduce_partials(g, 0.0f, &total) && threadIdx.x == 0) {
+    if (reduce_partials(g, P, it.cloth, 0.0f, &total) && threadIdx.x == 0) {
         if (status == kStatusOk && isfinite(rz_new) && rz_new >= 0.0f) {
-            g.red[kRedRZ] = rz_new;
-            g.red[kRedDAD] = 0.0f;
-            g.red[kRedRZNext] = 0.0f;
-            g.red[kRedStatus] = kStatusOk;
+            R[kRedRZ] = rz_new;
+            R[kRedDAD] = 0.0f;
+            R[kRedRZNext] = 0.0f;
+            R[kRedStatus] = kStatusOk;
         }
     }
 }
@@ -362,10 +391,12 @@ __device__ bool averaged_delta(const Params& P, bool tiny, float4 pi, float4 pj,
 }
 
 // Gather of the averaged corrections of a vertex's edges into sum / count.
+// Vertices of cloths without the hard polish are left alone.
 __global__ void __launch_bounds__(kThreads) k_avg_gather(View v, PcgView g, int tiny) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.pcg_hard) return;
     const float4 p4 = v.pos[i];
     const F3 prev_self = f3(v.prev[i]);
     F3 sum{0.0f, 0.0f, 0.0f};
@@ -389,9 +420,10 @@ __global__ void __launch_bounds__(kThreads) k_avg_gather(View v, PcgView g, int 
 
 // Apply the averaged corrections (abi41.cu:2084-2112, 2469-2494).
 __global__ void __launch_bounds__(kThreads) k_avg_apply(View v, PcgView g, int tiny) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.pcg_hard) return;
     const float4 p4 = v.pos[i];
     if (!(p4.w > 0.0f)) return;
     const float4 a = g.avg[i];
@@ -413,9 +445,9 @@ __global__ void __launch_bounds__(kThreads) k_avg_apply(View v, PcgView g, int t
 // ---------------------------------------------------- colour-range caps --
 // Ratio caps applied in place one edge colour at a time (no two edges of a
 // colour share a vertex): normal (abi41.cu:2249-2362), tiny (2496-2601) and
-// extreme (2603-2708).
-__global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int count, float dt, int kind) {
-    const Params& P = v.P[0];  // the solve runs on single-cloth solvers
+// extreme (2603-2708).  In a batch a launch covers one colour of every cloth
+// with the hard polish; the time step is the cloth's substep length.
+__global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int count, int kind) {
     const int local = blockIdx.x * blockDim.x + threadIdx.x;
     if (local >= count) return;
     const int s = start + local;
@@ -427,6 +459,8 @@ __global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int c
     const int2 ed = __ldg(&v.edges[s]);
     const int i = ed.x, j = ed.y;
     if (i < 0 || j < 0 || i >= v.nV || j >= v.nV || i == j) return;
+    const Params& P = params_v(v, i);
+    const float dt = P.sub_dt;
     const float4 pi4 = v.pos[i], pj4 = v.pos[j];
     const float wi = pi4.w, wj = pj4.w, weight = wi + wj;
     if (!isfinite(weight) || weight <= 0.0f) return;
@@ -492,11 +526,11 @@ __global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int c
 
 }  // namespace
 
-int pcg_warp_partials(int V) { return blocks_for(V) * (kThreads / 32); }
+int pcg_blocks(int V) { return V > 0 ? blocks_for(V) : 0; }
 
-void pcg_solve(const View& v, const PcgView& g, int V, cudaStream_t s, long long* launches) {
-    if (V <= 0) return;
-    const int b = blocks_for(V);
+void pcg_solve(const View& v, const PcgView& g, int blocks, cudaStream_t s, long long* launches) {
+    if (blocks <= 0) return;
+    const int b = blocks;
     k_pcg_build<<<b, kThreads, 0, s>>>(v, g);
     for (int it = 0; it < 8; ++it) {
         k_pcg_ad<<<b, kThreads, 0, s>>>(v, g);
@@ -516,8 +550,8 @@ void pcg_averaged_pass(const View& v, const PcgView& g, int V, bool tiny, cudaSt
     k_avg_apply<<<blocks_for(V), kThreads, 0, s>>>(v, g, tiny ? 1 : 0);
 }
 
-void pcg_cap_range(const View& v, int start, int count, float dt, int kind, cudaStream_t s) {
-    if (count > 0) k_cap_range<<<blocks_for(count), kThreads, 0, s>>>(v, start, count, dt, kind);
+void pcg_cap_range(const View& v, int start, int count, int kind, cudaStream_t s) {
+    if (count > 0) k_cap_range<<<blocks_for(count), kThreads, 0, s>>>(v, start, count, kind);
 }
 
 }  // namespace xg

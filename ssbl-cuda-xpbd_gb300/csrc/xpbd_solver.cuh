@@ -171,6 +171,10 @@ struct Params {
     int vbase, tbase, ebase;           // offsets of its tables in the shared bucket arrays
     int vhash, thash, ehash;           // hash in use (else brute force)
     float stretch_strength;            // clamp01(stretch_optimization_strength)
+    // hard-stretch optimisation: this cloth runs the CG stretch solve in
+    // place of the spring gather (and, at strength >= 0.95, the averaged
+    // polish and ratio caps); its CG blocks are [pcg_block0, + pcg_nblocks)
+    int pcg_on, pcg_hard, pcg_block0, pcg_nblocks;
     // external accelerations of the prediction (force fields, volume pressure)
     const SsblXpbdForceField* fields;  // field_count records (device)
     int field_count;
@@ -200,9 +204,10 @@ struct PcgView {
     float4* q;
     float4* offdiag;     // per stretch-CSR entry: edge normal xyz, stiffness
     float4* avg;         // averaged caps: sum xyz, count
-    float* red;          // kRedSlots scalars
-    float* partials;     // one per warp of the solve grid
-    unsigned* ticket;    // last-block ticket
+    float* red;          // kRedSlots scalars per cloth
+    float* partials;     // one per warp of the solve grid (each cloth's warps contiguous)
+    unsigned* ticket;    // last-block ticket per cloth
+    const int* blk_cloth;  // cloth of each block of the solve grid
     unsigned long long* guard;
     unsigned* max_delta_bits;
 };
@@ -330,11 +335,14 @@ __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 void set_last_error(const std::string& msg);
 
 // ---- host launchers (defined in the .cu files) ----
-int pcg_warp_partials(int V);
-void pcg_solve(const View& v, const PcgView& g, int V, cudaStream_t s, long long* launches);
+// Blocks of the CG solve grid for a cloth of V vertices (each cloth of a
+// batch gets the grid a one-cloth solver of its size would launch).
+int pcg_blocks(int V);
+void pcg_solve(const View& v, const PcgView& g, int blocks, cudaStream_t s, long long* launches);
 void pcg_averaged_pass(const View& v, const PcgView& g, int V, bool tiny, cudaStream_t s);
-// kind: 0 normal cap, 1 tiny cap, 2 extreme cap
-void pcg_cap_range(const View& v, int start, int count, float dt, int kind, cudaStream_t s);
+// kind: 0 normal cap, 1 tiny cap, 2 extreme cap; over the colour-sorted cap
+// edges [start, start + count) (v.edges / v.edge_rest / v.nE point at them)
+void pcg_cap_range(const View& v, int start, int count, int kind, cudaStream_t s);
 void launch_predict(const View& v, int V, cudaStream_t s);
 // pass flags for launch_vertex_pass
 enum PassFlags : unsigned {

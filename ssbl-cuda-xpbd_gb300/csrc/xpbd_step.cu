@@ -420,8 +420,11 @@ __device__ __forceinline__ void vertex_pass_item(const View& v, int i, unsigned 
     s.prev = f3(v.prev[i]);
     s.vel = f3(v.vel[i]);
     const float inv_mass = __ldg(&v.inv_mass[i]);
-    if (flags & (kPassSpring | kPassTether | kPassBend)) {
-        const int kind = (flags & kPassSpring) ? 0 : ((flags & kPassTether) ? 1 : 2);
+    // a cloth with the CG stretch solve has no spring gather (in a batch the
+    // pass still carries its vertices to the other buffer)
+    const unsigned gather = flags & (P.pcg_on ? (kPassTether | kPassBend) : (kPassSpring | kPassTether | kPassBend));
+    if (gather) {
+        const int kind = (gather & kPassSpring) ? 0 : ((gather & kPassTether) ? 1 : 2);
         const int* off = kind == 0 ? v.sp_off : (kind == 1 ? v.te_off : v.bj_off);
         const int2* ent = kind == 0 ? v.sp_ent : (kind == 1 ? v.te_ent : v.bj_ent);
         const int begin = __ldg(&off[i]), end = __ldg(&off[i + 1]);

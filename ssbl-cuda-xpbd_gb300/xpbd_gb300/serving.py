@@ -77,6 +77,10 @@ def estimate_device_bytes(req: ClothRequest) -> int:
         eb = pow2(max(1024, 4 * E)) if E >= 64 else 0
         b += V * (4 + 4 * 32 + 32 + 16 + 4) + (vb + tb + eb) * 8 + T * 64 * 4 + E * 64 * 4 + 3 * (max(vb, tb, eb) // 4096 + 2) * 4
         b += 3 * max(vb, tb, eb) * 4 + 3 * 4  # lists of buckets of more than 32 members
+    if o.stretch_optimization_enabled:
+        # CG blocks, preconditioner, r / z / d / q, cap sums, off-diagonal per
+        # stretch-CSR entry (two per edge), colour-sorted cap edges, partials
+        b += V * (32 + 32 + 4 * 16 + 16) + E * (2 * 16 + 12) + (V // 256 + 1) * 36 + 1024
     nst = len(req.static_triangles)
     if nst:
         res = max(o.static_sdf_max_resolution if o.static_sdf_max_resolution > 0 else 160, 16)

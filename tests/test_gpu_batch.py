@@ -133,12 +133,48 @@ def test_batch_per_cloth_updates(gpu_lib, oracle_lib):
             assert np.array_equal(batch.download_cloth_positions(k), o.download_positions()), k
 
 
-def test_batch_rejects_hard_stretch(gpu_lib):
-    scs = _mixed_scenes()[:2]
-    scs[1].options.stretch_optimization_enabled = True
-    scs[1].options.stretch_optimization_strength = 0.5
-    with pytest.raises(NativeSolverError, match="batch cloth 1: hard stretch optimization runs on one-cloth solvers only"):
-        NativeXpbdBatch(_items(scs))
+def _hard_stretch_scenes():
+    scs = [scene.hardness_grid_scene(20, 1.0, 6), scene.hardness_grid_scene(16, 0.4, 6)]
+    # the hard polish with greedy edge colours (no caller colouring)
+    sc = scene.hardness_grid_scene(14, 1.0, 6)
+    sc.cloth.edge_color_offsets = np.asarray([0], np.int32)
+    scs.append(sc)
+    # a cloth without the optimisation between them (spring gather)
+    scs.append(scene.plain_grid_scene(12, 6))
+    # the CG solve on a self-colliding drop
+    sc = scene.drop_scene(14, 6, seed=5)
+    sc.options.stretch_optimization_enabled = True
+    sc.options.stretch_optimization_strength = 1.0
+    scs.append(sc)
+    return scs
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_batch_hard_stretch_matches_each_cloth_alone(graphs, gpu_lib, oracle_lib):
+    """Cloths with the CG stretch solve (strength 0.4: solve only; 1.0: plus
+    averaged polish and ratio caps, with caller and greedy colourings) next
+    to a spring-gather cloth in one batch: each cloth equals the oracle run
+    on it alone, bit for bit, after every frame."""
+    scs = _hard_stretch_scenes()
+    batch = NativeXpbdBatch(_items(scs))
+    batch.set_graph_capture(graphs)
+    oras = _oracles(scs, oracle_lib)
+    for frame in range(4):
+        batch.step(10, 2, diagnostics=frame == 3, synchronize=True)
+        for k, ora in enumerate(oras):
+            ora.step(10, 2)
+            pg, po = batch.download_cloth_positions(k), ora.download_positions()
+            err = float(np.abs(pg - po).max())
+            assert err <= 1e-4 * scs[k].extent, (frame, k, err)
+            assert np.array_equal(pg, po), (frame, k, err)
+    d = batch.diagnostics()
+    solo = [NativeXpbdSolver(s.cloth, s.options, s.static_triangles) for s in scs if s.options.stretch_optimization_enabled]
+    nnz = 0
+    for s in solo:
+        s.step(10, 2, diagnostics=True, synchronize=True)
+        nnz += s.diagnostics()["abi41_pcg_csr_nnz"]
+    assert d["abi41_pcg_csr_nnz"] == nnz
+    assert d["abi41_pcg_iterations"] > 0 and np.isfinite(d["abi41_pcg_final_residual"])
 
 
 def test_whole_handle_transfers_use_the_callers_cloth_order(gpu_lib, oracle_lib):

@@ -1,6 +1,8 @@
 """Serving form on the GPU: requests that arrive while others run are
 admitted as memory frees up, share cohorts, and each result is bit-identical
 to the same request run alone (and to the oracle)."""
+import copy
+
 import numpy as np
 import pytest
 
@@ -46,7 +48,12 @@ def test_result_same_alone_and_in_mix(gpu_lib, oracle_lib):
 
 
 def test_memory_estimate_covers_allocation(gpu_lib):
-    for r in _mix()[:5]:
+    reqs = _mix()[:5]
+    # one request with the hard-stretch CG buffers
+    hard = copy.deepcopy(reqs[0])
+    hard.options.stretch_optimization_enabled = True
+    hard.options.stretch_optimization_strength = 1.0
+    for r in reqs + [hard]:
         s = NativeXpbdSolver(r.cloth, r.options, r.static_triangles)
         assert s.device_bytes() <= estimate_device_bytes(r), (len(r.cloth.positions_world), s.device_bytes())
         s.close()
