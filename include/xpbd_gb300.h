@@ -116,10 +116,13 @@ __attribute__((visibility("default"))) int xpbd_gb300_solver_info(void* handle, 
 __attribute__((visibility("default"))) int xpbd_gb300_autotune(void* handle, int substeps, int iterations, int rounds,
                                                                float* ms_out2);
 
-/* Work counters of the last xpbd_gb300_profile_frame: out4 = EE query items,
- * EE bucket slots evaluated, VT query items (strict cloths), VT slots
- * evaluated.  They size the algorithmic bytes of the query kernels. */
-__attribute__((visibility("default"))) int xpbd_gb300_profile_counters(void* handle, long long* out4);
+/* Work counters of the last xpbd_gb300_profile_frame, out[10]: EE query
+ * items, EE bucket slots evaluated, VT query items (strict cloths), VT slots
+ * evaluated; entries written by the frame's last triangle-hash build and
+ * last edge-hash build; triangles and edges hashed per build; triangle and
+ * edge bucket counts.  They size the algorithmic bytes of the query kernels
+ * and of the hash builds. */
+__attribute__((visibility("default"))) int xpbd_gb300_profile_counters(void* handle, long long* out);
 
 /* No counterpart in the reference.  Vertex spatial hash that allocates no
  * device memory, for callers that cannot call cudaMalloc / cudaFree (a host

@@ -490,15 +490,34 @@ XG_EXPORT int xpbd_gb300_autotune(void* handle, int substeps, int iterations, in
     return ok_or_zero(autotune(as_solver(handle), std::max(substeps, 1), std::max(iterations, 1), rounds, ms_out2));
 }
 
-XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out4) {
+XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out) {
     g_error.clear();
     Solver* S = as_solver(handle);
-    if (!S || !out4) return fail("invalid profile counter request") ? 1 : 0;
+    if (!S || !out) return fail("invalid profile counter request") ? 1 : 0;
     unsigned long long c[kPerfSlots];
+    int entries[2] = {0, 0};  // the scans' totals: entries of the last build of each hash
     if (!cuda_ok(cudaMemcpyAsync(c, S->perf, sizeof(c), cudaMemcpyDeviceToHost, S->stream), "read work counters") ||
+        (S->tb_start && S->nTB > 0 &&
+         !cuda_ok(cudaMemcpyAsync(&entries[0], S->tb_start + S->nTB, sizeof(int), cudaMemcpyDeviceToHost, S->stream),
+                  "read triangle hash size")) ||
+        (S->eb_start && S->nEB > 0 &&
+         !cuda_ok(cudaMemcpyAsync(&entries[1], S->eb_start + S->nEB, sizeof(int), cudaMemcpyDeviceToHost, S->stream),
+                  "read edge hash size")) ||
         !cuda_ok(cudaStreamSynchronize(S->stream), "read work counters"))
         return 0;
-    for (int k = 0; k < kPerfSlots; ++k) out4[k] = (long long)c[k];
+    for (int k = 0; k < kPerfSlots; ++k) out[k] = (long long)c[k];
+    long long tris = 0, edges = 0;
+    for (const Params& P : S->hp) {
+        if (!P.self_on) continue;
+        if (P.thash) tris += P.T;
+        if (P.ehash) edges += P.E;
+    }
+    out[4] = entries[0];
+    out[5] = entries[1];
+    out[6] = tris;
+    out[7] = edges;
+    out[8] = S->nTB;
+    out[9] = S->nEB;
     return 1;
 }
 

@@ -339,13 +339,14 @@ __device__ __forceinline__ bool bucket_order_needed(const Params& P) {
 }
 
 // Order bucket members by primitive id.  One warp per 32 consecutive buckets:
-// each lane sorts its own bucket of up to 8 members in registers (odd-even
-// transposition network); a bucket of 9-32 members is sorted by the whole
-// warp (each lane ranks one member against all others with shuffles); a
-// larger one gets its 32 smallest ids moved to the front in order (queries
-// read no further).
+// each lane sorts its own bucket of up to 16 members in registers (bitonic
+// network over 16, padded with INT_MAX); a bucket of 17-32 members is sorted
+// by the whole warp (each lane ranks one member against all others with
+// shuffles); a larger one gets its 32 smallest ids moved to the front in
+// order (queries read no further).
 // `mode`: 0 order only buckets of more than 32, 1 order every bucket, 2 ask
-// the cloth of the bucket's first member (bucket_order_needed).  `kind`:
+// the cloth of the bucket's first member (bucket_order_needed), 3 order the
+// buckets of up to 32 (k_bucket_trim has ordered the larger ones).  `kind`:
 // 1 triangle, 2 edge buckets (for mode 2).
 __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* start, int* ent, int nbuckets, int kind,
                                                           int mode) {
@@ -358,28 +359,35 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
         s = start[b];
         n = start[b + 1] - s;
     }
-    bool need = n > kBucketSlots;
+    bool need = n > kBucketSlots && mode != 3;
     if (n >= 2 && n <= kBucketSlots) {
-        if (mode == 1) {
+        if (mode == 1 || mode == 3) {
             need = true;
         } else if (mode == 2) {
             const int first = ent[s];
             need = bucket_order_needed(kind == 1 ? params_t(v, first) : params_e(v, first));
         }
     }
-    constexpr int kSmall = 8;
+    constexpr int kSmall = 16;
     if (need && n <= kSmall) {
         int r[kSmall];
         int* e = ent + s;
 #pragma unroll
         for (int k = 0; k < kSmall; ++k) r[k] = k < n ? e[k] : 0x7fffffff;
 #pragma unroll
-        for (int round = 0; round < kSmall; ++round) {
+        for (int size = 2; size <= kSmall; size <<= 1) {
 #pragma unroll
-            for (int k = round & 1; k + 1 < kSmall; k += 2) {
-                const int lo = min(r[k], r[k + 1]), hi = max(r[k], r[k + 1]);
-                r[k] = lo;
-                r[k + 1] = hi;
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+                for (int k = 0; k < kSmall; ++k) {
+                    const int l = k ^ stride;
+                    if (l > k) {
+                        const int lo = min(r[k], r[l]), hi = max(r[k], r[l]);
+                        const bool up = (k & size) == 0;
+                        r[k] = up ? lo : hi;
+                        r[l] = up ? hi : lo;
+                    }
+                }
             }
         }
 #pragma unroll
@@ -1908,7 +1916,7 @@ void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange&
         // overflowing buckets of every cloth from the scan's list, then every
         // bucket of the cloths whose queries follow bucket order
         bucket_trim(v, start, ent, s);
-        if (order != 0) bucket_order(v, ordered, start, ent, nb, tri ? 1 : 2, 1, s);
+        if (order != 0) bucket_order(v, ordered, start, ent, nb, tri ? 1 : 2, 3, s);
     } else {
         bucket_order(v, buckets, start, ent, nb, tri ? 1 : 2, order, s);
     }

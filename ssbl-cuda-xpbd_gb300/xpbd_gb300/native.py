@@ -688,11 +688,14 @@ class NativeXpbdSolver:
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
 
     def profile_counters(self) -> dict:
-        """Work counters of the last profile_frame (EE / VT query items and
-        bucket slots evaluated)."""
-        out = np.zeros(4, np.int64)
+        """Work counters of the last profile_frame: EE / VT query items and
+        bucket slots evaluated, entries of the last triangle / edge hash
+        build, primitives hashed per build and the bucket counts."""
+        out = np.zeros(10, np.int64)
         self._check(self._lib.xpbd_gb300_profile_counters(self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
-        return {"ee_items": int(out[0]), "ee_slots": int(out[1]), "vt_items": int(out[2]), "vt_slots": int(out[3])}
+        keys = ("ee_items", "ee_slots", "vt_items", "vt_slots", "tri_entries", "edge_entries", "tri_hashed", "edge_hashed",
+                "tri_buckets", "edge_buckets")
+        return {k: int(v) for k, v in zip(keys, out)}
 
 
 class NativeXpbdBatch(NativeXpbdSolver):
