@@ -1691,8 +1691,82 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
 // ------------------------------------------------- fast overlap islands --
 // Fast mode, final pass: aggregate push for a vertex buried in >= 3 nearby
 // triangles of the 27-cell neighbourhood (abi41.cu:5226-5439).
-__global__ void __launch_bounds__(kThreads) k_island(View v) {
-    const int vertex = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+//
+// One candidate slot of the walk, everything but the duplicate check: 0 =
+// skipped, 1 = skipped with a guard count, 2 = a contact with its
+// penetration, normal and inverse-mass term.
+struct IslandHit {
+    float pen, wterm;
+    F3 nrm;
+};
+
+__device__ int island_eval(const View& v, int vertex, F3 p, F3 pp, float target, float onset, int tri, IslandHit* out) {
+    if (tri < 0 || tri >= v.nT) return 1;
+    const int4 t = __ldg(&v.tris[tri]);
+    if (!tri_valid(v.nV, t)) return 0;
+    // The reference tests the rest pose, then finiteness, then the current
+    // distance.  Both the rest and the distance test only skip the
+    // candidate, so for finite positions the (cheaper, usually failing)
+    // distance test runs first; non-finite positions keep the reference
+    // order, which decides the guard count.
+    const F3 a = f3(v.pos[t.x]), b2 = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
+    const F3 ap = f3(v.prev[t.x]), bp = f3(v.prev[t.y]), cp = f3(v.prev[t.z]);
+    const bool finite = finite3(a) && finite3(b2) && finite3(c) && finite3(ap) && finite3(bp) && finite3(cp);
+    F3 q{0.0f, 0.0f, 0.0f};
+    float dsq = 0.0f, dist = 0.0f;
+    if (finite) {
+        if (point_triangle_far(p, a, b2, c, target)) return 0;
+        q = closest_on_triangle(p, a, b2, c);
+        const F3 d0 = p - q;
+        dsq = dot3(d0, d0);
+        dist = sqrtf(fmaxf(dsq, kEps));
+        if (dist >= target) return 0;
+    }
+    if (rest_vt_neighbor(v, vertex, t, target, onset)) return 0;
+    if (!finite) return 1;
+    F3 delta = p - q;
+    F3 nrm{0.0f, 0.0f, 1.0f};
+    if (dsq > kEps) {
+        nrm = delta * (1.0f / dist);
+    } else {
+        nrm = cross3(b2 - a, c - a);
+        const float nl = dot3(nrm, nrm);
+        if (nl > kEps) {
+            nrm = nrm * (1.0f / sqrtf(nl));
+        } else {
+            const F3 rv = f3(ld4(&v.rest[vertex]));
+            const F3 rd = rv - closest_on_triangle(rv, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])), f3(ld4(&v.rest[t.z])));
+            const float rl = dot3(rd, rd);
+            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+        }
+        delta = nrm * dist;
+        dist = 0.0f;
+    }
+    if (!finite3(nrm)) return 1;
+    const F3 qprev = closest_on_triangle(pp, ap, bp, cp);
+    const F3 pdelta = pp - qprev;
+    if (dot3(pdelta, nrm) > target * 0.25f && dot3(delta, nrm) > -target * 0.10f) return 0;
+    float wa, wb, wc;
+    barycentric(q, a, b2, c, &wa, &wb, &wc);
+    const float pen = target - dist;
+    if (pen <= 0.0f) return 0;
+    out->pen = pen;
+    out->nrm = nrm;
+    out->wterm = __ldg(&v.inv_mass[t.x]) * wa + __ldg(&v.inv_mass[t.y]) * wb + __ldg(&v.inv_mass[t.z]) * wc;
+    return 2;
+}
+
+// One warp per vertex.  Lane c < 27 reads the range of cell (dz, dy, dx) =
+// (c/9-1, c/3%3-1, c%3-1), the serial walk's order; the slots of the 27
+// buckets are laid end to end (warp prefix sum) and evaluated 32 at a time,
+// one slot per lane; then the warp replays the slots in walk order with the
+// walk's rules -- stop at max_contacts contacts or scan_limit slots, skip a
+// triangle already accepted, count guards of visited slots only -- and sums
+// the accepted contacts in that order (every lane holds the same sums; the
+// accepted ids are spread over the lanes for the duplicate test).
+__global__ void __launch_bounds__(kThreads, 4) k_island(View v) {
+    const int vertex = v.lo + warp_global_id();
+    const int lane = threadIdx.x & 31;
     if (vertex >= v.hi) return;
     const Params& P = params_v(v, vertex);
     if (!fast_mode(P) || !P.thash || P.T <= 0 || !self_scheduled(P, v) || v.pass != P.self_passes - 1) return;
@@ -1702,7 +1776,7 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const F3 p = f3(v.pos[vertex]), pp = f3(v.prev[vertex]);
     if (!finite3(p) || !finite3(pp)) {
-        count1(v.counts, kCntIslandGuarded);
+        if (lane == 0) count1(v.counts, kCntIslandGuarded);
         return;
     }
     int maxn = P.max_neighbors < 1 ? 1 : P.max_neighbors;
@@ -1710,97 +1784,73 @@ __global__ void __launch_bounds__(kThreads) k_island(View v) {
     if (max_contacts > 48) max_contacts = 48;
     if (max_contacts < 3) max_contacts = 3;
     const int scan_limit = max_contacts * 10;
-    int accepted_tris[48];
     const int cx = cell_of(p.x, P.tcell), cy = cell_of(p.y, P.tcell), cz = cell_of(p.z, P.tcell);
-    int scanned = 0, contacts = 0;
+    int st = 0, lim = 0;
+    if (lane < 27) {
+        const int b = P.tbase + (int)bucket_of(cx + lane % 3 - 1, cy + (lane / 3) % 3 - 1, cz + lane / 9 - 1, P.tbuckets);
+        st = v.tb_start[b];
+        lim = min(v.tb_start[b + 1] - st, kBucketSlots);
+    }
+    int incl = lim;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    const int visit = min(__shfl_sync(0xffffffffu, incl, 31), scan_limit);
+    const int excl = incl - lim;
+    int contacts = 0, scanned = 0, guards = 0;
+    int acc_lo = -1, acc_hi = -1;  // accepted ids: lane q holds number q and q + 32
     float pen_sum = 0.0f, wsum = 0.0f, max_pen = 0.0f;
     F3 axis{0.0f, 0.0f, 0.0f}, best{0.0f, 0.0f, 1.0f};
-    for (int dz = -1; dz <= 1 && contacts < max_contacts && scanned < scan_limit; ++dz)
-        for (int dy = -1; dy <= 1 && contacts < max_contacts && scanned < scan_limit; ++dy)
-            for (int dx = -1; dx <= 1 && contacts < max_contacts && scanned < scan_limit; ++dx) {
-                const int b = P.tbase + (int)bucket_of(cx + dx, cy + dy, cz + dz, P.tbuckets);
-                const int s = v.tb_start[b];
-                const int lim = min(v.tb_start[b + 1] - s, kBucketSlots);
-                for (int k = 0; k < lim && contacts < max_contacts && scanned < scan_limit; ++k) {
-                    ++scanned;
-                    const int tri = v.tb_ent[s + k];
-                    bool dup = false;
-                    for (int q = 0; q < contacts; ++q)
-                        if (accepted_tris[q] == tri) {
-                            dup = true;
-                            break;
-                        }
-                    if (dup) continue;
-                    if (tri < 0 || tri >= v.nT) {
-                        count1(v.counts, kCntIslandGuarded);
-                        continue;
-                    }
-                    const int4 t = __ldg(&v.tris[tri]);
-                    if (!tri_valid(v.nV, t)) continue;
-                    // The reference tests the rest pose, then finiteness, then
-                    // the current distance.  Both the rest and the distance
-                    // test only skip the candidate, so for finite positions
-                    // the (cheaper, usually failing) distance test runs
-                    // first; non-finite positions keep the reference order,
-                    // which decides the guard count.
-                    const F3 a = f3(v.pos[t.x]), b2 = f3(v.pos[t.y]), c = f3(v.pos[t.z]);
-                    const F3 ap = f3(v.prev[t.x]), bp = f3(v.prev[t.y]), cp = f3(v.prev[t.z]);
-                    const bool finite = finite3(a) && finite3(b2) && finite3(c) && finite3(ap) && finite3(bp) && finite3(cp);
-                    F3 q{0.0f, 0.0f, 0.0f};
-                    float dsq = 0.0f, dist = 0.0f;
-                    if (finite) {
-                        if (point_triangle_far(p, a, b2, c, target)) continue;
-                        q = closest_on_triangle(p, a, b2, c);
-                        const F3 d0 = p - q;
-                        dsq = dot3(d0, d0);
-                        dist = sqrtf(fmaxf(dsq, kEps));
-                        if (dist >= target) continue;
-                    }
-                    if (rest_vt_neighbor(v, vertex, t, target, onset)) continue;
-                    if (!finite) {
-                        count1(v.counts, kCntIslandGuarded);
-                        continue;
-                    }
-                    F3 delta = p - q;
-                    F3 nrm{0.0f, 0.0f, 1.0f};
-                    if (dsq > kEps) {
-                        nrm = delta * (1.0f / dist);
-                    } else {
-                        nrm = cross3(b2 - a, c - a);
-                        const float nl = dot3(nrm, nrm);
-                        if (nl > kEps) {
-                            nrm = nrm * (1.0f / sqrtf(nl));
-                        } else {
-                            const F3 rv = f3(ld4(&v.rest[vertex]));
-                            const F3 rd = rv - closest_on_triangle(rv, f3(ld4(&v.rest[t.x])), f3(ld4(&v.rest[t.y])),
-                                                                   f3(ld4(&v.rest[t.z])));
-                            const float rl = dot3(rd, rd);
-                            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
-                        }
-                        delta = nrm * dist;
-                        dist = 0.0f;
-                    }
-                    if (!finite3(nrm)) {
-                        count1(v.counts, kCntIslandGuarded);
-                        continue;
-                    }
-                    const F3 qprev = closest_on_triangle(pp, ap, bp, cp);
-                    const F3 pdelta = pp - qprev;
-                    if (dot3(pdelta, nrm) > target * 0.25f && dot3(delta, nrm) > -target * 0.10f) continue;
-                    float wa, wb, wc;
-                    barycentric(q, a, b2, c, &wa, &wb, &wc);
-                    const float pen = target - dist;
-                    if (pen <= 0.0f) continue;
-                    accepted_tris[contacts++] = tri;
-                    pen_sum += pen;
-                    wsum += __ldg(&v.inv_mass[t.x]) * wa + __ldg(&v.inv_mass[t.y]) * wb + __ldg(&v.inv_mass[t.z]) * wc;
-                    axis = axis + nrm * pen;
-                    if (pen > max_pen) {
-                        max_pen = pen;
-                        best = nrm;
-                    }
-                }
+    bool stop = false;
+    for (int base = 0; base < visit && !stop; base += 32) {
+        const int g = base + lane;
+        int j = 0;  // owner cell: the first lane whose inclusive slot count exceeds g
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= g) j += step;
+        const int o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
+        int tri = -1, code = 0;
+        IslandHit h{0.0f, 0.0f, F3{0.0f, 0.0f, 0.0f}};
+        if (g < visit) {
+            tri = v.tb_ent[o_first + g];
+            code = island_eval(v, vertex, p, pp, target, onset, tri, &h);
+        }
+        const int n = min(32, visit - base);
+        for (int k = 0; k < n; ++k) {
+            if (contacts >= max_contacts || scanned >= scan_limit) {
+                stop = true;
+                break;
             }
+            ++scanned;
+            const int t_k = __shfl_sync(0xffffffffu, tri, k);
+            const int c_k = __shfl_sync(0xffffffffu, code, k);
+            const float pen_k = __shfl_sync(0xffffffffu, h.pen, k), w_k = __shfl_sync(0xffffffffu, h.wterm, k);
+            const F3 n_k{__shfl_sync(0xffffffffu, h.nrm.x, k), __shfl_sync(0xffffffffu, h.nrm.y, k),
+                         __shfl_sync(0xffffffffu, h.nrm.z, k)};
+            if (__any_sync(0xffffffffu, (lane < contacts && acc_lo == t_k) || (lane + 32 < contacts && acc_hi == t_k)))
+                continue;
+            if (c_k == 1) ++guards;
+            if (c_k != 2) continue;
+            if (lane == (contacts & 31)) {
+                if (contacts < 32)
+                    acc_lo = t_k;
+                else
+                    acc_hi = t_k;
+            }
+            ++contacts;
+            pen_sum += pen_k;
+            wsum += w_k;
+            axis = axis + n_k * pen_k;
+            if (pen_k > max_pen) {
+                max_pen = pen_k;
+                best = n_k;
+            }
+        }
+    }
+    if (lane != 0) return;
+    if (guards > 0) count_add(v.counts, kCntIslandGuarded, (unsigned long long)guards);
     if (contacts <= 0) return;
     count_add(v.counts, kCntIslandCandidates, (unsigned long long)contacts);
     if (contacts < 3) {
@@ -2000,8 +2050,8 @@ void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
     if (sv.brute_e && sv.e_all.size() > 0) k_ee_brute<<<grid(sv.e_all.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.e_all));
 }
 void self_island(const View& v, const SelfVariants& sv, cudaStream_t s) {
-    const int qb = tune_of(v.tune, kTuneQueryBlock);
-    if (sv.v_fast.size() > 0) k_island<<<grid(sv.v_fast.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_fast));
+    const int wb = tune_of(v.tune, kTuneWarpBlock);
+    if (sv.v_fast.size() > 0) k_island<<<grid(sv.v_fast.size(), 32, wb), wb, 0, s>>>(ranged(v, sv.v_fast));
 }
 void self_apply(const View& v, const SelfVariants& sv, cudaStream_t s) {
     const int qb = tune_of(v.tune, kTuneQueryBlock);
