@@ -1265,7 +1265,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
 // and pushes as the 8-lane group kernels, which keep the cloths with a
 // smaller budget.
 template <bool kEdge>
-__global__ void __launch_bounds__(kThreads, 4) k_flat_query(View v) {
+__global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
     const int lane = threadIdx.x & 31;
     const int item = v.lo + warp_global_id() * 32 + lane;
     int st = 0, lim = 0;
@@ -1425,7 +1425,7 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
 // recomputed by the same classify call, accumulated in fixed point.
 constexpr int kFastWarps = kThreads / 32;
 
-__global__ void __launch_bounds__(kThreads, 3) k_ee_fast_flat(View v) {
+__global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
     __shared__ unsigned char cls_s[kFastWarps][32 * kBucketSlots];
     __shared__ unsigned key_s[kFastWarps][32 * kBucketSlots];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
