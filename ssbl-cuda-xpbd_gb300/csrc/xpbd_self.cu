@@ -511,7 +511,7 @@ __global__ void k_neighbors_brute(View v, int mode) {
 // Swept-sphere time of impact between the two vertices' prev->current paths,
 // else an overlap push; responses clamped to 0.35 thickness
 // (abi41.cu:4816-4951).
-__global__ void __launch_bounds__(kThreads) k_vv(View v) {
+__global__ void __launch_bounds__(kThreads, 6) k_vv(View v) {
     const int src = v.lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (src >= v.hi) return;
     const Params& P = params_v(v, src);
@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v, int mode) {
 }
 
 // VV responses (strict): lane n handles neighbour n of the source vertex.
-__global__ void __launch_bounds__(kThreads) k_vv_warp(View v) {
+__global__ void __launch_bounds__(kThreads, 8) k_vv_warp(View v) {
     const int src = v.lo + warp_global_id();
     const int lane = threadIdx.x & 31;
     if (src >= v.hi) return;
