@@ -87,8 +87,8 @@ __attribute__((visibility("default"))) long long xpbd_gb300_pc2_close(void* writ
 
 /* Launch configuration (no counterpart in the reference): 11 slots, in order
  * block size of the per-vertex passes (default 128), of the hash count /
- * scatter kernels (256), lanes per primitive of the edge hash (4, 8 or 16;
- * default 8), block size of the warp-per-item kernels (256), of
+ * scatter kernels (256), lanes per primitive of the edge hash (1, 2, 4, 8
+ * or 16; default 8), block size of the warp-per-item kernels (256), of
  * the thread-per-item queries (256), lanes per item of the strict group
  * queries (4, 8 or 16; default 8), block size of the group queries (256), of
  * the dynamic-collider pass (128), the form of the fast-mode edge-edge query

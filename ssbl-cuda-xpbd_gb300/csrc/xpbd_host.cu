@@ -2116,10 +2116,10 @@ namespace {
 
 bool tune_value_ok(int slot, int v) {
     if (v == 0) return true;
-    if (slot == kTunePrimLanes || slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
+    if (slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
+    if (slot == kTunePrimLanes || slot == kTuneTriLanes) return v == 1 || v == 2 || v == 4 || v == 8 || v == 16;
     if (slot == kTuneFastEeForm) return v == 8 || v == 32;
     if (slot == kTuneFusedFrame) return v == 1 || v == 2 || v == 8;
-    if (slot == kTuneTriLanes) return v == 1 || v == 2 || v == 4 || v == 8 || v == 16;
     return v >= 32 && v <= kMaxBlock && v % 32 == 0;
 }
 
@@ -2185,7 +2185,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
     const std::vector<std::vector<short>> cand = {
         {64, 128, 256},   // vertex passes
         {128, 256},       // hash count / scatter
-        {4, 8, 16},       // lanes per primitive
+        {1, 2, 4, 8, 16}, // lanes per edge of the edge hash
         {128, 256},       // warp kernels
         {64, 128, 256},   // thread-per-item queries
         {4, 8, 16},       // group lanes

@@ -219,7 +219,7 @@ struct PcgView {
 enum TuneSlot {
     kTuneVertexBlock = 0,  // per-vertex constraint passes and prediction (default 128)
     kTuneHashBlock,        // hash count / scatter kernels (256)
-    kTunePrimLanes,        // lanes per primitive of the edge hash: 4, 8, 16 (8)
+    kTunePrimLanes,        // lanes per primitive of the edge hash: 1, 2, 4, 8, 16 (8)
     kTuneWarpBlock,        // warp-per-item kernels: neighbour table, strict VV, flat queries, bucket order (256)
     kTuneQueryBlock,       // thread-per-item queries: fast VV / VT, brute queries, islands, apply (256)
     kTuneGroupLanes,       // lanes per item of the strict group queries: 4, 8, 16 (8)
