@@ -2184,7 +2184,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
     }
     const std::vector<std::vector<short>> cand = {
         {64, 128, 256},   // vertex passes
-        {128, 256},       // hash count / scatter
+        {64, 128, 256},   // hash count / scatter
         {1, 2, 4, 8, 16}, // lanes per edge of the edge hash
         {128, 256},       // warp kernels
         {64, 128, 256},   // thread-per-item queries

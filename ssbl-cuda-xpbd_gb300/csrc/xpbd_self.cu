@@ -1891,6 +1891,7 @@ __global__ void __launch_bounds__(kThreads) k_self_apply(View v) {
     const Params& P = params_v(v, i);
     if (!self_scheduled(P, v)) return;
     const Acc4 a = v.acc[i];
+    if (a.w == 0) return;  // every push adds a weight: nothing accumulated, the row is still zero
     v.acc[i] = Acc4{0, 0, 0, 0};
     if (!(__ldg(&v.inv_mass[i]) > 0.0f) || a.w <= 0) return;
     F3 avg = F3{from_fix(a.x), from_fix(a.y), from_fix(a.z)} * (1.0f / (float)a.w);
