@@ -865,53 +865,10 @@ __device__ __forceinline__ long long warp_sum64(long long v) {
     return v;
 }
 
-// VV neighbour table: lane l < 27 scans cell (dz, dy, dx) = (l/9-1, l/3%3-1,
-// l%3-1), the reference's nested-loop order (abi41.cu:4756-4781).
-__global__ void __launch_bounds__(kThreads) k_neighbors_warp(View v, int mode) {
-    const int src = v.lo + warp_global_id();
-    const int lane = threadIdx.x & 31;
-    if (src >= v.hi) return;
-    const Params& P = params_v(v, src);
-    if (!P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
-    const float target = contact_radius(P);
-    if (target <= 0.0f) {
-        if (lane == 0) v.nb_count[src] = 0;
-        return;
-    }
-    const float onset = fmaxf(target * 1.8f, target + kEps);
-    const float4 p = v.pos[src];
-    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
-    int found[kNeighborSlots];
-    int nfound = 0;
-    if (lane < 27) {
-        const int qx = cx + lane % 3 - 1, qy = cy + (lane / 3) % 3 - 1, qz = cz + lane / 9 - 1;
-        const int b = P.vbase + (int)bucket_of(qx, qy, qz, P.vbuckets);
-        const int st = v.vb_start[b];
-        const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
-        for (int k = 0; k < lim; ++k) {
-            const int other = v.vb_ent[st + k];
-            const int4 oc = v.vcell[other];
-            if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
-            found[nfound++] = other;
-        }
-    }
-    const int offset = warp_exclusive_sum(nfound, lane);
-    const int total = __shfl_sync(0xffffffffu, offset + nfound, 31);
-    for (int k = 0; k < nfound && offset + k < kNeighborSlots; ++k) v.nb_idx[src * kNeighborSlots + offset + k] = found[k];
-    if (lane == 0) {
-        if (total >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
-        v.nb_count[src] = min(total, kNeighborSlots);
-    }
-}
-
 // VV responses (strict): lane n handles neighbour n of the source vertex.
-__global__ void __launch_bounds__(kThreads, 8) k_vv_warp(View v) {
-    const int src = v.lo + warp_global_id();
-    const int lane = threadIdx.x & 31;
-    if (src >= v.hi) return;
-    const Params& P = params_v(v, src);
-    if (fast_mode(P) || !self_scheduled(P, v)) return;
-    if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
+// The responses of one strict vertex against its neighbour table (lane n:
+// neighbour n); shared by k_vv_warp and the fused neighbour kernel.
+__device__ __forceinline__ void vv_strict_warp(const View& v, const Params& P, int src, int lane) {
     const int count = min(v.nb_count[src], kNeighborSlots);
     if (count == 0) return;
     long long ax = 0, ay = 0, az = 0;
@@ -1000,6 +957,67 @@ __global__ void __launch_bounds__(kThreads, 8) k_vv_warp(View v) {
             atomicAdd(acc + 2, (unsigned long long)az);
             atomicAdd(acc + 3, (unsigned long long)__popc(hit_mask));
         }
+    }
+}
+
+
+// VV responses of strict cloths whose table k_neighbors_brute built (the
+// hashed ones run fused into k_neighbors_warp); `all` = 1 covers every
+// strict cloth.
+__global__ void __launch_bounds__(kThreads, 8) k_vv_warp(View v, int all) {
+    const int src = v.lo + warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if (src >= v.hi) return;
+    const Params& P = params_v(v, src);
+    if (fast_mode(P) || !self_scheduled(P, v) || (!all && P.vhash)) return;
+    if (!(__ldg(&v.inv_mass[src]) > 0.0f)) return;
+    vv_strict_warp(v, P, src, lane);
+}
+
+// VV neighbour table: lane l < 27 scans cell (dz, dy, dx) = (l/9-1, l/3%3-1,
+// l%3-1), the reference's nested-loop order (abi41.cu:4756-4781).  With kVv
+// (strict passes) the warp then computes the vertex's VV responses from the
+// table it just wrote (the next operation on that branch; positions do not
+// change in between), saving the separate launch and its table reads.
+template <bool kVv>
+__global__ void __launch_bounds__(kThreads, 8) k_neighbors_warp(View v, int mode) {
+    const int src = v.lo + warp_global_id();
+    const int lane = threadIdx.x & 31;
+    if (src >= v.hi) return;
+    const Params& P = params_v(v, src);
+    if (!P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
+    const float target = contact_radius(P);
+    if (target <= 0.0f) {
+        if (lane == 0) v.nb_count[src] = 0;
+        return;
+    }
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    const float4 p = v.pos[src];
+    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
+    int found[kNeighborSlots];
+    int nfound = 0;
+    if (lane < 27) {
+        const int qx = cx + lane % 3 - 1, qy = cy + (lane / 3) % 3 - 1, qz = cz + lane / 9 - 1;
+        const int b = P.vbase + (int)bucket_of(qx, qy, qz, P.vbuckets);
+        const int st = v.vb_start[b];
+        const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
+        for (int k = 0; k < lim; ++k) {
+            const int other = v.vb_ent[st + k];
+            const int4 oc = v.vcell[other];
+            if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
+            found[nfound++] = other;
+        }
+    }
+    const int offset = warp_exclusive_sum(nfound, lane);
+    const int total = __shfl_sync(0xffffffffu, offset + nfound, 31);
+    for (int k = 0; k < nfound && offset + k < kNeighborSlots; ++k) v.nb_idx[src * kNeighborSlots + offset + k] = found[k];
+    if (lane == 0) {
+        if (total >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
+        v.nb_count[src] = min(total, kNeighborSlots);
+    }
+    if (kVv) {
+        __syncwarp();  // the table's writes are visible to the whole warp
+        if (__ldg(&v.inv_mass[src]) > 0.0f) vv_strict_warp(v, P, src, lane);
     }
 }
 
@@ -2017,12 +2035,17 @@ void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_
     const ItemRange& r = mode == 1 ? sv.v_fast : (mode == 2 ? sv.v_strict : sv.v_all);
     if (r.size() == 0) return;
     const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
-    if (sv.hashed_v) k_neighbors_warp<<<grid(r.size(), 32, wb), wb, 0, s>>>(ranged(v, r), mode);
+    if (sv.hashed_v && mode == 2)
+        k_neighbors_warp<true><<<grid(r.size(), 32, wb), wb, 0, s>>>(ranged(v, r), mode);
+    else if (sv.hashed_v)
+        k_neighbors_warp<false><<<grid(r.size(), 32, wb), wb, 0, s>>>(ranged(v, r), mode);
     if (sv.brute_v) k_neighbors_brute<<<grid(r.size(), 1, qb), qb, 0, s>>>(ranged(v, r), mode);
 }
 void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s) {
     const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
-    if (sv.strict && sv.v_strict.size() > 0) k_vv_warp<<<grid(sv.v_strict.size(), 32, wb), wb, 0, s>>>(ranged(v, sv.v_strict));
+    // hashed strict cloths get their responses in the fused neighbour kernel
+    if (sv.strict && sv.brute_v && sv.v_strict.size() > 0)
+        k_vv_warp<<<grid(sv.v_strict.size(), 32, wb), wb, 0, s>>>(ranged(v, sv.v_strict), 0);
     if (sv.fast && sv.v_fast.size() > 0) k_vv<<<grid(sv.v_fast.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_fast));
 }
 void self_vt(const View& v, const SelfVariants& sv, cudaStream_t s) {
