@@ -127,14 +127,15 @@ struct CellRange {
     int x0, x1, y0, y1, z0, z1;
 };
 
-__device__ CellRange primitive_cells(const View& v, F3 lo, F3 hi, F3 fallback, float cell, bool count_guard) {
+// *collapsed is set when the range collapsed (the caller counts it).
+__device__ CellRange primitive_cells(F3 lo, F3 hi, F3 fallback, float cell, bool* collapsed) {
     CellRange r{cell_of(lo.x, cell), cell_of(hi.x, cell), cell_of(lo.y, cell),
                 cell_of(hi.y, cell), cell_of(lo.z, cell), cell_of(hi.z, cell)};
     const long long sx = (long long)r.x1 - r.x0 + 1, sy = (long long)r.y1 - r.y0 + 1, sz = (long long)r.z1 - r.z0 + 1;
     if (sx <= 0 || sy <= 0 || sz <= 0) return r;
     if (sx * sy * sz <= (long long)kMaxPrimitiveCells) return r;
     const int fx = cell_of(fallback.x, cell), fy = cell_of(fallback.y, cell), fz = cell_of(fallback.z, cell);
-    if (count_guard) count1(v.counts, kCntSelfOverflow);
+    *collapsed = true;
     return CellRange{fx, fx, fy, fy, fz, fz};
 }
 
@@ -144,7 +145,7 @@ __device__ bool tri_valid(int nV, int4 t) {
 
 __device__ bool edge_valid(int nV, int2 e) { return e.x >= 0 && e.y >= 0 && e.x < nV && e.y < nV && e.x != e.y; }
 
-__device__ CellRange tri_cells(const View& v, const Params& P, int t, bool* ok, bool count_guard) {
+__device__ CellRange tri_cells(const View& v, const Params& P, int t, bool* ok, bool* collapsed) {
     const int4 tr = __ldg(&v.tris[t]);
     *ok = tri_valid(v.nV, tr);
     if (!*ok) return CellRange{0, -1, 0, -1, 0, -1};
@@ -153,10 +154,10 @@ __device__ CellRange tri_cells(const View& v, const Params& P, int t, bool* ok, 
     const F3 lo{fminf(a.x, fminf(b.x, c.x)) - m, fminf(a.y, fminf(b.y, c.y)) - m, fminf(a.z, fminf(b.z, c.z)) - m};
     const F3 hi{fmaxf(a.x, fmaxf(b.x, c.x)) + m, fmaxf(a.y, fmaxf(b.y, c.y)) + m, fmaxf(a.z, fmaxf(b.z, c.z)) + m};
     const F3 centroid = ((a + b) + c) * (1.0f / 3.0f);
-    return primitive_cells(v, lo, hi, centroid, P.tcell, count_guard);
+    return primitive_cells(lo, hi, centroid, P.tcell, collapsed);
 }
 
-__device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok, bool count_guard) {
+__device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok, bool* collapsed) {
     const int2 ed = __ldg(&v.edges[e]);
     *ok = edge_valid(v.nV, ed);
     if (!*ok) return CellRange{0, -1, 0, -1, 0, -1};
@@ -165,7 +166,7 @@ __device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok,
     const F3 lo{fminf(a.x, b.x) - m, fminf(a.y, b.y) - m, fminf(a.z, b.z) - m};
     const F3 hi{fmaxf(a.x, b.x) + m, fmaxf(a.y, b.y) + m, fmaxf(a.z, b.z) + m};
     const F3 mid = (a + b) * 0.5f;
-    return primitive_cells(v, lo, hi, mid, P.ecell, count_guard);
+    return primitive_cells(lo, hi, mid, P.ecell, collapsed);
 }
 
 __global__ void k_vhash_count(View v) {
@@ -198,31 +199,40 @@ __global__ void k_vhash_scatter(View v) {
 // fixed afterwards by k_bucket_sort where a query depends on it.
 
 
+// Collapsed ranges are counted as guard events in the count pass, once per
+// primitive, with one ballot per warp (every lane reaches it).
 template <bool kTri, int L>
 __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = v.lo + (int)(t / L), r0 = (int)(t % L);
-    if (k >= v.hi) return;
-    const Params& P = kTri ? params_t(v, k) : params_e(v, k);
-    if (!(kTri ? P.thash : P.ehash) || !self_scheduled(P, v)) return;
-    bool ok = false;
-    const CellRange r = kTri ? tri_cells(v, P, k, &ok, !scatter && r0 == 0) : edge_cells(v, P, k, &ok, !scatter && r0 == 0);
-    if (!ok) return;
-    const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
-    if (nx <= 0 || ny <= 0 || nz <= 0) return;
-    int* cnt = kTri ? v.tb_count : v.eb_count;
-    int* ent = kTri ? v.tb_ent : v.eb_ent;
-    const int nb = kTri ? P.tbuckets : P.ebuckets;
-    const int base = kTri ? P.tbase : P.ebase;
-    for (int row = r0; row < ny * nz; row += L) {
-        const int y = r.y0 + row % ny, z = r.z0 + row / ny;
-        for (int x = r.x0; x <= r.x1; ++x) {
-            int* slot_counter = &cnt[base + (int)bucket_of(x, y, z, nb)];
-            if (scatter)
-                ent[atomicAdd(slot_counter, 1)] = k;
-            else
-                atomicAdd(slot_counter, 1);  // no return value needed: a reduction
+    bool collapsed = false;
+    if (k < v.hi) {
+        const Params& P = kTri ? params_t(v, k) : params_e(v, k);
+        if ((kTri ? P.thash : P.ehash) && self_scheduled(P, v)) {
+            bool ok = false;
+            const CellRange r = kTri ? tri_cells(v, P, k, &ok, &collapsed) : edge_cells(v, P, k, &ok, &collapsed);
+            const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
+            if (ok && nx > 0 && ny > 0 && nz > 0) {
+                int* cnt = kTri ? v.tb_count : v.eb_count;
+                int* ent = kTri ? v.tb_ent : v.eb_ent;
+                const int nb = kTri ? P.tbuckets : P.ebuckets;
+                const int base = kTri ? P.tbase : P.ebase;
+                for (int row = r0; row < ny * nz; row += L) {
+                    const int y = r.y0 + row % ny, z = r.z0 + row / ny;
+                    for (int x = r.x0; x <= r.x1; ++x) {
+                        int* slot_counter = &cnt[base + (int)bucket_of(x, y, z, nb)];
+                        if (scatter)
+                            ent[atomicAdd(slot_counter, 1)] = k;
+                        else
+                            atomicAdd(slot_counter, 1);  // no return value needed: a reduction
+                    }
+                }
+            }
         }
+    }
+    if (!scatter) {
+        const unsigned m = __ballot_sync(0xffffffffu, collapsed && r0 == 0);
+        if ((threadIdx.x & 31) == 0 && m) count_add(v.counts, kCntSelfOverflow, (unsigned long long)__popc(m));
     }
 }
 
