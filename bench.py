@@ -69,6 +69,9 @@ DESCRIPTIONS = {
     "serve": "serving: Poisson arrivals 200/s of cloth solves, V log-uniform 1k-250k (16 grid sizes), horizons "
              "30-240 frames, random sphere and/or box/torus SDF, strict self collision 2 mm, admitted by a "
              "device-memory budget, resident until done, one frame per resident request per tick",
+    "prep": "input preprocessing: constraint inputs of a 500x500 cloth (250,000 verts, 498,002 tris, jittered, "
+            "2 hard pins + hidden tethers) from host arrays to host arrays; edges, rest lengths and inverse masses "
+            "on the device, colouring and bend pairs native on the host",
 }
 
 
@@ -286,6 +289,85 @@ def time_plain(native, scs, frames: int) -> dict:
             "handles": len(scs), "launches_per_step": launches}
 
 
+def run_prep(args, world, rank, local):
+    """Input preprocessing of a 250k-vertex cloth: one step = one cloth's
+    constraint inputs built from host arrays (scene.build_cloth with the
+    device path), against the numpy restatement of the add-on's builder.
+    The metric is vertices per second."""
+    n = 500
+    pos, tris = scene.grid_mesh(n, 5.0, 0.0)
+    pos = (pos + np.random.default_rng(0).uniform(-1e-3, 1e-3, pos.shape)).astype(np.float32)
+    w = np.zeros(len(pos), np.float32)
+    w[[0, n - 1]] = 1.0
+    V = len(pos)
+
+    def numpy_build():
+        return scene.build_cloth(pos, tris, 0.2, w, tether_slack=1.05)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        for _ in range(args.warmup):
+            numpy_build()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            numpy_build()
+        el = time.perf_counter() - t0
+        value = V * args.steps / el
+        print(json.dumps({"impl": "reference", "metric": "vertices/s", "value": value, "unit": "vertices/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered grid)",
+                          "config": {"workload": DESCRIPTIONS["prep"], "vertices": V, "triangles": len(tris)},
+                          "cpu_baseline": {"value": value, "unit": "vertices/s", "cores": 1, "kind": "port",
+                                           "sample": "the whole workload: numpy restatement of the builder"},
+                          "e2e": {"value": value, "unit": "vertices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    from xpbd_gb300 import build
+
+    build.build()
+    hard = w >= scene.PIN_HARD_WEIGHT_THRESHOLD
+    for _ in range(args.warmup):
+        scene.build_cloth(pos, tris, 0.2, w, tether_slack=1.05, device=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        scene.build_cloth(pos, tris, 0.2, w, tether_slack=1.05, device=True)
+    el = time.perf_counter() - t0
+    # the device step alone, and the numpy steps it replaces
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        scene.cloth_inputs_device(pos, tris, 0.2, hard)
+    dev = (time.perf_counter() - t1) / args.steps
+    t2 = time.perf_counter()
+    scene.edge_constraints(tris, pos)
+    scene.vertex_inverse_mass(pos, tris, 0.2, hard)
+    ref_steps = time.perf_counter() - t2
+    t3 = time.perf_counter()
+    numpy_build()
+    ref_full = time.perf_counter() - t3
+    value = V * args.steps * world / el
+    if rank != 0:
+        return
+    line = {
+        "metric": "vertices/s", "value": value, "unit": "vertices/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered grid)",
+        "config": {"workload": DESCRIPTIONS["prep"], "vertices": V, "triangles": len(tris), "parallelism": f"replicas x{world}"},
+        "device_step": {"ms": 1000.0 * dev, "replaces_numpy_ms": 1000.0 * ref_steps,
+                        "what": "edges + rest lengths + inverse masses (host arrays in and out)"},
+        "gpu_launches": 12 * args.steps,
+        "cpu_baseline": {"value": V / ref_full, "unit": "vertices/s", "cores": 1, "kind": "port",
+                         "sample": "one numpy build of the same cloth"},
+        "e2e": {"value": value, "unit": "vertices/s", "h2d_bytes_per_step": int(pos.nbytes + tris.nbytes + V),
+                "d2h_bytes_per_step": int(3 * len(tris) * 12 + V * 4)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_diff(args, world, rank, local):
     """Differentiable form: one step = a 60-frame rollout of the 64 x 64
     cloth and the adjoint of an L2 loss (vertex-substeps/s of the forward
@@ -436,6 +518,9 @@ def main():
         return
     if args.workload == "diff":
         run_diff(args, world, rank, local)
+        return
+    if args.workload == "prep":
+        run_prep(args, world, rank, local)
         return
     scs = workload(args.workload, args.batch_cloths)
     if args.batch_cloths != 256 and args.workload == "batch256":

@@ -141,6 +141,13 @@ def _native_prep():
                 lib.xpbd_gb300_greedy_color.restype = ctypes.c_int
                 lib.xpbd_gb300_bend_pairs.argtypes = [pi, ctypes.c_int, pi, ctypes.c_int]
                 lib.xpbd_gb300_bend_pairs.restype = ctypes.c_int
+                if hasattr(lib, "xpbd_gb300_prepare_cloth_device"):
+                    pf = ctypes.POINTER(ctypes.c_float)
+                    lib.xpbd_gb300_prepare_cloth_device.argtypes = [
+                        pf, ctypes.c_int, pi, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                        ctypes.POINTER(ctypes.c_ubyte), pi, pf, pf]
+                    lib.xpbd_gb300_prepare_cloth_device.restype = ctypes.c_int
+                    lib.ssbl_last_error.restype = ctypes.c_char_p
                 _PREP = lib
             else:
                 _PREP = False
@@ -239,6 +246,33 @@ def greedy_colors_py(pairs: np.ndarray, vertex_count: int) -> np.ndarray:
     return colors
 
 
+def cloth_inputs_device(rest: np.ndarray, triangles: np.ndarray, density: float, pin_mask: np.ndarray):
+    """Edges, edge rest lengths and inverse masses computed on the GPU
+    (xpbd_gb300_prepare_cloth_device); bit-identical to edge_constraints
+    and vertex_inverse_mass.  Needs the built library and a GPU."""
+    import ctypes
+
+    lib = _native_prep()
+    if lib is None or not hasattr(lib, "xpbd_gb300_prepare_cloth_device"):
+        raise RuntimeError("device preprocessing needs the built GB300 library")
+    pos = np.ascontiguousarray(rest, np.float32)
+    tris = np.ascontiguousarray(triangles, np.int32)
+    hard = np.ascontiguousarray(pin_mask, np.uint8)
+    V, T = len(pos), len(tris)
+    edges = np.empty((max(3 * T, 1), 2), np.int32)
+    edge_rest = np.empty(max(3 * T, 1), np.float32)
+    inv = np.empty(max(V, 1), np.float32)
+    pf, pi = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
+    # the builders scale areas by max(density, eps) as a float32 factor
+    n = lib.xpbd_gb300_prepare_cloth_device(
+        pos.ctypes.data_as(pf), V, tris.ctypes.data_as(pi), T, float(np.float32(max(density, _EPS))), float(np.float32(_EPS)),
+        hard.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), edges.ctypes.data_as(pi), edge_rest.ctypes.data_as(pf),
+        inv.ctypes.data_as(pf))
+    if n < 0:
+        raise RuntimeError((lib.ssbl_last_error() or b"").decode() or "device preprocessing failed")
+    return edges[:n].copy(), edge_rest[:n].copy(), inv[:V].copy()
+
+
 def vertex_inverse_mass(rest: np.ndarray, triangles: np.ndarray, density: float, pin_mask: np.ndarray) -> np.ndarray:
     mass = np.zeros(len(rest), dtype=np.float64)
     p0, p1, p2 = rest[triangles[:, 0]], rest[triangles[:, 1]], rest[triangles[:, 2]]
@@ -306,15 +340,22 @@ def build_cloth(
     density: float,
     pin_weights_by_vertex: np.ndarray,
     tether_slack: float | None = None,
+    device: bool = False,
 ) -> ClothData:
     """Constraint inputs of a cloth from its rest pose and per-vertex pin
-    weights (the steps of xpbd_core.py:_build_cloth_data_uncached)."""
+    weights (the steps of xpbd_core.py:_build_cloth_data_uncached).  With
+    `device`, edges, rest lengths and inverse masses come from the GPU
+    (cloth_inputs_device), the same arrays bit for bit."""
     world = np.ascontiguousarray(positions, dtype=np.float32)
     tris = np.ascontiguousarray(triangles, dtype=np.int32)
     weights = np.asarray(pin_weights_by_vertex, dtype=np.float32)
     pin_mask = weights > 0.0
     hard = weights >= PIN_HARD_WEIGHT_THRESHOLD
-    edges, edge_rest = edge_constraints(tris, world)
+    if device:
+        edges, edge_rest, inv = cloth_inputs_device(world, tris, density, hard)
+    else:
+        edges, edge_rest = edge_constraints(tris, world)
+        inv = None
     edges, edge_rest, edge_off = color_constraints(edges, edge_rest, len(world))
     bends, bend_rest = bend_constraints(tris, world)
     bends, bend_rest, bend_off = color_constraints(bends, bend_rest, len(world))
@@ -322,7 +363,8 @@ def build_cloth(
         lra, lra_rest = hidden_tethers(world, hard, tether_slack)
     else:
         lra, lra_rest = np.empty((0, 2), np.int32), np.empty(0, np.float32)
-    inv = vertex_inverse_mass(world, tris, density, hard)
+    if inv is None:
+        inv = vertex_inverse_mass(world, tris, density, hard)
     pins = np.flatnonzero(pin_mask).astype(np.int32)
     return ClothData(
         positions_world=world,
