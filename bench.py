@@ -70,8 +70,8 @@ DESCRIPTIONS = {
              "30-240 frames, random sphere and/or box/torus SDF, strict self collision 2 mm, admitted by a "
              "device-memory budget, resident until done, one frame per resident request per tick",
     "prep": "input preprocessing: constraint inputs of a 500x500 cloth (250,000 verts, 498,002 tris, jittered, "
-            "2 hard pins + hidden tethers) from host arrays to host arrays; edges, rest lengths and inverse masses "
-            "on the device, colouring and bend pairs native on the host",
+            "2 hard pins + hidden tethers) from host arrays to host arrays; edges, bend pairs, rest lengths and "
+            "inverse masses on the device, greedy colouring and tethers on the host",
 }
 
 
@@ -344,6 +344,7 @@ def run_prep(args, world, rank, local):
     dev = (time.perf_counter() - t1) / args.steps
     t2 = time.perf_counter()
     scene.edge_constraints(tris, pos)
+    scene.bend_constraints(tris, pos)
     scene.vertex_inverse_mass(pos, tris, 0.2, hard)
     ref_steps = time.perf_counter() - t2
     t3 = time.perf_counter()
@@ -358,8 +359,8 @@ def run_prep(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered grid)",
         "config": {"workload": DESCRIPTIONS["prep"], "vertices": V, "triangles": len(tris), "parallelism": f"replicas x{world}"},
         "device_step": {"ms": 1000.0 * dev, "replaces_numpy_ms": 1000.0 * ref_steps,
-                        "what": "edges + rest lengths + inverse masses (host arrays in and out)"},
-        "gpu_launches": 12 * args.steps,
+                        "what": "edges + bend pairs + rest lengths + inverse masses (host arrays in and out)"},
+        "gpu_launches": 33 * args.steps,  # kernels of one xpbd_gb300_prepare_cloth_device call
         "cpu_baseline": {"value": V / ref_full, "unit": "vertices/s", "cores": 1, "kind": "port",
                          "sample": "one numpy build of the same cloth"},
         "e2e": {"value": value, "unit": "vertices/s", "h2d_bytes_per_step": int(pos.nbytes + tris.nbytes + V),

@@ -221,18 +221,21 @@ __attribute__((visibility("default"))) int xpbd_gb300_greedy_color(const int* pa
 __attribute__((visibility("default"))) int xpbd_gb300_bend_pairs(const int* triangles, int triangle_count, int* pairs,
                                                                   int max_pairs);
 /* Device input preprocessing (replaces the per-element steps of the add-on's
- * cloth builder, xpbd_core.py:715-727 and 862-881): from rest positions
+ * cloth builder, xpbd_core.py:715-747 and 862-881): from rest positions
  * (V x 3), triangles (T x 3, indices in [0, V)), the area density factor
  * max(density, eps) and the hard-pin mask (V bytes, may be null), writes the
  * distinct triangle sides as (lower, upper) pairs in lexicographic order with
- * rest lengths max(|x_b - x_a|, eps) (room for 3T pairs) and the inverse
- * masses (float64 area sums; 0 for hard pins).  Returns the edge count, or
- * -1 with ssbl_last_error() set (an index outside the vertices included). */
+ * rest lengths max(|x_b - x_a|, eps) (room for 3T pairs), the inverse masses
+ * (float64 area sums; 0 for hard pins) and, when `bends` is not null, the
+ * bend pairs of xpbd_gb300_bend_pairs with their rest lengths (room for 3T;
+ * count in *bend_count).  Returns the edge count, or -1 with
+ * ssbl_last_error() set (an index outside the vertices included). */
 __attribute__((visibility("default"))) int xpbd_gb300_prepare_cloth_device(const float* positions, int vertex_count,
                                                                             const int* triangles, int triangle_count,
                                                                             float density, float eps,
                                                                             const unsigned char* hard, int* edges,
-                                                                            float* edge_rest, float* inv_mass);
+                                                                            float* edge_rest, float* inv_mass, int* bends,
+                                                                            float* bend_rest, int* bend_count);
 
 /* Wait for the solver's stream. */
 __attribute__((visibility("default"))) int xpbd_gb300_synchronize(void* handle);

@@ -1,9 +1,11 @@
 // Device preprocessing of a cloth's constraint inputs: the unique edges of a
-// triangle mesh with their rest lengths and the per-vertex inverse masses
-// from triangle areas, the per-element steps of the reference's input
-// pipeline (xpbd_core.py:715-727 edges, 862-881 masses) that dominate the
-// cost of building large cloths.  Greedy colouring stays on the host
-// (xpbd_prep.cu): first-fit in constraint order is sequential by definition.
+// triangle mesh with their rest lengths, the bend pairs with theirs, and the
+// per-vertex inverse masses from triangle areas, the per-element steps of the
+// reference's input pipeline (xpbd_core.py:715-747 edges and bends, 862-881
+// masses) that dominate the cost of building large cloths.  Greedy colouring
+// stays on the host (xpbd_prep.cu): first-fit in constraint order is
+// sequential by definition; so do the hidden tethers (a k-d tree query whose
+// tie-breaking between equidistant pins a device argmin would not repeat).
 //
 // Results are bit-identical to the cloth builders' numpy restatement:
 // * edges are the distinct (min, max) endpoint pairs of every triangle side
@@ -11,6 +13,8 @@
 //   endpoint (count, scan, scatter), each row sorted and deduplicated;
 // * rest length = max(|x_b - x_a|, eps) in float32 with the sum of squares
 //   taken x, y, z in order (np.linalg.norm over a row of three);
+// * bend pairs as xpbd_gb300_bend_pairs writes them (below), rest lengths
+//   as for edges;
 // * mass = float64 sum of float32 shares max(area * density, eps) / 3 in
 //   np.add.at order (corner 0 of every triangle in index order, then corner
 //   1, then 2): a CSR keyed by vertex with entries corner * T + t, sorted;
@@ -98,6 +102,63 @@ __global__ void k_edge_emit(const int* start, const int* ent, const int* edge_st
     }
 }
 
+// Bend pairs (xpbd_core.py:730-747): sides keyed by their lower endpoint,
+// entries (upper endpoint << 32 | side index s = 3 t + j), so a sorted row
+// lists every edge's sides in triangle order.  The first side of an edge
+// gives the reference opposite vertex; each later side whose opposite vertex
+// differs yields the pair (min, max) of the two opposite vertices.  Pairs are
+// written into the row's own slots (at most one per side).
+__global__ void k_side_scatter64(const int* tris, int T, int* cursor, long long* ent) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= 3ll * T) return;
+    int lo, hi;
+    side(tris, (int)(s / 3), (int)(s % 3), &lo, &hi);
+    ent[atomicAdd(&cursor[lo], 1)] = ((long long)hi << 32) | (long long)s;
+}
+
+__global__ void k_bend_rows(const int* start, long long* ent, const int* tris, int V, int* pair_p, int* pair_q,
+                            int* row_pairs) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= V) return;
+    long long* r = ent + start[x];
+    const int n = start[x + 1] - start[x];
+    for (int i = 1; i < n; ++i) {
+        const long long key = r[i];
+        int j = i - 1;
+        while (j >= 0 && r[j] > key) {
+            r[j + 1] = r[j];
+            --j;
+        }
+        r[j + 1] = key;
+    }
+    int m = 0, first_opp = 0;
+    for (int i = 0; i < n; ++i) {
+        const int y = (int)(r[i] >> 32), s = (int)(r[i] & 0xffffffffll);
+        const int opp = tris[3 * (s / 3) + (s % 3 + 2) % 3];
+        if (i == 0 || y != (int)(r[i - 1] >> 32)) {
+            first_opp = opp;
+        } else if (opp != first_opp) {
+            pair_p[start[x] + m] = min(first_opp, opp);
+            pair_q[start[x] + m] = max(first_opp, opp);
+            ++m;
+        }
+    }
+    row_pairs[x] = m;
+}
+
+__global__ void k_pair_count(const int* start, const int* pair_p, const int* row_pairs, int V, int* count) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= V) return;
+    for (int i = 0; i < row_pairs[x]; ++i) atomicAdd(&count[pair_p[start[x] + i]], 1);
+}
+
+__global__ void k_pair_scatter(const int* start, const int* pair_p, const int* pair_q, const int* row_pairs, int V,
+                               int* cursor, int* ent) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= V) return;
+    for (int i = 0; i < row_pairs[x]; ++i) ent[atomicAdd(&cursor[pair_p[start[x] + i]], 1)] = pair_q[start[x] + i];
+}
+
 // Per triangle: max(area * density, eps) / 3 in float32.
 __global__ void k_share(const int* tris, int T, const float* pos, float density, float eps, float* share) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -149,14 +210,22 @@ bool alloc(T** p, size_t n, std::vector<void*>* owned) {
 
 using namespace xg;
 
-// Edges, rest lengths and inverse masses of a cloth from its rest positions
-// (V x 3 float), triangles (T x 3 int, indices in [0, V)), density and hard
-// pin mask (V bytes, non-zero = pinned; may be null).  `edges` holds room
-// for 3T pairs, `edge_rest` for 3T floats, `inv_mass` for V floats.
-// Returns the number of edges, or -1 (ssbl_last_error() says why).
+// Edges, rest lengths, inverse masses and (when `bends` is given) bend pairs
+// with their rest lengths of a cloth from its rest positions (V x 3 float),
+// triangles (T x 3 int, indices in [0, V)), density and hard pin mask (V
+// bytes, non-zero = pinned; may be null).  `edges` / `bends` hold room for
+// 3T pairs, `edge_rest` / `bend_rest` for 3T floats, `inv_mass` for V
+// floats; *bend_count receives the bend count.  Returns the number of edges,
+// or -1 (ssbl_last_error() says why).
 XG_EXPORT int xpbd_gb300_prepare_cloth_device(const float* positions, int vertex_count, const int* triangles,
                                               int triangle_count, float density, float eps, const unsigned char* hard,
-                                              int* edges, float* edge_rest, float* inv_mass) {
+                                              int* edges, float* edge_rest, float* inv_mass, int* bends,
+                                              float* bend_rest, int* bend_count) {
+    if (bend_count) *bend_count = 0;
+    if (bends && (!bend_rest || !bend_count)) {
+        set_last_error("invalid cloth preprocessing request");
+        return -1;
+    }
     const int V = vertex_count, T = triangle_count;
     if (V < 0 || T < 0 || (V > 0 && (!positions || !inv_mass)) || (T > 0 && (!triangles || !edges || !edge_rest)) ||
         3ll * T > (1ll << 30)) {
@@ -214,6 +283,39 @@ XG_EXPORT int xpbd_gb300_prepare_cloth_device(const float* positions, int vertex
     scan_bucket_counts(d_count, d_start, V, d_sums, st);
     if (S > 0) k_corner_scatter<<<blocks_of(S), kPrepThreads, 0, st>>>(d_tris, T, d_count, d_ent);
     k_inverse_mass<<<blocks_of(V), kPrepThreads, 0, st>>>(d_start, d_ent, d_share, std::max(T, 1), d_hard, V, d_inv);
+    // bend pairs: side CSR with (upper << 32 | side) entries, pairs per row,
+    // then a CSR of the pairs by lower vertex, sorted and deduplicated
+    int NB = 0;
+    if (bends && S > 0) {
+        long long* d_ent64;
+        int *d_pp, *d_pq, *d_rowp, *d_bent, *d_bstart, *d_bedges;
+        float* d_brest;
+        if (!alloc(&d_ent64, (size_t)S, &owned) || !alloc(&d_pp, (size_t)S, &owned) || !alloc(&d_pq, (size_t)S, &owned) ||
+            !alloc(&d_rowp, V, &owned) || !alloc(&d_bent, (size_t)S, &owned) || !alloc(&d_bstart, V + 1ull, &owned) ||
+            !alloc(&d_bedges, 2ull * S, &owned) || !alloc(&d_brest, (size_t)S, &owned))
+            return finish(0, "device allocation");
+        int* d_side_start = d_estart;  // free after the edge emit: reuse for the side CSR offsets
+        int* d_pstart = d_distinct;    // and for the pair CSR offsets' scratch counts
+        cudaMemsetAsync(d_count, 0, sizeof(int) * V, st);
+        k_side_count<<<blocks_of(S), kPrepThreads, 0, st>>>(d_tris, T, d_count);
+        scan_bucket_counts(d_count, d_side_start, V, d_sums, st);
+        k_side_scatter64<<<blocks_of(S), kPrepThreads, 0, st>>>(d_tris, T, d_count, d_ent64);
+        k_bend_rows<<<blocks_of(V), kPrepThreads, 0, st>>>(d_side_start, d_ent64, d_tris, V, d_pp, d_pq, d_rowp);
+        cudaMemsetAsync(d_count, 0, sizeof(int) * V, st);
+        k_pair_count<<<blocks_of(V), kPrepThreads, 0, st>>>(d_side_start, d_pp, d_rowp, V, d_count);
+        scan_bucket_counts(d_count, d_start, V, d_sums, st);
+        k_pair_scatter<<<blocks_of(V), kPrepThreads, 0, st>>>(d_side_start, d_pp, d_pq, d_rowp, V, d_count, d_bent);
+        k_side_unique<<<blocks_of(V), kPrepThreads, 0, st>>>(d_start, d_bent, V, d_pstart);
+        scan_bucket_counts(d_pstart, d_bstart, V, d_sums, st);
+        k_edge_emit<<<blocks_of(V), kPrepThreads, 0, st>>>(d_start, d_bent, d_bstart, d_pos, V, eps, d_bedges, d_brest);
+        if (cudaMemcpyAsync(&NB, d_bstart + V, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return finish(0, "bend build");
+        if (NB > 0 && (cudaMemcpyAsync(bends, d_bedges, sizeof(int) * 2 * NB, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                       cudaMemcpyAsync(bend_rest, d_brest, sizeof(float) * NB, cudaMemcpyDeviceToHost, st) != cudaSuccess))
+            return finish(0, "bend download");
+    }
+    if (bend_count) *bend_count = NB;
     ok = (E == 0 || (cudaMemcpyAsync(edges, d_edges, sizeof(int) * 2 * E, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
                      cudaMemcpyAsync(edge_rest, d_rest, sizeof(float) * E, cudaMemcpyDeviceToHost, st) == cudaSuccess)) &&
          cudaMemcpyAsync(inv_mass, d_inv, sizeof(float) * V, cudaMemcpyDeviceToHost, st) == cudaSuccess &&

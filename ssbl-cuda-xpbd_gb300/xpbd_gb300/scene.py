@@ -145,7 +145,7 @@ def _native_prep():
                     pf = ctypes.POINTER(ctypes.c_float)
                     lib.xpbd_gb300_prepare_cloth_device.argtypes = [
                         pf, ctypes.c_int, pi, ctypes.c_int, ctypes.c_float, ctypes.c_float,
-                        ctypes.POINTER(ctypes.c_ubyte), pi, pf, pf]
+                        ctypes.POINTER(ctypes.c_ubyte), pi, pf, pf, pi, pf, pi]
                     lib.xpbd_gb300_prepare_cloth_device.restype = ctypes.c_int
                     lib.ssbl_last_error.restype = ctypes.c_char_p
                 _PREP = lib
@@ -247,9 +247,10 @@ def greedy_colors_py(pairs: np.ndarray, vertex_count: int) -> np.ndarray:
 
 
 def cloth_inputs_device(rest: np.ndarray, triangles: np.ndarray, density: float, pin_mask: np.ndarray):
-    """Edges, edge rest lengths and inverse masses computed on the GPU
-    (xpbd_gb300_prepare_cloth_device); bit-identical to edge_constraints
-    and vertex_inverse_mass.  Needs the built library and a GPU."""
+    """Edges, edge rest lengths, inverse masses, bend pairs and bend rest
+    lengths computed on the GPU (xpbd_gb300_prepare_cloth_device);
+    bit-identical to edge_constraints, vertex_inverse_mass and
+    bend_constraints.  Needs the built library and a GPU."""
     import ctypes
 
     lib = _native_prep()
@@ -262,15 +263,19 @@ def cloth_inputs_device(rest: np.ndarray, triangles: np.ndarray, density: float,
     edges = np.empty((max(3 * T, 1), 2), np.int32)
     edge_rest = np.empty(max(3 * T, 1), np.float32)
     inv = np.empty(max(V, 1), np.float32)
+    bends = np.empty((max(3 * T, 1), 2), np.int32)
+    bend_rest = np.empty(max(3 * T, 1), np.float32)
+    nb = ctypes.c_int(0)
     pf, pi = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
     # the builders scale areas by max(density, eps) as a float32 factor
     n = lib.xpbd_gb300_prepare_cloth_device(
         pos.ctypes.data_as(pf), V, tris.ctypes.data_as(pi), T, float(np.float32(max(density, _EPS))), float(np.float32(_EPS)),
         hard.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), edges.ctypes.data_as(pi), edge_rest.ctypes.data_as(pf),
-        inv.ctypes.data_as(pf))
+        inv.ctypes.data_as(pf), bends.ctypes.data_as(pi), bend_rest.ctypes.data_as(pf), ctypes.byref(nb))
     if n < 0:
         raise RuntimeError((lib.ssbl_last_error() or b"").decode() or "device preprocessing failed")
-    return edges[:n].copy(), edge_rest[:n].copy(), inv[:V].copy()
+    return (edges[:n].copy(), edge_rest[:n].copy(), inv[:V].copy(), bends[:nb.value].copy(),
+            bend_rest[:nb.value].copy())
 
 
 def vertex_inverse_mass(rest: np.ndarray, triangles: np.ndarray, density: float, pin_mask: np.ndarray) -> np.ndarray:
@@ -352,12 +357,12 @@ def build_cloth(
     pin_mask = weights > 0.0
     hard = weights >= PIN_HARD_WEIGHT_THRESHOLD
     if device:
-        edges, edge_rest, inv = cloth_inputs_device(world, tris, density, hard)
+        edges, edge_rest, inv, bends, bend_rest = cloth_inputs_device(world, tris, density, hard)
     else:
         edges, edge_rest = edge_constraints(tris, world)
+        bends, bend_rest = bend_constraints(tris, world)
         inv = None
     edges, edge_rest, edge_off = color_constraints(edges, edge_rest, len(world))
-    bends, bend_rest = bend_constraints(tris, world)
     bends, bend_rest, bend_off = color_constraints(bends, bend_rest, len(world))
     if tether_slack is not None:
         lra, lra_rest = hidden_tethers(world, hard, tether_slack)

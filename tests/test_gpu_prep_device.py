@@ -1,8 +1,8 @@
-"""Device preprocessing of the cloth builder (edges, rest lengths, inverse
-masses) against the numpy restatement: the same arrays bit for bit on a
-jittered grid, a fan with a high-degree vertex, a triangle soup with
-repeated and degenerate triangles and unused vertices, and a whole cloth
-built either way."""
+"""Device preprocessing of the cloth builder (edges, bend pairs, rest
+lengths, inverse masses) against the numpy restatement: the same arrays bit
+for bit on a jittered grid, a fan with a high-degree vertex, a triangle soup
+with repeated and degenerate triangles and unused vertices, and a whole
+cloth built either way."""
 import numpy as np
 import pytest
 
@@ -49,10 +49,14 @@ def test_device_inputs_equal_numpy(case, density, gpu_lib):
     hard[::41] = True
     e_ref, r_ref = scene.edge_constraints(tris, pos)
     inv_ref = scene.vertex_inverse_mass(pos, tris, density, hard).astype(np.float32)
-    e, r, inv = scene.cloth_inputs_device(pos, tris, density, hard)
+    b_ref, br_ref = scene.bend_constraints(tris, pos)
+    e, r, inv, b, br = scene.cloth_inputs_device(pos, tris, density, hard)
     assert _same_bits(e, e_ref.astype(np.int32))
     assert _same_bits(r, r_ref.astype(np.float32))
     assert _same_bits(inv, inv_ref)
+    assert len(b_ref) > 0
+    assert _same_bits(b, b_ref.astype(np.int32))
+    assert _same_bits(br, br_ref.astype(np.float32))
 
 
 def test_device_built_cloth_equals_numpy_built(gpu_lib):
