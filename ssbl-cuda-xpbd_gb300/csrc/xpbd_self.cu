@@ -1375,6 +1375,8 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
 // current distance), without the cluster filter.  Returns 0 (no pair),
 // 1 (rejected by the rest pose), 2 (beyond the onset distance) or 3 (a
 // candidate: *key is its cluster key, *out its push).
+// kPush = false stops at the class and key (the push is left unset).
+template <bool kPush = true>
 __device__ int ee_fast_classify(const View& v, int ia, int ib, float target, float onset, SoftPush* out, unsigned* key) {
     if (ib <= ia || ia < 0 || ib < 0 || ia >= v.nE || ib >= v.nE || target <= 0.0f || onset <= target) return 0;
     const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
@@ -1410,6 +1412,7 @@ __device__ int ee_fast_classify(const View& v, int ia, int ib, float target, flo
         dist = 0.0f;
     }
     *key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+    if (!kPush) return 3;
     const float pen = target - dist;
     float push;
     if (pen > 0.0f) {
@@ -1508,7 +1511,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
             SoftPush sp;
             sp.apply = false;
             unsigned key = 0u;
-            const int cls = dup ? 4 : ee_fast_classify(v, o_item, id, o_target, o_onset, &sp, &key);
+            const int cls = dup ? 4 : ee_fast_classify<false>(v, o_item, id, o_target, o_onset, &sp, &key);
             cls_w[j * kBucketSlots + slot] = (unsigned char)cls;
             key_w[j * kBucketSlots + slot] = key;
         }
