@@ -228,6 +228,22 @@ def cpu_oracle_rate(scs: list, budget_s: float) -> tuple[float, int, str]:
     return work / elapsed, threads, what
 
 
+def max_over_ranks(value: float, world: int) -> float:
+    """The largest of every rank's value (the slowest replica's time), then a
+    barrier; the value itself with one rank.  Works on the NCCL process group
+    of the GPU runs (CUDA tensor) and on gloo (host tensor)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
 def run_reference(args, scs, world, rank):
     """Reference arm: the CPU restatement on a bounded sample per step."""
     if rank != 0:
@@ -573,12 +589,7 @@ def main():
             solver.step(S, I, diagnostics=False, synchronize=False)
             events[k][1].record(stream)
         torch.cuda.synchronize()
-    total_ms = sum(a.elapsed_time(b) for a, b in events)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-        torch.distributed.barrier()
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in events), world)
     launches_per_step = solver.last_step_launches()
     value = V * S * args.steps * world / (total_ms / 1000.0)
 
