@@ -85,7 +85,7 @@ __attribute__((visibility("default"))) void* xpbd_gb300_pc2_open(void* handle, i
 __attribute__((visibility("default"))) int xpbd_gb300_pc2_write(void* handle, void* writer, const float* matrix_world_inv16);
 __attribute__((visibility("default"))) long long xpbd_gb300_pc2_close(void* writer, int commit);
 
-/* Launch configuration (no counterpart in the reference): 11 slots, in order
+/* Launch configuration (no counterpart in the reference): 12 slots, in order
  * block size of the per-vertex passes (default 128), of the hash count /
  * scatter kernels (256), lanes per primitive of the edge hash (1, 2, 4, 8
  * or 16; default 8), block size of the warp-per-item kernels (256), of
@@ -97,8 +97,9 @@ __attribute__((visibility("default"))) long long xpbd_gb300_pc2_close(void* writ
  * collision, hard stretch or dynamic colliders) run each frame as one fused
  * launch, a block per cloth (1, default) or an 8-CTA thread-block cluster per
  * cloth exchanging through distributed shared memory (8), or as launched
- * kernels (2), and lanes per primitive of the triangle hash (1, 2, 4, 8 or
- * 16; default 8).  Block sizes
+ * kernels (2), lanes per primitive of the triangle hash (1, 2, 4, 8 or 16;
+ * default 8), and lanes per vertex of the neighbour table and strict VV
+ * responses (1, 2, 4, 8, 16 or 32; default 2).  Block sizes
  * are multiples of 32 up to 256; 0 selects the default.  No value changes a
  * result.  Setting drops the captured frame graphs. */
 __attribute__((visibility("default"))) int xpbd_gb300_set_launch_config(void* handle, const int* values, int count);

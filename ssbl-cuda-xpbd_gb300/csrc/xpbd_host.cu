@@ -2118,6 +2118,7 @@ bool tune_value_ok(int slot, int v) {
     if (v == 0) return true;
     if (slot == kTuneGroupLanes) return v == 4 || v == 8 || v == 16;
     if (slot == kTunePrimLanes || slot == kTuneTriLanes) return v == 1 || v == 2 || v == 4 || v == 8 || v == 16;
+    if (slot == kTuneNeighborLanes) return v == 1 || v == 2 || v == 4 || v == 8 || v == 16 || v == 32;
     if (slot == kTuneFastEeForm) return v == 8 || v == 32;
     if (slot == kTuneFusedFrame) return v == 1 || v == 2 || v == 8;
     return v >= 32 && v <= kMaxBlock && v % 32 == 0;
@@ -2194,6 +2195,7 @@ bool autotune(Solver* S, int substeps, int iterations, int rounds, float* ms_out
         {8, 32},          // fast EE: groups of 8 lanes or flattened warps
         {1, 2, 8},        // small cloths: fused frame (block or cluster per cloth) or launched kernels
         {1, 2, 4, 16},    // lanes per triangle of the triangle hash
+        {1, 2, 4, 8},     // lanes per vertex of the neighbour table
     };
     const LaunchTune start = S->tune;
     LaunchTune best = start;

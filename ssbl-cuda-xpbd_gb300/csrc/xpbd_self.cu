@@ -861,15 +861,6 @@ __global__ void __launch_bounds__(kThreads) k_ee_brute(View v) {
 // does.  Fixed-point sums make the accumulation order irrelevant.
 
 
-__device__ __forceinline__ int warp_exclusive_sum(int v, int lane) {
-    int incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    return incl - v;
-}
-
 __device__ __forceinline__ long long warp_sum64(long long v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
@@ -878,80 +869,92 @@ __device__ __forceinline__ long long warp_sum64(long long v) {
 // VV responses (strict): lane n handles neighbour n of the source vertex.
 // The responses of one strict vertex against its neighbour table (lane n:
 // neighbour n); shared by k_vv_warp and the fused neighbour kernel.
+// Response of strict vertex src to neighbour `other` (abi41.cu:4816-4951):
+// *candidate = 1 for a valid neighbour, returns 1 with the fixed-point push in
+// ax / ay / az when it makes a contact.
+__device__ __forceinline__ int vv_pair(const View& v, const Params& P, int src, int other, long long* pax, long long* pay,
+                                       long long* paz, int* pcandidate) {
+    long long ax = 0, ay = 0, az = 0;
+    int candidate = 0, contact = 0;
+    if (other >= 0 && other < v.nV && other != src) {
+        candidate = 1;
+        const F3 pc = f3(v.pos[src]), pp = f3(v.prev[src]);
+        const float target = contact_radius(P);
+        const float th = target * 0.5f + target * 0.5f;
+        const F3 qc = f3(v.pos[other]), qp = f3(v.prev[other]);
+        if (th > 0.0f) {
+            const float scale = !(__ldg(&v.inv_mass[other]) > 0.0f) ? 1.0f : 0.5f;
+            F3 resp{0.0f, 0.0f, 0.0f};
+            bool hit = false;
+            const F3 d_ref = pp - qp;
+            const float cc = dot3(d_ref, d_ref) - th * th;
+            const F3 rel = (pc - pp) - (qc - qp);
+            const float a = dot3(rel, rel), b = dot3(d_ref, rel);
+            if (cc >= 0.0f && b < 0.0f && a > 1.0e-5f) {
+                const float disc = b * b - a * cc;
+                if (disc >= 0.0f) {
+                    const float t = (-b - sqrtf(disc)) / a;
+                    if (t > 0.0f && t <= 1.0f) {
+                        const float sg = 1.0f - t;
+                        const F3 ph = pp * sg + pc * t, qh = qp * sg + qc * t;
+                        F3 nrm = ph - qh;
+                        const float nl = dot3(nrm, nrm);
+                        if (nl > kEps) {
+                            nrm = nrm * (1.0f / sqrtf(nl));
+                            const float vn = dot3((pc - ph) - (qc - qh), nrm);
+                            if (vn > 0.0f) {
+                                resp = nrm * (-vn * scale);
+                                hit = true;
+                            }
+                        }
+                    }
+                }
+            }
+            bool skip = false;
+            if (!hit) {
+                const F3 delta = pc - qc;
+                const float dsq = dot3(delta, delta);
+                if (dsq >= th * th) {
+                    skip = true;
+                } else {
+                    F3 nrm{0.0f, 0.0f, 1.0f};
+                    float dist = sqrtf(fmaxf(dsq, kEps));
+                    if (dsq > kEps) {
+                        nrm = delta * (1.0f / dist);
+                    } else {
+                        const F3 rd = f3(ld4(&v.rest[src])) - f3(ld4(&v.rest[other]));
+                        const float rl = dot3(rd, rd);
+                        if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
+                        dist = 0.0f;
+                    }
+                    resp = nrm * fminf((th - dist) * scale, th * 0.35f);
+                    hit = true;
+                }
+            }
+            if (!skip && hit && dot3(resp, resp) > kEps) {
+                const float max_len = fmaxf(th * 0.35f, 1.0e-4f);
+                const float rl = len3(resp);
+                if (rl > max_len) resp = resp * (max_len / rl);
+                ax = to_fix(resp.x);
+                ay = to_fix(resp.y);
+                az = to_fix(resp.z);
+                contact = 1;
+            }
+        }
+    }
+    *pax = ax;
+    *pay = ay;
+    *paz = az;
+    *pcandidate = candidate;
+    return contact;
+}
+
 __device__ __forceinline__ void vv_strict_warp(const View& v, const Params& P, int src, int lane) {
     const int count = min(v.nb_count[src], kNeighborSlots);
     if (count == 0) return;
     long long ax = 0, ay = 0, az = 0;
     int candidate = 0, contact = 0;
-    if (lane < count) {
-        const int other = v.nb_idx[src * kNeighborSlots + lane];
-        if (other >= 0 && other < v.nV && other != src) {
-            candidate = 1;
-            const F3 pc = f3(v.pos[src]), pp = f3(v.prev[src]);
-            const float target = contact_radius(P);
-            const float th = target * 0.5f + target * 0.5f;
-            const F3 qc = f3(v.pos[other]), qp = f3(v.prev[other]);
-            if (th > 0.0f) {
-                const float scale = !(__ldg(&v.inv_mass[other]) > 0.0f) ? 1.0f : 0.5f;
-                F3 resp{0.0f, 0.0f, 0.0f};
-                bool hit = false;
-                const F3 d_ref = pp - qp;
-                const float cc = dot3(d_ref, d_ref) - th * th;
-                const F3 rel = (pc - pp) - (qc - qp);
-                const float a = dot3(rel, rel), b = dot3(d_ref, rel);
-                if (cc >= 0.0f && b < 0.0f && a > 1.0e-5f) {
-                    const float disc = b * b - a * cc;
-                    if (disc >= 0.0f) {
-                        const float t = (-b - sqrtf(disc)) / a;
-                        if (t > 0.0f && t <= 1.0f) {
-                            const float sg = 1.0f - t;
-                            const F3 ph = pp * sg + pc * t, qh = qp * sg + qc * t;
-                            F3 nrm = ph - qh;
-                            const float nl = dot3(nrm, nrm);
-                            if (nl > kEps) {
-                                nrm = nrm * (1.0f / sqrtf(nl));
-                                const float vn = dot3((pc - ph) - (qc - qh), nrm);
-                                if (vn > 0.0f) {
-                                    resp = nrm * (-vn * scale);
-                                    hit = true;
-                                }
-                            }
-                        }
-                    }
-                }
-                bool skip = false;
-                if (!hit) {
-                    const F3 delta = pc - qc;
-                    const float dsq = dot3(delta, delta);
-                    if (dsq >= th * th) {
-                        skip = true;
-                    } else {
-                        F3 nrm{0.0f, 0.0f, 1.0f};
-                        float dist = sqrtf(fmaxf(dsq, kEps));
-                        if (dsq > kEps) {
-                            nrm = delta * (1.0f / dist);
-                        } else {
-                            const F3 rd = f3(ld4(&v.rest[src])) - f3(ld4(&v.rest[other]));
-                            const float rl = dot3(rd, rd);
-                            if (rl > kEps) nrm = rd * (1.0f / sqrtf(rl));
-                            dist = 0.0f;
-                        }
-                        resp = nrm * fminf((th - dist) * scale, th * 0.35f);
-                        hit = true;
-                    }
-                }
-                if (!skip && hit && dot3(resp, resp) > kEps) {
-                    const float max_len = fmaxf(th * 0.35f, 1.0e-4f);
-                    const float rl = len3(resp);
-                    if (rl > max_len) resp = resp * (max_len / rl);
-                    ax = to_fix(resp.x);
-                    ay = to_fix(resp.y);
-                    az = to_fix(resp.z);
-                    contact = 1;
-                }
-            }
-        }
-    }
+    if (lane < count) contact = vv_pair(v, P, src, v.nb_idx[src * kNeighborSlots + lane], &ax, &ay, &az, &candidate);
     const unsigned cand_mask = __ballot_sync(0xffffffffu, candidate);
     const unsigned hit_mask = __ballot_sync(0xffffffffu, contact);
     ax = warp_sum64(ax);
@@ -972,7 +975,7 @@ __device__ __forceinline__ void vv_strict_warp(const View& v, const Params& P, i
 
 
 // VV responses of strict cloths whose table k_neighbors_brute built (the
-// hashed ones run fused into k_neighbors_warp); `all` = 1 covers every
+// hashed ones run fused into k_neighbors_group); `all` = 1 covers every
 // strict cloth.
 __global__ void __launch_bounds__(kThreads, 8) k_vv_warp(View v, int all) {
     const int src = v.lo + warp_global_id();
@@ -984,50 +987,110 @@ __global__ void __launch_bounds__(kThreads, 8) k_vv_warp(View v, int all) {
     vv_strict_warp(v, P, src, lane);
 }
 
-// VV neighbour table: lane l < 27 scans cell (dz, dy, dx) = (l/9-1, l/3%3-1,
-// l%3-1), the reference's nested-loop order (abi41.cu:4756-4781).  With kVv
-// (strict passes) the warp then computes the vertex's VV responses from the
-// table it just wrote (the next operation on that branch; positions do not
-// change in between), saving the separate launch and its table reads.
-template <bool kVv>
-__global__ void __launch_bounds__(kThreads, 8) k_neighbors_warp(View v, int mode) {
-    const int src = v.lo + warp_global_id();
-    const int lane = threadIdx.x & 31;
-    if (src >= v.hi) return;
-    const Params& P = params_v(v, src);
-    if (!P.vhash || !self_scheduled(P, v) || (mode == 1 && !fast_mode(P)) || (mode == 2 && fast_mode(P))) return;
-    const float target = contact_radius(P);
-    if (target <= 0.0f) {
-        if (lane == 0) v.nb_count[src] = 0;
-        return;
+
+// VV neighbour table (abi41.cu:4756-4781) and, with kVv (strict passes), the
+// VV responses computed from it at once (the next operation on that branch;
+// positions do not change in between).  G lanes per vertex (a tile choice of
+// the autotuner; 32 / G vertices per warp): lane l scans cells c = l, G + l,
+// ... in rounds, cell c = (dz, dy, dx) = (c/9-1, c/3%3-1, c%3-1), the
+// reference's nested-loop order; each round's hits are placed after the
+// earlier cells' by a prefix sum over the vertex's lanes, so the table lists
+// neighbours in walk order.  The VV responses take neighbours l, G + l, ...
+// and sum their fixed-point pushes.  With few lanes per vertex the
+// per-vertex set-up and response arithmetic of several vertices share one
+// instruction stream (the table walk is issue-bound).
+template <bool kVv, int G>
+__global__ void __launch_bounds__(kThreads, 8) k_neighbors_group(View v, int mode) {
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+    const int src = v.lo + warp_global_id() * (32 / G) + lane / G;
+    bool run = src < v.hi;
+    const Params* P = nullptr;
+    if (run) {
+        P = &params_v(v, src);
+        run = P->vhash && self_scheduled(*P, v) && !(mode == 1 && !fast_mode(*P)) && !(mode == 2 && fast_mode(*P));
     }
-    const float onset = fmaxf(target * 1.8f, target + kEps);
-    const float4 p = v.pos[src];
-    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
-    int found[kNeighborSlots];
-    int nfound = 0;
-    if (lane < 27) {
-        const int qx = cx + lane % 3 - 1, qy = cy + (lane / 3) % 3 - 1, qz = cz + lane / 9 - 1;
-        const int b = P.vbase + (int)bucket_of(qx, qy, qz, P.vbuckets);
-        const int st = v.vb_start[b];
-        const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
-        for (int k = 0; k < lim; ++k) {
-            const int other = v.vb_ent[st + k];
-            const int4 oc = v.vcell[other];
-            if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
-            found[nfound++] = other;
+    float target = 0.0f;
+    if (run) {
+        target = contact_radius(*P);
+        if (target <= 0.0f) {
+            if (gl == 0) v.nb_count[src] = 0;
+            run = false;
         }
     }
-    const int offset = warp_exclusive_sum(nfound, lane);
-    const int total = __shfl_sync(0xffffffffu, offset + nfound, 31);
-    for (int k = 0; k < nfound && offset + k < kNeighborSlots; ++k) v.nb_idx[src * kNeighborSlots + offset + k] = found[k];
-    if (lane == 0) {
+    const float onset = fmaxf(target * 1.8f, target + kEps);
+    int cx = 0, cy = 0, cz = 0;
+    if (run) {
+        const float4 p = v.pos[src];
+        cx = cell_of(p.x, P->vcell);
+        cy = cell_of(p.y, P->vcell);
+        cz = cell_of(p.z, P->vcell);
+    }
+    int total = 0;  // neighbours of the earlier rounds (the same in the vertex's lanes)
+    for (int c0 = 0; c0 < 27; c0 += G) {
+        const int c = c0 + gl;
+        int found[kNeighborSlots];
+        int nfound = 0;
+        if (run && c < 27) {
+            const int qx = cx + c % 3 - 1, qy = cy + (c / 3) % 3 - 1, qz = cz + c / 9 - 1;
+            const int b = P->vbase + (int)bucket_of(qx, qy, qz, P->vbuckets);
+            const int st = v.vb_start[b];
+            const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
+            for (int k = 0; k < lim; ++k) {
+                const int other = v.vb_ent[st + k];
+                const int4 oc = v.vcell[other];
+                if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
+                found[nfound++] = other;
+            }
+        }
+        int incl = nfound;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o, G);
+            if (gl >= o) incl += t;
+        }
+        const int offset = total + incl - nfound;
+        for (int k = 0; k < nfound && offset + k < kNeighborSlots; ++k) v.nb_idx[src * kNeighborSlots + offset + k] = found[k];
+        total += __shfl_sync(0xffffffffu, incl, G - 1, G);
+    }
+    if (run && gl == 0) {
         if (total >= kNeighborSlots) count1(v.counts, kCntSelfOverflow);
         v.nb_count[src] = min(total, kNeighborSlots);
     }
-    if (kVv) {
-        __syncwarp();  // the table's writes are visible to the whole warp
-        if (__ldg(&v.inv_mass[src]) > 0.0f) vv_strict_warp(v, P, src, lane);
+    if (!kVv) return;
+    __syncwarp();  // the table's writes are visible to the whole warp
+    const bool vv = run && __ldg(&v.inv_mass[src]) > 0.0f;
+    const int count = vv ? min(total, kNeighborSlots) : 0;
+    long long ax = 0, ay = 0, az = 0;
+    int candidates = 0, contacts = 0;
+    for (int n = gl; n < count; n += G) {
+        long long px, py, pz;
+        int cand = 0;
+        if (vv_pair(v, *P, src, v.nb_idx[src * kNeighborSlots + n], &px, &py, &pz, &cand)) {
+            ax += px;
+            ay += py;
+            az += pz;
+            ++contacts;
+        }
+        candidates += cand;
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        ax += __shfl_down_sync(0xffffffffu, ax, o, G);
+        ay += __shfl_down_sync(0xffffffffu, ay, o, G);
+        az += __shfl_down_sync(0xffffffffu, az, o, G);
+        candidates += __shfl_down_sync(0xffffffffu, candidates, o, G);
+        contacts += __shfl_down_sync(0xffffffffu, contacts, o, G);
+    }
+    if (vv && gl == 0) {
+        if (candidates) count_add(v.counts, kCntSelfCandidates, (unsigned long long)candidates);
+        if (contacts) {
+            count_add(v.counts, kCntExactImpulseContacts, (unsigned long long)contacts);
+            unsigned long long* acc = reinterpret_cast<unsigned long long*>(&v.acc[src]);
+            atomicAdd(acc + 0, (unsigned long long)ax);
+            atomicAdd(acc + 1, (unsigned long long)ay);
+            atomicAdd(acc + 2, (unsigned long long)az);
+            atomicAdd(acc + 3, (unsigned long long)contacts);
+        }
     }
 }
 
@@ -1969,6 +2032,14 @@ void prim_pass_lanes(const View& iv, long long items, int lanes, int b, bool sca
     }
 }
 
+template <int G>
+void neighbors_group(const View& v, const ItemRange& r, bool vv, int mode, int b, cudaStream_t s) {
+    if (vv)
+        k_neighbors_group<true, G><<<grid(r.size(), G, b), b, 0, s>>>(ranged(v, r), mode);
+    else
+        k_neighbors_group<false, G><<<grid(r.size(), G, b), b, 0, s>>>(ranged(v, r), mode);
+}
+
 void bucket_order(const View& v, const ItemRange& buckets, const int* start, int* ent, int nb, int kind, int mode,
                   cudaStream_t s) {
     if (buckets.size() == 0) return;
@@ -2048,10 +2119,17 @@ void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_
     const ItemRange& r = mode == 1 ? sv.v_fast : (mode == 2 ? sv.v_strict : sv.v_all);
     if (r.size() == 0) return;
     const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
-    if (sv.hashed_v && mode == 2)
-        k_neighbors_warp<true><<<grid(r.size(), 32, wb), wb, 0, s>>>(ranged(v, r), mode);
-    else if (sv.hashed_v)
-        k_neighbors_warp<false><<<grid(r.size(), 32, wb), wb, 0, s>>>(ranged(v, r), mode);
+    if (sv.hashed_v) {
+        const bool vv = mode == 2;  // strict passes: VV responses fused
+        switch (tune_of(v.tune, kTuneNeighborLanes)) {
+            case 1: neighbors_group<1>(v, r, vv, mode, wb, s); break;
+            case 4: neighbors_group<4>(v, r, vv, mode, wb, s); break;
+            case 8: neighbors_group<8>(v, r, vv, mode, wb, s); break;
+            case 16: neighbors_group<16>(v, r, vv, mode, wb, s); break;
+            case 32: neighbors_group<32>(v, r, vv, mode, wb, s); break;
+            default: neighbors_group<2>(v, r, vv, mode, wb, s); break;
+        }
+    }
     if (sv.brute_v) k_neighbors_brute<<<grid(r.size(), 1, qb), qb, 0, s>>>(ranged(v, r), mode);
 }
 void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s) {

@@ -229,12 +229,13 @@ enum TuneSlot {
     kTuneFusedFrame,       // small cloths: 1 = whole frame in one block per cloth, 8 = in an 8-CTA cluster per cloth,
                            // 2 = launched kernels (1)
     kTuneTriLanes,         // lanes per primitive of the triangle hash: 1, 2, 4, 8, 16 (8)
+    kTuneNeighborLanes,    // lanes per vertex of the neighbour table (+ strict VV): 1, 2, 4, 8, 16, 32 (2)
     kTuneSlots
 };
 struct LaunchTune {
     short v[kTuneSlots];
 };
-constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 0, 8};
+constexpr short kTuneDefault[kTuneSlots] = {128, 256, 8, 256, 256, 8, 256, 128, 32, 0, 8, 2};
 constexpr int kMaxBlock = 256;  // the kernels' launch bounds
 inline int tune_of(const LaunchTune& t, int slot) { return t.v[slot] > 0 ? t.v[slot] : kTuneDefault[slot]; }
 inline int grid_for(long long threads, int block) { return (int)((threads + block - 1) / block); }

@@ -630,7 +630,7 @@ class NativeXpbdSolver:
         return int(self._lib.xpbd_gb300_device_bytes(self._handle))
 
     LAUNCH_SLOTS = ("vertex_block", "hash_block", "prim_lanes", "warp_block", "query_block", "group_lanes",
-                    "group_block", "dynamic_block", "fast_ee_form", "fused_frame", "tri_lanes")
+                    "group_block", "dynamic_block", "fast_ee_form", "fused_frame", "tri_lanes", "neighbor_lanes")
 
     def launch_config(self) -> dict:
         """Effective launch configuration (block sizes and tiles) by slot."""

@@ -7,12 +7,12 @@ from xpbd_gb300 import autotune
 
 class FakeSolver:
     LAUNCH_SLOTS = ("vertex_block", "hash_block", "prim_lanes", "warp_block", "query_block", "group_lanes",
-                    "group_block", "dynamic_block", "fast_ee_form", "fused_frame", "tri_lanes")
+                    "group_block", "dynamic_block", "fast_ee_form", "fused_frame", "tri_lanes", "neighbor_lanes")
 
     def __init__(self, vertices=1000):
         self.info = {"cloths": 2, "vertices": vertices, "edges": 2900, "triangles": 1900, "fast": 1, "strict": 1,
                      "dynamic": 0, "sdf": 0}
-        self.config = dict(zip(self.LAUNCH_SLOTS, (128, 256, 8, 256, 256, 8, 256, 128, 32, 1, 8)))
+        self.config = dict(zip(self.LAUNCH_SLOTS, (128, 256, 8, 256, 256, 8, 256, 128, 32, 1, 8, 2)))
         self.native_calls = 0
 
     def solver_info(self):

@@ -12,9 +12,9 @@ pytestmark = pytest.mark.gpu
 
 CONFIGS = [
     {"vertex_block": 64, "hash_block": 128, "prim_lanes": 4, "warp_block": 128, "query_block": 64, "group_lanes": 4,
-     "group_block": 128, "dynamic_block": 64, "fast_ee_form": 8, "tri_lanes": 1},
+     "group_block": 128, "dynamic_block": 64, "fast_ee_form": 8, "tri_lanes": 1, "neighbor_lanes": 1},
     {"vertex_block": 256, "hash_block": 256, "prim_lanes": 16, "warp_block": 256, "query_block": 256, "group_lanes": 16,
-     "group_block": 256, "dynamic_block": 256, "fast_ee_form": 32, "tri_lanes": 16},
+     "group_block": 256, "dynamic_block": 256, "fast_ee_form": 32, "tri_lanes": 16, "neighbor_lanes": 32},
     {"vertex_block": 96, "query_block": 160, "warp_block": 32},
 ]
 
