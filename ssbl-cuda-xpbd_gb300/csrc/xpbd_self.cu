@@ -1850,100 +1850,132 @@ __device__ int island_eval(const View& v, int vertex, F3 p, F3 pp, float target,
     return 2;
 }
 
-// One warp per vertex.  Lane c < 27 reads the range of cell (dz, dy, dx) =
-// (c/9-1, c/3%3-1, c%3-1), the serial walk's order; the slots of the 27
-// buckets are laid end to end (warp prefix sum) and evaluated 32 at a time,
-// one slot per lane; then the warp replays the slots in walk order with the
-// walk's rules -- stop at max_contacts contacts or scan_limit slots, skip a
-// triangle already accepted, count guards of visited slots only -- and sums
-// the accepted contacts in that order (every lane holds the same sums; the
-// accepted ids are spread over the lanes for the duplicate test).
+// G lanes per vertex (32 / G vertices per warp).  The 27 cells (dz, dy, dx)
+// = (c/9-1, c/3%3-1, c%3-1), the serial walk's order, are read in rounds of
+// G (lane l: cell c0 + l); a round's slots are laid end to end (prefix sum
+// over the vertex's lanes) and evaluated G at a time, one slot per lane; then
+// the vertex's lanes replay those slots in walk order with the walk's rules
+// -- stop at max_contacts contacts or scan_limit slots, skip a triangle
+// already accepted, count guards of visited slots only -- and sum the
+// accepted contacts in that order (every lane of the vertex holds the same
+// sums; the accepted ids are spread over its lanes for the duplicate test).
+// Loop bounds are the warp's maximum so the shuffles stay converged.
+constexpr int kIslandLanes = 4;  // lanes per vertex of the island walk
+
+template <int G>
 __global__ void __launch_bounds__(kThreads, 4) k_island(View v) {
-    const int vertex = v.lo + warp_global_id();
-    const int lane = threadIdx.x & 31;
-    if (vertex >= v.hi) return;
-    const Params& P = params_v(v, vertex);
-    if (!fast_mode(P) || !P.thash || P.T <= 0 || !self_scheduled(P, v) || v.pass != P.self_passes - 1) return;
-    if (!(__ldg(&v.inv_mass[vertex]) > 0.0f)) return;
-    const float target = contact_radius(P);
-    if (target <= 0.0f) return;
+    constexpr int kHeld = (48 + G - 1) / G;  // accepted ids per lane (at most 48 per vertex)
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~(G - 1));
+    const int vertex = v.lo + warp_global_id() * (32 / G) + lane / G;
+    bool run = vertex < v.hi;
+    const Params* P = nullptr;
+    if (run) {
+        P = &params_v(v, vertex);
+        run = fast_mode(*P) && P->thash && P->T > 0 && self_scheduled(*P, v) && v.pass == P->self_passes - 1 &&
+              __ldg(&v.inv_mass[vertex]) > 0.0f;
+    }
+    float target = 0.0f;
+    if (run) {
+        target = contact_radius(*P);
+        run = target > 0.0f;
+    }
     const float onset = fmaxf(target * 1.8f, target + kEps);
-    const F3 p = f3(v.pos[vertex]), pp = f3(v.prev[vertex]);
-    if (!finite3(p) || !finite3(pp)) {
-        if (lane == 0) count1(v.counts, kCntIslandGuarded);
-        return;
+    F3 p{0.0f, 0.0f, 0.0f}, pp{0.0f, 0.0f, 0.0f};
+    int guards = 0;
+    if (run) {
+        p = f3(v.pos[vertex]);
+        pp = f3(v.prev[vertex]);
+        if (!finite3(p) || !finite3(pp)) {
+            guards = 1;
+            run = false;
+        }
     }
-    int maxn = P.max_neighbors < 1 ? 1 : P.max_neighbors;
-    int max_contacts = maxn * 2;
-    if (max_contacts > 48) max_contacts = 48;
-    if (max_contacts < 3) max_contacts = 3;
-    const int scan_limit = max_contacts * 10;
-    const int cx = cell_of(p.x, P.tcell), cy = cell_of(p.y, P.tcell), cz = cell_of(p.z, P.tcell);
-    int st = 0, lim = 0;
-    if (lane < 27) {
-        const int b = P.tbase + (int)bucket_of(cx + lane % 3 - 1, cy + (lane / 3) % 3 - 1, cz + lane / 9 - 1, P.tbuckets);
-        st = v.tb_start[b];
-        lim = min(v.tb_start[b + 1] - st, kBucketSlots);
+    int max_contacts = 3, scan_limit = 30, cx = 0, cy = 0, cz = 0;
+    if (run) {
+        const int maxn = P->max_neighbors < 1 ? 1 : P->max_neighbors;
+        max_contacts = min(max(maxn * 2, 3), 48);
+        scan_limit = max_contacts * 10;
+        cx = cell_of(p.x, P->tcell);
+        cy = cell_of(p.y, P->tcell);
+        cz = cell_of(p.z, P->tcell);
     }
-    int incl = lim;
+    int contacts = 0, scanned = 0;
+    int held[kHeld];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int n = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += n;
-    }
-    const int visit = min(__shfl_sync(0xffffffffu, incl, 31), scan_limit);
-    const int excl = incl - lim;
-    int contacts = 0, scanned = 0, guards = 0;
-    int acc_lo = -1, acc_hi = -1;  // accepted ids: lane q holds number q and q + 32
+    for (int q = 0; q < kHeld; ++q) held[q] = -1;
     float pen_sum = 0.0f, wsum = 0.0f, max_pen = 0.0f;
     F3 axis{0.0f, 0.0f, 0.0f}, best{0.0f, 0.0f, 1.0f};
-    bool stop = false;
-    for (int base = 0; base < visit && !stop; base += 32) {
-        const int g = base + lane;
-        int j = 0;  // owner cell: the first lane whose inclusive slot count exceeds g
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= g) j += step;
-        const int o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
-        int tri = -1, code = 0;
-        IslandHit h{0.0f, 0.0f, F3{0.0f, 0.0f, 0.0f}};
-        if (g < visit) {
-            tri = v.tb_ent[o_first + g];
-            code = island_eval(v, vertex, p, pp, target, onset, tri, &h);
+    bool stop = !run;
+    for (int c0 = 0; c0 < 27; c0 += G) {
+        const int c = c0 + gl;
+        int st = 0, lim = 0;
+        if (!stop && c < 27) {
+            const int b = P->tbase + (int)bucket_of(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1, P->tbuckets);
+            st = v.tb_start[b];
+            lim = min(v.tb_start[b + 1] - st, kBucketSlots);
         }
-        const int n = min(32, visit - base);
-        for (int k = 0; k < n; ++k) {
-            if (contacts >= max_contacts || scanned >= scan_limit) {
-                stop = true;
-                break;
+        int incl = lim;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o, G);
+            if (gl >= o) incl += t;
+        }
+        const int round_total = __shfl_sync(0xffffffffu, incl, G - 1, G);
+        const int excl = incl - lim;
+        const int warp_total = __reduce_max_sync(0xffffffffu, stop ? 0 : round_total);
+        for (int base = 0; base < warp_total; base += G) {
+            const int g = base + gl;
+            int j = 0;  // owner lane: the first of the vertex's lanes whose inclusive count exceeds g
+#pragma unroll
+            for (int step = G / 2; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, incl, j + step - 1, G) <= g) j += step;
+            const int o_first = __shfl_sync(0xffffffffu, st, j, G) - __shfl_sync(0xffffffffu, excl, j, G);
+            int tri = -1, code = 0;
+            IslandHit h{0.0f, 0.0f, F3{0.0f, 0.0f, 0.0f}};
+            if (!stop && g < round_total) {
+                tri = v.tb_ent[o_first + g];
+                code = island_eval(v, vertex, p, pp, target, onset, tri, &h);
             }
-            ++scanned;
-            const int t_k = __shfl_sync(0xffffffffu, tri, k);
-            const int c_k = __shfl_sync(0xffffffffu, code, k);
-            const float pen_k = __shfl_sync(0xffffffffu, h.pen, k), w_k = __shfl_sync(0xffffffffu, h.wterm, k);
-            const F3 n_k{__shfl_sync(0xffffffffu, h.nrm.x, k), __shfl_sync(0xffffffffu, h.nrm.y, k),
-                         __shfl_sync(0xffffffffu, h.nrm.z, k)};
-            if (__any_sync(0xffffffffu, (lane < contacts && acc_lo == t_k) || (lane + 32 < contacts && acc_hi == t_k)))
-                continue;
-            if (c_k == 1) ++guards;
-            if (c_k != 2) continue;
-            if (lane == (contacts & 31)) {
-                if (contacts < 32)
-                    acc_lo = t_k;
-                else
-                    acc_hi = t_k;
-            }
-            ++contacts;
-            pen_sum += pen_k;
-            wsum += w_k;
-            axis = axis + n_k * pen_k;
-            if (pen_k > max_pen) {
-                max_pen = pen_k;
-                best = n_k;
+            const int n = stop ? 0 : min(G, round_total - base);
+            const int warp_n = __reduce_max_sync(0xffffffffu, max(n, 0));
+            for (int k = 0; k < warp_n; ++k) {
+                bool live = k < n && !stop;
+                if (live && (contacts >= max_contacts || scanned >= scan_limit)) {
+                    stop = true;
+                    live = false;
+                }
+                const int t_k = __shfl_sync(0xffffffffu, tri, k, G);
+                const int c_k = __shfl_sync(0xffffffffu, code, k, G);
+                const float pen_k = __shfl_sync(0xffffffffu, h.pen, k, G), w_k = __shfl_sync(0xffffffffu, h.wterm, k, G);
+                const F3 n_k{__shfl_sync(0xffffffffu, h.nrm.x, k, G), __shfl_sync(0xffffffffu, h.nrm.y, k, G),
+                             __shfl_sync(0xffffffffu, h.nrm.z, k, G)};
+                bool mine = false;
+#pragma unroll
+                for (int q = 0; q < kHeld; ++q) mine = mine || (q * G + gl < contacts && held[q] == t_k);
+                const bool dup = (__ballot_sync(0xffffffffu, live && mine) & gmask) != 0u;
+                if (!live) continue;
+                ++scanned;
+                if (dup) continue;
+                if (c_k == 1) ++guards;
+                if (c_k != 2) continue;
+                if (gl == contacts % G) {
+#pragma unroll
+                    for (int q = 0; q < kHeld; ++q)
+                        if (q == contacts / G) held[q] = t_k;
+                }
+                ++contacts;
+                pen_sum += pen_k;
+                wsum += w_k;
+                axis = axis + n_k * pen_k;
+                if (pen_k > max_pen) {
+                    max_pen = pen_k;
+                    best = n_k;
+                }
             }
         }
     }
-    if (lane != 0) return;
+    if (gl != 0) return;
     if (guards > 0) count_add(v.counts, kCntIslandGuarded, (unsigned long long)guards);
     if (contacts <= 0) return;
     count_add(v.counts, kCntIslandCandidates, (unsigned long long)contacts);
@@ -2166,7 +2198,8 @@ void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
 }
 void self_island(const View& v, const SelfVariants& sv, cudaStream_t s) {
     const int wb = tune_of(v.tune, kTuneWarpBlock);
-    if (sv.v_fast.size() > 0) k_island<<<grid(sv.v_fast.size(), 32, wb), wb, 0, s>>>(ranged(v, sv.v_fast));
+    constexpr int G = kIslandLanes;
+    if (sv.v_fast.size() > 0) k_island<G><<<grid(sv.v_fast.size(), G, wb), wb, 0, s>>>(ranged(v, sv.v_fast));
 }
 void self_apply(const View& v, const SelfVariants& sv, cudaStream_t s) {
     const int qb = tune_of(v.tune, kTuneQueryBlock);
