@@ -200,11 +200,14 @@ __global__ void k_vhash_scatter(View v) {
 
 
 // Collapsed ranges are counted as guard events in the count pass, once per
-// primitive, with one ballot per warp (every lane reaches it).
+// primitive: a ballot per warp, a sum per block (every thread reaches both).
 template <bool kTri, int L>
 __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
+    __shared__ unsigned collapsed_s;  // the block's collapsed ranges: one global atomic per block
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = v.lo + (int)(t / L), r0 = (int)(t % L);
+    if (threadIdx.x == 0) collapsed_s = 0u;
+    __syncthreads();
     bool collapsed = false;
     if (k < v.hi) {
         const Params& P = kTri ? params_t(v, k) : params_e(v, k);
@@ -232,7 +235,9 @@ __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     }
     if (!scatter) {
         const unsigned m = __ballot_sync(0xffffffffu, collapsed && r0 == 0);
-        if ((threadIdx.x & 31) == 0 && m) count_add(v.counts, kCntSelfOverflow, (unsigned long long)__popc(m));
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(&collapsed_s, (unsigned)__popc(m));
+        __syncthreads();
+        if (threadIdx.x == 0 && collapsed_s) count_add(v.counts, kCntSelfOverflow, (unsigned long long)collapsed_s);
     }
 }
 
