@@ -1547,7 +1547,7 @@ int fused_block(const Solver* S) {
 }
 
 void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Profile* prof) {
-    const int nV = S->nV, nE = S->nE;
+    const int nV = S->nV;
     const int dyn = dynamic_kinds(S);
     if (!prof && !S->rec) {
         const auto f = S->fused_ops.find(frame_key(S, substeps, iterations));
