@@ -91,3 +91,68 @@ def self_vv_line():
     opts = options(self_collision=True, cloth_thickness=0.10, collision_margin=0.0, contact_friction=0.0,
                    contact_tangent_damping=0.0)
     return cloth(pos), opts, close
+
+
+# ---- tools/abi41_self_collision_smoke.py: fast-mode self collision, 0.1
+# thickness, no margin or friction (:26-67), one 1 x 6 step each -----------
+def smoke_options() -> scene.SolverOptions:
+    return options(self_collision=True, self_collision_mode=1, cloth_thickness=0.10, collision_margin=0.0,
+                   contact_friction=0.0, contact_tangent_damping=0.0, static_sdf_voxel_size=0.0,
+                   static_sdf_band_voxels=4, static_sdf_max_resolution=160, self_probe_interval=4,
+                   self_surface_pair_interval=4)
+
+
+def smoke_vv():
+    """600 vertices on a line, the last moved 3 cm from vertex 0 (:70-90,
+    :185-199); returns (cloth, moved positions, gap(out))."""
+    cl = cloth(np.stack([np.arange(600, dtype=np.float32), np.zeros(600, np.float32), np.zeros(600, np.float32)], 1))
+    close = cl.positions_world.copy()
+    close[-1] = [0.03, 0.0, 0.0]
+    return cl, close, lambda o: float(np.linalg.norm(o[-1] - o[0]))
+
+
+def smoke_vt():
+    """A pinned triangle and 63 far ones, vertex 599 moved 3 cm above the
+    first (:93-132, :221-233); returns (cloth, moved positions, height(out))."""
+    n, nt = 600, 64
+    pos = np.zeros((n, 3), np.float32)
+    inv = np.ones(n, np.float32)
+    pos[0], pos[1], pos[2] = [-1.0, -1.0, 0.0], [1.0, -1.0, 0.0], [0.0, 1.0, 0.0]
+    inv[:3] = 0.0
+    for i in range(3, n):
+        pos[i] = [20.0 + float(i), 20.0 + float(i % 7) * 0.25, float(i % 5) * 0.20]
+    pos[n - 1] = [5.0, 5.0, 1.0]
+    tris = np.array([[0, 1, 2]] + [[3 + t * 3, 4 + t * 3, 5 + t * 3] for t in range(1, nt)], np.int32)
+    cl = cloth(pos, inv)
+    cl.triangles = tris
+    close = pos.copy()
+    close[n - 1] = [0.0, -0.2, 0.03]
+    return cl, close, lambda o: float(o[n - 1, 2])
+
+
+def smoke_ee():
+    """A pinned edge and a crossing edge moved 3 cm above it, 62 far edges
+    (:135-176, :266-278); returns (cloth, moved positions, height(out))."""
+    n, ne = 600, 64
+    pos = np.zeros((n, 3), np.float32)
+    inv = np.ones(n, np.float32)
+    for i in range(n):
+        pos[i] = [200.0 + float(i) * 3.0, 100.0 + float(i % 11), 0.0]
+    pos[0], pos[1], pos[2], pos[3] = [-1.0, 0.0, 0.0], [1.0, 0.0, 0.0], [5.0, -1.0, 0.0], [5.0, 1.0, 0.0]
+    inv[:2] = 0.0
+    edges = np.zeros((ne, 2), np.int32)
+    edges[0], edges[1] = [0, 1], [2, 3]
+    for e in range(2, ne):
+        a = 4 + (e - 2) * 2
+        pos[a] = [50.0 + float(e) * 4.0, 30.0, 0.0]
+        pos[a + 1] = [51.0 + float(e) * 4.0, 30.0, 0.0]
+        edges[e] = [a, a + 1]
+    cl = cloth(pos, inv)
+    cl.edges = edges
+    cl.edge_rest_lengths = np.linalg.norm(pos[edges[:, 0]] - pos[edges[:, 1]], axis=1).astype(np.float32)
+    close = pos.copy()
+    close[2], close[3] = [0.0, -1.0, 0.03], [0.0, 1.0, 0.03]
+    return cl, close, lambda o: float((o[2, 2] + o[3, 2]) * 0.5)
+
+
+SMOKES = {"vv": smoke_vv, "vt": smoke_vt, "ee": smoke_ee}

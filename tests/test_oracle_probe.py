@@ -44,3 +44,20 @@ def test_probe_self_vv_pushes_apart(oracle_lib):
     assert np.isfinite(out).all() and np.isfinite(follow).all()
     assert gap1 > gap0  # the pair was separated
     assert gap2 >= gap1 - 1e-6  # and does not fall back
+
+
+@pytest.mark.parametrize("case", sorted(kp.SMOKES))
+def test_self_collision_smoke_oracle(case, oracle_lib):
+    """tools/abi41_self_collision_smoke.py's conditions on the oracle: the
+    pair separates by more than 1e-4 and contacts are counted (counter slots:
+    0 soft, 1 exact impulse, 2 edge-edge, 9 self candidates)."""
+    cl, close, measure = kp.SMOKES[case]()
+    s = oracle_lib.OracleSolver.from_scene(cl, kp.smoke_options(), kp.NO_STATIC)
+    s.update_positions(close)
+    s.step(1, 6)
+    out = s.download_positions().copy()
+    c = s.read_buffer(13, np.uint64, 38)
+    assert np.isfinite(out).all()
+    assert measure(out) > measure(close) + 1.0e-4
+    contacts = {"vv": int(c[0]) + int(c[1]), "vt": int(c[0]), "ee": int(c[2])}[case]
+    assert contacts > 0 and (case == "ee" or int(c[9]) > 0)
