@@ -353,9 +353,38 @@ __device__ __forceinline__ bool bucket_order_needed(const Params& P) {
     return fast_mode(P) || budget < kBucketSlots;
 }
 
+// Sort e[0..n) (n <= N) in registers: bitonic network over N, padded with
+// INT_MAX.
+template <int N>
+__device__ __forceinline__ void sort_small(int* e, int n) {
+    int r[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) r[k] = k < n ? e[k] : 0x7fffffff;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const int l = k ^ stride;
+                if (l > k) {
+                    const int lo = min(r[k], r[l]), hi = max(r[k], r[l]);
+                    const bool up = (k & size) == 0;
+                    r[k] = up ? lo : hi;
+                    r[l] = up ? hi : lo;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if (k < n) e[k] = r[k];
+}
+
 // Order bucket members by primitive id.  One warp per 32 consecutive buckets:
 // each lane sorts its own bucket of up to 16 members in registers (bitonic
-// network over 16, padded with INT_MAX); a bucket of 17-32 members is sorted
+// network over 8, or 16 when a bucket of the warp needs it, padded with
+// INT_MAX); a bucket of 17-32 members is sorted
 // by the whole warp (each lane ranks one member against all others with
 // shuffles); a larger one gets its 32 smallest ids moved to the front in
 // order (queries read no further).
@@ -384,32 +413,14 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
         }
     }
     constexpr int kSmall = 16;
-    if (need && n <= kSmall) {
-        int r[kSmall];
-        int* e = ent + s;
-#pragma unroll
-        for (int k = 0; k < kSmall; ++k) r[k] = k < n ? e[k] : 0x7fffffff;
-#pragma unroll
-        for (int size = 2; size <= kSmall; size <<= 1) {
-#pragma unroll
-            for (int stride = size >> 1; stride > 0; stride >>= 1) {
-#pragma unroll
-                for (int k = 0; k < kSmall; ++k) {
-                    const int l = k ^ stride;
-                    if (l > k) {
-                        const int lo = min(r[k], r[l]), hi = max(r[k], r[l]);
-                        const bool up = (k & size) == 0;
-                        r[k] = up ? lo : hi;
-                        r[l] = up ? hi : lo;
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kSmall; ++k)
-            if (k < n) e[k] = r[k];
-        need = false;
+    const bool small = need && n <= kSmall;
+    // the network size follows the warp's largest small bucket (8 or 16)
+    if (__any_sync(0xffffffffu, small && n > 8)) {
+        if (small) sort_small<16>(ent + s, n);
+    } else if (small) {
+        sort_small<8>(ent + s, n);
     }
+    if (small) need = false;
     unsigned mask = __ballot_sync(0xffffffffu, need);
     while (mask) {
         const int j = __ffs(mask) - 1;
