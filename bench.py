@@ -116,6 +116,20 @@ def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict)
     return None
 
 
+# DRAM bytes (read + write) per evaluated bucket slot of the edge-edge query
+# passes, measured by ncu on the 96-cloth batch and scaled by the slots of
+# the measured workload (profiles/edge_edge_dram_per_slot_batch96.md).
+EE_DRAM_BYTES_PER_SLOT = 11.4
+
+
+def measured_traffic(kind: str, counters: dict, launches: int) -> float | None:
+    """DRAM traffic per launch of a kernel kind, scaled from an ncu capture
+    of a smaller case, or None where none was taken."""
+    if kind == "edge_edge" and counters.get("ee_slots") and launches > 0:
+        return EE_DRAM_BYTES_PER_SLOT * counters["ee_slots"] / launches
+    return None
+
+
 def peaks() -> tuple[float, str]:
     try:
         with open(PEAKS_FILE) as f:
@@ -619,8 +633,11 @@ def main():
         # query counters cover all profiled frames: bytes per launch
         per_launch = alg_total / max(k_n, 1) if kind in ("edge_edge", "vertex_triangle") else alg_total
         achieved = per_launch / (avg_ms / 1000.0) / 1e9
+        traffic = measured_traffic(kind, counters, k_n)
         roof = {"bound": "hbm", "kernel": kind, "dominant": kind == dominant, "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": None,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": traffic,
+                "traffic_source": ("ncu DRAM bytes per evaluated slot on 96 cloths, scaled by this workload's slots per "
+                                   "launch" if traffic is not None else None),
                 "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch}
         break
     profile_summary = {k: {"ms_per_frame": v[0] / reps, "launches_per_frame": v[1] / reps} for k, v in prof.items() if v[1]}
