@@ -120,6 +120,9 @@ def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict)
 # passes, measured by ncu on the 96-cloth batch and scaled by the slots of
 # the measured workload (profiles/edge_edge_dram_per_slot_batch96.md).
 EE_DRAM_BYTES_PER_SLOT = 11.4
+# ... and per entry of an edge-hash build (count, scans, scatter, trim and
+# bucket ordering; profiles/edge_hash_dram_per_entry_batch96.md).
+EDGE_HASH_DRAM_BYTES_PER_ENTRY = 16.7
 
 
 def measured_traffic(kind: str, counters: dict, launches: int) -> float | None:
@@ -127,6 +130,8 @@ def measured_traffic(kind: str, counters: dict, launches: int) -> float | None:
     of a smaller case, or None where none was taken."""
     if kind == "edge_edge" and counters.get("ee_slots") and launches > 0:
         return EE_DRAM_BYTES_PER_SLOT * counters["ee_slots"] / launches
+    if kind == "edge_hash" and counters.get("edge_entries"):
+        return EDGE_HASH_DRAM_BYTES_PER_ENTRY * counters["edge_entries"]  # one build
     return None
 
 
@@ -636,8 +641,8 @@ def main():
         traffic = measured_traffic(kind, counters, k_n)
         roof = {"bound": "hbm", "kernel": kind, "dominant": kind == dominant, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": traffic,
-                "traffic_source": ("ncu DRAM bytes per evaluated slot on 96 cloths, scaled by this workload's slots per "
-                                   "launch" if traffic is not None else None),
+                "traffic_source": ("ncu DRAM bytes per evaluated slot (edge-edge) or per entry (edge hash) on 96 cloths, "
+                                   "scaled by this workload's units per launch" if traffic is not None else None),
                 "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch}
         break
     profile_summary = {k: {"ms_per_frame": v[0] / reps, "launches_per_frame": v[1] / reps} for k, v in prof.items() if v[1]}
