@@ -19,11 +19,14 @@
 //     call left there: each call clears the counters it uses first, and two
 //     calls whose work overlaps on the GPU (different streams, or host threads
 //     without ordering) race on it and corrupt each other's result;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture begins.
+//   * every call looks up the array's device address in the current context
+//     (cudaGetSymbolAddress, with the caller's device current), so a device
+//     reset or another context on the same device never leaves a stale
+//     address behind; the first lookup on a device also loads the library's
+//     device code there, so make the first call on a device before any
+//     stream capture begins.
+#include <climits>
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "xpbd_solver.cuh"
@@ -31,36 +34,23 @@
 namespace {
 
 constexpr int kNoAllocMaxBuckets = 1 << 18;
-constexpr int kMaxDevices = 64;
 
 // Bucket counters, then scatter cursors, of the last call on this device.
 static __device__ __align__(256) int g_noalloc_bucket_scratch[kNoAllocMaxBuckets];
-
-// Host-side device addresses of the array, one per device, filled on the
-// first call made with that device current.  The array's name itself is not
-// a device address in host code.
-int* g_scratch_addr[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
 
 bool noalloc_fail(const std::string& msg) {
     xg::set_last_error(msg);
     return false;
 }
 
+// Device address of the scratch array in the current context.  In host code
+// the array's name is only a host-side stand-in, never a device address.
 bool scratch_for_current_device(int** out) {
-    int dev = -1;
-    cudaError_t err = cudaGetDevice(&dev);
-    if (err != cudaSuccess) return noalloc_fail(std::string("no current CUDA device: ") + cudaGetErrorString(err));
-    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail("CUDA device index out of range");
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        err = cudaGetSymbolAddress(&ptr, g_noalloc_bucket_scratch);
-        if (err != cudaSuccess || !ptr)
-            return noalloc_fail(std::string("cudaGetSymbolAddress of the hash scratch failed: ") + cudaGetErrorString(err));
-        g_scratch_addr[dev] = static_cast<int*>(ptr);
-    }
-    *out = g_scratch_addr[dev];
+    void* ptr = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_bucket_scratch);
+    if (err != cudaSuccess || !ptr)
+        return noalloc_fail(std::string("cudaGetSymbolAddress of the hash scratch failed: ") + cudaGetErrorString(err));
+    *out = static_cast<int*>(ptr);
     return true;
 }
 
@@ -72,7 +62,7 @@ __global__ void k_cells(const float* __restrict__ pos, int n, float cell, int bu
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    const int cx = xg::cell_of(x, cell), cy = xg::cell_of(y, cell), cz = xg::cell_of(z, cell);
+    const int cx = xg::cell_of(x, cell, 0), cy = xg::cell_of(y, cell, 0), cz = xg::cell_of(z, cell, 0);
     const int b = (int)xg::bucket_of(cx, cy, cz, buckets);
     if (cells) cells[i] = make_int4(cx, cy, cz, b);
     atomicAdd(&counts[b], 1);
@@ -128,27 +118,66 @@ __global__ void __launch_bounds__(1024) k_scan_counts(int* counts, int* start, i
 __global__ void k_scatter(const float* __restrict__ pos, int n, float cell, int buckets, int* cursor, int* entries) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int b = (int)xg::bucket_of(xg::cell_of(pos[3 * i], cell), xg::cell_of(pos[3 * i + 1], cell),
-                                     xg::cell_of(pos[3 * i + 2], cell), buckets);
+    const int b = (int)xg::bucket_of(xg::cell_of(pos[3 * i], cell, 0), xg::cell_of(pos[3 * i + 1], cell, 0),
+                                     xg::cell_of(pos[3 * i + 2], cell, 0), buckets);
     entries[atomicAdd(&cursor[b], 1)] = i;
 }
 
 // Members of each bucket in increasing vertex id (the 32 smallest first when
-// a bucket holds more, as the solver's queries read no further).
+// a bucket holds more, as the solver's queries read no further).  A thread
+// orders its own bucket when it has at most 32 members; a crowded bucket
+// (say a collapsed cloth with every vertex in one cell) is ordered by the
+// whole warp: 32 rounds, each a warp-wide minimum over the unplaced members,
+// O(n) steps per lane instead of O(32 n) on one thread.  Every thread of
+// the grid reaches the ballot (no early return), so the full mask is valid.
 __global__ void k_order(const int* start, int* entries, int buckets) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= buckets) return;
-    const int s = start[b], n = start[b + 1] - s;
-    int* e = entries + s;
-    if (n <= 1) return;
-    const int keep = n <= 32 ? n : 32;
-    for (int i = 0; i < keep; ++i) {
-        int best = i;
-        for (int j = i + 1; j < n; ++j)
-            if (e[j] < e[best]) best = j;
-        const int t = e[i];
-        e[i] = e[best];
-        e[best] = t;
+    const int lane = threadIdx.x & 31;
+    int s = 0, n = 0;
+    if (b < buckets) {
+        s = start[b];
+        n = start[b + 1] - s;
+    }
+    if (n > 1 && n <= 32) {
+        int* e = entries + s;
+        for (int i = 0; i < n; ++i) {
+            int best = i;
+            for (int j = i + 1; j < n; ++j)
+                if (e[j] < e[best]) best = j;
+            const int t = e[i];
+            e[i] = e[best];
+            e[best] = t;
+        }
+    }
+    unsigned crowded = __ballot_sync(0xffffffffu, n > 32);
+    while (crowded) {
+        const int src = __ffs(crowded) - 1;
+        crowded &= crowded - 1;
+        const int bs = __shfl_sync(0xffffffffu, s, src), bn = __shfl_sync(0xffffffffu, n, src);
+        int* e = entries + bs;
+        for (int i = 0; i < 32; ++i) {
+            int best_v = INT_MAX, best_j = bn;
+            for (int j = i + lane; j < bn; j += 32) {
+                const int v = e[j];
+                if (v < best_v) {
+                    best_v = v;
+                    best_j = j;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const int ov = __shfl_xor_sync(0xffffffffu, best_v, o);
+                const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
+                if (ov < best_v || (ov == best_v && oj < best_j)) {
+                    best_v = ov;
+                    best_j = oj;
+                }
+            }
+            if (lane == 0 && best_j != i && best_j < bn) {
+                e[best_j] = e[i];
+                e[i] = best_v;
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -159,7 +188,8 @@ __global__ void k_order(const int* start, int* entries, int buckets) {
 // `cell_size` metres and `bucket_count` buckets (a power of two, at most
 // 262144): bucket_start[0..bucket_count] (device, bucket_count + 1 ints),
 // bucket_entries[0..vertex_count) (device) and, when non-null, cells (device,
-// 4 ints per vertex: cell x, y, z, bucket).  Work is queued on `stream`
+// 4 ints per vertex: cell x, y, z, bucket; written as int4, so the pointer
+// must be 16-byte aligned).  Work is queued on `stream`
 // (a cudaStream_t; null = the default stream) and the call returns without
 // waiting.  Returns 1, or 0 with the reason in ssbl_last_error().  Allocates
 // nothing; see the notes at the top of this file.
@@ -167,6 +197,9 @@ extern "C" __attribute__((visibility("default"))) int xpbd_gb300_vertex_hash_noa
     const float* positions, int vertex_count, float cell_size, int bucket_count, int* bucket_start, int* bucket_entries,
     int* cells, void* stream) {
     xg::set_last_error(std::string());
+    // A launch error left pending by earlier, unrelated work on this thread
+    // would otherwise be reported as this call's failure below.
+    (void)cudaGetLastError();
     if (vertex_count < 0 || (vertex_count > 0 && (!positions || !bucket_entries)) || !bucket_start)
         return noalloc_fail("invalid vertex hash request") ? 1 : 0;
     if (!std::isfinite(cell_size) || cell_size <= 0.0f) return noalloc_fail("cell size must be finite and positive") ? 1 : 0;
