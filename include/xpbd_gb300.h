@@ -42,6 +42,19 @@ __attribute__((visibility("default"))) long long xpbd_gb300_read_buffer(void* ha
  * counts, out[3..5] = 1 when that hash is used (else brute force). */
 __attribute__((visibility("default"))) int xpbd_gb300_hash_info(void* handle, int* out6);
 
+/* Division of the spatial-hash cell keys, floor(x / cell) (no counterpart in
+ * the reference; its keys are compiled with --use_fast_math, abi41.cu:654-656,
+ * native/CMakeLists.txt:109).  mode 0 (the default): the reference's
+ * approximate, flush-to-zero division, so cells, bucket ids and bucket
+ * contents are the reference's integers; mode 1: the correctly rounded IEEE
+ * quotient, which the CPU oracle reproduces bit for bit.  The two differ only
+ * for quotients within a few ulp of an integer.  set_key_division applies to
+ * one solver or batch (dynamic colliders uploaded afterwards);
+ * set_default_key_division to the solvers and global dynamic scenes created
+ * afterwards in this process. */
+__attribute__((visibility("default"))) int xpbd_gb300_set_key_division(void* handle, int mode);
+__attribute__((visibility("default"))) int xpbd_gb300_set_default_key_division(int mode);
+
 /* Capture each frame's launch sequence as a CUDA graph (default 1). */
 __attribute__((visibility("default"))) int xpbd_gb300_set_graph_capture(void* handle, int enabled);
 
@@ -131,13 +144,16 @@ __attribute__((visibility("default"))) int xpbd_gb300_profile_counters(void* han
  * absorb the device synchronisation those calls may cause).  Inputs and
  * outputs are the caller's device arrays: positions (x y z per vertex),
  * bucket_start (bucket_count + 1 ints), bucket_entries (vertex_count ints),
- * cells (4 ints per vertex, may be NULL).  bucket_count must be a power of
- * two of at most 262144: the bucket counters live in a fixed 1 MiB array
- * inside the library, one per device, kept until the process exits and
- * shared by every call, so calls that overlap on the GPU race.  The first
- * call on a device looks up that array's address; make it before any stream
- * capture.  Work is queued on `stream` (cudaStream_t, NULL = default).
- * Returns 1, or 0 with ssbl_last_error() set. */
+ * cells (4 ints per vertex, written as int4: 16-byte aligned; may be NULL).
+ * bucket_count must be a power of two of at most 262144: the bucket counters
+ * live in a fixed 1 MiB array inside the library, one per device, kept until
+ * the process exits and shared by every call, so calls that overlap on the
+ * GPU race.  Each call looks up that array's address in the current context;
+ * the first call on a device also loads the library's device code, so make
+ * it before any stream capture.  Buckets are ordered by a thread each, or by
+ * a warp when one holds more than 32 members.  Work is queued on `stream`
+ * (cudaStream_t, NULL = default).  Returns 1, or 0 with ssbl_last_error()
+ * set. */
 __attribute__((visibility("default"))) int xpbd_gb300_vertex_hash_noalloc(const float* positions, int vertex_count,
                                                                            float cell_size, int bucket_count,
                                                                            int* bucket_start, int* bucket_entries,
@@ -213,6 +229,11 @@ __attribute__((visibility("default"))) int xpbd_gb300_diff_rollout(void* handle,
 __attribute__((visibility("default"))) int xpbd_gb300_diff_backward(void* handle, const float* grad_positions,
                                                                      float* grad_stretch, float* grad_bend);
 __attribute__((visibility("default"))) void* xpbd_gb300_diff_stream(void* handle);
+/* State at the start of frame `frame` of the last rollout (frame = frames:
+ * the final state) as 3 x V float4 rows (positions, previous positions,
+ * velocities; device array of 12 V floats), so a caller can evaluate other
+ * derivatives along the rollout's own trajectory. */
+__attribute__((visibility("default"))) int xpbd_gb300_diff_checkpoint(void* handle, int frame, float* out_rows);
 
 /* Host-side input preprocessing of the cloth builders (no device work):
  * greedy first-fit colouring of constraint pairs in order (writes a colour

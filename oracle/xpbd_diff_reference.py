@@ -10,6 +10,11 @@ stretch 1927-1980 as a snapshot gather, pins 3466-3509, bends by colour
 that autograd yields a reference gradient with respect to per-constraint
 compliances.  Branch decisions (caps, clamps, sign tests) are taken in
 float64, so near a threshold they may differ from the float32 solver.
+
+Every operation works on leading batch dimensions: compliance tensors of
+shape (..., E) and (..., B) roll out states of shape (..., V, 3), so many
+parameter sets (the perturbations of a finite-difference check) run as one
+rollout, on any torch device.
 """
 from __future__ import annotations
 
@@ -35,20 +40,20 @@ def frame_ops(substeps: int, iterations: int, bends: bool) -> list:
 
 
 class Rollout:
-    def __init__(self, cloth, options, dtype=torch.float64):
-        t = lambda a: torch.as_tensor(np.asarray(a, np.float64)).to(dtype)  # noqa: E731
+    def __init__(self, cloth, options, dtype=torch.float64, device="cpu"):
+        t = lambda a: torch.as_tensor(np.asarray(a, np.float64)).to(device=device, dtype=dtype)  # noqa: E731
         self.rest = t(cloth.positions_world)
         self.w = t(np.maximum(cloth.inv_mass, 0.0))
         self.V = len(self.rest)
         e = np.asarray(cloth.edges, np.int64).reshape(-1, 2)
-        self.ei, self.ej = torch.as_tensor(e[:, 0]), torch.as_tensor(e[:, 1])
+        self.ei, self.ej = torch.as_tensor(e[:, 0], device=device), torch.as_tensor(e[:, 1], device=device)
         self.erest = t(cloth.edge_rest_lengths)
         b = np.asarray(cloth.bends, np.int64).reshape(-1, 2)
-        self.bi, self.bj = torch.as_tensor(b[:, 0]), torch.as_tensor(b[:, 1])
+        self.bi, self.bj = torch.as_tensor(b[:, 0], device=device), torch.as_tensor(b[:, 1], device=device)
         self.brest = t(cloth.bend_rest_lengths)
         self.colors = [int(x) for x in cloth.bend_color_offsets]
-        self.pinned = torch.zeros(self.V, dtype=torch.bool)
-        self.target = torch.zeros(self.V, 3, dtype=dtype)
+        self.pinned = torch.zeros(self.V, dtype=torch.bool, device=device)
+        self.target = torch.zeros(self.V, 3, dtype=dtype, device=device)
         for idx, pos, wt in zip(cloth.pin_indices, cloth.pin_targets_world, cloth.pin_weights):
             if wt >= 0.75:
                 self.pinned[int(idx)] = True
@@ -63,22 +68,22 @@ class Rollout:
         wi, wj = self.w[self.ei], self.w[self.ej]
         W = wi + wj
         live = W > 0
-        delta = p[self.ej] - p[self.ei]
-        length = torch.sqrt(torch.clamp((delta * delta).sum(1), min=EPS))
+        delta = p[..., self.ej, :] - p[..., self.ei, :]
+        length = torch.sqrt(torch.clamp((delta * delta).sum(-1), min=EPS))
         c = length - self.erest
         alpha = torch.clamp(k, min=0.0) / max(dt * dt, EPS)
         dl = -c / torch.where(live, W + alpha, torch.ones_like(W))
-        corr = delta * (0.18 * dl / torch.clamp(length, min=EPS))[:, None]
-        clen = torch.sqrt(torch.clamp((corr * corr).sum(1), min=1e-30))
+        corr = delta * (0.18 * dl / torch.clamp(length, min=EPS))[..., None]
+        clen = torch.sqrt(torch.clamp((corr * corr).sum(-1), min=1e-30))
         maxc = torch.clamp(torch.clamp(torch.clamp(self.erest, min=0.0) * 0.10, max=0.025), min=0.0025)
         capped = clen > maxc
-        corr = torch.where(capped[:, None], corr * (maxc / torch.clamp(clen, min=EPS))[:, None], corr)
+        corr = torch.where(capped[..., None], corr * (maxc / torch.clamp(clen, min=EPS))[..., None], corr)
         corr = corr * live[:, None]
         di = -corr * wi[:, None]
         dj = corr * wj[:, None]
-        kp = torch.where(c > 0, torch.full_like(c, 0.08), torch.zeros_like(c))[:, None]
-        p = p.index_add(0, self.ei, di).index_add(0, self.ej, dj)
-        prev = prev.index_add(0, self.ei, di * kp).index_add(0, self.ej, dj * kp)
+        kp = torch.where(c > 0, torch.full_like(c, 0.08), torch.zeros_like(c))[..., None]
+        p = p.index_add(-2, self.ei, di).index_add(-2, self.ej, dj)
+        prev = prev.index_add(-2, self.ei, di * kp).index_add(-2, self.ej, dj * kp)
         return p, prev
 
     def _bends(self, p, prev, k, dt):
@@ -86,11 +91,11 @@ class Rollout:
             if c1 <= c0:
                 continue
             sl = slice(c0, c1)
-            i, j, rest, kk = self.bi[sl], self.bj[sl], self.brest[sl], k[sl]
+            i, j, rest, kk = self.bi[sl], self.bj[sl], self.brest[sl], k[..., sl]
             wi, wj = self.w[i], self.w[j]
             W = wi + wj
-            delta = p[j] - p[i]
-            len_sq = (delta * delta).sum(1)
+            delta = p[..., j, :] - p[..., i, :]
+            len_sq = (delta * delta).sum(-1)
             ok = (W > 0) & (rest > EPS) & (len_sq > 1.0e-10)
             inv_len = 1.0 / torch.sqrt(torch.where(ok, len_sq, torch.ones_like(len_sq)))
             length = len_sq * inv_len
@@ -98,15 +103,15 @@ class Rollout:
             ok = ok & (torch.abs(c) > 1.0e-6)
             alpha = torch.clamp(kk, min=0.0) / max(dt * dt, EPS)
             dl = -c / torch.clamp(W + alpha, min=EPS)
-            corr = delta * (0.10 * dl * inv_len)[:, None]
-            clen = torch.sqrt(torch.clamp((corr * corr).sum(1), min=1e-30))
+            corr = delta * (0.10 * dl * inv_len)[..., None]
+            clen = torch.sqrt(torch.clamp((corr * corr).sum(-1), min=1e-30))
             maxc = torch.clamp(torch.clamp(torch.clamp(rest, min=self.thickness) * 0.08, max=0.020), min=2.5e-4)
             capped = clen > maxc
-            corr = torch.where(capped[:, None], corr * (maxc / torch.clamp(clen, min=EPS))[:, None], corr)
-            corr = corr * ok[:, None]
+            corr = torch.where(capped[..., None], corr * (maxc / torch.clamp(clen, min=EPS))[..., None], corr)
+            corr = corr * ok[..., None]
             di, dj = -corr * wi[:, None], corr * wj[:, None]
-            p = p.index_add(0, i, di).index_add(0, j, dj)
-            prev = prev.index_add(0, i, di * 0.06).index_add(0, j, dj * 0.06)
+            p = p.index_add(-2, i, di).index_add(-2, j, dj)
+            prev = prev.index_add(-2, i, di * 0.06).index_add(-2, j, dj * 0.06)
         return p, prev
 
     def _velocity(self, p, prev, vel, dt):
@@ -114,43 +119,49 @@ class Rollout:
         free = (self.w > 0)[:, None]
         measured = (p - prev) * (1.0 / sdt)
         proj = measured - vel
-        pdb = (proj * vel).sum(1)
-        scale = torch.where(pdb > 0, torch.full_like(pdb, 0.9), torch.ones_like(pdb))[:, None]
+        pdb = (proj * vel).sum(-1)
+        scale = torch.where(pdb > 0, torch.full_like(pdb, 0.9), torch.ones_like(pdb))[..., None]
         fb = proj * scale
-        fspeed = torch.sqrt(torch.clamp((fb * fb).sum(1), min=1e-30))
+        fspeed = torch.sqrt(torch.clamp((fb * fb).sum(-1), min=1e-30))
         max_speed = max(2.0e-4, max(self.thickness, 0.0) * 0.35) / sdt
-        clamp = (scale[:, 0] < 1.0) & (fspeed > max_speed) & (fspeed > EPS)
-        fb = torch.where(clamp[:, None], fb * (max_speed / torch.clamp(fspeed, min=EPS))[:, None], fb)
+        clamp = (scale[..., 0] < 1.0) & (fspeed > max_speed) & (fspeed > EPS)
+        fb = torch.where(clamp[..., None], fb * (max_speed / torch.clamp(fspeed, min=EPS))[..., None], fb)
         return torch.where(free, vel + fb, torch.zeros_like(vel))
 
-    def run(self, stretch_k, bend_k, frames: int, substeps: int, iterations: int):
+    def frame(self, p, prev, vel, stretch_k, bend_k, substeps: int, iterations: int):
+        """One frame from the state (p, prev, vel); returns the next state."""
         dt = self.dt_frame / substeps
-        p = self.rest.clone()
-        prev = self.rest.clone()
-        vel = torch.zeros_like(p)
         free = (self.w > 0)[:, None]
         pin = self.pinned[:, None]
         ops = frame_ops(substeps, iterations, len(self.colors) > 1 and self.colors[-1] > 0)
-        for _ in range(frames):
-            for kind, flags in ops:
-                if kind == "predict":
-                    prev = p
-                    vf = (vel + self.gravity * dt) * self.damping
-                    pf = p + vf * dt
-                    p = torch.where(free, pf, self.rest)
-                    vel = torch.where(free, vf, torch.zeros_like(vf))
+        for kind, flags in ops:
+            if kind == "predict":
+                prev = p
+                vf = (vel + self.gravity * dt) * self.damping
+                pf = p + vf * dt
+                p = torch.where(free, pf, self.rest)
+                vel = torch.where(free, vf, torch.zeros_like(vf))
+                p = torch.where(pin, self.target, p)
+                prev = torch.where(pin, self.target, prev)
+                vel = torch.where(pin, torch.zeros_like(vel), vel)
+            elif kind == "pass":
+                if "gather" in flags:
+                    p, prev = self._stretch(p, prev, stretch_k, dt)
+                if "pin" in flags:
                     p = torch.where(pin, self.target, p)
                     prev = torch.where(pin, self.target, prev)
                     vel = torch.where(pin, torch.zeros_like(vel), vel)
-                elif kind == "pass":
-                    if "gather" in flags:
-                        p, prev = self._stretch(p, prev, stretch_k, dt)
-                    if "pin" in flags:
-                        p = torch.where(pin, self.target, p)
-                        prev = torch.where(pin, self.target, prev)
-                        vel = torch.where(pin, torch.zeros_like(vel), vel)
-                    if "velocity" in flags:
-                        vel = self._velocity(p, prev, vel, dt)
-                else:
-                    p, prev = self._bends(p, prev, bend_k, dt)
+                if "velocity" in flags:
+                    vel = self._velocity(p, prev, vel, dt)
+            else:
+                p, prev = self._bends(p, prev, bend_k, dt)
+        return p, prev, vel
+
+    def run(self, stretch_k, bend_k, frames: int, substeps: int, iterations: int):
+        batch = torch.broadcast_shapes(stretch_k.shape[:-1], bend_k.shape[:-1])
+        p = self.rest.expand(*batch, self.V, 3).clone()
+        prev = p.clone()
+        vel = torch.zeros_like(p)
+        for _ in range(frames):
+            p, prev, vel = self.frame(p, prev, vel, stretch_k, bend_k, substeps, iterations)
         return p

@@ -180,6 +180,7 @@ struct OracleSolver {
     V3* avg_sum; float* avg_cnt;
     float red[8]; unsigned long long pcg_guard; float pcg_max_delta;
     int* cap_edges; float* cap_rest; int* cap_colors; int n_cap_colors;
+    int cap_jacobi; V3* snap_prev; /* caps without a caller colouring (cap_jacobi) */
     /* prediction extras: incident triangles, volume pressure, force fields */
     int *vt_off, *vt_tri;
     int pressure_on; float *p_area, *p_rest;
@@ -1753,62 +1754,110 @@ static void averaged_pass(OracleSolver* s, int tiny) {
     }
 }
 
-/* Ratio caps in place one colour at a time: kind 0 normal
- * (abi41.cu:2249-2362), 1 tiny (2496-2601), 2 extreme (2603-2708). */
+/* One edge of a ratio cap, kind 0 normal (abi41.cu:2249-2362), 1 tiny
+ * (2496-2601), 2 extreme (2603-2708): the position correction d* and the
+ * previous-position shift pd* of each endpoint, ok* = 0 where that endpoint
+ * gets nothing.  Returns 0 when the edge is skipped. */
+static int cap_edge(const OracleSolver* s, int kind, float dt, float rest, V3 pi, V3 pj, V3 qi, V3 qj, float wi, float wj,
+                    V3* di, V3* pdi_out, int* oki, V3* dj, V3* pdj_out, int* okj) {
+    *oki = *okj = 0;
+    if (!isfinite(rest) || rest <= K_EPS) return 0;
+    if (kind == 1 ? rest > 7.5e-4f : rest <= 7.5e-4f) return 0;
+    float weight = wi + wj;
+    if (!isfinite(weight) || weight <= 0.0f) return 0;
+    if (!vfinite(pi) || !vfinite(pj) || !vfinite(qi) || !vfinite(qj)) return 0;
+    V3 edge = vsub(pj, pi);
+    float lsq = vdot(edge, edge);
+    if (!isfinite(lsq) || lsq <= 1.0e-14f) return 0;
+    float len = sqrtf(lsq);
+    int high = s->strength >= 0.95f;
+    float sr, tr, md, ps;
+    float th = s->cfg.cloth_thickness;
+    if (kind == 0) { sr = high ? 1.12f : 1.32f; tr = high ? 1.04f : 1.22f; md = fminf(fmaxf(rest * 0.60f, th * 0.10f), 0.010f); ps = 0.08f; }
+    else if (kind == 1) { sr = 1.35f; tr = 1.12f; md = fminf(fmaxf(rest * 6.0f, 5.0e-4f), 1.5e-3f); ps = 1.0f; }
+    else { sr = 1.24f; tr = 1.10f; md = fminf(fmaxf(rest * 1.25f, th * 0.10f), 0.006f); ps = 0.30f; }
+    if (!isfinite(len) || len <= rest * sr) return 0;
+    float excess = len - rest * tr;
+    if (!isfinite(excess) || excess <= 0.0f) return 0;
+    V3 corr = vmul(edge, -excess / fmaxf(weight * len, K_EPS));
+    if (!vfinite(corr) || vlen(corr) <= 1.0e-20f) return 0;
+    V3 pdi = v3(0, 0, 0), pdj = v3(0, 0, 0);
+    V3 n = vmul(edge, 1.0f / fmaxf(len, K_EPS));
+    float sdt = kind == 0 ? fmaxf(dt, K_EPS) : dt;
+    if (isfinite(sdt) && sdt > K_EPS) {
+        float inv_dt = 1.0f / sdt;
+        V3 vi = vmul(vsub(pi, qi), inv_dt), vj = vmul(vsub(pj, qj), inv_dt);
+        float sep = vdot(vsub(vj, vi), n);
+        if (isfinite(sep) && sep > 0.0f) {
+            float trim = sep * sdt * 1.0f / weight;
+            if (wi > 0.0f) pdi = vadd(pdi, vmul(n, -wi * trim));
+            if (wj > 0.0f) pdj = vadd(pdj, vmul(n, wj * trim));
+        }
+    }
+    if (wi > 0.0f) {
+        V3 d = limit_delta(vmul(corr, -wi), md);
+        if (vfinite(d) && vlen(d) > 0.0f) { *di = d; *pdi_out = vadd(pdi, vmul(d, ps)); *oki = 1; }
+    }
+    if (wj > 0.0f) {
+        V3 d = limit_delta(vmul(corr, wj), md);
+        if (vfinite(d) && vlen(d) > 0.0f) { *dj = d; *pdj_out = vadd(pdj, vmul(d, ps)); *okj = 1; }
+    }
+    return 1;
+}
+
+/* Ratio caps in place one colour at a time (no two edges of a colour share
+ * a vertex), as the reference runs them over a caller's edge colouring. */
 static void cap_range(OracleSolver* s, int start, int count, float dt, int kind) {
 #pragma omp parallel for schedule(static)
     for (int l = 0; l < count; ++l) {
         int e = start + l;
         if (e < 0 || e >= s->E) continue;
-        float rest = s->cap_rest[e];
-        if (!isfinite(rest) || rest <= K_EPS) continue;
-        if (kind == 1 ? rest > 7.5e-4f : rest <= 7.5e-4f) continue;
         int i = s->cap_edges[2 * e], j = s->cap_edges[2 * e + 1];
         if (i < 0 || j < 0 || i >= s->V || j >= s->V || i == j) continue;
-        float wi = s->w[i], wj = s->w[j], weight = wi + wj;
-        if (!isfinite(weight) || weight <= 0.0f) continue;
         V3 pi = s->pos[i], pj = s->pos[j], qi = s->prev[i], qj = s->prev[j];
-        if (!vfinite(pi) || !vfinite(pj) || !vfinite(qi) || !vfinite(qj)) continue;
-        V3 edge = vsub(pj, pi);
-        float lsq = vdot(edge, edge);
-        if (!isfinite(lsq) || lsq <= 1.0e-14f) continue;
-        float len = sqrtf(lsq);
-        int high = s->strength >= 0.95f;
-        float sr, tr, md, ps;
-        float th = s->cfg.cloth_thickness;
-        if (kind == 0) { sr = high ? 1.12f : 1.32f; tr = high ? 1.04f : 1.22f; md = fminf(fmaxf(rest * 0.60f, th * 0.10f), 0.010f); ps = 0.08f; }
-        else if (kind == 1) { sr = 1.35f; tr = 1.12f; md = fminf(fmaxf(rest * 6.0f, 5.0e-4f), 1.5e-3f); ps = 1.0f; }
-        else { sr = 1.24f; tr = 1.10f; md = fminf(fmaxf(rest * 1.25f, th * 0.10f), 0.006f); ps = 0.30f; }
-        if (!isfinite(len) || len <= rest * sr) continue;
-        float excess = len - rest * tr;
-        if (!isfinite(excess) || excess <= 0.0f) continue;
-        V3 corr = vmul(edge, -excess / fmaxf(weight * len, K_EPS));
-        if (!vfinite(corr) || vlen(corr) <= 1.0e-20f) continue;
-        V3 pdi = v3(0, 0, 0), pdj = v3(0, 0, 0);
-        V3 n = vmul(edge, 1.0f / fmaxf(len, K_EPS));
-        float sdt = kind == 0 ? fmaxf(dt, K_EPS) : dt;
-        if (isfinite(sdt) && sdt > K_EPS) {
-            float inv_dt = 1.0f / sdt;
-            V3 vi = vmul(vsub(pi, qi), inv_dt), vj = vmul(vsub(pj, qj), inv_dt);
-            float sep = vdot(vsub(vj, vi), n);
-            if (isfinite(sep) && sep > 0.0f) {
-                float trim = sep * sdt * 1.0f / weight;
-                if (wi > 0.0f) pdi = vadd(pdi, vmul(n, -wi * trim));
-                if (wj > 0.0f) pdj = vadd(pdj, vmul(n, wj * trim));
-            }
-        }
-        if (wi > 0.0f) {
-            V3 d = limit_delta(vmul(corr, -wi), md);
-            if (vfinite(d) && vlen(d) > 0.0f) { pdi = vadd(pdi, vmul(d, ps)); s->pos[i] = vadd(pi, d); s->prev[i] = vadd(qi, pdi); }
-        }
-        if (wj > 0.0f) {
-            V3 d = limit_delta(vmul(corr, wj), md);
-            if (vfinite(d) && vlen(d) > 0.0f) { pdj = vadd(pdj, vmul(d, ps)); s->pos[j] = vadd(pj, d); s->prev[j] = vadd(qj, pdj); }
-        }
+        V3 di, dj, pdi, pdj;
+        int oki, okj;
+        if (!cap_edge(s, kind, dt, s->cap_rest[e], pi, pj, qi, qj, s->w[i], s->w[j], &di, &pdi, &oki, &dj, &pdj, &okj)) continue;
+        if (oki) { s->pos[i] = vadd(pi, di); s->prev[i] = vadd(qi, pdi); }
+        if (okj) { s->pos[j] = vadd(pj, dj); s->prev[j] = vadd(qj, pdj); }
     }
 }
+
+/* Without a caller's colouring the reference runs a cap pass as one launch
+ * over every edge, each adding its corrections to both endpoints with
+ * atomics (abi41.cu:7794-7801): a Jacobi pass.  Restated deterministically:
+ * every edge sees the positions and previous positions at the start of the
+ * pass, and each vertex adds its edges' corrections in edge order. */
+static void cap_jacobi(OracleSolver* s, float dt, int kind) {
+    memcpy(s->snap, s->pos, sizeof(V3) * (size_t)s->V);
+    memcpy(s->snap_prev, s->prev, sizeof(V3) * (size_t)s->V);
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < s->V; ++v) {
+        V3 p = s->snap[v], q = s->snap_prev[v];
+        for (int k = s->sp_off[v]; k < s->sp_off[v + 1]; ++k) {
+            int o = s->sp_other[k], is_j = s->sp_side[k];
+            int i = is_j ? o : v, j = is_j ? v : o;
+            V3 di, dj, pdi, pdj;
+            int oki, okj;
+            if (!cap_edge(s, kind, dt, s->sp_rest[k], s->snap[i], s->snap[j], s->snap_prev[i], s->snap_prev[j], s->w[i], s->w[j],
+                          &di, &pdi, &oki, &dj, &pdj, &okj))
+                continue;
+            if (is_j ? okj : oki) {
+                p = vadd(p, is_j ? dj : di);
+                q = vadd(q, is_j ? pdj : pdi);
+            }
+        }
+        s->pos[v] = p;
+        s->prev[v] = q;
+    }
+}
+
 static void caps(OracleSolver* s, float dt, int kind, int passes, int both) {
     for (int p = 0; p < passes; ++p) {
+        if (s->cap_jacobi) {
+            cap_jacobi(s, dt, kind);
+            continue;
+        }
         for (int k = 0; k < s->n_cap_colors; ++k) cap_range(s, s->cap_colors[k], s->cap_colors[k + 1] - s->cap_colors[k], dt, kind);
         if (both)
             for (int k = s->n_cap_colors - 1; k >= 0; --k) cap_range(s, s->cap_colors[k], s->cap_colors[k + 1] - s->cap_colors[k], dt, kind);
@@ -1843,7 +1892,7 @@ void oracle_destroy(OracleSolver* s) {
                  s->bend_rest, s->bend_colors, s->tris, s->edges, s->pin_w, s->pin_t, s->pin_relax, s->sdf, s->stris,
                  s->vcell, s->vb_start, s->vb_ent, s->tb_start, s->tb_ent, s->eb_start, s->eb_ent, s->nb_count, s->nb_idx, s->acc,
                  s->diag, s->pinv, s->r, s->z, s->d, s->q, s->off, s->avg_sum, s->avg_cnt, s->cap_edges, s->cap_rest, s->cap_colors,
-                 s->vt_off, s->vt_tri, s->p_area, s->p_rest};
+                 s->snap_prev, s->vt_off, s->vt_tri, s->p_area, s->p_rest};
     for (size_t k = 0; k < sizeof(p) / sizeof(p[0]); ++k) free(p[k]);
     odyn_free(&s->own);
     free(s);
@@ -2016,30 +2065,9 @@ OracleSolver* oracle_create(const SsblXpbdConfig* config, const SsblXpbdMesh* me
             memcpy(s->cap_colors, mesh->edge_color_offsets, sizeof(int) * (size_t)(s->n_cap_colors + 1));
             memcpy(s->cap_edges, sp, sizeof(int) * 2 * (size_t)E); memcpy(s->cap_rest, spr, sizeof(float) * (size_t)E);
         } else {
-            /* greedy first-fit colouring in edge order, stable grouping */
-            int* color = (int*)calloc((size_t)E + 1, sizeof(int));
-            int ncol = 0;
-            unsigned char* used = (unsigned char*)calloc(nv * 64, 1);
-            for (int e = 0; e < E; ++e) {
-                int a = sp[2 * e], b = sp[2 * e + 1], k = 0;
-                while (k < 64 && ((a < V && used[(size_t)a * 64 + k]) || (b < V && used[(size_t)b * 64 + k]))) ++k;
-                color[e] = k;
-                if (a < V && k < 64) used[(size_t)a * 64 + k] = 1;
-                if (b < V && k < 64) used[(size_t)b * 64 + k] = 1;
-                if (k + 1 > ncol) ncol = k + 1;
-            }
-            free(used);
-            s->n_cap_colors = ncol;
-            s->cap_colors = (int*)calloc((size_t)ncol + 1, sizeof(int));
-            for (int e = 0; e < E; ++e) s->cap_colors[color[e] + 1]++;
-            for (int k = 0; k < ncol; ++k) s->cap_colors[k + 1] += s->cap_colors[k];
-            int* cur = (int*)malloc(sizeof(int) * (size_t)(ncol + 1));
-            memcpy(cur, s->cap_colors, sizeof(int) * (size_t)(ncol + 1));
-            for (int e = 0; e < E; ++e) {
-                int at = cur[color[e]]++;
-                s->cap_edges[2 * at] = sp[2 * e]; s->cap_edges[2 * at + 1] = sp[2 * e + 1]; s->cap_rest[at] = spr[e];
-            }
-            free(cur); free(color);
+            /* no colouring: each cap pass is one Jacobi pass over all edges */
+            s->cap_jacobi = 1;
+            s->snap_prev = (V3*)xcalloc(nv, sizeof(V3));
         }
     }
     free(sp); free(spr);

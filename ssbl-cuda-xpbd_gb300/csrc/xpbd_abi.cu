@@ -415,6 +415,24 @@ XG_EXPORT int xpbd_gb300_set_graph_capture(void* handle, int enabled) {
     return 1;
 }
 
+XG_EXPORT int xpbd_gb300_set_key_division(void* handle, int mode) {
+    g_error.clear();
+    Solver* S = as_solver(handle);
+    if (!S) return fail("invalid solver handle") ? 1 : 0;
+    if (mode != 0 && mode != 1) return fail("key division mode must be 0 (reference) or 1 (IEEE)") ? 1 : 0;
+    S->key_ieee = mode;
+    for (Params& P : S->hp) P.key_ieee = mode;
+    S->params_dirty = true;
+    return 1;
+}
+
+XG_EXPORT int xpbd_gb300_set_default_key_division(int mode) {
+    g_error.clear();
+    if (mode != 0 && mode != 1) return fail("key division mode must be 0 (reference) or 1 (IEEE)") ? 1 : 0;
+    g_default_key_ieee.store(mode);
+    return 1;
+}
+
 XG_EXPORT long long xpbd_gb300_last_step_launches(void* handle) {
     Solver* S = as_solver(handle);
     return S ? S->last_launches : -1;

@@ -717,6 +717,23 @@ XG_EXPORT int xpbd_gb300_diff_backward(void* handle, const float* grad_positions
                : 0;
 }
 
+// Copy the state at the start of frame `frame` of the last rollout (frame =
+// frames: its final state): positions, previous positions and velocities as
+// 3 x V float4 rows into `out_rows` (device array of 12 V floats).
+XG_EXPORT int xpbd_gb300_diff_checkpoint(void* handle, int frame, float* out_rows) {
+    g_error.clear();
+    DiffSolver* D = as_diff(handle);
+    if (!D || D->frames < 1 || frame < 0 || frame > D->frames || !out_rows)
+        return fail("invalid checkpoint request (run a rollout first; frame in [0, frames])") ? 1 : 0;
+    const size_t n = 3 * (size_t)D->V;
+    return (cuda_ok(cudaMemcpyAsync(out_rows, D->ck + (size_t)frame * n, sizeof(float4) * n, cudaMemcpyDeviceToDevice,
+                                    D->stream),
+                    "copy checkpoint") &&
+            cuda_ok(cudaStreamSynchronize(D->stream), "copy checkpoint"))
+               ? 1
+               : 0;
+}
+
 XG_EXPORT void* xpbd_gb300_diff_stream(void* handle) {
     DiffSolver* D = as_diff(handle);
     return D ? reinterpret_cast<void*>(D->stream) : nullptr;

@@ -38,8 +38,8 @@ constexpr float kNeighborImpulse = 0.5f;
 // Per triangle: bounds, centre, radius and (hashed meshes) the cell span of
 // the bounds grown by the collision margin; an invalid span collapses to
 // the centre's cell (abi41.cu:3686-3760).
-__global__ void k_dyn_bounds(const float4* tris, int T, float cell, float margin, bool spans, float4* amin, float4* amax,
-                             float4* center, float* radius, int4* cmin, int4* cmax) {
+__global__ void k_dyn_bounds(const float4* tris, int T, float cell, float margin, bool spans, int ieee, float4* amin,
+                             float4* amax, float4* center, float* radius, int4* cmin, int4* cmax) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
     const F3 a = f3(tris[3 * t]), b = f3(tris[3 * t + 1]), c = f3(tris[3 * t + 2]);
@@ -54,13 +54,13 @@ __global__ void k_dyn_bounds(const float4* tris, int T, float cell, float margin
     radius[t] = r;
     if (!spans) return;
     const float cs = fmaxf(cell, 1.0e-3f);
-    int x0 = cell_of(lo.x - margin, cs), y0 = cell_of(lo.y - margin, cs), z0 = cell_of(lo.z - margin, cs);
-    int x1 = cell_of(hi.x + margin, cs), y1 = cell_of(hi.y + margin, cs), z1 = cell_of(hi.z + margin, cs);
+    int x0 = cell_of(lo.x - margin, cs, ieee), y0 = cell_of(lo.y - margin, cs, ieee), z0 = cell_of(lo.z - margin, cs, ieee);
+    int x1 = cell_of(hi.x + margin, cs, ieee), y1 = cell_of(hi.y + margin, cs, ieee), z1 = cell_of(hi.z + margin, cs, ieee);
     const long long sx = (long long)x1 - x0 + 1, sy = (long long)y1 - y0 + 1, sz = (long long)z1 - z0 + 1;
     if (!(sx > 0 && sy > 0 && sz > 0)) {
-        x0 = x1 = cell_of(ce.x, cs);
-        y0 = y1 = cell_of(ce.y, cs);
-        z0 = z1 = cell_of(ce.z, cs);
+        x0 = x1 = cell_of(ce.x, cs, ieee);
+        y0 = y1 = cell_of(ce.y, cs, ieee);
+        z0 = z1 = cell_of(ce.z, cs, ieee);
     }
     cmin[t] = make_int4(x0, y0, z0, 0);
     cmax[t] = make_int4(x1, y1, z1, 0);
@@ -103,11 +103,12 @@ __global__ void k_dyn_large_list(int T, const int4* cmin, const int4* cmax, cons
 }
 
 // Particle cells and bucket counts / placement.
-__global__ void k_dyn_par_hash(const float4* pos, int n, float cell, int nb, int4* cellc, int* cnt, int* ent, bool scatter) {
+__global__ void k_dyn_par_hash(const float4* pos, int n, float cell, int nb, int ieee, int4* cellc, int* cnt, int* ent,
+                               bool scatter) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = pos[i];
-    const int cx = cell_of(p.x, cell), cy = cell_of(p.y, cell), cz = cell_of(p.z, cell);
+    const int cx = cell_of(p.x, cell, ieee), cy = cell_of(p.y, cell, ieee), cz = cell_of(p.z, cell, ieee);
     int* c = &cnt[bucket_of(cx, cy, cz, nb)];
     if (scatter) {
         ent[atomicAdd(c, 1)] = i;
@@ -321,7 +322,8 @@ __device__ void dyn_triangles(const View& v, const Params& P, const DynSet& D, i
     DynBest b{F3{0.0f, 0.0f, 0.0f}, F3{0.0f, 0.0f, 0.0f}, F3{0.0f, 0.0f, 0.0f}, 0.0f, 3.402823466e+38f, 0.0f};
     unsigned candidates = 0, rejects = 0;
     if (D.tri_hashed) {
-        const int cx = cell_of(p.x, D.tri_cell), cy = cell_of(p.y, D.tri_cell), cz = cell_of(p.z, D.tri_cell);
+        const int cx = cell_of(p.x, D.tri_cell, D.key_ieee), cy = cell_of(p.y, D.tri_cell, D.key_ieee),
+                  cz = cell_of(p.z, D.tri_cell, D.key_ieee);
         int R = 0;
         if (D.signed_mode) {
             if (!inside) {
@@ -410,7 +412,8 @@ __device__ void dyn_particles(const View& v, const Params& P, const DynSet& D, i
         }
     };
     if (D.par_hashed) {
-        const int cx = cell_of(p.x, D.par_cell), cy = cell_of(p.y, D.par_cell), cz = cell_of(p.z, D.par_cell);
+        const int cx = cell_of(p.x, D.par_cell, D.key_ieee), cy = cell_of(p.y, D.par_cell, D.key_ieee),
+                  cz = cell_of(p.z, D.par_cell, D.key_ieee);
         for (int dz = -1; dz <= 1; ++dz)
             for (int dy = -1; dy <= 1; ++dy)
                 for (int dx = -1; dx <= 1; ++dx) {
@@ -480,11 +483,13 @@ struct DynCtx {
     long long* bytes;
     float margin;
     float thickness;
+    int key_ieee;  // cell-key division of the hashes built
 };
 
 DynCtx cloth_ctx(Solver* S, int k) {
     const SsblXpbdConfig& c = S->cl[k].cfg;
-    return DynCtx{S->stream, &S->device_bytes, std::max(c.collision_margin, 0.0f), std::max(c.cloth_thickness, 0.0f)};
+    return DynCtx{S->stream, &S->device_bytes, std::max(c.collision_margin, 0.0f), std::max(c.cloth_thickness, 0.0f),
+                  S->key_ieee};
 }
 
 // (Re)allocate a device array of at least n elements; the old contents are
@@ -547,12 +552,13 @@ bool finish_triangles(const DynCtx& c, DynHost& D, int T, bool signed_mode, bool
     if (motion_valid &&
         !cuda_ok(cudaMemcpyAsync(D.prev_center, D.center, sizeof(float4) * T, cudaMemcpyDeviceToDevice, st), "keep dynamic centres"))
         return false;
-    k_dyn_bounds<<<dyn_blocks(T), kThreadsDyn, 0, st>>>(D.tris, T, cell, c.margin, hashed, D.amin, D.amax, D.center, D.radius,
-                                                         D.cmin, D.cmax);
+    k_dyn_bounds<<<dyn_blocks(T), kThreadsDyn, 0, st>>>(D.tris, T, cell, c.margin, hashed, c.key_ieee, D.amin, D.amax, D.center,
+                                                         D.radius, D.cmin, D.cmax);
     if (!motion_valid &&
         !cuda_ok(cudaMemcpyAsync(D.prev_center, D.center, sizeof(float4) * T, cudaMemcpyDeviceToDevice, st), "init dynamic centres"))
         return false;
     DynSet& h = D.h;
+    h.key_ieee = c.key_ieee;
     h.tri_count = T;
     h.signed_mode = signed_mode ? 1 : 0;
     h.motion_valid = motion_valid ? 1 : 0;
@@ -687,6 +693,7 @@ bool put_particles(const DynCtx& c, DynHost& D, const float* pos, const float* p
     if (!prev && !motion &&
         !cuda_ok(cudaMemcpyAsync(D.pprev, D.ppos, sizeof(float4) * count, cudaMemcpyDeviceToDevice, st), "init dynamic particle positions"))
         return false;
+    h.key_ieee = c.key_ieee;
     h.par_count = count;
     h.par_motion_valid = motion ? 1 : 0;
     h.par_hashed = count >= kParHashMin ? 1 : 0;
@@ -702,9 +709,11 @@ bool put_particles(const DynCtx& c, DynHost& D, const float* pos, const float* p
             D.pb_cap = nb;
         }
         if (!cuda_ok(cudaMemsetAsync(D.pcount, 0, sizeof(int) * nb, st), "reset dynamic particle hash")) return false;
-        k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, D.pcell, D.pcount, nullptr, false);
+        k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, c.key_ieee, D.pcell, D.pcount,
+                                                                   nullptr, false);
         scan_bucket_counts(D.pcount, D.pstart, nb, D.pscan, st);
-        k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, D.pcell, D.pcount, D.pent, true);
+        k_dyn_par_hash<<<dyn_blocks(count), kThreadsDyn, 0, st>>>(D.ppos, count, h.par_cell, nb, c.key_ieee, D.pcell, D.pcount,
+                                                                   D.pent, true);
         k_dyn_sort_buckets<<<dyn_blocks(nb), kThreadsDyn, 0, st>>>(D.pstart, D.pent, nb);
         if (overflow_out) k_dyn_overflow<<<dyn_blocks(nb), kThreadsDyn, 0, st>>>(D.pstart, nb, overflow_out);
         h.par_buckets = nb;
@@ -852,6 +861,7 @@ bool upload_dynamic_particles(Solver* S, int cloth, const float* pos, const floa
 
 GlobalScene* scene_create() {
     GlobalScene* G = new GlobalScene();
+    G->key_ieee = g_default_key_ieee.load();
     if (!cuda_ok(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking), "global dynamic scene stream")) {
         delete G;
         return nullptr;
@@ -889,7 +899,7 @@ bool scene_update(GlobalScene* G, const SsblXpbdGlobalDynamicSceneInputs* in) {
     G->thickness = std::max(in->cloth_thickness, 0.0f);
     G->hash_overflow = 0;
     AllocAccount account(&G->device_bytes);
-    const DynCtx c{G->stream, &G->device_bytes, G->margin, G->thickness};
+    const DynCtx c{G->stream, &G->device_bytes, G->margin, G->thickness, G->key_ieee};
     DynHost& D = G->dyn;
     if (!G->overflow && !dalloc(&G->overflow, 1, "global dynamic scene counters")) return false;
     if (!cuda_ok(cudaMemsetAsync(G->overflow, 0, sizeof(unsigned long long), c.st), "global dynamic scene counters")) return false;
@@ -949,7 +959,7 @@ bool scene_attach(Solver* S, int cloth, GlobalScene* G, int source_id, int layer
         if (C.gscene && C.gscene != G) C.gscene->attached.erase({S, k});
         if (!G->dyn.dev) {
             AllocAccount account(&G->device_bytes);
-            if (!publish_set(DynCtx{G->stream, &G->device_bytes, G->margin, G->thickness}, G->dyn)) return false;
+            if (!publish_set(DynCtx{G->stream, &G->device_bytes, G->margin, G->thickness, G->key_ieee}, G->dyn)) return false;
         }
         C.gscene = G;
         G->attached.insert({S, k});

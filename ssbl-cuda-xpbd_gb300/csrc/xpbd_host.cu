@@ -22,6 +22,7 @@ namespace host {
 
 thread_local std::string g_error;
 thread_local long long* g_alloc_account = nullptr;
+std::atomic<int> g_default_key_ieee{0};
 
 namespace {
 
@@ -279,33 +280,6 @@ void load_colliders(Params& P, const SsblXpbdRuntimeColliders& c) {
     P.use_sphere = c.use_sphere;
     std::memcpy(P.sphere_center, c.sphere_center, sizeof(P.sphere_center));
     P.sphere_radius = c.sphere_radius;
-}
-
-// Greedy first-fit edge colouring in edge order (used for the hard-stretch
-// caps when the caller gives no colouring).
-void greedy_edge_colors(int V, const std::vector<int2>& springs, std::vector<int>* offsets, std::vector<int>* order) {
-    const int E = (int)springs.size();
-    std::vector<int> color(E, 0);
-    std::vector<std::vector<int>> used(V);
-    int ncol = 0;
-    for (int e = 0; e < E; ++e) {
-        const int a = springs[e].x, b = springs[e].y;
-        int k = 0;
-        auto taken = [&](int v, int col) {
-            return v >= 0 && v < V && std::find(used[v].begin(), used[v].end(), col) != used[v].end();
-        };
-        while (taken(a, k) || taken(b, k)) ++k;
-        color[e] = k;
-        if (a >= 0 && a < V) used[a].push_back(k);
-        if (b >= 0 && b < V) used[b].push_back(k);
-        ncol = std::max(ncol, k + 1);
-    }
-    offsets->assign(ncol + 1, 0);
-    for (int e = 0; e < E; ++e) (*offsets)[color[e] + 1]++;
-    for (int k = 0; k < ncol; ++k) (*offsets)[k + 1] += (*offsets)[k];
-    std::vector<int> cursor(offsets->begin(), offsets->end() - 1);
-    order->assign(E, 0);
-    for (int e = 0; e < E; ++e) (*order)[cursor[color[e]]++] = e;
 }
 
 template <class T>
@@ -923,6 +897,7 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
     Solver* S = new Solver();
     AllocAccount account(&S->device_bytes);
     S->K = K;
+    S->key_ieee = g_default_key_ieee.load();
     S->cl.resize(K);
     S->hp.assign(K, Params{});
     // internal order: grouped by self-collision mode, stable within a group
@@ -1191,6 +1166,7 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
         load_colliders(P, C.colliders);
         const float radius = self_radius(c);
         P.self_radius = radius;
+        P.key_ieee = S->key_ieee;
         P.self_mode = c.self_collision_mode;
         P.max_neighbors = c.max_self_collision_neighbors;
         P.stretch_strength = c.stretch_optimization_strength;
@@ -1294,13 +1270,15 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
                  dalloc(&S->eb_start, S->nEB + 1, "self edge hash start allocation") &&
                  dalloc(&S->eb_ent, (size_t)edge_entries, "self edge hash index allocation");
     }
-    // Hard-stretch buffers (one-cloth solvers); the caps need edges grouped
-    // by colour: the caller's colouring when given (edges already sorted by
-    // colour), else a greedy first-fit colouring in edge order.
-    // In a batch each cloth is coloured on its own and colour c of every
-    // cloth with the hard polish forms cap launch c (cloths share no vertex);
-    // a caller's offsets are clamped to the cloth's edges, which is what the
-    // bounds check of a one-cloth launch does with them.
+    // Hard-stretch buffers.  The caps follow the caller's edge colouring when
+    // one is given (edges already sorted by colour; each pass sweeps the
+    // colours forward then backward, abi41.cu:7769-7793); without one each
+    // pass is a single Jacobi pass over all of the cloth's edges
+    // (abi41.cu:7794-7801), run as a per-vertex gather (P.cap_jacobi).
+    // In a batch colour c of every coloured cloth with the hard polish forms
+    // cap launch c (cloths share no vertex); a caller's offsets are clamped to
+    // the cloth's edges, which is what the bounds check of a one-cloth launch
+    // does with them.
     std::vector<int2> cap_edges;
     std::vector<float> cap_rest;
     std::vector<int> blk_cloth;
@@ -1308,6 +1286,7 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
         S->pcg_nnz = 0;
         S->pcg_blocks = 0;
         S->pcg_hard = false;
+        S->cap_jacobi = false;
         std::vector<std::vector<int>> col_off(K), col_order(K);
         int ncol = 0;
         for (int k = 0; k < K; ++k) {
@@ -1323,20 +1302,17 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
             P.pcg_nblocks = pcg_blocks(P.V);
             S->pcg_blocks += P.pcg_nblocks;
             blk_cloth.insert(blk_cloth.end(), P.pcg_nblocks, k);
+            P.cap_jacobi = 0;
             if (!P.pcg_hard) continue;
             S->pcg_hard = true;
-            if (!S->cl[k].edge_colors.empty()) {
-                col_off[k] = S->cl[k].edge_colors;
-                col_order[k].resize(P.E);
-                for (int e = 0; e < P.E; ++e) col_order[k][e] = e;
-            } else {
-                std::vector<int2> local(P.E);
-                for (int e = 0; e < P.E; ++e) {
-                    const int2 g = springs[P.estart + e];
-                    local[e] = make_int2(g.x >= 0 ? g.x - P.vstart : g.x, g.y >= 0 ? g.y - P.vstart : g.y);
-                }
-                greedy_edge_colors(P.V, local, &col_off[k], &col_order[k]);
+            if (S->cl[k].edge_colors.empty()) {
+                P.cap_jacobi = 1;
+                S->cap_jacobi = true;
+                continue;
             }
+            col_off[k] = S->cl[k].edge_colors;
+            col_order[k].resize(P.E);
+            for (int e = 0; e < P.E; ++e) col_order[k][e] = e;
             ncol = std::max(ncol, (int)col_off[k].size() - 1);
         }
         S->cap_colors.assign(1, 0);
@@ -1631,6 +1607,10 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
         const int ncol = (int)S->cap_colors.size() - 1;
         timed(kKStretchCaps, 0, [&] {
             for (int p = 0; p < passes; ++p) {
+                if (S->cap_jacobi) {
+                    pcg_cap_jacobi(cv, S->pcg, nV, kind, S->stream);
+                    st->launches += 2;
+                }
                 for (int k = 0; k < ncol; ++k) {
                     const int n = S->cap_colors[k + 1] - S->cap_colors[k];
                     if (n > 0) {

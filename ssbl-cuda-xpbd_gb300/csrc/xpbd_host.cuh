@@ -9,6 +9,7 @@
 // substeps / iterations, in one launch sequence captured as one CUDA graph.
 #pragma once
 
+#include <atomic>
 #include <chrono>
 #include <map>
 #include <set>
@@ -29,6 +30,9 @@ extern thread_local std::string g_error;
 // Device bytes of the solver being built or updated on this thread: every
 // successful dalloc adds to it while an AllocAccount is in scope.
 extern thread_local long long* g_alloc_account;
+// Cell-key division given to solvers and shared scenes when they are created
+// (0 the reference's, 1 IEEE; xpbd_math.cuh).
+extern std::atomic<int> g_default_key_ieee;
 
 struct AllocAccount {
     long long* prev;
@@ -182,6 +186,7 @@ struct GlobalScene {
     int tri_meta_cap = 0, par_meta_cap = 0;
     unsigned long long* overflow = nullptr;  // particles past the 16 queried slots of a bucket
     float margin = 0.0f, thickness = 0.0f;
+    int key_ieee = 0;  // cell-key division of the scene's hashes (xpbd_math.cuh)
     long long hash_overflow = 0;
     float upload_ms = 0.0f;
     long long device_bytes = 0;
@@ -216,6 +221,7 @@ struct Cloth {
 
 struct Solver {
     int K = 0;
+    int key_ieee = 0;  // cell-key division (xpbd_math.cuh): 0 the reference's, 1 IEEE
     // Cloths are stored grouped by self-collision mode (none, fast, strict;
     // caller order within a group) so that each mode-specific kernel covers
     // contiguous items.  The batch entry points take the caller's cloth
@@ -304,6 +310,7 @@ struct Solver {
     // hard-stretch optimisation (every cloth that enables it)
     bool pcg_on = false;         // some cloth runs the CG stretch solve
     bool pcg_hard = false;       // some cloth runs the averaged polish and caps
+    bool cap_jacobi = false;     // some such cloth has no edge colouring (Jacobi caps)
     bool spring_any = false;     // some cloth with edges keeps the spring gather
     PcgView pcg{};
     int* pcg_blk = nullptr;      // cloth of each block of the CG grid

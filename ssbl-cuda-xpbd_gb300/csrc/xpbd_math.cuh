@@ -62,8 +62,25 @@ XG_HD F3 limit_delta(F3 delta, float max_len) {
     return len > max_len ? delta * (max_len / len) : delta;
 }
 
-// Grid cell of one coordinate (abi41.cu:654-656), IEEE division.
-XG_HD int cell_of(float value, float cell_size) { return (int)floorf(value / fmaxf(cell_size, kEps)); }
+// Grid cell of one coordinate: floor(value / max(cell, 1e-7)) (abi41.cu:
+// 654-656).  The reference is compiled with --use_fast_math, which makes its
+// float division the approximate, flush-to-zero division of the PTX ISA
+// (div.approx.ftz.f32: at most 2 ulp from the exact quotient); near a cell
+// boundary that quotient can fall on the other side of an integer from the
+// correctly rounded one, so hash keys computed with IEEE division differ
+// from the reference's in rare cases.  `ieee` = 0 (the default of every
+// solver) uses the reference's division, so cells, bucket ids and bucket
+// contents are the reference's integers; `ieee` = 1 uses the correctly
+// rounded quotient, which is what the CPU oracle computes.
+__device__ __forceinline__ float key_quotient(float value, float cell, int ieee) {
+    if (ieee) return __fdiv_rn(value, cell);
+    float q;
+    asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(q) : "f"(value), "f"(cell));
+    return q;
+}
+__device__ __forceinline__ int cell_of(float value, float cell_size, int ieee) {
+    return (int)floorf(key_quotient(value, fmaxf(cell_size, kEps), ieee));
+}
 
 // Spatial-hash bucket of a cell: the three large primes of Teschner et al.,
 // "Optimized Spatial Hashing for Collision Detection of Deformable Objects"

@@ -442,33 +442,29 @@ __global__ void __launch_bounds__(kThreads) k_avg_apply(View v, PcgView g, int t
     v.prev[i] = f4(f3(v.prev[i]) + delta * (tiny ? 0.24f : 0.16f), 0.0f);
 }
 
-// ---------------------------------------------------- colour-range caps --
-// Ratio caps applied in place one edge colour at a time (no two edges of a
-// colour share a vertex): normal (abi41.cu:2249-2362), tiny (2496-2601) and
-// extreme (2603-2708).  In a batch a launch covers one colour of every cloth
-// with the hard polish; the time step is the cloth's substep length.
-__global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int count, int kind) {
-    const int local = blockIdx.x * blockDim.x + threadIdx.x;
-    if (local >= count) return;
-    const int s = start + local;
-    if (s < 0 || s >= v.nE) return;
-    const float rest = __ldg(&v.edge_rest[s]);
+// ------------------------------------------------------------ ratio caps --
+// One edge of a ratio cap: normal (kind 0, abi41.cu:2249-2362), tiny (1,
+// 2496-2601) or extreme (2, 2603-2708).  Writes each endpoint's position
+// correction d and previous-position shift pd; ok = false where that
+// endpoint gets nothing.  Returns false when the edge is skipped.
+struct CapSide {
+    F3 d, pd;
+    bool ok;
+};
+
+__device__ bool cap_edge(const Params& P, int kind, float rest, float4 pi4, float4 pj4, F3 qi, F3 qj, CapSide* si, CapSide* sj) {
+    si->ok = sj->ok = false;
     const bool tiny = kind == 1;
-    if (!isfinite(rest) || rest <= kEps) return;
-    if (tiny ? rest > 7.5e-4f : rest <= 7.5e-4f) return;
-    const int2 ed = __ldg(&v.edges[s]);
-    const int i = ed.x, j = ed.y;
-    if (i < 0 || j < 0 || i >= v.nV || j >= v.nV || i == j) return;
-    const Params& P = params_v(v, i);
+    if (!isfinite(rest) || rest <= kEps) return false;
+    if (tiny ? rest > 7.5e-4f : rest <= 7.5e-4f) return false;
     const float dt = P.sub_dt;
-    const float4 pi4 = v.pos[i], pj4 = v.pos[j];
     const float wi = pi4.w, wj = pj4.w, weight = wi + wj;
-    if (!isfinite(weight) || weight <= 0.0f) return;
-    const F3 pi = f3(pi4), pj = f3(pj4), qi = f3(v.prev[i]), qj = f3(v.prev[j]);
-    if (!finite3(pi) || !finite3(pj) || !finite3(qi) || !finite3(qj)) return;
+    if (!isfinite(weight) || weight <= 0.0f) return false;
+    const F3 pi = f3(pi4), pj = f3(pj4);
+    if (!finite3(pi) || !finite3(pj) || !finite3(qi) || !finite3(qj)) return false;
     const F3 edge = pj - pi;
     const float len_sq = dot3(edge, edge);
-    if (!isfinite(len_sq) || len_sq <= 1.0e-14f) return;
+    if (!isfinite(len_sq) || len_sq <= 1.0e-14f) return false;
     const float len = sqrtf(len_sq);
     const bool high = P.stretch_strength >= 0.95f;
     float start_ratio, target_ratio, max_delta, prev_sync;
@@ -488,11 +484,11 @@ __global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int c
         max_delta = fminf(fmaxf(rest * 1.25f, P.thickness * 0.10f), 0.006f);
         prev_sync = 0.30f;
     }
-    if (!isfinite(len) || len <= rest * start_ratio) return;
+    if (!isfinite(len) || len <= rest * start_ratio) return false;
     const float excess = len - rest * target_ratio;
-    if (!isfinite(excess) || excess <= 0.0f) return;
+    if (!isfinite(excess) || excess <= 0.0f) return false;
     const F3 corr = edge * (-excess / fmaxf(weight * len, kEps));
-    if (!finite3(corr) || len3(corr) <= 1.0e-20f) return;
+    if (!finite3(corr) || len3(corr) <= 1.0e-20f) return false;
     F3 pdi{0.0f, 0.0f, 0.0f}, pdj{0.0f, 0.0f, 0.0f};
     const F3 normal = edge * (1.0f / fmaxf(len, kEps));
     const float sdt = kind == 0 ? fmaxf(dt, kEps) : dt;
@@ -508,20 +504,83 @@ __global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int c
     }
     if (wi > 0.0f) {
         const F3 d = limit_delta(corr * (-wi), max_delta);
-        if (finite3(d) && len3(d) > 0.0f) {
-            pdi = pdi + d * prev_sync;
-            v.pos[i] = f4(pi + d, wi);
-            v.prev[i] = f4(qi + pdi, 0.0f);
-        }
+        if (finite3(d) && len3(d) > 0.0f) *si = CapSide{d, pdi + d * prev_sync, true};
     }
     if (wj > 0.0f) {
         const F3 d = limit_delta(corr * wj, max_delta);
-        if (finite3(d) && len3(d) > 0.0f) {
-            pdj = pdj + d * prev_sync;
-            v.pos[j] = f4(pj + d, wj);
-            v.prev[j] = f4(qj + pdj, 0.0f);
+        if (finite3(d) && len3(d) > 0.0f) *sj = CapSide{d, pdj + d * prev_sync, true};
+    }
+    return true;
+}
+
+// Caps applied in place one edge colour at a time (no two edges of a colour
+// share a vertex), over a caller's edge colouring.  In a batch a launch
+// covers one colour of every cloth that uses its colouring; the time step is
+// the cloth's substep length.
+__global__ void __launch_bounds__(kThreads) k_cap_range(View v, int start, int count, int kind) {
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= count) return;
+    const int s = start + local;
+    if (s < 0 || s >= v.nE) return;
+    const int2 ed = __ldg(&v.edges[s]);
+    const int i = ed.x, j = ed.y;
+    if (i < 0 || j < 0 || i >= v.nV || j >= v.nV || i == j) return;
+    const Params& P = params_v(v, i);
+    const float4 pi4 = v.pos[i], pj4 = v.pos[j];
+    const F3 qi = f3(v.prev[i]), qj = f3(v.prev[j]);
+    CapSide si, sj;
+    if (!cap_edge(P, kind, __ldg(&v.edge_rest[s]), pi4, pj4, qi, qj, &si, &sj)) return;
+    if (si.ok) {
+        v.pos[i] = f4(f3(pi4) + si.d, pi4.w);
+        v.prev[i] = f4(qi + si.pd, 0.0f);
+    }
+    if (sj.ok) {
+        v.pos[j] = f4(f3(pj4) + sj.d, pj4.w);
+        v.prev[j] = f4(qj + sj.pd, 0.0f);
+    }
+}
+
+// Caps of a cloth without a caller's colouring: the reference launches one
+// kernel over every edge, each adding its corrections to both endpoints with
+// float atomics (abi41.cu:7794-7801), i.e. a Jacobi pass.  Here every edge
+// sees the positions and previous positions at the start of the pass and
+// each vertex adds its edges' corrections in edge order (vertex -> edge CSR)
+// into pos_out / prev_out; k_cap_store copies them back.
+__global__ void __launch_bounds__(kThreads) k_cap_jacobi(View v, int kind, float4* pos_out, float4* prev_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.pcg_hard || !P.cap_jacobi) return;
+    const float4 self4 = v.pos[i];
+    const F3 self_prev = f3(v.prev[i]);
+    F3 p = f3(self4), q = self_prev;
+    for (int k = v.sp_off[i]; k < v.sp_off[i + 1]; ++k) {
+        const int2 e = __ldg(&v.sp_ent[k]);
+        const bool self_is_j = (e.x & kSideBit) != 0;
+        const int o = e.x & 0x7fffffff;
+        const float4 o4 = v.pos[o];
+        const F3 oq = f3(v.prev[o]);
+        CapSide si, sj;
+        if (!cap_edge(P, kind, __int_as_float(e.y), self_is_j ? o4 : self4, self_is_j ? self4 : o4, self_is_j ? oq : self_prev,
+                      self_is_j ? self_prev : oq, &si, &sj))
+            continue;
+        const CapSide& me = self_is_j ? sj : si;
+        if (me.ok) {
+            p = p + me.d;
+            q = q + me.pd;
         }
     }
+    pos_out[i] = f4(p, self4.w);
+    prev_out[i] = f4(q, 0.0f);
+}
+
+__global__ void __launch_bounds__(kThreads) k_cap_store(View v, const float4* pos_in, const float4* prev_in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nV) return;
+    const Params& P = params_v(v, i);
+    if (!P.pcg_hard || !P.cap_jacobi) return;
+    v.pos[i] = pos_in[i];
+    v.prev[i] = prev_in[i];
 }
 
 }  // namespace
@@ -552,6 +611,12 @@ void pcg_averaged_pass(const View& v, const PcgView& g, int V, bool tiny, cudaSt
 
 void pcg_cap_range(const View& v, int start, int count, int kind, cudaStream_t s) {
     if (count > 0) k_cap_range<<<blocks_for(count), kThreads, 0, s>>>(v, start, count, kind);
+}
+
+void pcg_cap_jacobi(const View& v, const PcgView& g, int V, int kind, cudaStream_t s) {
+    if (V <= 0) return;
+    k_cap_jacobi<<<blocks_for(V), kThreads, 0, s>>>(v, kind, g.r, g.z);
+    k_cap_store<<<blocks_for(V), kThreads, 0, s>>>(v, g.r, g.z);
 }
 
 }  // namespace xg

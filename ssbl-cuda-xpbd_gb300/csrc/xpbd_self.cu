@@ -41,9 +41,9 @@ __device__ __forceinline__ void accumulate(const View& v, int i, F3 d) {
 // Fast-mode per-thread filters (abi41.cu:714-832).
 __device__ int normal_bucket(float v) { return v > 0.45f ? 2 : (v < -0.45f ? 0 : 1); }
 
-__device__ unsigned cluster_key(int pair_type, F3 point, F3 normal, float cell) {
+__device__ unsigned cluster_key(int pair_type, F3 point, F3 normal, float cell, int ieee) {
     const float c = fmaxf(cell, 1.0e-3f);
-    unsigned key = bucket_of(cell_of(point.x, c), cell_of(point.y, c), cell_of(point.z, c), 1 << 20);
+    unsigned key = bucket_of(cell_of(point.x, c, ieee), cell_of(point.y, c, ieee), cell_of(point.z, c, ieee), 1 << 20);
     const unsigned nk = (unsigned)normal_bucket(normal.x) | ((unsigned)normal_bucket(normal.y) << 2) |
                         ((unsigned)normal_bucket(normal.z) << 4);
     key ^= nk * 2654435761u;
@@ -128,13 +128,13 @@ struct CellRange {
 };
 
 // *collapsed is set when the range collapsed (the caller counts it).
-__device__ CellRange primitive_cells(F3 lo, F3 hi, F3 fallback, float cell, bool* collapsed) {
-    CellRange r{cell_of(lo.x, cell), cell_of(hi.x, cell), cell_of(lo.y, cell),
-                cell_of(hi.y, cell), cell_of(lo.z, cell), cell_of(hi.z, cell)};
+__device__ CellRange primitive_cells(F3 lo, F3 hi, F3 fallback, float cell, int ieee, bool* collapsed) {
+    CellRange r{cell_of(lo.x, cell, ieee), cell_of(hi.x, cell, ieee), cell_of(lo.y, cell, ieee),
+                cell_of(hi.y, cell, ieee), cell_of(lo.z, cell, ieee), cell_of(hi.z, cell, ieee)};
     const long long sx = (long long)r.x1 - r.x0 + 1, sy = (long long)r.y1 - r.y0 + 1, sz = (long long)r.z1 - r.z0 + 1;
     if (sx <= 0 || sy <= 0 || sz <= 0) return r;
     if (sx * sy * sz <= (long long)kMaxPrimitiveCells) return r;
-    const int fx = cell_of(fallback.x, cell), fy = cell_of(fallback.y, cell), fz = cell_of(fallback.z, cell);
+    const int fx = cell_of(fallback.x, cell, ieee), fy = cell_of(fallback.y, cell, ieee), fz = cell_of(fallback.z, cell, ieee);
     *collapsed = true;
     return CellRange{fx, fx, fy, fy, fz, fz};
 }
@@ -154,7 +154,7 @@ __device__ CellRange tri_cells(const View& v, const Params& P, int t, bool* ok, 
     const F3 lo{fminf(a.x, fminf(b.x, c.x)) - m, fminf(a.y, fminf(b.y, c.y)) - m, fminf(a.z, fminf(b.z, c.z)) - m};
     const F3 hi{fmaxf(a.x, fmaxf(b.x, c.x)) + m, fmaxf(a.y, fmaxf(b.y, c.y)) + m, fmaxf(a.z, fmaxf(b.z, c.z)) + m};
     const F3 centroid = ((a + b) + c) * (1.0f / 3.0f);
-    return primitive_cells(lo, hi, centroid, P.tcell, collapsed);
+    return primitive_cells(lo, hi, centroid, P.tcell, P.key_ieee, collapsed);
 }
 
 __device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok, bool* collapsed) {
@@ -166,7 +166,7 @@ __device__ CellRange edge_cells(const View& v, const Params& P, int e, bool* ok,
     const F3 lo{fminf(a.x, b.x) - m, fminf(a.y, b.y) - m, fminf(a.z, b.z) - m};
     const F3 hi{fmaxf(a.x, b.x) + m, fmaxf(a.y, b.y) + m, fmaxf(a.z, b.z) + m};
     const F3 mid = (a + b) * 0.5f;
-    return primitive_cells(lo, hi, mid, P.ecell, collapsed);
+    return primitive_cells(lo, hi, mid, P.ecell, P.key_ieee, collapsed);
 }
 
 __global__ void k_vhash_count(View v) {
@@ -175,7 +175,7 @@ __global__ void k_vhash_count(View v) {
     const Params& P = params_v(v, i);
     if (!P.vhash || !self_scheduled(P, v)) return;
     const float4 p = v.pos[i];
-    const int cx = cell_of(p.x, P.vcell), cy = cell_of(p.y, P.vcell), cz = cell_of(p.z, P.vcell);
+    const int cx = cell_of(p.x, P.vcell, P.key_ieee), cy = cell_of(p.y, P.vcell, P.key_ieee), cz = cell_of(p.z, P.vcell, P.key_ieee);
     const int b = P.vbase + (int)bucket_of(cx, cy, cz, P.vbuckets);
     v.vcell[i] = make_int4(cx, cy, cz, b);
     atomicAdd(&v.vb_count[b], 1);  // overflow past 32 slots is counted from the totals in the scan
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_vv(View v) {
             if (fast) {
                 const F3 nrm = resp * (1.0f / fmaxf(len3(resp), kEps));
                 const F3 mid = (pc + qc) * 0.5f;
-                const unsigned key = cluster_key(0, mid, nrm, fmaxf(th * 2.5f, 1.0e-3f));
+                const unsigned key = cluster_key(0, mid, nrm, fmaxf(th * 2.5f, 1.0e-3f), P.key_ieee);
                 if (!try_local_accept(v, P, 0, key, &cl)) continue;
                 count1(v.counts, kCntSelfCandidates);
             }
@@ -683,7 +683,7 @@ __device__ bool vt_pair(const View& v, const Params& P, int vertex, int tri, flo
         dist = 0.0f;
     }
     if (fast_mode(P)) {
-        const unsigned key = cluster_key(1, q, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+        const unsigned key = cluster_key(1, q, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f), P.key_ieee);
         if (!try_local_accept(v, P, 1, key, cl)) return true;
     }
     count1(v.counts, kCntSelfCandidates);
@@ -732,7 +732,7 @@ __global__ void __launch_bounds__(kThreads) k_vt_hash(View v) {
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const int budget = neighbor_budget(P);
     const float4 p = v.pos[vertex];
-    const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
+    const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell, P.key_ieee), cell_of(p.y, P.tcell, P.key_ieee), cell_of(p.z, P.tcell, P.key_ieee), P.tbuckets);
     const int s = v.tb_start[b];
     const int lim = min(v.tb_start[b + 1] - s, kBucketSlots);
     int accepted = 0;
@@ -820,7 +820,7 @@ __device__ bool ee_pair(const View& v, const Params& P, int ia, int ib, float ta
         dist = 0.0f;
     }
     if (fast_mode(P)) {
-        const unsigned key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+        const unsigned key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f), P.key_ieee);
         if (!try_local_accept(v, P, 2, key, cl)) return true;
     }
     count1(v.counts, kCntSelfCandidates);
@@ -1037,9 +1037,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_neighbors_group(View v, int mod
     int cx = 0, cy = 0, cz = 0;
     if (run) {
         const float4 p = v.pos[src];
-        cx = cell_of(p.x, P->vcell);
-        cy = cell_of(p.y, P->vcell);
-        cz = cell_of(p.z, P->vcell);
+        cx = cell_of(p.x, P->vcell, P->key_ieee);
+        cy = cell_of(p.y, P->vcell, P->key_ieee);
+        cz = cell_of(p.z, P->vcell, P->key_ieee);
     }
     int total = 0;  // neighbours of the earlier rounds (the same in the vertex's lanes)
     for (int c0 = 0; c0 < 27; c0 += G) {
@@ -1311,7 +1311,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const float4 p = v.pos[vertex];
-    const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell), cell_of(p.y, P.tcell), cell_of(p.z, P.tcell), P.tbuckets);
+    const int b = P.tbase + (int)bucket_of(cell_of(p.x, P.tcell, P.key_ieee), cell_of(p.y, P.tcell, P.key_ieee), cell_of(p.z, P.tcell, P.key_ieee), P.tbuckets);
     const int st = v.tb_start[b];
     const int lim = min(v.tb_start[b + 1] - st, kBucketSlots);
     const int budget = neighbor_budget(P);
@@ -1344,7 +1344,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     if (target <= 0.0f) return;
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
-    const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell), cell_of(mid.y, P.ecell), cell_of(mid.z, P.ecell), P.ebuckets);
+    const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell, P.key_ieee), cell_of(mid.y, P.ecell, P.key_ieee), cell_of(mid.z, P.ecell, P.key_ieee), P.ebuckets);
     const int st = v.eb_start[b];
     const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     const int budget = neighbor_budget(P);
@@ -1394,7 +1394,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
             onset = fmaxf(target * 1.8f, target + kEps);
             const float cell = kEdge ? P.ecell : P.tcell;
             const int b = (kEdge ? P.ebase : P.tbase) +
-                          (int)bucket_of(cell_of(q.x, cell), cell_of(q.y, cell), cell_of(q.z, cell), kEdge ? P.ebuckets : P.tbuckets);
+                          (int)bucket_of(cell_of(q.x, cell, P.key_ieee), cell_of(q.y, cell, P.key_ieee), cell_of(q.z, cell, P.key_ieee), kEdge ? P.ebuckets : P.tbuckets);
             const int* start = kEdge ? v.eb_start : v.tb_start;
             st = start[b];
             lim = min(start[b + 1] - st, kBucketSlots);
@@ -1456,7 +1456,8 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
 // candidate: *key is its cluster key, *out its push).
 // kPush = false stops at the class and key (the push is left unset).
 template <bool kPush = true>
-__device__ int ee_fast_classify(const View& v, int ia, int ib, float target, float onset, SoftPush* out, unsigned* key) {
+__device__ int ee_fast_classify(const View& v, int ia, int ib, float target, float onset, int ieee, SoftPush* out,
+                                unsigned* key) {
     if (ib <= ia || ia < 0 || ib < 0 || ia >= v.nE || ib >= v.nE || target <= 0.0f || onset <= target) return 0;
     const int2 ea = __ldg(&v.edges[ia]), eb = __ldg(&v.edges[ib]);
     if (!edge_valid(v.nV, ea) || !edge_valid(v.nV, eb)) return 0;
@@ -1490,7 +1491,7 @@ __device__ int ee_fast_classify(const View& v, int ia, int ib, float target, flo
         }
         dist = 0.0f;
     }
-    *key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f));
+    *key = cluster_key(2, (pa + pb) * 0.5f, F3{0.0f, 0.0f, 0.0f}, fmaxf(onset * 12.0f, 1.0e-3f), ieee);
     if (!kPush) return 3;
     const float pen = target - dist;
     float push;
@@ -1559,7 +1560,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         budget = neighbor_budget(*P);
         const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
         const int b =
-            P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell), cell_of(mid.y, P->ecell), cell_of(mid.z, P->ecell), P->ebuckets);
+            P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell, P->key_ieee), cell_of(mid.y, P->ecell, P->key_ieee), cell_of(mid.z, P->ecell, P->key_ieee), P->ebuckets);
         st = v.eb_start[b];
         lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     }
@@ -1583,6 +1584,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         const int o_st = __shfl_sync(0xffffffffu, st, j);
         const int o_excl = __shfl_sync(0xffffffffu, excl, j);
         const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
+        const int o_ieee = __shfl_sync(0xffffffffu, run ? P->key_ieee : 0, j);
         if (w < total) {
             const int slot = w - o_excl;
             const int id = v.eb_ent[o_st + slot];
@@ -1590,7 +1592,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
             SoftPush sp;
             sp.apply = false;
             unsigned key = 0u;
-            const int cls = dup ? 4 : ee_fast_classify<false>(v, o_item, id, o_target, o_onset, &sp, &key);
+            const int cls = dup ? 4 : ee_fast_classify<false>(v, o_item, id, o_target, o_onset, o_ieee, &sp, &key);
             cls_w[j * kBucketSlots + slot] = (unsigned char)cls;
             key_w[j * kBucketSlots + slot] = key;
         }
@@ -1627,7 +1629,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
             SoftPush sp;
             sp.apply = false;
             unsigned k2 = 0u;
-            ee_fast_classify(v, e, v.eb_ent[st + slot], target, onset, &sp, &k2);
+            ee_fast_classify(v, e, v.eb_ent[st + slot], target, onset, P->key_ieee, &sp, &k2);
             if (sp.apply) {
                 ++c_contact;
                 for (int k = 0; k < 4; ++k) {
@@ -1697,7 +1699,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
         budget = neighbor_budget(*P);
         const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
         const int b =
-            P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell), cell_of(mid.y, P->ecell), cell_of(mid.z, P->ecell), P->ebuckets);
+            P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell, P->key_ieee), cell_of(mid.y, P->ecell, P->key_ieee), cell_of(mid.z, P->ecell, P->key_ieee), P->ebuckets);
         st = v.eb_start[b];
         lim = min(v.eb_start[b + 1] - st, kBucketSlots);
     }
@@ -1716,7 +1718,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
             SoftPush sp;
             sp.apply = false;
             unsigned key = 0u;
-            const int cls = (valid && !dup) ? ee_fast_classify(v, e, id, target, onset, &sp, &key) : 0;
+            const int cls = (valid && !dup) ? ee_fast_classify(v, e, id, target, onset, P->key_ieee, &sp, &key) : 0;
             const unsigned pass_mask = (__ballot_sync(gm, cls == 3) >> gbase) & 0xffu;
             const int remaining = budget - accepted;
             const int cut = __popc(pass_mask) >= remaining ? nth_set_bit(pass_mask, remaining - 1) : kQueryLanes;
@@ -1912,9 +1914,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_island(View v) {
         const int maxn = P->max_neighbors < 1 ? 1 : P->max_neighbors;
         max_contacts = min(max(maxn * 2, 3), 48);
         scan_limit = max_contacts * 10;
-        cx = cell_of(p.x, P->tcell);
-        cy = cell_of(p.y, P->tcell);
-        cz = cell_of(p.z, P->tcell);
+        cx = cell_of(p.x, P->tcell, P->key_ieee);
+        cy = cell_of(p.y, P->tcell, P->key_ieee);
+        cz = cell_of(p.z, P->tcell, P->key_ieee);
     }
     int contacts = 0, scanned = 0;
     int held[kHeld];

@@ -120,6 +120,7 @@ struct DynSet {
     const int* tri_layer;
     const int* par_src;
     const int* par_layer;
+    int key_ieee;         // cell-key division of both hashes (xpbd_math.cuh)
 };
 
 // Parameters of one cloth.  A solver holds one or more cloths concatenated
@@ -170,11 +171,13 @@ struct Params {
     int vbuckets, tbuckets, ebuckets;  // this cloth's table sizes
     int vbase, tbase, ebase;           // offsets of its tables in the shared bucket arrays
     int vhash, thash, ehash;           // hash in use (else brute force)
+    int key_ieee;                      // cell-key division: 0 the reference's, 1 IEEE (xpbd_math.cuh)
     float stretch_strength;            // clamp01(stretch_optimization_strength)
     // hard-stretch optimisation: this cloth runs the CG stretch solve in
     // place of the spring gather (and, at strength >= 0.95, the averaged
     // polish and ratio caps); its CG blocks are [pcg_block0, + pcg_nblocks)
     int pcg_on, pcg_hard, pcg_block0, pcg_nblocks;
+    int cap_jacobi;  // no caller edge colouring: each cap pass is one Jacobi pass over the cloth's edges
     // external accelerations of the prediction (force fields, volume pressure)
     const SsblXpbdForceField* fields;  // field_count records (device)
     int field_count;
@@ -344,6 +347,7 @@ void pcg_averaged_pass(const View& v, const PcgView& g, int V, bool tiny, cudaSt
 // kind: 0 normal cap, 1 tiny cap, 2 extreme cap; over the colour-sorted cap
 // edges [start, start + count) (v.edges / v.edge_rest / v.nE point at them)
 void pcg_cap_range(const View& v, int start, int count, int kind, cudaStream_t s);
+void pcg_cap_jacobi(const View& v, const PcgView& g, int V, int kind, cudaStream_t s);
 void launch_predict(const View& v, int V, cudaStream_t s);
 // pass flags for launch_vertex_pass
 enum PassFlags : unsigned {

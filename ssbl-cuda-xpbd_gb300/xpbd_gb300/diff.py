@@ -37,6 +37,8 @@ def _lib():
         lib.xpbd_gb300_diff_rollout.restype = ctypes.c_int
         lib.xpbd_gb300_diff_backward.argtypes = [_VP, _VP, _VP, _VP]
         lib.xpbd_gb300_diff_backward.restype = ctypes.c_int
+        lib.xpbd_gb300_diff_checkpoint.argtypes = [_VP, ctypes.c_int, _VP]
+        lib.xpbd_gb300_diff_checkpoint.restype = ctypes.c_int
         lib._diff_bound = True
     return lib
 
@@ -105,6 +107,18 @@ class DiffCloth:
         if not ok:
             raise NativeSolverError(_last_error(self._lib))
         return gs, gb
+
+    def checkpoint(self, frame: int):
+        """State at the start of `frame` of the last rollout (frame = frames:
+        the final state): a (3, V, 4) CUDA tensor of positions, previous
+        positions and velocities (xyz + a fourth lane)."""
+        import torch
+
+        out = torch.empty((3, self.vertex_count, 4), dtype=torch.float32, device="cuda")
+        torch.cuda.current_stream().synchronize()
+        if not self._lib.xpbd_gb300_diff_checkpoint(self._handle, int(frame), out.data_ptr()):
+            raise NativeSolverError(_last_error(self._lib))
+        return out
 
 
 def _autograd_function():

@@ -167,7 +167,7 @@ class NativeDiagnostics(ctypes.Structure):
 
 
 # ------------------------------------------------------------ loading ----
-_LIB = None
+_LIBS: dict = {}
 
 
 def dll_path() -> str:
@@ -180,11 +180,13 @@ def dll_path() -> str:
     return library_path()
 
 
-def _load_library():
-    global _LIB
-    if _LIB is not None:
-        return _LIB
-    path = dll_path()
+def _load_library(path: str | None = None):
+    """Load (once per path) an ABI41 library: this repository's by default,
+    or any drop-in of the same interface given by `path` (the parity tests
+    load the reference's solver beside it)."""
+    path = path or dll_path()
+    if path in _LIBS:
+        return _LIBS[path]
     if not os.path.exists(path):
         raise NativeBackendUnavailable(f"Missing GB300 XPBD library: {path} (run the package build first)")
     try:
@@ -217,6 +219,8 @@ def _load_library():
         "xpbd_gb300_read_buffer": (ctypes.c_longlong, [vp, ctypes.c_int, vp, ctypes.c_longlong]),
         "xpbd_gb300_hash_info": (ctypes.c_int, [vp, _PI]),
         "xpbd_gb300_set_graph_capture": (ctypes.c_int, [vp, ctypes.c_int]),
+        "xpbd_gb300_set_key_division": (ctypes.c_int, [vp, ctypes.c_int]),
+        "xpbd_gb300_set_default_key_division": (ctypes.c_int, [ctypes.c_int]),
         "xpbd_gb300_last_step_launches": (ctypes.c_longlong, [vp]),
         "xpbd_gb300_synchronize": (ctypes.c_int, [vp]),
         "xpbd_gb300_stream": (vp, [vp]),
@@ -249,7 +253,7 @@ def _load_library():
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-    _LIB = lib
+    _LIBS[path] = lib
     return lib
 
 
@@ -266,8 +270,21 @@ def _last_error(lib) -> str:
     return raw.decode("utf-8", errors="replace") if raw else "GB300 XPBD call failed without an error message."
 
 
-def capabilities() -> int:
-    return int(_load_library().ssbl_capabilities())
+KEY_DIVISION = {"reference": 0, "ieee": 1}
+
+
+def set_default_key_division(mode: str) -> None:
+    """Cell-key division of the solvers and scenes created from now on in this
+    process: "reference" (the default; the reference's fast-math division, so
+    hash keys are its integers) or "ieee" (the correctly rounded quotient of
+    the CPU oracle)."""
+    lib = _load_library()
+    if not lib.xpbd_gb300_set_default_key_division(KEY_DIVISION[mode]):
+        raise NativeSolverError(_last_error(lib))
+
+
+def capabilities(library: str | None = None) -> int:
+    return int(_load_library(library).ssbl_capabilities())
 
 
 def config_from_options(cloth: ClothData, options: SolverOptions, static_triangles: np.ndarray) -> NativeConfig:
@@ -443,9 +460,10 @@ def _dynamic_frame_inputs(triangles, indexed, particles):
 class NativeXpbdSolver:
     """One cloth on the GPU (the reference's NativeXpbdSolver interface)."""
 
-    def __init__(self, cloth: ClothData, options: SolverOptions, static_triangles: np.ndarray):
-        self._lib = _load_library()
-        caps = capabilities()
+    def __init__(self, cloth: ClothData, options: SolverOptions, static_triangles: np.ndarray,
+                 library: str | None = None, key_division: str | None = None):
+        self._lib = _load_library(library)
+        caps = capabilities(library)
         if options.stretch_optimization_enabled and not caps & _CAP_STRETCH_OPTIMIZATION:
             raise NativeSolverError("Loaded CUDA solver library does not support hard stretch optimization.")
         if not caps & _CAP_PIN_WEIGHTS:
@@ -459,15 +477,17 @@ class NativeXpbdSolver:
         del keep
         if not self._handle:
             raise NativeSolverError(_last_error(self._lib))
+        if key_division is not None:
+            self.set_key_division(key_division)
         if len(cloth.pin_indices) > 0:
             self.update_pin_targets(cloth.pin_indices, cloth.pin_targets_world, cloth.pin_weights)
 
     @classmethod
-    def from_raw(cls, config: NativeConfig, mesh: NativeMesh, pins=None) -> "NativeXpbdSolver":
+    def from_raw(cls, config: NativeConfig, mesh: NativeMesh, pins=None, library: str | None = None) -> "NativeXpbdSolver":
         """Create from ABI41 structs directly (the pointers in `mesh` must
         stay valid for the call)."""
         self = cls.__new__(cls)
-        self._lib = _load_library()
+        self._lib = _load_library(library)
         self._vertex_count = int(config.vertex_count)
         self._positions_out = np.empty((self._vertex_count, 3), np.float32)
         self._static_triangle_count = int(config.static_triangle_count)
@@ -612,6 +632,10 @@ class NativeXpbdSolver:
         self._check(self._lib.xpbd_gb300_hash_info(self._handle, _ip(out)))
         return out
 
+    def set_key_division(self, mode: str) -> None:
+        """"reference" or "ieee" cell-key division (set_default_key_division)."""
+        self._check(self._lib.xpbd_gb300_set_key_division(self._handle, KEY_DIVISION[mode]))
+
     def set_graph_capture(self, enabled: bool) -> None:
         self._check(self._lib.xpbd_gb300_set_graph_capture(self._handle, 1 if enabled else 0))
 
@@ -705,7 +729,7 @@ class NativeXpbdBatch(NativeXpbdSolver):
     address all cloths (positions concatenated in cloth order); the per-cloth
     methods address one."""
 
-    def __init__(self, items):
+    def __init__(self, items, key_division: str | None = None):
         """`items`: sequence of (ClothData, SolverOptions, static_triangles)."""
         self._lib = _load_library()
         items = list(items)
@@ -730,6 +754,8 @@ class NativeXpbdBatch(NativeXpbdSolver):
         self._vertex_count = int(self._ranges[:, 1].sum())
         self._positions_out = np.empty((self._vertex_count, 3), np.float32)
         self._static_triangle_count = max(len(it[2]) for it in items)
+        if key_division is not None:
+            self.set_key_division(key_division)
         for k, (cloth, _, _) in enumerate(items):
             if len(cloth.pin_indices) > 0:
                 self.update_cloth_pin_targets(k, cloth.pin_indices, cloth.pin_targets_world, cloth.pin_weights)

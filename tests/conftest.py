@@ -30,3 +30,20 @@ def gpu_lib():
     build.build()
     lib = native._load_library()
     return native
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _oracle_key_division():
+    """Most GPU tests compare the solver with the CPU oracle bit for bit, so
+    the solvers the tests create use the oracle's IEEE cell-key division.  The
+    library's default, the reference's own division, is checked against the
+    reference solver in test_gpu_ref_parity.py, whose solvers ask for it by
+    name (and by the smoke check of the entry module)."""
+    from xpbd_gb300 import build, native
+
+    if not os.path.exists(build.library_path()):
+        yield
+        return
+    native.set_default_key_division("ieee")
+    yield
+    native.set_default_key_division("reference")

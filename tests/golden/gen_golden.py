@@ -134,4 +134,7 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SSBL_REFERENCE_ROOT", "")
+    if not root:
+        sys.exit("usage: gen_golden.py REFERENCE_CHECKOUT (or set SSBL_REFERENCE_ROOT)")
+    main(root)

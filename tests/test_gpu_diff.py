@@ -136,3 +136,135 @@ def test_cdiff_configuration_runs(gpu_lib):
     loss.backward()
     assert torch.isfinite(ksd.grad).all() and torch.isfinite(kbd.grad).all()
     assert float(loss.detach()) > 0
+
+
+# ---------------------------------------------------------------- Cdiff --
+# The differentiable configuration itself: 64 x 64 cloth, 60 frames x 10
+# substeps x 2 iterations, per-constraint compliance fields log-uniform
+# within a decade of 1e-7 (stretch) and 1e-4 (bend), loss = squared distance
+# of the final positions to the rollout of another seeded compliance field.
+
+def _cdiff(frames=60):
+    sc = scene.diff_scene(64, frames)
+    ks, kb = _fields(sc, 1e-7, 1e-4, 0)
+    kts, ktb = _fields(sc, 1e-7, 1e-4, 1)
+    return sc, ks, kb, kts, ktb
+
+
+def _report(key, value):
+    import json
+    import os
+
+    path = os.environ.get("XPBD_DIFF_REPORT")
+    if path:
+        data = json.load(open(path)) if os.path.exists(path) else {}
+        data[key] = value
+        with open(path, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+    print(key, value)
+
+
+def test_cdiff_reference_gradient_matches_finite_differences(gpu_lib):
+    """float64 central differences of the restated rollout at the Cdiff
+    configuration against its autograd gradient: 64 random single
+    compliances and 8 random directions, at h = 1e-3 relative (the
+    configured step) and at h = 1e-4.  All 288 perturbed rollouts run as one
+    batched float64 rollout on the GPU.  At h = 1e-4 every difference
+    matches the gradient closely.  At h = 1e-3 a perturbation of all the
+    compliances moves some of the step's clamps (stretch / bend correction
+    caps, the velocity-feedback clamp) across their thresholds somewhere in
+    the 600 substeps, so the loss has kinks at that scale; there the
+    differences are required to agree in sign and, in the median, within
+    15 %."""
+    dev = "cuda"
+    sc, ks, kb, kts, ktb = _cdiff()
+    r = Rollout(sc.cloth, sc.options, device=dev)
+    f64 = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)  # noqa: E731
+    target = r.run(f64(kts), f64(ktb), sc.frames, 10, 2).detach()
+    ksr, kbr = f64(ks).requires_grad_(), f64(kb).requires_grad_()
+    loss0 = ((r.run(ksr, kbr, sc.frames, 10, 2) - target) ** 2).sum()
+    loss0.backward()
+    gs, gb = ksr.grad.detach(), kbr.grad.detach()
+    E, B = len(ks), len(kb)
+    rng = np.random.default_rng(5)
+    idx = rng.choice(E + B, 64, replace=False)
+    S = torch.zeros(72, E, dtype=torch.float64, device=dev)
+    Bm = torch.zeros(72, B, dtype=torch.float64, device=dev)
+    for n, k in enumerate(idx):
+        if k < E:
+            S[n, k] = 1.0
+        else:
+            Bm[n, k - E] = 1.0
+    S[64:] = f64(rng.standard_normal((8, E)))
+    Bm[64:] = f64(rng.standard_normal((8, B)))
+    base_s, base_b = f64(ks), f64(kb)
+    an = ((gs * base_s * S).sum(-1) + (gb * base_b * Bm).sum(-1)).cpu().numpy()
+    scale = float(np.abs(an[:64]).max())
+    hs = (1.0e-3, 1.0e-4)
+    with torch.no_grad():
+        ps = torch.cat([base_s * (1 + h * sg * S) for h in hs for sg in (1, -1)])
+        pb = torch.cat([base_b * (1 + h * sg * Bm) for h in hs for sg in (1, -1)])
+        L = ((r.run(ps, pb, sc.frames, 10, 2) - target) ** 2).sum((-1, -2)).cpu().numpy()
+    rep = {"loss": float(loss0.detach()), "largest_single_effect": scale}
+    for n, h in enumerate(hs):
+        lp, lm = L[144 * n:144 * n + 72], L[144 * n + 72:144 * n + 144]
+        fd = (lp - lm) / (2 * h)
+        single = np.abs(fd[:64] - an[:64]) / scale
+        dirs = np.abs(fd[64:] - an[64:]) / np.abs(an[64:])
+        rep[f"h={h:g}"] = {"single_abs_err_over_scale_max": float(single.max()),
+                           "single_abs_err_over_scale_median": float(np.median(single)),
+                           "direction_rel_err": [float(x) for x in dirs]}
+        if h == 1.0e-4:
+            assert single.max() <= 2e-3, (fd[:64], an[:64])
+            assert dirs.max() <= 2e-3, (fd[64:], an[64:])
+        else:
+            assert (np.sign(fd[64:]) == np.sign(an[64:])).all(), (fd[64:], an[64:])
+            assert np.median(dirs) <= 0.15 and np.median(single) <= 0.02, rep
+    _report("cdiff/float64_fd", rep)
+
+
+def test_cdiff_adjoint_along_its_trajectory(gpu_lib):
+    """The GPU's float32 adjoint at the Cdiff configuration against float64
+    autograd taken along the GPU rollout's own trajectory: for every frame,
+    from the last back, the float64 restatement re-runs that frame from the
+    GPU's checkpoint (upcast) and its vector-Jacobian product carries the
+    adjoint of the state back and adds the compliance gradient.  (An
+    independent float64 rollout drifts millimetres away from the float32 one
+    over 60 frames, the clamps of the step switching at different substeps,
+    so its gradient belongs to another trajectory; that drift is recorded.)"""
+    dev = "cuda"
+    sc, ks, kb, kts, ktb = _cdiff()
+    frames = sc.frames
+    dc = DiffCloth(sc.cloth, sc.options)
+    target = dc.rollout(torch.tensor(kts, device=dev), torch.tensor(ktb, device=dev), frames, 10, 2).double()
+    x = dc.rollout(torch.tensor(ks, device=dev), torch.tensor(kb, device=dev), frames, 10, 2)
+    seed = 2.0 * (x.double() - target)
+    gs, gb = dc.backward(seed.float())
+    r = Rollout(sc.cloth, sc.options, device=dev)
+    ks64 = torch.tensor(ks, dtype=torch.float64, device=dev)
+    kb64 = torch.tensor(kb, dtype=torch.float64, device=dev)
+    gs64, gb64 = torch.zeros_like(ks64), torch.zeros_like(kb64)
+    lam = [seed, torch.zeros_like(seed), torch.zeros_like(seed)]
+    for f in range(frames - 1, -1, -1):
+        ck = dc.checkpoint(f)[..., :3].double()
+        state = [ck[0].clone().requires_grad_(), ck[1].clone().requires_grad_(), ck[2].clone().requires_grad_()]
+        k1, k2 = ks64.clone().requires_grad_(), kb64.clone().requires_grad_()
+        out = r.frame(*state, k1, k2, 10, 2)
+        torch.autograd.backward(list(out), lam)
+        gs64 += k1.grad
+        gb64 += k2.grad
+        lam = [t.grad if t.grad is not None else torch.zeros_like(t) for t in state]
+    mine = torch.cat([gs.double(), gb.double()])
+    theirs = torch.cat([gs64, gb64])
+    rel = float(torch.linalg.norm(mine - theirs) / torch.linalg.norm(theirs))
+    cos = float(torch.dot(mine, theirs) / (torch.linalg.norm(mine) * torch.linalg.norm(theirs)))
+    rel_s = float(torch.linalg.norm(gs.double() - gs64) / torch.linalg.norm(gs64))
+    rel_b = float(torch.linalg.norm(gb.double() - gb64) / torch.linalg.norm(gb64))
+    # the independent float64 rollout, for the record
+    x64 = r.run(ks64, kb64, frames, 10, 2)
+    drift = float((x.double() - x64).abs().max())
+    _report("cdiff/adjoint_along_trajectory", {"rel_l2": rel, "cosine": cos, "rel_l2_stretch": rel_s, "rel_l2_bend": rel_b,
+                                               "independent_float64_drift_m": drift,
+                                               "signal_m": float((x.double() - target).abs().max())})
+    assert torch.isfinite(mine).all()
+    assert rel < 2e-2 and cos > 0.9998, (rel, cos, rel_s, rel_b)

@@ -50,6 +50,29 @@ def test_plain_grid_with_tethers_and_graph_off(gpu_lib, oracle_lib):
     _run_and_compare(sc, gpu, ora, 6)
 
 
+def test_plain32_full_horizon_parity(gpu_lib, oracle_lib):
+    """The plain 32 x 32 configuration over all of its 120 frames."""
+    sc = scene.plain_grid_scene(32, 120)
+    gpu, ora = _pair(sc, oracle_lib)
+    _run_and_compare(sc, gpu, ora, 120)
+
+
+@pytest.mark.parametrize("mode", [2, 1], ids=["strict", "fast"])
+def test_drop10k_full_size_parity(mode, gpu_lib, oracle_lib):
+    """The 10k configuration at full size (100 x 100 with seeded jitter, sphere
+    and 64^3 box / torus SDF, self collision 2 mm, friction 0.3) through the
+    first contacts with the sphere and the collider (40 frames), with every
+    diagnostic counter."""
+    sc = scene.drop_scene(100, 40, seed=0, self_mode=mode)
+    gpu, ora = _pair(sc, oracle_lib)
+    _run_and_compare(sc, gpu, ora, 40)
+    assert float(np.abs(gpu.download_positions() - sc.cloth.positions_world).max()) > 0.3  # it fell onto the colliders
+    gpu.step(sc.substeps, sc.iterations, diagnostics=True)
+    ora.step(sc.substeps, sc.iterations)
+    assert np.array_equal(gpu.download_positions(), ora.download_positions())
+    assert np.array_equal(gpu.read_buffer(13, np.uint64, 38), ora.read_buffer(13, np.uint64, 38))
+
+
 @pytest.mark.parametrize("hardness", [0.4, 1.0])
 def test_hard_stretch_grid_parity(hardness, gpu_lib, oracle_lib):
     """CG stretch path (hardness 0.4) and CG + averaged polish + ratio caps +
