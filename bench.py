@@ -28,10 +28,20 @@ un-graphed frame and the roofline of the dominant kernel kind, SM clocks
 sampled during the timed region, and the CPU oracle timed on a bounded
 sample of the same workload.
 
-``--impl reference``: the reference's step has no CPU implementation and its
-CUDA solver cannot be carried to the GPU machine, so that arm times the CPU
-restatement of the reference's algorithm (oracle/) with all host threads, on
-a bounded sample of the workload's cloths per step.
+Also in the default line (``--extras 1``): the plain32 and drop10k
+workloads device-timed the same way; the serving loop over 60 s of Poisson
+arrivals with its p50 / p99 frame latency under a frame-latency target
+(``--serve-latency-ms``, default 100); the differentiable rollout + adjoint;
+and ``reference_gpu``, the reference's own CUDA solver (built unchanged for
+sm_103a from its sources by oracle/build_ref.py) stepping the same 256 cloths
+one handle at a time on the default stream, one wait per frame, as the add-on
+does: the plain baseline of the batched form.
+
+``--impl reference``: the reference's step has no CPU implementation, so that
+arm times the CPU restatement of the reference's algorithm (oracle/) with
+all host threads, on every 16th cloth of the workload per step; its scenes
+come from the pure-Python builders, so it loads no library of this
+repository.
 """
 from __future__ import annotations
 
@@ -88,40 +98,60 @@ def workload(name: str, cloths: int = 256) -> list:
 
 
 def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict) -> float | None:
-    """Compulsory bytes of one launch of a kernel kind (x, v rows of 12 B,
-    constraint entries of 12 B: two indices and a rest length).  The query
-    kinds count what a query must read: its own item, its bucket range, and
-    per bucket slot evaluated the candidate id, indices and positions (slot
-    counts measured in the profiled frame)."""
+    """Compulsory bytes of one launch of a kernel kind, by the per-kernel
+    model of the cloth step (12 B per position / velocity row read or
+    written):
+      predict              52 B per vertex (read x, v, w; write x, prev)
+      stretch pass         12 B per edge + 24 B per vertex (constraint stream,
+                           x read and written) + 36 B per vertex for the
+                           contact stages fused into the same pass
+      velocity pass        52 B per vertex
+      bend colour          12 B per bend + 2 endpoints read and written
+      vertex-triangle /    12 B per candidate gather: the candidate's row,
+      edge-edge query      per evaluated bucket slot (slots counted in the
+                           profiled frames)
+      hash build           12 B per primitive row read, 32 B per entry (key
+                           and id through a two-pass sort, read and written),
+                           8 B per bucket (cell start / end)
+    Returns None for kinds without a model."""
     if kind == "predict":
-        return 52.0 * V                                   # R x v w, W x prev
+        return 52.0 * V
     if kind == "stretch_pass":
-        return 12.0 * E + 24.0 * V + 36.0 * V             # constraint stream, x R/W, contact stages R x v W x
+        return 12.0 * E + 24.0 * V + 36.0 * V
     if kind == "vertex_pass":
-        return 52.0 * V                                   # velocity update R x prev W v x
+        return 52.0 * V
     if kind == "bend_color":
-        return 12.0 * B + 48.0 * B                        # constraint stream, 2 endpoints R/W
+        return 12.0 * B + 48.0 * B
+    if kind == "edge_edge" and counters.get("ee_slots"):
+        return 12.0 * counters["ee_slots"]
+    if kind == "vertex_triangle" and counters.get("vt_slots"):
+        return 12.0 * counters["vt_slots"]
+    if kind == "edge_hash" and counters.get("edge_entries"):
+        return 2 * F3 * counters["edge_hashed"] + 32.0 * counters["edge_entries"] + 8.0 * counters["edge_buckets"]
+    if kind == "triangle_hash" and counters.get("tri_entries"):
+        return 3 * F3 * counters["tri_hashed"] + 32.0 * counters["tri_entries"] + 8.0 * counters["tri_buckets"]
+    return None
+
+
+def full_gather_bytes(kind: str, counters: dict) -> float | None:
+    """What a query evaluation actually loads, beside the per-gather model:
+    per item its own indices and rows and its bucket range, per evaluated
+    slot the candidate id, its indices and its rows (40 + 36 B per edge-edge
+    slot, 20 + 52 B per vertex-triangle slot)."""
     if kind == "edge_edge" and counters.get("ee_items"):
         return (8 + 2 * F3 + 8) * counters["ee_items"] + (4 + 8 + 2 * F3) * counters["ee_slots"]
     if kind == "vertex_triangle" and counters.get("vt_items"):
         return (F3 + 8) * counters["vt_items"] + (4 + 12 + 3 * F3) * counters["vt_slots"]
-    # one hash build (count pass, scan, scatter pass): per primitive its
-    # indices and positions in both passes, per entry the count reduction,
-    # the cursor atomic and the entry write, per bucket the cleared count,
-    # the scan's read and its start / cursor writes
-    if kind == "edge_hash" and counters.get("edge_entries"):
-        return 2 * (8 + 2 * F3) * counters["edge_hashed"] + 12 * counters["edge_entries"] + 16 * counters["edge_buckets"]
-    if kind == "triangle_hash" and counters.get("tri_entries"):
-        return 2 * (12 + 3 * F3) * counters["tri_hashed"] + 12 * counters["tri_entries"] + 16 * counters["tri_buckets"]
     return None
 
 
 # DRAM bytes (read + write) per evaluated bucket slot of the edge-edge query
-# passes, measured by ncu on the 96-cloth batch and scaled by the slots of
-# the measured workload (profiles/edge_edge_dram_per_slot_batch96.md).
+# passes: dram__bytes_read.sum + dram__bytes_write.sum of every edge-edge
+# launch of two frames of the 96-cloth batch under ncu, divided by the slots
+# those frames evaluated; scaled by the slots of the measured workload.
 EE_DRAM_BYTES_PER_SLOT = 11.4
 # ... and per entry of an edge-hash build (count, scans, scatter, trim and
-# bucket ordering; profiles/edge_hash_dram_per_entry_batch96.md).
+# bucket ordering), from the same kind of capture of the hash kernels.
 EDGE_HASH_DRAM_BYTES_PER_ENTRY = 16.7
 
 
@@ -205,26 +235,24 @@ def dist_setup():
     return world, rank, local
 
 
-def oracle_sample(scs: list, target_vertices: int) -> list:
-    """The first cloths of the workload, up to about `target_vertices`."""
-    out, v = [], 0
-    for sc in scs:
-        out.append(sc)
-        v += len(sc.cloth.positions_world)
-        if v >= target_vertices:
-            break
-    return out
+def sample_indices(count: int, stride: int = 16) -> list:
+    """Evenly spaced cloths of a batched workload (every `stride`-th), the
+    bounded sample the CPU timings step: the same mix of sizes and fast /
+    strict self collision as the whole set."""
+    return list(range(0, count, stride)) if count > 1 else [0]
 
 
 def cpu_oracle_rate(scs: list, budget_s: float) -> tuple[float, int, str]:
-    """The oracle (all host threads) stepping cloths of the workload one
-    frame each, in workload order, for about `budget_s` seconds."""
+    """The oracle (all host threads) stepping an evenly spaced sample of the
+    workload's cloths one frame each, for about `budget_s` seconds."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import xpbd_oracle
 
     threads = xpbd_oracle.set_threads(os.cpu_count() or 1)
+    sample = [scs[k] for k in sample_indices(len(scs))]
     work, elapsed, cloths, frames_per = 0, 0.0, 0, 1 if len(scs) > 1 else 400
-    for sc in scs:
+    n = 0
+    for sc in sample:
         o = xpbd_oracle.OracleSolver.from_scene(sc.cloth, sc.options, sc.static_triangles)
         o.step(sc.substeps, sc.iterations)  # warm-up frame
         V = len(sc.cloth.positions_world)
@@ -241,7 +269,8 @@ def cpu_oracle_rate(scs: list, budget_s: float) -> tuple[float, int, str]:
         if elapsed >= budget_s:
             break
     if len(scs) > 1:
-        what = f"first {cloths} cloths of the workload, one warm-up frame then one timed frame each, {elapsed:.1f} s"
+        what = (f"{cloths} cloths (every 16th of the workload's {len(scs)}), one warm-up frame then one timed frame "
+                f"each, {elapsed:.1f} s")
     else:
         what = f"{n} frames after one warm-up frame, {elapsed:.1f} s"
     return work / elapsed, threads, what
@@ -264,17 +293,20 @@ def max_over_ranks(value: float, world: int) -> float:
 
 
 def run_reference(args, scs, world, rank):
-    """Reference arm: the CPU restatement on a bounded sample per step."""
+    """Reference arm: the reference's step exists only as CUDA code, so this
+    arm times its CPU restatement (oracle/) with all host threads, on an
+    evenly spaced sample of the workload's cloths per step.  The scenes are
+    built by the pure-Python builders: no library of this repository is
+    loaded."""
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import xpbd_oracle
 
     threads = xpbd_oracle.set_threads(os.cpu_count() or 1)
-    sample = oracle_sample(scs, 60000) if len(scs) > 1 else scs
-    solvers = [xpbd_oracle.OracleSolver.from_scene(s.cloth, s.options, s.static_triangles) for s in sample]
-    V = sum(len(s.cloth.positions_world) for s in sample)
-    S, I = sample[0].substeps, sample[0].iterations
+    solvers = [xpbd_oracle.OracleSolver.from_scene(s.cloth, s.options, s.static_triangles) for s in scs]
+    V = sum(len(s.cloth.positions_world) for s in scs)
+    S, I = scs[0].substeps, scs[0].iterations
     for _ in range(args.warmup):
         for o in solvers:
             o.step(S, I)
@@ -284,8 +316,9 @@ def run_reference(args, scs, world, rank):
             o.step(S, I)
     el = time.perf_counter() - t0
     value = V * S * args.steps / el
-    what = (f"first {len(sample)} of the workload's {len(scs)} cloths ({V} vertices) per step, one frame each"
-            if len(scs) > 1 else "the whole workload, one frame per step")
+    what = (f"{len(scs)} of the workload's {args.batch_cloths} cloths (every 16th: sizes 16-128, fast and strict self "
+            f"collision; {V} vertices) per step, one frame each" if args.workload == "batch256"
+            else "the whole workload, one frame per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -296,6 +329,71 @@ def run_reference(args, scs, world, rank):
         "note": "the reference's step exists only as CUDA code; this arm is the C restatement of its algorithm on the host cores",
     }
     print(json.dumps(line), flush=True)
+
+
+def device_time(solver, S: int, I: int, steps: int, torch, world: int = 1, clocks=None) -> float:
+    """K frames, each bracketed by CUDA events on the solver's stream after a
+    256 MiB write on that stream (L2 starts cold); returns the summed
+    milliseconds (max over ranks)."""
+    stream = torch.cuda.ExternalStream(solver.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        events[k][0].record(stream)
+        solver.step(S, I, diagnostics=False, synchronize=False)
+        events[k][1].record(stream)
+    torch.cuda.synchronize()
+    return max_over_ranks(sum(a.elapsed_time(b) for a, b in events), world)
+
+
+def time_single(native, torch, name: str, steps: int, warmup: int) -> dict:
+    """One of the single-cloth workloads (plain32, drop10k), device-timed."""
+    sc = workload(name)[0]
+    solver = native.NativeXpbdSolver(sc.cloth, sc.options, sc.static_triangles)
+    S, I = sc.substeps, sc.iterations
+    for _ in range(warmup):
+        solver.step(S, I, diagnostics=False, synchronize=False)
+    ms = device_time(solver, S, I, steps, torch)
+    launches = solver.last_step_launches()
+    solver.close()
+    V = len(sc.cloth.positions_world)
+    return {"value": V * S * steps / (ms / 1000.0), "unit": METRIC, "ms_per_step": ms / steps, "frames": steps,
+            "launches_per_step": launches, "workload": DESCRIPTIONS[name]}
+
+
+def time_reference_gpu(scs, frames: int, torch) -> dict:
+    """The reference's own CUDA solver (native/src/ssbl_xpbd_cuda_abi41.cu,
+    built unchanged with its own flags for sm_103a by oracle/build_ref.py)
+    on the same cloths, the way the add-on steps them: one handle per cloth,
+    each step(diagnostics=False, synchronize=False) in turn on the default
+    stream, one device wait per frame (session_manager.py:2528-2591)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_solver
+
+    if not ref_solver.available():
+        return {"unavailable": "reference solver not built (oracle/build_ref.py needs the reference sources)"}
+    solvers = [ref_solver.RefSolver.from_scene(s) for s in scs]
+    S, I = scs[0].substeps, scs[0].iterations
+    V = sum(len(s.cloth.positions_world) for s in scs)
+    for r in solvers:
+        r.step(S, I, diagnostics=False, synchronize=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        for r in solvers:
+            r.step(S, I, diagnostics=False, synchronize=False)
+        torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    for r in solvers:
+        r.close()
+    return {"value": V * S * frames / el, "unit": METRIC, "ms_per_step": 1000.0 * el / frames, "frames": frames,
+            "handles": len(scs), "what": "reference CUDA solver, one handle per cloth on the default stream, "
+            "one wait per frame (host-timed)"}
 
 
 def time_plain(native, scs, frames: int) -> dict:
@@ -404,21 +502,12 @@ def run_prep(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def run_diff(args, world, rank, local):
-    """Differentiable form: one step = a 60-frame rollout of the 64 x 64
-    cloth and the adjoint of an L2 loss (vertex-substeps/s of the forward
-    frames; the backward recomputes each frame once more)."""
-    if args.impl == "reference":
-        if rank == 0:
-            print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable rollout"}), flush=True)
-        return
-    import torch
-
-    torch.cuda.set_device(local)
-    from xpbd_gb300 import build
+def diff_measure(steps: int, warmup: int, torch) -> dict:
+    """Differentiable form: one step = a 60-frame rollout of the 64 x 64 cloth
+    and the adjoint of an L2 loss (vertex-substeps/s of the forward frames;
+    the backward recomputes each frame once more)."""
     from xpbd_gb300.diff import DiffCloth
 
-    build.build()
     sc = scene.diff_scene(64, 60)
     ks = torch.tensor(scene.compliance_field(len(sc.cloth.edges), 1e-7, 1.0, 0), device="cuda")
     kb = torch.tensor(scene.compliance_field(len(sc.cloth.bends), 1e-4, 1.0, 1), device="cuda")
@@ -431,37 +520,84 @@ def run_diff(args, world, rank, local):
         x = dc.rollout(ks, kb, sc.frames, sc.substeps, sc.iterations)
         return dc.backward(2.0 * (x - target))
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         gs, gb = step()
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
     t1 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         dc.rollout(ks, kb, sc.frames, sc.substeps, sc.iterations)
     torch.cuda.synchronize()
     fwd = time.perf_counter() - t1
     V = len(sc.cloth.positions_world)
-    value = V * sc.substeps * sc.frames * args.steps / el
+    return {"value": V * sc.substeps * sc.frames * steps / el, "unit": METRIC, "ms_per_step": 1000.0 * el / steps,
+            "forward_only": {"value": V * sc.substeps * sc.frames * steps / fwd, "unit": METRIC,
+                             "ms_per_rollout": 1000.0 * fwd / steps},
+            "grad_norms": {"stretch": float(gs.norm()), "bend": float(gb.norm())},
+            "sizes": {"vertices": V, "edges": len(sc.cloth.edges), "bends": len(sc.cloth.bends), "frames": sc.frames,
+                      "substeps": sc.substeps}}
+
+
+def run_diff(args, world, rank, local):
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable rollout"}), flush=True)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    from xpbd_gb300 import build
+
+    build.build()
+    d = diff_measure(args.steps, args.warmup, torch)
+    value = d["value"] * world
     if rank != 0:
         return
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": d["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded compliance fields)",
-        "config": {"workload": DESCRIPTIONS["diff"], "vertices": V, "edges": len(sc.cloth.edges),
-                   "bends": len(sc.cloth.bends), "frames": sc.frames, "substeps": sc.substeps,
-                   "parallelism": f"replicas x{world}"},
-        "forward_only": {"value": V * sc.substeps * sc.frames * args.steps / fwd, "unit": METRIC,
-                         "ms_per_rollout": 1000.0 * fwd / args.steps},
-        "grad_norms": {"stretch": float(gs.norm()), "bend": float(gb.norm())},
+        "config": {"workload": DESCRIPTIONS["diff"], **d["sizes"], "parallelism": f"replicas x{world}"},
+        "forward_only": d["forward_only"], "grad_norms": d["grad_norms"],
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "note": "inputs and gradients stay on the device (torch tensors)"},
     }
     print(json.dumps(line), flush=True)
+
+
+def serve_measure(seconds: float, budget_gb: float, latency_ms: float | None, warmup: int, seed: int, torch,
+                  clock_index: int | None = None) -> tuple[dict, dict | None]:
+    """The request loop for `seconds` of Poisson arrivals (200/s); returns its
+    statistics (results removed, their downloaded bytes kept) and the clock
+    summary when sampled."""
+    from xpbd_gb300.serving import ServingEngine
+
+    reqs = scene.serving_requests(rate=200.0, duration=seconds, seed=seed)
+    # warm-up: a few small requests through a separate engine (module load, first graph capture)
+    warm = ServingEngine(hbm_budget_bytes=int(8e9))
+    warm.run(scene.serving_requests(rate=50.0, duration=0.1, seed=99, v_range=(1000, 4000), horizon=(3, 5),
+                                    max_requests=warmup), duration=None, drain=True)
+    warm.close()
+    torch.cuda.synchronize()
+    eng = ServingEngine(hbm_budget_bytes=int(budget_gb * 1e9), frame_latency_ms=latency_ms)
+    sampler = ClockSampler(clock_index) if clock_index is not None else None
+    if sampler:
+        sampler.__enter__()
+    try:
+        st = eng.run(reqs, duration=seconds)
+        eng.close()  # waits for solvers still being built (their graph captures) before any device-wide sync
+        torch.cuda.synchronize()
+    finally:
+        if sampler:
+            sampler.__exit__(None, None, None)
+    results = st.pop("results")
+    st["offered_requests"] = len(reqs)
+    st["d2h_bytes"] = int(sum(r.positions.nbytes for r in results))
+    return st, (sampler.summary() if sampler else None)
 
 
 def run_serving(args, world, rank, local):
@@ -477,23 +613,10 @@ def run_serving(args, world, rank, local):
 
     torch.cuda.set_device(local)
     from xpbd_gb300 import build
-    from xpbd_gb300.serving import ServingEngine
 
     build.build()
-    reqs = scene.serving_requests(rate=200.0, duration=args.serve_seconds, seed=rank)
-    # warm-up: a few small requests through a separate engine (module load, first graph capture)
-    warm = ServingEngine(hbm_budget_bytes=int(8e9))
-    warm.run(scene.serving_requests(rate=50.0, duration=0.1, seed=99, v_range=(1000, 4000), horizon=(3, 5),
-                                    max_requests=args.warmup), duration=None, drain=True)
-    warm.close()
-    torch.cuda.synchronize()
-    eng = ServingEngine(hbm_budget_bytes=int(args.serve_budget_gb * 1e9))
-    with ClockSampler(local) as clocks:
-        st = eng.run(reqs, duration=args.serve_seconds)
-        eng.close()  # waits for solvers still being built (their graph captures) before any device-wide sync
-        torch.cuda.synchronize()
-    results = st.pop("results")
-    d2h = sum(r.positions.nbytes for r in results)
+    st, clocks = serve_measure(args.serve_seconds, args.serve_budget_gb, args.serve_latency_ms, args.warmup, rank,
+                               torch, local)
     value = st["throughput"] * world
     if rank != 0:
         return
@@ -501,13 +624,14 @@ def run_serving(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": st["ticks"], "warmup": args.warmup,
         "ms_per_step": 1000.0 * st["elapsed_s"] / max(st["ticks"], 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request stream)",
-        "config": {"workload": DESCRIPTIONS["serve"], "seconds": args.serve_seconds, "offered_requests": len(reqs),
-                   "budget_gb": args.serve_budget_gb, "parallelism": f"replicas x{world}"},
-        "serving": {k: v for k, v in st.items()},
+        "config": {"workload": DESCRIPTIONS["serve"], "seconds": args.serve_seconds, "offered_requests": st["offered_requests"],
+                   "budget_gb": args.serve_budget_gb, "frame_latency_target_ms": args.serve_latency_ms,
+                   "parallelism": f"replicas x{world}"},
+        "serving": st,
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": None,
-                "d2h_bytes_per_step": d2h / max(st["ticks"], 1),
+                "d2h_bytes_per_step": st["d2h_bytes"] / max(st["ticks"], 1),
                 "note": "the loop is end to end: requests enter from host arrays and results return to host memory"},
-        "clocks": clocks.summary(),
+        "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
@@ -543,10 +667,15 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--plain-frames", type=int, default=3, help="frames of the plain comparison (0 skips it)")
     ap.add_argument("--batch-cloths", type=int, default=256, help="cloths of the batch256 workload (smaller for profiling)")
-    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--serve-latency-ms", type=float, default=100.0,
+                    help="frame-latency target of the serving admission (0: admission by memory only)")
     ap.add_argument("--autotune", type=int, default=1, help="1: launch configuration from the autotuner (default); 0: built-in defaults")
+    ap.add_argument("--extras", type=int, default=1,
+                    help="1: also measure plain32, drop10k, serving, diff and the reference solver (default line)")
     args = ap.parse_args()
+    args.serve_latency_ms = args.serve_latency_ms if args.serve_latency_ms > 0 else None
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
     if args.workload == "serve":
@@ -558,14 +687,21 @@ def main():
     if args.workload == "prep":
         run_prep(args, world, rank, local)
         return
+    if args.impl == "reference":
+        # the reference arm builds its sample with the Python builders only
+        # (no library of this repository is loaded)
+        scene.set_native_prep(False)
+        if args.workload == "batch256":
+            scs = scene.batched_scenes(args.batch_cloths, seed=0, frames=120, only=sample_indices(args.batch_cloths))
+        else:
+            scs = workload(args.workload)
+        run_reference(args, scs, world, rank)
+        return
     scs = workload(args.workload, args.batch_cloths)
     if args.batch_cloths != 256 and args.workload == "batch256":
         nv = sum(len(s.cloth.positions_world) for s in scs)
         DESCRIPTIONS["batch256"] = DESCRIPTIONS["batch256"].replace("256 independent cloths", f"{args.batch_cloths} independent cloths").replace(
             "1,589,788 verts", f"{nv:,} verts")
-    if args.impl == "reference":
-        run_reference(args, scs, world, rank)
-        return
 
     import torch
 
@@ -594,21 +730,8 @@ def main():
     for _ in range(args.warmup):
         solver.step(S, I, diagnostics=False, synchronize=False)
     solver.synchronize()
-    stream = torch.cuda.ExternalStream(solver.stream())
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xFF)
-            events[k][0].record(stream)
-            solver.step(S, I, diagnostics=False, synchronize=False)
-            events[k][1].record(stream)
-        torch.cuda.synchronize()
-    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in events), world)
+        total_ms = device_time(solver, S, I, args.steps, torch, world)
     launches_per_step = solver.last_step_launches()
     value = V * S * args.steps * world / (total_ms / 1000.0)
 
@@ -643,8 +766,23 @@ def main():
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": traffic,
                 "traffic_source": ("ncu DRAM bytes per evaluated slot (edge-edge) or per entry (edge hash) on 96 cloths, "
                                    "scaled by this workload's units per launch" if traffic is not None else None),
-                "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch}
+                "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch,
+                "byte_model": "12 B per candidate gather" if kind in ("edge_edge", "vertex_triangle") else "per-kernel state bytes"}
+        full = full_gather_bytes(kind, counters)
+        if full is not None:
+            full_launch = full / max(k_n, 1)
+            roof["full_gather"] = {"bytes_per_launch": full_launch, "achieved": full_launch / (avg_ms / 1000.0) / 1e9,
+                                   "frac": full_launch / (avg_ms / 1000.0) / 1e9 / peak,
+                                   "model": "per item its rows and bucket range, per slot id + indices + rows"}
         break
+    kernel_rooflines = {}
+    for kind, (k_ms, k_n) in ranked:
+        alg_total = algorithmic_bytes(kind, V, E, T, B, counters)
+        if alg_total is None or k_n <= 0 or k_ms <= 0:
+            continue
+        per_launch = alg_total / k_n if kind in ("edge_edge", "vertex_triangle") else alg_total
+        gbs = per_launch / (k_ms / k_n / 1000.0) / 1e9
+        kernel_rooflines[kind] = {"achieved_gbs": gbs, "frac": gbs / peak, "ms_per_frame": k_ms / reps}
     profile_summary = {k: {"ms_per_frame": v[0] / reps, "launches_per_frame": v[1] / reps} for k, v in prof.items() if v[1]}
 
     # end to end through the C-ABI with host buffers: every frame the pin
@@ -691,6 +829,19 @@ def main():
 
     plain = time_plain(native, scs, args.plain_frames) if batched and args.plain_frames > 0 else None
     plain_serial = time_plain_serial(native, scs) if batched and args.plain_frames > 0 else None
+    launch_cfg = solver.launch_config()
+    solver.close()
+    extras = {}
+    if args.extras and rank == 0:
+        extras["reference_gpu"] = time_reference_gpu(scs, max(args.plain_frames, 1), torch) if batched else None
+        extras["plain32"] = time_single(native, torch, "plain32", 50, args.warmup)
+        extras["drop10k"] = time_single(native, torch, "drop10k", 50, args.warmup)
+        extras["diff"] = diff_measure(3, 1, torch)
+        st, _ = serve_measure(args.serve_seconds, args.serve_budget_gb, args.serve_latency_ms, args.warmup, 0, torch)
+        extras["serving"] = {"value": st["throughput"], "unit": METRIC, "workload": DESCRIPTIONS["serve"],
+                             "seconds": args.serve_seconds, "frame_latency_target_ms": args.serve_latency_ms,
+                             "frame_latency_ms_p50": st["frame_latency_ms_p50"],
+                             "frame_latency_ms_p99": st["frame_latency_ms_p99"], "stats": st}
 
     if rank != 0:
         return
@@ -705,14 +856,22 @@ def main():
         "e2e": e2e, "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks.summary(),
         "roofline": roof, "kernel_profile": profile_summary, "work_counters_per_frame": {k: (c / reps if k in summed else c) for k, c in counters.items()},
         "cpu_baseline": {"value": cpu_value, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
-        "launch_config": {"config": solver.launch_config(), "autotune": tuned},
+        "launch_config": {"config": launch_cfg, "autotune": tuned},
     }
+    line["kernel_rooflines"] = kernel_rooflines
     if plain is not None:
         line["plain"] = plain
         line["batched_over_plain"] = value / plain["value"]
     if plain_serial is not None:
         line["plain_serial"] = plain_serial
         line["batched_over_plain_serial"] = value / plain_serial["value"]
+    for k, v in extras.items():
+        if v is not None:
+            line[k] = v
+    ref = extras.get("reference_gpu")
+    if ref and "value" in ref:
+        line["batched_over_reference_plain"] = value / ref["value"]
+        line["e2e_over_reference_plain"] = e2e["value"] / ref["value"]
     print(json.dumps(line), flush=True)
 
 

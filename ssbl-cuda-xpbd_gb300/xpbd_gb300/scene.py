@@ -122,10 +122,23 @@ def edge_constraints(triangles: np.ndarray, rest: np.ndarray) -> tuple[np.ndarra
     return pairs, np.maximum(np.linalg.norm(delta, axis=1), _EPS)
 
 
+def set_native_prep(enabled: bool) -> None:
+    """Whether the builders may call the library's host-side preprocessing
+    (greedy colouring, bend pairs); off, they use only the Python
+    restatement, and this module loads no native library (the benchmark's
+    reference arm runs that way)."""
+    global _PREP, _PREP_ENABLED
+    _PREP_ENABLED = bool(enabled)
+    _PREP = None
+_PREP_ENABLED = True
+
+
 def _native_prep():
     """The library's host-side preprocessing entry points, when it is built
     (same results as the Python loops below, which remain the restatement)."""
     global _PREP
+    if not _PREP_ENABLED:
+        return None
     if _PREP is None:
         try:
             import ctypes
@@ -553,20 +566,28 @@ def _unpinned_grid(n: int, z: float, side: float = 1.0) -> ClothData:
     return _GRID_CACHE[key]
 
 
-def batched_scenes(count: int = 256, seed: int = 0, frames: int = 120, side_range: tuple = (16, 128)) -> list[Scene]:
+def batched_scenes(count: int = 256, seed: int = 0, frames: int = 120, side_range: tuple = (16, 128),
+                   only=None) -> list[Scene]:
     """Independent cloths of uneven sizes for the batched form: side drawn
     uniformly from `side_range` vertices (1 m cloths at z = 0.5), stretch and
     bend compliance each log-uniform in [1e-8, 1e-4], 2-8 random hard pins,
     self collision fast or strict with probability 0.5 (2 mm thickness), a
     sphere (r = 0.3 m) below and the ground at z = -1; 10 substeps x 2
-    iterations."""
+    iterations.  `only` (cloth indices) builds just those cloths of the same
+    seeded set."""
     rng = np.random.default_rng(seed)
+    keep = None if only is None else set(int(k) for k in only)
     out = []
     for k in range(count):
         n = int(rng.integers(side_range[0], side_range[1] + 1))
-        base = _unpinned_grid(n, 0.5)
         V = n * n
         pins = np.sort(rng.choice(V, size=int(rng.integers(2, 9)), replace=False)).astype(np.int32)
+        if keep is not None and k not in keep:
+            rng.uniform(-8.0, -4.0)
+            rng.uniform(-8.0, -4.0)
+            rng.random()
+            continue
+        base = _unpinned_grid(n, 0.5)
         inv = base.inv_mass.copy()
         inv[pins] = 0.0
         cloth = ClothData(

@@ -20,6 +20,16 @@ every kernel); a cohort's memory returns to the budget when its last request
 finishes.  A cloth's result does not depend on the cohort it runs in: each
 cloth of a batched solver is stepped exactly as it is stepped alone.
 
+Latency-aware admission.  A request's frame latency is the duration of the
+tick that advances it, and a tick advances every resident request, so the
+tick time follows the resident work (vertex-substeps per tick) divided by
+the device's throughput.  With ``frame_latency_ms`` set, a request is
+admitted only while the resident work plus its own stays within the work one
+tick can do in that time at the throughput measured over recent ticks
+(exponential average of vertex-substeps per second of tick time, seeded by
+``rate_guess``); the rest waits in the queue in arrival order.  Without a
+target, admission is by device memory alone.
+
 The solver back end is injectable (``backend``) so the scheduling logic can
 be exercised without a GPU.
 """
@@ -150,8 +160,12 @@ class ServingEngine:
     """Continuous-batching request loop under a device-memory budget."""
 
     def __init__(self, hbm_budget_bytes: int, group_below: int = 50_000, max_cohort_vertices: int = 2_000_000,
-                 max_admit_per_tick: int = 64, backend=None, clock=time.perf_counter, workers: int = 4):
+                 max_admit_per_tick: int = 64, backend=None, clock=time.perf_counter, workers: int = 4,
+                 frame_latency_ms: float | None = None, rate_guess: float = 2.0e8):
         self.budget = int(hbm_budget_bytes)
+        self.frame_latency_ms = frame_latency_ms
+        self.rate = float(rate_guess)     # vertex-substeps per second of tick time (measured)
+        self.resident_work = 0            # vertex-substeps per tick of admitted requests
         self.workers = workers
         self.pool = None
         if workers > 0:
@@ -202,6 +216,7 @@ class ServingEngine:
             self.backend.close(c.solver)
         self.cohorts = []
         self.used_bytes = 0
+        self.resident_work = 0
         if self.pool is not None:
             self.pool.shutdown(wait=True)
             self.pool = None
@@ -219,6 +234,7 @@ class ServingEngine:
             starts.append(self.clock())
             self.backend.step(c.solver, c.substeps, c.iterations)
         finished = []
+        tick_work = 0
         for c, t_launch in zip(self.cohorts, starts):
             self.backend.wait(c.solver)
             lat = (self.clock() - t_launch) * 1000.0
@@ -227,9 +243,14 @@ class ServingEngine:
                     continue
                 c.done[k] += 1
                 c.latency[k].append(lat)
-                self.completed_vertex_substeps += len(r.cloth.positions_world) * r.substeps
+                work = len(r.cloth.positions_world) * r.substeps
+                self.completed_vertex_substeps += work
+                tick_work += work
                 if c.done[k] >= r.frames:
                     finished.append(self._retire(c, k))
+        tick_s = self.clock() - starts[0]
+        if tick_work > 0 and tick_s > 0:
+            self.rate = 0.8 * self.rate + 0.2 * (tick_work / tick_s)
         for c in [c for c in self.cohorts if not any(c.live)]:
             self.backend.close(c.solver)
             self.used_bytes -= c.bytes
@@ -280,6 +301,8 @@ class ServingEngine:
             "queue_delay_s_p99": float(np.percentile(queue_delay, 99)) if queue_delay else None,
             "peak_device_bytes": self.peak_bytes,
             "budget_bytes": self.budget,
+            "frame_latency_target_ms": self.frame_latency_ms,
+            "measured_rate": self.rate,
             "results": results,
         }
 
@@ -290,13 +313,18 @@ class ServingEngine:
         share a cohort."""
         admitted: list[ClothRequest] = []
         reserve = 0
+        work_cap = None if self.frame_latency_ms is None else self.rate * self.frame_latency_ms / 1000.0
         while self.queue and len(admitted) < self.max_admit_per_tick:
             need = estimate_device_bytes(self.queue[0])
             if self.used_bytes + reserve + need > self.budget:
                 if not self.cohorts and not self.building and not admitted and reserve == 0:
                     raise MemoryError(f"request {self.queue[0].request_id} needs {need} bytes, over the whole budget")
                 break
+            work = len(self.queue[0].cloth.positions_world) * self.queue[0].substeps
+            if work_cap is not None and self.resident_work > 0 and self.resident_work + work > work_cap:
+                break  # one tick would take longer than the frame-latency target
             reserve += need
+            self.resident_work += work
             admitted.append(self.queue.popleft())
         if not admitted:
             return
@@ -361,6 +389,7 @@ class ServingEngine:
 
     def _retire(self, c: _Cohort, k: int) -> RequestResult:
         r = c.reqs[k]
+        self.resident_work -= len(r.cloth.positions_world) * r.substeps
         pos = self.backend.download(c.solver, k, c.batched)
         self.backend.deactivate(c.solver, k, c.batched)
         c.live[k] = False

@@ -149,3 +149,58 @@ def test_serving_request_mix_shapes():
     for r in reqs:
         assert 30 <= r.frames <= 240
         assert 900 <= len(r.cloth.positions_world) <= 5500
+
+
+class WorkClock:
+    """Engine clock that advances only while a cohort's frame runs: by its
+    work (vertex-substeps) over a fixed device rate."""
+
+    def __init__(self, rate):
+        self.t, self.rate = 0.0, rate
+
+    def __call__(self):
+        return self.t
+
+
+class TimedBackend(FakeBackend):
+    def __init__(self, clock):
+        super().__init__()
+        self.clock = clock
+        self.max_resident = 0
+
+    def wait(self, solver):
+        live = [r for r, a in zip(solver.reqs, solver.active) if a]
+        self.clock.t += sum(len(r.cloth.positions_world) * r.substeps for r in live) / self.clock.rate
+
+    def step(self, solver, substeps, iterations):
+        super().step(solver, substeps, iterations)
+
+
+def test_latency_target_bounds_resident_work():
+    """With a frame-latency target the engine keeps the resident work per
+    tick within what the measured rate does in that time: 1,600-vertex
+    requests at 10 substeps take 10 ms each at the fake device's rate, so a
+    35 ms target keeps at most three resident and every frame within it,
+    while all requests still complete in arrival order."""
+    clock = WorkClock(rate=1.6e6)
+    be = TimedBackend(clock)
+    reqs = [_req(k, 40, 4) for k in range(9)]
+    eng = ServingEngine(hbm_budget_bytes=1 << 40, backend=be, clock=clock, workers=0, frame_latency_ms=35.0,
+                        rate_guess=1.6e6, max_admit_per_tick=64)
+    for r in reqs:
+        eng.submit(r)
+    results, resident = [], []
+    while not eng.idle():
+        results += eng.tick()
+        resident.append(eng.live_requests)
+    assert max(resident) <= 3
+    assert sorted(r.request_id for r in results) == list(range(9))
+    lat = [x for r in results for x in r.frame_latency_ms]
+    assert max(lat) <= 35.0 + 1e-6
+    # without a target the memory budget alone admits everything at once
+    clock2 = WorkClock(rate=1.6e6)
+    eng2 = ServingEngine(hbm_budget_bytes=1 << 40, backend=TimedBackend(clock2), clock=clock2, workers=0)
+    for r in [_req(k, 40, 4) for k in range(9)]:
+        eng2.submit(r)
+    eng2.tick()
+    assert eng2.live_requests == 9
