@@ -48,6 +48,21 @@ class Rollout:
         e = np.asarray(cloth.edges, np.int64).reshape(-1, 2)
         self.ei, self.ej = torch.as_tensor(e[:, 0], device=device), torch.as_tensor(e[:, 1], device=device)
         self.erest = t(cloth.edge_rest_lengths)
+        # every vertex's incident edges (edge index, endpoint side) padded to
+        # the largest degree: the stretch pass sums a vertex's corrections in
+        # this fixed order, so the rollout is deterministic on any device
+        # (an atomic index_add on a GPU sums in arrival order)
+        V = len(cloth.positions_world)
+        verts = np.concatenate([e[:, 0], e[:, 1]])
+        slots = np.concatenate([np.arange(len(e)), np.arange(len(e)) + len(e)])  # i side: k, j side: E + k
+        order = np.lexsort((slots, verts))
+        verts, slots = verts[order], slots[order]
+        deg = np.bincount(verts, minlength=V)
+        width = max(int(deg.max()) if len(deg) else 0, 1)
+        rank = np.arange(len(verts)) - np.repeat(np.cumsum(deg) - deg, deg)
+        inc = np.full((V, width), 2 * len(e), np.int64)  # padding points at a zero row
+        inc[verts, rank] = slots
+        self.inc = torch.as_tensor(inc, device=device)
         b = np.asarray(cloth.bends, np.int64).reshape(-1, 2)
         self.bi, self.bj = torch.as_tensor(b[:, 0], device=device), torch.as_tensor(b[:, 1], device=device)
         self.brest = t(cloth.bend_rest_lengths)
@@ -82,8 +97,10 @@ class Rollout:
         di = -corr * wi[:, None]
         dj = corr * wj[:, None]
         kp = torch.where(c > 0, torch.full_like(c, 0.08), torch.zeros_like(c))[..., None]
-        p = p.index_add(-2, self.ei, di).index_add(-2, self.ej, dj)
-        prev = prev.index_add(-2, self.ei, di * kp).index_add(-2, self.ej, dj * kp)
+        both = torch.cat([di, dj, torch.zeros_like(di[..., :1, :])], -2)  # (..., 2E + 1, 3)
+        both_prev = torch.cat([di * kp, dj * kp, torch.zeros_like(di[..., :1, :])], -2)
+        p = p + both[..., self.inc, :].sum(-2)
+        prev = prev + both_prev[..., self.inc, :].sum(-2)
         return p, prev
 
     def _bends(self, p, prev, k, dt):
