@@ -332,12 +332,69 @@ XG_EXPORT int xpbd_gb300_build_self_structures(void* handle) {
         self_build_triangle_hash(v, sv, S->nTB, 1, S->stream);
     }
     if (S->nEB > 0) {
-        cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, S->stream);
-        self_build_edge_hash(v, sv, S->nEB, 1, S->stream);
+        View ev = v;  // the edge hash lists its buckets of more than 32 members in trim segment 2
+        const size_t trim_seg = (size_t)std::max(std::max(S->nVB, S->nTB), S->nEB);
+        ev.trim_list = S->trim_list + 2 * trim_seg;
+        ev.trim_count = S->trim_count + 2;
+        reset_edge_hash(S, S->stream);
+        self_build_edge_hash(ev, sv, S->nEB, 3, S->stream);
     }
     self_neighbors(v, 0, sv, S->stream);
     return (cuda_ok(cudaGetLastError(), "build self structures") && cuda_ok(cudaStreamSynchronize(S->stream), "build self structures")) ? 1 : 0;
 }
+
+namespace {
+
+// The edge hash as a bucket CSR (start[nEB + 1], then the members bucket
+// after bucket), as the triangle and vertex hashes are kept: a bucket of up
+// to kEdgeSlots members lists its slots (a bucket of more than 32 with its 32
+// smallest ids first, in increasing order), a larger one its full member
+// list in increasing id order.
+long long read_edge_buckets(Solver* S, bool starts, void* out, long long max_bytes) {
+    const size_t nb = (size_t)S->nEB;
+    std::vector<int> cnt(nb), first(nb);
+    if (!cuda_ok(cudaStreamSynchronize(S->stream), "read edge hash") ||
+        !cuda_ok(cudaMemcpy(cnt.data(), S->eb_count, sizeof(int) * nb, cudaMemcpyDeviceToHost), "read edge hash") ||
+        !cuda_ok(cudaMemcpy(first.data(), S->eb_start, sizeof(int) * nb, cudaMemcpyDeviceToHost), "read edge hash"))
+        return -1;
+    std::vector<int> start(nb + 1, 0);
+    for (size_t b = 0; b < nb; ++b) start[b + 1] = start[b] + cnt[b];
+    if (starts) {
+        const long long bytes = 4ll * (long long)(nb + 1);
+        if (bytes > max_bytes) {
+            fail("output buffer too small");
+            return -1;
+        }
+        std::memcpy(out, start.data(), (size_t)bytes);
+        return bytes;
+    }
+    const long long bytes = 4ll * start[nb];
+    if (bytes > max_bytes) {
+        fail("output buffer too small");
+        return -1;
+    }
+    std::vector<int> slots(nb * kEdgeSlots);
+    std::vector<int> all(std::max(start[nb], 1));
+    if (!cuda_ok(cudaMemcpy(slots.data(), S->eb_slot, sizeof(int) * slots.size(), cudaMemcpyDeviceToHost), "read edge hash") ||
+        (start[nb] > 0 && !cuda_ok(cudaMemcpy(all.data(), S->eb_ent, sizeof(int) * (size_t)start[nb], cudaMemcpyDeviceToHost),
+                                   "read edge hash")))
+        return -1;
+    int* o = static_cast<int*>(out);
+    for (size_t b = 0; b < nb; ++b) {
+        const int n = cnt[b];
+        int* dst = o + start[b];
+        if (n <= kEdgeSlots) {
+            std::memcpy(dst, slots.data() + b * kEdgeSlots, sizeof(int) * (size_t)n);
+        } else {
+            // overflow region [eb_start[b] - n, eb_start[b]) of the last build
+            std::memcpy(dst, all.data() + (first[b] - n), sizeof(int) * (size_t)n);
+            std::sort(dst, dst + n);
+        }
+    }
+    return bytes;
+}
+
+}  // namespace
 
 XG_EXPORT long long xpbd_gb300_read_buffer(void* handle, int id, void* out, long long max_bytes) {
     g_error.clear();
@@ -348,15 +405,17 @@ XG_EXPORT long long xpbd_gb300_read_buffer(void* handle, int id, void* out, long
     }
     const void* src = nullptr;
     long long bytes = 0;
-    int total_t = 0, total_e = 0;
-    if ((id == XPBD_BUF_TRI_BUCKET_ENTRIES && S->tb_start) || (id == XPBD_BUF_EDGE_BUCKET_ENTRIES && S->eb_start)) {
-        const int* st = id == XPBD_BUF_TRI_BUCKET_ENTRIES ? S->tb_start : S->eb_start;
-        const int nb = id == XPBD_BUF_TRI_BUCKET_ENTRIES ? S->nTB : S->nEB;
+    int total_t = 0;
+    if ((id == XPBD_BUF_EDGE_BUCKET_START || id == XPBD_BUF_EDGE_BUCKET_ENTRIES) && S->eb_slot)
+        return read_edge_buckets(S, id == XPBD_BUF_EDGE_BUCKET_START, out, max_bytes);
+    if (id == XPBD_BUF_TRI_BUCKET_ENTRIES && S->tb_start) {
+        const int* st = S->tb_start;
+        const int nb = S->nTB;
         int total = 0;
         if (!cuda_ok(cudaStreamSynchronize(S->stream), "read bucket total") ||
             !cuda_ok(cudaMemcpy(&total, st + nb, sizeof(int), cudaMemcpyDeviceToHost), "read bucket total"))
             return -1;
-        (id == XPBD_BUF_TRI_BUCKET_ENTRIES ? total_t : total_e) = total;
+        total_t = total;
     }
     const Params& P0 = S->hp[0];
     switch (id) {
@@ -368,8 +427,8 @@ XG_EXPORT long long xpbd_gb300_read_buffer(void* handle, int id, void* out, long
         case XPBD_BUF_VERTEX_BUCKET_ENTRIES: src = S->vb_ent; bytes = 4ll * S->nV; break;
         case XPBD_BUF_TRI_BUCKET_START: src = S->tb_start; bytes = 4ll * (S->nTB + 1); break;
         case XPBD_BUF_TRI_BUCKET_ENTRIES: src = S->tb_ent; bytes = 4ll * total_t; break;
-        case XPBD_BUF_EDGE_BUCKET_START: src = S->eb_start; bytes = 4ll * (S->nEB + 1); break;
-        case XPBD_BUF_EDGE_BUCKET_ENTRIES: src = S->eb_ent; bytes = 4ll * total_e; break;
+        case XPBD_BUF_EDGE_BUCKET_START:
+        case XPBD_BUF_EDGE_BUCKET_ENTRIES: src = nullptr; bytes = 0; break;  // no edge hash
         case XPBD_BUF_NEIGHBOR_COUNTS: src = S->nb_count; bytes = 4ll * S->nV; break;
         case XPBD_BUF_NEIGHBOR_INDICES: src = S->nb_idx; bytes = 4ll * S->nV * kNeighborSlots; break;
         case XPBD_BUF_STATIC_SDF:
@@ -513,16 +572,20 @@ XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out) {
     Solver* S = as_solver(handle);
     if (!S || !out) return fail("invalid profile counter request") ? 1 : 0;
     unsigned long long c[kPerfSlots];
-    int entries[2] = {0, 0};  // the scans' totals: entries of the last build of each hash
+    int entries[1] = {0};  // the triangle hash scan's total: entries of its last build
     if (!cuda_ok(cudaMemcpyAsync(c, S->perf, sizeof(c), cudaMemcpyDeviceToHost, S->stream), "read work counters") ||
         (S->tb_start && S->nTB > 0 &&
          !cuda_ok(cudaMemcpyAsync(&entries[0], S->tb_start + S->nTB, sizeof(int), cudaMemcpyDeviceToHost, S->stream),
                   "read triangle hash size")) ||
-        (S->eb_start && S->nEB > 0 &&
-         !cuda_ok(cudaMemcpyAsync(&entries[1], S->eb_start + S->nEB, sizeof(int), cudaMemcpyDeviceToHost, S->stream),
-                  "read edge hash size")) ||
         !cuda_ok(cudaStreamSynchronize(S->stream), "read work counters"))
         return 0;
+    long long edge_entries = 0;  // the edge hash keeps counts, not starts: their sum
+    if (S->eb_count && S->nEB > 0) {
+        std::vector<int> cnt((size_t)S->nEB);
+        if (!cuda_ok(cudaMemcpy(cnt.data(), S->eb_count, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost), "read edge hash size"))
+            return 0;
+        for (int x : cnt) edge_entries += x;
+    }
     for (int k = 0; k < kPerfSlots; ++k) out[k] = (long long)c[k];
     long long tris = 0, edges = 0;
     for (const Params& P : S->hp) {
@@ -531,7 +594,7 @@ XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out) {
         if (P.ehash) edges += P.E;
     }
     out[4] = entries[0];
-    out[5] = entries[1];
+    out[5] = edge_entries;
     out[6] = tris;
     out[7] = edges;
     out[8] = S->nTB;

@@ -307,6 +307,15 @@ void release_grid(Solver* S, Cloth& c) {
 
 }  // namespace
 
+// Zero what the slotted edge hash counts from: bucket counts, overflow bits
+// and list, and the edge hash's trim list (segment 2).
+void reset_edge_hash(Solver* S, cudaStream_t s) {
+    cudaMemsetAsync(S->eb_count, 0, sizeof(int) * (size_t)S->nEB, s);
+    cudaMemsetAsync(S->eb_ovf_bits, 0, sizeof(unsigned) * (((size_t)S->nEB + 31) / 32), s);
+    cudaMemsetAsync(S->eb_ovf_count, 0, sizeof(int), s);
+    cudaMemsetAsync(S->trim_count + 2, 0, sizeof(int), s);
+}
+
 View Solver::view() const {
     View v{};
     v.tune = tune;
@@ -358,6 +367,10 @@ View Solver::view() const {
     v.eb_count = eb_count;
     v.eb_start = eb_start;
     v.eb_ent = eb_ent;
+    v.eb_slot = eb_slot;
+    v.eb_ovf_bits = eb_ovf_bits;
+    v.eb_ovf_list = eb_ovf_list;
+    v.eb_ovf_count = eb_ovf_count;
     v.nb_count = nb_count;
     v.nb_idx = nb_idx;
     v.scan_tmp = scan_tmp;
@@ -424,6 +437,10 @@ void free_solver(Solver* S) {
     dfree(S->eb_count);
     dfree(S->eb_start);
     dfree(S->eb_ent);
+    dfree(S->eb_slot);
+    dfree(S->eb_ovf_bits);
+    dfree(S->eb_ovf_list);
+    dfree(S->eb_ovf_count);
     dfree(S->nb_count);
     dfree(S->nb_idx);
     dfree(S->acc);
@@ -1265,10 +1282,17 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
             ok = dalloc(&S->tb_count, S->nTB, "self triangle hash count allocation") &&
                  dalloc(&S->tb_start, S->nTB + 1, "self triangle hash start allocation") &&
                  dalloc(&S->tb_ent, (size_t)tri_entries, "self triangle hash index allocation");
-        if (ok && S->nEB > 0)
+        if (ok && S->nEB > 0) {
+            // a bucket past kEdgeSlots members holds at least kEdgeSlots + 1 entries
+            S->eb_ovf_cap = std::min<long long>(S->nEB, edge_entries / (kEdgeSlots + 1) + 1);
             ok = dalloc(&S->eb_count, S->nEB, "self edge hash count allocation") &&
                  dalloc(&S->eb_start, S->nEB + 1, "self edge hash start allocation") &&
-                 dalloc(&S->eb_ent, (size_t)edge_entries, "self edge hash index allocation");
+                 dalloc(&S->eb_ent, (size_t)edge_entries, "self edge hash index allocation") &&
+                 dalloc(&S->eb_slot, (size_t)S->nEB * kEdgeSlots, "self edge hash slot allocation") &&
+                 dalloc(&S->eb_ovf_bits, ((size_t)S->nEB + 31) / 32, "self edge hash overflow allocation") &&
+                 dalloc(&S->eb_ovf_list, (size_t)S->eb_ovf_cap, "self edge hash overflow allocation") &&
+                 dalloc(&S->eb_ovf_count, 1, "self edge hash overflow allocation");
+        }
     }
     // Hard-stretch buffers.  The caps follow the caller's edge colouring when
     // one is given (edges already sorted by colour; each pass sweeps the
@@ -1746,8 +1770,7 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                     });
                 if (sp.ehash)
                     timed(kKEdgeHash, 6, [&] {
-                        cudaMemsetAsync(S->eb_count, 0, sizeof(int) * S->nEB, lane_stream(2));
-                        cudaMemsetAsync(S->trim_count + 2, 0, sizeof(int), lane_stream(2));
+                        reset_edge_hash(S, lane_stream(2));
                         self_build_edge_hash(hv[2], sp.sv, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
                     });
                 join();

@@ -298,6 +298,9 @@ struct Solver {
     int *vb_count = nullptr, *vb_start = nullptr, *vb_ent = nullptr;
     int *tb_count = nullptr, *tb_start = nullptr, *tb_ent = nullptr;
     int *eb_count = nullptr, *eb_start = nullptr, *eb_ent = nullptr;
+    int *eb_slot = nullptr, *eb_ovf_list = nullptr, *eb_ovf_count = nullptr;
+    unsigned* eb_ovf_bits = nullptr;
+    long long eb_ovf_cap = 0;  // entries of eb_ovf_list
     int* nb_count = nullptr;
     int* nb_idx = nullptr;
     int* scan_tmp = nullptr;  // three segments: vertex, triangle, edge hash scans
@@ -344,6 +347,7 @@ struct Solver {
 // Returns nullptr with g_error set on failure.
 Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes, int count);
 void free_solver(Solver* S);
+void reset_edge_hash(Solver* S, cudaStream_t s);
 
 // Cloth-level updates; cloth < 0 applies to every cloth (pins then take
 // indices over the concatenated vertices).

@@ -5,14 +5,18 @@
 //
 // Hash layout.  The reference inserts primitives into fixed 32-slot buckets
 // with atomicAdd slot counters, so bucket contents depend on thread timing.
-// Here each hash is a counting sort over the bucket id: count entries per
-// bucket, exclusive-scan the counts into bucket starts, scatter the entries
-// with atomic cursors, then sort each bucket's ids so that its first
+// Here the vertex and triangle hashes are a counting sort over the bucket id
+// (count entries per bucket, exclusive-scan the counts into bucket starts,
+// scatter the entries with atomic cursors), and the edge hash, by far the
+// largest (about 20 cells per edge), keeps 64 member slots per bucket filled
+// in one atomic pass (k_edge_insert; larger buckets get overflow regions).
+// Either way each bucket's ids are then ordered so that its first
 // min(count, 32) members are the 32 smallest primitive ids in increasing
-// order.  Queries read exactly those members, which makes candidate order,
-// the 32-slot caps and the fast-mode cluster filter deterministic.  Bucket
-// ids, cell coordinates, pre-clamp counts and member multisets are the same
-// integers as the reference's when no bucket overflows.
+// order where a query reads order.  Queries read exactly those members,
+// which makes candidate order, the 32-slot caps and the fast-mode cluster
+// filter deterministic.  Bucket ids, cell coordinates, pre-clamp counts and
+// member multisets are the same integers as the reference's when no bucket
+// overflows.
 //
 // Accumulation.  Pushes are scattered into per-vertex fixed-point int64
 // accumulators (2^-32 m units) with integer atomics, so the per-vertex sums do
@@ -190,19 +194,17 @@ __global__ void k_vhash_scatter(View v) {
     v.vb_ent[atomicAdd(&v.vb_count[b], 1)] = i;
 }
 
-// L threads per primitive (4, 8 or 16, a tile choice of the autotuner;
-// default 8): thread r of primitive k walks the x rows r, r + L, ... of its
-// cell box (at most 64 cells; rows indexed over (y, z)),
-// so the cell coordinates come from one division per row rather than per
-// cell.  `scatter` = false counts entries per bucket; true writes them
-// through the cursors left by the scan.  Entry order within a bucket is
-// fixed afterwards by k_bucket_sort where a query depends on it.
-
-
-// Collapsed ranges are counted as guard events in the count pass, once per
-// primitive: a ballot per warp, a sum per block (every thread reaches both).
-template <bool kTri, int L>
-__global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
+// Triangle hash.  L threads per triangle (1, 2, 4, 8 or 16, a tile choice of
+// the autotuner): thread r of triangle k walks the x rows r, r + L, ... of
+// its cell box (at most 64 cells; rows indexed over (y, z)), so the cell
+// coordinates come from one division per row rather than per cell.
+// `scatter` = false counts entries per bucket; true writes them through the
+// cursors left by the scan.  Entry order within a bucket is fixed afterwards
+// by k_bucket_sort where a query depends on it.  Collapsed ranges are counted
+// as guard events in the count pass, once per triangle: a ballot per warp, a
+// sum per block (every thread reaches both).
+template <int L>
+__global__ void __launch_bounds__(kThreads) k_tri_hash(View v, bool scatter) {
     __shared__ unsigned collapsed_s;  // the block's collapsed ranges: one global atomic per block
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = v.lo + (int)(t / L), r0 = (int)(t % L);
@@ -210,22 +212,18 @@ __global__ void __launch_bounds__(kThreads) k_prim_hash(View v, bool scatter) {
     __syncthreads();
     bool collapsed = false;
     if (k < v.hi) {
-        const Params& P = kTri ? params_t(v, k) : params_e(v, k);
-        if ((kTri ? P.thash : P.ehash) && self_scheduled(P, v)) {
+        const Params& P = params_t(v, k);
+        if (P.thash && self_scheduled(P, v)) {
             bool ok = false;
-            const CellRange r = kTri ? tri_cells(v, P, k, &ok, &collapsed) : edge_cells(v, P, k, &ok, &collapsed);
+            const CellRange r = tri_cells(v, P, k, &ok, &collapsed);
             const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
             if (ok && nx > 0 && ny > 0 && nz > 0) {
-                int* cnt = kTri ? v.tb_count : v.eb_count;
-                int* ent = kTri ? v.tb_ent : v.eb_ent;
-                const int nb = kTri ? P.tbuckets : P.ebuckets;
-                const int base = kTri ? P.tbase : P.ebase;
                 for (int row = r0; row < ny * nz; row += L) {
                     const int y = r.y0 + row % ny, z = r.z0 + row / ny;
                     for (int x = r.x0; x <= r.x1; ++x) {
-                        int* slot_counter = &cnt[base + (int)bucket_of(x, y, z, nb)];
+                        int* slot_counter = &v.tb_count[P.tbase + (int)bucket_of(x, y, z, P.tbuckets)];
                         if (scatter)
-                            ent[atomicAdd(slot_counter, 1)] = k;
+                            v.tb_ent[atomicAdd(slot_counter, 1)] = k;
                         else
                             atomicAdd(slot_counter, 1);  // no return value needed: a reduction
                     }
@@ -344,6 +342,178 @@ void scan_counts(int* counts, int* start, int n, int* block_sums, unsigned long 
 
 __device__ __forceinline__ int warp_global_id() { return (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); }
 
+// ------------------------------------------------- edge hash (slotted) --
+// The edge hash keeps each bucket's members in kEdgeSlots slots of its own
+// (bucket b's at b * kEdgeSlots), filled in a single pass: an insertion takes
+// the next slot from the bucket's counter, so the counts come from the same
+// atomics that place the members, with no count pass and no scan.  A bucket
+// whose count passes the 32 query slots is listed for ordering (its 32
+// smallest ids first, in increasing order: queries read no further); one that
+// passes kEdgeSlots is listed as an overflow, and its full member list is
+// rebuilt from a second walk of the cells into a region of its own (rare:
+// a fold or crumple that packs more than 64 edge boxes into one bucket).
+// Every insertion past the 32 query slots counts as an overflow guard event,
+// as the reference counts an insertion into a full bucket (abi41.cu:5584-
+// 5590), and so does a collapsed cell range.  Members end up where the
+// reference's 32 slots would hold the same multiset whenever no bucket
+// passes 32 (abi41.cu:5532-5593).
+
+// Walks edge k's cells (rows r0, r0 + L, ... of its box) and calls f(bucket)
+// for each; nothing when the edge is not hashed in this substep or pass.
+template <int L, class F>
+__device__ __forceinline__ void edge_cells_walk(const View& v, int k, int r0, bool* collapsed, F&& f) {
+    const Params& P = params_e(v, k);
+    if (!P.ehash || !self_scheduled(P, v)) return;
+    bool ok = false;
+    const CellRange r = edge_cells(v, P, k, &ok, collapsed);
+    const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
+    if (!ok || nx <= 0 || ny <= 0 || nz <= 0) return;
+    for (int row = r0; row < ny * nz; row += L) {
+        const int y = r.y0 + row % ny, z = r.z0 + row / ny;
+        for (int x = r.x0; x <= r.x1; ++x) f(P.ebase + (int)bucket_of(x, y, z, P.ebuckets));
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(kThreads) k_edge_insert(View v) {
+    __shared__ unsigned guard_s;  // the block's guard events: one global atomic per block
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = v.lo + (int)(t / L), r0 = (int)(t % L);
+    if (threadIdx.x == 0) guard_s = 0u;
+    __syncthreads();
+    bool collapsed = false;
+    unsigned past = 0u;
+    if (k < v.hi) {
+        edge_cells_walk<L>(v, k, r0, &collapsed, [&](int b) {
+            const int slot = atomicAdd(&v.eb_count[b], 1);
+            if (slot < kEdgeSlots) v.eb_slot[edge_bucket_base(b) + slot] = k;
+            if (slot >= kBucketSlots) {
+                ++past;
+                if (slot == kBucketSlots) v.trim_list[atomicAdd(v.trim_count, 1)] = b;
+                if (slot == kEdgeSlots) {
+                    v.eb_ovf_list[atomicAdd(v.eb_ovf_count, 1)] = b;
+                    atomicOr(&v.eb_ovf_bits[b >> 5], 1u << (b & 31));
+                }
+            }
+        });
+    }
+    const unsigned events = __reduce_add_sync(0xffffffffu, past + ((collapsed && r0 == 0) ? 1u : 0u));
+    if ((threadIdx.x & 31) == 0 && events) atomicAdd(&guard_s, events);
+    __syncthreads();
+    if (threadIdx.x == 0 && guard_s) count_add(v.counts, kCntSelfOverflow, (unsigned long long)guard_s);
+}
+
+// Overflow regions: each listed bucket gets [start, start + count) of eb_ent,
+// in list order; eb_start[b] then serves as the region's fill cursor.  One
+// block; nothing to do in the usual build without overflow.
+__global__ void __launch_bounds__(1024) k_edge_ovf_offsets(View v) {
+    __shared__ int ws[32];
+    __shared__ int carry;
+    const int n = *v.eb_ovf_count;
+    if (n == 0) return;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += kScanTile) {
+        int vals[4];
+        const int i0 = base + threadIdx.x * 4;
+        for (int q = 0; q < 4; ++q) vals[q] = i0 + q < n ? v.eb_count[v.eb_ovf_list[i0 + q]] : 0;
+        int total;
+        int run = carry + block_exclusive_scan4(vals, ws, &total);
+        for (int q = 0; q < 4; ++q) {
+            if (i0 + q < n) v.eb_start[v.eb_ovf_list[i0 + q]] = run;
+            run += vals[q];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+}
+
+// Second walk, only when some bucket overflowed: every insertion into an
+// overflowing bucket is written to that bucket's region.  A fixed grid
+// striding over the edges, so the usual build without overflow pays for a
+// few hundred blocks that exit at once.
+template <int L>
+__global__ void __launch_bounds__(kThreads) k_edge_ovf_collect(View v) {
+    if (*v.eb_ovf_count == 0) return;
+    const long long threads = (long long)gridDim.x * blockDim.x;
+    const long long items = (long long)(v.hi - v.lo) * L;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += threads) {
+        const int k = v.lo + (int)(t / L), r0 = (int)(t % L);
+        bool collapsed = false;
+        edge_cells_walk<L>(v, k, r0, &collapsed, [&](int b) {
+            if ((__ldg(&v.eb_ovf_bits[b >> 5]) >> (b & 31)) & 1u) v.eb_ent[atomicAdd(&v.eb_start[b], 1)] = k;
+        });
+    }
+}
+
+// The 32 smallest ids (with multiplicity) of each overflowing bucket's region,
+// in increasing order, into its first 32 slots: one warp per bucket, 32
+// rounds of a warp-wide minimum above the last value taken.
+__global__ void __launch_bounds__(kThreads) k_edge_ovf_select(View v) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
+    const int total = *v.eb_ovf_count;
+    for (int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); w < total; w += warps) {
+        const int b = v.eb_ovf_list[w];
+        const int n = v.eb_count[b];
+        const int* e = v.eb_ent + (v.eb_start[b] - n);
+        int* out = v.eb_slot + edge_bucket_base(b);
+        long long last = -1;  // ids are >= 0
+        int filled = 0;
+        while (filled < kBucketSlots) {
+            int best = 0x7fffffff, mult = 0;
+            for (int i = lane; i < n; i += 32) {
+                const int id = e[i];
+                if ((long long)id > last) {
+                    if (id < best) {
+                        best = id;
+                        mult = 1;
+                    } else if (id == best) {
+                        ++mult;
+                    }
+                }
+            }
+            const int m = __reduce_min_sync(0xffffffffu, best);
+            if (m == 0x7fffffff) break;
+            const int c = __reduce_add_sync(0xffffffffu, best == m ? mult : 0);
+            for (int q = lane; q < c && filled + q < kBucketSlots; q += 32) out[filled + q] = m;
+            filled += c;
+            last = m;
+            __syncwarp();
+        }
+    }
+}
+
+// Buckets of 33 to kEdgeSlots members (listed by the insertion): all members
+// sorted by id in place, so the 32 smallest come first.  One warp per bucket,
+// two members per lane ranked against all members (ties by slot).
+__global__ void __launch_bounds__(kThreads) k_edge_trim(View v) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
+    const int total = *v.trim_count;
+    for (int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); w < total; w += warps) {
+        const int b = v.trim_list[w];
+        const int n = v.eb_count[b];
+        if (n > kEdgeSlots) continue;  // ordered by k_edge_ovf_select
+        int* e = v.eb_slot + edge_bucket_base(b);
+        const int k0 = lane < n ? e[lane] : 0x7fffffff, k1 = lane + 32 < n ? e[lane + 32] : 0x7fffffff;
+        int r0 = 0, r1 = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int a = __shfl_sync(0xffffffffu, k0, j), c = __shfl_sync(0xffffffffu, k1, j);
+            r0 += (a < k0 || (a == k0 && j < lane)) ? 1 : 0;
+            r0 += (c < k0) ? 1 : 0;  // slot j + 32 comes after slot lane
+            r1 += (a <= k1) ? 1 : 0;  // slot j comes before slot lane + 32
+            r1 += (c < k1 || (c == k1 && j < lane)) ? 1 : 0;
+        }
+        __syncwarp();
+        if (lane < n) e[r0] = k0;
+        if (lane + 32 < n) e[r1] = k1;
+        __syncwarp();
+    }
+}
+
+
 // Whether a cloth's queries depend on the order of a bucket's members: fast
 // mode (order-dependent filters) or a candidate budget under 32.  Strict
 // queries with a 32-candidate budget read every member of a bucket of up to
@@ -398,10 +568,11 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
     const int lane = threadIdx.x & 31;
     if (v.lo + (long long)warp * 32 >= v.hi || v.hi > nbuckets) return;
     const int b = v.lo + warp * 32 + lane;
-    int s = 0, n = 0;
+    long long s = 0;  // first member: a CSR start, or the edge hash's slots (start == null)
+    int n = 0;
     if (b < v.hi) {
-        s = start[b];
-        n = start[b + 1] - s;
+        s = start ? start[b] : edge_bucket_base(b);
+        n = start ? start[b + 1] - (int)s : v.eb_count[b];
     }
     bool need = n > kBucketSlots && mode != 3;
     if (n >= 2 && n <= kBucketSlots) {
@@ -425,7 +596,8 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
     while (mask) {
         const int j = __ffs(mask) - 1;
         mask &= mask - 1;
-        const int sj = __shfl_sync(0xffffffffu, s, j), nj = __shfl_sync(0xffffffffu, n, j);
+        const long long sj = __shfl_sync(0xffffffffu, s, j);
+        const int nj = __shfl_sync(0xffffffffu, n, j);
         int* e = ent + sj;
         if (nj <= kBucketSlots) {
             const int key = lane < nj ? e[lane] : 0x7fffffff;
@@ -1345,8 +1517,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     const float onset = fmaxf(target * 1.8f, target + kEps);
     const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
     const int b = P.ebase + (int)bucket_of(cell_of(mid.x, P.ecell, P.key_ieee), cell_of(mid.y, P.ecell, P.key_ieee), cell_of(mid.z, P.ecell, P.key_ieee), P.ebuckets);
-    const int st = v.eb_start[b];
-    const int lim = min(v.eb_start[b + 1] - st, kBucketSlots);
+    const int* mem = v.eb_slot + edge_bucket_base(b);
+    const int lim = edge_bucket_size(v, b);
     const int budget = neighbor_budget(P);
     int prior = 0, evaluated = 0;
     for (int base = 0; base < lim && prior < budget; base += L) {
@@ -1354,7 +1526,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
         sp.apply = false;
         const int slot = base + gl;
         evaluated += min(lim - base, L);
-        const bool accepted = slot < lim && ee_eval(v, e, v.eb_ent[st + slot], target, onset, &sp);
+        const bool accepted = slot < lim && ee_eval(v, e, mem[slot], target, onset, &sp);
         prior += commit_chunk<L>(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
     }
     if (v.perf && gl == 0) {
@@ -1375,7 +1547,8 @@ template <bool kEdge>
 __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
     const int lane = threadIdx.x & 31;
     const int item = v.lo + warp_global_id() * 32 + lane;
-    int st = 0, lim = 0;
+    long long st = 0;  // first member: edge-hash slots or triangle-hash CSR start
+    int lim = 0;
     float target = 0.0f, onset = 0.0f;
     bool counted = false;
     if (item < v.hi) {
@@ -1395,9 +1568,13 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
             const float cell = kEdge ? P.ecell : P.tcell;
             const int b = (kEdge ? P.ebase : P.tbase) +
                           (int)bucket_of(cell_of(q.x, cell, P.key_ieee), cell_of(q.y, cell, P.key_ieee), cell_of(q.z, cell, P.key_ieee), kEdge ? P.ebuckets : P.tbuckets);
-            const int* start = kEdge ? v.eb_start : v.tb_start;
-            st = start[b];
-            lim = min(start[b + 1] - st, kBucketSlots);
+            if (kEdge) {
+                st = edge_bucket_base(b);
+                lim = edge_bucket_size(v, b);
+            } else {
+                st = v.tb_start[b];
+                lim = min(v.tb_start[b + 1] - (int)st, kBucketSlots);
+            }
             counted = true;
         }
     }
@@ -1409,7 +1586,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int excl = incl - lim;
-    const int* ent = kEdge ? v.eb_ent : v.tb_ent;
+    const int* ent = kEdge ? v.eb_slot : v.tb_ent;
     constexpr int contact_slot = kEdge ? kCntEdgeEdgeContacts : kCntSoftContacts;
     unsigned takes = 0, pushes = 0;
     for (int base = 0; base < total; base += 32) {
@@ -1419,7 +1596,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
         for (int step = 16; step > 0; step >>= 1)
             if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
         const int o_item = __shfl_sync(0xffffffffu, item, j);
-        const int o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
+        const long long o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
         const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
         SoftPush sp;
         sp.apply = false;
@@ -1552,7 +1729,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         ed = __ldg(&v.edges[e]);
         run = edge_valid(v.nV, ed) && contact_radius(*P) > 0.0f;
     }
-    int st = 0, lim = 0, budget = 0;
+    long long st = 0;
+    int lim = 0, budget = 0;
     float target = 0.0f, onset = 0.0f;
     if (run) {
         target = contact_radius(*P);
@@ -1561,8 +1739,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
         const int b =
             P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell, P->key_ieee), cell_of(mid.y, P->ecell, P->key_ieee), cell_of(mid.z, P->ecell, P->key_ieee), P->ebuckets);
-        st = v.eb_start[b];
-        lim = min(v.eb_start[b + 1] - st, kBucketSlots);
+        st = edge_bucket_base(b);
+        lim = edge_bucket_size(v, b);
     }
     int incl = lim;
 #pragma unroll
@@ -1581,14 +1759,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         for (int step = 16; step > 0; step >>= 1)
             if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
         const int o_item = __shfl_sync(0xffffffffu, e, j);
-        const int o_st = __shfl_sync(0xffffffffu, st, j);
+        const long long o_st = __shfl_sync(0xffffffffu, st, j);
         const int o_excl = __shfl_sync(0xffffffffu, excl, j);
         const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
         const int o_ieee = __shfl_sync(0xffffffffu, run ? P->key_ieee : 0, j);
         if (w < total) {
             const int slot = w - o_excl;
-            const int id = v.eb_ent[o_st + slot];
-            const bool dup = slot > 0 && id == v.eb_ent[o_st + slot - 1];
+            const int id = v.eb_slot[o_st + slot];
+            const bool dup = slot > 0 && id == v.eb_slot[o_st + slot - 1];
             SoftPush sp;
             sp.apply = false;
             unsigned key = 0u;
@@ -1629,7 +1807,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
             SoftPush sp;
             sp.apply = false;
             unsigned k2 = 0u;
-            ee_fast_classify(v, e, v.eb_ent[st + slot], target, onset, P->key_ieee, &sp, &k2);
+            ee_fast_classify(v, e, v.eb_slot[st + slot], target, onset, P->key_ieee, &sp, &k2);
             if (sp.apply) {
                 ++c_contact;
                 for (int k = 0; k < 4; ++k) {
@@ -1691,7 +1869,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
         ed = __ldg(&v.edges[e]);
         run = edge_valid(v.nV, ed) && contact_radius(*P) > 0.0f;
     }
-    int st = 0, lim = 0, budget = 0;
+    long long st = 0;
+    int lim = 0, budget = 0;
     float target = 0.0f, onset = 0.0f;
     if (run) {
         target = contact_radius(*P);
@@ -1700,8 +1879,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
         const F3 mid = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
         const int b =
             P->ebase + (int)bucket_of(cell_of(mid.x, P->ecell, P->key_ieee), cell_of(mid.y, P->ecell, P->key_ieee), cell_of(mid.z, P->ecell, P->key_ieee), P->ebuckets);
-        st = v.eb_start[b];
-        lim = min(v.eb_start[b + 1] - st, kBucketSlots);
+        st = edge_bucket_base(b);
+        lim = edge_bucket_size(v, b);
     }
     unsigned keys[2] = {0u, 0u};
     int nkeys = 0, accepted = 0, last_id = -1, evaluated = 0;
@@ -1711,7 +1890,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
             const int slot = c * kQueryLanes + gl;
             const bool valid = slot < lim;
             evaluated += valid ? 1 : 0;
-            const int id = valid ? v.eb_ent[st + slot] : -1;
+            const int id = valid ? v.eb_slot[st + slot] : -1;
             const int before = __shfl_sync(gm, id, gbase + ((gl + kQueryLanes - 1) & (kQueryLanes - 1)));
             const bool dup = valid && id == (gl == 0 ? last_id : before);
             last_id = __shfl_sync(gm, id, gbase + kQueryLanes - 1);
@@ -2066,19 +2245,18 @@ inline int grid(long long items, int per_item, int b) { return grid_for(items * 
 
 constexpr int kTrimBlocks = 152 * 4;  // fixed grid of the trim pass (4 blocks per SM)
 
-template <bool kTri, int L>
-void prim_pass(const View& iv, int blocks, int b, bool scatter, cudaStream_t s) {
-    k_prim_hash<kTri, L><<<blocks, b, 0, s>>>(iv, scatter);
+template <int L>
+void tri_pass(const View& iv, int blocks, int b, bool scatter, cudaStream_t s) {
+    k_tri_hash<L><<<blocks, b, 0, s>>>(iv, scatter);
 }
 
-template <bool kTri>
-void prim_pass_lanes(const View& iv, long long items, int lanes, int b, bool scatter, cudaStream_t s) {
+void tri_pass_lanes(const View& iv, long long items, int lanes, int b, bool scatter, cudaStream_t s) {
     switch (lanes) {
-        case 1: prim_pass<kTri, 1>(iv, grid(items, 1, b), b, scatter, s); break;
-        case 2: prim_pass<kTri, 2>(iv, grid(items, 2, b), b, scatter, s); break;
-        case 4: prim_pass<kTri, 4>(iv, grid(items, 4, b), b, scatter, s); break;
-        case 16: prim_pass<kTri, 16>(iv, grid(items, 16, b), b, scatter, s); break;
-        default: prim_pass<kTri, 8>(iv, grid(items, 8, b), b, scatter, s); break;
+        case 1: tri_pass<1>(iv, grid(items, 1, b), b, scatter, s); break;
+        case 2: tri_pass<2>(iv, grid(items, 2, b), b, scatter, s); break;
+        case 4: tri_pass<4>(iv, grid(items, 4, b), b, scatter, s); break;
+        case 16: tri_pass<16>(iv, grid(items, 16, b), b, scatter, s); break;
+        default: tri_pass<8>(iv, grid(items, 8, b), b, scatter, s); break;
     }
 }
 
@@ -2101,27 +2279,22 @@ void bucket_trim(const View& v, const int* start, int* ent, cudaStream_t s) {
     k_bucket_trim<<<kTrimBlocks, kThreads, 0, s>>>(start, ent, v.trim_list, v.trim_count);
 }
 
-void prim_hash(const View& v, bool tri, const ItemRange& items, const ItemRange& buckets, const ItemRange& ordered, int* count,
-               int* start, int* ent, int nb, int order, cudaStream_t s) {
+void tri_hash(const View& v, const ItemRange& items, const ItemRange& buckets, const ItemRange& ordered, int nb, int order,
+              cudaStream_t s) {
     if (items.size() == 0) return;
     const View iv = ranged(v, items);
-    const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, tri ? kTuneTriLanes : kTunePrimLanes);
-    if (tri)
-        prim_pass_lanes<true>(iv, items.size(), lanes, b, false, s);
-    else
-        prim_pass_lanes<false>(iv, items.size(), lanes, b, false, s);
-    scan_counts(count, start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s, v.trim_list, v.trim_count);
-    if (tri)
-        prim_pass_lanes<true>(iv, items.size(), lanes, b, true, s);
-    else
-        prim_pass_lanes<false>(iv, items.size(), lanes, b, true, s);
+    const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, kTuneTriLanes);
+    tri_pass_lanes(iv, items.size(), lanes, b, false, s);
+    scan_counts(v.tb_count, v.tb_start, nb, v.scan_tmp, v.counts ? v.counts + kCntSelfOverflow : nullptr, s, v.trim_list,
+                v.trim_count);
+    tri_pass_lanes(iv, items.size(), lanes, b, true, s);
     if (v.trim_list) {
         // overflowing buckets of every cloth from the scan's list, then every
         // bucket of the cloths whose queries follow bucket order
-        bucket_trim(v, start, ent, s);
-        if (order != 0) bucket_order(v, ordered, start, ent, nb, tri ? 1 : 2, 3, s);
+        bucket_trim(v, v.tb_start, v.tb_ent, s);
+        if (order != 0) bucket_order(v, ordered, v.tb_start, v.tb_ent, nb, 1, 3, s);
     } else {
-        bucket_order(v, buckets, start, ent, nb, tri ? 1 : 2, order, s);
+        bucket_order(v, buckets, v.tb_start, v.tb_ent, nb, 1, order, s);
     }
 }
 
@@ -2159,10 +2332,37 @@ void self_build_vertex_hash(const View& v, const SelfVariants& sv, int nb, cudaS
     bucket_order(v, sv.vb, v.vb_start, v.vb_ent, nb, 0, 1, s);
 }
 void self_build_triangle_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
-    prim_hash(v, true, sv.t_all, sv.tb, sv.tb_ord, v.tb_count, v.tb_start, v.tb_ent, nb, order, s);
+    tri_hash(v, sv.t_all, sv.tb, sv.tb_ord, nb, order, s);
 }
+// The slotted edge hash: insertion, the overflow regions (kernels that exit
+// at once when no bucket overflowed), ordering of the listed buckets of more
+// than 32 members, then of the buckets of up to 32 where queries follow
+// bucket order (order 1 / 2: the cloths that need it, 3: every bucket).
+// The counts, overflow bits and counters and the trim count must be zero.
 void self_build_edge_hash(const View& v, const SelfVariants& sv, int nb, int order, cudaStream_t s) {
-    prim_hash(v, false, sv.e_all, sv.eb, sv.eb_ord, v.eb_count, v.eb_start, v.eb_ent, nb, order, s);
+    const ItemRange& items = sv.e_all;
+    if (items.size() == 0) return;
+    const View iv = ranged(v, items);
+    const int b = tune_of(v.tune, kTuneHashBlock), lanes = tune_of(v.tune, kTunePrimLanes);
+    const long long n = items.size();
+    switch (lanes) {
+        case 1: k_edge_insert<1><<<grid(n, 1, b), b, 0, s>>>(iv); break;
+        case 2: k_edge_insert<2><<<grid(n, 2, b), b, 0, s>>>(iv); break;
+        case 4: k_edge_insert<4><<<grid(n, 4, b), b, 0, s>>>(iv); break;
+        case 16: k_edge_insert<16><<<grid(n, 16, b), b, 0, s>>>(iv); break;
+        default: k_edge_insert<8><<<grid(n, 8, b), b, 0, s>>>(iv); break;
+    }
+    k_edge_ovf_offsets<<<1, 1024, 0, s>>>(v);
+    switch (lanes) {
+        case 1: k_edge_ovf_collect<1><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;
+        case 2: k_edge_ovf_collect<2><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;
+        case 4: k_edge_ovf_collect<4><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;
+        case 16: k_edge_ovf_collect<16><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;
+        default: k_edge_ovf_collect<8><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;
+    }
+    k_edge_ovf_select<<<kTrimBlocks, kThreads, 0, s>>>(v);
+    k_edge_trim<<<kTrimBlocks, kThreads, 0, s>>>(v);
+    if (order != 0) bucket_order(v, order == 3 ? sv.eb : sv.eb_ord, nullptr, v.eb_slot, nb, 2, 3, s);
 }
 
 void self_neighbors(const View& v, int mode, const SelfVariants& sv, cudaStream_t s) {

@@ -26,6 +26,7 @@ namespace xg {
 constexpr int kThreads = 256;
 constexpr int kNeighborSlots = 32;    // VV neighbour table width (abi41.cu:38)
 constexpr int kBucketSlots = 32;      // per-bucket query cap (abi41.cu:29, 32, 36)
+constexpr int kEdgeSlots = 64;        // member slots per edge-hash bucket (more: overflow regions)
 constexpr int kMaxPrimitiveCells = 64;
 constexpr int kSideBit = (int)0x80000000u;
 
@@ -287,9 +288,17 @@ struct View {
     int* tb_count;
     int* tb_start;
     int* tb_ent;
+    // edge hash: bucket b's members in eb_slot[b * kEdgeSlots ...], its count
+    // in eb_count[b]; buckets of more than kEdgeSlots members are listed in
+    // eb_ovf_list (bit set in eb_ovf_bits) and their full member lists kept
+    // in eb_ent at [eb_start[b] - eb_count[b], eb_start[b])
     int* eb_count;
     int* eb_start;
     int* eb_ent;
+    int* eb_slot;
+    unsigned* eb_ovf_bits;
+    int* eb_ovf_list;
+    int* eb_ovf_count;
     int* scan_tmp;          // block sums of the bucket scans
     int* trim_list;         // buckets of more than 32 members found by the scan (null: none kept)
     int* trim_count;
@@ -312,6 +321,11 @@ __device__ __forceinline__ int cloth_of(const int* map, int i) { return map ? __
 __device__ __forceinline__ const Params& params_v(const View& v, int i) { return v.P[cloth_of(v.vcloth, i)]; }
 __device__ __forceinline__ const Params& params_e(const View& v, int e) { return v.P[cloth_of(v.ecloth, e)]; }
 __device__ __forceinline__ const Params& params_t(const View& v, int t) { return v.P[cloth_of(v.tcloth, t)]; }
+
+// First member slot of edge-hash bucket b and the members a query reads
+// (at most the 32 query slots).
+__device__ __forceinline__ long long edge_bucket_base(int b) { return (long long)b * kEdgeSlots; }
+__device__ __forceinline__ int edge_bucket_size(const View& v, int b) { return min(v.eb_count[b], kBucketSlots); }
 
 // Whether a cloth runs self collision in this substep (and, inside the
 // passes, in this pass) (abi41.cu:9255-9262, 9291).

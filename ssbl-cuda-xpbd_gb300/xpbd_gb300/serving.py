@@ -72,7 +72,8 @@ class RequestResult:
 def estimate_device_bytes(req: ClothRequest) -> int:
     """Upper estimate of a request's device memory, from its sizes and the
     allocation rules of the solver (state rows, constraint CSRs, pins, the
-    self-collision tables with 64 cells per triangle / edge, static SDF)."""
+    self-collision tables with 64 cells per triangle / edge and 64 member
+    slots per edge-hash bucket, static SDF)."""
     c, o = req.cloth, req.options
     V, E, T = len(c.positions_world), len(c.edges), len(c.triangles)
     B, L = len(c.bends), len(c.lra_edges)
@@ -87,6 +88,8 @@ def estimate_device_bytes(req: ClothRequest) -> int:
         eb = pow2(max(1024, 4 * E)) if E >= 64 else 0
         b += V * (4 + 4 * 32 + 32 + 16 + 4) + (vb + tb + eb) * 8 + T * 64 * 4 + E * 64 * 4 + 3 * (max(vb, tb, eb) // 4096 + 2) * 4
         b += 3 * max(vb, tb, eb) * 4 + 3 * 4  # lists of buckets of more than 32 members
+        # edge hash: 64 member slots per bucket, overflow bits and list
+        b += eb * 64 * 4 + (eb // 32 + 1) * 4 + (min(eb, E * 64 // 65 + 1) + 1) * 4
     if o.stretch_optimization_enabled:
         # CG blocks, preconditioner, r / z / d / q, cap sums, off-diagonal per
         # stretch-CSR entry (two per edge), colour-sorted cap edges, partials

@@ -154,6 +154,41 @@ def test_hash_and_neighbor_tables_bit_exact(gpu_lib, oracle_lib):
     assert g["nbcount"].sum() > 0
 
 
+@pytest.mark.parametrize("mode", [2, 1], ids=["strict", "fast"])
+def test_crowded_buckets_parity(mode, gpu_lib, oracle_lib):
+    """A cloth shrunk into a 1.2 cm square: every edge's cell box covers the
+    same few cells, so each edge-hash bucket holds about 1,600 members, far
+    past the 64 member slots a bucket keeps: the overflow regions and their
+    selection of the 32 smallest ids run (and the vertex and triangle hashes'
+    trims).  Hash tables, neighbour lists, positions after a frame and all
+    38 counters must equal the oracle's."""
+    sc = scene.drop_scene(24, 1, seed=5, self_mode=mode)
+    gpu, ora = _pair(sc, oracle_lib)
+    p = sc.cloth.positions_world.copy()
+    c = p.mean(0)
+    p = (c + (p - c) * 0.012).astype(np.float32)
+    gpu.update_positions(p)
+    ora.update_positions(p)
+    gpu.build_self_structures()
+    ora.build_self_structures()
+    V = len(p)
+    g, o = _integer_structures(gpu, V), _integer_structures(ora, V)
+    counts = np.diff(g["estart"])
+    assert counts.max() > 64 and np.array_equal(g["estart"], o["estart"])
+    gb, ob = _sorted_buckets(g["estart"], g["eent"]), _sorted_buckets(o["estart"], o["eent"])
+    assert all(np.array_equal(a, b) for a, b in zip(gb, ob))
+    for b in np.flatnonzero(counts):
+        n = min(counts[b], 32)
+        assert np.array_equal(g["eent"][g["estart"][b]:g["estart"][b] + n], o["eent"][o["estart"][b]:o["estart"][b] + n]), b
+    gpu.update_positions(p)
+    ora.update_positions(p)
+    gpu.step(sc.substeps, sc.iterations, diagnostics=True)
+    ora.step(sc.substeps, sc.iterations)
+    pg = gpu.download_positions()
+    assert np.isfinite(pg).all() and np.array_equal(pg, ora.download_positions())
+    assert np.array_equal(gpu.read_buffer(13, np.uint64, 38), ora.read_buffer(13, np.uint64, 38))
+
+
 @pytest.mark.parametrize("mode,budget", [(2, 64), (2, 6), (1, 32)], ids=["strict", "strict-budget6", "fast"])
 def test_folded_cloth_self_contact_parity(mode, budget, gpu_lib, oracle_lib):
     """A cloth folded onto itself 1.2 mm apart (inside the 2 mm contact
