@@ -147,12 +147,14 @@ def full_gather_bytes(kind: str, counters: dict) -> float | None:
 
 # DRAM bytes (read + write) per evaluated bucket slot of the edge-edge query
 # passes: dram__bytes_read.sum + dram__bytes_write.sum of every edge-edge
-# launch of two frames of the 96-cloth batch under ncu, divided by the slots
-# those frames evaluated; scaled by the slots of the measured workload.
-EE_DRAM_BYTES_PER_SLOT = 11.4
-# ... and per entry of an edge-hash build (count, scans, scatter, trim and
-# bucket ordering), from the same kind of capture of the hash kernels.
-EDGE_HASH_DRAM_BYTES_PER_ENTRY = 16.7
+# launch of one profiled frame of the 64-cloth batch under ncu (cold caches:
+# ncu flushes them before each launch), divided by the slots that frame
+# evaluated (`--profile-frame`); scaled by the slots of the measured workload.
+EE_DRAM_BYTES_PER_SLOT = 14.3
+# ... and per insertion of an edge-hash build (slot insertion, overflow
+# kernels, trim and bucket ordering) from the same capture: the frame's last
+# build over its insertions.
+EDGE_HASH_DRAM_BYTES_PER_ENTRY = 20.4
 
 
 def measured_traffic(kind: str, counters: dict, launches: int) -> float | None:
@@ -674,6 +676,9 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, help="1: launch configuration from the autotuner (default); 0: built-in defaults")
     ap.add_argument("--extras", type=int, default=1,
                     help="1: also measure plain32, drop10k, serving, diff and the reference solver (default line)")
+    ap.add_argument("--profile-frame", action="store_true",
+                    help="only: after the warm-up frames, one profiled frame (kernels serialised on the solver stream) "
+                         "inside the NVTX range 'prof' (for ncu --nvtx-include), then its work counters as JSON")
     args = ap.parse_args()
     args.serve_latency_ms = args.serve_latency_ms if args.serve_latency_ms > 0 else None
     args.warmup = max(args.warmup, 3)
@@ -727,6 +732,17 @@ def main():
     # launch configuration from the autotuner (cached per device and
     # workload; measured from the initial state, which it restores)
     tuned = solver.autotune(S, I, rounds=2) if args.autotune else None
+    if args.profile_frame:
+        for _ in range(args.warmup):
+            solver.step(S, I, diagnostics=False, synchronize=True)
+        torch.cuda.nvtx.range_push("prof")
+        prof = solver.profile_frame(S, I)
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"workload": DESCRIPTIONS[args.workload], "launch_config": solver.launch_config(),
+                          "counters": solver.profile_counters(),
+                          "profile": {k: {"ms": ms, "launches": n} for k, (ms, n) in prof.items() if n}}))
+        solver.close()
+        return
     for _ in range(args.warmup):
         solver.step(S, I, diagnostics=False, synchronize=False)
     solver.synchronize()
@@ -764,7 +780,7 @@ def main():
         traffic = measured_traffic(kind, counters, k_n)
         roof = {"bound": "hbm", "kernel": kind, "dominant": kind == dominant, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": traffic,
-                "traffic_source": ("ncu DRAM bytes per evaluated slot (edge-edge) or per entry (edge hash) on 96 cloths, "
+                "traffic_source": ("ncu DRAM bytes (cold caches) per evaluated slot (edge-edge) or per insertion (edge hash) of one profiled frame on 64 cloths, "
                                    "scaled by this workload's units per launch" if traffic is not None else None),
                 "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch,
                 "byte_model": "12 B per candidate gather" if kind in ("edge_edge", "vertex_triangle") else "per-kernel state bytes"}
