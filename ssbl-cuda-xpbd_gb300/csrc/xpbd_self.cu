@@ -1703,7 +1703,8 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
 }
 
 // Fast-mode EE query, flattened: the same outcome as k_ee_fast.  Phase 1
-// classifies every (item, slot) pair of a warp's 32 items, 32 pairs per round
+// classifies every (item, slot) pair of a warp's 32 items past the item's
+// own id in its ordered bucket (the earlier slots give no pair), 32 pairs per round
 // with the slots of the items laid end to end (duplicate = the same id as the
 // slot before; classify is side-effect free, so pairs past an item's budget
 // cut may be classified for nothing); classes and cluster keys go to shared
@@ -1742,14 +1743,33 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         st = edge_bucket_base(b);
         lim = edge_bucket_size(v, b);
     }
-    int incl = lim;
+    // A fast cloth's bucket lists its members in increasing id order, and a
+    // pair is taken from its lower edge: the members up to this edge's own
+    // id form a prefix whose slots are each visited (seen) and give no pair,
+    // an id equal to the one before being a duplicate.  Only the slots after
+    // the prefix are classified.
+    int skip = 0, skip_dup = 0;
+    if (run) {
+        int lo = 0, hi = lim;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (v.eb_slot[st + mid] > e)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        skip = lo;
+        for (int j = 1; j < skip; ++j) skip_dup += v.eb_slot[st + j] == v.eb_slot[st + j - 1] ? 1 : 0;
+    }
+    const int cnt = lim - skip;
+    int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int n = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += n;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    const int excl = incl - lim;
+    const int excl = incl - cnt - skip;  // so that slot = w - excl starts after the prefix
     unsigned char* cls_w = cls_s[wib];
     unsigned* key_w = key_s[wib];
     for (int base = 0; base < total; base += 32) {
@@ -1776,11 +1796,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         }
     }
     __syncwarp();
-    int c_seen = 0, c_dup = 0, c_rest = 0, c_own = 0, c_acc = 0, c_contact = 0, visited = 0;
+    int c_seen = skip, c_dup = skip_dup, c_rest = 0, c_own = 0, c_acc = 0, c_contact = 0, visited = skip;
     if (run) {
         unsigned keys[16];
         int nkeys = 0, passed = 0;
-        for (int slot = 0; slot < lim && passed < budget; ++slot) {
+        for (int slot = skip; slot < lim && passed < budget; ++slot) {
             ++visited;
             ++c_seen;
             const int cls = cls_w[lane * kBucketSlots + slot];
@@ -1882,12 +1902,33 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
         st = edge_bucket_base(b);
         lim = edge_bucket_size(v, b);
     }
+    // the members up to this edge's own id (a prefix of the ordered bucket)
+    // are seen and give no pair, as in k_ee_fast_flat
+    int skip = 0, skip_dup = 0;
+    if (run) {
+        int lo = 0, hi = lim;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (v.eb_slot[st + mid] > e)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        skip = lo;
+        if (gl == 0)
+            for (int j = 1; j < skip; ++j) skip_dup += v.eb_slot[st + j] == v.eb_slot[st + j - 1] ? 1 : 0;
+    }
     unsigned keys[2] = {0u, 0u};
-    int nkeys = 0, accepted = 0, last_id = -1, evaluated = 0;
+    int nkeys = 0, accepted = 0, last_id = skip > 0 ? v.eb_slot[st + skip - 1] : -1;
+    int evaluated = gl == 0 ? skip : 0;
+    if (gl == 0) {
+        c_seen += skip;
+        c_dup += skip_dup;
+    }
     for (int c = 0; c < kBucketSlots / kQueryLanes; ++c) {
-        if (!(run && c * kQueryLanes < lim && accepted < budget)) break;  // uniform within the group
+        if (!(run && skip + c * kQueryLanes < lim && accepted < budget)) break;  // uniform within the group
         {
-            const int slot = c * kQueryLanes + gl;
+            const int slot = skip + c * kQueryLanes + gl;
             const bool valid = slot < lim;
             evaluated += valid ? 1 : 0;
             const int id = valid ? v.eb_slot[st + slot] : -1;
