@@ -108,8 +108,11 @@ def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict)
       velocity pass        52 B per vertex
       bend colour          12 B per bend + 2 endpoints read and written
       vertex-triangle /    12 B per candidate gather: the candidate's row,
-      edge-edge query      per evaluated bucket slot (slots counted in the
-                           profiled frames)
+      edge-edge query      per evaluated bucket slot (vertex-triangle) or per
+                           visited slot whose candidate id is above the query
+                           edge's (edge-edge: a pair is evaluated from its
+                           lower edge, so the other slots end at the id);
+                           counted in the profiled frames
       hash build           12 B per primitive row read, 32 B per entry (key
                            and id through a two-pass sort, read and written),
                            8 B per bucket (cell start / end)
@@ -122,8 +125,8 @@ def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict)
         return 52.0 * V
     if kind == "bend_color":
         return 12.0 * B + 48.0 * B
-    if kind == "edge_edge" and counters.get("ee_slots"):
-        return 12.0 * counters["ee_slots"]
+    if kind == "edge_edge" and counters.get("ee_gathers"):
+        return 12.0 * counters["ee_gathers"]
     if kind == "vertex_triangle" and counters.get("vt_slots"):
         return 12.0 * counters["vt_slots"]
     if kind == "edge_hash" and counters.get("edge_entries"):
@@ -135,11 +138,13 @@ def algorithmic_bytes(kind: str, V: int, E: int, T: int, B: int, counters: dict)
 
 def full_gather_bytes(kind: str, counters: dict) -> float | None:
     """What a query evaluation actually loads, beside the per-gather model:
-    per item its own indices and rows and its bucket range, per evaluated
-    slot the candidate id, its indices and its rows (40 + 36 B per edge-edge
-    slot, 20 + 52 B per vertex-triangle slot)."""
+    per item its own indices and rows and its bucket range, per visited slot
+    the candidate id, per gathered candidate its indices and rows (40 B per
+    edge-edge item, 4 B per slot and 32 B per gather; 20 + 52 B per
+    vertex-triangle slot)."""
     if kind == "edge_edge" and counters.get("ee_items"):
-        return (8 + 2 * F3 + 8) * counters["ee_items"] + (4 + 8 + 2 * F3) * counters["ee_slots"]
+        return ((8 + 2 * F3 + 8) * counters["ee_items"] + 4 * counters["ee_slots"]
+                + (8 + 2 * F3) * counters.get("ee_gathers", counters["ee_slots"]))
     if kind == "vertex_triangle" and counters.get("vt_items"):
         return (F3 + 8) * counters["vt_items"] + (4 + 12 + 3 * F3) * counters["vt_slots"]
     return None
@@ -755,7 +760,7 @@ def main():
     # the solver stream) and the work counters of the query kernels
     prof, counters = {}, {}
     reps = 2
-    summed = ("ee_items", "ee_slots", "vt_items", "vt_slots")  # the others describe one build
+    summed = ("ee_items", "ee_slots", "vt_items", "vt_slots", "ee_gathers")  # the others describe one build
     for _ in range(reps):
         p = solver.profile_frame(S, I)
         for k, (ms, n) in p.items():
@@ -783,13 +788,14 @@ def main():
                 "traffic_source": ("ncu DRAM bytes (cold caches) per evaluated slot (edge-edge) or per insertion (edge hash) of one profiled frame on 64 cloths, "
                                    "scaled by this workload's units per launch" if traffic is not None else None),
                 "avg_launch_us": avg_ms * 1000.0, "algorithmic_bytes_per_launch": per_launch,
-                "byte_model": "12 B per candidate gather" if kind in ("edge_edge", "vertex_triangle") else "per-kernel state bytes"}
+                "byte_model": ("12 B per candidate gather (edge-edge: visited slots whose candidate id is above the query edge's)"
+                               if kind in ("edge_edge", "vertex_triangle") else "per-kernel state bytes")}
         full = full_gather_bytes(kind, counters)
         if full is not None:
             full_launch = full / max(k_n, 1)
             roof["full_gather"] = {"bytes_per_launch": full_launch, "achieved": full_launch / (avg_ms / 1000.0) / 1e9,
                                    "frac": full_launch / (avg_ms / 1000.0) / 1e9 / peak,
-                                   "model": "per item its rows and bucket range, per slot id + indices + rows"}
+                                   "model": "per item its rows and bucket range, per slot its id, per gather indices + rows"}
         break
     kernel_rooflines = {}
     for kind, (k_ms, k_n) in ranked:

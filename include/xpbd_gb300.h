@@ -130,12 +130,13 @@ __attribute__((visibility("default"))) int xpbd_gb300_solver_info(void* handle, 
 __attribute__((visibility("default"))) int xpbd_gb300_autotune(void* handle, int substeps, int iterations, int rounds,
                                                                float* ms_out2);
 
-/* Work counters of the last xpbd_gb300_profile_frame, out[10]: EE query
- * items, EE bucket slots evaluated, VT query items (strict cloths), VT slots
+/* Work counters of the last xpbd_gb300_profile_frame, out[11]: EE query
+ * items, EE bucket slots visited, VT query items (strict cloths), VT slots
  * evaluated; entries written by the frame's last triangle-hash build and
  * last edge-hash build; triangles and edges hashed per build; triangle and
- * edge bucket counts.  They size the algorithmic bytes of the query kernels
- * and of the hash builds. */
+ * edge bucket counts; EE candidate gathers (visited slots whose candidate's
+ * id is above the query edge's, the pairs whose rows are read).  They size
+ * the algorithmic bytes of the query kernels and of the hash builds. */
 __attribute__((visibility("default"))) int xpbd_gb300_profile_counters(void* handle, long long* out);
 
 /* No counterpart in the reference.  Vertex spatial hash that allocates no

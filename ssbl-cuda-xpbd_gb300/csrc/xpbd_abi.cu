@@ -586,7 +586,8 @@ XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out) {
             return 0;
         for (int x : cnt) edge_entries += x;
     }
-    for (int k = 0; k < kPerfSlots; ++k) out[k] = (long long)c[k];
+    for (int k = 0; k < 4; ++k) out[k] = (long long)c[k];
+    out[10] = (long long)c[kPerfEeGathers];
     long long tris = 0, edges = 0;
     for (const Params& P : S->hp) {
         if (!P.self_on) continue;

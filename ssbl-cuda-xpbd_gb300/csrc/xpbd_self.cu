@@ -1520,61 +1520,134 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
     const int* mem = v.eb_slot + edge_bucket_base(b);
     const int lim = edge_bucket_size(v, b);
     const int budget = neighbor_budget(P);
-    int prior = 0, evaluated = 0;
+    int prior = 0, evaluated = 0, gathered = 0;
     for (int base = 0; base < lim && prior < budget; base += L) {
         SoftPush sp;
         sp.apply = false;
         const int slot = base + gl;
         evaluated += min(lim - base, L);
-        const bool accepted = slot < lim && ee_eval(v, e, mem[slot], target, onset, &sp);
+        const int other = slot < lim ? mem[slot] : -1;
+        gathered += other > e ? 1 : 0;
+        const bool accepted = slot < lim && ee_eval(v, e, other, target, onset, &sp);
         prior += commit_chunk<L>(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
     }
-    if (v.perf && gl == 0) {
-        atomicAdd(&v.perf[kPerfEeItems], 1ull);
-        atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)evaluated);
+    if (v.perf) {
+        atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)gathered);
+        if (gl == 0) {
+            atomicAdd(&v.perf[kPerfEeItems], 1ull);
+            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)evaluated);
+        }
     }
 }
 
-// Strict VT / EE queries whose candidate budget is at least the 32 query
+// Strict VT query for cloths whose candidate budget is at least the 32 query
 // slots: every accepted pair of an item's slots is taken, so the pairs are
 // independent and their order does not matter (pushes are summed in fixed
-// point).  One warp per 32 consecutive query items lays the items' bucket
-// slots end to end and evaluates 32 (item, slot) pairs per round, so the
+// point).  One warp per 32 consecutive query vertices lays their bucket
+// slots end to end and evaluates 32 (vertex, slot) pairs per round, so the
 // lanes stay busy however the slot counts vary.  The same pairs, counters
-// and pushes as the 8-lane group kernels, which keep the cloths with a
+// and pushes as the 8-lane group kernel, which keeps the cloths with a
 // smaller budget.
-template <bool kEdge>
-__global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
+__global__ void __launch_bounds__(kThreads, 6) k_flat_vt(View v) {
     const int lane = threadIdx.x & 31;
     const int item = v.lo + warp_global_id() * 32 + lane;
-    long long st = 0;  // first member: edge-hash slots or triangle-hash CSR start
+    int st = 0, lim = 0;
+    float target = 0.0f, onset = 0.0f;
+    bool counted = false;
+    if (item < v.hi) {
+        const Params& P = params_v(v, item);
+        if (P.thash && !fast_mode(P) && self_scheduled(P, v) && neighbor_budget(P) >= kBucketSlots) {
+            const F3 q = f3(v.pos[item]);
+            target = contact_radius(P);
+            if (target > 0.0f) {
+                onset = fmaxf(target * 1.8f, target + kEps);
+                const int b = P.tbase + (int)bucket_of(cell_of(q.x, P.tcell, P.key_ieee), cell_of(q.y, P.tcell, P.key_ieee),
+                                                       cell_of(q.z, P.tcell, P.key_ieee), P.tbuckets);
+                st = v.tb_start[b];
+                lim = min(v.tb_start[b + 1] - st, kBucketSlots);
+                counted = true;
+            }
+        }
+    }
+    int incl = lim;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - lim;
+    unsigned takes = 0, pushes = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int w = base + lane;
+        int j = 0;  // owner: the first lane whose inclusive slot count exceeds w
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
+        const int o_item = __shfl_sync(0xffffffffu, item, j);
+        const int o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
+        const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
+        SoftPush sp;
+        sp.apply = false;
+        const bool accepted = w < total && vt_eval(v, o_item, v.tb_ent[o_first + w], o_target, o_onset, &sp);
+        const bool push = accepted && sp.apply;
+        takes += __popc(__ballot_sync(0xffffffffu, accepted));
+        pushes += __popc(__ballot_sync(0xffffffffu, push));
+        if (push) {
+            for (int k = 0; k < 4; ++k) {
+                const float wk = sp.w[k];
+                if ((k > 0 ? -wk : wk) > 0.0f) accumulate(v, sp.idx[k], sp.delta * wk);
+            }
+        }
+    }
+    const unsigned items = __popc(__ballot_sync(0xffffffffu, counted));
+    if (lane == 0) {
+        count_add(v.counts, kCntSelfCandidates, takes);
+        count_add(v.counts, kCntSoftContacts, pushes);
+        if (v.perf && items) {
+            atomicAdd(&v.perf[kPerfVtItems], (unsigned long long)items);
+            atomicAdd(&v.perf[kPerfVtSlots], (unsigned long long)total);
+        }
+    }
+}
+
+// Strict edge-edge query for cloths whose candidate budget covers the 32
+// query slots, flattened like k_flat_vt with one more step: a pair (item a,
+// candidate b) counts only when b > a (it is evaluated from its lower edge),
+// which about two thirds of the bucket slots fail as soon as their id is
+// read.  Round after round the warp reads 32 slot ids (the items' slots laid
+// end to end), keeps the surviving pairs in a 64-entry ring in shared memory
+// (owner lane, candidate), and evaluates them 32 at a time whenever 32 are
+// waiting, so the evaluation rounds carry only pairs that can be taken.
+// Pushes go through the integer accumulators and the counters through warp
+// ballots, so the result does not depend on the order of evaluation.
+constexpr int kEeRing = 64;
+
+__global__ void __launch_bounds__(kThreads, 6) k_flat_ee(View v) {
+    __shared__ int2 ring_s[kThreads / 32][kEeRing];
+    const int lane = threadIdx.x & 31;
+    int2* ring = ring_s[threadIdx.x >> 5];
+    const int item = v.lo + warp_global_id() * 32 + lane;
+    long long st = 0;
     int lim = 0;
     float target = 0.0f, onset = 0.0f;
     bool counted = false;
     if (item < v.hi) {
-        const Params& P = kEdge ? params_e(v, item) : params_v(v, item);
-        bool want = (kEdge ? P.ehash : P.thash) && !fast_mode(P) && self_scheduled(P, v) && neighbor_budget(P) >= kBucketSlots;
+        const Params& P = params_e(v, item);
+        bool want = P.ehash && !fast_mode(P) && self_scheduled(P, v) && neighbor_budget(P) >= kBucketSlots;
         F3 q{0.0f, 0.0f, 0.0f};
-        if (want && kEdge) {
+        if (want) {
             const int2 ed = __ldg(&v.edges[item]);
             want = edge_valid(v.nV, ed);
             if (want) q = (f3(v.pos[ed.x]) + f3(v.pos[ed.y])) * 0.5f;
-        } else if (want) {
-            q = f3(v.pos[item]);
         }
         if (want) target = contact_radius(P);
         if (want && target > 0.0f) {
             onset = fmaxf(target * 1.8f, target + kEps);
-            const float cell = kEdge ? P.ecell : P.tcell;
-            const int b = (kEdge ? P.ebase : P.tbase) +
-                          (int)bucket_of(cell_of(q.x, cell, P.key_ieee), cell_of(q.y, cell, P.key_ieee), cell_of(q.z, cell, P.key_ieee), kEdge ? P.ebuckets : P.tbuckets);
-            if (kEdge) {
-                st = edge_bucket_base(b);
-                lim = edge_bucket_size(v, b);
-            } else {
-                st = v.tb_start[b];
-                lim = min(v.tb_start[b + 1] - (int)st, kBucketSlots);
-            }
+            const int b = P.ebase + (int)bucket_of(cell_of(q.x, P.ecell, P.key_ieee), cell_of(q.y, P.ecell, P.key_ieee),
+                                                   cell_of(q.z, P.ecell, P.key_ieee), P.ebuckets);
+            st = edge_bucket_base(b);
+            lim = edge_bucket_size(v, b);
             counted = true;
         }
     }
@@ -1586,43 +1659,54 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_query(View v) {
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int excl = incl - lim;
-    const int* ent = kEdge ? v.eb_slot : v.tb_ent;
-    constexpr int contact_slot = kEdge ? kCntEdgeEdgeContacts : kCntSoftContacts;
-    unsigned takes = 0, pushes = 0;
-    for (int base = 0; base < total; base += 32) {
-        const int w = base + lane;
-        int j = 0;  // owner: the first lane whose inclusive slot count exceeds w
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
-        const int o_item = __shfl_sync(0xffffffffu, item, j);
-        const long long o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
-        const float o_target = __shfl_sync(0xffffffffu, target, j), o_onset = __shfl_sync(0xffffffffu, onset, j);
+    unsigned takes = 0, pushes = 0, gathers = 0;
+    int head = 0, tail = 0;  // warp-uniform ring positions
+    auto drain = [&](int n) {
+        const int2 e = lane < n ? ring[(head + lane) & (kEeRing - 1)] : make_int2(0, -1);
+        const int o_item = __shfl_sync(0xffffffffu, item, e.x);
+        const float o_target = __shfl_sync(0xffffffffu, target, e.x), o_onset = __shfl_sync(0xffffffffu, onset, e.x);
         SoftPush sp;
         sp.apply = false;
-        bool accepted = false;
-        if (w < total) {
-            const int other = ent[o_first + w];
-            accepted = kEdge ? ee_eval(v, o_item, other, o_target, o_onset, &sp) : vt_eval(v, o_item, other, o_target, o_onset, &sp);
-        }
+        const bool accepted = lane < n && ee_eval(v, o_item, e.y, o_target, o_onset, &sp);
         const bool push = accepted && sp.apply;
         takes += __popc(__ballot_sync(0xffffffffu, accepted));
         pushes += __popc(__ballot_sync(0xffffffffu, push));
         if (push) {
             for (int k = 0; k < 4; ++k) {
                 const float wk = sp.w[k];
-                const bool far = kEdge ? (k > 1) : (k > 0);
-                if ((far ? -wk : wk) > 0.0f) accumulate(v, sp.idx[k], sp.delta * wk);
+                if ((k > 1 ? -wk : wk) > 0.0f) accumulate(v, sp.idx[k], sp.delta * wk);
             }
         }
+        head += n;
+        __syncwarp();
+    };
+    const unsigned lower = (1u << lane) - 1u;
+    for (int base = 0; base < total; base += 32) {
+        const int w = base + lane;
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
+        const int o_item = __shfl_sync(0xffffffffu, item, j);
+        const long long o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
+        const int other = w < total ? v.eb_slot[o_first + w] : -1;
+        const bool keep = w < total && other > o_item;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) ring[(tail + __popc(m & lower)) & (kEeRing - 1)] = make_int2(j, other);
+        tail += __popc(m);
+        gathers += __popc(m);
+        __syncwarp();
+        if (tail - head >= 32) drain(32);
     }
+    if (tail > head) drain(tail - head);
     const unsigned items = __popc(__ballot_sync(0xffffffffu, counted));
     if (lane == 0) {
         count_add(v.counts, kCntSelfCandidates, takes);
-        count_add(v.counts, contact_slot, pushes);
+        count_add(v.counts, kCntEdgeEdgeContacts, pushes);
         if (v.perf && items) {
-            atomicAdd(&v.perf[kEdge ? kPerfEeItems : kPerfVtItems], (unsigned long long)items);
-            atomicAdd(&v.perf[kEdge ? kPerfEeSlots : kPerfVtSlots], (unsigned long long)total);
+            atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
+            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)total);
+            atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)gathers);
         }
     }
 }
@@ -1851,6 +1935,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         if (lane == 0) {
             atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
             atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)slots_total);
+            atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)total);
         }
     }
     const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);
@@ -2007,9 +2092,11 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
     if (v.perf) {
         const int items = __reduce_add_sync(0xffffffffu, (run && gl == 0) ? 1 : 0);
         const int slots_total = __reduce_add_sync(0xffffffffu, evaluated);
+        const int gathers = __reduce_add_sync(0xffffffffu, evaluated - (gl == 0 ? skip : 0));
         if (lane == 0) {
             atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
             atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)slots_total);
+            atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)gathers);
         }
     }
     const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);
@@ -2433,7 +2520,7 @@ void self_vv(const View& v, const SelfVariants& sv, cudaStream_t s) {
 void self_vt(const View& v, const SelfVariants& sv, cudaStream_t s) {
     const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
     if (sv.hashed_t && sv.strict_wide && sv.v_strict.size() > 0)
-        k_flat_query<false><<<grid(sv.v_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.v_strict));
+        k_flat_vt<<<grid(sv.v_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.v_strict));
     if (sv.hashed_t && sv.strict_narrow && sv.v_strict.size() > 0) group_queries_lanes(v, sv, s, false);
     if (sv.hashed_t && sv.fast && sv.v_fast.size() > 0)
         k_vt_hash<<<grid(sv.v_fast.size(), 1, qb), qb, 0, s>>>(ranged(v, sv.v_fast));
@@ -2443,7 +2530,7 @@ void self_ee(const View& v, const SelfVariants& sv, cudaStream_t s) {
     const int wb = tune_of(v.tune, kTuneWarpBlock), qb = tune_of(v.tune, kTuneQueryBlock);
     const int gb = tune_of(v.tune, kTuneGroupBlock);
     if (sv.hashed_e && sv.strict_wide && sv.e_strict.size() > 0)
-        k_flat_query<true><<<grid(sv.e_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.e_strict));
+        k_flat_ee<<<grid(sv.e_strict.size(), 1, wb), wb, 0, s>>>(ranged(v, sv.e_strict));
     if (sv.hashed_e && sv.strict_narrow && sv.e_strict.size() > 0) group_queries_lanes(v, sv, s, true);
     if (sv.hashed_e && sv.fast && sv.e_fast.size() > 0) {
         if (tune_of(v.tune, kTuneFastEeForm) == 32) {

@@ -315,7 +315,10 @@ struct View {
     LaunchTune tune;  // read by the launchers only
 };
 
-enum PerfSlot { kPerfEeItems = 0, kPerfEeSlots = 1, kPerfVtItems = 2, kPerfVtSlots = 3, kPerfSlots = 4 };
+// EE gathers: visited slots whose candidate id is above the query edge's
+// (the pairs whose indices and rows are read; a pair is taken from its lower
+// edge, so the others end at the id).
+enum PerfSlot { kPerfEeItems = 0, kPerfEeSlots = 1, kPerfVtItems = 2, kPerfVtSlots = 3, kPerfEeGathers = 4, kPerfSlots = 5 };
 
 __device__ __forceinline__ int cloth_of(const int* map, int i) { return map ? __ldg(&map[i]) : 0; }
 __device__ __forceinline__ const Params& params_v(const View& v, int i) { return v.P[cloth_of(v.vcloth, i)]; }

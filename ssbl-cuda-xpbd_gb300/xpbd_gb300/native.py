@@ -714,11 +714,13 @@ class NativeXpbdSolver:
     def profile_counters(self) -> dict:
         """Work counters of the last profile_frame: EE / VT query items and
         bucket slots evaluated, entries of the last triangle / edge hash
-        build, primitives hashed per build and the bucket counts."""
-        out = np.zeros(10, np.int64)
+        build, primitives hashed per build, the bucket counts and the EE
+        candidate gathers (visited slots whose candidate id is above the
+        query edge's)."""
+        out = np.zeros(11, np.int64)
         self._check(self._lib.xpbd_gb300_profile_counters(self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
         keys = ("ee_items", "ee_slots", "vt_items", "vt_slots", "tri_entries", "edge_entries", "tri_hashed", "edge_hashed",
-                "tri_buckets", "edge_buckets")
+                "tri_buckets", "edge_buckets", "ee_gathers")
         return {k: int(v) for k, v in zip(keys, out)}
 
 
