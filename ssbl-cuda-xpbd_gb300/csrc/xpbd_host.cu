@@ -1773,16 +1773,19 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                         reset_edge_hash(S, lane_stream(2));
                         self_build_edge_hash(hv[2], sp.sv, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
                     });
-                join();
+                // No join here: each branch's first pass needs only its own
+                // hash (neighbour table + VV: the vertex hash, VT + islands:
+                // the triangle hash, EE: the edge hash), so the queries of the
+                // finished branches overlap the longer builds.
                 if (sp.sv.fast) {
-                    timed(kKNeighbors, 1, [&] { self_neighbors(sv, 1, sp.sv, S->stream); });
+                    timed(kKNeighbors, 1, [&] { self_neighbors(sv, 1, sp.sv, lane_stream(0)); });
                     st->cache_hits += sp.hits;
                     st->cache_misses += sp.misses;
                 }
                 for (int pass = 0; pass < sp.passes; ++pass) {
                     View pv2 = sv;
                     pv2.pass = pass;
-                    fork();
+                    if (pass > 0) fork();
                     if (sp.sv.strict) timed(kKNeighbors, 1, [&] { self_neighbors(pv2, 2, sp.sv, lane_stream(0)); });
                     timed(kKVertexVertex, 1, [&] { self_vv(pv2, sp.sv, lane_stream(0)); });
                     if (sp.any_t) timed(kKVertexTriangle, 1, [&] { self_vt(pv2, sp.sv, lane_stream(1)); });
