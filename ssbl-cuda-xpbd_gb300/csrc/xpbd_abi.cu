@@ -571,9 +571,9 @@ XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out) {
     g_error.clear();
     Solver* S = as_solver(handle);
     if (!S || !out) return fail("invalid profile counter request") ? 1 : 0;
-    unsigned long long c[kPerfSlots];
+    unsigned long long stripes[kPerfStripes * kPerfStride], c[kPerfSlots] = {};
     int entries[1] = {0};  // the triangle hash scan's total: entries of its last build
-    if (!cuda_ok(cudaMemcpyAsync(c, S->perf, sizeof(c), cudaMemcpyDeviceToHost, S->stream), "read work counters") ||
+    if (!cuda_ok(cudaMemcpyAsync(stripes, S->perf, sizeof(stripes), cudaMemcpyDeviceToHost, S->stream), "read work counters") ||
         (S->tb_start && S->nTB > 0 &&
          !cuda_ok(cudaMemcpyAsync(&entries[0], S->tb_start + S->nTB, sizeof(int), cudaMemcpyDeviceToHost, S->stream),
                   "read triangle hash size")) ||
@@ -586,6 +586,8 @@ XG_EXPORT int xpbd_gb300_profile_counters(void* handle, long long* out) {
             return 0;
         for (int x : cnt) edge_entries += x;
     }
+    for (int q = 0; q < kPerfStripes; ++q)
+        for (int k = 0; k < kPerfSlots; ++k) c[k] += stripes[q * kPerfStride + k];
     for (int k = 0; k < 4; ++k) out[k] = (long long)c[k];
     out[10] = (long long)c[kPerfEeGathers];
     long long tris = 0, edges = 0;

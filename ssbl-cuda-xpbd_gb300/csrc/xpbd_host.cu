@@ -1248,7 +1248,7 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
               dalloc(&S->edges, nE, "edge allocation") && dalloc(&S->edge_rest, nE, "edge rest allocation") &&
               dalloc(&S->pin_target, nV, "pin target allocation") && dalloc(&S->pin_weight, nV, "pin weight allocation") &&
               dalloc(&S->pin_relax, nV, "pin relaxation allocation") &&
-              dalloc(&S->counts, kCntSlots, "ABI41 diagnostic allocation") && dalloc(&S->perf, kPerfSlots, "work counter allocation") &&
+              dalloc(&S->counts, kCntSlots, "ABI41 diagnostic allocation") && dalloc(&S->perf, kPerfStripes * kPerfStride, "work counter allocation") &&
               dalloc(&S->max_delta_bits, 1, "self max smoothed delta allocation") &&
               dalloc(&S->pack, (size_t)nV * 3, "download staging allocation");
     if (ok && !S->h_bend_ranges.empty())
@@ -1581,7 +1581,7 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
     base.substeps = substeps;
     if (prof) {
         base.perf = S->perf;
-        cudaMemsetAsync(S->perf, 0, sizeof(unsigned long long) * kPerfSlots, S->stream);
+        cudaMemsetAsync(S->perf, 0, sizeof(unsigned long long) * kPerfStripes * kPerfStride, S->stream);
     }
     int cur = 0;
     unsigned pending = 0;

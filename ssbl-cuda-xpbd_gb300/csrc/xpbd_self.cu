@@ -1497,8 +1497,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_vt_warp(View v) {
         prior += commit_chunk<L>(v, accepted, sp, prior, budget, kCntSoftContacts);
     }
     if (v.perf && gl == 0) {
-        atomicAdd(&v.perf[kPerfVtItems], 1ull);
-        atomicAdd(&v.perf[kPerfVtSlots], (unsigned long long)evaluated);
+        perf_add(v.perf, kPerfVtItems, 1ull);
+        perf_add(v.perf, kPerfVtSlots, (unsigned long long)evaluated);
     }
 }
 
@@ -1532,10 +1532,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_warp(View v) {
         prior += commit_chunk<L>(v, accepted, sp, prior, budget, kCntEdgeEdgeContacts);
     }
     if (v.perf) {
-        atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)gathered);
+        perf_add(v.perf, kPerfEeGathers, (unsigned long long)gathered);
         if (gl == 0) {
-            atomicAdd(&v.perf[kPerfEeItems], 1ull);
-            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)evaluated);
+            perf_add(v.perf, kPerfEeItems, 1ull);
+            perf_add(v.perf, kPerfEeSlots, (unsigned long long)evaluated);
         }
     }
 }
@@ -1605,8 +1605,8 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_vt(View v) {
         count_add(v.counts, kCntSelfCandidates, takes);
         count_add(v.counts, kCntSoftContacts, pushes);
         if (v.perf && items) {
-            atomicAdd(&v.perf[kPerfVtItems], (unsigned long long)items);
-            atomicAdd(&v.perf[kPerfVtSlots], (unsigned long long)total);
+            perf_add(v.perf, kPerfVtItems, (unsigned long long)items);
+            perf_add(v.perf, kPerfVtSlots, (unsigned long long)total);
         }
     }
 }
@@ -1704,9 +1704,9 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_ee(View v) {
         count_add(v.counts, kCntSelfCandidates, takes);
         count_add(v.counts, kCntEdgeEdgeContacts, pushes);
         if (v.perf && items) {
-            atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
-            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)total);
-            atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)gathers);
+            perf_add(v.perf, kPerfEeItems, (unsigned long long)items);
+            perf_add(v.perf, kPerfEeSlots, (unsigned long long)total);
+            perf_add(v.perf, kPerfEeGathers, (unsigned long long)gathers);
         }
     }
 }
@@ -1933,9 +1933,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_ee_fast_flat(View v) {
         const int items = __reduce_add_sync(0xffffffffu, run ? 1 : 0);
         const int slots_total = __reduce_add_sync(0xffffffffu, visited);
         if (lane == 0) {
-            atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
-            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)slots_total);
-            atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)total);
+            perf_add(v.perf, kPerfEeItems, (unsigned long long)items);
+            perf_add(v.perf, kPerfEeSlots, (unsigned long long)slots_total);
+            perf_add(v.perf, kPerfEeGathers, (unsigned long long)total);
         }
     }
     const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);
@@ -2094,9 +2094,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_ee_fast(View v) {
         const int slots_total = __reduce_add_sync(0xffffffffu, evaluated);
         const int gathers = __reduce_add_sync(0xffffffffu, evaluated - (gl == 0 ? skip : 0));
         if (lane == 0) {
-            atomicAdd(&v.perf[kPerfEeItems], (unsigned long long)items);
-            atomicAdd(&v.perf[kPerfEeSlots], (unsigned long long)slots_total);
-            atomicAdd(&v.perf[kPerfEeGathers], (unsigned long long)gathers);
+            perf_add(v.perf, kPerfEeItems, (unsigned long long)items);
+            perf_add(v.perf, kPerfEeSlots, (unsigned long long)slots_total);
+            perf_add(v.perf, kPerfEeGathers, (unsigned long long)gathers);
         }
     }
     const int acc_total = __reduce_add_sync(0xffffffffu, c_acc);

@@ -319,6 +319,12 @@ struct View {
 // (the pairs whose indices and rows are read; a pair is taken from its lower
 // edge, so the others end at the id).
 enum PerfSlot { kPerfEeItems = 0, kPerfEeSlots = 1, kPerfVtItems = 2, kPerfVtSlots = 3, kPerfEeGathers = 4, kPerfSlots = 5 };
+// The work counters are kept in kPerfStripes copies 64 bytes apart, a block
+// adding to copy blockIdx.x % kPerfStripes, and summed on the host: one
+// counter address taking an atomic from every warp of a query launch would
+// serialise in one L2 slice and slow the profiled kernels themselves.
+constexpr int kPerfStripes = 32;
+constexpr int kPerfStride = 8;
 
 __device__ __forceinline__ int cloth_of(const int* map, int i) { return map ? __ldg(&map[i]) : 0; }
 __device__ __forceinline__ const Params& params_v(const View& v, int i) { return v.P[cloth_of(v.vcloth, i)]; }
@@ -344,6 +350,10 @@ __device__ __forceinline__ void count1(unsigned long long* counts, int slot) {
     if (!counts) return;
     const unsigned mask = __activemask();
     if ((threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(&counts[slot], (unsigned long long)__popc(mask));
+}
+
+__device__ __forceinline__ void perf_add(unsigned long long* perf, int slot, unsigned long long v) {
+    if (perf && v) atomicAdd(&perf[(blockIdx.x % kPerfStripes) * kPerfStride + slot], v);
 }
 
 __device__ __forceinline__ void count_add(unsigned long long* counts, int slot, unsigned long long v) {
