@@ -150,12 +150,12 @@ def full_gather_bytes(kind: str, counters: dict) -> float | None:
     return None
 
 
-# DRAM bytes (read + write) per evaluated bucket slot of the edge-edge query
+# DRAM bytes (read + write) per visited bucket slot of the edge-edge query
 # passes: dram__bytes_read.sum + dram__bytes_write.sum of every edge-edge
 # launch of one profiled frame of the 64-cloth batch under ncu (cold caches:
 # ncu flushes them before each launch), divided by the slots that frame
 # evaluated (`--profile-frame`); scaled by the slots of the measured workload.
-EE_DRAM_BYTES_PER_SLOT = 14.3
+EE_DRAM_BYTES_PER_SLOT = 14.4
 # ... and per insertion of an edge-hash build (slot insertion, overflow
 # kernels, trim and bucket ordering) from the same capture: the frame's last
 # build over its insertions.
