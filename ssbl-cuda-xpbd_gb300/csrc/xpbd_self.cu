@@ -2262,28 +2262,57 @@ __global__ void __launch_bounds__(kThreads, 4) k_island(View v) {
                 tri = v.tb_ent[o_first + g];
                 code = island_eval(v, vertex, p, pp, target, onset, tri, &h);
             }
-            const int n = stop ? 0 : min(G, round_total - base);
-            const int warp_n = __reduce_max_sync(0xffffffffu, max(n, 0));
-            for (int k = 0; k < warp_n; ++k) {
-                bool live = k < n && !stop;
+            // Replay in walk order.  A triangle gives the same code every
+            // time this vertex meets it, and only contacts (code 2) enter
+            // the accepted set, so a slot of code 0 or 1 is never a
+            // duplicate: it only advances the scan count (and the guard
+            // count for code 1) under the walk's two limits, which stay
+            // fixed until the next contact.  Such runs are settled in one
+            // step from ballot masks; only the contacts go through the
+            // serial duplicate test, one per iteration.
+            const int n = stop ? 0 : max(min(G, round_total - base), 0);
+            const int first = lane & ~(G - 1);
+            const unsigned m1 = (__ballot_sync(0xffffffffu, code == 1) & gmask) >> first;
+            unsigned m2 = (__ballot_sync(0xffffffffu, code == 2) & gmask) >> first;
+            const int warp_c2 = __reduce_max_sync(0xffffffffu, __popc(m2));
+            int pos = 0;
+            auto run_plain = [&](int end) {  // slots [pos, end), none of them a contact
+                if (stop || end <= pos) return;
+                if (contacts >= max_contacts || scanned >= scan_limit) {
+                    stop = true;
+                    return;
+                }
+                const int take = min(end - pos, scan_limit - scanned);
+                const unsigned span = take >= 32 ? 0xffffffffu : (1u << take) - 1u;
+                guards += __popc(m1 & (span << pos));
+                scanned += take;
+                if (take < end - pos) stop = true;
+                pos = end;
+            };
+            for (int it = 0; it < warp_c2; ++it) {
+                const int k = m2 ? __ffs(m2) - 1 : n;
+                run_plain(k);
+                bool live = m2 != 0u && !stop;
                 if (live && (contacts >= max_contacts || scanned >= scan_limit)) {
                     stop = true;
                     live = false;
                 }
-                const int t_k = __shfl_sync(0xffffffffu, tri, k, G);
-                const int c_k = __shfl_sync(0xffffffffu, code, k, G);
-                const float pen_k = __shfl_sync(0xffffffffu, h.pen, k, G), w_k = __shfl_sync(0xffffffffu, h.wterm, k, G);
-                const F3 n_k{__shfl_sync(0xffffffffu, h.nrm.x, k, G), __shfl_sync(0xffffffffu, h.nrm.y, k, G),
-                             __shfl_sync(0xffffffffu, h.nrm.z, k, G)};
+                const int src = m2 ? k : 0;
+                const int t_k = __shfl_sync(0xffffffffu, tri, src, G);
+                const float pen_k = __shfl_sync(0xffffffffu, h.pen, src, G), w_k = __shfl_sync(0xffffffffu, h.wterm, src, G);
+                const F3 n_k{__shfl_sync(0xffffffffu, h.nrm.x, src, G), __shfl_sync(0xffffffffu, h.nrm.y, src, G),
+                             __shfl_sync(0xffffffffu, h.nrm.z, src, G)};
                 bool mine = false;
 #pragma unroll
                 for (int q = 0; q < kHeld; ++q) mine = mine || (q * G + gl < contacts && held[q] == t_k);
                 const bool dup = (__ballot_sync(0xffffffffu, live && mine) & gmask) != 0u;
+                if (m2) {
+                    m2 &= m2 - 1u;
+                    pos = k + 1;
+                }
                 if (!live) continue;
                 ++scanned;
                 if (dup) continue;
-                if (c_k == 1) ++guards;
-                if (c_k != 2) continue;
                 if (gl == contacts % G) {
 #pragma unroll
                     for (int q = 0; q < kHeld; ++q)
@@ -2298,6 +2327,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_island(View v) {
                     best = n_k;
                 }
             }
+            run_plain(n);
         }
     }
     if (gl != 0) return;
