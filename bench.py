@@ -35,7 +35,10 @@ arrivals with its p50 / p99 frame latency under a frame-latency target
 and ``reference_gpu``, the reference's own CUDA solver (built unchanged for
 sm_103a from its sources by oracle/build_ref.py) stepping the same 256 cloths
 one handle at a time on the default stream, one wait per frame, as the add-on
-does: the plain baseline of the batched form.
+does: the plain baseline of the batched form; and ``reference_gpu_plain32`` /
+``reference_gpu_drop10k``, the same solver on the two single-cloth workloads
+(one handle, one wait per frame), beside which ``plain32_over_reference`` and
+``drop10k_over_reference`` give this repository's ratio.
 
 ``--impl reference``: the reference's step has no CPU implementation, so that
 arm times the CPU restatement of the reference's algorithm (oracle/) with
@@ -401,6 +404,34 @@ def time_reference_gpu(scs, frames: int, torch) -> dict:
     return {"value": V * S * frames / el, "unit": METRIC, "ms_per_step": 1000.0 * el / frames, "frames": frames,
             "handles": len(scs), "what": "reference CUDA solver, one handle per cloth on the default stream, "
             "one wait per frame (host-timed)"}
+
+
+def time_reference_single(name: str, frames: int, warmup: int, torch) -> dict:
+    """The reference's own CUDA solver on one of the single-cloth workloads
+    (plain32, drop10k), stepped as the add-on steps a cloth: step(diagnostics
+    =False, synchronize=False) on the default stream, then a device wait
+    (host-timed per frame, after `warmup` frames)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_solver
+
+    if not ref_solver.available():
+        return {"unavailable": "reference solver not built (oracle/build_ref.py needs the reference sources)"}
+    sc = workload(name)[0]
+    r = ref_solver.RefSolver.from_scene(sc)
+    S, I = sc.substeps, sc.iterations
+    for _ in range(warmup):
+        r.step(S, I, diagnostics=False, synchronize=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        r.step(S, I, diagnostics=False, synchronize=False)
+        torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    r.close()
+    V = len(sc.cloth.positions_world)
+    return {"value": V * S * frames / el, "unit": METRIC, "ms_per_step": 1000.0 * el / frames, "frames": frames,
+            "what": "reference CUDA solver, one handle, default stream, one wait per frame (host-timed)",
+            "workload": DESCRIPTIONS[name]}
 
 
 def time_plain(native, scs, frames: int) -> dict:
@@ -858,6 +889,11 @@ def main():
         extras["reference_gpu"] = time_reference_gpu(scs, max(args.plain_frames, 1), torch) if batched else None
         extras["plain32"] = time_single(native, torch, "plain32", 50, args.warmup)
         extras["drop10k"] = time_single(native, torch, "drop10k", 50, args.warmup)
+        for name in ("plain32", "drop10k"):
+            ref_single = time_reference_single(name, 20, args.warmup, torch)
+            extras[f"reference_gpu_{name}"] = ref_single
+            if "value" in ref_single:
+                extras[f"{name}_over_reference"] = extras[name]["value"] / ref_single["value"]
         extras["diff"] = diff_measure(3, 1, torch)
         st, _ = serve_measure(args.serve_seconds, args.serve_budget_gb, args.serve_latency_ms, args.warmup, 0, torch)
         extras["serving"] = {"value": st["throughput"], "unit": METRIC, "workload": DESCRIPTIONS["serve"],
