@@ -270,6 +270,30 @@ __device__ __forceinline__ int block_exclusive_scan4(int (&vals)[4], int* warp_s
     return before;
 }
 
+// Four consecutive counters from `base` (zero past n): one int4 load when
+// the array is 16-byte aligned and the quad lies inside it (base is a
+// multiple of 4).
+__device__ __forceinline__ void load_quad(const int* a, int base, int n, int (&vals)[4]) {
+    if (base + 3 < n && (reinterpret_cast<uintptr_t>(a) & 15u) == 0u) {
+        const int4 q = *reinterpret_cast<const int4*>(a + base);
+        vals[0] = q.x;
+        vals[1] = q.y;
+        vals[2] = q.z;
+        vals[3] = q.w;
+    } else {
+        for (int k = 0; k < 4; ++k) vals[k] = base + k < n ? a[base + k] : 0;
+    }
+}
+
+__device__ __forceinline__ void store_quad(int* a, int base, int n, const int (&vals)[4]) {
+    if (base + 3 < n && (reinterpret_cast<uintptr_t>(a) & 15u) == 0u) {
+        *reinterpret_cast<int4*>(a + base) = make_int4(vals[0], vals[1], vals[2], vals[3]);
+    } else {
+        for (int k = 0; k < 4; ++k)
+            if (base + k < n) a[base + k] = vals[k];
+    }
+}
+
 // Also adds the number of insertions past each bucket's 32 query slots,
 // sum(max(0, count - 32)), to the overflow counter (the reference counts an
 // overflow for every insertion that finds its bucket full, abi41.cu:4569).
@@ -281,8 +305,8 @@ __global__ void __launch_bounds__(1024) k_scan_reduce(const int* counts, int n, 
     int vals[4];
     const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
     int over = 0;
+    load_quad(counts, base, n, vals);
     for (int k = 0; k < 4; ++k) {
-        vals[k] = base + k < n ? counts[base + k] : 0;
         over += vals[k] > kBucketSlots ? vals[k] - kBucketSlots : 0;
         if (trim && vals[k] > kBucketSlots) trim[atomicAdd(trim_count, 1)] = base + k;
     }
@@ -319,16 +343,16 @@ __global__ void __launch_bounds__(1024) k_scan_down(int* counts, int* start, int
     __shared__ int ws[32];
     int vals[4];
     const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
-    for (int k = 0; k < 4; ++k) vals[k] = base + k < n ? counts[base + k] : 0;
+    load_quad(counts, base, n, vals);
     int total;
     int run = block_offsets[blockIdx.x] + block_exclusive_scan4(vals, ws, &total);
+    int starts[4];
     for (int k = 0; k < 4; ++k) {
-        if (base + k < n) {
-            start[base + k] = run;
-            counts[base + k] = run;
-        }
+        starts[k] = run;
         run += vals[k];
     }
+    store_quad(start, base, n, starts);
+    store_quad(counts, base, n, starts);
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) start[n] = run;
 }
 
@@ -551,6 +575,55 @@ __device__ __forceinline__ void sort_small(int* e, int n) {
         if (k < n) e[k] = r[k];
 }
 
+// sort_small for a bucket of the slotted edge hash: its slot block is
+// 256-byte aligned and always holds kEdgeSlots ints, so the members are read
+// as whole int4 quads (slots past n hold stale ids and are replaced by the
+// padding) and whole quads are written back.
+template <int N>
+__device__ __forceinline__ void sort_small_slots(int* e, int n) {
+    int r[N];
+    const int4* q4 = reinterpret_cast<const int4*>(e);
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q) {
+        int4 t = make_int4(0, 0, 0, 0);
+        if (4 * q < n) t = q4[q];
+        r[4 * q] = t.x;
+        r[4 * q + 1] = t.y;
+        r[4 * q + 2] = t.z;
+        r[4 * q + 3] = t.w;
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if (k >= n) r[k] = 0x7fffffff;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const int l = k ^ stride;
+                if (l > k) {
+                    const int lo = min(r[k], r[l]), hi = max(r[k], r[l]);
+                    const bool up = (k & size) == 0;
+                    r[k] = up ? lo : hi;
+                    r[l] = up ? hi : lo;
+                }
+            }
+        }
+    }
+    int4* w4 = reinterpret_cast<int4*>(e);
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q) {
+        if (4 * q + 3 < n) {
+            w4[q] = make_int4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int k = 4 * q; k < 4 * q + 4; ++k)
+                if (k < n) e[k] = r[k];
+        }
+    }
+}
+
 // Order bucket members by primitive id.  One warp per 32 consecutive buckets:
 // each lane sorts its own bucket of up to 16 members in registers (bitonic
 // network over 8, or 16 when a bucket of the warp needs it, padded with
@@ -587,9 +660,13 @@ __global__ void __launch_bounds__(kThreads) k_bucket_sort(View v, const int* sta
     const bool small = need && n <= kSmall;
     // the network size follows the warp's largest small bucket (8 or 16)
     if (__any_sync(0xffffffffu, small && n > 8)) {
-        if (small) sort_small<16>(ent + s, n);
+        if (small && start) sort_small<16>(ent + s, n);
+        if (small && !start) sort_small_slots<16>(ent + s, n);
     } else if (small) {
-        sort_small<8>(ent + s, n);
+        if (start)
+            sort_small<8>(ent + s, n);
+        else
+            sort_small_slots<8>(ent + s, n);
     }
     if (small) need = false;
     unsigned mask = __ballot_sync(0xffffffffu, need);
