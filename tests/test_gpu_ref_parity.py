@@ -28,8 +28,8 @@ same ctypes mirror.
   threads read positions that others are updating, so in contact phases
   the product parts from the reference by more than the reference's runs
   part from one another: on the 16-cloth batch sample after ten frames the
-  99th percentile measured 0.8-5.4 spreads per cloth, the spread itself
-  varying by a third between sets of four reference runs; in fast mode the
+  99th percentile measured up to 5.7 spreads per cloth, and the same
+  cloth 2.6-5.4 spreads from one set of four reference runs to the next; in fast mode the
   cluster filter also keeps the first contact in candidate order (atomic
   arrival in the reference, increasing id here).
 
