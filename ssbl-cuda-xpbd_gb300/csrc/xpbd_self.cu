@@ -1291,7 +1291,24 @@ __global__ void __launch_bounds__(kThreads, 8) k_neighbors_group(View v, int mod
         cz = cell_of(p.z, P->vcell, P->key_ieee);
     }
     int total = 0;  // neighbours of the earlier rounds (the same in the vertex's lanes)
-    for (int c0 = 0; c0 < 27; c0 += G) {
+    if (G == 1) {
+        // one lane per vertex: the cells in walk order, each neighbour
+        // written to the table as it is found
+        for (int c = 0; c < 27 && run; ++c) {
+            const int qx = cx + c % 3 - 1, qy = cy + (c / 3) % 3 - 1, qz = cz + c / 9 - 1;
+            const int b = P->vbase + (int)bucket_of(qx, qy, qz, P->vbuckets);
+            const int st = v.vb_start[b];
+            const int lim = min(v.vb_start[b + 1] - st, kBucketSlots);
+            for (int k = 0; k < lim; ++k) {
+                const int other = v.vb_ent[st + k];
+                const int4 oc = v.vcell[other];
+                if (oc.x != qx || oc.y != qy || oc.z != qz || !vv_valid(v, src, other, target, onset)) continue;
+                if (total < kNeighborSlots) v.nb_idx[src * kNeighborSlots + total] = other;
+                ++total;
+            }
+        }
+    }
+    for (int c0 = 0; G > 1 && c0 < 27; c0 += G) {
         const int c = c0 + gl;
         int found[kNeighborSlots];
         int nfound = 0;
