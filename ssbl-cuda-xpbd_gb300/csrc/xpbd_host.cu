@@ -313,6 +313,7 @@ void reset_edge_hash(Solver* S, cudaStream_t s) {
     cudaMemsetAsync(S->eb_count, 0, sizeof(int) * (size_t)S->nEB, s);
     cudaMemsetAsync(S->eb_ovf_bits, 0, sizeof(unsigned) * (((size_t)S->nEB + 31) / 32), s);
     cudaMemsetAsync(S->eb_ovf_count, 0, sizeof(int), s);
+    cudaMemsetAsync(S->eb_late_count, 0, sizeof(unsigned long long), s);
     cudaMemsetAsync(S->trim_count + 2, 0, sizeof(int), s);
 }
 
@@ -371,6 +372,10 @@ View Solver::view() const {
     v.eb_ovf_bits = eb_ovf_bits;
     v.eb_ovf_list = eb_ovf_list;
     v.eb_ovf_count = eb_ovf_count;
+    v.eb_ovf_start = eb_ovf_start;
+    v.eb_late = eb_late;
+    v.eb_late_count = eb_late_count;
+    v.eb_late_cap = eb_late_cap;
     v.nb_count = nb_count;
     v.nb_idx = nb_idx;
     v.scan_tmp = scan_tmp;
@@ -440,7 +445,10 @@ void free_solver(Solver* S) {
     dfree(S->eb_slot);
     dfree(S->eb_ovf_bits);
     dfree(S->eb_ovf_list);
+    dfree(S->eb_ovf_start);
     dfree(S->eb_ovf_count);
+    dfree(S->eb_late);
+    dfree(S->eb_late_count);
     dfree(S->nb_count);
     dfree(S->nb_idx);
     dfree(S->acc);
@@ -1285,13 +1293,25 @@ Solver* create_solver(const SsblXpbdConfig* in_configs, const SsblXpbdMesh* in_m
         if (ok && S->nEB > 0) {
             // a bucket past kEdgeSlots members holds at least kEdgeSlots + 1 entries
             S->eb_ovf_cap = std::min<long long>(S->nEB, edge_entries / (kEdgeSlots + 1) + 1);
+            // room for the insertions past the slots of a crowded build (the
+            // hashed edges' count, at least 2^20); a build with more falls
+            // back to a second walk of the cells.  XPBD_GB300_EDGE_LATE_CAP
+            // lowers it (tests run the fallback that way).
+            S->eb_late_cap = std::min<long long>(edge_entries, std::max<long long>(1ll << 20, edge_entries / kMaxPrimitiveCells));
+            if (const char* raw = std::getenv("XPBD_GB300_EDGE_LATE_CAP")) {
+                const long long cap = std::atoll(raw);
+                if (cap >= 0) S->eb_late_cap = std::min(S->eb_late_cap, cap);
+            }
             ok = dalloc(&S->eb_count, S->nEB, "self edge hash count allocation") &&
                  dalloc(&S->eb_start, S->nEB + 1, "self edge hash start allocation") &&
                  dalloc(&S->eb_ent, (size_t)edge_entries, "self edge hash index allocation") &&
                  dalloc(&S->eb_slot, (size_t)S->nEB * kEdgeSlots, "self edge hash slot allocation") &&
                  dalloc(&S->eb_ovf_bits, ((size_t)S->nEB + 31) / 32, "self edge hash overflow allocation") &&
                  dalloc(&S->eb_ovf_list, (size_t)S->eb_ovf_cap, "self edge hash overflow allocation") &&
-                 dalloc(&S->eb_ovf_count, 1, "self edge hash overflow allocation");
+                 dalloc(&S->eb_ovf_start, (size_t)S->eb_ovf_cap, "self edge hash overflow allocation") &&
+                 dalloc(&S->eb_ovf_count, 1, "self edge hash overflow allocation") &&
+                 dalloc(&S->eb_late, (size_t)std::max<long long>(S->eb_late_cap, 1), "self edge hash overflow allocation") &&
+                 dalloc(&S->eb_late_count, 1, "self edge hash overflow allocation");
         }
     }
     // Hard-stretch buffers.  The caps follow the caller's edge colouring when

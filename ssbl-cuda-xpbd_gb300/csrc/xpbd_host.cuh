@@ -298,9 +298,12 @@ struct Solver {
     int *vb_count = nullptr, *vb_start = nullptr, *vb_ent = nullptr;
     int *tb_count = nullptr, *tb_start = nullptr, *tb_ent = nullptr;
     int *eb_count = nullptr, *eb_start = nullptr, *eb_ent = nullptr;
-    int *eb_slot = nullptr, *eb_ovf_list = nullptr, *eb_ovf_count = nullptr;
+    int *eb_slot = nullptr, *eb_ovf_list = nullptr, *eb_ovf_count = nullptr, *eb_ovf_start = nullptr;
     unsigned* eb_ovf_bits = nullptr;
     long long eb_ovf_cap = 0;  // entries of eb_ovf_list
+    int2* eb_late = nullptr;   // insertions past a bucket's slots, as (bucket, edge)
+    unsigned long long* eb_late_count = nullptr;
+    long long eb_late_cap = 0;
     int* nb_count = nullptr;
     int* nb_idx = nullptr;
     int* scan_tmp = nullptr;  // three segments: vertex, triangle, edge hash scans

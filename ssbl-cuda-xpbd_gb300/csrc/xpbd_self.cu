@@ -418,6 +418,10 @@ __global__ void __launch_bounds__(kThreads) k_edge_insert(View v) {
                     v.eb_ovf_list[atomicAdd(v.eb_ovf_count, 1)] = b;
                     atomicOr(&v.eb_ovf_bits[b >> 5], 1u << (b & 31));
                 }
+                if (slot >= kEdgeSlots) {
+                    const unsigned long long q = atomicAdd(v.eb_late_count, 1ull);
+                    if (q < (unsigned long long)v.eb_late_cap) v.eb_late[q] = make_int2(b, k);
+                }
             }
         });
     }
@@ -427,14 +431,22 @@ __global__ void __launch_bounds__(kThreads) k_edge_insert(View v) {
     if (threadIdx.x == 0 && guard_s) count_add(v.counts, kCntSelfOverflow, (unsigned long long)guard_s);
 }
 
+// Whether every insertion past the slots was recorded in eb_late.
+__device__ __forceinline__ bool edge_late_complete(const View& v) {
+    return *v.eb_late_count <= (unsigned long long)v.eb_late_cap;
+}
+
 // Overflow regions: each listed bucket gets [start, start + count) of eb_ent,
-// in list order; eb_start[b] then serves as the region's fill cursor.  One
-// block; nothing to do in the usual build without overflow.
+// in list order (start also kept in eb_ovf_start); eb_start[b] then serves as
+// the region's fill cursor, past the kEdgeSlots members the slots hold when
+// the late insertions were all recorded.  One block; nothing to do in the
+// usual build without overflow.
 __global__ void __launch_bounds__(1024) k_edge_ovf_offsets(View v) {
     __shared__ int ws[32];
     __shared__ int carry;
     const int n = *v.eb_ovf_count;
     if (n == 0) return;
+    const int skip = edge_late_complete(v) ? kEdgeSlots : 0;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     for (int base = 0; base < n; base += kScanTile) {
@@ -444,7 +456,10 @@ __global__ void __launch_bounds__(1024) k_edge_ovf_offsets(View v) {
         int total;
         int run = carry + block_exclusive_scan4(vals, ws, &total);
         for (int q = 0; q < 4; ++q) {
-            if (i0 + q < n) v.eb_start[v.eb_ovf_list[i0 + q]] = run;
+            if (i0 + q < n) {
+                v.eb_start[v.eb_ovf_list[i0 + q]] = run + skip;
+                v.eb_ovf_start[i0 + q] = run;
+            }
             run += vals[q];
         }
         __syncthreads();
@@ -453,13 +468,34 @@ __global__ void __launch_bounds__(1024) k_edge_ovf_offsets(View v) {
     }
 }
 
-// Second walk, only when some bucket overflowed: every insertion into an
-// overflowing bucket is written to that bucket's region.  A fixed grid
-// striding over the edges, so the usual build without overflow pays for a
-// few hundred blocks that exit at once.
+// Overflow regions from what the insertion kept: each listed bucket's
+// kEdgeSlots slot members, then its recorded late insertions through the
+// region's fill cursor.  A fixed grid striding over both; nothing to do
+// without overflow, or when the late insertions did not all fit (the second
+// walk below fills the regions then).
+__global__ void __launch_bounds__(kThreads) k_edge_ovf_late(View v) {
+    const int n = *v.eb_ovf_count;
+    if (n == 0 || !edge_late_complete(v)) return;
+    const long long threads = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long t = t0; t < (long long)n * kEdgeSlots; t += threads) {
+        const int w = (int)(t / kEdgeSlots), i = (int)(t % kEdgeSlots);
+        v.eb_ent[v.eb_ovf_start[w] + i] = v.eb_slot[edge_bucket_base(v.eb_ovf_list[w]) + i];
+    }
+    const long long late = (long long)*v.eb_late_count;
+    for (long long t = t0; t < late; t += threads) {
+        const int2 e = v.eb_late[t];
+        v.eb_ent[atomicAdd(&v.eb_start[e.x], 1)] = e.y;
+    }
+}
+
+// Second walk, only when some bucket overflowed and its late insertions were
+// not all recorded: every insertion into an overflowing bucket is written to
+// that bucket's region.  A fixed grid striding over the edges, so the usual
+// build pays for a few hundred blocks that exit at once.
 template <int L>
 __global__ void __launch_bounds__(kThreads) k_edge_ovf_collect(View v) {
-    if (*v.eb_ovf_count == 0) return;
+    if (*v.eb_ovf_count == 0 || edge_late_complete(v)) return;
     const long long threads = (long long)gridDim.x * blockDim.x;
     const long long items = (long long)(v.hi - v.lo) * L;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += threads) {
@@ -2605,6 +2641,7 @@ void self_build_edge_hash(const View& v, const SelfVariants& sv, int nb, int ord
         default: k_edge_insert<8><<<grid(n, 8, b), b, 0, s>>>(iv); break;
     }
     k_edge_ovf_offsets<<<1, 1024, 0, s>>>(v);
+    k_edge_ovf_late<<<kTrimBlocks, kThreads, 0, s>>>(v);
     switch (lanes) {
         case 1: k_edge_ovf_collect<1><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;
         case 2: k_edge_ovf_collect<2><<<kTrimBlocks, kThreads, 0, s>>>(iv); break;

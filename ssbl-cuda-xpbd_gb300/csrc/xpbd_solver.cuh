@@ -291,7 +291,9 @@ struct View {
     // edge hash: bucket b's members in eb_slot[b * kEdgeSlots ...], its count
     // in eb_count[b]; buckets of more than kEdgeSlots members are listed in
     // eb_ovf_list (bit set in eb_ovf_bits) and their full member lists kept
-    // in eb_ent at [eb_start[b] - eb_count[b], eb_start[b])
+    // in eb_ent at [eb_start[b] - eb_count[b], eb_start[b]); the insertions
+    // past a bucket's kEdgeSlots slots are recorded as (bucket, edge) in
+    // eb_late while eb_late_count stays within eb_late_cap
     int* eb_count;
     int* eb_start;
     int* eb_ent;
@@ -299,6 +301,10 @@ struct View {
     unsigned* eb_ovf_bits;
     int* eb_ovf_list;
     int* eb_ovf_count;
+    int* eb_ovf_start;      // [eb_ovf_list index] first entry of the bucket's region
+    int2* eb_late;
+    unsigned long long* eb_late_count;
+    long long eb_late_cap;
     int* scan_tmp;          // block sums of the bucket scans
     int* trim_list;         // buckets of more than 32 members found by the scan (null: none kept)
     int* trim_count;

@@ -88,8 +88,11 @@ def estimate_device_bytes(req: ClothRequest) -> int:
         eb = pow2(max(1024, 4 * E)) if E >= 64 else 0
         b += V * (4 + 4 * 32 + 32 + 16 + 4) + (vb + tb + eb) * 8 + T * 64 * 4 + E * 64 * 4 + 3 * (max(vb, tb, eb) // 4096 + 2) * 4
         b += 3 * max(vb, tb, eb) * 4 + 3 * 4  # lists of buckets of more than 32 members
-        # edge hash: 64 member slots per bucket, overflow bits and list
-        b += eb * 64 * 4 + (eb // 32 + 1) * 4 + (min(eb, E * 64 // 65 + 1) + 1) * 4
+        # edge hash: 64 member slots per bucket, overflow bits, list and region
+        # starts, the record of insertions past the slots (8 B each)
+        if eb:
+            b += eb * 64 * 4 + (eb // 32 + 1) * 4 + 2 * (min(eb, E * 64 // 65 + 1) + 1) * 4
+            b += min(E * 64, max(1 << 20, E)) * 8 + 8
     if o.stretch_optimization_enabled:
         # CG blocks, preconditioner, r / z / d / q, cap sums, off-diagonal per
         # stretch-CSR entry (two per edge), colour-sorted cap edges, partials

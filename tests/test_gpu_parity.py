@@ -154,14 +154,19 @@ def test_hash_and_neighbor_tables_bit_exact(gpu_lib, oracle_lib):
     assert g["nbcount"].sum() > 0
 
 
+@pytest.mark.parametrize("late_cap", [None, "0"], ids=["late-list", "second-walk"])
 @pytest.mark.parametrize("mode", [2, 1], ids=["strict", "fast"])
-def test_crowded_buckets_parity(mode, gpu_lib, oracle_lib):
+def test_crowded_buckets_parity(mode, late_cap, gpu_lib, oracle_lib, monkeypatch):
     """A cloth shrunk into a 1.2 cm square: every edge's cell box covers the
     same few cells, so each edge-hash bucket holds about 1,600 members, far
     past the 64 member slots a bucket keeps: the overflow regions and their
     selection of the 32 smallest ids run (and the vertex and triangle hashes'
-    trims).  Hash tables, neighbour lists, positions after a frame and all
-    38 counters must equal the oracle's."""
+    trims).  The regions are filled from the recorded insertions past the
+    slots, or (record capacity 0) by the second walk of the cells.  Hash
+    tables, neighbour lists, positions after a frame and all 38 counters must
+    equal the oracle's."""
+    if late_cap is not None:
+        monkeypatch.setenv("XPBD_GB300_EDGE_LATE_CAP", late_cap)
     sc = scene.drop_scene(24, 1, seed=5, self_mode=mode)
     gpu, ora = _pair(sc, oracle_lib)
     p = sc.cloth.positions_world.copy()
