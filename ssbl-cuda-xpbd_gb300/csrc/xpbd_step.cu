@@ -460,7 +460,10 @@ __device__ __forceinline__ void vertex_pass_item(const View& v, int i, unsigned 
     v.vel[i] = f4(s.vel, 0.0f);
 }
 
-__global__ void __launch_bounds__(kThreads) k_vertex_pass(View v, unsigned flags) {
+// Six 256-thread blocks per SM (40 registers): the gathers are latency
+// bound, and the extra resident warps outweigh the spills (batch256 stretch
+// passes 2.05 -> 1.85 ms per frame; five blocks 1.98).
+__global__ void __launch_bounds__(kThreads, 6) k_vertex_pass(View v, unsigned flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < v.nV) vertex_pass_item(v, i, flags);
 }
