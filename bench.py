@@ -162,7 +162,7 @@ EE_DRAM_BYTES_PER_SLOT = 14.4
 # ... and per insertion of an edge-hash build (slot insertion, overflow
 # kernels, trim and bucket ordering) from the same capture: the frame's last
 # build over its insertions.
-EDGE_HASH_DRAM_BYTES_PER_ENTRY = 20.4
+EDGE_HASH_DRAM_BYTES_PER_ENTRY = 20.2
 
 
 def measured_traffic(kind: str, counters: dict, launches: int) -> float | None:
