@@ -307,15 +307,71 @@ void release_grid(Solver* S, Cloth& c) {
 
 }  // namespace
 
-// Zero what the slotted edge hash counts from: bucket counts, overflow bits
-// and list, and the edge hash's trim list (segment 2).
-void reset_edge_hash(Solver* S, cudaStream_t s) {
-    cudaMemsetAsync(S->eb_count, 0, sizeof(int) * (size_t)S->nEB, s);
-    cudaMemsetAsync(S->eb_ovf_bits, 0, sizeof(unsigned) * (((size_t)S->nEB + 31) / 32), s);
-    cudaMemsetAsync(S->eb_ovf_count, 0, sizeof(int), s);
-    cudaMemsetAsync(S->eb_late_count, 0, sizeof(unsigned long long), s);
-    cudaMemsetAsync(S->trim_count + 2, 0, sizeof(int), s);
+namespace {
+
+// Zeroes up to six int arrays in one launch: one graph node where a memset
+// per array would be one node each, on the path every hash build waits on.
+// Arrays whose start is 16-byte aligned are written as int4 quads.
+struct ZeroSpans {
+    int* p[6];
+    long long n[6];
+    int count;
+};
+
+__global__ void k_zero_spans(ZeroSpans z) {
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (int k = 0; k < z.count; ++k) {
+        int* p = z.p[k];
+        const long long n = z.n[k];
+        long long quads = 0;
+        if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0u) {
+            quads = n / 4;
+            int4* p4 = reinterpret_cast<int4*>(p);
+            for (long long i = t0; i < quads; i += step) p4[i] = make_int4(0, 0, 0, 0);
+        }
+        for (long long i = 4 * quads + t0; i < n; i += step) p[i] = 0;
+    }
 }
+
+void zero_spans(const ZeroSpans& z, cudaStream_t s) {
+    long long work = 0;
+    for (int k = 0; k < z.count; ++k) work += (z.n[k] + 3) / 4;
+    const long long blocks = std::min<long long>(std::max<long long>((work + 255) / 256, 1), 152 * 8);
+    k_zero_spans<<<(int)blocks, 256, 0, s>>>(z);
+}
+
+}  // namespace
+
+// Zero what the slotted edge hash counts from: bucket counts, overflow bits,
+// list count and record count, and the edge hash's trim list (segment 2).
+void reset_edge_hash(Solver* S, cudaStream_t s) {
+    ZeroSpans z{};
+    z.p[0] = S->eb_count;
+    z.n[0] = S->nEB;
+    z.p[1] = reinterpret_cast<int*>(S->eb_ovf_bits);
+    z.n[1] = ((long long)S->nEB + 31) / 32;
+    z.p[2] = S->eb_ovf_count;
+    z.n[2] = 1;
+    z.p[3] = reinterpret_cast<int*>(S->eb_late_count);
+    z.n[3] = 2;
+    z.p[4] = S->trim_count + 2;
+    z.n[4] = 1;
+    z.count = 5;
+    zero_spans(z, s);
+}
+
+// Zero the triangle hash's bucket counts and its trim list count (segment 1).
+void reset_triangle_hash(Solver* S, cudaStream_t s) {
+    ZeroSpans z{};
+    z.p[0] = S->tb_count;
+    z.n[0] = S->nTB;
+    z.p[1] = S->trim_count + 1;
+    z.n[1] = 1;
+    z.count = 2;
+    zero_spans(z, s);
+}
+
 
 View Solver::view() const {
     View v{};
@@ -1783,13 +1839,14 @@ void enqueue_frame(Solver* S, int substeps, int iterations, FrameStats* st, Prof
                         self_build_vertex_hash(hv[0], sp.sv, S->nVB, lane_stream(0));
                     });
                 if (sp.thash)
-                    timed(kKTriangleHash, 6, [&] {
-                        cudaMemsetAsync(S->tb_count, 0, sizeof(int) * S->nTB, lane_stream(1));
-                        cudaMemsetAsync(S->trim_count + 1, 0, sizeof(int), lane_stream(1));
+                    // zeroing, count, three scan kernels, scatter, trim (+ ordering)
+                    timed(kKTriangleHash, 7 + (order_mode(sp.t_order, sp.t_plain) != 0), [&] {
+                        reset_triangle_hash(S, lane_stream(1));
                         self_build_triangle_hash(hv[1], sp.sv, S->nTB, order_mode(sp.t_order, sp.t_plain), lane_stream(1));
                     });
                 if (sp.ehash)
-                    timed(kKEdgeHash, 6, [&] {
+                    // zeroing, insertion, four overflow kernels, trim (+ ordering)
+                    timed(kKEdgeHash, 7 + (order_mode(sp.e_order, sp.e_plain) != 0), [&] {
                         reset_edge_hash(S, lane_stream(2));
                         self_build_edge_hash(hv[2], sp.sv, S->nEB, order_mode(sp.e_order, sp.e_plain), lane_stream(2));
                     });

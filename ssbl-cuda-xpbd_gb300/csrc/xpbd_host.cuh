@@ -351,6 +351,7 @@ struct Solver {
 Solver* create_solver(const SsblXpbdConfig* configs, const SsblXpbdMesh* meshes, int count);
 void free_solver(Solver* S);
 void reset_edge_hash(Solver* S, cudaStream_t s);
+void reset_triangle_hash(Solver* S, cudaStream_t s);
 
 // Cloth-level updates; cloth < 0 applies to every cloth (pins then take
 // indices over the concatenated vertices).
