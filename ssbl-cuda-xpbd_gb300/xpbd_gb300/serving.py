@@ -25,9 +25,12 @@ tick that advances it, and a tick advances every resident request, so the
 tick time follows the resident work (vertex-substeps per tick) divided by
 the device's throughput.  With ``frame_latency_ms`` set, a request is
 admitted only while the resident work plus its own stays within the work one
-tick can do in that time at the throughput measured over recent ticks
-(exponential average of vertex-substeps per second of tick time, seeded by
-``rate_guess``); the rest waits in the queue in arrival order.  Without a
+tick can do in ``latency_headroom`` (default 0.9) of that time at the
+throughput measured over recent ticks (exponential average of
+vertex-substeps per second of tick time, seeded by ``rate_guess``); the rest
+waits in the queue in arrival order.  The headroom absorbs the tick-to-tick
+variation of the measured rate, so the 99th percentile of frame latency
+stays under the target rather than around it.  Without a
 target, admission is by device memory alone.
 
 The solver back end is injectable (``backend``) so the scheduling logic can
@@ -167,9 +170,10 @@ class ServingEngine:
 
     def __init__(self, hbm_budget_bytes: int, group_below: int = 50_000, max_cohort_vertices: int = 2_000_000,
                  max_admit_per_tick: int = 64, backend=None, clock=time.perf_counter, workers: int = 4,
-                 frame_latency_ms: float | None = None, rate_guess: float = 2.0e8):
+                 frame_latency_ms: float | None = None, rate_guess: float = 2.0e8, latency_headroom: float = 0.9):
         self.budget = int(hbm_budget_bytes)
         self.frame_latency_ms = frame_latency_ms
+        self.latency_headroom = float(latency_headroom)
         self.rate = float(rate_guess)     # vertex-substeps per second of tick time (measured)
         self.resident_work = 0            # vertex-substeps per tick of admitted requests
         self.workers = workers
@@ -319,7 +323,8 @@ class ServingEngine:
         share a cohort."""
         admitted: list[ClothRequest] = []
         reserve = 0
-        work_cap = None if self.frame_latency_ms is None else self.rate * self.frame_latency_ms / 1000.0
+        work_cap = (None if self.frame_latency_ms is None
+                    else self.latency_headroom * self.rate * self.frame_latency_ms / 1000.0)
         while self.queue and len(admitted) < self.max_admit_per_tick:
             need = estimate_device_bytes(self.queue[0])
             if self.used_bytes + reserve + need > self.budget:
