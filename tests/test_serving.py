@@ -204,3 +204,24 @@ def test_latency_target_bounds_resident_work():
         eng2.submit(r)
     eng2.tick()
     assert eng2.live_requests == 9
+
+
+def test_latency_headroom_scales_the_admitted_work():
+    """Admission keeps the resident work within `latency_headroom` of what
+    the measured rate does in one target: 16,000 vertex-substeps per
+    request at 1.6e6 per second, a 31 ms target holds 49,600 at full
+    headroom (three requests) and 44,640 at the default 0.9 (two)."""
+    for headroom, most in ((1.0, 3), (0.9, 2)):
+        clock = WorkClock(rate=1.6e6)
+        eng = ServingEngine(hbm_budget_bytes=1 << 40, backend=TimedBackend(clock), clock=clock, workers=0,
+                            frame_latency_ms=31.0, rate_guess=1.6e6, max_admit_per_tick=64,
+                            latency_headroom=headroom)
+        for r in [_req(k, 40, 4) for k in range(6)]:
+            eng.submit(r)
+        resident = []
+        results = []
+        while not eng.idle():
+            results += eng.tick()
+            resident.append(eng.live_requests)
+        assert max(resident) == most, (headroom, resident)
+        assert sorted(r.request_id for r in results) == list(range(6))
