@@ -376,8 +376,10 @@ __device__ __forceinline__ int warp_global_id() { return (int)((blockIdx.x * (lo
 // whose count passes the 32 query slots is listed for ordering (its 32
 // smallest ids first, in increasing order: queries read no further); one that
 // passes kEdgeSlots is listed as an overflow, and its full member list is
-// rebuilt from a second walk of the cells into a region of its own (rare:
-// a fold or crumple that packs more than 64 edge boxes into one bucket).
+// gathered into a region of its own (a fold or crumple that packs more than
+// 64 edge boxes into one bucket): its slot members plus the insertions past
+// them, which the insertion records as (bucket, edge); only when that record
+// fills up are the cells walked a second time instead.
 // Every insertion past the 32 query slots counts as an overflow guard event,
 // as the reference counts an insertion into a full bucket (abi41.cu:5584-
 // 5590), and so does a collapsed cell range.  Members end up where the
