@@ -402,6 +402,28 @@ __device__ __forceinline__ void edge_cells_walk(const View& v, int k, int r0, bo
     }
 }
 
+// The same walk, handing the cells of a row to f four at a time (f(b, n):
+// buckets b[0..n) in walk order), so an insertion can have four atomics in
+// flight before it uses their results.
+template <int L, class F>
+__device__ __forceinline__ void edge_cells_walk4(const View& v, int k, int r0, bool* collapsed, F&& f) {
+    const Params& P = params_e(v, k);
+    if (!P.ehash || !self_scheduled(P, v)) return;
+    bool ok = false;
+    const CellRange r = edge_cells(v, P, k, &ok, collapsed);
+    const int nx = r.x1 - r.x0 + 1, ny = r.y1 - r.y0 + 1, nz = r.z1 - r.z0 + 1;
+    if (!ok || nx <= 0 || ny <= 0 || nz <= 0) return;
+    for (int row = r0; row < ny * nz; row += L) {
+        const int y = r.y0 + row % ny, z = r.z0 + row / ny;
+        for (int x = r.x0; x <= r.x1; x += 4) {
+            int b[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = P.ebase + (int)bucket_of(x + j, y, z, P.ebuckets);
+            f(b, min(4, r.x1 - x + 1));
+        }
+    }
+}
+
 template <int L>
 __global__ void __launch_bounds__(kThreads) k_edge_insert(View v) {
     __shared__ unsigned guard_s;  // the block's guard events: one global atomic per block
@@ -412,19 +434,26 @@ __global__ void __launch_bounds__(kThreads) k_edge_insert(View v) {
     bool collapsed = false;
     unsigned past = 0u;
     if (k < v.hi) {
-        edge_cells_walk<L>(v, k, r0, &collapsed, [&](int b) {
-            const int slot = atomicAdd(&v.eb_count[b], 1);
-            if (slot < kEdgeSlots) v.eb_slot[edge_bucket_base(b) + slot] = k;
-            if (slot >= kBucketSlots) {
-                ++past;
-                if (slot == kBucketSlots) v.trim_list[atomicAdd(v.trim_count, 1)] = b;
-                if (slot == kEdgeSlots) {
-                    v.eb_ovf_list[atomicAdd(v.eb_ovf_count, 1)] = b;
-                    atomicOr(&v.eb_ovf_bits[b >> 5], 1u << (b & 31));
-                }
-                if (slot >= kEdgeSlots) {
-                    const unsigned long long q = atomicAdd(v.eb_late_count, 1ull);
-                    if (q < (unsigned long long)v.eb_late_cap) v.eb_late[q] = make_int2(b, k);
+        edge_cells_walk4<L>(v, k, r0, &collapsed, [&](const int (&bs)[4], int n) {
+            int slots[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) slots[j] = j < n ? atomicAdd(&v.eb_count[bs[j]], 1) : 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (j >= n) continue;
+                const int b = bs[j], slot = slots[j];
+                if (slot < kEdgeSlots) v.eb_slot[edge_bucket_base(b) + slot] = k;
+                if (slot >= kBucketSlots) {
+                    ++past;
+                    if (slot == kBucketSlots) v.trim_list[atomicAdd(v.trim_count, 1)] = b;
+                    if (slot == kEdgeSlots) {
+                        v.eb_ovf_list[atomicAdd(v.eb_ovf_count, 1)] = b;
+                        atomicOr(&v.eb_ovf_bits[b >> 5], 1u << (b & 31));
+                    }
+                    if (slot >= kEdgeSlots) {
+                        const unsigned long long q = atomicAdd(v.eb_late_count, 1ull);
+                        if (q < (unsigned long long)v.eb_late_cap) v.eb_late[q] = make_int2(b, k);
+                    }
                 }
             }
         });
