@@ -1779,12 +1779,12 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_vt(View v) {
 // candidate b) counts only when b > a (it is evaluated from its lower edge),
 // which about two thirds of the bucket slots fail as soon as their id is
 // read.  Round after round the warp reads 32 slot ids (the items' slots laid
-// end to end), keeps the surviving pairs in a 64-entry ring in shared memory
+// end to end), keeps the surviving pairs in a 128-entry ring in shared memory
 // (owner lane, candidate), and evaluates them 32 at a time whenever 32 are
 // waiting, so the evaluation rounds carry only pairs that can be taken.
 // Pushes go through the integer accumulators and the counters through warp
 // ballots, so the result does not depend on the order of evaluation.
-constexpr int kEeRing = 64;
+constexpr int kEeRing = 128;
 
 __global__ void __launch_bounds__(kThreads, 6) k_flat_ee(View v) {
     __shared__ int2 ring_s[kThreads / 32][kEeRing];
@@ -1844,22 +1844,32 @@ __global__ void __launch_bounds__(kThreads, 6) k_flat_ee(View v) {
         __syncwarp();
     };
     const unsigned lower = (1u << lane) - 1u;
-    for (int base = 0; base < total; base += 32) {
-        const int w = base + lane;
-        int j = 0;
+    // Two rounds of 32 slot ids per step, both loads issued before either
+    // is used; the ring holds what two rounds add to fewer than 32 waiting.
+    for (int base = 0; base < total; base += 64) {
+        int jr[2], other[2], owner[2];
 #pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-            if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
-        const int o_item = __shfl_sync(0xffffffffu, item, j);
-        const long long o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
-        const int other = w < total ? v.eb_slot[o_first + w] : -1;
-        const bool keep = w < total && other > o_item;
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (keep) ring[(tail + __popc(m & lower)) & (kEeRing - 1)] = make_int2(j, other);
-        tail += __popc(m);
-        gathers += __popc(m);
+        for (int r = 0; r < 2; ++r) {
+            const int w = base + 32 * r + lane;
+            int j = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, incl, j + step - 1) <= w) j += step;
+            jr[r] = j;
+            owner[r] = __shfl_sync(0xffffffffu, item, j);
+            const long long o_first = __shfl_sync(0xffffffffu, st, j) - __shfl_sync(0xffffffffu, excl, j);
+            other[r] = w < total ? v.eb_slot[o_first + w] : -1;
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const bool keep = base + 32 * r + lane < total && other[r] > owner[r];
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) ring[(tail + __popc(m & lower)) & (kEeRing - 1)] = make_int2(jr[r], other[r]);
+            tail += __popc(m);
+            gathers += __popc(m);
+        }
         __syncwarp();
-        if (tail - head >= 32) drain(32);
+        while (tail - head >= 32) drain(32);
     }
     if (tail > head) drain(tail - head);
     const unsigned items = __popc(__ballot_sync(0xffffffffu, counted));
